@@ -1,0 +1,196 @@
+/*
+ * mdgpu.h - C ABI of the GB300 force / neighbour-list / SHAKE library for md_sim.
+ *
+ * The reference reaches its hot path through three argument-less Fortran calls that talk
+ * through module globals:
+ *   call force_get     src/main.f90:42,62      (definition src/forcem.f90:93-129)
+ *   call nnlist_make   src/forcem.f90:250      (definition src/nnlist.f90:92-165)
+ *   call move_shake    src/move.f90:376        (definition src/move.f90:408-529)
+ * and prepares them once in force_init (src/forcem.f90:54-81, which calls nnlist_init
+ * src/nnlist.f90:14-90) and move_shake_init (src/move.f90:385-406).
+ *
+ * This header replaces those calls with plain C entry points.  Every pointer is a host
+ * pointer to a contiguous array exactly as the Fortran modules hold it (real*8 -> double,
+ * integer*8 -> int64_t), so an ISO_C_BINDING interface can pass the module arrays straight
+ * through.  Atom and type indices inside the arrays stay 1-based, as in the reference.
+ * Errors are returned as negative codes (the reference calls `stop`); mdg_last_error()
+ * gives the message.  A context owns all device memory; calls on one context are
+ * synchronous on return and must come from one host thread at a time.
+ */
+#ifndef MDGPU_H
+#define MDGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDG_SMX 3 /* max sites / constraints / angles per molecule, src/global.f90:7 */
+
+/* return codes */
+#define MDG_OK 0
+#define MDG_E_ARG (-1)           /* bad argument or inconsistent system description */
+#define MDG_E_CUDA (-2)          /* CUDA runtime failure or no device */
+#define MDG_E_LIST_OVERFLOW (-3) /* neighbour list capacity exceeded, src/nnlist.f90:136-139,157-160 */
+#define MDG_E_SHAKE_MAXIT (-4)   /* 'shake(): Too many constraint iterations!', src/move.f90:526 */
+#define MDG_E_SHAKE_RPTOL (-5)   /* 'Constraint failure', src/move.f90:487-496 */
+#define MDG_E_NAN (-6)           /* non-finite force or energy */
+#define MDG_E_UNSUPPORTED (-7)   /* feature outside this library (e.g. Couette-pulled walls) */
+
+/* force-field variants */
+#define MDG_SLAB 0 /* src/forcem.f90: z not periodic in real space, wall LR tail, EW3DC dipole term */
+#define MDG_BULK 1 /* src/forcem_back.f90: z minimum image in pair/angle loops, no LR tail, no EW3DC */
+
+/* arithmetic of the force phases */
+#define MDG_FP64 0  /* every phase in FP64 (reproduces the reference) */
+#define MDG_MIXED 1 /* FP32 pairs with compensated sums, tensor-core reciprocal sum, FP64 state */
+
+/* quirk switches (mdg_params.quirks); default 0 reproduces the reference */
+#define MDG_QUIRK_CLEAN_SHAKE_DONE 1u /* SHAKE stops when no molecule moved (global test) instead of
+                                         the reference's last-molecule test, src/move.f90:458 */
+
+/*
+ * System description: the sysdef/config module tables the hot path reads
+ * (src/sysdef.f90:9-59 after sysdef_init :356-457).  Arrays are borrowed for the duration of
+ * mdg_create only.
+ */
+typedef struct mdg_sysdesc {
+    /* counts, src/sysdef.f90:16-25 */
+    int64_t ntype;                                          /* molecule types */
+    int64_t nrig, nriga, nliqa, nsurf, nmove, nwall, ntota; /* molecules / atom ranges */
+    int64_t ngogo;                                          /* atoms in the k-space sum (= nmove) */
+    int64_t nit, nijt;                                      /* site types, site-type pairs */
+    int64_t nltype;                                         /* last liquid molecule type */
+    int64_t ncons, nang;                                    /* constrained molecules, angle molecules */
+    /* per molecule type, length ntype */
+    const int64_t* moltypen; /* 0 rigmol, 1 atmol, 2 surfmol, 3 crystal */
+    const int64_t* nt;       /* molecules of the type */
+    const int64_t* ns;       /* sites per molecule */
+    const int64_t* nst;      /* site types per molecule type */
+    const int64_t* nconst;   /* constraints per molecule */
+    const int64_t* nangt;    /* angles per molecule */
+    const int64_t* nss_wall; /* nss(ntype,:): sites per crystal site type, max(2,nst(ntype))
+                                entries (missing ones 0) */
+    /* per site type, length nit */
+    const int64_t* nsi; /* sites handled by a head atom of this type (0: not a head) */
+    /* per site-type pair */
+    const int64_t* ijtype; /* nit x nit, column-major, 1-based pair id */
+    const int64_t* vdwnum; /* nijt: 0 none, 1 Lennard-Jones, 2 Buckingham */
+    const double* eps;     /* nijt, 4*epsilon */
+    const double* sig;     /* nijt, sigma**6 */
+    const double* aa;      /* nijt, Buckingham A */
+    const double* rhoi;    /* nijt, Buckingham 1/rho */
+    const double* cc;      /* nijt, Buckingham C */
+    /* per atom, length ntota */
+    const int64_t* itype; /* 1-based site type */
+    const double* qs;     /* charge in e */
+    const double* mi;     /* mass, internal units (src/sysdef.f90:378-379) */
+    const double* mii;    /* inverse mass, 0 for frozen sites */
+    /* constraints and angles */
+    const int64_t* ictype;  /* ncons: molecule type of each constrained molecule */
+    const int64_t* constra; /* MDG_SMX x ncons, column-major, 1-based atoms */
+    const int64_t* constrb; /* MDG_SMX x ncons */
+    const double* length;   /* ntype x MDG_SMX, column-major: constraint lengths */
+    const int64_t* iatype;  /* nang */
+    const int64_t* ang1;    /* MDG_SMX x nang */
+    const int64_t* ang2;
+    const int64_t* ang3;
+    const double* kt;    /* ntype x MDG_SMX: bend force constants */
+    const double* theta; /* ntype x MDG_SMX: equilibrium angles, radians */
+    /* geometry, src/config.f90:13 and src/sysdef.f90:46 */
+    double lx, ly, lz;
+    double cx, cy, cz, lw; /* crystal cell and wall-to-wall slab width */
+    double dt;             /* time step, fs */
+} mdg_sysdesc;
+
+typedef struct mdg_params {
+    double rcut;   /* real-space cutoff, A */
+    double skin;   /* Verlet skin, A */
+    double alpha;  /* Ewald alpha, 1/A; <= 0 selects 3.09/rcut as src/forcem.f90:59 */
+    int64_t kmax;  /* reciprocal cutoff index */
+    double dshsq;  /* squared wall shift per step (Couette), 0 otherwise, src/nnlist.f90:28 */
+    int32_t variant;    /* MDG_SLAB or MDG_BULK */
+    int32_t pbc_z_list; /* 1: the neighbour list also applies the z minimum image (bulk boxes);
+                           the reference never does, src/nnlist.f90:129,150 */
+    int32_t precision;  /* MDG_FP64 or MDG_MIXED */
+    uint32_t quirks;    /* MDG_QUIRK_* bits */
+    int64_t list_capacity;  /* max head-head pairs kept; 0 = sized automatically */
+    int64_t wlist_capacity; /* max head-wall pairs kept; 0 = sized automatically */
+    int32_t shake_maxit;    /* SHAKE sweep limit; 0 selects 10, src/move.f90:398 */
+    double shake_tol2;      /* relative tolerance; 0 selects 1e-8, src/move.f90:399 */
+    double shake_rptol;     /* failure ratio; 0 selects 0.85, src/move.f90:400 */
+} mdg_params;
+
+/*
+ * Energies and statistics of one force evaluation (the scalars force_sum leaves,
+ * src/forcem.f90:969-1124).  elj/eqq are caller arrays of length nijt, or NULL.
+ * fws*[0..2] hold the reference's fws*(-1:1).
+ */
+typedef struct mdg_energies {
+    double* elj;
+    double* eqq;
+    double uewa, urf, ulr, uself, uconf, uavex, press, vir;
+    double ewqLL, ewqWL, ewqWW;
+    double fwsx[3], fwsy[3], fwsz[3];
+} mdg_energies;
+
+typedef struct mdg_ctx mdg_ctx;
+
+/* Replaces force_init (src/forcem.f90:54-81) with nnlist_init (src/nnlist.f90:14-90) and
+ * move_shake_init (src/move.f90:385-406): uploads the tables and the frozen wall sites, builds
+ * the k-vector set, Ak, the static wall structure factors, the self energy, the wall
+ * long-range tail tables and the first neighbour list.  x0/y0/z0: ntota; cx0..: nrig. */
+int mdg_create(const mdg_sysdesc* sys, const mdg_params* prm, const double* x0, const double* y0,
+               const double* z0, const double* cx0, const double* cy0, const double* cz0,
+               mdg_ctx** out);
+
+void mdg_destroy(mdg_ctx* ctx);
+
+/* Message of the last failure on this context (or of the last failed mdg_create if ctx is NULL). */
+const char* mdg_last_error(const mdg_ctx* ctx);
+
+/* Replaces nnlist_make (src/nnlist.f90:92-165): unconditional rebuild from the given positions.
+ * x0..: nmove (or ntota), cx0..: nrig.  ipack/wpack receive the list lengths (may be NULL). */
+int mdg_nnlist_make(mdg_ctx* ctx, const double* x0, const double* y0, const double* z0,
+                    const double* cx0, const double* cy0, const double* cz0, int64_t* ipack,
+                    int64_t* wpack);
+
+/* Copies the current neighbour lists out as 1-based (i, j) pairs, in no particular order.
+ * Arrays may be NULL; at most cap / wcap pairs are written.  Returns MDG_OK. */
+int mdg_get_lists(mdg_ctx* ctx, int64_t* li, int64_t* lj, int64_t cap, int64_t* wi, int64_t* wj,
+                  int64_t wcap, int64_t* ipack, int64_t* wpack);
+
+/* Replaces force_get (src/forcem.f90:93-129) with force_real, force_fouri, force_intra and the
+ * serial force_sum (src/forcem_3d.f90:1031-1058), including the rebuild trigger
+ * (src/forcem.f90:245-250).
+ *   x0,y0,z0   in  ntota site positions (walls are read at create and ignored here)
+ *   cx0..      in  nrig centres of mass
+ *   rsx,rsy,rsz in/out nmove site offsets; on return rsx(1:3) hold the last rigid molecule's
+ *                  sites relative to its centre, as force_sum leaves them (src/forcem.f90:1006)
+ *   ftx,fty,ftz out nmove-nriga forces on the flexible atoms (Fortran ftx(nriga+1:nmove))
+ *   fcx..,tx..  out nrig centre-of-mass forces and torques
+ *   fx,fy,fz    out optional (NULL to skip): nmove site forces before the rigid-body reduction
+ *   e           out energies and wall statistics (NULL to skip) */
+int mdg_force_get(mdg_ctx* ctx, const double* x0, const double* y0, const double* z0,
+                  const double* cx0, const double* cy0, const double* cz0, double* rsx,
+                  double* rsy, double* rsz, double* ftx, double* fty, double* ftz, double* fcx,
+                  double* fcy, double* fcz, double* tx, double* ty, double* tz, double* fx,
+                  double* fy, double* fz, mdg_energies* e);
+
+/* Replaces move_shake (src/move.f90:408-529): Verlet step of the surface atoms plus SHAKE.
+ *   x0,y0,z0      in/out ntota positions (atoms nliqa+1..nmove are updated)
+ *   xold,yold,zold in/out ntota-nliqa previous positions (Fortran xold(nliqa+1:ntota))
+ *   ftx,fty,ftz   in  nmove-nriga forces (Fortran ftx(nriga+1:nmove))
+ *   kps           out nit per-type kinetic sums (may be NULL)
+ *   tkps          out SHAKE temperature (may be NULL)
+ *   sweeps        out SHAKE sweeps executed (may be NULL) */
+int mdg_shake(mdg_ctx* ctx, double* x0, double* y0, double* z0, double* xold, double* yold,
+              double* zold, const double* ftx, const double* fty, const double* ftz, double* kps,
+              double* tkps, int32_t* sweeps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MDGPU_H */

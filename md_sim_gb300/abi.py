@@ -1,0 +1,265 @@
+"""ctypes mirror of include/mdgpu.h and a thin host-side wrapper around one context.
+
+`Context` plays the role of the Fortran caller: it owns the host arrays the reference keeps in
+module globals (positions, site offsets, forces, SHAKE old positions) and passes them to
+  mdg_create      <- force_init + nnlist_init + move_shake_init  (src/forcem.f90:54-81)
+  mdg_force_get   <- force_get                                   (src/forcem.f90:93-129)
+  mdg_nnlist_make <- nnlist_make                                 (src/nnlist.f90:92-165)
+  mdg_shake       <- move_shake                                  (src/move.f90:408-529)
+The same wrapper drives any library exporting these entry points under another prefix.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from typing import Dict, Optional
+
+import numpy as np
+
+from .system import System
+
+I64P = C.POINTER(C.c_int64)
+DP = C.POINTER(C.c_double)
+
+MDG_OK = 0
+MDG_SLAB, MDG_BULK = 0, 1
+MDG_FP64, MDG_MIXED = 0, 1
+MDG_QUIRK_CLEAN_SHAKE_DONE = 1
+
+ERRORS = {
+    -1: "MDG_E_ARG", -2: "MDG_E_CUDA", -3: "MDG_E_LIST_OVERFLOW", -4: "MDG_E_SHAKE_MAXIT",
+    -5: "MDG_E_SHAKE_RPTOL", -6: "MDG_E_NAN", -7: "MDG_E_UNSUPPORTED",
+}
+
+
+class MdgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SysDesc(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "ntype", "nrig", "nriga", "nliqa", "nsurf", "nmove", "nwall", "ntota", "ngogo",
+        "nit", "nijt", "nltype", "ncons", "nang")] + [
+        ("moltypen", I64P), ("nt", I64P), ("ns", I64P), ("nst", I64P), ("nconst", I64P),
+        ("nangt", I64P), ("nss_wall", I64P), ("nsi", I64P), ("ijtype", I64P), ("vdwnum", I64P),
+        ("eps", DP), ("sig", DP), ("aa", DP), ("rhoi", DP), ("cc", DP),
+        ("itype", I64P), ("qs", DP), ("mi", DP), ("mii", DP),
+        ("ictype", I64P), ("constra", I64P), ("constrb", I64P), ("length", DP),
+        ("iatype", I64P), ("ang1", I64P), ("ang2", I64P), ("ang3", I64P), ("kt", DP),
+        ("theta", DP),
+        ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+        ("cx", C.c_double), ("cy", C.c_double), ("cz", C.c_double), ("lw", C.c_double),
+        ("dt", C.c_double)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("rcut", C.c_double), ("skin", C.c_double), ("alpha", C.c_double), ("kmax", C.c_int64),
+        ("dshsq", C.c_double), ("variant", C.c_int32), ("pbc_z_list", C.c_int32),
+        ("precision", C.c_int32), ("quirks", C.c_uint32), ("list_capacity", C.c_int64),
+        ("wlist_capacity", C.c_int64), ("shake_maxit", C.c_int32), ("shake_tol2", C.c_double),
+        ("shake_rptol", C.c_double)]
+
+
+class Energies(C.Structure):
+    _fields_ = [("elj", DP), ("eqq", DP)] + [(n, C.c_double) for n in (
+        "uewa", "urf", "ulr", "uself", "uconf", "uavex", "press", "vir", "ewqLL", "ewqWL",
+        "ewqWW")] + [("fwsx", C.c_double * 3), ("fwsy", C.c_double * 3), ("fwsz", C.c_double * 3)]
+
+
+@dataclasses.dataclass
+class RunParams:
+    rcut: float
+    skin: float
+    kmax: int
+    alpha: float = 0.0
+    variant: int = MDG_SLAB
+    pbc_z_list: int = 0
+    precision: int = MDG_FP64
+    quirks: int = 0
+    dshsq: float = 0.0
+    list_capacity: int = 0
+    wlist_capacity: int = 0
+    shake_maxit: int = 0
+    shake_tol2: float = 0.0
+    shake_rptol: float = 0.0
+
+    def to_c(self) -> Params:
+        return Params(self.rcut, self.skin, self.alpha, self.kmax, self.dshsq, self.variant,
+                      self.pbc_z_list, self.precision, self.quirks, self.list_capacity,
+                      self.wlist_capacity, self.shake_maxit, self.shake_tol2, self.shake_rptol)
+
+
+def _p(a: np.ndarray, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def make_sysdesc(s: System):
+    """Builds the C description; returns (struct, keep-alive list)."""
+    keep = []
+
+    def i64(a):
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.int64))
+        keep.append(a)
+        return _p(a, C.c_int64)
+
+    def f64(a):
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+        keep.append(a)
+        return _p(a, C.c_double)
+
+    nstw = int(s.nst[s.ntype - 1])
+    crys = s.fld.moltypes[s.ntype - 1]
+    nss_wall = list(crys.nss) + [0] * max(0, 2 - len(crys.nss))
+    d = SysDesc(
+        s.ntype, s.nrig, s.nriga, s.nliqa, s.nsurf, s.nmove, s.nwall, s.ntota, s.ngogo,
+        s.nit, s.nijt, s.nltype, s.ncons, s.nang,
+        i64(s.moltypen), i64(s.nt), i64(s.ns), i64(s.nst), i64(s.nconst), i64(s.nangt),
+        i64(nss_wall[:max(2, nstw)]), i64(s.nsi), i64(s.ijtype), i64(s.vdwnum),
+        f64(s.eps), f64(s.sig), f64(s.aa), f64(s.rhoi), f64(s.cc),
+        i64(s.itype), f64(s.qs), f64(s.mi), f64(s.mii),
+        i64(s.ictype), i64(s.constra.flatten(order="F")), i64(s.constrb.flatten(order="F")),
+        f64(s.length.flatten(order="F")),
+        i64(s.iatype), i64(s.ang[0].flatten(order="F")), i64(s.ang[1].flatten(order="F")),
+        i64(s.ang[2].flatten(order="F")), f64(s.kt.flatten(order="F")),
+        f64(s.theta.flatten(order="F")),
+        s.lx, s.ly, s.lz, s.cx, s.cy, s.cz, s.lw, s.dt)
+    return d, keep
+
+
+class Lib:
+    """Binds the entry points of one shared library (`prefix` = 'mdg_' for the product)."""
+
+    def __init__(self, path: str, prefix: str = "mdg_"):
+        self.path = path
+        self.prefix = prefix
+        self.so = C.CDLL(path)
+        g = self.fn
+        g("create", C.c_int, [C.POINTER(SysDesc), C.POINTER(Params)] + [DP] * 6 + [C.POINTER(C.c_void_p)])
+        g("destroy", None, [C.c_void_p])
+        g("last_error", C.c_char_p, [C.c_void_p])
+        g("nnlist_make", C.c_int, [C.c_void_p] + [DP] * 6 + [I64P, I64P])
+        g("get_lists", C.c_int, [C.c_void_p, I64P, I64P, C.c_int64, I64P, I64P, C.c_int64, I64P, I64P])
+        g("force_get", C.c_int, [C.c_void_p] + [DP] * 21 + [C.POINTER(Energies)])
+        g("shake", C.c_int, [C.c_void_p] + [DP] * 10 + [C.POINTER(C.c_double), C.POINTER(C.c_int32)])
+
+    def fn(self, name, restype, argtypes):
+        f = getattr(self.so, self.prefix + name)
+        f.restype = restype
+        f.argtypes = argtypes
+        setattr(self, name, f)
+        return f
+
+    def has(self, name: str) -> bool:
+        return hasattr(self.so, self.prefix + name)
+
+
+def _dp(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(DP)
+
+
+class Context:
+    """One system on one library context; numpy in, numpy out."""
+
+    def __init__(self, lib: Lib, s: System, prm: RunParams):
+        self.lib, self.sys, self.prm = lib, s, prm
+        self._desc, self._keep = make_sysdesc(s)
+        self._cprm = prm.to_c()
+        h = C.c_void_p()
+        cx = np.ascontiguousarray(s.c[0, 0]) if s.nrig else np.zeros(1)
+        cy = np.ascontiguousarray(s.c[0, 1]) if s.nrig else np.zeros(1)
+        cz = np.ascontiguousarray(s.c[0, 2]) if s.nrig else np.zeros(1)
+        rc = lib.create(C.byref(self._desc), C.byref(self._cprm), _dp(s.x0), _dp(s.y0), _dp(s.z0),
+                        _dp(cx), _dp(cy), _dp(cz), C.byref(h))
+        if rc != MDG_OK:
+            raise MdgError(rc, (lib.last_error(None) or b"").decode())
+        self.h = h
+        n = s.nijt
+        self.elj = np.zeros(n)
+        self.eqq = np.zeros(n)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != MDG_OK:
+            raise MdgError(rc, (self.lib.last_error(self.h) or b"").decode())
+
+    @staticmethod
+    def _com(s: System):
+        if s.nrig:
+            return [np.ascontiguousarray(s.c[0, d]) for d in range(3)]
+        return [np.zeros(1)] * 3
+
+    def nnlist_make(self, s: Optional[System] = None):
+        s = s or self.sys
+        cx, cy, cz = self._com(s)
+        ip, wp = C.c_int64(), C.c_int64()
+        self._check(self.lib.nnlist_make(self.h, _dp(s.x0), _dp(s.y0), _dp(s.z0), _dp(cx), _dp(cy),
+                                         _dp(cz), C.byref(ip), C.byref(wp)))
+        return ip.value, wp.value
+
+    def get_lists(self):
+        ip, wp = C.c_int64(), C.c_int64()
+        self._check(self.lib.get_lists(self.h, None, None, 0, None, None, 0, C.byref(ip), C.byref(wp)))
+        n, nw = ip.value, wp.value
+        li, lj = np.zeros(max(n, 1), np.int64), np.zeros(max(n, 1), np.int64)
+        wi, wj = np.zeros(max(nw, 1), np.int64), np.zeros(max(nw, 1), np.int64)
+        self._check(self.lib.get_lists(self.h, _p(li, C.c_int64), _p(lj, C.c_int64), n,
+                                       _p(wi, C.c_int64), _p(wj, C.c_int64), nw, C.byref(ip), C.byref(wp)))
+        return (li[:n], lj[:n]), (wi[:nw], wj[:nw])
+
+    def force_get(self, s: Optional[System] = None, want_sites: bool = True) -> Dict[str, object]:
+        """One force evaluation; updates s.rsx[0:3] as force_sum does."""
+        s = s or self.sys
+        nm, nr = s.nmove, s.nriga
+        nrig = max(s.nrig, 1)
+        ft = [np.zeros(max(nm - nr, 1)) for _ in range(3)]
+        fc = [np.zeros(nrig) for _ in range(3)]
+        tq = [np.zeros(nrig) for _ in range(3)]
+        fs = [np.zeros(nm) for _ in range(3)] if want_sites else [None] * 3
+        cx, cy, cz = self._com(s)
+        e = Energies()
+        e.elj = _dp(self.elj)
+        e.eqq = _dp(self.eqq)
+        self._check(self.lib.force_get(
+            self.h, _dp(s.x0), _dp(s.y0), _dp(s.z0), _dp(cx), _dp(cy), _dp(cz),
+            _dp(s.rsx), _dp(s.rsy), _dp(s.rsz), *[_dp(a) for a in ft], *[_dp(a) for a in fc],
+            *[_dp(a) for a in tq], *[_dp(a) for a in fs], C.byref(e)))
+        out: Dict[str, object] = {
+            "ft": np.stack(ft)[:, : nm - nr], "fc": np.stack(fc)[:, : s.nrig],
+            "torque": np.stack(tq)[:, : s.nrig], "elj": self.elj.copy(), "eqq": self.eqq.copy(),
+        }
+        if want_sites:
+            out["f"] = np.stack(fs)
+        for k in ("uewa", "urf", "ulr", "uself", "uconf", "uavex", "press", "vir", "ewqLL",
+                  "ewqWL", "ewqWW"):
+            out[k] = getattr(e, k)
+        out["fws"] = np.array([list(e.fwsx), list(e.fwsy), list(e.fwsz)])
+        return out
+
+    def shake(self, s: System, ft: np.ndarray):
+        """Verlet + SHAKE on s in place (x0.., xold..); ft: (3, nmove-nriga)."""
+        nl = s.nliqa
+        xo = np.ascontiguousarray(s.xold[nl:])
+        yo = np.ascontiguousarray(s.yold[nl:])
+        zo = np.ascontiguousarray(s.zold[nl:])
+        f = [np.ascontiguousarray(ft[d]) for d in range(3)]
+        kps = np.zeros(s.nit)
+        tk = C.c_double()
+        sw = C.c_int32()
+        rc = self.lib.shake(self.h, _dp(s.x0), _dp(s.y0), _dp(s.z0), _dp(xo), _dp(yo), _dp(zo),
+                            _dp(f[0]), _dp(f[1]), _dp(f[2]), _dp(kps), C.byref(tk), C.byref(sw))
+        s.xold[nl:], s.yold[nl:], s.zold[nl:] = xo, yo, zo
+        self._check(rc)
+        return {"kps": kps, "tkps": tk.value, "sweeps": sw.value}

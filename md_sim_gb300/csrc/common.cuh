@@ -1,0 +1,66 @@
+// common.cuh - device helpers shared by the md_sim GB300 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+// Single-precision Fortran literals promoted to real*8 (src/global.f90:18-24, src/forcem.f90:11-13).
+#define F32D(x) ((double)(x##f))
+
+namespace mdg {
+
+constexpr double kA1 = F32D(0.254829592), kA2 = F32D(-0.284496736), kA3 = F32D(1.421413741);
+constexpr double kA4 = F32D(-1.453152027), kA5 = F32D(1.061405429), kP = F32D(0.3275911);
+
+// status words written by kernels, read by the host after a phase
+enum StatusWord {
+    ST_LIST_OVF = 0,   // head-head list overflow (count stored)
+    ST_WLIST_OVF = 1,  // head-wall list overflow
+    ST_SHAKE_MAXIT = 2,
+    ST_SHAKE_RPTOL = 3,  // 1 + first failing constraint (molecule * 8 + is)
+    ST_CELL_OVF = 4,
+    ST_REBUILD = 5,    // 1 when the current step rebuilt the list
+    ST_SWEEPS = 6,     // SHAKE sweeps of the last call
+    ST_NWORDS = 8
+};
+
+// Minimum image with the reference's rounding, no multiply-add contraction:
+// d - l*anint(d*li)   (src/nnlist.f90:125, src/forcem.f90:293).  anint = round half away.
+__device__ __forceinline__ double minimg(double d, double l, double li) {
+    return __dsub_rn(d, __dmul_rn(l, round(__dmul_rn(d, li))));
+}
+
+// x*x + y*y + z*z evaluated as ((x*x + y*y) + z*z) with separately rounded products.
+__device__ __forceinline__ double dist2_exact(double x, double y, double z) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum into *dst with one atomic per block; all threads must call.
+template <int NT>
+__device__ __forceinline__ void block_atomic_sum(double v, double* dst) {
+    __shared__ double red[NT / 32];
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        double s = (l < NT / 32) ? red[l] : 0.0;
+        s = warp_sum(s);
+        if (l == 0) atomicAdd(dst, s);
+    }
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+}  // namespace mdg

@@ -1,0 +1,169 @@
+// ctx.h - device-side state of one md_sim system and the launch interface of each phase.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mdgpu.h"
+
+namespace mdg {
+
+// Offsets in the FP64 accumulator block (after elj[nijt], eqq[nijt]).
+enum AccSlot {
+    ACC_UEWA = 0,
+    ACC_EWQLL,
+    ACC_ULR,
+    ACC_DIPZ,
+    ACC_MAXD,   // max squared displacement since the last rebuild
+    ACC_FWS,    // 9 values: fwsx(-1:1), fwsy(-1:1), fwsz(-1:1)
+    ACC_FWS0 = ACC_FWS + 9,  // sum of all forces x,y,z (fws*(0))
+    ACC_NSLOT = ACC_FWS0 + 3
+};
+
+// Plain view of the device arrays, passed to kernels by value.
+struct View {
+    int nrig, nriga, nliqa, nmove, nwall, ntota, nit, nijt, nltype, nheads;
+    int bulk;   // MDG_BULK semantics in the real-space loops
+    int pbcz;   // z minimum image in the neighbour list
+    double lx, ly, lz, lxi, lyi, lzi, lwh;
+    double rcut, rcutsq, skin, alfa, spii, facq, rskinsq, dshsq;
+    // atoms
+    double *x, *y, *z;         // ntota
+    double *rsx, *rsy, *rsz;   // nmove
+    double *cx, *cy, *cz;      // nrig (current centres of mass)
+    double *ocx, *ocy, *ocz;   // nrig at the last rebuild
+    double *ox, *oy, *oz;      // flexible atoms at the last rebuild (index - nriga)
+    const double *q, *mii, *mi;
+    const int* type;           // 0-based site type, ntota
+    // type tables
+    const int* nsi;            // nit
+    const int* ijt;            // nit*nit, 0-based pair index, [it*nit + jt]
+    const int* vdw;            // nijt
+    const double *eps, *sig, *aa, *rhoi, *cc;
+    // forces
+    double *fx, *fy, *fz;      // nmove
+    // heads and lists
+    const int* head_atom;      // nheads
+    int* nb;                   // nheads * maxnb: partner atoms j > i
+    int* nbcnt;                // nheads
+    int maxnb;
+    int* wnb;                  // nheads * maxwnb: wall atoms
+    int* wnbcnt;
+    int maxwnb;
+    const int* excl_off;       // ntota + 1
+    const int* excl;
+    // accumulators and status
+    double* acc;               // 2*nijt + ACC_NSLOT
+    int* status;               // ST_NWORDS
+};
+
+// Cell grid used by the list build.
+struct Grid {
+    int nc[3];
+    double cs[3];
+    double org[3];
+    int periodic[3];
+    int ncell;
+};
+
+struct KSet {
+    int nk = 0;          // valid k vectors (reference order: l outer, m, n innermost)
+    int nrow = 0;        // (l, m) rows
+    int klmax = 0, kmmax = 0, knmax = 0;
+    double pipix = 0, pipiy = 0, pipiz = 0;
+    // device
+    int4* row = nullptr;          // per row: l, m, n_first, k_first (n runs n_first..|n_first| or 1..)
+    int* row_nlen = nullptr;      // per row: number of n
+    double* ak = nullptr;         // nk
+    double2* qw = nullptr;        // nk static wall structure factor
+    double2* s = nullptr;         // nk moving-atom structure factor (accumulated)
+    double2* c = nullptr;         // nk: Ak * conj(S_total)
+    int3* kvec = nullptr;         // nk: (l, m, n)
+    int* witem_row = nullptr;     // k_sfac work items: row
+    int* witem_n0 = nullptr;      //                    n offset inside the row
+    int nwork = 0, tile = 0, splits = 1, atoms_per_split = 0, sfac_smem = 0, force_smem = 0;
+};
+
+struct Ctx {
+    mdg_sysdesc sysc;   // sizes only (pointers not kept)
+    View v{};
+    Grid grid{}, wgrid{};
+    KSet ks;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int precision = MDG_FP64;
+    int variant = MDG_SLAB;
+    uint32_t quirks = 0;
+    double uself = 0, ewqWW = 0;
+    double lr_tab[9][16];  // flr_l, flr_w, flr_lja, flr_ljc, flr_bua, flr_buc, flr_bur, ulr_l, ulr_w per type
+    double* d_lr = nullptr;  // same table on the device [9][nit]
+    // device buffers owned here
+    std::vector<void*> owned;
+    // list build scratch
+    int *d_cell_start = nullptr, *d_cell_count = nullptr, *d_head_cell = nullptr;
+    int* d_wcell_start = nullptr;
+    float4* d_cpos = nullptr;     // wrapped head positions sorted by cell, w = atom index bits
+    float4* d_wpos = nullptr;     // wrapped wall positions sorted by cell
+    double4* d_hpos = nullptr;    // wrapped head positions in head order
+    // SHAKE
+    int ncons = 0, ncmax = 0, shake_seq = 0, maxit = 10;
+    double tol2 = 1e-8, rptol = 0.85;
+    int* d_cons = nullptr;        // ncons * 3 * 2 atom indices (0-based), -1 unused
+    double* d_clen2 = nullptr;    // ncons * 3 squared lengths
+    int* d_cons_n = nullptr;      // ncons constraints per molecule
+    double *d_xold = nullptr, *d_yold = nullptr, *d_zold = nullptr;  // ntota - nliqa
+    double* d_kps = nullptr;      // nit
+    double* d_ft_in = nullptr;    // 3 x (nmove - nriga) forces handed to SHAKE
+    int* d_sweeps = nullptr;      // [0] sweeps, [1] done
+    int* d_seq_flags = nullptr;   // moving/moved of the sequential SHAKE
+    int64_t nfreed = 0;
+    // angles
+    int nang_terms = 0;
+    int* d_ang = nullptr;         // per term i, j, k (0-based), type slot
+    double *d_ang_kt = nullptr, *d_ang_th = nullptr;
+    std::vector<double> h_qs_wall;  // wall charges (for the static structure factor)
+    double *d_ft = nullptr, *d_fc = nullptr, *d_tq = nullptr;  // force_sum outputs
+    bool alloc_failed = false;
+    // host staging (pinned)
+    double* h_acc = nullptr;
+    int* h_status = nullptr;
+    std::string err;
+};
+
+// ---- phase launchers (each .cu file) -------------------------------------------------
+// nnlist.cu
+int nnlist_setup(Ctx& c, const double* x0, const double* y0, const double* z0);
+void nnlist_trigger(Ctx& c, bool force);
+void nnlist_build(Ctx& c);
+// pair.cu
+void pair_forces_fp64(Ctx& c);
+void wall_forces_fp64(Ctx& c);
+void surf_partition(Ctx& c);
+void lr_tail(Ctx& c);
+void pair_forces_fp32(Ctx& c);
+void wall_forces_fp32(Ctx& c);
+// recip.cu
+int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const double* z0);
+void recip_fp64(Ctx& c);
+// epilogue.cu
+void dipole_correction(Ctx& c);
+void angle_forces(Ctx& c);
+void force_sum(Ctx& c, double* d_ft, double* d_fc, double* d_tq);
+// shake.cu
+int shake_setup(Ctx& c, const mdg_sysdesc* s);
+void shake_launch(Ctx& c);
+
+int set_err(Ctx* c, int code, const std::string& msg);
+void* dalloc(Ctx& c, size_t bytes);
+
+}  // namespace mdg
+
+#define MDG_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return ::mdg::set_err(&c, MDG_E_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)

@@ -1,0 +1,349 @@
+// nnlist.cu - Verlet list rebuild on the GPU (replaces nnlist_init/nnlist_make,
+// src/nnlist.f90:14-165) and the rebuild trigger of force_real (src/forcem.f90:245-250).
+//
+// The reference filters a stored O(heads^2) candidate list.  Here heads are binned into a cell
+// grid whose cells are at least rskin wide, so every pair the reference keeps lies in the same
+// or a neighbouring cell.  Candidates from the 27 (or fewer) cells pass a conservative FP32
+// test on wrapped coordinates and then the reference's own FP64 test, evaluated with the same
+// roundings (separate multiplies and adds, anint = round half away from zero), so the kept set
+// is identical to the reference's.  Pairs are stored under the lower atom index as in
+// list1/list2 (i < j); head-wall pairs under the head.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+#include "ctx.h"
+
+namespace mdg {
+
+namespace {
+
+constexpr int kNT = 256;
+
+__device__ __forceinline__ int cell_coord(double w, int d, const Grid& g) {
+    int c = (int)floor((w - g.org[d]) / g.cs[d]);
+    return min(max(c, 0), g.nc[d] - 1);
+}
+
+__device__ __forceinline__ double wrap(double x, double l, int periodic) {
+    return periodic ? x - l * floor(x / l) : x;
+}
+
+// Max squared displacement since the last rebuild; sets the rebuild flag.
+__global__ void k_trigger(View v, int force) {
+    double m = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.nrig + (v.nmove - v.nriga);
+         i += gridDim.x * blockDim.x) {
+        double a, b, c;
+        if (i < v.nrig) {
+            a = v.ocx[i] - v.cx[i];
+            b = v.ocy[i] - v.cy[i];
+            c = v.ocz[i] - v.cz[i];
+        } else {
+            const int k = i - v.nrig, at = k + v.nriga;
+            a = v.ox[k] - v.x[at];
+            b = v.oy[k] - v.y[at];
+            c = v.oz[k] - v.z[at];
+        }
+        m = fmax(m, a * a + b * b + c * c);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&v.acc[2 * v.nijt + ACC_MAXD], m);
+    (void)force;
+}
+
+__global__ void k_trigger_decide(View v, int force) {
+    const double aux = fmax(v.acc[2 * v.nijt + ACC_MAXD], v.dshsq);
+    v.status[ST_REBUILD] = (force || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
+    v.acc[2 * v.nijt + ACC_MAXD] = 0.0;
+}
+
+// Bin heads: cell index + count; saves the reference positions of the rebuild.
+__global__ void k_bin_heads(View v, Grid g, int* head_cell, int* cell_count, double4* hpos) {
+    if (!v.status[ST_REBUILD]) return;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < v.nheads) {
+        const int a = v.head_atom[h];
+        const double wx = wrap(v.x[a], v.lx, g.periodic[0]);
+        const double wy = wrap(v.y[a], v.ly, g.periodic[1]);
+        const double wz = wrap(v.z[a], v.lz, g.periodic[2]);
+        const int c = (cell_coord(wz, 2, g) * g.nc[1] + cell_coord(wy, 1, g)) * g.nc[0] + cell_coord(wx, 0, g);
+        head_cell[h] = c;
+        hpos[h] = make_double4(wx, wy, wz, 0.0);
+        atomicAdd(&cell_count[c], 1);
+    }
+    // reference positions (src/nnlist.f90:99-119)
+    for (int i = h; i < v.nrig; i += gridDim.x * blockDim.x) {
+        v.ocx[i] = v.cx[i];
+        v.ocy[i] = v.cy[i];
+        v.ocz[i] = v.cz[i];
+    }
+    for (int i = h; i < v.nmove - v.nriga; i += gridDim.x * blockDim.x) {
+        v.ox[i] = v.x[i + v.nriga];
+        v.oy[i] = v.y[i + v.nriga];
+        v.oz[i] = v.z[i + v.nriga];
+    }
+}
+
+// Exclusive scan of the cell counts (one block) -> cell_start; resets counts to use as cursors.
+__global__ void k_scan_cells(View v, int ncell, int* cell_count, int* cell_start) {
+    if (!v.status[ST_REBUILD]) return;
+    __shared__ int carry;
+    __shared__ int part[kNT];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ncell; base += kNT) {
+        const int i = base + threadIdx.x;
+        const int val = i < ncell ? cell_count[i] : 0;
+        part[threadIdx.x] = val;
+        __syncthreads();
+        for (int o = 1; o < kNT; o <<= 1) {
+            int t = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+            __syncthreads();
+            part[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < ncell) {
+            cell_start[i] = carry + part[threadIdx.x] - val;
+            cell_count[i] = 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == kNT - 1) carry += part[kNT - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cell_start[ncell] = carry;
+}
+
+__global__ void k_scatter_heads(View v, const int* head_cell, int* cell_count, const int* cell_start,
+                                const double4* hpos, float4* cpos) {
+    if (!v.status[ST_REBUILD]) return;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= v.nheads) return;
+    const int c = head_cell[h];
+    const int slot = cell_start[c] + atomicAdd(&cell_count[c], 1);
+    const double4 p = hpos[h];
+    cpos[slot] = make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float(v.head_atom[h]));
+}
+
+__device__ __forceinline__ bool excluded(const View& v, int i, int j) {
+    for (int k = v.excl_off[i]; k < v.excl_off[i + 1]; ++k)
+        if (v.excl[k] == j) return true;
+    return false;
+}
+
+// Reference test of src/nnlist.f90:124-130 with identical rounding.
+__device__ __forceinline__ bool keep_pair(const View& v, double xi, double yi, double zi, double xj,
+                                          double yj, double zj) {
+    const double dx = minimg(__dsub_rn(xi, xj), v.lx, v.lxi);
+    const double dy = minimg(__dsub_rn(yi, yj), v.ly, v.lyi);
+    double dz = __dsub_rn(zi, zj);
+    if (v.pbcz) dz = minimg(dz, v.lz, v.lzi);
+    return dist2_exact(dx, dy, dz) < v.rskinsq;
+}
+
+__device__ __forceinline__ float fmin_img(float d, float l, float li, int periodic) {
+    return periodic ? d - l * rintf(d * li) : d;
+}
+
+// One thread per head: scan neighbouring cells, keep partners j > i.
+__global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* cpos, const double4* hpos) {
+    if (!v.status[ST_REBUILD]) return;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= v.nheads) return;
+    const int ia = v.head_atom[h];
+    const double4 pw = hpos[h];
+    const float px = (float)pw.x, py = (float)pw.y, pz = (float)pw.z;
+    const double xi = v.x[ia], yi = v.y[ia], zi = v.z[ia];
+    const float lxf = (float)v.lx, lyf = (float)v.ly, lzf = (float)v.lz;
+    const float lxif = 1.0f / lxf, lyif = 1.0f / lyf, lzif = 1.0f / lzf;
+    const float lim = (float)v.rskinsq * 1.0001f + 0.05f;  // conservative: FP32 errors are ~1e-4 A^2
+    const int cx = cell_coord(pw.x, 0, g), cy = cell_coord(pw.y, 1, g), cz = cell_coord(pw.z, 2, g);
+    const bool surf_i = ia >= v.nliqa;
+    int cnt = 0;
+    int* out = v.nb + (size_t)h * v.maxnb;
+    const int rz = g.nc[2] >= 3 ? 1 : 0, ry = g.nc[1] >= 3 ? 1 : 0, rx = g.nc[0] >= 3 ? 1 : 0;
+    for (int dz = -rz; dz <= rz; ++dz) {
+        int zz = cz + dz;
+        if (g.periodic[2]) zz = (zz + g.nc[2]) % g.nc[2];
+        else if (zz < 0 || zz >= g.nc[2]) continue;
+        for (int dy = -ry; dy <= ry; ++dy) {
+            const int yy = (cy + dy + g.nc[1]) % g.nc[1];
+            for (int dx = -rx; dx <= rx; ++dx) {
+                const int xx = (cx + dx + g.nc[0]) % g.nc[0];
+                const int c = (zz * g.nc[1] + yy) * g.nc[0] + xx;
+                for (int s = cell_start[c]; s < cell_start[c + 1]; ++s) {
+                    const float4 q = cpos[s];
+                    const int ja = __float_as_int(q.w);
+                    if (ja <= ia) continue;
+                    float ddx = fmin_img(px - q.x, lxf, lxif, 1);
+                    float ddy = fmin_img(py - q.y, lyf, lyif, 1);
+                    float ddz = fmin_img(pz - q.z, lzf, lzif, g.periodic[2]);
+                    if (ddx * ddx + ddy * ddy + ddz * ddz > lim) continue;
+                    if (surf_i && ja >= v.nliqa && excluded(v, ia, ja)) continue;
+                    if (!keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja])) continue;
+                    if (cnt < v.maxnb) out[cnt] = ja;
+                    ++cnt;
+                }
+            }
+        }
+    }
+    if (cnt > v.maxnb) atomicMax(&v.status[ST_LIST_OVF], cnt);
+    v.nbcnt[h] = min(cnt, v.maxnb);
+}
+
+// One thread per head: all wall atoms within rskin (src/nnlist.f90:143-161).
+__global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4* wpos, const double4* hpos) {
+    if (!v.status[ST_REBUILD]) return;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= v.nheads) return;
+    const int ia = v.head_atom[h];
+    const double xi = v.x[ia], yi = v.y[ia], zi = v.z[ia];
+    const double4 pw = hpos[h];
+    const float px = (float)pw.x, py = (float)pw.y, pz = (float)pw.z;
+    const float lxf = (float)v.lx, lyf = (float)v.ly, lzf = (float)v.lz;
+    const float lxif = 1.0f / lxf, lyif = 1.0f / lyf, lzif = 1.0f / lzf;
+    const float lim = (float)v.rskinsq * 1.0001f + 0.05f;
+    const double wz = wrap(zi, v.lz, g.periodic[2]);
+    const int cx = cell_coord(pw.x, 0, g), cy = cell_coord(pw.y, 1, g), cz = cell_coord(wz, 2, g);
+    const bool surf_i = ia >= v.nliqa;
+    int cnt = 0;
+    int* out = v.wnb + (size_t)h * v.maxwnb;
+    const int rz = g.nc[2] >= 3 ? 1 : 0, ry = g.nc[1] >= 3 ? 1 : 0, rx = g.nc[0] >= 3 ? 1 : 0;
+    for (int dz = -rz; dz <= rz; ++dz) {
+        int zz = cz + dz;
+        if (g.periodic[2]) zz = (zz + g.nc[2]) % g.nc[2];
+        else if (zz < 0 || zz >= g.nc[2]) continue;
+        for (int dy = -ry; dy <= ry; ++dy) {
+            const int yy = (cy + dy + g.nc[1]) % g.nc[1];
+            for (int dx = -rx; dx <= rx; ++dx) {
+                const int xx = (cx + dx + g.nc[0]) % g.nc[0];
+                const int c = (zz * g.nc[1] + yy) * g.nc[0] + xx;
+                for (int s = wcell_start[c]; s < wcell_start[c + 1]; ++s) {
+                    const float4 q = wpos[s];
+                    const int ja = __float_as_int(q.w);
+                    float ddx = fmin_img(px - q.x, lxf, lxif, 1);
+                    float ddy = fmin_img(py - q.y, lyf, lyif, 1);
+                    float ddz = fmin_img(pz - q.z, lzf, lzif, g.periodic[2]);
+                    if (ddx * ddx + ddy * ddy + ddz * ddz > lim) continue;
+                    if (surf_i && excluded(v, ia, ja)) continue;
+                    if (!keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja])) continue;
+                    if (cnt < v.maxwnb) out[cnt] = ja;
+                    ++cnt;
+                }
+            }
+        }
+    }
+    if (cnt > v.maxwnb) atomicMax(&v.status[ST_WLIST_OVF], cnt);
+    v.wnbcnt[h] = min(cnt, v.maxwnb);
+}
+
+Grid make_grid(double lx, double ly, double lz, double rs, int pz, double zlo, double zhi) {
+    Grid g{};
+    const double L[3] = {lx, ly, lz};
+    for (int d = 0; d < 3; ++d) {
+        const bool per = d < 2 || pz;
+        g.periodic[d] = per ? 1 : 0;
+        double span = per ? L[d] : std::max(zhi - zlo, 1e-6);
+        int n = (int)std::floor(span / (rs * (1.0 + 1e-9)));
+        if (n < 3) n = 1;
+        n = std::min(n, 256);
+        g.nc[d] = n;
+        g.cs[d] = span / n;
+        g.org[d] = per ? 0.0 : zlo;
+        if (n == 1) g.cs[d] = std::max(span, rs) * 2.0;  // everything in one cell
+    }
+    g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
+    return g;
+}
+
+}  // namespace
+
+int nnlist_setup(Ctx& c, const double* x0, const double* y0, const double* z0) {
+    View& v = c.v;
+    const double rs = std::sqrt(v.rskinsq);
+    // head grid: z spans the box (clamped for non-periodic boxes)
+    c.grid = make_grid(v.lx, v.ly, v.lz, rs, v.pbcz, -0.5 * v.lz, 0.5 * v.lz);
+    // wall grid: static wall atoms binned once
+    double zlo = 0, zhi = 1;
+    if (v.nwall > 0) {
+        zlo = 1e300;
+        zhi = -1e300;
+        for (int i = v.nmove; i < v.ntota; ++i) {
+            double w = v.pbcz ? z0[i] - v.lz * std::floor(z0[i] / v.lz) : z0[i];
+            zlo = std::min(zlo, w);
+            zhi = std::max(zhi, w);
+        }
+        zlo -= 1e-3;
+        zhi += 1e-3;
+    }
+    c.wgrid = make_grid(v.lx, v.ly, v.lz, rs, v.pbcz, zlo, zhi);
+    const Grid& g = c.grid;
+    c.d_cell_start = (int*)dalloc(c, sizeof(int) * (g.ncell + 1));
+    c.d_cell_count = (int*)dalloc(c, sizeof(int) * g.ncell);
+    c.d_head_cell = (int*)dalloc(c, sizeof(int) * std::max(v.nheads, 1));
+    c.d_hpos = (double4*)dalloc(c, sizeof(double4) * std::max(v.nheads, 1));
+    // wall bins on the host (once)
+    const Grid& wg = c.wgrid;
+    std::vector<int> wcount(wg.ncell + 1, 0), wcell(std::max(v.nwall, 1));
+    auto cc = [&](double w, int d) {
+        int k = (int)std::floor((w - wg.org[d]) / wg.cs[d]);
+        return std::min(std::max(k, 0), wg.nc[d] - 1);
+    };
+    std::vector<float4> wp(std::max(v.nwall, 1));
+    for (int k = 0; k < v.nwall; ++k) {
+        const int i = v.nmove + k;
+        double wx = x0[i] - v.lx * std::floor(x0[i] / v.lx);
+        double wy = y0[i] - v.ly * std::floor(y0[i] / v.ly);
+        double wz = v.pbcz ? z0[i] - v.lz * std::floor(z0[i] / v.lz) : z0[i];
+        wcell[k] = (cc(wz, 2) * wg.nc[1] + cc(wy, 1)) * wg.nc[0] + cc(wx, 0);
+        wcount[wcell[k] + 1]++;
+    }
+    for (int k = 0; k < wg.ncell; ++k) wcount[k + 1] += wcount[k];
+    std::vector<int> cur(wcount.begin(), wcount.end() - 1);
+    std::vector<float4> wsorted(std::max(v.nwall, 1));
+    for (int k = 0; k < v.nwall; ++k) {
+        const int i = v.nmove + k;
+        double wx = x0[i] - v.lx * std::floor(x0[i] / v.lx);
+        double wy = y0[i] - v.ly * std::floor(y0[i] / v.ly);
+        double wz = v.pbcz ? z0[i] - v.lz * std::floor(z0[i] / v.lz) : z0[i];
+        float4 f;
+        f.x = (float)wx;
+        f.y = (float)wy;
+        f.z = (float)wz;
+        int ia = i;
+        std::memcpy(&f.w, &ia, 4);
+        wsorted[cur[wcell[k]]++] = f;
+    }
+    c.d_wcell_start = (int*)dalloc(c, sizeof(int) * (wg.ncell + 1));
+    c.d_wpos = (float4*)dalloc(c, sizeof(float4) * std::max(v.nwall, 1));
+    MDG_CUDA(cudaMemcpy(c.d_wcell_start, wcount.data(), sizeof(int) * (wg.ncell + 1), cudaMemcpyHostToDevice));
+    MDG_CUDA(cudaMemcpy(c.d_wpos, wsorted.data(), sizeof(float4) * std::max(v.nwall, 1), cudaMemcpyHostToDevice));
+    c.d_cpos = (float4*)dalloc(c, sizeof(float4) * std::max(v.nheads, 1));
+    return MDG_OK;
+}
+
+void nnlist_trigger(Ctx& c, bool force) {
+    View& v = c.v;
+    const int n = v.nrig + (v.nmove - v.nriga);
+    const int nb = std::max(1, std::min((n + kNT - 1) / kNT, 1024));
+    k_trigger<<<nb, kNT, 0, c.stream>>>(v, force ? 1 : 0);
+    k_trigger_decide<<<1, 1, 0, c.stream>>>(v, force ? 1 : 0);
+}
+
+void nnlist_build(Ctx& c) {
+    View& v = c.v;
+    const Grid& g = c.grid;
+    const int nh = std::max(v.nheads, 1);
+    const int nbk = std::max((std::max(nh, std::max(v.nrig, v.nmove - v.nriga)) + kNT - 1) / kNT, 1);
+    cudaMemsetAsync(c.d_cell_count, 0, sizeof(int) * g.ncell, c.stream);
+    k_bin_heads<<<nbk, kNT, 0, c.stream>>>(v, g, c.d_head_cell, c.d_cell_count, c.d_hpos);
+    k_scan_cells<<<1, kNT, 0, c.stream>>>(v, g.ncell, c.d_cell_count, c.d_cell_start);
+    k_scatter_heads<<<(nh + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, c.d_head_cell, c.d_cell_count, c.d_cell_start,
+                                                                 c.d_hpos, c.d_cpos);
+    k_build_hh<<<(nh + 127) / 128, 128, 0, c.stream>>>(v, g, c.d_cell_start, c.d_cpos, c.d_hpos);
+    if (v.nwall > 0)
+        k_build_hw<<<(nh + 127) / 128, 128, 0, c.stream>>>(v, c.wgrid, c.d_wcell_start, c.d_wpos, c.d_hpos);
+}
+
+}  // namespace mdg

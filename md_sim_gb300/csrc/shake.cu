@@ -1,0 +1,329 @@
+// shake.cu - move_shake (src/move.f90:408-529) on the GPU.
+//
+// Verlet step of the surface atoms (:416-439) with the per-type kinetic sums kps, then SHAKE.
+// The reference sweeps molecules in order (Gauss-Seidel), skips a constraint when neither atom
+// moved in the previous sweep, and resets `done` per molecule (:458), so the loop length is
+// decided by the last molecule alone (stop after its first sweep without an update, at most
+// maxit+1 sweeps).  When no moving atom belongs to two constrained molecules, molecules evolve
+// independently; then
+//   k_shake_last  replays the last molecule on private copies to get that sweep count, and
+//   k_shake_mol   runs every molecule for exactly that many sweeps, one thread per molecule,
+// which gives the reference's positions exactly.  Frozen atoms (index >= nmove) never count as
+// moved, as moved(ismax+1:ntota) = 1 in the reference.  Topologies that share moving atoms
+// between molecules fall back to k_shake_seq, a single-thread copy of the reference loop.
+// Every loop is bounded by maxit+1 sweeps.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "ctx.h"
+
+namespace mdg {
+
+namespace {
+
+constexpr int kNT = 128;
+constexpr int kMaxAt = 6;
+
+struct ShakeArgs {
+    int ncons, maxit, clean, nliqa, nmove;
+    double tol2, rptol;
+    const int* cons;      // ncons * 6: (a0,b0,a1,b1,a2,b2), -1 unused
+    const double* clen2;  // ncons * 3
+    const int* cons_n;    // ncons
+    double *xo, *yo, *zo; // xold(nliqa:ntota)
+    int* sweeps_out;      // [0] sweeps decided, [1] done flag
+};
+
+__global__ void k_verlet(View v, const double* ft, double* xo, double* yo, double* zo, double* kps) {
+    const int i = v.nliqa + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.nmove) return;
+    const int k = i - v.nliqa, f = i - v.nriga;
+    const int nflex = v.nmove - v.nriga;
+    const double m = v.mii[i];
+    double aux = v.x[i] - xo[k];
+    xo[k] = v.x[i];
+    aux = minimg(aux, v.lx, v.lxi);
+    v.x[i] = v.x[i] + aux + ft[f] * m;
+    double kaux = aux * aux;
+    aux = v.y[i] - yo[k];
+    yo[k] = v.y[i];
+    aux = minimg(aux, v.ly, v.lyi);
+    v.y[i] = v.y[i] + aux + ft[nflex + f] * m;
+    kaux = kaux + aux * aux;
+    aux = v.z[i] - zo[k];
+    zo[k] = v.z[i];
+    v.z[i] = v.z[i] + aux + ft[2 * nflex + f] * m;
+    kaux = kaux + aux * aux;
+    atomicAdd(&kps[v.type[i]], v.mi[i] * kaux);
+}
+
+// One molecule's state in registers.
+struct Mol {
+    int n;               // constraints
+    int at[kMaxAt];      // distinct atoms
+    int na;
+    int ca[3], cb[3];    // local slots of the constraint atoms
+    double l2[3];
+};
+
+__device__ __forceinline__ int slot_of(Mol& m, int a) {
+    for (int s = 0; s < m.na; ++s)
+        if (m.at[s] == a) return s;
+    m.at[m.na] = a;
+    return m.na++;
+}
+
+__device__ void load_mol(const ShakeArgs& A, int ic, Mol& m) {
+    m.n = A.cons_n[ic];
+    m.na = 0;
+    for (int s = 0; s < m.n; ++s) {
+        m.ca[s] = slot_of(m, A.cons[ic * 6 + 2 * s]);
+        m.cb[s] = slot_of(m, A.cons[ic * 6 + 2 * s + 1]);
+        m.l2[s] = A.clen2[ic * 3 + s];
+    }
+}
+
+// One sweep over the molecule; returns true when some constraint was corrected.
+// moved bit s = 1: atom in slot s was NOT moved in the previous sweep (reference `moved` = 1).
+__device__ bool sweep(const View& v, const ShakeArgs& A, const Mol& m, double* px, double* py, double* pz,
+                      const double* ox, const double* oy, const double* oz, unsigned& moved, int* fail) {
+    unsigned moving = (1u << kMaxAt) - 1u;
+    bool upd = false;
+    for (int s = 0; s < m.n; ++s) {
+        const int a = m.ca[s], b = m.cb[s];
+        if (((moved >> a) & 1u) && ((moved >> b) & 1u)) continue;
+        double pxab = minimg(px[a] - px[b], v.lx, v.lxi);
+        double pyab = minimg(py[a] - py[b], v.ly, v.lyi);
+        double pzab = minimg(pz[a] - pz[b], v.lz, v.lzi);
+        const double rabsq = m.l2[s];
+        const double diffsq = rabsq - (pxab * pxab + pyab * pyab + pzab * pzab);
+        if (fabs(diffsq) > rabsq * A.tol2) {
+            const double rx = minimg(ox[a] - ox[b], v.lx, v.lxi);
+            const double ry = minimg(oy[a] - oy[b], v.ly, v.lyi);
+            const double rz = minimg(oz[a] - oz[b], v.lz, v.lzi);
+            const double rpab = rx * pxab + ry * pyab + rz * pzab;
+            if (rpab < rabsq * A.rptol) {
+                *fail = 1;
+                return upd;
+            }
+            double rma = v.mii[m.at[a]], rmb = v.mii[m.at[b]];
+            const double aux = diffsq / (2.0 * (rma + rmb) * rpab);
+            rma = rma * aux;
+            rmb = rmb * aux;
+            px[a] = px[a] + rx * rma; py[a] = py[a] + ry * rma; pz[a] = pz[a] + rz * rma;
+            px[b] = px[b] - rx * rmb; py[b] = py[b] - ry * rmb; pz[b] = pz[b] - rz * rmb;
+            moving &= ~((1u << a) | (1u << b));
+            upd = true;
+        }
+    }
+    // frozen atoms keep moved = 1
+    unsigned frozen = 0;
+    for (int s = 0; s < m.na; ++s)
+        if (m.at[s] >= A.nmove) frozen |= 1u << s;
+    moved = moving | frozen;
+    return upd;
+}
+
+__device__ void gather(const View& v, const ShakeArgs& A, const Mol& m, double* px, double* py, double* pz,
+                       double* ox, double* oy, double* oz, unsigned& moved) {
+    moved = 0;
+    for (int s = 0; s < m.na; ++s) {
+        const int a = m.at[s];
+        px[s] = v.x[a]; py[s] = v.y[a]; pz[s] = v.z[a];
+        const int k = a - A.nliqa;
+        ox[s] = A.xo[k]; oy[s] = A.yo[k]; oz[s] = A.zo[k];
+        if (a >= A.nmove) moved |= 1u << s;
+    }
+}
+
+__global__ void k_shake_init(ShakeArgs A) {
+    A.sweeps_out[0] = 0;
+    A.sweeps_out[1] = 1;
+}
+
+__global__ void k_shake_last(View v, ShakeArgs A) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Mol m;
+    load_mol(A, A.ncons - 1, m);
+    double px[kMaxAt], py[kMaxAt], pz[kMaxAt], ox[kMaxAt], oy[kMaxAt], oz[kMaxAt];
+    unsigned moved;
+    gather(v, A, m, px, py, pz, ox, oy, oz, moved);
+    int fail = 0, s = 0;
+    bool done = false;
+    while (!done && s <= A.maxit) {
+        done = !sweep(v, A, m, px, py, pz, ox, oy, oz, moved, &fail);
+        ++s;
+        if (fail) break;
+    }
+    A.sweeps_out[0] = s;
+    A.sweeps_out[1] = done ? 1 : 0;
+}
+
+__global__ void k_shake_mol(View v, ShakeArgs A) {
+    const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ic >= A.ncons) return;
+    Mol m;
+    load_mol(A, ic, m);
+    double px[kMaxAt], py[kMaxAt], pz[kMaxAt], ox[kMaxAt], oy[kMaxAt], oz[kMaxAt];
+    unsigned moved;
+    gather(v, A, m, px, py, pz, ox, oy, oz, moved);
+    int fail = 0;
+    int s = 0;
+    const int nsw = A.clean ? A.maxit + 1 : A.sweeps_out[0];
+    bool converged = false;
+    for (; s < nsw; ++s) {
+        const bool upd = sweep(v, A, m, px, py, pz, ox, oy, oz, moved, &fail);
+        if (fail) {
+            atomicCAS(&v.status[ST_SHAKE_RPTOL], 0, 1 + ic * 8 + 0);
+            break;
+        }
+        if (!upd) {
+            converged = true;
+            if (A.clean) break;
+        }
+    }
+    if (A.clean) {
+        atomicMax(&A.sweeps_out[0], s + (converged ? 1 : 0));
+        if (!converged) atomicAnd(&A.sweeps_out[1], 0);
+    }
+    for (int t = 0; t < m.na; ++t) {
+        const int a = m.at[t];
+        if (a < A.nmove) {
+            v.x[a] = px[t]; v.y[a] = py[t]; v.z[a] = pz[t];
+        }
+    }
+}
+
+// Single-thread copy of the reference loop for topologies with shared moving atoms.
+__global__ void k_shake_seq(View v, ShakeArgs A, int* moving, int* movd) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int nsurf = A.nmove - A.nliqa;
+    for (int i = 0; i < nsurf; ++i) {
+        moving[i] = 1;
+        movd[i] = 0;
+    }
+    bool done = false;
+    int ite = 0;
+    while (!(done || ite > A.maxit)) {
+        bool any = false;
+        for (int ic = 0; ic < A.ncons; ++ic) {
+            done = true;
+            for (int s = 0; s < A.cons_n[ic]; ++s) {
+                const int ia = A.cons[ic * 6 + 2 * s], ib = A.cons[ic * 6 + 2 * s + 1];
+                const int ma = ia < A.nmove ? movd[ia - A.nliqa] : 1;
+                const int mb = ib < A.nmove ? movd[ib - A.nliqa] : 1;
+                if (ma * mb != 0) continue;
+                const double pxab = minimg(v.x[ia] - v.x[ib], v.lx, v.lxi);
+                const double pyab = minimg(v.y[ia] - v.y[ib], v.ly, v.lyi);
+                const double pzab = minimg(v.z[ia] - v.z[ib], v.lz, v.lzi);
+                const double rabsq = A.clen2[ic * 3 + s];
+                const double diffsq = rabsq - (pxab * pxab + pyab * pyab + pzab * pzab);
+                if (fabs(diffsq) > rabsq * A.tol2) {
+                    const int ka = ia - A.nliqa, kb = ib - A.nliqa;
+                    const double rx = minimg(A.xo[ka] - A.xo[kb], v.lx, v.lxi);
+                    const double ry = minimg(A.yo[ka] - A.yo[kb], v.ly, v.lyi);
+                    const double rz = minimg(A.zo[ka] - A.zo[kb], v.lz, v.lzi);
+                    const double rpab = rx * pxab + ry * pyab + rz * pzab;
+                    if (rpab < rabsq * A.rptol) {
+                        v.status[ST_SHAKE_RPTOL] = 1 + ic * 8 + s;
+                        A.sweeps_out[0] = ite + 1;
+                        A.sweeps_out[1] = 0;
+                        return;
+                    }
+                    double rma = v.mii[ia], rmb = v.mii[ib];
+                    const double aux = diffsq / (2.0 * (rma + rmb) * rpab);
+                    rma *= aux;
+                    rmb *= aux;
+                    v.x[ia] += rx * rma; v.y[ia] += ry * rma; v.z[ia] += rz * rma;
+                    v.x[ib] -= rx * rmb; v.y[ib] -= ry * rmb; v.z[ib] -= rz * rmb;
+                    if (ia < A.nmove) moving[ia - A.nliqa] = 0;
+                    if (ib < A.nmove) moving[ib - A.nliqa] = 0;
+                    done = false;
+                    any = true;
+                }
+            }
+        }
+        if (A.clean) done = !any;
+        ++ite;
+        for (int i = 0; i < nsurf; ++i) {
+            movd[i] = moving[i];
+            moving[i] = 1;
+        }
+    }
+    A.sweeps_out[0] = ite;
+    A.sweeps_out[1] = done ? 1 : 0;
+}
+
+}  // namespace
+
+int shake_setup(Ctx& c, const mdg_sysdesc* s) {
+    const View& v = c.v;
+    c.ncons = (int)s->ncons;
+    const int nsurfold = v.ntota - v.nliqa;
+    c.d_xold = (double*)dalloc(c, sizeof(double) * std::max(nsurfold, 1));
+    c.d_yold = (double*)dalloc(c, sizeof(double) * std::max(nsurfold, 1));
+    c.d_zold = (double*)dalloc(c, sizeof(double) * std::max(nsurfold, 1));
+    c.d_kps = (double*)dalloc(c, sizeof(double) * std::max(v.nit, 1));
+    c.d_ft_in = (double*)dalloc(c, sizeof(double) * 3 * std::max(v.nmove - v.nriga, 1));
+    c.d_sweeps = (int*)dalloc(c, sizeof(int) * 2);
+    c.d_seq_flags = (int*)dalloc(c, sizeof(int) * 2 * std::max(v.nmove - v.nliqa, 1));
+    if (c.ncons == 0) return MDG_OK;
+    std::vector<int> cons(6 * c.ncons, -1), cn(c.ncons, 0);
+    std::vector<double> l2(3 * c.ncons, 0.0);
+    std::vector<int> owner(v.nmove, -1);
+    c.shake_seq = 0;
+    for (int ic = 0; ic < c.ncons; ++ic) {
+        const int64_t it = s->ictype[ic] - 1;
+        if (it < 0 || it >= s->ntype) return set_err(&c, MDG_E_ARG, "ictype out of range");
+        const int nc = (int)s->nconst[it];
+        if (nc > MDG_SMX) return set_err(&c, MDG_E_ARG, "more than 3 constraints per molecule");
+        cn[ic] = nc;
+        for (int k = 0; k < nc; ++k) {
+            const int64_t a = s->constra[k + MDG_SMX * ic] - 1, b = s->constrb[k + MDG_SMX * ic] - 1;
+            if (a < v.nliqa || b < v.nliqa || a >= v.ntota || b >= v.ntota)
+                return set_err(&c, MDG_E_ARG, "constraint atom outside the surface/wall range");
+            cons[ic * 6 + 2 * k] = (int)a;
+            cons[ic * 6 + 2 * k + 1] = (int)b;
+            const double L = s->length[it + s->ntype * k];
+            l2[ic * 3 + k] = L * L;
+            for (int64_t at : {a, b})
+                if (at < v.nmove) {
+                    if (owner[at] >= 0 && owner[at] != ic) c.shake_seq = 1;
+                    owner[at] = ic;
+                }
+        }
+    }
+    c.d_cons = (int*)dalloc(c, sizeof(int) * cons.size());
+    c.d_clen2 = (double*)dalloc(c, sizeof(double) * l2.size());
+    c.d_cons_n = (int*)dalloc(c, sizeof(int) * cn.size());
+    MDG_CUDA(cudaMemcpy(c.d_cons, cons.data(), sizeof(int) * cons.size(), cudaMemcpyHostToDevice));
+    MDG_CUDA(cudaMemcpy(c.d_clen2, l2.data(), sizeof(double) * l2.size(), cudaMemcpyHostToDevice));
+    MDG_CUDA(cudaMemcpy(c.d_cons_n, cn.data(), sizeof(int) * cn.size(), cudaMemcpyHostToDevice));
+    return MDG_OK;
+}
+
+// Verlet + SHAKE on the device state (x/y/z, xold, forces in c.d_ft_in).
+void shake_launch(Ctx& c) {
+    const View& v = c.v;
+    const int nsurf = v.nmove - v.nliqa;
+    cudaMemsetAsync(c.d_kps, 0, sizeof(double) * v.nit, c.stream);
+    if (nsurf > 0)
+        k_verlet<<<(nsurf + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, c.d_ft_in, c.d_xold, c.d_yold, c.d_zold, c.d_kps);
+    if (c.ncons == 0) return;
+    const int clean = (c.quirks & MDG_QUIRK_CLEAN_SHAKE_DONE) ? 1 : 0;
+    ShakeArgs A{c.ncons, c.maxit, clean, v.nliqa, v.nmove, c.tol2, c.rptol, c.d_cons, c.d_clen2,
+                c.d_cons_n, c.d_xold, c.d_yold, c.d_zold, c.d_sweeps};
+    if (c.shake_seq) {
+        k_shake_seq<<<1, 1, 0, c.stream>>>(v, A, c.d_seq_flags, c.d_seq_flags + std::max(nsurf, 1));
+        return;
+    }
+    if (clean) {
+        k_shake_init<<<1, 1, 0, c.stream>>>(A);
+    } else {
+        k_shake_last<<<1, 1, 0, c.stream>>>(v, A);
+    }
+    k_shake_mol<<<(c.ncons + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, A);
+}
+
+}  // namespace mdg

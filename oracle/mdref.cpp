@@ -1,0 +1,1029 @@
+// mdref.cpp - CPU restatement of md_sim's force / neighbour-list / SHAKE / Gear path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle the CUDA library is checked against and
+// the CPU baseline that bench.py times.  It is never linked into, loaded by or called from the
+// product library (md_sim_gb300/csrc).
+//
+// Parity status: the reference (Fortran 90 + MPI) cannot be compiled in this environment (no
+// Fortran compiler) and ships no tests, golden vectors or known answers for this path, so this
+// restatement is "parity unpinned" against the reference's own outputs.  It is validated by
+// independent checks instead (finite-difference forces, Ewald vs direct lattice sums, Newton's
+// third law, invariances; see tests/test_oracle_physics.py).
+//
+// Each routine follows the reference loop by loop, in the same order, so that sums match to
+// rounding.  References are to files under src/ of the reference tree:
+//   global.f90:18-24           constants (single-precision literals promoted to real*8)
+//   forcem.f90:11-13           Abramowitz-Stegun 7.1.26 erfc coefficients
+//   forcem.f90:54-81           force_init
+//   forcem.f90:157-231         force_real_init (wall long-range tail tables)
+//   forcem.f90:233-552         force_real
+//   forcem.f90:565-652         force_intra
+//   forcem.f90:657-825         force_fouri_init
+//   forcem.f90:827-937         force_fouri
+//   forcem_3d.f90:1031-1058    serial force_sum
+//   forcem_back.f90:297,410,489-522,561,568,903-907   bulk variant
+//   nnlist.f90:14-208          nnlist_init / nnlist_make / nnlist_constr
+//   move.f90:48-529            move_predict / move_correct / move_shake(_init)
+//
+// Built with -ffp-contract=off so that no multiply-add is fused (the reference targets x86-64
+// without FMA); with -fopenmp the pair, k-vector and atom loops are split over threads the way
+// the reference splits them over MPI ranks, each thread summing into private buffers that are
+// reduced at the end (the mpi_allreduce of force_sum).
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_set>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/mdgpu.h"
+
+namespace {
+
+typedef std::complex<double> cplx;
+
+inline double F(float x) { return (double)x; }  // single-precision literal in real*8 context
+
+const double M_PI_R = F(3.1415926535898f);
+const double PH_e = F(1.6021892e-19f);
+const double PH_Na = F(6.022045e23f);
+const double PH_R = F(8.31441f);
+const double PH_eps0 = F(8.85418782e-12f);
+const double PH_4epi = F(8.987551784952e+9f);
+const double PH_A2m = F(1.0e-10f);
+const double A1 = F(0.254829592f), A2 = F(-0.284496736f), A3 = F(1.421413741f);
+const double A4 = F(-1.453152027f), A5 = F(1.061405429f), PP = F(0.3275911f);
+
+inline double anint(double x) { return std::round(x); }  // Fortran ANINT: half away from zero
+inline double fsign(double z) { return std::signbit(z) ? -1.0 : 1.0; }
+inline double pw3(double x) { return x * x * x; }
+
+struct Ref {
+    // sizes
+    int64_t ntype, nrig, nriga, nliqa, nsurf, nmove, nwall, ntota, ngogo, nit, nijt, nltype;
+    int64_t ncons, nang;
+    std::vector<int64_t> moltypen, nt, ns, nst, nconst, nangt, nsi, ijtype, vdwnum, itype;
+    std::vector<int64_t> ictype, constra, constrb, iatype, ang1, ang2, ang3;
+    std::vector<int64_t> nss_wall;
+    std::vector<double> eps, sig, aa, rhoi, cc, qs, mi, mii, length, kt, theta;
+    double lx, ly, lz, lxi, lyi, lzi, cx, cy, cz, lw, lwh, dt;
+    // params
+    double rcut, rcutsq, skin, alfa, spii, facq, dshsq;
+    int variant, pbcz;
+    uint32_t quirks;
+    int maxit;
+    double tol2, rptol;
+    // wall positions (frozen), full position copies for create-time work
+    std::vector<double> wx, wy, wz;
+    // neighbour lists
+    double rskinsq;
+    std::vector<int64_t> list1, list2, listw1, listw2;  // 0-based
+    std::vector<double> ocx0, ocy0, ocz0, ox0, oy0, oz0;
+    std::vector<std::vector<int64_t>> excl;  // constrained partners of surface atoms
+    // reciprocal
+    int64_t kmax, klmax, kmmax, knmax;
+    double pipix, pipiy, pipiz;
+    std::vector<int> kl_, km_, kn_;  // valid k in reference order
+    std::vector<double> Ak;
+    std::vector<cplx> Qsumw;  // Qsumw1 + Qsumw2
+    std::vector<cplx> Qsumw1, Qsumw2;
+    double ewqWW, uself;
+    // long-range tail
+    std::vector<double> flr_l, flr_w, flr_lja, flr_ljc, flr_bua, flr_buc, flr_bur, ulr_l, ulr_w;
+    // SHAKE
+    int64_t nfreed;
+    std::string err;
+
+    int ij(int64_t it, int64_t jt) const { return (int)ijtype[(it - 1) + nit * (jt - 1)] - 1; }
+    double mx(double d) const { return d - lx * anint(d * lxi); }
+    double my(double d) const { return d - ly * anint(d * lyi); }
+    double mz_real(double d) const { return variant == MDG_BULK ? d - lz * anint(d * lzi) : d; }
+    double mz_list(double d) const { return pbcz ? d - lz * anint(d * lzi) : d; }
+    bool constrained(int64_t i, int64_t j) const {  // nnlist_constr (0-based atoms)
+        if (i < 0 || i >= (int64_t)excl.size()) return false;
+        for (int64_t p : excl[i])
+            if (p == j) return true;
+        return false;
+    }
+};
+
+std::string g_err;
+
+int fail(Ref* r, int code, const std::string& msg) {
+    if (r) r->err = msg;
+    g_err = msg;
+    return code;
+}
+
+// ------------------------------------------------------------------------------------------
+// nnlist_init (src/nnlist.f90:14-90) and nnlist_make (:92-165).  The candidate arrays
+// list3/list4 and listw3/listw4 are enumerated on the fly in the same i-major, j-ascending
+// order instead of being stored (they would need O(heads^2) memory).
+// ------------------------------------------------------------------------------------------
+void nnlist_make(Ref* r, const double* x0, const double* y0, const double* z0, const double* cx0,
+                 const double* cy0, const double* cz0) {
+    for (int64_t i = 0; i < r->nrig; ++i) {
+        r->ocx0[i] = cx0[i];
+        r->ocy0[i] = cy0[i];
+        r->ocz0[i] = cz0[i];
+    }
+    for (int64_t i = r->nriga; i < r->nmove; ++i) {
+        r->ox0[i - r->nriga] = x0[i];
+        r->oy0[i - r->nriga] = y0[i];
+        r->oz0[i - r->nriga] = z0[i];
+    }
+    r->list1.clear();
+    r->list2.clear();
+    const int64_t nmove = r->nmove, nliqa = r->nliqa;
+    for (int64_t i = 0; i < nmove - 1; ++i) {
+        if (r->nsi[r->itype[i] - 1] == 0) continue;
+        for (int64_t j = i + 1; j < nmove; ++j) {
+            if (r->nsi[r->itype[j] - 1] == 0) continue;
+            if (i >= nliqa && j >= nliqa && r->constrained(i, j)) continue;
+            double xijs = r->mx(x0[i] - x0[j]);
+            double yijs = r->my(y0[i] - y0[j]);
+            double zijs = r->mz_list(z0[i] - z0[j]);
+            if (xijs * xijs + yijs * yijs + zijs * zijs < r->rskinsq) {
+                r->list1.push_back(i);
+                r->list2.push_back(j);
+            }
+        }
+    }
+    r->listw1.clear();
+    r->listw2.clear();
+    for (int64_t i = 0; i < nmove; ++i) {
+        if (r->nsi[r->itype[i] - 1] == 0) continue;
+        for (int64_t j = nmove; j < r->ntota; ++j) {
+            if (i >= nliqa && r->constrained(i, j)) continue;
+            const int64_t w = j - nmove;
+            double xijs = r->mx(x0[i] - r->wx[w]);
+            double yijs = r->my(y0[i] - r->wy[w]);
+            double zijs = r->mz_list(z0[i] - r->wz[w]);
+            if (xijs * xijs + yijs * yijs + zijs * zijs < r->rskinsq) {
+                r->listw1.push_back(i);
+                r->listw2.push_back(j);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// force_real_init long-range tables (src/forcem.f90:167-228)
+// ------------------------------------------------------------------------------------------
+void lr_init(Ref* r) {
+    const int64_t nit = r->nit;
+    const int64_t nstw = r->nst[r->ntype - 1];
+    r->flr_l.assign(nit, 0.0);
+    r->flr_w.assign(nit, 0.0);
+    r->flr_lja.assign(nit, 0.0);
+    r->flr_ljc.assign(nit, 0.0);
+    r->flr_bua.assign(nit, 0.0);
+    r->flr_buc.assign(nit, 0.0);
+    r->flr_bur.assign(nit, 1.0);
+    r->ulr_l.assign(nit, 0.0);
+    r->ulr_w.assign(nit, 0.0);
+    if (r->variant != MDG_SLAB) return;
+    const double rholiq = (double)r->nmove / (r->lx * r->ly * r->lw);
+    int64_t nsswsum = 0;
+    for (int64_t s = 0; s < nstw; ++s) nsswsum += r->nss_wall[s];
+    const double rhowall = (double)nsswsum / (2.0 * r->cx * r->cy * r->cz);
+    std::vector<double> xdens(nit, 0.0);
+    for (int64_t i = 0; i < r->nmove; ++i) xdens[r->itype[i] - 1] += 1.0;
+    for (int64_t t = 0; t < nit - nstw; ++t) xdens[t] = xdens[t] / (double)(float)r->nmove * rholiq;
+    // real(nss)/real(sum(nss)) is a default-real (single precision) quotient
+    const float nss12 = (float)(r->nss_wall[0] + r->nss_wall[1]);
+    if (nit >= 2) {
+        xdens[nit - 2] = (double)((float)r->nss_wall[0] / nss12) * rhowall;
+        xdens[nit - 1] = (double)((float)r->nss_wall[1] / nss12) * rhowall;
+    }
+    const double rc = r->rcut;
+    for (int64_t it = 1; it <= nit - nstw; ++it) {
+        for (int64_t jt = 1; jt <= nit; ++jt) {
+            const int k = r->ij(it, jt);
+            double sgn = (jt <= nit - nstw) ? -1.0 : 1.0;
+            double flr = 0.0, ul = 0.0;
+            const double e = r->eps[k], s = r->sig[k];
+            switch (r->vdwnum[k]) {
+                case 0: break;
+                case 1: {
+                    double rc10 = std::pow(rc, 10), rc4 = std::pow(rc, 4), rc9 = std::pow(rc, 9),
+                           rc3 = rc * rc * rc;
+                    flr = e * s * (s / (10.0 * rc10) - 1.0 / (4.0 * rc4));
+                    ul = e * s * (s / (90.0 * rc9) - 1.0 / (12.0 * rc3));
+                    r->flr_lja[it - 1] += sgn * xdens[jt - 1] * e * (s * s) / 10.0;
+                    r->flr_ljc[it - 1] += sgn * xdens[jt - 1] * e * s / 4.0;
+                } break;
+                case 2: {
+                    double ro = 1.0 / r->rhoi[k];
+                    double rc4 = std::pow(rc, 4), rc3 = rc * rc * rc;
+                    flr = ro * (ro + rc) * r->aa[k] * std::exp(-rc / ro) - r->cc[k] / (4.0 * rc4);
+                    ul = ro * ro * (2.0 * ro + rc) * r->aa[k] * std::exp(-rc / ro) -
+                         r->cc[k] / (12.0 * rc3);
+                    r->flr_bua[it - 1] += sgn * xdens[jt - 1] * r->aa[k] * ro;
+                    r->flr_buc[it - 1] += sgn * xdens[jt - 1] * r->cc[k] / 4.0;
+                    r->flr_bur[it - 1] = ro;
+                } break;
+                default: break;
+            }
+            if (sgn < 0.0) {
+                r->flr_l[it - 1] += flr * xdens[jt - 1];
+                r->ulr_l[it - 1] += ul * xdens[jt - 1];
+            } else {
+                r->flr_w[it - 1] += flr * xdens[jt - 1];
+                r->ulr_w[it - 1] += ul * xdens[jt - 1];
+            }
+        }
+    }
+    const double tp = 2.0 * M_PI_R;
+    for (int64_t t = 0; t < nit; ++t) {
+        r->flr_lja[t] *= tp;
+        r->flr_ljc[t] *= tp;
+        r->flr_bua[t] *= tp;
+        r->flr_buc[t] *= tp;
+        r->flr_l[t] *= tp;
+        r->flr_w[t] *= tp;
+        r->ulr_l[t] *= tp;
+        r->ulr_w[t] *= tp;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// force_fouri_init (src/forcem.f90:657-825)
+// ------------------------------------------------------------------------------------------
+void fouri_init(Ref* r, const double* x0, const double* y0, const double* z0) {
+    r->pipix = 2.0 * M_PI_R / r->lx;
+    r->pipiy = 2.0 * M_PI_R / r->ly;
+    r->pipiz = 2.0 * M_PI_R / r->lz;
+    const double alf4i = -1.0 / (4.0 * r->alfa * r->alfa);
+    const double fac = 2.0 * PH_e * PH_e * PH_Na / (PH_eps0 * PH_A2m * 1000.0 * r->lx * r->ly * r->lz);
+    const double lmin = std::min(r->lx, std::min(r->ly, r->lz));
+    const double rk = (double)(float)r->kmax;
+    r->klmax = (int64_t)std::lround(rk * r->lx / lmin);
+    r->kmmax = (int64_t)std::lround(rk * r->ly / lmin);
+    r->knmax = (int64_t)std::lround(rk * r->lz / lmin);
+    const int64_t nw = r->nwall, KL = r->klmax, KM = r->kmmax, KN = r->knmax;
+    // wall phase factors by recurrence
+    std::vector<cplx> el((size_t)nw * (KL + 1)), em((size_t)nw * (2 * KM + 1)), en((size_t)nw * (2 * KN + 1));
+    auto EL = [&](int64_t i, int64_t l) -> cplx& { return el[i * (KL + 1) + l]; };
+    auto EM = [&](int64_t i, int64_t m) -> cplx& { return em[i * (2 * KM + 1) + m + KM]; };
+    auto EN = [&](int64_t i, int64_t n) -> cplx& { return en[i * (2 * KN + 1) + n + KN]; };
+    for (int64_t i = 0; i < nw; ++i) {
+        EL(i, 0) = EM(i, 0) = EN(i, 0) = cplx(1.0, 0.0);
+        double tx = r->pipix * r->wx[i], ty = r->pipiy * r->wy[i], tz = r->pipiz * r->wz[i];
+        EL(i, 1) = cplx(std::cos(tx), std::sin(tx));
+        EM(i, 1) = cplx(std::cos(ty), std::sin(ty));
+        EN(i, 1) = cplx(std::cos(tz), std::sin(tz));
+        for (int64_t l = 2; l <= KL; ++l) EL(i, l) = EL(i, l - 1) * EL(i, 1);
+        for (int64_t m = 2; m <= KM; ++m) EM(i, m) = EM(i, m - 1) * EM(i, 1);
+        for (int64_t m = 1; m <= KM; ++m) EM(i, -m) = std::conj(EM(i, m));
+        for (int64_t n = 2; n <= KN; ++n) EN(i, n) = EN(i, n - 1) * EN(i, 1);
+        for (int64_t n = 1; n <= KN; ++n) EN(i, -n) = std::conj(EN(i, n));
+    }
+    // ranges of the two static walls (src/forcem.f90:690-701, ngogo = nmove)
+    const int64_t h1a = 0, h1b = nw / 2, h2a = nw / 2, h2b = nw;
+    r->kl_.clear();
+    r->km_.clear();
+    r->kn_.clear();
+    r->Ak.clear();
+    r->Qsumw.clear();
+    r->Qsumw1.clear();
+    r->Qsumw2.clear();
+    r->ewqWW = 0.0;
+    std::vector<cplx> elm(nw);
+    int64_t kmmin = 0, knmin = 1;
+    const float kmaxsq_lim = (float)(r->kmax * r->kmax) + 2.01f;
+    for (int64_t kl = 0; kl <= KL; ++kl) {
+        double rl = r->pipix * (double)(float)kl;
+        for (int64_t km = kmmin; km <= KM; ++km) {
+            double rm = r->pipiy * (double)(float)km;
+            for (int64_t i = 0; i < nw; ++i) elm[i] = r->qs[r->nmove + i] * EL(i, kl) * EM(i, km);
+            for (int64_t kn = knmin; kn <= KN; ++kn) {
+                double rn = r->pipiz * (double)(float)kn;
+                volatile float a = (float)(kl * kl + km * km);
+                volatile float b = (float)(kn * kn * r->kmax * r->kmax) / (float)(KN * KN);
+                volatile float ksq = a + b;
+                if (ksq < kmaxsq_lim) {
+                    double rksq = rl * rl + rm * rm + rn * rn;
+                    r->kl_.push_back((int)kl);
+                    r->km_.push_back((int)km);
+                    r->kn_.push_back((int)kn);
+                    r->Ak.push_back(fac * std::exp(rksq * alf4i) / rksq);
+                    cplx q1(0.0, 0.0), q2(0.0, 0.0);
+                    for (int64_t i = h1a; i < h1b; ++i) q1 += elm[i] * EN(i, kn);
+                    for (int64_t i = h2a; i < h2b; ++i) q2 += elm[i] * EN(i, kn);
+                    r->Qsumw1.push_back(q1);
+                    r->Qsumw2.push_back(q2);
+                    cplx qws = q1 + q2;
+                    r->Qsumw.push_back(qws);
+                    r->ewqWW += (r->Ak.back() * qws * std::conj(qws)).real();
+                }
+            }
+            knmin = -KN;
+        }
+        kmmin = -KM;
+    }
+    r->ewqWW *= 0.5;
+
+    // self energy (src/forcem.f90:793-822)
+    double sq = 0.0;
+    for (int64_t i = 0; i < r->ntota; ++i) sq += r->qs[i] * r->qs[i];
+    r->uself = -0.5 * r->spii * r->facq * r->alfa * sq;
+    int64_t ix = 0;
+    int64_t ntprev = 0;
+    for (int64_t it = 0; it < r->ntype; ++it) {
+        if (r->moltypen[it] == 0) {
+            const int64_t i0 = ntprev;  // nt(it-1) used as an atom offset, as the reference does
+            for (int64_t is = i0; is < i0 + r->ns[it]; ++is)
+                for (int64_t js = is + 1; js < i0 + r->ns[it]; ++js) {
+                    double dx = x0[is] - x0[js], dy = y0[is] - y0[js], dz = z0[is] - z0[js];
+                    double rij = std::sqrt(dx * dx + dy * dy + dz * dz);
+                    double t = 1.0 / (1.0 + PP * r->alfa * rij);
+                    double ar = r->alfa * rij;
+                    double erfv = 1.0 - ((((A5 * t + A4) * t + A3) * t + A2) * t + A1) * t * std::exp(-(ar * ar));
+                    r->uself -= (double)r->nt[it] * r->facq * r->qs[is] * r->qs[js] * erfv / rij;
+                }
+        } else if (r->moltypen[it] == 2) {
+            for (int64_t iq = 0; iq < r->nt[it]; ++iq) {
+                ++ix;
+                for (int64_t is = 1; is <= r->nconst[it]; ++is) {
+                    // constra(ix, is): the reference indexes the (SMX, ncons) table transposed
+                    int64_t flat = (ix - 1) + MDG_SMX * (is - 1);
+                    int64_t i = flat < (int64_t)r->constra.size() ? r->constra[flat] : 0;
+                    int64_t j = flat < (int64_t)r->constrb.size() ? r->constrb[flat] : 0;
+                    if (i <= 0 || j <= 0) continue;  // unset table entry: the reference reads qs(0)
+                    double rij = r->length[it + r->ntype * (is - 1)];
+                    double t = 1.0 / (1.0 + PP * r->alfa * rij);
+                    double ar = r->alfa * rij;
+                    double erfv = 1.0 - ((((A5 * t + A4) * t + A3) * t + A2) * t + A1) * t * std::exp(-(ar * ar));
+                    r->uself -= r->facq * r->qs[i - 1] * r->qs[j - 1] * erfv / rij;
+                }
+            }
+        }
+        ntprev = r->nt[it];
+    }
+}
+
+}  // namespace
+
+struct RefCtx : Ref {};
+
+extern "C" {
+
+const char* ref_last_error(const RefCtx* c) { return c ? c->err.c_str() : g_err.c_str(); }
+
+void ref_destroy(RefCtx* c) { delete c; }
+
+int ref_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, const double* y0,
+               const double* z0, const double* cx0, const double* cy0, const double* cz0,
+               RefCtx** out) {
+    if (!s || !p || !out) return fail(nullptr, MDG_E_ARG, "null argument");
+    if (s->ngogo != s->nmove) return fail(nullptr, MDG_E_UNSUPPORTED, "ngogo /= nmove (pulled walls)");
+    RefCtx* r = new RefCtx();
+    r->ntype = s->ntype; r->nrig = s->nrig; r->nriga = s->nriga; r->nliqa = s->nliqa;
+    r->nsurf = s->nsurf; r->nmove = s->nmove; r->nwall = s->nwall; r->ntota = s->ntota;
+    r->ngogo = s->ngogo; r->nit = s->nit; r->nijt = s->nijt; r->nltype = s->nltype;
+    r->ncons = s->ncons; r->nang = s->nang;
+    auto cp = [](const int64_t* a, int64_t n) { return std::vector<int64_t>(a, a + n); };
+    auto cpd = [](const double* a, int64_t n) { return std::vector<double>(a, a + n); };
+    r->moltypen = cp(s->moltypen, s->ntype); r->nt = cp(s->nt, s->ntype); r->ns = cp(s->ns, s->ntype);
+    r->nst = cp(s->nst, s->ntype); r->nconst = cp(s->nconst, s->ntype); r->nangt = cp(s->nangt, s->ntype);
+    r->nss_wall = cp(s->nss_wall, std::max<int64_t>(2, s->nst[s->ntype - 1]));
+    r->nsi = cp(s->nsi, s->nit); r->ijtype = cp(s->ijtype, s->nit * s->nit);
+    r->vdwnum = cp(s->vdwnum, s->nijt);
+    r->eps = cpd(s->eps, s->nijt); r->sig = cpd(s->sig, s->nijt); r->aa = cpd(s->aa, s->nijt);
+    r->rhoi = cpd(s->rhoi, s->nijt); r->cc = cpd(s->cc, s->nijt);
+    r->itype = cp(s->itype, s->ntota); r->qs = cpd(s->qs, s->ntota); r->mi = cpd(s->mi, s->ntota);
+    r->mii = cpd(s->mii, s->ntota);
+    if (s->ncons > 0) {
+        r->ictype = cp(s->ictype, s->ncons);
+        r->constra = cp(s->constra, MDG_SMX * s->ncons);
+        r->constrb = cp(s->constrb, MDG_SMX * s->ncons);
+    }
+    if (s->nang > 0) {
+        r->iatype = cp(s->iatype, s->nang);
+        r->ang1 = cp(s->ang1, MDG_SMX * s->nang);
+        r->ang2 = cp(s->ang2, MDG_SMX * s->nang);
+        r->ang3 = cp(s->ang3, MDG_SMX * s->nang);
+    }
+    r->length = cpd(s->length, s->ntype * MDG_SMX);
+    r->kt = cpd(s->kt, s->ntype * MDG_SMX);
+    r->theta = cpd(s->theta, s->ntype * MDG_SMX);
+    r->lx = s->lx; r->ly = s->ly; r->lz = s->lz;
+    r->lxi = 1.0 / s->lx; r->lyi = 1.0 / s->ly; r->lzi = 1.0 / s->lz;
+    r->cx = s->cx; r->cy = s->cy; r->cz = s->cz; r->lw = s->lw; r->lwh = 0.5 * s->lw; r->dt = s->dt;
+    for (int64_t k = 0; k < r->nijt; ++k)
+        if (r->vdwnum[k] < 0 || r->vdwnum[k] > 2) {
+            delete r;
+            return fail(nullptr, MDG_E_ARG, "force_real(): unknown interaction type");
+        }
+
+    // force_init (src/forcem.f90:58-60)
+    r->rcut = p->rcut;
+    r->rcutsq = p->rcut * p->rcut;
+    r->skin = p->skin;
+    r->spii = 2.0 / std::sqrt(M_PI_R);
+    r->alfa = p->alpha > 0.0 ? p->alpha : F(3.09f) / p->rcut;
+    r->facq = PH_4epi * PH_e * PH_e * PH_Na / (1000.0 * PH_A2m);
+    r->dshsq = p->dshsq;
+    r->variant = p->variant;
+    r->pbcz = p->pbc_z_list;
+    r->quirks = p->quirks;
+    r->kmax = p->kmax;
+    r->maxit = p->shake_maxit > 0 ? p->shake_maxit : 10;
+    r->tol2 = p->shake_tol2 > 0.0 ? p->shake_tol2 : F(1.e-8f);
+    r->rptol = p->shake_rptol > 0.0 ? p->shake_rptol : F(0.85f);
+
+    r->wx.assign(x0 + r->nmove, x0 + r->ntota);
+    r->wy.assign(y0 + r->nmove, y0 + r->ntota);
+    r->wz.assign(z0 + r->nmove, z0 + r->ntota);
+
+    // exclusion table for nnlist_constr (O(1) per test instead of a scan of all constraints)
+    r->excl.assign(r->ntota, {});
+    for (int64_t ic = 0; ic < r->ncons; ++ic) {
+        const int64_t it = r->ictype[ic] - 1;
+        for (int64_t is = 0; is < r->nconst[it]; ++is) {
+            int64_t a = r->constra[is + MDG_SMX * ic] - 1, b = r->constrb[is + MDG_SMX * ic] - 1;
+            if (a < 0 || b < 0 || a >= r->ntota || b >= r->ntota) {
+                std::string m = "constraint atom out of range";
+                delete r;
+                return fail(nullptr, MDG_E_ARG, m);
+            }
+            r->excl[a].push_back(b);
+            r->excl[b].push_back(a);
+        }
+    }
+
+    fouri_init(r, x0, y0, z0);
+    // nnlist_init (src/nnlist.f90:18-28)
+    r->ocx0.assign(r->nrig, 0.0); r->ocy0.assign(r->nrig, 0.0); r->ocz0.assign(r->nrig, 0.0);
+    r->ox0.assign(r->nmove - r->nriga, 0.0); r->oy0.assign(r->nmove - r->nriga, 0.0);
+    r->oz0.assign(r->nmove - r->nriga, 0.0);
+    double rs = r->rcut + r->skin;
+    if (r->nrig > 0) {
+        double dx = x0[0] - cx0[0], dy = y0[0] - cy0[0], dz = z0[0] - cz0[0];
+        rs = rs + 2.0 * std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    r->rskinsq = rs * rs;
+    lr_init(r);
+    nnlist_make(r, x0, y0, z0, cx0, cy0, cz0);
+    // move_shake_init (src/move.f90:402)
+    r->nfreed = 3 * (r->nmove - r->nliqa);
+    for (int64_t it = r->nltype; it < r->ntype; ++it)
+        if (r->moltypen[it] == 2) r->nfreed -= r->nt[it] * r->nconst[it];
+    *out = r;
+    return MDG_OK;
+}
+
+int ref_nnlist_make(RefCtx* r, const double* x0, const double* y0, const double* z0, const double* cx0,
+                    const double* cy0, const double* cz0, int64_t* ipack, int64_t* wpack) {
+    nnlist_make(r, x0, y0, z0, cx0, cy0, cz0);
+    if (ipack) *ipack = (int64_t)r->list1.size();
+    if (wpack) *wpack = (int64_t)r->listw1.size();
+    return MDG_OK;
+}
+
+int ref_get_lists(RefCtx* r, int64_t* li, int64_t* lj, int64_t cap, int64_t* wi, int64_t* wj,
+                  int64_t wcap, int64_t* ipack, int64_t* wpack) {
+    int64_t n = (int64_t)r->list1.size(), nw = (int64_t)r->listw1.size();
+    for (int64_t k = 0; k < n && k < cap && li; ++k) {
+        li[k] = r->list1[k] + 1;
+        lj[k] = r->list2[k] + 1;
+    }
+    for (int64_t k = 0; k < nw && k < wcap && wi; ++k) {
+        wi[k] = r->listw1[k] + 1;
+        wj[k] = r->listw2[k] + 1;
+    }
+    if (ipack) *ipack = n;
+    if (wpack) *wpack = nw;
+    return MDG_OK;
+}
+
+// k-vector table, for tests: kl/km/kn per valid k in reference order and Ak.
+int64_t ref_kvectors(RefCtx* r, int32_t* kl, int32_t* km, int32_t* kn, double* ak, int64_t cap) {
+    int64_t n = (int64_t)r->Ak.size();
+    for (int64_t k = 0; k < n && k < cap; ++k) {
+        if (kl) kl[k] = r->kl_[k];
+        if (km) km[k] = r->km_[k];
+        if (kn) kn[k] = r->kn_[k];
+        if (ak) ak[k] = r->Ak[k];
+    }
+    return n;
+}
+
+double ref_uself(RefCtx* r) { return r->uself; }
+
+int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z0, const double* cx0,
+                  const double* cy0, const double* cz0, double* rsx, double* rsy, double* rsz,
+                  double* ftx, double* fty, double* ftz, double* fcx, double* fcy, double* fcz,
+                  double* tx, double* ty, double* tz, double* fxo, double* fyo, double* fzo,
+                  mdg_energies* e) {
+    const int64_t nmove = r->nmove, nrig = r->nrig, nriga = r->nriga, nijt = r->nijt;
+    std::vector<double> fx(nmove, 0.0), fy(nmove, 0.0), fz(nmove, 0.0);
+    std::vector<double> elj(nijt, 0.0), eqq(nijt, 0.0);
+    double fwsx[3] = {0, 0, 0}, fwsy[3] = {0, 0, 0}, fwsz[3] = {0, 0, 0};  // index sgn+1
+    double uewa = 0.0, urf = 0.0, ulr = 0.0, uavex = 0.0;
+
+    // ---- force_real: rebuild trigger (src/forcem.f90:245-250)
+    {
+        double aux = r->dshsq;
+        double m1 = -HUGE_VAL, m2 = -HUGE_VAL;
+        for (int64_t i = 0; i < nrig; ++i) {
+            double a = r->ocx0[i] - cx0[i], b = r->ocy0[i] - cy0[i], c = r->ocz0[i] - cz0[i];
+            m1 = std::max(m1, a * a + b * b + c * c);
+        }
+        for (int64_t i = nriga; i < nmove; ++i) {
+            double a = r->ox0[i - nriga] - x0[i], b = r->oy0[i - nriga] - y0[i], c = r->oz0[i - nriga] - z0[i];
+            m2 = std::max(m2, a * a + b * b + c * c);
+        }
+        aux = std::max(std::max(m1, m2), aux);
+        if (4.0 * aux > r->skin * r->skin) nnlist_make(r, x0, y0, z0, cx0, cy0, cz0);
+    }
+    const double alfa = r->alfa, facq = r->facq, spii = r->spii, rcutsq = r->rcutsq;
+    const int64_t npair = (int64_t)r->list1.size();
+    const int64_t nwpair = (int64_t)r->listw1.size();
+
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+        std::vector<double> tfx(nmove, 0.0), tfy(nmove, 0.0), tfz(nmove, 0.0), telj(nijt, 0.0),
+            teqq(nijt, 0.0);
+        double tuav = 0.0;
+        // ---- moving-moving pairs (src/forcem.f90:288-403)
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (int64_t k = 0; k < npair; ++k) {
+            const int64_t i = r->list1[k], j = r->list2[k];
+            double xio = r->mx(x0[i] - x0[j]);
+            double yio = r->my(y0[i] - y0[j]);
+            double zio = r->mz_real(z0[i] - z0[j]);
+            double rsq = xio * xio + yio * yio + zio * zio;
+            if (rsq > rcutsq) continue;
+            const int64_t it = r->itype[i], jt = r->itype[j];
+            const int ijt = r->ij(it, jt);
+            double rsqi = 1.0 / rsq;
+            double rij = std::sqrt(rsq);
+            double fij = 0.0, r6, aux;
+            switch (r->vdwnum[ijt]) {
+                case 1:
+                    r6 = r->sig[ijt] * pw3(rsqi);
+                    telj[ijt] += r->eps[ijt] * r6 * (r6 - 1.0);
+                    tuav += r->eps[ijt] * r6 * (r6 - 1.0);
+                    fij = 6.0 * rsqi * r->eps[ijt] * r6 * (2.0 * r6 - 1.0);
+                    break;
+                case 2:
+                    r6 = r->cc[ijt] * pw3(rsqi);
+                    aux = r->aa[ijt] * std::exp(-rij * r->rhoi[ijt]);
+                    telj[ijt] += aux - r6;
+                    tuav += aux - r6;
+                    fij = aux * r->rhoi[ijt] / rij - 6.0 * rsqi * r6;
+                    break;
+                default: fij = 0.0;
+            }
+            aux = facq * r->qs[i] * r->qs[j] / rij;
+            double alfar = alfa * rij;
+            double t = 1.0 / (1.0 + PP * alfar);
+            double exp2a = std::exp(-alfar * alfar);
+            double erfx = ((((A5 * t + A4) * t + A3) * t + A2) * t + A1) * t * exp2a;
+            teqq[ijt] += erfx * aux;
+            tuav += erfx * aux;
+            fij = fij + (spii * alfar * exp2a + erfx) * aux * rsqi;
+            tfx[i] += xio * fij; tfy[i] += yio * fij; tfz[i] += zio * fij;
+            tfx[j] -= xio * fij; tfy[j] -= yio * fij; tfz[j] -= zio * fij;
+            int64_t jmin = j + 1;
+            const int64_t nsi_i = r->nsi[it - 1], nsi_j = r->nsi[jt - 1];
+            for (int64_t ix = i; ix < i + nsi_i; ++ix) {
+                double xi = xio + rsx[ix], yi = yio + rsy[ix], zi = zio + rsz[ix];
+                double qx = facq * r->qs[ix];
+                for (int64_t jx = jmin; jx < j + nsi_j; ++jx) {
+                    double xd = xi - rsx[jx], yd = yi - rsy[jx], zd = zi - rsz[jx];
+                    double rs2 = xd * xd + yd * yd + zd * zd;
+                    double rs2i = 1.0 / rs2;
+                    double rr = std::sqrt(rs2);
+                    double au = qx * r->qs[jx] / rr;
+                    double ar = alfa * rr;
+                    double tt = 1.0 / (1.0 + PP * ar);
+                    double e2 = std::exp(-ar * ar);
+                    double ef = ((((A5 * tt + A4) * tt + A3) * tt + A2) * tt + A1) * tt * e2;
+                    teqq[ijt] += ef * au;
+                    tuav += ef * au;
+                    double fj = (spii * ar * e2 + ef) * au * rs2i;
+                    tfx[ix] += xd * fj; tfy[ix] += yd * fj; tfz[ix] += zd * fj;
+                    tfx[jx] -= xd * fj; tfy[jx] -= yd * fj; tfz[jx] -= zd * fj;
+                }
+                jmin = j;
+            }
+        }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        {
+            for (int64_t i = 0; i < nmove; ++i) {
+                fx[i] += tfx[i]; fy[i] += tfy[i]; fz[i] += tfz[i];
+            }
+            for (int64_t k = 0; k < nijt; ++k) {
+                elj[k] += telj[k]; eqq[k] += teqq[k];
+            }
+            uavex += tuav;
+        }
+    }
+
+    // wall partition of the surface-atom z forces (src/forcem.f90:408-413)
+    for (int64_t i = r->nliqa; i < nmove; ++i) fwsz[(int)fsign(z0[i]) + 1] += fz[i];
+
+    // ---- moving-wall pairs (src/forcem.f90:418-498)
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+        std::vector<double> tfx(nmove, 0.0), tfy(nmove, 0.0), tfz(nmove, 0.0), telj(nijt, 0.0),
+            teqq(nijt, 0.0);
+        double tuav = 0.0, tws[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (int64_t k = 0; k < nwpair; ++k) {
+            const int64_t i = r->listw1[k], j = r->listw2[k];
+            const int64_t w = j - nmove;
+            double xi = r->mx(x0[i] - r->wx[w]);
+            double yi = r->my(y0[i] - r->wy[w]);
+            double zi = r->mz_real(z0[i] - r->wz[w]);
+            double rsq = xi * xi + yi * yi + zi * zi;
+            if (rsq > rcutsq) continue;
+            const int sg = (int)fsign(r->wz[w]) + 1;
+            const int64_t it = r->itype[i];
+            const int ijt = r->ij(it, r->itype[j]);
+            double fij = 0.0, rsqi, rij, r6, aux;
+            switch (r->vdwnum[ijt]) {
+                case 1:
+                    rsqi = 1.0 / rsq;
+                    r6 = r->sig[ijt] * pw3(rsqi);
+                    telj[ijt] += r->eps[ijt] * r6 * (r6 - 1.0);
+                    tuav += r->eps[ijt] * r6 * (r6 - 1.0);
+                    fij = 6.0 * rsqi * r->eps[ijt] * r6 * (2.0 * r6 - 1.0);
+                    break;
+                case 2:
+                    rsqi = 1.0 / rsq;
+                    rij = std::sqrt(rsq);
+                    r6 = r->cc[ijt] * pw3(rsqi);
+                    aux = r->aa[ijt] * std::exp(-rij * r->rhoi[ijt]);
+                    telj[ijt] += aux - r6;
+                    tuav += aux - r6;
+                    fij = aux * r->rhoi[ijt] / rij - 6.0 * rsqi * r6;
+                    break;
+                default: fij = 0.0;
+            }
+            const double qx = facq * r->qs[j];
+            for (int64_t ix = i; ix < i + r->nsi[it - 1]; ++ix) {
+                double xd = xi + rsx[ix], yd = yi + rsy[ix], zd = zi + rsz[ix];
+                double rs2 = xd * xd + yd * yd + zd * zd;
+                double rr = std::sqrt(rs2);
+                double rs2i = 1.0 / rs2;
+                double au = qx * r->qs[ix] / rr;
+                double ar = alfa * rr;
+                double tt = 1.0 / (1.0 + PP * ar);
+                double e2 = std::exp(-ar * ar);
+                double ef = ((((A5 * tt + A4) * tt + A3) * tt + A2) * tt + A1) * tt * e2;
+                teqq[ijt] += ef * au;
+                tuav += ef * au;
+                fij = fij + (spii * ar * e2 + ef) * au * rs2i;
+                tfx[ix] += xd * fij; tfy[ix] += yd * fij; tfz[ix] += zd * fij;
+                if (it <= r->nltype) {
+                    tws[0][sg] -= xd * fij; tws[1][sg] -= yd * fij; tws[2][sg] -= zd * fij;
+                }
+                fij = 0.0;
+            }
+        }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        {
+            for (int64_t i = 0; i < nmove; ++i) {
+                fx[i] += tfx[i]; fy[i] += tfy[i]; fz[i] += tfz[i];
+            }
+            for (int64_t k = 0; k < nijt; ++k) {
+                elj[k] += telj[k]; eqq[k] += teqq[k];
+            }
+            uavex += tuav;
+            for (int c = 0; c < 3; ++c) {
+                fwsx[c] += tws[0][c]; fwsy[c] += tws[1][c]; fwsz[c] += tws[2][c];
+            }
+        }
+    }
+
+    // ---- wall long-range tail (src/forcem.f90:509-543; absent in the bulk variant)
+    if (r->variant == MDG_SLAB) {
+        for (int64_t i = 0; i < nmove; ++i) {
+            const int64_t it = r->itype[i];
+            if (std::fabs(r->qs[i]) < F(0.7f)) continue;
+            for (int j = -1; j <= 1; j += 2) {
+                double aux = 0.0, sgn = (double)j;
+                double dw = r->lwh - sgn * z0[i];
+                const int64_t t0 = it - 1;
+                if (dw < r->rcut) {
+                    aux = aux + sgn * r->flr_w[t0];
+                    ulr += r->ulr_w[t0];
+                } else {
+                    aux = aux + sgn * r->flr_l[t0];
+                    ulr += r->ulr_l[t0];
+                    double dwa = 1.0 / (dw * dw);
+                    double dwa2 = dwa * dwa;
+                    double dwa5 = dwa2 * dwa2 * dwa;
+                    aux = aux + sgn * (r->flr_lja[t0] * dwa5 - r->flr_ljc[t0] * dwa2);
+                    double dw3 = dw * dw * dw;
+                    double dw9 = dw3 * dw3 * dw3;
+                    ulr += (r->flr_lja[t0] / (9.0 * dw9) - r->flr_ljc[t0] / (3.0 * dw3));
+                    double t = r->flr_bur[t0];
+                    double exp2a = r->flr_bua[t0] * std::exp(-dw / t);
+                    aux = aux + sgn * ((t + dw) * exp2a - r->flr_buc[t0] * dwa2);
+                    ulr += (t * (2.0 * t + dw) * exp2a - r->flr_buc[t0] / (3.0 * dw3));
+                }
+                fz[i] -= aux;
+                if (it <= r->nltype) fwsz[j + 1] += aux;
+            }
+        }
+        uavex += ulr;
+    }
+
+    // ---- force_fouri (src/forcem.f90:827-937)
+    {
+        const int64_t ng = r->ngogo, KL = r->klmax, KM = r->kmmax, KN = r->knmax;
+        std::vector<cplx> el((size_t)ng * (KL + 1)), em((size_t)ng * (2 * KM + 1)), en((size_t)ng * (2 * KN + 1));
+        auto EL = [&](int64_t i, int64_t l) -> cplx& { return el[i * (KL + 1) + l]; };
+        auto EM = [&](int64_t i, int64_t m) -> cplx& { return em[i * (2 * KM + 1) + m + KM]; };
+        auto EN = [&](int64_t i, int64_t n) -> cplx& { return en[i * (2 * KN + 1) + n + KN]; };
+        for (int64_t i = 0; i < ng; ++i) {
+            EL(i, 0) = EM(i, 0) = EN(i, 0) = cplx(1.0, 0.0);
+            double ax = r->pipix * x0[i], ay = r->pipiy * y0[i], az = r->pipiz * z0[i];
+            EL(i, 1) = cplx(std::cos(ax), std::sin(ax));
+            EM(i, 1) = cplx(std::cos(ay), std::sin(ay));
+            EN(i, 1) = cplx(std::cos(az), std::sin(az));
+            for (int64_t l = 2; l <= KL; ++l) EL(i, l) = EL(i, l - 1) * EL(i, 1);
+            for (int64_t m = 2; m <= KM; ++m) EM(i, m) = EM(i, m - 1) * EM(i, 1);
+            for (int64_t m = 1; m <= KM; ++m) EM(i, -m) = std::conj(EM(i, m));
+            for (int64_t n = 2; n <= KN; ++n) EN(i, n) = EN(i, n - 1) * EN(i, 1);
+            for (int64_t n = 1; n <= KN; ++n) EN(i, -n) = std::conj(EN(i, n));
+        }
+        const int64_t nk = (int64_t)r->Ak.size();
+        double ewqLL = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+        {
+            std::vector<double> tfx(nmove, 0.0), tfy(nmove, 0.0), tfz(nmove, 0.0);
+            std::vector<cplx> elmn(ng);
+            double tLL = 0.0, tew = 0.0;
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+            for (int64_t k = 0; k < nk; ++k) {
+                const int kl = r->kl_[k], km = r->km_[k], kn = r->kn_[k];
+                const double rl = r->pipix * (double)(float)kl, rm = r->pipiy * (double)(float)km,
+                             rn = r->pipiz * (double)(float)kn;
+                cplx qll(0.0, 0.0);
+                for (int64_t i = 0; i < ng; ++i) {
+                    elmn[i] = r->qs[i] * EL(i, kl) * EM(i, km) * EN(i, kn);
+                    qll += elmn[i];
+                }
+                cplx qsum = qll + r->Qsumw1[k] + r->Qsumw2[k];
+                const double akx = r->Ak[k];
+                tLL += (akx * qll * std::conj(qll)).real();
+                tew += akx * (qsum * std::conj(qsum)).real();
+                for (int64_t i = 0; i < nmove; ++i) {
+                    double ft = akx * (std::conj(qsum) * elmn[i]).imag();
+                    tfx[i] += ft * rl; tfy[i] += ft * rm; tfz[i] += ft * rn;
+                }
+            }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+            {
+                for (int64_t i = 0; i < nmove; ++i) {
+                    fx[i] += tfx[i]; fy[i] += tfy[i]; fz[i] += tfz[i];
+                }
+                ewqLL += tLL;
+                uewa += tew;
+            }
+        }
+        ewqLL *= 0.5;
+        uewa *= 0.5;
+        uavex += uewa;
+        if (e) {
+            e->ewqLL = ewqLL;
+            e->ewqWW = r->ewqWW;
+            e->ewqWL = uewa - r->ewqWW - ewqLL;
+        }
+        if (r->variant == MDG_SLAB) {  // EW3DC (src/forcem.f90:924-928)
+            double dipz = 0.0;
+            for (int64_t i = 0; i < nmove; ++i) dipz += r->qs[i] * z0[i];
+            double crf = -2.0 * M_PI_R * r->lzi * r->lxi * r->lyi;
+            urf = -crf * facq * dipz * dipz;
+            crf = 2.0 * crf * facq * dipz;
+            for (int64_t i = 0; i < nmove; ++i) fz[i] += crf * r->qs[i];
+        }
+    }
+
+    // ---- force_intra (src/forcem.f90:565-652)
+    for (int64_t ia = 0; ia < r->nang; ++ia) {
+        const int64_t it = r->iatype[ia] - 1;
+        for (int64_t is = 0; is < r->nangt[it]; ++is) {
+            const int64_t i = r->ang1[is + MDG_SMX * ia] - 1, j = r->ang2[is + MDG_SMX * ia] - 1,
+                          k = r->ang3[is + MDG_SMX * ia] - 1;
+            auto X = [&](int64_t a) { return a < nmove ? x0[a] : r->wx[a - nmove]; };
+            auto Y = [&](int64_t a) { return a < nmove ? y0[a] : r->wy[a - nmove]; };
+            auto Z = [&](int64_t a) { return a < nmove ? z0[a] : r->wz[a - nmove]; };
+            double ax = r->mx(X(k) - X(j)), ay = r->my(Y(k) - Y(j)), az = r->mz_real(Z(k) - Z(j));
+            double bx = r->mx(X(j) - X(i)), by = r->my(Y(j) - Y(i)), bz = r->mz_real(Z(j) - Z(i));
+            double ai = 1.0 / std::sqrt(ax * ax + ay * ay + az * az);
+            double bi = 1.0 / std::sqrt(bx * bx + by * by + bz * bz);
+            double ab = ax * bx + ay * by + az * bz;
+            double cang = -ab * ai * bi;
+            double fij = r->kt[it + r->ntype * is] * (std::acos(cang) - r->theta[it + r->ntype * is]) /
+                         std::sqrt(1.0 - cang * cang);
+            fij = fij * ai * bi;
+            double bb = ab * bi * bi, aa = ab * ai * ai;
+            double tmp = aa * ax - bx;
+            if (k < nmove) fx[k] += fij * tmp;
+            if (j < nmove) fx[j] += fij * (bb * bx - ax - tmp);
+            tmp = aa * ay - by;
+            if (k < nmove) fy[k] += fij * tmp;
+            if (j < nmove) fy[j] += fij * (bb * by - ay - tmp);
+            tmp = aa * az - bz;
+            if (k < nmove) fz[k] += fij * tmp;
+            if (j < nmove) fz[j] += fij * (bb * bz - az - tmp);
+        }
+    }
+
+    // ---- serial force_sum (src/forcem_3d.f90:1031-1070)
+    uavex += urf;
+    {
+        double sx = 0, sy = 0, sz = 0;
+        for (int64_t i = 0; i < nmove; ++i) {
+            sx += fx[i]; sy += fy[i]; sz += fz[i];
+        }
+        fwsx[1] = sx; fwsy[1] = sy; fwsz[1] = sz;
+    }
+    if (fxo)
+        for (int64_t i = 0; i < nmove; ++i) {
+            fxo[i] = fx[i]; fyo[i] = fy[i]; fzo[i] = fz[i];
+        }
+    for (int64_t i = nriga; i < nmove; ++i) {
+        if (ftx) {
+            ftx[i - nriga] = fx[i]; fty[i - nriga] = fy[i]; ftz[i - nriga] = fz[i];
+        }
+    }
+    for (int64_t i = 0; i < nrig; ++i) {
+        const int64_t j = 3 * i;
+        if (fcx) {
+            fcx[i] = fx[j] + fx[j + 1] + fx[j + 2];
+            fcy[i] = fy[j] + fy[j + 1] + fy[j + 2];
+            fcz[i] = fz[j] + fz[j + 1] + fz[j + 2];
+        }
+    }
+    for (int64_t i = 0; i < nrig; ++i) {
+        const int64_t j = 3 * i;
+        for (int s = 0; s < 3; ++s) {
+            rsx[s] = x0[j + s] - cx0[i];
+            rsy[s] = y0[j + s] - cy0[i];
+            rsz[s] = z0[j + s] - cz0[i];
+        }
+        if (tx) {
+            tx[i] = (rsy[0] * fz[j] - rsz[0] * fy[j]) + (rsy[1] * fz[j + 1] - rsz[1] * fy[j + 1]) +
+                    (rsy[2] * fz[j + 2] - rsz[2] * fy[j + 2]);
+            ty[i] = (rsz[0] * fx[j] - rsx[0] * fz[j]) + (rsz[1] * fx[j + 1] - rsx[1] * fz[j + 1]) +
+                    (rsz[2] * fx[j + 2] - rsx[2] * fz[j + 2]);
+            tz[i] = (rsx[0] * fy[j] - rsy[0] * fx[j]) + (rsx[1] * fy[j + 1] - rsy[1] * fx[j + 1]) +
+                    (rsx[2] * fy[j + 2] - rsy[2] * fx[j + 2]);
+        }
+    }
+    if (e) {
+        double sumlj = 0.0, sumqq = 0.0;
+        for (int64_t k = 0; k < nijt; ++k) {
+            sumlj += elj[k];
+            sumqq += eqq[k];
+            if (e->elj) e->elj[k] = elj[k];
+            if (e->eqq) e->eqq[k] = eqq[k];
+        }
+        e->uewa = uewa;
+        e->urf = urf;
+        e->ulr = ulr;
+        e->uself = r->uself;
+        double uconf = sumlj + sumqq + uewa + r->uself + urf;
+        e->uconf = uconf - r->uself;
+        e->uavex = uavex;
+        e->vir = 0.0;
+        e->press = (fwsz[2] - fwsz[0]) / (2.0 * r->lx * r->ly) * 1000.0 / (PH_Na * F(1e-30f)) * F(1e-5f);
+        for (int c = 0; c < 3; ++c) {
+            e->fwsx[c] = fwsx[c]; e->fwsy[c] = fwsy[c]; e->fwsz[c] = fwsz[c];
+        }
+    }
+    return MDG_OK;
+}
+
+// move_shake (src/move.f90:408-529).  x0..: ntota; xold..: ntota-nliqa; ftx..: nmove-nriga.
+int ref_shake(RefCtx* r, double* x0, double* y0, double* z0, double* xold, double* yold, double* zold,
+              const double* ftx, const double* fty, const double* ftz, double* kps_out, double* tkps,
+              int32_t* sweeps) {
+    const int64_t ismin = r->nliqa, ismax = r->nmove;  // 0-based [ismin, ismax)
+    const int64_t nl = r->nliqa, nr = r->nriga;
+    std::vector<double> kps(r->nit, 0.0);
+    for (int64_t i = ismin; i < ismax; ++i) {
+        const int64_t it = r->itype[i] - 1;
+        double aux = xold[i - nl];
+        xold[i - nl] = x0[i];
+        aux = x0[i] - aux;
+        aux = r->mx(aux);
+        x0[i] = x0[i] + aux + ftx[i - nr] * r->mii[i];
+        double kaux = aux * aux;
+        aux = yold[i - nl];
+        yold[i - nl] = y0[i];
+        aux = y0[i] - aux;
+        aux = r->my(aux);
+        y0[i] = y0[i] + aux + fty[i - nr] * r->mii[i];
+        kaux = kaux + aux * aux;
+        aux = zold[i - nl];
+        zold[i - nl] = z0[i];
+        aux = z0[i] - aux;
+        z0[i] = z0[i] + aux + ftz[i - nr] * r->mii[i];
+        kaux = kaux + aux * aux;
+        kps[it] += r->mi[i] * kaux;
+    }
+    double ks = 0.0;
+    for (double v : kps) ks += v;
+    if (tkps) *tkps = r->nfreed > 0 ? ks * 1000.0 / (PH_R * (double)(float)r->nfreed) : 0.0;
+    if (kps_out)
+        for (int64_t t = 0; t < r->nit; ++t) kps_out[t] = kps[t];
+
+    // moving/moved flags over ismin..ntota (walls stay "not moved" = 1)
+    std::vector<int> moving(r->ntota - ismin, 1), moved(r->ntota - ismin, 1);
+    for (int64_t i = ismin; i < ismax; ++i) moved[i - ismin] = 0;
+    auto X = [&](int64_t a) -> double& { return x0[a]; };
+    const bool clean = (r->quirks & MDG_QUIRK_CLEAN_SHAKE_DONE) != 0;
+    bool done = false;
+    int ite = 0;
+    const double lx = r->lx, ly = r->ly, lz = r->lz, lxi = r->lxi, lyi = r->lyi, lzi = r->lzi;
+    for (;;) {
+        if (done || ite > r->maxit) break;
+        bool any = false;
+        for (int64_t ic = 0; ic < r->ncons; ++ic) {
+            done = true;
+            const int64_t it = r->ictype[ic] - 1;
+            for (int64_t is = 0; is < r->nconst[it]; ++is) {
+                const int64_t ia = r->constra[is + MDG_SMX * ic] - 1, ib = r->constrb[is + MDG_SMX * ic] - 1;
+                if (ia < ismin || ib < ismin) return fail(r, MDG_E_ARG, "constraint atom below the surface range");
+                if (moved[ia - ismin] * moved[ib - ismin] != 0) continue;
+                double px = x0[ia] - x0[ib]; px = px - lx * anint(px * lxi);
+                double py = y0[ia] - y0[ib]; py = py - ly * anint(py * lyi);
+                double pz = z0[ia] - z0[ib]; pz = pz - lz * anint(pz * lzi);
+                const double L = r->length[it + r->ntype * is];
+                double rabsq = L * L;
+                double diffsq = rabsq - (px * px + py * py + pz * pz);
+                if (std::fabs(diffsq) > rabsq * r->tol2) {
+                    auto OX = [&](int64_t a, int c) -> double {
+                        if (a >= nl) return c == 0 ? xold[a - nl] : c == 1 ? yold[a - nl] : zold[a - nl];
+                        return 0.0;
+                    };
+                    double rx = OX(ia, 0) - OX(ib, 0); rx = rx - lx * anint(rx * lxi);
+                    double ry = OX(ia, 1) - OX(ib, 1); ry = ry - ly * anint(ry * lyi);
+                    double rz = OX(ia, 2) - OX(ib, 2); rz = rz - lz * anint(rz * lzi);
+                    double rpab = rx * px + ry * py + rz * pz;
+                    if (rpab < rabsq * r->rptol) {
+                        char b[160];
+                        snprintf(b, sizeof b, "Constraint failure: atoms %lld %lld", (long long)ia + 1, (long long)ib + 1);
+                        if (sweeps) *sweeps = ite + 1;
+                        return fail(r, MDG_E_SHAKE_RPTOL, b);
+                    }
+                    double rma = r->mii[ia], rmb = r->mii[ib];
+                    double aux = diffsq / (2.0 * (rma + rmb) * rpab);
+                    rma = rma * aux;
+                    rmb = rmb * aux;
+                    X(ia) += rx * rma; y0[ia] += ry * rma; z0[ia] += rz * rma;
+                    x0[ib] -= rx * rmb; y0[ib] -= ry * rmb; z0[ib] -= rz * rmb;
+                    moving[ia - ismin] = 0;
+                    moving[ib - ismin] = 0;
+                    done = false;
+                    any = true;
+                }
+            }
+        }
+        if (clean) done = !any;
+        ++ite;
+        for (int64_t i = ismin; i < ismax; ++i) {
+            moved[i - ismin] = moving[i - ismin];
+            moving[i - ismin] = 1;
+        }
+    }
+    if (sweeps) *sweeps = ite;
+    if (!done && r->ncons > 0) return fail(r, MDG_E_SHAKE_MAXIT, "shake(): Too many constraint iterations!");
+    return MDG_OK;
+}
+
+}  // extern "C"
