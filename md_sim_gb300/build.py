@@ -32,8 +32,8 @@ def _deps():
         os.path.join(HERE, "..", "include", "mdgpu.h")]
 
 
-def _compile(src, extra=()):
-    obj = os.path.join(OUT, os.path.basename(src) + ".o")
+def _compile(src, extra=(), out=OUT):
+    obj = os.path.join(out, os.path.basename(src) + ".o")
     newest = max([os.path.getmtime(src)] + [os.path.getmtime(d) for d in _deps() if os.path.exists(d)])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
         return obj
@@ -44,22 +44,28 @@ def _compile(src, extra=()):
     return obj
 
 
-def build(verbose=False, extra=()):
-    os.makedirs(OUT, exist_ok=True)
+def build(verbose=False, debug=False):
+    """debug=True builds md_sim_gb300/_build_dbg/libmdgpu.so with index checks (MDG_DEBUG_BOUNDS)."""
+    out = OUT + "_dbg" if debug else OUT
+    lib = os.path.join(out, "libmdgpu.so")
+    extra = ("-DMDG_DEBUG_BOUNDS",) if debug else ()
+    os.makedirs(out, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(SRC, "*.cu")))
     with ThreadPoolExecutor(max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
-    if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, extra, out), srcs))
+    if not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs):
+        tmp = lib + ".tmp"
         cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib)
     if verbose:
-        print(LIB)
-    return LIB
+        print(lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(verbose=True)
+    import sys
+
+    build(verbose=True, debug="--debug" in sys.argv)

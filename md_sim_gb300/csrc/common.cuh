@@ -21,8 +21,19 @@ enum StatusWord {
     ST_CELL_OVF = 4,
     ST_REBUILD = 5,    // 1 when the current step rebuilt the list
     ST_SWEEPS = 6,     // SHAKE sweeps of the last call
+    ST_OOB = 7,        // debug builds: tag of the first out-of-range index seen
     ST_NWORDS = 8
 };
+
+// Debug builds (-DMDG_DEBUG_BOUNDS) check indices on the force path: an index outside [0, n)
+// records its site tag in status[ST_OOB] and is redirected to element 0, so the kernel reports
+// instead of faulting.  Release builds compile the check away.
+#ifdef MDG_DEBUG_BOUNDS
+#define CK(i, n, tag) \
+    (((unsigned)(i) < (unsigned)(n)) ? (int)(i) : (atomicCAS(&v.status[ST_OOB], 0, (tag)), 0))
+#else
+#define CK(i, n, tag) (i)
+#endif
 
 // Minimum image with the reference's rounding, no multiply-add contraction:
 // d - l*anint(d*li)   (src/nnlist.f90:125, src/forcem.f90:293).  anint = round half away.

@@ -127,6 +127,7 @@ struct Ctx {
     std::vector<double> h_qs_wall;  // wall charges (for the static structure factor)
     double *d_ft = nullptr, *d_fc = nullptr, *d_tq = nullptr;  // force_sum outputs
     bool alloc_failed = false;
+    bool debug_sync = false;
     // host staging (pinned)
     double* h_acc = nullptr;
     int* h_status = nullptr;

@@ -76,13 +76,13 @@ __global__ void k_force_sum(View v, double* ft, double* fc, double* tq) {
         sz += v.fz[i];
         if (i >= v.nriga) {
             const int k = i - v.nriga;
-            ft[k] = v.fx[i];
-            ft[nflex + k] = v.fy[i];
-            ft[2 * nflex + k] = v.fz[i];
+            ft[CK(k, nflex, 301)] = v.fx[i];
+            ft[CK(nflex + k, 3 * nflex, 302)] = v.fy[i];
+            ft[CK(2 * nflex + k, 3 * nflex, 303)] = v.fz[i];
         }
     }
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < v.nrig; m += stride) {
-        const int j = 3 * m;
+        const int j = CK(3 * m, v.nmove - 2, 304);
         const double f0x = v.fx[j], f1x = v.fx[j + 1], f2x = v.fx[j + 2];
         const double f0y = v.fy[j], f1y = v.fy[j + 1], f2y = v.fy[j + 2];
         const double f0z = v.fz[j], f1z = v.fz[j + 1], f2z = v.fz[j + 2];

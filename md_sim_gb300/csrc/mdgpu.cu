@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -182,6 +183,30 @@ int read_status(Ctx& c) {
     return sync_check(c, "status");
 }
 
+// Debug runs (MDG_DEBUG_SYNC=1 in the environment at mdg_create): synchronise after every
+// phase and report the first phase that failed or saw an out-of-range index.
+int phase_check(Ctx& c, const char* name) {
+    if (!c.debug_sync) return MDG_OK;
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return set_err(&c, MDG_E_CUDA, std::string("phase ") + name + ": " + cudaGetErrorString(e));
+    int st[ST_NWORDS];
+    cudaMemcpy(st, c.v.status, sizeof(st), cudaMemcpyDeviceToHost);
+    if (st[ST_OOB]) {
+        char b[160];
+        snprintf(b, sizeof b, "phase %s: out-of-range index at site %d", name, st[ST_OOB]);
+        return set_err(&c, MDG_E_CUDA, b);
+    }
+    return MDG_OK;
+}
+
+#define PHASE(call, name)                   \
+    do {                                    \
+        call;                               \
+        int prc_ = phase_check(c, name);    \
+        if (prc_) return prc_;              \
+    } while (0)
+
 // Runs the force phases on device-resident positions.  Returns MDG_OK or an error.
 int run_force(Ctx& c, bool force_rebuild) {
     View& v = c.v;
@@ -191,16 +216,16 @@ int run_force(Ctx& c, bool force_rebuild) {
         cudaMemsetAsync(v.fz, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
         cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
         cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
-        nnlist_trigger(c, force_rebuild || attempt > 0);
-        nnlist_build(c);
-        pair_forces_fp64(c);
-        surf_partition(c);
-        wall_forces_fp64(c);
-        lr_tail(c);
-        recip_fp64(c);
-        dipole_correction(c);
-        angle_forces(c);
-        force_sum(c, c.d_ft, c.d_fc, c.d_tq);
+        PHASE(nnlist_trigger(c, force_rebuild || attempt > 0), "trigger");
+        PHASE(nnlist_build(c), "nnlist");
+        PHASE(pair_forces_fp64(c), "pairs");
+        PHASE(surf_partition(c), "surf_partition");
+        PHASE(wall_forces_fp64(c), "walls");
+        PHASE(lr_tail(c), "lr_tail");
+        PHASE(recip_fp64(c), "reciprocal");
+        PHASE(dipole_correction(c), "dipole");
+        PHASE(angle_forces(c), "angles");
+        PHASE(force_sum(c, c.d_ft, c.d_fc, c.d_tq), "force_sum");
         int rc = read_status(c);
         if (rc) return rc;
         const int ovf = c.h_status[ST_LIST_OVF], wovf = c.h_status[ST_WLIST_OVF];
@@ -262,6 +287,10 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
     cudaGetDevice(&c.device);
     c.sysc = *s;
     c.precision = p->precision;
+    {
+        const char* dbg = getenv("MDG_DEBUG_SYNC");
+        c.debug_sync = dbg && dbg[0] == '1';
+    }
     c.variant = p->variant;
     c.quirks = p->quirks;
     auto bail = [&](int code) {

@@ -64,33 +64,33 @@ __global__ void __launch_bounds__(kNT) k_pair_fp64(View v) {
     const int nwarps = gridDim.x * kWarps;
     EAcc e;
     for (int h = warp; h < v.nheads; h += nwarps) {
-        const int i = v.head_atom[h];
-        const int it = v.type[i];
-        const int nsi_i = v.nsi[it];
-        const double xi0 = v.x[i], yi0 = v.y[i], zi0 = v.z[i];
+        const int i = v.head_atom[CK(h, v.nheads, 101)];
+        const int it = v.type[CK(i, v.ntota, 102)];
+        const int nsi_i = v.nsi[CK(it, v.nit, 103)];
+        const double xi0 = v.x[CK(i, v.ntota, 104)], yi0 = v.y[CK(i, v.ntota, 104)], zi0 = v.z[CK(i, v.ntota, 104)];
         double rix[3], riy[3], riz[3], qi[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const bool ok = a < nsi_i;
-            rix[a] = ok ? v.rsx[i + a] : 0.0;
-            riy[a] = ok ? v.rsy[i + a] : 0.0;
-            riz[a] = ok ? v.rsz[i + a] : 0.0;
-            qi[a] = ok ? v.q[i + a] : 0.0;
+            rix[a] = ok ? v.rsx[CK(i + a, v.nmove, 105)] : 0.0;
+            riy[a] = ok ? v.rsy[CK(i + a, v.nmove, 105)] : 0.0;
+            riz[a] = ok ? v.rsz[CK(i + a, v.nmove, 105)] : 0.0;
+            qi[a] = ok ? v.q[CK(i + a, v.ntota, 106)] : 0.0;
         }
         double fix[3] = {0, 0, 0}, fiy[3] = {0, 0, 0}, fiz[3] = {0, 0, 0};
-        const int n = v.nbcnt[h];
-        const int* nb = v.nb + (size_t)h * v.maxnb;
+        const int n = v.nbcnt[CK(h, v.nheads, 107)];
+        const int* nb = v.nb + (size_t)CK(h, v.nheads, 120) * v.maxnb;
         for (int k = lane; k < n; k += 32) {
-            const int j = nb[k];
-            double xio = minimg(xi0 - v.x[j], v.lx, v.lxi);
+            const int j = nb[CK(k, v.maxnb, 108)];
+            double xio = minimg(xi0 - v.x[CK(j, v.nmove, 109)], v.lx, v.lxi);
             double yio = minimg(yi0 - v.y[j], v.ly, v.lyi);
             double zio = zi0 - v.z[j];
             if (v.bulk) zio = minimg(zio, v.lz, v.lzi);
             const double rsq = xio * xio + yio * yio + zio * zio;
             if (rsq > v.rcutsq) continue;
-            const int jt = v.type[j];
-            const int ijt = v.ijt[it * v.nit + jt];
-            const int nsi_j = v.nsi[jt];
+            const int jt = v.type[CK(j, v.ntota, 110)];
+            const int ijt = CK(v.ijt[CK(it * v.nit + jt, v.nit * v.nit, 111)], v.nijt, 112);
+            const int nsi_j = v.nsi[CK(jt, v.nit, 113)];
             const double rsqi = 1.0 / rsq;
             const double rij = sqrt(rsq);
             double fij = 0.0, elj = 0.0;
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kNT) k_pair_fp64(View v) {
                 fij = aux * v.rhoi[ijt] / rij - 6.0 * rsqi * r6;
             }
             double ff;
-            const double auxq = v.facq * qi[0] * v.q[j] / rij;
+            const double auxq = v.facq * qi[0] * v.q[CK(j, v.ntota, 114)] / rij;
             const double erfx = ewald_erfc(v.alfa * rij, &ff, v.spii);
             double eqq = erfx * auxq;
             fij = fij + ff * auxq * rsqi;
@@ -118,12 +118,12 @@ __global__ void __launch_bounds__(kNT) k_pair_fp64(View v) {
             for (int b = 1; b < 3; ++b) {
                 fjx[b] = fjy[b] = fjz[b] = 0.0;
                 const bool ok = b < nsi_j;
-                rjx[b] = ok ? v.rsx[j + b] : 0.0;
-                rjy[b] = ok ? v.rsy[j + b] : 0.0;
-                rjz[b] = ok ? v.rsz[j + b] : 0.0;
-                qj[b] = ok ? v.q[j + b] : 0.0;
+                rjx[b] = ok ? v.rsx[CK(j + b, v.nmove, 115)] : 0.0;
+                rjy[b] = ok ? v.rsy[CK(j + b, v.nmove, 115)] : 0.0;
+                rjz[b] = ok ? v.rsz[CK(j + b, v.nmove, 115)] : 0.0;
+                qj[b] = ok ? v.q[CK(j + b, v.ntota, 116)] : 0.0;
             }
-            rjx[0] = v.rsx[j]; rjy[0] = v.rsy[j]; rjz[0] = v.rsz[j]; qj[0] = v.q[j];
+            rjx[0] = v.rsx[CK(j, v.nmove, 117)]; rjy[0] = v.rsy[CK(j, v.nmove, 117)]; rjz[0] = v.rsz[CK(j, v.nmove, 117)]; qj[0] = v.q[CK(j, v.ntota, 117)];
             // remaining site pairs (src/forcem.f90:360-402): (head of i, sites 2.. of j), then
             // (sites 2.. of i, all sites of j)
 #pragma unroll
@@ -151,9 +151,9 @@ __global__ void __launch_bounds__(kNT) k_pair_fp64(View v) {
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
                 if (b >= nsi_j) break;
-                atomicAdd(&v.fx[j + b], fjx[b]);
-                atomicAdd(&v.fy[j + b], fjy[b]);
-                atomicAdd(&v.fz[j + b], fjz[b]);
+                atomicAdd(&v.fx[CK(j + b, v.nmove, 118)], fjx[b]);
+                atomicAdd(&v.fy[CK(j + b, v.nmove, 118)], fjy[b]);
+                atomicAdd(&v.fz[CK(j + b, v.nmove, 118)], fjz[b]);
             }
             e_add(e, ijt, elj, eqq, s_e, v.nijt);
         }
@@ -162,9 +162,9 @@ __global__ void __launch_bounds__(kNT) k_pair_fp64(View v) {
             if (a >= nsi_i) break;
             const double sx = warp_sum(fix[a]), sy = warp_sum(fiy[a]), sz = warp_sum(fiz[a]);
             if (lane == 0) {
-                atomicAdd(&v.fx[i + a], sx);
-                atomicAdd(&v.fy[i + a], sy);
-                atomicAdd(&v.fz[i + a], sz);
+                atomicAdd(&v.fx[CK(i + a, v.nmove, 119)], sx);
+                atomicAdd(&v.fy[CK(i + a, v.nmove, 119)], sy);
+                atomicAdd(&v.fz[CK(i + a, v.nmove, 119)], sz);
             }
         }
     }

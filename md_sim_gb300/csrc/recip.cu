@@ -65,12 +65,17 @@ __device__ void phase_tables(double x, double y, double z, const KDims& d, doubl
 }
 
 __device__ __forceinline__ double2 pw(const double2* t, int k) { return k >= 0 ? t[k] : conjd(t[-k]); }
+#ifdef MDG_DEBUG_BOUNDS
+#define PW(t, k, lim, tag) pw((t), ((k) > (lim) || (k) < -(lim)) ? (atomicCAS(&v.status[ST_OOB], 0, (tag)), 0) : (k))
+#else
+#define PW(t, k, lim, tag) pw((t), (k))
+#endif
 
 // rows: (l, m, n_first, k_first); nlen: kept n in the row (n = n_first .. n_first + nlen - 1)
 __global__ void __launch_bounds__(kSfacNT) k_sfac(View v, KDims d, int nrow, const int4* rows,
                                                   const int* nlen, const int* witem_row,
                                                   const int* witem_n0, int nwork, int tile,
-                                                  int atoms_per_split, double2* S) {
+                                                  int atoms_per_split, double2* S, int nk_total) {
     extern __shared__ double2 sm[];
     const int per = d.KL + 1 + d.KM + 1 + d.KN + 1;
     double2* tab = sm;                                  // tile * per
@@ -78,7 +83,7 @@ __global__ void __launch_bounds__(kSfacNT) k_sfac(View v, KDims d, int nrow, con
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     int l = 0, m = 0, n0 = 0, nn = 0, k0 = 0;
     if (w < nwork) {
-        const int r = witem_row[w];
+        const int r = CK(witem_row[w], nrow, 201);
         const int4 rw = rows[r];
         l = rw.x;
         m = rw.y;
@@ -97,8 +102,8 @@ __global__ void __launch_bounds__(kSfacNT) k_sfac(View v, KDims d, int nrow, con
         __syncthreads();
         for (int s = threadIdx.x; s < nt * 3; s += blockDim.x) {
             const int a = s % nt, which = s / nt;
-            const int at = t0 + a;
-            double2* base = tab + (size_t)a * per;
+            const int at = CK(t0 + a, v.nmove, 202);
+            double2* base = tab + (size_t)CK(a, tile, 203) * per;
             phase_tables(v.x[at], v.y[at], v.z[at], d, base, base + d.KL + 1, base + d.KL + 1 + d.KM + 1, which);
             if (which == 0) qt[a] = v.q[at];
         }
@@ -106,8 +111,8 @@ __global__ void __launch_bounds__(kSfacNT) k_sfac(View v, KDims d, int nrow, con
         if (nn > 0) {
             for (int a = 0; a < nt; ++a) {
                 const double2* base = tab + (size_t)a * per;
-                const double2 el = base[l];
-                const double2 em = pw(base + d.KL + 1, m);
+                const double2 el = base[CK(l, d.KL + 1, 204)];
+                const double2 em = PW(base + d.KL + 1, m, d.KM, 209);
                 const double2* en = base + d.KL + 1 + d.KM + 1;
                 // elm = q*el*em (src/forcem.f90:874), elmn = elm*en (:879)
                 const double q = qt[a];
@@ -115,7 +120,7 @@ __global__ void __launch_bounds__(kSfacNT) k_sfac(View v, KDims d, int nrow, con
 #pragma unroll
                 for (int c = 0; c < kChunk; ++c) {
                     if (c < nn) {
-                        const double2 e = cmul(elm, pw(en, n0 + c));
+                        const double2 e = cmul(elm, PW(en, n0 + c, d.KN, 210));
                         acc[c].x += e.x;
                         acc[c].y += e.y;
                     }
@@ -126,8 +131,8 @@ __global__ void __launch_bounds__(kSfacNT) k_sfac(View v, KDims d, int nrow, con
 #pragma unroll
     for (int c = 0; c < kChunk; ++c) {
         if (c < nn) {
-            atomicAdd(&S[k0 + c].x, acc[c].x);
-            atomicAdd(&S[k0 + c].y, acc[c].y);
+            atomicAdd(&S[CK(k0 + c, nk_total, 205)].x, acc[c].x);
+            atomicAdd(&S[CK(k0 + c, nk_total, 205)].y, acc[c].y);
         }
     }
 }
@@ -147,10 +152,10 @@ __global__ void k_kenergy(View v, int nk, const double* ak, const double2* S, co
 }
 
 __global__ void __launch_bounds__(kForceNT) k_kforce(View v, KDims d, int nrow, const int4* rows,
-                                                     const int* nlen, const double2* C) {
+                                                     const int* nlen, const double2* C, int nk_total) {
     extern __shared__ double2 sm[];
     const int per = d.KM + 1 + d.KN + 1;
-    double2* em = sm + (size_t)threadIdx.x * per;
+    double2* em = sm + (size_t)CK(threadIdx.x, blockDim.x, 206) * per;
     double2* en = em + d.KM + 1;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = j < v.nmove;
@@ -170,15 +175,15 @@ __global__ void __launch_bounds__(kForceNT) k_kforce(View v, KDims d, int nrow, 
             el = cmul(el, el1);
             ++lcur;
         }
-        const double2 emm = pw(em, rw.y);
+        const double2 emm = PW(em, rw.y, d.KM, 211);
         const double2 elm = cmul(make_double2(q * el.x, q * el.y), emm);
         const int n0 = rw.z, cnt = nlen[r];
-        const double2* Ck = C + rw.w;
+        const double2* Ck = C + CK(rw.w, nk_total, 207);
         double st = 0.0, stn = 0.0;
         for (int t = 0; t < cnt; ++t) {
             const int n = n0 + t;
-            const double2 e = cmul(elm, pw(en, n));
-            const double2 ck = Ck[t];
+            const double2 e = cmul(elm, PW(en, n, d.KN, 212));
+            const double2 ck = Ck[CK(t, nk_total - rw.w, 208)];
             const double f = ck.x * e.y + ck.y * e.x;  // Im(C * e), C = Ak conj(S)
             st += f;
             stn += f * (double)n;
@@ -226,7 +231,7 @@ int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const 
         const double rl = ks.pipix * (double)(float)kl;
         for (int km = kmmin; km <= KM; ++km) {
             const double rm = ks.pipiy * (double)(float)km;
-            int first = -1, cnt = 0;
+            int first = 0, cnt = 0;
             for (int kn = knmin; kn <= KN; ++kn) {
                 volatile float a = (float)(kl * kl + km * km);
                 volatile float b = (float)((int64_t)kn * kn * kmax * kmax) / (float)((int64_t)KN * KN);
@@ -234,7 +239,7 @@ int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const 
                 if (!(ksq < lim)) continue;
                 const double rn = ks.pipiz * (double)(float)kn;
                 const double rksq = rl * rl + rm * rm + rn * rn;
-                if (first < 0) first = kn;
+                if (cnt == 0) first = kn;
                 ++cnt;
                 kvec.push_back(make_int3(kl, km, kn));
                 ak.push_back(fac * std::exp(rksq * alf4i) / rksq);
@@ -335,10 +340,10 @@ void recip_fp64(Ctx& c) {
     cudaMemsetAsync(ks.s, 0, sizeof(double2) * ks.nk, c.stream);
     dim3 g((ks.nwork + kSfacNT - 1) / kSfacNT, ks.splits);
     k_sfac<<<g, kSfacNT, ks.sfac_smem, c.stream>>>(v, d, ks.nrow, ks.row, ks.row_nlen, ks.witem_row,
-                                                   ks.witem_n0, ks.nwork, ks.tile, ks.atoms_per_split, ks.s);
+                                                   ks.witem_n0, ks.nwork, ks.tile, ks.atoms_per_split, ks.s, ks.nk);
     k_kenergy<<<std::min((ks.nk + 255) / 256, 256), 256, 0, c.stream>>>(v, ks.nk, ks.ak, ks.s, ks.qw, ks.c);
     k_kforce<<<(v.nmove + kForceNT - 1) / kForceNT, kForceNT, ks.force_smem, c.stream>>>(v, d, ks.nrow, ks.row,
-                                                                                        ks.row_nlen, ks.c);
+                                                                                        ks.row_nlen, ks.c, ks.nk);
 }
 
 }  // namespace mdg
