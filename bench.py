@@ -1,0 +1,441 @@
+"""Benchmark of the md_sim GB300 hot path: ns/day of the MD step on one GPU.
+
+Default workload: the interfacial slab (2048 rigid SPC/E-type waters between two rocksalt walls
+of 1600 sites each, 42.1 x 42.1 x 84.2 A, rcut 10 A, kmax 10 / knmax 20, dt 1 fs), synthetic and
+seeded (no public dataset exists for this path).
+
+  value     ns/day of the resident MD step (move_predict, force_get, move_correct, SHAKE on the
+            device), inputs resident in HBM; each of the K timed steps is bracketed by CUDA events
+            on the library's stream and L2 is flushed (256 MB write) between steps.
+  e2e       ns/day through the drop-in C ABI (mdg_force_get [+ mdg_shake]) with pinned host
+            buffers: per step the positions go host->device and forces, torques and energies
+            come back; positions replay a trajectory recorded during warm-up (the caller's
+            integrator is not part of this library).
+  roofline  dominant phase of the step, from mdg_phase_times (CUDA events), against the peak
+            of its pipe.
+  cpu_baseline  the oracle (CPU restatement of the reference loops, OpenMP over all host
+            cores, -O2 -ffast-math) on a bounded sample of the same workload.
+
+--impl reference times that CPU implementation alone and prints its own line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ns/day on 1 GB300: mixed+learned vs plain FP64 GPU at ΔF_rms≤1e-5; %roofline"
+UNIT = "ns/day"
+
+
+def ns_per_day(sec_per_step, dt_fs=1.0):
+    return 86400.0 / sec_per_step * dt_fs * 1e-6
+
+
+# --------------------------------------------------------------------------------------------
+def make_workload(name):
+    from md_sim_gb300 import configs
+
+    if name == "slab2048":
+        s, prm = configs.slab_water()
+        desc = ("interfacial slab: 2048 rigid SPC/E-type waters between two rocksalt (001) walls "
+                "(3200 sites, q +-1.2 e, Buckingham wall-O), 42.1x42.1x84.2 A, EW3DC, alpha 0.30, "
+                "rcut 10 A, kmax 10/knmax 20 (4338 k), dt 1 fs")
+    elif name == "bulk256":
+        s, prm = configs.bulk_water()
+        desc = "bulk water: 256 rigid SPC/E-type waters, 19.73 A box, alpha 0.30, rcut 9, kmax 7 (775 k)"
+    elif name == "bulk32k":
+        s, prm = configs.large_bulk_water()
+        desc = ("large bulk water: 32768 rigid waters (98304 atoms), 99.3 A box, alpha 0.32, rcut 10, "
+                "kmax 24 (29038 k)")
+    elif name == "shake8k":
+        s, prm = configs.shake_water()
+        desc = ("8192 SHAKE-constrained 3-site waters on rocksalt walls (19x19 cells, 11552 sites), "
+                "tol 1e-10")
+    else:
+        raise SystemExit(f"unknown config {name}")
+    return s, prm, desc
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index=0):
+        self.rows = []
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "bf16_tflops": d.get("bf16_tflops", 1900.0),
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", 1700.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+# FP64 has no measured peak on this machine; the nominal GB300 dense FP64 rate is used for FP64 phases.
+FP64_NOMINAL_TFLOPS = 1.25
+
+
+def site_pairs(s, ctx, rcut):
+    """Accepted site pairs of one force evaluation: listed head pairs with head distance within rcut
+    (molecular cutoff, src/forcem.f90:299) times the site products; plus head-wall site terms."""
+    (li, lj), (wi, wj) = ctx.get_lists()
+    t = s.itype - 1
+    nsi = s.nsi[t]
+
+    def acc(i, j, wall):
+        i, j = i - 1, j - 1
+        dx = s.x0[i] - s.x0[j]
+        dy = s.y0[i] - s.y0[j]
+        dz = s.z0[i] - s.z0[j]
+        dx -= s.lx * np.round(dx / s.lx)
+        dy -= s.ly * np.round(dy / s.ly)
+        ok = dx * dx + dy * dy + dz * dz <= rcut * rcut
+        return int((nsi[i][ok] * (1 if wall else nsi[j][ok])).sum())
+
+    return acc(li, lj, False), acc(wi, wj, True) if len(wi) else 0
+
+
+def roofline(ctx, s, prm, precision, pk):
+    from md_sim_gb300.abi import MDG_MIXED
+
+    ph = ctx.phase_times(reps=5)
+    dom = max(("pairs", "walls", "reciprocal"), key=lambda k: ph[k])
+    nk = ctx_nk(s, prm)
+    hh, hw = site_pairs(s, ctx, prm.rcut)
+    if dom == "reciprocal":
+        units = s.nmove * nk
+        flops = 18.0 * units
+        if precision == MDG_MIXED:
+            bound, peak, unit = "tensor", pk["bf16_tflops"], "TFLOP/s"
+        else:
+            bound, peak, unit = "fp64", FP64_NOMINAL_TFLOPS, "TFLOP/s"
+    else:
+        units = hh if dom == "pairs" else hw
+        flops = 45.0 * units
+        bound, peak, unit = "fp64", FP64_NOMINAL_TFLOPS, "TFLOP/s"
+    t = ph[dom] * 1e-3
+    achieved = flops / t / 1e12
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get(f"{dom}:{'mixed' if precision == MDG_MIXED else 'fp64'}")
+    return {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak, "traffic": traffic, "kernel": dom, "ms_per_launch": ph[dom],
+            "units_per_launch": int(units), "flops_per_unit": flops / max(units, 1),
+            "peak_source": pk["source"] if bound == "tensor" else "nominal (no measured FP64 peak)",
+            "phase_ms": ph}
+
+
+def ctx_nk(s, prm):
+    """Number of k vectors of the reference selection (src/forcem.f90:743-776)."""
+    lmin = min(s.lx, s.ly, s.lz)
+    rk = float(np.float32(prm.kmax))
+    KL, KM, KN = (int(round(rk * L / lmin)) for L in (s.lx, s.ly, s.lz))
+    lim = np.float32(prm.kmax * prm.kmax) + np.float32(2.01)
+    n = 0
+    kmmin, knmin = 0, 1
+    for kl in range(KL + 1):
+        for km in range(kmmin, KM + 1):
+            for kn in range(knmin, KN + 1):
+                a = np.float32(kl * kl + km * km)
+                b = np.float32(kn * kn * prm.kmax * prm.kmax) / np.float32(KN * KN)
+                if np.float32(a + b) < lim:
+                    n += 1
+            knmin = -KN
+        kmmin = -KM
+    return n
+
+
+# --------------------------------------------------------------------------------------------
+def cpu_reference(s, prm, sample_steps, threads=None, target_s=10.0):
+    """CPU restatement of the reference (oracle, OpenMP) on a bounded sample: ns/day."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build as oracle_build
+
+    from md_sim_gb300 import abi
+
+    oracle_build.build()
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    lib = abi.Lib(oracle_build.path("libmdref_omp.so"), "ref_")
+    s2 = s.copy()
+    t0 = time.perf_counter()
+    ctx = abi.Context(lib, s2, prm)
+    ctx.set_state(s2)
+    t_init = time.perf_counter() - t0
+    ctx.run(1)  # first step includes lazy allocations
+    t0 = time.perf_counter()
+    ctx.run(sample_steps)
+    dt = (time.perf_counter() - t0) / sample_steps
+    # grow the sample to about target_s of CPU work
+    n = int(min(2000, max(0, target_s / max(dt, 1e-9) - sample_steps)))
+    if n > 0:
+        t0 = time.perf_counter()
+        ctx.run(n)
+        dt = (time.perf_counter() - t0) / n
+        sample_steps += n
+    return ns_per_day(dt, s.dt), dt, sample_steps
+
+
+def gpu_arm(args):
+    import torch
+
+    import md_sim_gb300
+    from md_sim_gb300 import abi, configs
+    from md_sim_gb300.abi import MDG_FP64, MDG_MIXED
+
+    lib = md_sim_gb300.load()
+    s, prm, desc = make_workload(args.config)
+    precision = MDG_MIXED if args.precision == "mixed" else MDG_FP64
+    prm.precision = precision
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # ---------------- resident MD step
+    ctx = abi.Context(lib, s, prm)
+    ctx.set_stream(stream.cuda_stream)
+    configs.equilibrate(ctx, s, steps=args.equil, every=20)
+    ctx.set_state(s)
+    ctx.run(args.warmup)
+    rep0 = ctx.run(1)
+    K = args.steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    torch.cuda.synchronize()
+    with ClockSampler() as clk:
+        with torch.cuda.stream(stream):
+            for k in range(K):
+                flush.zero_()
+                ev[k][0].record(stream)
+                ctx.run_async(1)
+                ev[k][1].record(stream)
+        stream.synchronize()
+    rep = ctx.check()
+    per_step = [a.elapsed_time(b) for a, b in ev]
+    t_step = float(np.sum(per_step)) / K * 1e-3
+    value = ns_per_day(t_step, s.dt)
+    kps = ctx.kernels_per_step()
+    ctx.get_state(s)
+    pk = peaks()
+    roof = roofline(ctx, s, prm, precision, pk)
+
+    # ---------------- e2e through the drop-in ABI with pinned host buffers
+    e2e = e2e_arm(lib, s, prm, args, torch)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if precision == MDG_FP64 else "f32+bf16x3 (f64 state)", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "precision": args.precision, "config": args.config,
+                   "l2": "flushed (256 MB write) between timed steps", "equilibration_steps": args.equil,
+                   "ensemble": "NVE" if s.temper == -1.0 else f"NVT {s.temper} K"},
+        "e2e": e2e,
+        "gpu_launches": int(kps * K),
+        "kernels_per_step": kps,
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "step_report": {k: rep[k] for k in ("tempnow", "htot", "uconf", "rebuilds", "steps")},
+        "step_ms_min_median_max": [min(per_step), float(np.median(per_step)), max(per_step)],
+    }
+    if args.cpu_baseline:
+        v, dt, n = cpu_reference(s, prm, args.cpu_steps)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"{n} MD steps of the same workload after one untimed step "
+                                         f"({dt * 1e3:.2f} ms/step), OpenMP over all host cores"}
+    return out
+
+
+def e2e_arm(lib, s, prm, args, torch):
+    from md_sim_gb300 import abi
+
+    K = min(args.steps, args.e2e_steps)
+    rec = abi.Context(lib, s.copy(), prm)
+    srec = s.copy()
+    rec.set_state(srec)
+    nm, nrig = s.nmove, max(s.nrig, 1)
+
+    def pinned(n):
+        return torch.zeros(n, dtype=torch.float64).pin_memory().numpy()
+
+    traj = []
+    for k in range(K):
+        rec.run(1)
+        rec.get_state(srec)
+        fr = {n: pinned(nm) for n in ("x", "y", "z", "rx", "ry", "rz")}
+        fr["x"][:], fr["y"][:], fr["z"][:] = srec.x0[:nm], srec.y0[:nm], srec.z0[:nm]
+        fr["rx"][:], fr["ry"][:], fr["rz"][:] = srec.rsx, srec.rsy, srec.rsz
+        for d, n in enumerate(("cx", "cy", "cz")):
+            fr[n] = pinned(nrig)
+            if s.nrig:
+                fr[n][:] = srec.c[0, d]
+        traj.append(fr)
+    rec.close()
+    # drop-in context created from the first frame
+    s0 = s.copy()
+    s0.x0[:nm], s0.y0[:nm], s0.z0[:nm] = traj[0]["x"], traj[0]["y"], traj[0]["z"]
+    if s.nrig:
+        s0.c[0] = np.stack([traj[0]["cx"], traj[0]["cy"], traj[0]["cz"]])
+    dctx = abi.Context(lib, s0, prm)
+    nflex = nm - s.nriga
+    outs = [pinned(max(nflex, 1)) for _ in range(3)] + [pinned(nrig) for _ in range(6)]
+    elj, eqq = pinned(s.nijt), pinned(s.nijt)
+    e = abi.Energies()
+    e.elj, e.eqq = abi._dp(elj), abi._dp(eqq)
+    import ctypes as C
+
+    dp = abi._dp
+    xold = [pinned(s.ntota - s.nliqa) for _ in range(3)]
+    for d, a in enumerate((s.xold, s.yold, s.zold)):
+        xold[d][:] = a[s.nliqa:]
+    kps = pinned(s.nit)
+    tk, sw = C.c_double(), C.c_int32()
+    shake = s.nmove > s.nliqa
+    h2d = 8 * (6 * nm + 3 * (s.nrig if s.nrig else 0)) + (8 * (3 * nflex + 3 * (s.ntota - s.nliqa)) if shake else 0)
+    d2h = 8 * (3 * nflex + 6 * s.nrig + 3 + 2 * s.nijt) + (8 * (3 * (s.nmove - s.nliqa) + 3 * (s.ntota - s.nliqa) + s.nit) if shake else 0)
+    times = []
+    for k in range(K):
+        fr = traj[k]
+        t0 = time.perf_counter()
+        rc = lib.force_get(dctx.h, dp(fr["x"]), dp(fr["y"]), dp(fr["z"]), dp(fr["cx"]), dp(fr["cy"]), dp(fr["cz"]),
+                           dp(fr["rx"]), dp(fr["ry"]), dp(fr["rz"]), *[dp(a) for a in outs], None, None, None,
+                           C.byref(e))
+        if rc == 0 and shake:
+            rc = lib.shake(dctx.h, dp(fr["x"]), dp(fr["y"]), dp(fr["z"]), dp(xold[0]), dp(xold[1]), dp(xold[2]),
+                           dp(outs[0]), dp(outs[1]), dp(outs[2]), dp(kps), C.byref(tk), C.byref(sw))
+        times.append(time.perf_counter() - t0)
+        if rc != 0:
+            raise RuntimeError(f"e2e step failed: {rc} {lib.last_error(dctx.h)}")
+    dctx.close()
+    t = float(np.mean(times[1:] if len(times) > 1 else times))
+    return {"value": ns_per_day(t, s.dt), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "path": "mdg_force_get" + (" + mdg_shake" if shake else "") + " with pinned host buffers",
+            "steps": K, "ms_per_step": t * 1e3}
+
+
+def reference_arm(args):
+    s, prm, desc = make_workload(args.config)
+    from md_sim_gb300.abi import MDG_FP64
+
+    prm.precision = MDG_FP64
+    samples, total = [], 0
+    for _ in range(max(1, min(args.steps, 3))):
+        v, dt, n = cpu_reference(s, prm, max(1, args.cpu_steps), target_s=20.0)
+        samples.append(dt)
+        total += n
+    t = float(np.mean(samples))
+    v = ns_per_day(t, s.dt)
+    steps = total // len(samples)
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": total,
+            "warmup": 1, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": desc, "config": args.config},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{len(samples)} x {steps} MD steps (CPU restatement of the reference "
+                                       "loops, OpenMP over all host cores; the Fortran reference has no "
+                                       "compiler here)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def profile_run(args):
+    """Minimal command for ncu: the steps run last, after create and two warm-up steps."""
+    import md_sim_gb300
+    from md_sim_gb300 import abi
+    from md_sim_gb300.abi import MDG_FP64, MDG_MIXED
+
+    lib = md_sim_gb300.load()
+    s, prm, desc = make_workload(args.config)
+    prm.precision = MDG_MIXED if args.precision == "mixed" else MDG_FP64
+    ctx = abi.Context(lib, s, prm)
+    ctx.set_state(s)
+    ctx.run(2)
+    ctx.run_async(args.steps)
+    rep = ctx.check()
+    print(json.dumps({"profile_steps": args.steps, "kernels_per_step": ctx.kernels_per_step(),
+                      "tempnow": rep["tempnow"]}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="slab2048", choices=["slab2048", "bulk256", "bulk32k", "shake8k"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--equil", type=int, default=200)
+    ap.add_argument("--e2e-steps", type=int, default=60)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: create, 2 warm-up steps, then --steps resident steps, no extras")
+    args = ap.parse_args()
+    if args.profile:
+        profile_run(args)
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(reference_arm(args)))
+        return
+    if args.gpus > 1 or int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        # replicas only: every rank runs its own system; rank 0 reports its own
+        pass
+    out = gpu_arm(args)
+    if rank == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -189,6 +189,72 @@ int mdg_shake(mdg_ctx* ctx, double* x0, double* y0, double* z0, double* xold, do
               double* zold, const double* ftx, const double* fty, const double* ftz, double* kps,
               double* tkps, int32_t* sweeps);
 
+/* ---------------------------------------------------------------------------------------------
+ * Resident mode: the whole MD step on the device.  The integrator that the reference keeps in
+ * Fortran (move_predict / move_correct, src/move.f90:48-383) runs as device kernels around the
+ * same force and SHAKE phases, so that many steps run without host traffic.
+ * ------------------------------------------------------------------------------------------- */
+
+/* Integrator state (src/config.f90:20-51 and the thermostat of src/config.f90:17), in time-step
+ * units as after config_init (src/config.f90:76-90).  Host arrays of the caller. */
+typedef struct mdg_state {
+    double *x0, *y0, *z0;          /* ntota positions */
+    double *xd[4], *yd[4], *zd[4]; /* ntota: x1..x4 etc. (atoms nriga+1..nliqa are integrated) */
+    double *cx[5], *cy[5], *cz[5]; /* nrig: cx0..cx4 */
+    double *q[4][5];               /* nrig: q[c][k] = q(c+1)k, i.e. q10..q14, q20..q24, ... */
+    double *wx[5], *wy[5], *wz[5]; /* nrig: body angular velocity and its derivatives */
+    double *xold, *yold, *zold;    /* ntota - nliqa */
+    double *rsx, *rsy, *rsz;       /* nmove site offsets */
+    double s[5], rs[5];            /* thermostat s0..s4, rs0..rs4 */
+} mdg_state;
+
+/* Rigid-water body and ensemble (src/sysdef.f90:443-452, src/main.f90:123-128). */
+typedef struct mdg_rigid {
+    double xbody[3], ybody[3], zbody[3]; /* site coordinates in the principal-axis frame */
+    double mw;                           /* water mass, internal units */
+    double inxx, inyy, inzz;             /* principal moments of inertia */
+    double temper;                       /* K; -1 selects NVE (src/move.f90:173) */
+} mdg_rigid;
+
+/* Scalars of the last step of mdg_run (the values prntout reports, src/main.f90:320-335). */
+typedef struct mdg_report {
+    double kp, kw, ke, htot, tempnow, uconf, tkps, press;
+    int64_t steps, rebuilds;
+    int32_t last_sweeps;
+} mdg_report;
+
+/* Uploads the full integrator state; the positions of frozen atoms are taken from mdg_create. */
+int mdg_set_state(mdg_ctx* ctx, const mdg_rigid* body, const mdg_state* st);
+
+/* Downloads the integrator state (for config_output / measure_do). */
+int mdg_get_state(mdg_ctx* ctx, mdg_state* st);
+
+/* Runs nsteps of move_predict -> force_get -> move_correct (-> move_shake when there are surface
+ * atoms), src/main.f90:58-68, entirely on the device.  rep may be NULL. */
+int mdg_run(mdg_ctx* ctx, int64_t nsteps, mdg_report* rep);
+
+/* Stream-ordered variant of mdg_run: queues nsteps on the context's stream and returns without
+ * waiting or checking.  mdg_check waits for the queued work and reports list overflow, SHAKE
+ * failures and non-finite energies of everything queued since the previous check (a list
+ * overflow is reported, not repaired: rerun the steps with mdg_run). */
+int mdg_run_async(mdg_ctx* ctx, int64_t nsteps);
+int mdg_check(mdg_ctx* ctx, mdg_report* rep);
+
+/* Kernel launches of one resident-mode step (counted in the captured step graph; 0 before the
+ * first mdg_run / mdg_run_async). */
+int64_t mdg_kernels_per_step(const mdg_ctx* ctx);
+
+/* Puts all work of the context on the caller's CUDA stream (a cudaStream_t; NULL restores the
+ * context's own stream), so that callers can order and time it with their own events. */
+int mdg_set_stream(mdg_ctx* ctx, void* stream);
+
+/* Phase timing: runs the force phases `reps` times on the current state (positions unchanged,
+ * list rebuilt every repetition) and writes the mean device time in ms of each phase:
+ * [0] list rebuild, [1] head-head pairs, [2] head-wall pairs, [3] reciprocal sum,
+ * [4] other force terms and force_sum, [5] integrator (resident mode, else 0), [6] SHAKE. */
+#define MDG_NPHASE 7
+int mdg_phase_times(mdg_ctx* ctx, int reps, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

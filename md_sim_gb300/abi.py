@@ -69,6 +69,25 @@ class Energies(C.Structure):
         "ewqWW")] + [("fwsx", C.c_double * 3), ("fwsy", C.c_double * 3), ("fwsz", C.c_double * 3)]
 
 
+class State(C.Structure):
+    _fields_ = [("x0", DP), ("y0", DP), ("z0", DP), ("xd", DP * 4), ("yd", DP * 4), ("zd", DP * 4),
+                ("cx", DP * 5), ("cy", DP * 5), ("cz", DP * 5), ("q", (DP * 5) * 4),
+                ("wx", DP * 5), ("wy", DP * 5), ("wz", DP * 5), ("xold", DP), ("yold", DP),
+                ("zold", DP), ("rsx", DP), ("rsy", DP), ("rsz", DP), ("s", C.c_double * 5),
+                ("rs", C.c_double * 5)]
+
+
+class Rigid(C.Structure):
+    _fields_ = [("xbody", C.c_double * 3), ("ybody", C.c_double * 3), ("zbody", C.c_double * 3),
+                ("mw", C.c_double), ("inxx", C.c_double), ("inyy", C.c_double), ("inzz", C.c_double),
+                ("temper", C.c_double)]
+
+
+class Report(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("kp", "kw", "ke", "htot", "tempnow", "uconf", "tkps", "press")] + [
+        ("steps", C.c_int64), ("rebuilds", C.c_int64), ("last_sweeps", C.c_int32)]
+
+
 @dataclasses.dataclass
 class RunParams:
     rcut: float
@@ -144,6 +163,17 @@ class Lib:
         g("get_lists", C.c_int, [C.c_void_p, I64P, I64P, C.c_int64, I64P, I64P, C.c_int64, I64P, I64P])
         g("force_get", C.c_int, [C.c_void_p] + [DP] * 21 + [C.POINTER(Energies)])
         g("shake", C.c_int, [C.c_void_p] + [DP] * 10 + [C.POINTER(C.c_double), C.POINTER(C.c_int32)])
+        if self.has("set_stream"):
+            g("set_stream", C.c_int, [C.c_void_p, C.c_void_p])
+            g("phase_times", C.c_int, [C.c_void_p, C.c_int, DP])
+        if self.has("run_async"):
+            g("run_async", C.c_int, [C.c_void_p, C.c_int64])
+            g("check", C.c_int, [C.c_void_p, C.POINTER(Report)])
+            g("kernels_per_step", C.c_int64, [C.c_void_p])
+        if self.has("run"):
+            g("set_state", C.c_int, [C.c_void_p, C.POINTER(Rigid), C.POINTER(State)])
+            g("get_state", C.c_int, [C.c_void_p, C.POINTER(State)])
+            g("run", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Report)])
 
     def fn(self, name, restype, argtypes):
         f = getattr(self.so, self.prefix + name)
@@ -263,3 +293,122 @@ class Context:
         s.xold[nl:], s.yold[nl:], s.zold[nl:] = xo, yo, zo
         self._check(rc)
         return {"kps": kps, "tkps": tk.value, "sweeps": sw.value}
+
+
+class _StateArrays:
+    """Contiguous copies of a System's integrator state, bound into an mdg_state struct."""
+
+    def __init__(self, s: System):
+        nl, nr = s.nliqa, max(s.nrig, 1)
+        c = np.ascontiguousarray
+        self.x = [c(s.x0), c(s.y0), c(s.z0)]
+        self.xd = [[c(s.xd[k, d]) for d in range(3)] for k in range(4)]
+        self.c = [[c(s.c[k, d]) if s.nrig else np.zeros(nr) for d in range(3)] for k in range(5)]
+        self.q = [[c(s.q[k, cc]) if s.nrig else np.zeros(nr) for k in range(5)] for cc in range(4)]
+        self.w = [[c(s.w[k, d]) if s.nrig else np.zeros(nr) for d in range(3)] for k in range(5)]
+        self.old = [c(s.xold[nl:]), c(s.yold[nl:]), c(s.zold[nl:])]
+        self.rs = [c(s.rsx), c(s.rsy), c(s.rsz)]
+        st = State()
+        st.x0, st.y0, st.z0 = (_dp(a) for a in self.x)
+        for k in range(4):
+            st.xd[k], st.yd[k], st.zd[k] = (_dp(a) for a in self.xd[k])
+        for k in range(5):
+            st.cx[k], st.cy[k], st.cz[k] = (_dp(a) for a in self.c[k])
+            st.wx[k], st.wy[k], st.wz[k] = (_dp(a) for a in self.w[k])
+            for cc in range(4):
+                st.q[cc][k] = _dp(self.q[cc][k])
+        st.xold, st.yold, st.zold = (_dp(a) for a in self.old)
+        st.rsx, st.rsy, st.rsz = (_dp(a) for a in self.rs)
+        for k in range(5):
+            st.s[k] = s.s[k]
+            st.rs[k] = s.rs[k]
+        self.st = st
+
+    def write_back(self, s: System):
+        nl = s.nliqa
+        s.x0[:], s.y0[:], s.z0[:] = self.x
+        for k in range(4):
+            for d in range(3):
+                s.xd[k, d] = self.xd[k][d]
+        if s.nrig:
+            for k in range(5):
+                for d in range(3):
+                    s.c[k, d] = self.c[k][d]
+                    s.w[k, d] = self.w[k][d]
+                for cc in range(4):
+                    s.q[k, cc] = self.q[cc][k]
+        s.xold[nl:], s.yold[nl:], s.zold[nl:] = self.old
+        s.rsx[:], s.rsy[:], s.rsz[:] = self.rs
+        s.s[:] = list(self.st.s)
+        s.rs[:] = list(self.st.rs)
+
+
+def rigid_of(s: System) -> Rigid:
+    r = Rigid()
+    for j in range(3):
+        r.xbody[j], r.ybody[j], r.zbody[j] = s.xbody[j], s.ybody[j], s.zbody[j]
+    r.mw, r.inxx, r.inyy, r.inzz = s.mw, s.inxx or 1.0, s.inyy or 1.0, s.inzz or 1.0
+    r.temper = s.temper
+    return r
+
+
+def _ctx_set_state(self, s: Optional[System] = None):
+    s = s or self.sys
+    self._state = _StateArrays(s)
+    self._rigid = rigid_of(s)
+    self._check(self.lib.set_state(self.h, C.byref(self._rigid), C.byref(self._state.st)))
+
+
+def _ctx_get_state(self, s: Optional[System] = None):
+    s = s or self.sys
+    arr = _StateArrays(s)
+    self._check(self.lib.get_state(self.h, C.byref(arr.st)))
+    arr.write_back(s)
+    return s
+
+
+def _ctx_run(self, nsteps: int) -> Dict[str, float]:
+    rep = Report()
+    self._check(self.lib.run(self.h, int(nsteps), C.byref(rep)))
+    return {f: getattr(rep, f) for f, _ in Report._fields_}
+
+
+Context.set_state = _ctx_set_state
+Context.get_state = _ctx_get_state
+Context.run = _ctx_run
+
+
+PHASES = ("list", "pairs", "walls", "reciprocal", "other", "integrator", "shake")
+
+
+def _ctx_set_stream(self, stream_handle: int):
+    self._check(self.lib.set_stream(self.h, C.c_void_p(stream_handle)))
+
+
+def _ctx_phase_times(self, reps: int = 5) -> Dict[str, float]:
+    out = np.zeros(len(PHASES))
+    self._check(self.lib.phase_times(self.h, int(reps), _dp(out)))
+    return dict(zip(PHASES, out.tolist()))
+
+
+Context.set_stream = _ctx_set_stream
+Context.phase_times = _ctx_phase_times
+
+
+def _ctx_run_async(self, nsteps: int):
+    self._check(self.lib.run_async(self.h, int(nsteps)))
+
+
+def _ctx_check(self) -> Dict[str, float]:
+    rep = Report()
+    self._check(self.lib.check(self.h, C.byref(rep)))
+    return {f: getattr(rep, f) for f, _ in Report._fields_}
+
+
+def _ctx_kernels_per_step(self) -> int:
+    return int(self.lib.kernels_per_step(self.h))
+
+
+Context.run_async = _ctx_run_async
+Context.check = _ctx_check
+Context.kernels_per_step = _ctx_kernels_per_step

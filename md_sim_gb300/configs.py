@@ -202,8 +202,9 @@ def _place_waters(rng, nwat, L, zlo, zhi, walls, dmin_oo=2.5, dmin_ow=2.2, max_t
 
 def slab_water(nwat: int = 2048, cells: int = 10, a: float = 4.21, lz: Optional[float] = None,
                seed: int = 4, T: float = 300.0, rcut: float = 10.0, skin: float = 1.0,
-               alpha: float = 0.30, kmax: int = 10) -> Tuple[S.System, RunParams]:
-    """Rigid waters between two rocksalt walls (4 layers, q +-1.2, Buckingham wall-O)."""
+               alpha: float = 0.30, kmax: int = 10, nvt: bool = False) -> Tuple[S.System, RunParams]:
+    """Rigid waters between two rocksalt walls (4 layers, q +-1.2, Buckingham wall-O).
+    NVE by default (T sets the initial velocities); nvt=True selects the reference's thermostat."""
     L = cells * a
     dens = 0.033427  # molecules / A^3 at 1 g/cm^3
     thick = nwat / (L * L * dens)
@@ -226,7 +227,7 @@ def slab_water(nwat: int = 2048, cells: int = 10, a: float = 4.21, lz: Optional[
     s.q[0] = _random_quaternions(np.random.default_rng(seed + 100), nwat)
     s.set_walls(wtyp, wpos)
     _rigid_velocities(s, T, seed + 200, seed + 300)
-    s.temper = T
+    s.temper = T if nvt else -1.0
     prm = RunParams(rcut=rcut, skin=skin, kmax=kmax, alpha=alpha, variant=MDG_SLAB)
     return _finish(s), prm
 
@@ -295,10 +296,50 @@ def shake_water(nwat: int = 8192, cells: int = 19, a: float = 4.21, seed: int = 
     nl = s.nliqa
     s.xold[nm:], s.yold[nm:], s.zold[nm:] = s.x0[nm:], s.y0[nm:], s.z0[nm:]
     del nl
-    s.temper = T
+    # surface molecules are integrated by the Verlet step of move_shake whatever the ensemble; the
+    # thermostat of move_predict has no rigid or free atoms to act on here, so NVE is used
+    s.temper = -1.0
     kmax = kmax if kmax is not None else int(round(10 * L / 42.1))
     prm = RunParams(rcut=rcut, skin=skin, kmax=kmax, alpha=alpha, variant=MDG_SLAB,
                     shake_tol2=tol2, shake_maxit=maxit,
                     quirks=1 if clean else 0)
     s.config_init()
     return s, prm
+
+
+def rescale_velocities(s: S.System, T: float) -> float:
+    """Scales the velocity-like Gear derivatives of the rigid molecules and ions to temperature T
+    (kinetic energy as in move_predict: ke = kp + kw, tempnow = ke*1000/(3 R (nfree + 2 nrig)),
+    src/move.f90:69-102,379).  Returns the factor applied."""
+    kp = float((s.mi[s.nriga:s.nliqa] * (s.xd[0, :, s.nriga:s.nliqa] ** 2).sum(0)).sum())
+    if s.nrig:
+        kp += s.mw * float((s.c[1] ** 2).sum())
+        kw = s.inxx * float((s.w[0, 0] ** 2).sum()) + s.inyy * float((s.w[0, 1] ** 2).sum()) + \
+            s.inzz * float((s.w[0, 2] ** 2).sum())
+    else:
+        kw = 0.0
+    ndf = (s.nliqa - s.nriga) + 2 * s.nrig
+    if ndf == 0 or kp + kw <= 0:
+        return 1.0
+    tnow = (kp + kw) * 1000.0 / (3.0 * S.PH_R * ndf)
+    lam = math.sqrt(T / tnow)
+    s.xd[:, :, s.nriga:s.nliqa] *= lam
+    if s.nrig:
+        s.c[1:] *= lam
+        s.w *= lam
+        s.q[1:] *= lam
+    return lam
+
+
+def equilibrate(ctx, s: S.System, steps: int = 400, T: float = 300.0, every: int = 20) -> S.System:
+    """Short MD with velocity rescaling every `every` steps through a resident-mode context
+    (GPU or oracle), to take the synthetic lattice/placement starts to a stable state."""
+    ctx.set_state(s)
+    done = 0
+    while done < steps:
+        ctx.run(every)
+        ctx.get_state(s)
+        rescale_velocities(s, T)
+        ctx.set_state(s)
+        done += every
+    return s

@@ -18,7 +18,7 @@ enum StatusWord {
     ST_WLIST_OVF = 1,  // head-wall list overflow
     ST_SHAKE_MAXIT = 2,
     ST_SHAKE_RPTOL = 3,  // 1 + first failing constraint (molecule * 8 + is)
-    ST_CELL_OVF = 4,
+    ST_FORCE_RB = 4,   // host request: rebuild the list at the next trigger
     ST_REBUILD = 5,    // 1 when the current step rebuilt the list
     ST_SWEEPS = 6,     // SHAKE sweeps of the last call
     ST_OOB = 7,        // debug builds: tag of the first out-of-range index seen

@@ -23,6 +23,24 @@ enum AccSlot {
     ACC_NSLOT = ACC_FWS0 + 3
 };
 
+// Thermostat and step scalars of the resident mode (device array c.d_thermo).
+enum ThermoSlot {
+    TH_S = 0,      // s0..s4
+    TH_RS = 5,     // rs0..rs4
+    TH_KP = 10,
+    TH_KW,
+    TH_KE,
+    TH_HTOT,
+    TH_SFT,
+    TH_SFR,
+    TH_UCONF,
+    TH_TEMPNOW,
+    TH_PRESS,
+    TH_STEPS,
+    TH_REBUILDS,
+    TH_N = 24
+};
+
 // Plain view of the device arrays, passed to kernels by value.
 struct View {
     int nrig, nriga, nliqa, nmove, nwall, ntota, nit, nijt, nltype, nheads;
@@ -93,6 +111,7 @@ struct Ctx {
     Grid grid{}, wgrid{};
     KSet ks;
     cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;  // the context's stream while a caller's stream is in use
     int device = 0;
     int precision = MDG_FP64;
     int variant = MDG_SLAB;
@@ -128,6 +147,16 @@ struct Ctx {
     double *d_ft = nullptr, *d_fc = nullptr, *d_tq = nullptr;  // force_sum outputs
     bool alloc_failed = false;
     bool debug_sync = false;
+    // resident mode
+    bool resident = false;
+    mdg_rigid body{};
+    double *d_xd = nullptr, *d_c = nullptr, *d_q = nullptr, *d_w = nullptr, *d_a = nullptr;
+    double *d_thermo = nullptr, *d_isum = nullptr;
+    std::vector<std::pair<void*, size_t>> snap_regions;
+    char* d_snap = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_steps = 0;
+    int64_t kernels_per_step = 0;
     // host staging (pinned)
     double* h_acc = nullptr;
     int* h_status = nullptr;
@@ -155,7 +184,11 @@ void angle_forces(Ctx& c);
 void force_sum(Ctx& c, double* d_ft, double* d_fc, double* d_tq);
 // shake.cu
 int shake_setup(Ctx& c, const mdg_sysdesc* s);
-void shake_launch(Ctx& c);
+void shake_launch(Ctx& c, const double* d_ft);
+// integrate.cu
+void predict_launch(Ctx& c);
+void correct_launch(Ctx& c);
+void thermo_finish_launch(Ctx& c);
 
 int set_err(Ctx* c, int code, const std::string& msg);
 void* dalloc(Ctx& c, size_t bytes);

@@ -1,0 +1,342 @@
+// integrate.cu - the MD step around the force phases, on the device (resident mode).
+//
+//   k_pred_ions / k_pred_rigid / k_thermo_pred   move_predict, src/move.f90:48-217: 5-value Gear
+//       predictor for ions, centres of mass, angular velocities and quaternions; quaternion
+//       normalisation, rotation matrix, site rebuild and the H offsets rsx (:148-162); kinetic
+//       energies, Nose-like thermostat predictor, htot, sft/sfr.
+//   k_uconf                                       uconf and press of force_sum (:1055,1079,1081)
+//   k_corr_ions / k_corr_rigid / k_thermo_corr   move_correct, src/move.f90:220-383.
+//
+// One thread per atom or molecule; kinetic sums go through block reductions into a small
+// accumulator array.  Gear coefficients are the reference's single-precision literals.
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+#include "ctx.h"
+
+namespace mdg {
+
+namespace {
+
+constexpr int kNT = 256;
+
+constexpr double Gf01 = F32D(0.348611111), Gf11 = 1.0, Gf21 = F32D(0.916666667), Gf31 = F32D(0.333333333),
+                 Gf41 = F32D(0.041666667);
+constexpr double Gf02 = F32D(0.158300000), Gf12 = F32D(0.757000000), Gf22 = 1.0, Gf32 = 0.5,
+                 Gf42 = F32D(0.083333333);
+
+__device__ __forceinline__ void gpred(double& a0, double& a1, double& a2, double& a3, double a4) {
+    a0 = a0 + a1 + a2 + a3 + a4;
+    a1 = a1 + 2 * a2 + 3 * a3 + 4 * a4;
+    a2 = a2 + 3 * a3 + 6 * a4;
+    a3 = a3 + 4 * a4;
+}
+
+struct Dyn {
+    double* xd;     // [4][3][nion]
+    double* c;      // [5][3][nrig]
+    double* q;      // [4][5][nrig]
+    double* w;      // [5][3][nrig]
+    double* a;      // [9][nrig]
+    double* th;     // thermostat + scalars
+    double* isum;   // kinetic partial sums
+    const double* ft;  // 3 x nflex
+    const double* fc;  // 3 x nrig
+    const double* tq;  // 3 x nrig
+    mdg_rigid body;
+    int nion;
+};
+
+__global__ void k_pred_ions(View v, Dyn D) {
+    double kp = 0.0;
+    const int n = D.nion;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = v.nriga + k;
+        double* X[3] = {v.x, v.y, v.z};
+        double s2 = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            double* x1 = D.xd + (0 * 3 + d) * n;
+            double* x2 = D.xd + (1 * 3 + d) * n;
+            double* x3 = D.xd + (2 * 3 + d) * n;
+            double* x4 = D.xd + (3 * 3 + d) * n;
+            double a0 = X[d][i], a1 = x1[k], a2 = x2[k], a3 = x3[k];
+            gpred(a0, a1, a2, a3, x4[k]);
+            X[d][i] = a0;
+            x1[k] = a1;
+            x2[k] = a2;
+            x3[k] = a3;
+            s2 += a1 * a1;
+        }
+        kp += v.mi[i] * s2;
+    }
+    block_atomic_sum<kNT>(kp, &D.isum[0]);
+}
+
+__global__ void k_pred_rigid(View v, Dyn D) {
+    double sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
+    const int nr = v.nrig;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += gridDim.x * blockDim.x) {
+        double cx[3];
+        for (int d = 0; d < 3; ++d) {
+            double a0 = D.c[(0 * 3 + d) * nr + i], a1 = D.c[(1 * 3 + d) * nr + i], a2 = D.c[(2 * 3 + d) * nr + i],
+                   a3 = D.c[(3 * 3 + d) * nr + i];
+            gpred(a0, a1, a2, a3, D.c[(4 * 3 + d) * nr + i]);
+            D.c[(0 * 3 + d) * nr + i] = a0;
+            D.c[(1 * 3 + d) * nr + i] = a1;
+            D.c[(2 * 3 + d) * nr + i] = a2;
+            D.c[(3 * 3 + d) * nr + i] = a3;
+            sc[d] += a1 * a1;
+            cx[d] = a0;
+        }
+        for (int d = 0; d < 3; ++d) {
+            double a0 = D.w[(0 * 3 + d) * nr + i], a1 = D.w[(1 * 3 + d) * nr + i], a2 = D.w[(2 * 3 + d) * nr + i],
+                   a3 = D.w[(3 * 3 + d) * nr + i];
+            gpred(a0, a1, a2, a3, D.w[(4 * 3 + d) * nr + i]);
+            D.w[(0 * 3 + d) * nr + i] = a0;
+            D.w[(1 * 3 + d) * nr + i] = a1;
+            D.w[(2 * 3 + d) * nr + i] = a2;
+            D.w[(3 * 3 + d) * nr + i] = a3;
+            sw[d] += a0 * a0;
+        }
+        double qq[4];
+        for (int cc = 0; cc < 4; ++cc) {
+            double* b = D.q + (cc * 5) * nr;
+            double a0 = b[i], a1 = b[nr + i], a2 = b[2 * nr + i], a3 = b[3 * nr + i];
+            gpred(a0, a1, a2, a3, b[4 * nr + i]);
+            b[nr + i] = a1;
+            b[2 * nr + i] = a2;
+            b[3 * nr + i] = a3;
+            qq[cc] = a0;
+        }
+        const double cr = 1.0 / sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
+        const double q1 = qq[0] * cr, q2 = qq[1] * cr, q3 = qq[2] * cr, q4 = qq[3] * cr;
+        D.q[(0 * 5) * nr + i] = q1;
+        D.q[(1 * 5) * nr + i] = q2;
+        D.q[(2 * 5) * nr + i] = q3;
+        D.q[(3 * 5) * nr + i] = q4;
+        double a[9];
+        a[0] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
+        a[1] = 2.0 * (q3 * q4 - q1 * q2);
+        a[2] = 2.0 * (q2 * q3 + q1 * q4);
+        a[3] = -2.0 * (q1 * q2 + q3 * q4);
+        a[4] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4;
+        a[5] = 2.0 * (q2 * q4 - q1 * q3);
+        a[6] = 2.0 * (q2 * q3 - q1 * q4);
+        a[7] = -2.0 * (q1 * q3 + q4 * q2);
+        a[8] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
+        for (int k = 0; k < 9; ++k) D.a[k * nr + i] = a[k];
+        const int ix = 3 * i;
+        double sx[3], sy[3], sz[3];
+        for (int j = 0; j < 3; ++j) {
+            sx[j] = cx[0] + a[0] * D.body.xbody[j] + a[3] * D.body.ybody[j] + a[6] * D.body.zbody[j];
+            sy[j] = cx[1] + a[1] * D.body.xbody[j] + a[4] * D.body.ybody[j] + a[7] * D.body.zbody[j];
+            sz[j] = cx[2] + a[2] * D.body.xbody[j] + a[5] * D.body.ybody[j] + a[8] * D.body.zbody[j];
+            v.x[ix + j] = sx[j];
+            v.y[ix + j] = sy[j];
+            v.z[ix + j] = sz[j];
+        }
+        for (int j = 1; j < 3; ++j) {
+            v.rsx[ix + j] = sx[j] - sx[0];
+            v.rsy[ix + j] = sy[j] - sy[0];
+            v.rsz[ix + j] = sz[j] - sz[0];
+        }
+    }
+    for (int d = 0; d < 3; ++d) block_atomic_sum<kNT>(sc[d], &D.isum[1 + d]);
+    for (int d = 0; d < 3; ++d) block_atomic_sum<kNT>(sw[d], &D.isum[4 + d]);
+}
+
+__global__ void k_thermo_pred(View v, Dyn D) {
+    double* th = D.th;
+    const mdg_rigid& b = D.body;
+    const double kp = D.isum[0] + b.mw * (D.isum[1] + D.isum[2] + D.isum[3]);
+    const double kw = b.inxx * D.isum[4] + b.inyy * D.isum[5] + b.inzz * D.isum[6];
+    double* s = th + TH_S;
+    double* rs = th + TH_RS;
+    if (b.temper == -1.0) {
+        s[0] = s[1] = rs[0] = rs[1] = 0.0;
+    } else {
+        gpred(s[0], s[1], s[2], s[3], s[4]);
+        gpred(rs[0], rs[1], rs[2], rs[3], rs[4]);
+    }
+    const long nfree = v.nliqa - v.nriga;
+    const double tstar = F32D(8.31441) * b.temper / 1000.0;
+    double qmass = (double)(float)(3 * (nfree + v.nrig)) * tstar * F32D(2e3);
+    double rmass = (double)(float)(3 * v.nrig) * tstar * F32D(1e3);
+    qmass = qmass / 10.0;
+    rmass = rmass / 10.0;
+    th[TH_KP] = kp;
+    th[TH_KW] = kw;
+    th[TH_KE] = kp + kw;
+    th[TH_HTOT] = 0.5 * (kp + kw + qmass * s[0] * s[0] + rmass * rs[0] * rs[0]) + th[TH_UCONF];
+    th[TH_SFT] = (kp - (double)(float)(3 * (nfree + v.nrig) - 2) * tstar) / qmass;
+    th[TH_SFR] = (kw - (double)(float)(3 * v.nrig + 1) * tstar) / rmass;
+}
+
+// uconf = sum(elj) + sum(eqq) + uewa + urf (src/forcem.f90:1055,1079) and the wall pressure.
+__global__ void k_uconf(View v, Dyn D, int slab) {
+    if (threadIdx.x != 0) return;
+    const double* a = v.acc;
+    const double* sl = a + 2 * v.nijt;
+    double slj = 0.0, sqq = 0.0;
+    for (int k = 0; k < v.nijt; ++k) {
+        slj += a[k];
+        sqq += a[v.nijt + k];
+    }
+    double urf = 0.0;
+    if (slab) {
+        const double crf = -2.0 * F32D(3.1415926535898) * v.lzi * v.lxi * v.lyi;
+        urf = -crf * v.facq * sl[ACC_DIPZ] * sl[ACC_DIPZ];
+    }
+    D.th[TH_UCONF] = slj + sqq + 0.5 * sl[ACC_UEWA] + urf;
+    D.th[TH_PRESS] = (sl[ACC_FWS + 8] - sl[ACC_FWS + 6]) / (2.0 * v.lx * v.ly) * 1000.0 /
+                     (F32D(6.022045e23) * F32D(1e-30)) * F32D(1e-5);
+}
+
+__global__ void k_corr_ions(View v, Dyn D) {
+    const int n = D.nion;
+    const double s0i = D.th[TH_S];
+    const int nflex = v.nmove - v.nriga;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = v.nriga + k;
+        double* X[3] = {v.x, v.y, v.z};
+        for (int d = 0; d < 3; ++d) {
+            double* x1 = D.xd + (0 * 3 + d) * n;
+            double* x2 = D.xd + (1 * 3 + d) * n;
+            double* x3 = D.xd + (2 * 3 + d) * n;
+            double* x4 = D.xd + (3 * 3 + d) * n;
+            const double cort = 0.5 * D.ft[d * nflex + k] * v.mii[i] - x1[k] * s0i - x2[k];
+            X[d][i] = X[d][i] + Gf02 * cort;
+            x1[k] = x1[k] + Gf12 * cort;
+            x2[k] = x2[k] + Gf22 * cort;
+            x3[k] = x3[k] + Gf32 * cort;
+            x4[k] = x4[k] + Gf42 * cort;
+        }
+    }
+}
+
+__global__ void k_corr_rigid(View v, Dyn D) {
+    const int nr = v.nrig;
+    const double s0i = D.th[TH_S], rs0i = D.th[TH_RS];
+    const mdg_rigid& b = D.body;
+    const double rcorr = 0.5 / b.mw;
+    const double inxxi = 1.0 / b.inxx, inyyi = 1.0 / b.inyy, inzzi = 1.0 / b.inzz;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += gridDim.x * blockDim.x) {
+        for (int d = 0; d < 3; ++d) {
+            double* c0 = D.c + (0 * 3 + d) * nr;
+            double* c1 = D.c + (1 * 3 + d) * nr;
+            double* c2 = D.c + (2 * 3 + d) * nr;
+            double* c3 = D.c + (3 * 3 + d) * nr;
+            double* c4 = D.c + (4 * 3 + d) * nr;
+            const double co = rcorr * D.fc[d * nr + i] - c1[i] * s0i - c2[i];
+            c0[i] = c0[i] + Gf02 * co;
+            c1[i] = c1[i] + Gf12 * co;
+            c2[i] = c2[i] + Gf22 * co;
+            c3[i] = c3[i] + Gf32 * co;
+            c4[i] = c4[i] + Gf42 * co;
+        }
+        const double q1 = D.q[0 * 5 * nr + i], q2 = D.q[1 * 5 * nr + i], q3 = D.q[2 * 5 * nr + i],
+                     q4 = D.q[3 * 5 * nr + i];
+        const double wx = D.w[0 * nr + i], wy = D.w[1 * nr + i], wz = D.w[2 * nr + i];
+        double cq[4];
+        cq[0] = 0.5 * (-q3 * wx - q4 * wy + q2 * wz);
+        cq[1] = 0.5 * (q4 * wx - q3 * wy - q1 * wz);
+        cq[2] = 0.5 * (q1 * wx + q2 * wy + q4 * wz);
+        cq[3] = 0.5 * (-q2 * wx + q1 * wy - q3 * wz);
+        for (int cc = 0; cc < 4; ++cc) {
+            double* bq = D.q + (cc * 5) * nr;
+            const double co = cq[cc] - bq[nr + i];
+            bq[i] = bq[i] + Gf01 * co;
+            bq[nr + i] = bq[nr + i] + Gf11 * co;
+            bq[2 * nr + i] = bq[2 * nr + i] + Gf21 * co;
+            bq[3 * nr + i] = bq[3 * nr + i] + Gf31 * co;
+            bq[4 * nr + i] = bq[4 * nr + i] + Gf41 * co;
+        }
+        double a[9];
+        for (int k = 0; k < 9; ++k) a[k] = D.a[k * nr + i];
+        const double tx = D.tq[i], ty = D.tq[nr + i], tz = D.tq[2 * nr + i];
+        double c1 = a[0] * tx + a[1] * ty + a[2] * tz;
+        c1 = ((c1 * 1.0 + wy * wz * (b.inyy - b.inzz)) * inxxi) - D.w[(1 * 3 + 0) * nr + i] - rs0i * wx;
+        double c2 = a[3] * tx + a[4] * ty + a[5] * tz;
+        c2 = ((c2 * 1.0 + wz * wx * (b.inzz - b.inxx)) * inyyi) - D.w[(1 * 3 + 1) * nr + i] - rs0i * wy;
+        double c3 = a[6] * tx + a[7] * ty + a[8] * tz;
+        c3 = ((c3 * 1.0 + wx * wy * (b.inxx - b.inyy)) * inzzi) - D.w[(1 * 3 + 2) * nr + i] - rs0i * wz;
+        const double cw[3] = {c1, c2, c3};
+        for (int d = 0; d < 3; ++d) {
+            D.w[(0 * 3 + d) * nr + i] += Gf01 * cw[d];
+            D.w[(1 * 3 + d) * nr + i] += Gf11 * cw[d];
+            D.w[(2 * 3 + d) * nr + i] += Gf21 * cw[d];
+            D.w[(3 * 3 + d) * nr + i] += Gf31 * cw[d];
+            D.w[(4 * 3 + d) * nr + i] += Gf41 * cw[d];
+        }
+    }
+}
+
+__global__ void k_thermo_corr(View v, Dyn D) {
+    double* th = D.th;
+    if (D.body.temper != -1.0) {
+        double* s = th + TH_S;
+        double* rs = th + TH_RS;
+        double rc = th[TH_SFT] - s[1];
+        s[0] = s[0] + Gf01 * rc;
+        s[1] = th[TH_SFT];
+        s[2] = s[2] + Gf21 * rc;
+        s[3] = s[3] + Gf31 * rc;
+        s[4] = s[4] + Gf41 * rc;
+        rc = th[TH_SFR] - rs[1];
+        rs[0] = rs[0] + Gf01 * rc;
+        rs[1] = th[TH_SFR];
+        rs[2] = rs[2] + Gf21 * rc;
+        rs[3] = rs[3] + Gf31 * rc;
+        rs[4] = rs[4] + Gf41 * rc;
+    }
+    const long nfree = v.nliqa - v.nriga;
+    th[TH_TEMPNOW] = th[TH_KE] * 1000.0 / (3.0 * F32D(8.31441) * (double)(float)(nfree + 2 * v.nrig));
+    th[TH_STEPS] += 1.0;
+    if (v.status[ST_REBUILD]) th[TH_REBUILDS] += 1.0;
+}
+
+Dyn dyn_of(Ctx& c) {
+    Dyn D;
+    D.xd = c.d_xd;
+    D.c = c.d_c;
+    D.q = c.d_q;
+    D.w = c.d_w;
+    D.a = c.d_a;
+    D.th = c.d_thermo;
+    D.isum = c.d_isum;
+    D.ft = c.d_ft;
+    D.fc = c.d_fc;
+    D.tq = c.d_tq;
+    D.body = c.body;
+    D.nion = c.v.nliqa - c.v.nriga;
+    return D;
+}
+
+int nblk(int n) { return std::max(1, std::min((n + kNT - 1) / kNT, 152 * 4)); }
+
+}  // namespace
+
+void predict_launch(Ctx& c) {
+    const View& v = c.v;
+    Dyn D = dyn_of(c);
+    cudaMemsetAsync(c.d_isum, 0, sizeof(double) * 8, c.stream);
+    if (D.nion > 0) k_pred_ions<<<nblk(D.nion), kNT, 0, c.stream>>>(v, D);
+    if (v.nrig > 0) k_pred_rigid<<<nblk(v.nrig), kNT, 0, c.stream>>>(v, D);
+    k_thermo_pred<<<1, 1, 0, c.stream>>>(v, D);
+}
+
+void correct_launch(Ctx& c) {
+    const View& v = c.v;
+    Dyn D = dyn_of(c);
+    k_uconf<<<1, 32, 0, c.stream>>>(v, D, c.variant == MDG_SLAB ? 1 : 0);
+    if (D.nion > 0) k_corr_ions<<<nblk(D.nion), kNT, 0, c.stream>>>(v, D);
+    if (v.nrig > 0) k_corr_rigid<<<nblk(v.nrig), kNT, 0, c.stream>>>(v, D);
+}
+
+void thermo_finish_launch(Ctx& c) {
+    Dyn D = dyn_of(c);
+    k_thermo_corr<<<1, 1, 0, c.stream>>>(c.v, D);
+}
+
+}  // namespace mdg

@@ -161,6 +161,10 @@ double self_energy(const mdg_sysdesc* s, const double* x0, const double* y0, con
 
 int alloc_lists(Ctx& c, int maxnb, int maxwnb) {
     View& v = c.v;
+    if (c.graph_exec) {
+        cudaGraphExecDestroy(c.graph_exec);
+        c.graph_exec = nullptr;
+    }
     dfree(c, v.nb);
     dfree(c, v.wnb);
     v.maxnb = std::max(maxnb, 8);
@@ -207,26 +211,34 @@ int phase_check(Ctx& c, const char* name) {
         if (prc_) return prc_;              \
     } while (0)
 
-// Runs the force phases on device-resident positions.  Returns MDG_OK or an error.
+// Queues the force phases on device-resident positions (no synchronisation).
+int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
+    View& v = c.v;
+    cudaMemsetAsync(v.fx, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+    cudaMemsetAsync(v.fy, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+    cudaMemsetAsync(v.fz, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+    cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
+    if (reset_status) cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
+    PHASE(nnlist_trigger(c, force_rebuild), "trigger");
+    PHASE(nnlist_build(c), "nnlist");
+    PHASE(pair_forces_fp64(c), "pairs");
+    PHASE(surf_partition(c), "surf_partition");
+    PHASE(wall_forces_fp64(c), "walls");
+    PHASE(lr_tail(c), "lr_tail");
+    PHASE(recip_fp64(c), "reciprocal");
+    PHASE(dipole_correction(c), "dipole");
+    PHASE(angle_forces(c), "angles");
+    PHASE(force_sum(c, c.d_ft, c.d_fc, c.d_tq), "force_sum");
+    return MDG_OK;
+}
+
+// Runs the force phases and checks the list capacity; regrows and redoes on overflow.
 int run_force(Ctx& c, bool force_rebuild) {
     View& v = c.v;
     for (int attempt = 0; attempt < 4; ++attempt) {
-        cudaMemsetAsync(v.fx, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
-        cudaMemsetAsync(v.fy, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
-        cudaMemsetAsync(v.fz, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
-        cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
-        cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
-        PHASE(nnlist_trigger(c, force_rebuild || attempt > 0), "trigger");
-        PHASE(nnlist_build(c), "nnlist");
-        PHASE(pair_forces_fp64(c), "pairs");
-        PHASE(surf_partition(c), "surf_partition");
-        PHASE(wall_forces_fp64(c), "walls");
-        PHASE(lr_tail(c), "lr_tail");
-        PHASE(recip_fp64(c), "reciprocal");
-        PHASE(dipole_correction(c), "dipole");
-        PHASE(angle_forces(c), "angles");
-        PHASE(force_sum(c, c.d_ft, c.d_fc, c.d_tq), "force_sum");
-        int rc = read_status(c);
+        int rc = launch_force(c, force_rebuild || attempt > 0, true);
+        if (rc) return rc;
+        rc = read_status(c);
         if (rc) return rc;
         const int ovf = c.h_status[ST_LIST_OVF], wovf = c.h_status[ST_WLIST_OVF];
         if (!ovf && !wovf) return MDG_OK;
@@ -254,9 +266,11 @@ void mdg_destroy(mdg_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (void* p : c->owned)
         if (p) cudaFree(p);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     if (c->h_acc) cudaFreeHost(c->h_acc);
     if (c->h_status) cudaFreeHost(c->h_status);
-    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    else if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
 
@@ -696,7 +710,7 @@ int mdg_shake(mdg_ctx* cp, double* x0, double* y0, double* z0, double* xold, dou
     MDG_CUDA(cudaMemcpyAsync(c.d_ft_in + nflex, fty, sizeof(double) * nflex, cudaMemcpyHostToDevice, c.stream));
     MDG_CUDA(cudaMemcpyAsync(c.d_ft_in + 2 * nflex, ftz, sizeof(double) * nflex, cudaMemcpyHostToDevice, c.stream));
     cudaMemsetAsync(v.status + ST_SHAKE_MAXIT, 0, sizeof(int) * 2, c.stream);
-    shake_launch(c);
+    shake_launch(c, c.d_ft_in);
     MDG_CUDA(cudaMemcpyAsync(x0 + nl, v.x + nl, sizeof(double) * ns, cudaMemcpyDeviceToHost, c.stream));
     MDG_CUDA(cudaMemcpyAsync(y0 + nl, v.y + nl, sizeof(double) * ns, cudaMemcpyDeviceToHost, c.stream));
     MDG_CUDA(cudaMemcpyAsync(z0 + nl, v.z + nl, sizeof(double) * ns, cudaMemcpyDeviceToHost, c.stream));
@@ -724,6 +738,361 @@ int mdg_shake(mdg_ctx* cp, double* x0, double* y0, double* z0, double* xold, dou
     }
     if (c.ncons > 0 && !sw[1]) return set_err(&c, MDG_E_SHAKE_MAXIT, "shake(): Too many constraint iterations!");
     return MDG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Resident mode
+// ---------------------------------------------------------------------------------------------
+static int resident_alloc(Ctx& c) {
+    if (c.d_thermo) return MDG_OK;
+    View& v = c.v;
+    const int nion = std::max(v.nliqa - v.nriga, 1), nr = std::max(v.nrig, 1);
+    c.d_xd = (double*)dalloc(c, sizeof(double) * 12 * nion);
+    c.d_c = (double*)dalloc(c, sizeof(double) * 15 * nr);
+    c.d_q = (double*)dalloc(c, sizeof(double) * 20 * nr);
+    c.d_w = (double*)dalloc(c, sizeof(double) * 15 * nr);
+    c.d_a = (double*)dalloc(c, sizeof(double) * 9 * nr);
+    c.d_thermo = (double*)dalloc(c, sizeof(double) * TH_N);
+    c.d_isum = (double*)dalloc(c, sizeof(double) * 8);
+    if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the integrator state");
+    // the centres of mass of the force phases become the first Gear slice
+    v.cx = c.d_c;
+    v.cy = c.d_c + nr;
+    v.cz = c.d_c + 2 * nr;
+    // regions saved before each chunk of steps (restored when the list must grow)
+    const int nold = v.ntota - v.nliqa, nflex = v.nmove - v.nriga;
+    auto add = [&](void* p, size_t b) {
+        if (p && b) c.snap_regions.push_back({p, b});
+    };
+    for (double* p : {v.x, v.y, v.z}) add(p, sizeof(double) * v.nmove);
+    for (double* p : {v.rsx, v.rsy, v.rsz}) add(p, sizeof(double) * v.nmove);
+    for (double* p : {c.d_xold, c.d_yold, c.d_zold}) add(p, sizeof(double) * nold);
+    for (double* p : {v.ocx, v.ocy, v.ocz}) add(p, sizeof(double) * v.nrig);
+    for (double* p : {v.ox, v.oy, v.oz}) add(p, sizeof(double) * nflex);
+    add(c.d_xd, sizeof(double) * 12 * nion);
+    add(c.d_c, sizeof(double) * 15 * nr);
+    add(c.d_q, sizeof(double) * 20 * nr);
+    add(c.d_w, sizeof(double) * 15 * nr);
+    add(c.d_thermo, sizeof(double) * TH_N);
+    size_t tot = 0;
+    for (auto& r : c.snap_regions) tot += (r.second + 255) / 256 * 256;
+    c.d_snap = (char*)dalloc(c, tot);
+    if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the step snapshot");
+    return MDG_OK;
+}
+
+static void snapshot(Ctx& c, bool restore) {
+    size_t off = 0;
+    for (auto& r : c.snap_regions) {
+        if (restore)
+            cudaMemcpyAsync(r.first, c.d_snap + off, r.second, cudaMemcpyDeviceToDevice, c.stream);
+        else
+            cudaMemcpyAsync(c.d_snap + off, r.first, r.second, cudaMemcpyDeviceToDevice, c.stream);
+        off += (r.second + 255) / 256 * 256;
+    }
+}
+
+// One MD step (src/main.f90:60-64): predict, forces, correct, SHAKE.
+static int step_launch(Ctx& c) {
+    predict_launch(c);
+    int rc = launch_force(c, false, false);
+    if (rc) return rc;
+    correct_launch(c);
+    if (c.v.nmove > c.v.nliqa) shake_launch(c, c.d_ft);
+    thermo_finish_launch(c);
+    return MDG_OK;
+}
+
+int mdg_set_state(mdg_ctx* cp, const mdg_rigid* b, const mdg_state* st) {
+    if (!cp || !b || !st) return set_err(cp, MDG_E_ARG, "null argument");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    View& v = c.v;
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    int rc = resident_alloc(c);
+    if (rc) return rc;
+    c.body = *b;
+    const int nm = v.nmove, nr = v.nrig, nion = v.nliqa - v.nriga, nold = v.ntota - v.nliqa;
+    MDG_CUDA(cudaMemcpy(v.x, st->x0, sizeof(double) * nm, cudaMemcpyHostToDevice));
+    MDG_CUDA(cudaMemcpy(v.y, st->y0, sizeof(double) * nm, cudaMemcpyHostToDevice));
+    MDG_CUDA(cudaMemcpy(v.z, st->z0, sizeof(double) * nm, cudaMemcpyHostToDevice));
+    for (int k = 0; k < 4 && nion > 0; ++k) {
+        const double* src[3] = {st->xd[k], st->yd[k], st->zd[k]};
+        for (int d = 0; d < 3; ++d)
+            MDG_CUDA(cudaMemcpy(c.d_xd + (k * 3 + d) * nion, src[d] + v.nriga, sizeof(double) * nion,
+                                cudaMemcpyHostToDevice));
+    }
+    for (int k = 0; k < 5 && nr > 0; ++k) {
+        const double* cs[3] = {st->cx[k], st->cy[k], st->cz[k]};
+        const double* ws[3] = {st->wx[k], st->wy[k], st->wz[k]};
+        for (int d = 0; d < 3; ++d) {
+            MDG_CUDA(cudaMemcpy(c.d_c + (k * 3 + d) * nr, cs[d], sizeof(double) * nr, cudaMemcpyHostToDevice));
+            MDG_CUDA(cudaMemcpy(c.d_w + (k * 3 + d) * nr, ws[d], sizeof(double) * nr, cudaMemcpyHostToDevice));
+        }
+        for (int q = 0; q < 4; ++q)
+            MDG_CUDA(cudaMemcpy(c.d_q + (q * 5 + k) * nr, st->q[q][k], sizeof(double) * nr, cudaMemcpyHostToDevice));
+    }
+    if (nold > 0) {
+        MDG_CUDA(cudaMemcpy(c.d_xold, st->xold, sizeof(double) * nold, cudaMemcpyHostToDevice));
+        MDG_CUDA(cudaMemcpy(c.d_yold, st->yold, sizeof(double) * nold, cudaMemcpyHostToDevice));
+        MDG_CUDA(cudaMemcpy(c.d_zold, st->zold, sizeof(double) * nold, cudaMemcpyHostToDevice));
+    }
+    MDG_CUDA(cudaMemcpy(v.rsx, st->rsx, sizeof(double) * nm, cudaMemcpyHostToDevice));
+    MDG_CUDA(cudaMemcpy(v.rsy, st->rsy, sizeof(double) * nm, cudaMemcpyHostToDevice));
+    MDG_CUDA(cudaMemcpy(v.rsz, st->rsz, sizeof(double) * nm, cudaMemcpyHostToDevice));
+    double th[TH_N] = {0};
+    for (int k = 0; k < 5; ++k) {
+        th[TH_S + k] = st->s[k];
+        th[TH_RS + k] = st->rs[k];
+    }
+    MDG_CUDA(cudaMemcpy(c.d_thermo, th, sizeof(th), cudaMemcpyHostToDevice));
+    const int one = 1;
+    MDG_CUDA(cudaMemcpy(v.status + ST_FORCE_RB, &one, sizeof(int), cudaMemcpyHostToDevice));
+    c.resident = true;
+    return MDG_OK;
+}
+
+int mdg_get_state(mdg_ctx* cp, mdg_state* st) {
+    if (!cp || !st) return set_err(cp, MDG_E_ARG, "null argument");
+    Ctx& c = *cp;
+    if (!c.resident) return set_err(&c, MDG_E_ARG, "mdg_get_state before mdg_set_state");
+    cudaSetDevice(c.device);
+    View& v = c.v;
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    const int nm = v.nmove, nr = v.nrig, nion = v.nliqa - v.nriga, nold = v.ntota - v.nliqa;
+    auto get = [&](double* dst, const double* src, size_t n) -> cudaError_t {
+        if (!dst || n == 0) return cudaSuccess;
+        return cudaMemcpy(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    };
+    MDG_CUDA(get(st->x0, v.x, nm));
+    MDG_CUDA(get(st->y0, v.y, nm));
+    MDG_CUDA(get(st->z0, v.z, nm));
+    for (int k = 0; k < 4 && nion > 0; ++k) {
+        double* dst[3] = {st->xd[k], st->yd[k], st->zd[k]};
+        for (int d = 0; d < 3; ++d)
+            if (dst[d]) MDG_CUDA(get(dst[d] + v.nriga, c.d_xd + (k * 3 + d) * nion, nion));
+    }
+    for (int k = 0; k < 5 && nr > 0; ++k) {
+        double* cs[3] = {st->cx[k], st->cy[k], st->cz[k]};
+        double* ws[3] = {st->wx[k], st->wy[k], st->wz[k]};
+        for (int d = 0; d < 3; ++d) {
+            MDG_CUDA(get(cs[d], c.d_c + (k * 3 + d) * nr, nr));
+            MDG_CUDA(get(ws[d], c.d_w + (k * 3 + d) * nr, nr));
+        }
+        for (int q = 0; q < 4; ++q) MDG_CUDA(get(st->q[q][k], c.d_q + (q * 5 + k) * nr, nr));
+    }
+    MDG_CUDA(get(st->xold, c.d_xold, nold));
+    MDG_CUDA(get(st->yold, c.d_yold, nold));
+    MDG_CUDA(get(st->zold, c.d_zold, nold));
+    MDG_CUDA(get(st->rsx, v.rsx, nm));
+    MDG_CUDA(get(st->rsy, v.rsy, nm));
+    MDG_CUDA(get(st->rsz, v.rsz, nm));
+    double th[TH_N];
+    MDG_CUDA(cudaMemcpy(th, c.d_thermo, sizeof(th), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 5; ++k) {
+        st->s[k] = th[TH_S + k];
+        st->rs[k] = th[TH_RS + k];
+    }
+    return MDG_OK;
+}
+
+static int ensure_graph(Ctx& c, int nstep) {
+    if (c.graph_exec) return MDG_OK;
+    cudaGraph_t g;
+    MDG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    int rc = MDG_OK;
+    for (int t = 0; t < nstep && rc == MDG_OK; ++t) rc = step_launch(c);
+    cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return set_err(&c, MDG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    size_t nn = 0;
+    cudaGraphGetNodes(g, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+    int64_t kern = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kern;
+    }
+    c.kernels_per_step = kern / std::max(nstep, 1);
+    e = cudaGraphInstantiate(&c.graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_err(&c, MDG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    c.graph_steps = nstep;
+    return MDG_OK;
+}
+
+static void fill_report(Ctx& c, const double* th, mdg_report* rep) {
+    View& v = c.v;
+    rep->kp = th[TH_KP];
+    rep->kw = th[TH_KW];
+    rep->ke = th[TH_KE];
+    rep->htot = th[TH_HTOT];
+    rep->tempnow = th[TH_TEMPNOW];
+    rep->uconf = th[TH_UCONF];
+    rep->press = th[TH_PRESS];
+    rep->steps = (int64_t)th[TH_STEPS];
+    rep->rebuilds = (int64_t)th[TH_REBUILDS];
+    rep->last_sweeps = c.h_status[ST_SWEEPS];
+    double hk[64] = {0};
+    cudaMemcpy(hk, c.d_kps, sizeof(double) * std::min(v.nit, 64), cudaMemcpyDeviceToHost);
+    double ks = 0.0;
+    for (int t = 0; t < std::min(v.nit, 64); ++t) ks += hk[t];
+    rep->tkps = c.nfreed > 0 ? ks * 1000.0 / ((double)8.31441f * (double)(float)c.nfreed) : 0.0;
+}
+
+int mdg_run_async(mdg_ctx* cp, int64_t nsteps) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    if (!c.resident) return set_err(&c, MDG_E_ARG, "mdg_run_async before mdg_set_state");
+    cudaSetDevice(c.device);
+    if (c.debug_sync) {
+        for (int64_t k = 0; k < nsteps; ++k) {
+            int rc = step_launch(c);
+            if (rc) return rc;
+        }
+        return MDG_OK;
+    }
+    int rc = ensure_graph(c, 1);
+    if (rc) return rc;
+    for (int64_t k = 0; k < nsteps; ++k) MDG_CUDA(cudaGraphLaunch(c.graph_exec, c.stream));
+    return MDG_OK;
+}
+
+int mdg_check(mdg_ctx* cp, mdg_report* rep) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    int rc = read_status(c);
+    if (rc) return rc;
+    MDG_CUDA(cudaMemsetAsync(c.v.status, 0, sizeof(int) * 4, c.stream));
+    if (c.h_status[ST_LIST_OVF] || c.h_status[ST_WLIST_OVF])
+        return set_err(&c, MDG_E_LIST_OVERFLOW, "nnlist_make(): nnlist too big! (rerun with mdg_run)");
+    if (c.h_status[ST_SHAKE_RPTOL]) return set_err(&c, MDG_E_SHAKE_RPTOL, "Constraint failure");
+    if (c.h_status[ST_SHAKE_MAXIT]) return set_err(&c, MDG_E_SHAKE_MAXIT, "shake(): Too many constraint iterations!");
+    if (c.resident) {
+        double th[TH_N];
+        MDG_CUDA(cudaMemcpy(th, c.d_thermo, sizeof(th), cudaMemcpyDeviceToHost));
+        if (!std::isfinite(th[TH_HTOT]) || !std::isfinite(th[TH_UCONF]))
+            return set_err(&c, MDG_E_NAN, "non-finite energy");
+        if (rep) fill_report(c, th, rep);
+    }
+    return MDG_OK;
+}
+
+int64_t mdg_kernels_per_step(const mdg_ctx* cp) { return cp ? cp->kernels_per_step : 0; }
+
+int mdg_run(mdg_ctx* cp, int64_t nsteps, mdg_report* rep) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    if (!c.resident) return set_err(&c, MDG_E_ARG, "mdg_run before mdg_set_state");
+    cudaSetDevice(c.device);
+    View& v = c.v;
+    const int kGraph = 1;     // steps per captured graph (relaunched; launch cost is a few us)
+    const int kChunk = 64;    // steps between status checks
+    const bool graphs = !c.debug_sync;
+    int64_t done = 0;
+    int retries = 0;
+    while (done < nsteps) {
+        const int64_t chunk = std::min<int64_t>(kChunk, nsteps - done);
+        snapshot(c, false);
+        MDG_CUDA(cudaMemsetAsync(v.status, 0, sizeof(int) * 4, c.stream));
+        int64_t k = 0;
+        if (graphs && chunk >= kGraph) {
+            int rc = ensure_graph(c, kGraph);
+            if (rc) return rc;
+            for (; k + kGraph <= chunk; k += kGraph) MDG_CUDA(cudaGraphLaunch(c.graph_exec, c.stream));
+        }
+        for (; k < chunk; ++k) {
+            int rc = step_launch(c);
+            if (rc) return rc;
+        }
+        int rc = read_status(c);
+        if (rc) return rc;
+        const int ovf = c.h_status[ST_LIST_OVF], wovf = c.h_status[ST_WLIST_OVF];
+        if (ovf || wovf) {
+            if (++retries > 4) return set_err(&c, MDG_E_LIST_OVERFLOW, "nnlist_make(): nnlist too big!");
+            rc = alloc_lists(c, ovf ? ovf + ovf / 4 + 32 : v.maxnb, wovf ? wovf + wovf / 4 + 32 : v.maxwnb);
+            if (rc) return rc;
+            snapshot(c, true);
+            const int one = 1;
+            MDG_CUDA(cudaMemcpyAsync(v.status + ST_FORCE_RB, &one, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+            MDG_CUDA(cudaStreamSynchronize(c.stream));
+            continue;
+        }
+        if (c.h_status[ST_SHAKE_RPTOL]) return set_err(&c, MDG_E_SHAKE_RPTOL, "Constraint failure");
+        if (c.h_status[ST_SHAKE_MAXIT]) return set_err(&c, MDG_E_SHAKE_MAXIT, "shake(): Too many constraint iterations!");
+        done += chunk;
+    }
+    double th[TH_N];
+    MDG_CUDA(cudaMemcpy(th, c.d_thermo, sizeof(th), cudaMemcpyDeviceToHost));
+    if (!std::isfinite(th[TH_HTOT]) || !std::isfinite(th[TH_UCONF])) return set_err(&c, MDG_E_NAN, "non-finite energy");
+    if (rep) fill_report(c, th, rep);
+    return MDG_OK;
+}
+
+int mdg_set_stream(mdg_ctx* cp, void* stream) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    if (!c.own_stream) c.own_stream = c.stream;
+    c.stream = stream ? (cudaStream_t)stream : c.own_stream;
+    if (c.graph_exec) {
+        cudaGraphExecDestroy(c.graph_exec);
+        c.graph_exec = nullptr;
+    }
+    return MDG_OK;
+}
+
+int mdg_phase_times(mdg_ctx* cp, int reps, double* ms) {
+    if (!cp || !ms || reps < 1) return set_err(cp, MDG_E_ARG, "bad argument");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    View& v = c.v;
+    cudaEvent_t ev[8];
+    for (auto& e : ev) MDG_CUDA(cudaEventCreate(&e));
+    double acc[MDG_NPHASE] = {0};
+    for (int r = 0; r < reps; ++r) {
+        cudaMemsetAsync(v.fx, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+        cudaMemsetAsync(v.fy, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+        cudaMemsetAsync(v.fz, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+        cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
+        cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
+        cudaEventRecord(ev[0], c.stream);
+        nnlist_trigger(c, true);
+        nnlist_build(c);
+        cudaEventRecord(ev[1], c.stream);
+        pair_forces_fp64(c);
+        surf_partition(c);
+        cudaEventRecord(ev[2], c.stream);
+        wall_forces_fp64(c);
+        cudaEventRecord(ev[3], c.stream);
+        recip_fp64(c);
+        cudaEventRecord(ev[4], c.stream);
+        lr_tail(c);
+        dipole_correction(c);
+        angle_forces(c);
+        force_sum(c, c.d_ft, c.d_fc, c.d_tq);
+        cudaEventRecord(ev[5], c.stream);
+        if (c.resident) {
+            predict_launch(c);
+            correct_launch(c);
+            thermo_finish_launch(c);
+        }
+        cudaEventRecord(ev[6], c.stream);
+        if (v.nmove > v.nliqa && c.ncons > 0 && c.resident) shake_launch(c, c.d_ft);
+        cudaEventRecord(ev[7], c.stream);
+        MDG_CUDA(cudaEventSynchronize(ev[7]));
+        for (int k = 0; k < MDG_NPHASE; ++k) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            acc[k] += t;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < MDG_NPHASE; ++k) ms[k] = acc[k] / reps;
+    return sync_check(c, "mdg_phase_times");
 }
 
 }  // extern "C"

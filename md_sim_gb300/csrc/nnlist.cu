@@ -55,7 +55,8 @@ __global__ void k_trigger(View v, int force) {
 
 __global__ void k_trigger_decide(View v, int force) {
     const double aux = fmax(v.acc[2 * v.nijt + ACC_MAXD], v.dshsq);
-    v.status[ST_REBUILD] = (force || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
+    v.status[ST_REBUILD] = (force || v.status[ST_FORCE_RB] || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
+    v.status[ST_FORCE_RB] = 0;
     v.acc[2 * v.nijt + ACC_MAXD] = 0.0;
 }
 

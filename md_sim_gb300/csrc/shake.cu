@@ -303,19 +303,25 @@ int shake_setup(Ctx& c, const mdg_sysdesc* s) {
     return MDG_OK;
 }
 
-// Verlet + SHAKE on the device state (x/y/z, xold, forces in c.d_ft_in).
-void shake_launch(Ctx& c) {
+__global__ void k_shake_status(View v, const int* sweeps) {
+    if (!sweeps[1]) v.status[ST_SHAKE_MAXIT] = 1;
+    v.status[ST_SWEEPS] = sweeps[0];
+}
+
+// Verlet + SHAKE on the device state (x/y/z, xold) with forces d_ft (3 x (nmove - nriga)).
+void shake_launch(Ctx& c, const double* d_ft) {
     const View& v = c.v;
     const int nsurf = v.nmove - v.nliqa;
     cudaMemsetAsync(c.d_kps, 0, sizeof(double) * v.nit, c.stream);
     if (nsurf > 0)
-        k_verlet<<<(nsurf + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, c.d_ft_in, c.d_xold, c.d_yold, c.d_zold, c.d_kps);
+        k_verlet<<<(nsurf + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, d_ft, c.d_xold, c.d_yold, c.d_zold, c.d_kps);
     if (c.ncons == 0) return;
     const int clean = (c.quirks & MDG_QUIRK_CLEAN_SHAKE_DONE) ? 1 : 0;
     ShakeArgs A{c.ncons, c.maxit, clean, v.nliqa, v.nmove, c.tol2, c.rptol, c.d_cons, c.d_clen2,
                 c.d_cons_n, c.d_xold, c.d_yold, c.d_zold, c.d_sweeps};
     if (c.shake_seq) {
         k_shake_seq<<<1, 1, 0, c.stream>>>(v, A, c.d_seq_flags, c.d_seq_flags + std::max(nsurf, 1));
+        k_shake_status<<<1, 1, 0, c.stream>>>(v, c.d_sweeps);
         return;
     }
     if (clean) {
@@ -324,6 +330,7 @@ void shake_launch(Ctx& c) {
         k_shake_last<<<1, 1, 0, c.stream>>>(v, A);
     }
     k_shake_mol<<<(c.ncons + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, A);
+    k_shake_status<<<1, 1, 0, c.stream>>>(v, c.d_sweeps);
 }
 
 }  // namespace mdg

@@ -100,6 +100,13 @@ struct Ref {
     // SHAKE
     int64_t nfreed;
     std::string err;
+    // resident-mode integrator state (src/config.f90:20-51)
+    bool have_state = false;
+    std::vector<double> X[3], XD[4][3], C[5][3], Q[4][5], W[5][3], OLD[3], RS[3], A[9];
+    double s[5], rs[5];
+    mdg_rigid body;
+    double kp = 0, kw = 0, ke = 0, htot = 0, sft = 0, sfr = 0, tempnow = 0, uconf = 0, tkps = 0, press = 0;
+    int32_t last_sweeps = 0;
 
     int ij(int64_t it, int64_t jt) const { return (int)ijtype[(it - 1) + nit * (jt - 1)] - 1; }
     double mx(double d) const { return d - lx * anint(d * lxi); }
@@ -1023,6 +1030,264 @@ int ref_shake(RefCtx* r, double* x0, double* y0, double* z0, double* xold, doubl
     }
     if (sweeps) *sweeps = ite;
     if (!done && r->ncons > 0) return fail(r, MDG_E_SHAKE_MAXIT, "shake(): Too many constraint iterations!");
+    return MDG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Resident mode: move_predict (src/move.f90:48-217), force_get, move_correct (:220-383) and
+// move_shake, in the order of the production loop (src/main.f90:58-68).
+// ------------------------------------------------------------------------------------------
+static const double Gf01 = F(0.348611111f), Gf11 = 1.0, Gf21 = F(0.916666667f), Gf31 = F(0.333333333f),
+                    Gf41 = F(0.041666667f);
+static const double Gf02 = F(0.158300000f), Gf12 = F(0.757000000f), Gf22 = 1.0, Gf32 = 0.5,
+                    Gf42 = F(0.083333333f);
+
+static void gear_predict(double& a0, double& a1, double& a2, double& a3, double a4) {
+    a0 = a0 + a1 + a2 + a3 + a4;
+    a1 = a1 + 2 * a2 + 3 * a3 + 4 * a4;
+    a2 = a2 + 3 * a3 + 6 * a4;
+    a3 = a3 + 4 * a4;
+}
+
+static void move_predict(RefCtx* r) {
+    const int64_t tmin = r->nriga, tmax = r->nliqa, nrig = r->nrig;
+    for (int64_t i = tmin; i < tmax; ++i)
+        for (int d = 0; d < 3; ++d)
+            gear_predict(r->X[d][i], r->XD[0][d][i], r->XD[1][d][i], r->XD[2][d][i], r->XD[3][d][i]);
+    double kp = 0.0;
+    for (int64_t i = tmin; i < tmax; ++i)
+        kp += r->mi[i] * (r->XD[0][0][i] * r->XD[0][0][i] + r->XD[0][1][i] * r->XD[0][1][i] +
+                          r->XD[0][2][i] * r->XD[0][2][i]);
+    for (int64_t i = 0; i < nrig; ++i)
+        for (int d = 0; d < 3; ++d) gear_predict(r->C[0][d][i], r->C[1][d][i], r->C[2][d][i], r->C[3][d][i], r->C[4][d][i]);
+    double sc[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d)
+        for (int64_t i = 0; i < nrig; ++i) sc[d] += r->C[1][d][i] * r->C[1][d][i];
+    kp = kp + r->body.mw * (sc[0] + sc[1] + sc[2]);
+    for (int64_t i = 0; i < nrig; ++i)
+        for (int d = 0; d < 3; ++d) gear_predict(r->W[0][d][i], r->W[1][d][i], r->W[2][d][i], r->W[3][d][i], r->W[4][d][i]);
+    double sw[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d)
+        for (int64_t i = 0; i < nrig; ++i) sw[d] += r->W[0][d][i] * r->W[0][d][i];
+    const double kw = r->body.inxx * sw[0] + r->body.inyy * sw[1] + r->body.inzz * sw[2];
+    for (int64_t i = 0; i < nrig; ++i) {
+        for (int c = 0; c < 4; ++c) gear_predict(r->Q[c][0][i], r->Q[c][1][i], r->Q[c][2][i], r->Q[c][3][i], r->Q[c][4][i]);
+        double& q1 = r->Q[0][0][i];
+        double& q2 = r->Q[1][0][i];
+        double& q3 = r->Q[2][0][i];
+        double& q4 = r->Q[3][0][i];
+        const double cr = 1.0 / std::sqrt(q1 * q1 + q2 * q2 + q3 * q3 + q4 * q4);
+        q1 = q1 * cr; q2 = q2 * cr; q3 = q3 * cr; q4 = q4 * cr;
+        r->A[0][i] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
+        r->A[1][i] = 2.0 * (q3 * q4 - q1 * q2);
+        r->A[2][i] = 2.0 * (q2 * q3 + q1 * q4);
+        r->A[3][i] = -2.0 * (q1 * q2 + q3 * q4);
+        r->A[4][i] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4;
+        r->A[5][i] = 2.0 * (q2 * q4 - q1 * q3);
+        r->A[6][i] = 2.0 * (q2 * q3 - q1 * q4);
+        r->A[7][i] = -2.0 * (q1 * q3 + q4 * q2);
+        r->A[8][i] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
+    }
+    const mdg_rigid& b = r->body;
+    for (int64_t i = 0; i < nrig; ++i) {
+        const int64_t ix = 3 * i;
+        for (int j = 0; j < 3; ++j) {
+            r->X[0][ix + j] = r->C[0][0][i] + r->A[0][i] * b.xbody[j] + r->A[3][i] * b.ybody[j] + r->A[6][i] * b.zbody[j];
+            r->X[1][ix + j] = r->C[0][1][i] + r->A[1][i] * b.xbody[j] + r->A[4][i] * b.ybody[j] + r->A[7][i] * b.zbody[j];
+            r->X[2][ix + j] = r->C[0][2][i] + r->A[2][i] * b.xbody[j] + r->A[5][i] * b.ybody[j] + r->A[8][i] * b.zbody[j];
+        }
+        for (int j = 1; j < 3; ++j)
+            for (int d = 0; d < 3; ++d) r->RS[d][ix + j] = r->X[d][ix + j] - r->X[d][ix];
+    }
+    if (b.temper == -1.0) {
+        r->s[0] = r->s[1] = r->rs[0] = r->rs[1] = 0.0;
+    } else {
+        gear_predict(r->s[0], r->s[1], r->s[2], r->s[3], r->s[4]);
+        gear_predict(r->rs[0], r->rs[1], r->rs[2], r->rs[3], r->rs[4]);
+    }
+    r->kp = kp;
+    r->kw = kw;
+    r->ke = kp + kw;
+    const int64_t nfree = r->nliqa - r->nriga;
+    const double tstar = PH_R * b.temper / 1000.0;
+    double qmass = (double)(float)(3 * (nfree + nrig)) * tstar * F(2e3f);
+    double rmass = (double)(float)(3 * nrig) * tstar * F(1e3f);
+    qmass = qmass / 10.0;
+    rmass = rmass / 10.0;
+    r->htot = 0.5 * (r->ke + qmass * r->s[0] * r->s[0] + rmass * r->rs[0] * r->rs[0]) + r->uconf;
+    r->sft = (kp - (double)(float)(3 * (nfree + nrig) - 2) * tstar) / qmass;
+    r->sfr = (kw - (double)(float)(3 * nrig + 1) * tstar) / rmass;
+}
+
+static void move_correct(RefCtx* r, const std::vector<double>* ft, const std::vector<double>* fc,
+                         const std::vector<double>* tq) {
+    const int64_t tmin = r->nriga, tmax = r->nliqa, nrig = r->nrig;
+    double rcorr = 0.5;
+    const double s0i = r->s[0];
+    for (int64_t i = tmin; i < tmax; ++i)
+        for (int d = 0; d < 3; ++d) {
+            const double cort = rcorr * ft[d][i - r->nriga] * r->mii[i] - r->XD[0][d][i] * s0i - r->XD[1][d][i];
+            r->X[d][i] = r->X[d][i] + Gf02 * cort;
+            r->XD[0][d][i] = r->XD[0][d][i] + Gf12 * cort;
+            r->XD[1][d][i] = r->XD[1][d][i] + Gf22 * cort;
+            r->XD[2][d][i] = r->XD[2][d][i] + Gf32 * cort;
+            r->XD[3][d][i] = r->XD[3][d][i] + Gf42 * cort;
+        }
+    rcorr = rcorr / r->body.mw;
+    for (int64_t i = 0; i < nrig; ++i)
+        for (int d = 0; d < 3; ++d) {
+            const double c1 = rcorr * fc[d][i] - r->C[1][d][i] * s0i - r->C[2][d][i];
+            r->C[0][d][i] = r->C[0][d][i] + Gf02 * c1;
+            r->C[1][d][i] = r->C[1][d][i] + Gf12 * c1;
+            r->C[2][d][i] = r->C[2][d][i] + Gf22 * c1;
+            r->C[3][d][i] = r->C[3][d][i] + Gf32 * c1;
+            r->C[4][d][i] = r->C[4][d][i] + Gf42 * c1;
+        }
+    for (int64_t i = 0; i < nrig; ++i) {
+        const double q1 = r->Q[0][0][i], q2 = r->Q[1][0][i], q3 = r->Q[2][0][i], q4 = r->Q[3][0][i];
+        const double wx = r->W[0][0][i], wy = r->W[0][1][i], wz = r->W[0][2][i];
+        double cq[4];
+        cq[0] = 0.5 * (-q3 * wx - q4 * wy + q2 * wz);
+        cq[1] = 0.5 * (q4 * wx - q3 * wy - q1 * wz);
+        cq[2] = 0.5 * (q1 * wx + q2 * wy + q4 * wz);
+        cq[3] = 0.5 * (-q2 * wx + q1 * wy - q3 * wz);
+        for (int c = 0; c < 4; ++c) {
+            const double co = cq[c] - r->Q[c][1][i];
+            r->Q[c][0][i] = r->Q[c][0][i] + Gf01 * co;
+            r->Q[c][1][i] = r->Q[c][1][i] + Gf11 * co;
+            r->Q[c][2][i] = r->Q[c][2][i] + Gf21 * co;
+            r->Q[c][3][i] = r->Q[c][3][i] + Gf31 * co;
+            r->Q[c][4][i] = r->Q[c][4][i] + Gf41 * co;
+        }
+    }
+    rcorr = 1.0;
+    const double rs0i = r->rs[0];
+    const mdg_rigid& b = r->body;
+    const double inxxi = 1.0 / b.inxx, inyyi = 1.0 / b.inyy, inzzi = 1.0 / b.inzz;
+    for (int64_t i = 0; i < nrig; ++i) {
+        const double wx = r->W[0][0][i], wy = r->W[0][1][i], wz = r->W[0][2][i];
+        double c1 = r->A[0][i] * tq[0][i] + r->A[1][i] * tq[1][i] + r->A[2][i] * tq[2][i];
+        c1 = ((c1 * rcorr + wy * wz * (b.inyy - b.inzz)) * inxxi) - r->W[1][0][i] - rs0i * wx;
+        double c2 = r->A[3][i] * tq[0][i] + r->A[4][i] * tq[1][i] + r->A[5][i] * tq[2][i];
+        c2 = ((c2 * rcorr + wz * wx * (b.inzz - b.inxx)) * inyyi) - r->W[1][1][i] - rs0i * wy;
+        double c3 = r->A[6][i] * tq[0][i] + r->A[7][i] * tq[1][i] + r->A[8][i] * tq[2][i];
+        c3 = ((c3 * rcorr + wx * wy * (b.inxx - b.inyy)) * inzzi) - r->W[1][2][i] - rs0i * wz;
+        const double cc[3] = {c1, c2, c3};
+        for (int d = 0; d < 3; ++d) {
+            r->W[0][d][i] = r->W[0][d][i] + Gf01 * cc[d];
+            r->W[1][d][i] = r->W[1][d][i] + Gf11 * cc[d];
+            r->W[2][d][i] = r->W[2][d][i] + Gf21 * cc[d];
+            r->W[3][d][i] = r->W[3][d][i] + Gf31 * cc[d];
+            r->W[4][d][i] = r->W[4][d][i] + Gf41 * cc[d];
+        }
+    }
+    if (b.temper != -1.0) {
+        double rc = r->sft - r->s[1];
+        r->s[0] = r->s[0] + Gf01 * rc;
+        r->s[1] = r->sft;
+        r->s[2] = r->s[2] + Gf21 * rc;
+        r->s[3] = r->s[3] + Gf31 * rc;
+        r->s[4] = r->s[4] + Gf41 * rc;
+        rc = r->sfr - r->rs[1];
+        r->rs[0] = r->rs[0] + Gf01 * rc;
+        r->rs[1] = r->sfr;
+        r->rs[2] = r->rs[2] + Gf21 * rc;
+        r->rs[3] = r->rs[3] + Gf31 * rc;
+        r->rs[4] = r->rs[4] + Gf41 * rc;
+    }
+}
+
+int ref_set_state(RefCtx* r, const mdg_rigid* b, const mdg_state* st) {
+    const int64_t nt = r->ntota, nrig = r->nrig, nold = r->ntota - r->nliqa, nm = r->nmove;
+    auto cpy = [](std::vector<double>& v, const double* p, int64_t n) { v.assign(p, p + n); };
+    cpy(r->X[0], st->x0, nt); cpy(r->X[1], st->y0, nt); cpy(r->X[2], st->z0, nt);
+    for (int k = 0; k < 4; ++k) {
+        cpy(r->XD[k][0], st->xd[k], nt); cpy(r->XD[k][1], st->yd[k], nt); cpy(r->XD[k][2], st->zd[k], nt);
+    }
+    for (int k = 0; k < 5; ++k) {
+        cpy(r->C[k][0], st->cx[k], nrig); cpy(r->C[k][1], st->cy[k], nrig); cpy(r->C[k][2], st->cz[k], nrig);
+        cpy(r->W[k][0], st->wx[k], nrig); cpy(r->W[k][1], st->wy[k], nrig); cpy(r->W[k][2], st->wz[k], nrig);
+        for (int c = 0; c < 4; ++c) cpy(r->Q[c][k], st->q[c][k], nrig);
+    }
+    cpy(r->OLD[0], st->xold, nold); cpy(r->OLD[1], st->yold, nold); cpy(r->OLD[2], st->zold, nold);
+    cpy(r->RS[0], st->rsx, nm); cpy(r->RS[1], st->rsy, nm); cpy(r->RS[2], st->rsz, nm);
+    for (int k = 0; k < 9; ++k) r->A[k].assign(nrig, 0.0);
+    for (int k = 0; k < 5; ++k) {
+        r->s[k] = st->s[k];
+        r->rs[k] = st->rs[k];
+    }
+    r->body = *b;
+    r->have_state = true;
+    return MDG_OK;
+}
+
+int ref_get_state(RefCtx* r, mdg_state* st) {
+    if (!r->have_state) return fail(r, MDG_E_ARG, "no state");
+    const int64_t nt = r->ntota, nrig = r->nrig, nold = r->ntota - r->nliqa, nm = r->nmove;
+    auto out = [](const std::vector<double>& v, double* p, int64_t n) {
+        if (p) std::copy(v.begin(), v.begin() + n, p);
+    };
+    out(r->X[0], st->x0, nt); out(r->X[1], st->y0, nt); out(r->X[2], st->z0, nt);
+    for (int k = 0; k < 4; ++k) {
+        out(r->XD[k][0], st->xd[k], nt); out(r->XD[k][1], st->yd[k], nt); out(r->XD[k][2], st->zd[k], nt);
+    }
+    for (int k = 0; k < 5; ++k) {
+        out(r->C[k][0], st->cx[k], nrig); out(r->C[k][1], st->cy[k], nrig); out(r->C[k][2], st->cz[k], nrig);
+        out(r->W[k][0], st->wx[k], nrig); out(r->W[k][1], st->wy[k], nrig); out(r->W[k][2], st->wz[k], nrig);
+        for (int c = 0; c < 4; ++c) out(r->Q[c][k], st->q[c][k], nrig);
+    }
+    out(r->OLD[0], st->xold, nold); out(r->OLD[1], st->yold, nold); out(r->OLD[2], st->zold, nold);
+    out(r->RS[0], st->rsx, nm); out(r->RS[1], st->rsy, nm); out(r->RS[2], st->rsz, nm);
+    for (int k = 0; k < 5; ++k) {
+        st->s[k] = r->s[k];
+        st->rs[k] = r->rs[k];
+    }
+    return MDG_OK;
+}
+
+int ref_run(RefCtx* r, int64_t nsteps, mdg_report* rep) {
+    if (!r->have_state) return fail(r, MDG_E_ARG, "mdg_run before mdg_set_state");
+    const int64_t nm = r->nmove, nflex = r->nmove - r->nriga, nrig = std::max<int64_t>(r->nrig, 1);
+    std::vector<double> ft[3], fc[3], tq[3];
+    for (int d = 0; d < 3; ++d) {
+        ft[d].assign(std::max<int64_t>(nflex, 1), 0.0);
+        fc[d].assign(nrig, 0.0);
+        tq[d].assign(nrig, 0.0);
+    }
+    std::vector<double> cx(nrig), cy(nrig), cz(nrig), elj(r->nijt), eqq(r->nijt);
+    for (int64_t step = 0; step < nsteps; ++step) {
+        move_predict(r);
+        for (int64_t i = 0; i < r->nrig; ++i) {
+            cx[i] = r->C[0][0][i]; cy[i] = r->C[0][1][i]; cz[i] = r->C[0][2][i];
+        }
+        mdg_energies e{};
+        e.elj = elj.data();
+        e.eqq = eqq.data();
+        int rc = ref_force_get(r, r->X[0].data(), r->X[1].data(), r->X[2].data(), cx.data(), cy.data(), cz.data(),
+                               r->RS[0].data(), r->RS[1].data(), r->RS[2].data(), ft[0].data(), ft[1].data(),
+                               ft[2].data(), fc[0].data(), fc[1].data(), fc[2].data(), tq[0].data(), tq[1].data(),
+                               tq[2].data(), nullptr, nullptr, nullptr, &e);
+        if (rc) return rc;
+        r->uconf = e.uconf;
+        r->press = e.press;
+        move_correct(r, ft, fc, tq);
+        if (nm > r->nliqa) {
+            int32_t sw = 0;
+            double tk = 0.0;
+            rc = ref_shake(r, r->X[0].data(), r->X[1].data(), r->X[2].data(), r->OLD[0].data(), r->OLD[1].data(),
+                           r->OLD[2].data(), ft[0].data(), ft[1].data(), ft[2].data(), nullptr, &tk, &sw);
+            if (rc) return rc;
+            r->last_sweeps = sw;
+            r->tkps = tk;
+        }
+        const int64_t nfree = r->nliqa - r->nriga;
+        r->tempnow = r->ke * 1000.0 / (3.0 * PH_R * (double)(float)(nfree + 2 * r->nrig));
+    }
+    if (rep) {
+        rep->kp = r->kp; rep->kw = r->kw; rep->ke = r->ke; rep->htot = r->htot; rep->tempnow = r->tempnow;
+        rep->uconf = r->uconf; rep->tkps = r->tkps; rep->press = r->press; rep->steps = nsteps;
+        rep->rebuilds = 0; rep->last_sweeps = r->last_sweeps;
+    }
     return MDG_OK;
 }
 
