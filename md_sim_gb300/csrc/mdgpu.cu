@@ -221,9 +221,15 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
     if (reset_status) cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
     PHASE(nnlist_trigger(c, force_rebuild), "trigger");
     PHASE(nnlist_build(c), "nnlist");
-    PHASE(pair_forces_fp64(c), "pairs");
-    PHASE(surf_partition(c), "surf_partition");
-    PHASE(wall_forces_fp64(c), "walls");
+    if (c.precision == MDG_MIXED) {
+        PHASE(pair_forces_fp32(c), "pairs");
+        PHASE(surf_partition(c), "surf_partition");
+        PHASE(wall_forces_fp32(c), "walls");
+    } else {
+        PHASE(pair_forces_fp64(c), "pairs");
+        PHASE(surf_partition(c), "surf_partition");
+        PHASE(wall_forces_fp64(c), "walls");
+    }
     PHASE(lr_tail(c), "lr_tail");
     PHASE(recip_fp64(c), "reciprocal");
     PHASE(dipole_correction(c), "dipole");
@@ -1063,10 +1069,12 @@ int mdg_phase_times(mdg_ctx* cp, int reps, double* ms) {
         nnlist_trigger(c, true);
         nnlist_build(c);
         cudaEventRecord(ev[1], c.stream);
-        pair_forces_fp64(c);
+        if (c.precision == MDG_MIXED) pair_forces_fp32(c);
+        else pair_forces_fp64(c);
         surf_partition(c);
         cudaEventRecord(ev[2], c.stream);
-        wall_forces_fp64(c);
+        if (c.precision == MDG_MIXED) wall_forces_fp32(c);
+        else wall_forces_fp64(c);
         cudaEventRecord(ev[3], c.stream);
         recip_fp64(c);
         cudaEventRecord(ev[4], c.stream);
