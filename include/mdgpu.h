@@ -255,6 +255,32 @@ int mdg_set_stream(mdg_ctx* ctx, void* stream);
 #define MDG_NPHASE 7
 int mdg_phase_times(mdg_ctx* ctx, int reps, double* ms);
 
+/* ---------------------------------------------------------------------------------------------
+ * Allocation-free reciprocal sum.  This entry point has no counterpart in the reference: it is
+ * offered to callers that must not allocate device memory while they run (a host that sized its
+ * device memory once at start-up, a framework whose caching allocator owns the device memory, or
+ * work queued into a CUDA stream capture).  It computes the reciprocal-space Ewald forces and energy
+ * of force_fouri (src/forcem.f90:827-937, no static walls, no slab term) for n charges, with the
+ * same kernels and results as the reciprocal phase of mdg_force_get.
+ *
+ *   x, y, z, q   in   device arrays of n doubles (positions in A, charges in e)
+ *   fx, fy, fz   out  device arrays of n doubles, overwritten with the reciprocal forces
+ *   uewa         out  device pointer to one double, the reciprocal energy (may be NULL)
+ *   stream       CUDA stream (cudaStream_t) the work is queued on; NULL is the default stream
+ * alpha and kmax as in mdg_params (alpha must be given).  Allocates nothing: its scratch is a static
+ * device array of MDG_NOALLOC_MAX_K k vectors (about 2 MB) that every GPU loading the library keeps
+ * until the process exits; larger k sets are rejected with MDG_E_UNSUPPORTED.  The first call on a
+ * device looks up that array's device address, so make the first call on each device before any
+ * stream capture.  Calls share the one array: calls whose GPU work overlaps (other streams, other
+ * host threads' streams) race on it; host calls themselves are serialised.  The call returns once
+ * the work is queued; errors of argument checking are returned, mdg_last_error(NULL) has the text.
+ * ------------------------------------------------------------------------------------------- */
+#define MDG_NOALLOC_MAX_K 32768
+#define MDG_NOALLOC_MAX_ROWS 4096
+int mdg_recip_forces_noalloc(const double* x, const double* y, const double* z, const double* q, int64_t n,
+                             double lx, double ly, double lz, double alpha, int64_t kmax, double* fx,
+                             double* fy, double* fz, double* uewa, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

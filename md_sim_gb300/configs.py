@@ -343,3 +343,29 @@ def equilibrate(ctx, s: S.System, steps: int = 400, T: float = 300.0, every: int
         ctx.set_state(s)
         done += every
     return s
+
+
+def ion_lattice(n_side: int = 6, spacing: float = 2.8, rcut: float = 2.0, alpha: float = 0.35,
+                kmax: int = 6, seed: int = 21, jitter: float = 0.2) -> Tuple[S.System, RunParams]:
+    """Rocksalt arrangement of +1/-1 point ions (two atmol types, no vdW) in a cubic periodic box,
+    jittered; rcut below the closest approach so that the real-space sum is empty and the
+    forces of force_get are the reciprocal-space forces alone."""
+    n = n_side ** 3
+    if n % 2:
+        raise ValueError("n_side must be even")
+    L = n_side * spacing
+    g = np.stack(np.meshgrid(*[np.arange(n_side)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    par = g.sum(1) % 2
+    rng = np.random.default_rng(seed)
+    pos = g * spacing + rng.uniform(-jitter, jitter, size=(n, 3)) - 0.5 * L
+    cat = S.MolType("Na", "atmol", int((par == 0).sum()), ["Na"], [1], [22.99e-3], [1.0], ns=1)
+    an = S.MolType("Cl", "atmol", int((par == 1).sum()), ["Cl"], [1], [35.45e-3], [-1.0], ns=1)
+    crys = S.MolType("none", "crystal", 1, ["X1", "X2"], [1, 1], [1e-3, 1e-3], [0.0, 0.0], ns=0,
+                     cx=L, cy=L, cz=L, lw=L)
+    fld = S.FieldFile([cat, an, crys], _vdw_table(["Na", "Cl", "X1", "X2"], {}))
+    s = S.System(fld, S.TopFile([], [], [], []), L, L, L, 1.0)
+    order = np.concatenate([np.nonzero(par == 0)[0], np.nonzero(par == 1)[0]])
+    s.x0[:n], s.y0[:n], s.z0[:n] = pos[order].T
+    s.temper = -1.0
+    prm = RunParams(rcut=rcut, skin=0.1, kmax=kmax, alpha=alpha, variant=MDG_BULK, pbc_z_list=1)
+    return s, prm

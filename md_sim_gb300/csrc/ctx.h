@@ -178,6 +178,10 @@ void wall_forces_fp32(Ctx& c);
 // recip.cu
 int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const double* z0);
 void recip_fp64(Ctx& c);
+int recip_forces_noalloc(const double* x, const double* y, const double* z, const double* q, int64_t n,
+                         double lx, double ly, double lz, double alpha, int64_t kmax, double* fx, double* fy,
+                         double* fz, double* uewa, cudaStream_t st);
+const char* recip_noalloc_error();
 // epilogue.cu
 void dipole_correction(Ctx& c);
 void angle_forces(Ctx& c);

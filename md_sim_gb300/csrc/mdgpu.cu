@@ -1103,4 +1103,12 @@ int mdg_phase_times(mdg_ctx* cp, int reps, double* ms) {
     return sync_check(c, "mdg_phase_times");
 }
 
+int mdg_recip_forces_noalloc(const double* x, const double* y, const double* z, const double* q, int64_t n,
+                             double lx, double ly, double lz, double alpha, int64_t kmax, double* fx, double* fy,
+                             double* fz, double* uewa, void* stream) {
+    const int rc = recip_forces_noalloc(x, y, z, q, n, lx, ly, lz, alpha, kmax, fx, fy, fz, uewa, (cudaStream_t)stream);
+    if (rc) g_err = recip_noalloc_error();
+    return rc;
+}
+
 }  // extern "C"

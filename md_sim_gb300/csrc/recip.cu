@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -344,6 +346,187 @@ void recip_fp64(Ctx& c) {
     k_kenergy<<<std::min((ks.nk + 255) / 256, 256), 256, 0, c.stream>>>(v, ks.nk, ks.ak, ks.s, ks.qw, ks.c);
     k_kforce<<<(v.nmove + kForceNT - 1) / kForceNT, kForceNT, ks.force_smem, c.stream>>>(v, d, ks.nrow, ks.row,
                                                                                         ks.row_nlen, ks.c, ks.nk);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free reciprocal sum (mdg_recip_forces_noalloc).
+//
+// Some callers cannot allocate device memory while they run: a host that has sized its device
+// memory once at start-up and forbids later driver allocations, a framework whose caching
+// allocator owns all device memory (a cudaMalloc behind its back fragments the pool and
+// synchronises the device), or code that queues work into a CUDA stream capture.  For them the
+// structure-factor sum runs here with all of its scratch in one static device array that the
+// library carries (every GPU that loads the library holds it until the process exits).  The caller
+// passes device arrays in and out; nothing is allocated by this path.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kNaMaxK = MDG_NOALLOC_MAX_K;
+constexpr int kNaMaxRows = MDG_NOALLOC_MAX_ROWS;
+constexpr int kNaMaxWork = kNaMaxK / kChunk + kNaMaxRows;
+
+// byte offsets of the regions inside the scratch array
+constexpr size_t kNaS = 0;                                              // double2 [MAX_K]  S(k)
+constexpr size_t kNaC = kNaS + sizeof(double2) * kNaMaxK;               // double2 [MAX_K]  C(k)
+constexpr size_t kNaQw = kNaC + sizeof(double2) * kNaMaxK;              // double2 [MAX_K]  zeros
+constexpr size_t kNaAk = kNaQw + sizeof(double2) * kNaMaxK;             // double  [MAX_K]
+constexpr size_t kNaRows = kNaAk + sizeof(double) * kNaMaxK;            // int4    [MAX_ROWS]
+constexpr size_t kNaNlen = kNaRows + sizeof(int4) * kNaMaxRows;         // int     [MAX_ROWS]
+constexpr size_t kNaWr = kNaNlen + sizeof(int) * kNaMaxRows;            // int     [MAX_WORK]
+constexpr size_t kNaWn = kNaWr + sizeof(int) * kNaMaxWork;              // int     [MAX_WORK]
+constexpr size_t kNaAcc = (kNaWn + sizeof(int) * kNaMaxWork + 255) / 256 * 256;  // double [64]
+constexpr size_t kNaStatus = kNaAcc + sizeof(double) * 64;              // int [ST_NWORDS]
+constexpr size_t kNaBytes = (kNaStatus + sizeof(int) * ST_NWORDS + 255) / 256 * 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+__global__ void k_noalloc_energy(const double* acc, double* uewa) {
+    if (threadIdx.x == 0 && blockIdx.x == 0 && uewa) *uewa = 0.5 * acc[ACC_UEWA];
+}
+
+std::mutex g_na_mutex;
+constexpr int kNaMaxDev = 64;
+unsigned char* g_na_ptr[kNaMaxDev] = {nullptr};
+// host-side k tables, reused by every call (calls are serialised by g_na_mutex)
+int4 g_na_rows[kNaMaxRows];
+int g_na_nlen[kNaMaxRows];
+double g_na_ak[kNaMaxK];
+int g_na_wr[kNaMaxWork], g_na_wn[kNaMaxWork];
+thread_local char g_na_err[256] = "";
+
+int na_fail(int code, const char* msg) {
+    std::snprintf(g_na_err, sizeof g_na_err, "%s", msg);
+    return code;
+}
+
+}  // namespace
+
+const char* recip_noalloc_error() { return g_na_err; }
+
+int recip_forces_noalloc(const double* x, const double* y, const double* z, const double* q, int64_t n,
+                         double lx, double ly, double lz, double alpha, int64_t kmax, double* fx, double* fy,
+                         double* fz, double* uewa, cudaStream_t st) {
+    if (!x || !y || !z || !q || !fx || !fy || !fz || n < 1 || n >= (1LL << 31) || kmax < 1 || alpha <= 0.0 ||
+        lx <= 0.0 || ly <= 0.0 || lz <= 0.0)
+        return na_fail(MDG_E_ARG, "mdg_recip_forces_noalloc: bad argument");
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDev)
+        return na_fail(MDG_E_CUDA, "mdg_recip_forces_noalloc: no current CUDA device");
+    if (!g_na_ptr[dev]) {
+        // once per device, with that device current: the device address of the static scratch
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return na_fail(MDG_E_CUDA, "mdg_recip_forces_noalloc: cudaGetSymbolAddress failed");
+        g_na_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    unsigned char* base = g_na_ptr[dev];
+    // k set in the reference's order and selection (src/forcem.f90:743-776)
+    const double pi_r = (double)3.1415926535898f;
+    const double PH_e = (double)1.6021892e-19f, PH_Na = (double)6.022045e23f, PH_eps0 = (double)8.85418782e-12f,
+                 PH_A2m = (double)1.0e-10f;
+    const double pipix = 2.0 * pi_r / lx, pipiy = 2.0 * pi_r / ly, pipiz = 2.0 * pi_r / lz;
+    const double alf4i = -1.0 / (4.0 * alpha * alpha);
+    const double fac = 2.0 * PH_e * PH_e * PH_Na / (PH_eps0 * PH_A2m * 1000.0 * lx * ly * lz);
+    const double lmin = std::min(lx, std::min(ly, lz));
+    const double rk = (double)(float)kmax;
+    const int KL = (int)std::lround(rk * lx / lmin), KM = (int)std::lround(rk * ly / lmin),
+              KN = (int)std::lround(rk * lz / lmin);
+    const float lim = (float)(kmax * kmax) + 2.01f;
+    int nk = 0, nrow = 0, nwork = 0;
+    int kmmin = 0, knmin = 1;
+    for (int kl = 0; kl <= KL; ++kl) {
+        const double rl = pipix * (double)(float)kl;
+        for (int km = kmmin; km <= KM; ++km) {
+            const double rm = pipiy * (double)(float)km;
+            int first = 0, cnt = 0;
+            for (int kn = knmin; kn <= KN; ++kn) {
+                volatile float a = (float)(kl * kl + km * km);
+                volatile float b = (float)((int64_t)kn * kn * kmax * kmax) / (float)((int64_t)KN * KN);
+                volatile float ksq = a + b;
+                if (!(ksq < lim)) continue;
+                if (nk >= kNaMaxK) return na_fail(MDG_E_UNSUPPORTED, "mdg_recip_forces_noalloc: more than MDG_NOALLOC_MAX_K k vectors");
+                const double rn = pipiz * (double)(float)kn;
+                const double rksq = rl * rl + rm * rm + rn * rn;
+                if (cnt == 0) first = kn;
+                ++cnt;
+                g_na_ak[nk++] = fac * std::exp(rksq * alf4i) / rksq;
+            }
+            if (cnt > 0) {
+                if (nrow >= kNaMaxRows) return na_fail(MDG_E_UNSUPPORTED, "mdg_recip_forces_noalloc: too many k rows");
+                g_na_rows[nrow] = make_int4(kl, km, first, nk - cnt);
+                g_na_nlen[nrow] = cnt;
+                for (int off = 0; off < cnt; off += kChunk) {
+                    if (nwork >= kNaMaxWork) return na_fail(MDG_E_UNSUPPORTED, "mdg_recip_forces_noalloc: too many work items");
+                    g_na_wr[nwork] = nrow;
+                    g_na_wn[nwork] = off;
+                    ++nwork;
+                }
+                ++nrow;
+            }
+            knmin = -KN;
+        }
+        kmmin = -KM;
+    }
+    if (nk == 0) return na_fail(MDG_E_ARG, "mdg_recip_forces_noalloc: empty k set");
+    const int sfac_smem = 64 * ((KL + 1 + KM + 1 + KN + 1) * (int)sizeof(double2) + (int)sizeof(double));
+    const int tile = std::max(8, std::min(64, (96 * 1024) / ((KL + 1 + KM + 1 + KN + 1) * (int)sizeof(double2) + (int)sizeof(double))));
+    const int smem1 = tile * ((KL + 1 + KM + 1 + KN + 1) * (int)sizeof(double2) + (int)sizeof(double));
+    const int smem2 = kForceNT * (KM + 1 + KN + 1) * (int)sizeof(double2);
+    (void)sfac_smem;
+    if (smem1 > 200 * 1024 || smem2 > 200 * 1024)
+        return na_fail(MDG_E_UNSUPPORTED, "mdg_recip_forces_noalloc: kmax too large for the phase tables");
+    auto ck = [](cudaError_t e) { return e == cudaSuccess; };
+    if (!ck(cudaFuncSetAttribute(k_sfac, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1)) ||
+        !ck(cudaFuncSetAttribute(k_kforce, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2)))
+        return na_fail(MDG_E_CUDA, "mdg_recip_forces_noalloc: cudaFuncSetAttribute failed");
+    double2* S = reinterpret_cast<double2*>(base + kNaS);
+    double2* C = reinterpret_cast<double2*>(base + kNaC);
+    double2* Qw = reinterpret_cast<double2*>(base + kNaQw);
+    double* Ak = reinterpret_cast<double*>(base + kNaAk);
+    int4* rows = reinterpret_cast<int4*>(base + kNaRows);
+    int* nlen = reinterpret_cast<int*>(base + kNaNlen);
+    int* wr = reinterpret_cast<int*>(base + kNaWr);
+    int* wn = reinterpret_cast<int*>(base + kNaWn);
+    double* acc = reinterpret_cast<double*>(base + kNaAcc);
+    int* status = reinterpret_cast<int*>(base + kNaStatus);
+    // the array keeps the previous call's contents: clear what the sums start from
+    bool ok = ck(cudaMemcpyAsync(Ak, g_na_ak, sizeof(double) * nk, cudaMemcpyHostToDevice, st)) &&
+              ck(cudaMemcpyAsync(rows, g_na_rows, sizeof(int4) * nrow, cudaMemcpyHostToDevice, st)) &&
+              ck(cudaMemcpyAsync(nlen, g_na_nlen, sizeof(int) * nrow, cudaMemcpyHostToDevice, st)) &&
+              ck(cudaMemcpyAsync(wr, g_na_wr, sizeof(int) * nwork, cudaMemcpyHostToDevice, st)) &&
+              ck(cudaMemcpyAsync(wn, g_na_wn, sizeof(int) * nwork, cudaMemcpyHostToDevice, st)) &&
+              ck(cudaMemsetAsync(S, 0, sizeof(double2) * nk, st)) &&
+              ck(cudaMemsetAsync(Qw, 0, sizeof(double2) * nk, st)) &&
+              ck(cudaMemsetAsync(acc, 0, sizeof(double) * 64, st)) &&
+              ck(cudaMemsetAsync(status, 0, sizeof(int) * ST_NWORDS, st)) &&
+              ck(cudaMemsetAsync(fx, 0, sizeof(double) * n, st)) && ck(cudaMemsetAsync(fy, 0, sizeof(double) * n, st)) &&
+              ck(cudaMemsetAsync(fz, 0, sizeof(double) * n, st));
+    if (!ok) return na_fail(MDG_E_CUDA, "mdg_recip_forces_noalloc: copy of the k tables failed");
+    View v{};
+    v.nmove = (int)n;
+    v.ntota = (int)n;
+    v.nijt = 0;
+    v.x = const_cast<double*>(x);
+    v.y = const_cast<double*>(y);
+    v.z = const_cast<double*>(z);
+    v.q = q;
+    v.fx = fx;
+    v.fy = fy;
+    v.fz = fz;
+    v.acc = acc;
+    v.status = status;
+    KDims d{KL, KM, KN, pipix, pipiy, pipiz};
+    const int kblocks = (nwork + kSfacNT - 1) / kSfacNT;
+    int splits = std::max(1, (152 * 4 + kblocks - 1) / std::max(kblocks, 1));
+    splits = std::min(splits, std::max(1, (int)((n + tile - 1) / tile)));
+    const int aps = (int)((n + splits - 1) / splits);
+    k_sfac<<<dim3(kblocks, splits), kSfacNT, smem1, st>>>(v, d, nrow, rows, nlen, wr, wn, nwork, tile, aps, S, nk);
+    k_kenergy<<<std::min((nk + 255) / 256, 256), 256, 0, st>>>(v, nk, Ak, S, Qw, C);
+    k_kforce<<<(int)((n + kForceNT - 1) / kForceNT), kForceNT, smem2, st>>>(v, d, nrow, rows, nlen, C, nk);
+    k_noalloc_energy<<<1, 32, 0, st>>>(acc, uewa);
+    if (cudaGetLastError() != cudaSuccess) return na_fail(MDG_E_CUDA, "mdg_recip_forces_noalloc: launch failed");
+    return MDG_OK;
 }
 
 }  // namespace mdg
