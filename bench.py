@@ -146,35 +146,56 @@ def site_pairs(s, ctx, rcut):
     return acc(li, lj, False), acc(wi, wj, True) if len(wi) else 0
 
 
+def fp32_nominal_tflops():
+    """152 SMs x 128 FP32 lanes x 2 flops x max SM clock (no measured FP32 peak on this machine)."""
+    mhz = 2070.0
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        mhz = json.load(open(p)).get("sm_max_mhz", mhz)
+    return 152 * 128 * 2 * mhz * 1e6 / 1e12
+
+
 def roofline(ctx, s, prm, precision, pk):
+    """Roofline of the dominant force phase (and of the reciprocal phase), from CUDA-event phase
+    times of mdg_phase_times and the algorithmic work per unit:
+      pair phases   45 flops per accepted site pair (FP64 pipe, or FP32 + MUFU when mixed)
+      reciprocal    18 flops per (atom, valid k) in FP64; 24 flops per (atom, valid k) for the
+                    three complex products of the tensor-core form, whose ceiling is the dense
+                    16-bit tensor peak / 3 (hi*hi + hi*lo + lo*hi)."""
     from md_sim_gb300.abi import MDG_MIXED
 
     ph = ctx.phase_times(reps=5)
-    dom = max(("pairs", "walls", "reciprocal"), key=lambda k: ph[k])
     nk = ctx_nk(s, prm)
     hh, hw = site_pairs(s, ctx, prm.rcut)
-    if dom == "reciprocal":
-        units = s.nmove * nk
-        flops = 18.0 * units
-        if precision == MDG_MIXED:
-            bound, peak, unit = "tensor", pk["bf16_tflops"], "TFLOP/s"
-        else:
-            bound, peak, unit = "fp64", FP64_NOMINAL_TFLOPS, "TFLOP/s"
-    else:
-        units = hh if dom == "pairs" else hw
-        flops = 45.0 * units
-        bound, peak, unit = "fp64", FP64_NOMINAL_TFLOPS, "TFLOP/s"
-    t = ph[dom] * 1e-3
-    achieved = flops / t / 1e12
-    traffic = None
+    mixed = precision == MDG_MIXED
     tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        traffic = json.load(open(tf)).get(f"{dom}:{'mixed' if precision == MDG_MIXED else 'fp64'}")
-    return {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak, "traffic": traffic, "kernel": dom, "ms_per_launch": ph[dom],
-            "units_per_launch": int(units), "flops_per_unit": flops / max(units, 1),
-            "peak_source": pk["source"] if bound == "tensor" else "nominal (no measured FP64 peak)",
-            "phase_ms": ph}
+    traffic_tab = json.load(open(tf)) if os.path.exists(tf) else {}
+
+    def one(kind):
+        t = ph[kind] * 1e-3
+        if kind == "reciprocal":
+            units = s.nmove * nk
+            if mixed:
+                flops, bound, peak, src = 24.0 * units, "tensor", pk["bf16_tflops"] / 3.0, pk["source"] + " /3"
+            else:
+                flops, bound, peak, src = 18.0 * units, "fp64", FP64_NOMINAL_TFLOPS, "nominal (no measured FP64 peak)"
+        else:
+            units = hh if kind == "pairs" else hw
+            flops = 45.0 * units
+            if mixed:
+                bound, peak, src = "fp32", fp32_nominal_tflops(), "nominal FP32 (152 SM x 128 lanes x 2 x max clock)"
+            else:
+                bound, peak, src = "fp64", FP64_NOMINAL_TFLOPS, "nominal (no measured FP64 peak)"
+        achieved = flops / max(t, 1e-12) / 1e12
+        return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": traffic_tab.get(f"{kind}:{'mixed' if mixed else 'fp64'}"), "kernel": kind,
+                "ms_per_launch": ph[kind], "units_per_launch": int(units), "flops_per_unit": flops / max(units, 1),
+                "peak_source": src}
+
+    dom = max(("pairs", "walls", "reciprocal"), key=lambda k: ph[k])
+    out = one(dom)
+    out["phase_ms"] = ph
+    return out, one("reciprocal")
 
 
 def ctx_nk(s, prm):
@@ -268,7 +289,7 @@ def gpu_arm(args):
     kps = ctx.kernels_per_step()
     ctx.get_state(s)
     pk = peaks()
-    roof = roofline(ctx, s, prm, precision, pk)
+    roof, roof_recip = roofline(ctx, s, prm, precision, pk)
 
     # ---------------- e2e through the drop-in ABI with pinned host buffers
     e2e = e2e_arm(lib, s, prm, args, torch)
@@ -284,6 +305,7 @@ def gpu_arm(args):
         "gpu_launches": int(kps * K),
         "kernels_per_step": kps,
         "roofline": roof,
+        "roofline_reciprocal": roof_recip,
         "clocks": clk.summary(),
         "step_report": {k: rep[k] for k in ("tempnow", "htot", "uconf", "rebuilds", "steps")},
         "step_ms_min_median_max": [min(per_step), float(np.median(per_step)), max(per_step)],

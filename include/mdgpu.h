@@ -255,6 +255,11 @@ int mdg_set_stream(mdg_ctx* ctx, void* stream);
 #define MDG_NPHASE 7
 int mdg_phase_times(mdg_ctx* ctx, int reps, double* ms);
 
+/* Diagnostic: one tcgen05 BF16 matrix product D (128 x n) = A (128 x k) . B^T (n x k) on the
+ * device with the shared-memory operand layout of the tensor-core reciprocal sum (host arrays,
+ * row-major floats rounded to BF16).  Lets a caller check the tensor-core path on its GPU. */
+int mdg_selftest_umma(int n, int k, const float* a, const float* b, float* d);
+
 /* ---------------------------------------------------------------------------------------------
  * Allocation-free reciprocal sum.  This entry point has no counterpart in the reference: it is
  * offered to callers that must not allocate device memory while they run (a host that sized its

@@ -22,7 +22,8 @@ enum StatusWord {
     ST_REBUILD = 5,    // 1 when the current step rebuilt the list
     ST_SWEEPS = 6,     // SHAKE sweeps of the last call
     ST_OOB = 7,        // debug builds: tag of the first out-of-range index seen
-    ST_NWORDS = 8
+    ST_TC_TIMEOUT = 8, // a tensor-core phase gave up waiting on an mbarrier (tag of the wait)
+    ST_NWORDS = 12
 };
 
 // Debug builds (-DMDG_DEBUG_BOUNDS) check indices on the force path: an index outside [0, n)

@@ -105,11 +105,22 @@ struct KSet {
     int nwork = 0, tile = 0, splits = 1, atoms_per_split = 0, sfac_smem = 0, force_smem = 0;
 };
 
+// Launch plan of the tensor-core reciprocal sum (recip_tc.cu).
+struct TcPlan {
+    bool ready = false;
+    int KN = 0, NN = 0, NP = 0, KS = 0;
+    int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, smem1 = 0, smem2 = 0;
+};
+
 struct Ctx {
     mdg_sysdesc sysc;   // sizes only (pointers not kept)
     View v{};
     Grid grid{}, wgrid{};
     KSet ks;
+    TcPlan tcp;
+    uint4* d_tc_atoms = nullptr;        // fixed-point phases + charge per moving atom
+    unsigned char* d_tc_img = nullptr;  // packed C(k) operand chunks
+    float* d_tc_cmax = nullptr;         // scale of the packed C(k) operand
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the context's stream while a caller's stream is in use
     int device = 0;
@@ -182,6 +193,11 @@ int recip_forces_noalloc(const double* x, const double* y, const double* z, cons
                          double lx, double ly, double lz, double alpha, int64_t kmax, double* fx, double* fy,
                          double* fz, double* uewa, cudaStream_t st);
 const char* recip_noalloc_error();
+void recip_energy_launch(Ctx& c);
+// recip_tc.cu
+int recip_tc_setup(Ctx& c);
+void recip_tc(Ctx& c);
+int umma_selftest(int n, int k, const float* a, const float* b, float* d, std::string& err);
 // epilogue.cu
 void dipole_correction(Ctx& c);
 void angle_forces(Ctx& c);

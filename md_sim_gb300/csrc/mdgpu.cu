@@ -184,7 +184,14 @@ int sync_check(Ctx& c, const char* where) {
 
 int read_status(Ctx& c) {
     MDG_CUDA(cudaMemcpyAsync(c.h_status, c.v.status, sizeof(int) * ST_NWORDS, cudaMemcpyDeviceToHost, c.stream));
-    return sync_check(c, "status");
+    int rc = sync_check(c, "status");
+    if (rc) return rc;
+    if (c.h_status[ST_TC_TIMEOUT]) {
+        char b[128];
+        snprintf(b, sizeof b, "tensor-core reciprocal phase timed out waiting (site %d)", c.h_status[ST_TC_TIMEOUT]);
+        return set_err(&c, MDG_E_CUDA, b);
+    }
+    return MDG_OK;
 }
 
 // Debug runs (MDG_DEBUG_SYNC=1 in the environment at mdg_create): synchronise after every
@@ -231,7 +238,11 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
         PHASE(wall_forces_fp64(c), "walls");
     }
     PHASE(lr_tail(c), "lr_tail");
-    PHASE(recip_fp64(c), "reciprocal");
+    if (c.precision == MDG_MIXED) {
+        PHASE(recip_tc(c), "reciprocal");
+    } else {
+        PHASE(recip_fp64(c), "reciprocal");
+    }
     PHASE(dipole_correction(c), "dipole");
     PHASE(angle_forces(c), "angles");
     PHASE(force_sum(c, c.d_ft, c.d_fc, c.d_tq), "force_sum");
@@ -459,6 +470,10 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
     c.uself = self_energy(s, x0, y0, z0, v.alfa, v.facq, v.spii);
     int rc = recip_setup(c, p->kmax, x0, y0, z0);
     if (rc) return bail(rc);
+    if (c.precision == MDG_MIXED) {
+        rc = recip_tc_setup(c);
+        if (rc) return bail(rc);
+    }
     rc = nnlist_setup(c, x0, y0, z0);
     if (rc) return bail(rc);
     rc = shake_setup(c, s);
@@ -1076,7 +1091,8 @@ int mdg_phase_times(mdg_ctx* cp, int reps, double* ms) {
         if (c.precision == MDG_MIXED) wall_forces_fp32(c);
         else wall_forces_fp64(c);
         cudaEventRecord(ev[3], c.stream);
-        recip_fp64(c);
+        if (c.precision == MDG_MIXED) recip_tc(c);
+        else recip_fp64(c);
         cudaEventRecord(ev[4], c.stream);
         lr_tail(c);
         dipole_correction(c);
@@ -1108,6 +1124,13 @@ int mdg_recip_forces_noalloc(const double* x, const double* y, const double* z, 
                              double* fz, double* uewa, void* stream) {
     const int rc = recip_forces_noalloc(x, y, z, q, n, lx, ly, lz, alpha, kmax, fx, fy, fz, uewa, (cudaStream_t)stream);
     if (rc) g_err = recip_noalloc_error();
+    return rc;
+}
+
+int mdg_selftest_umma(int n, int k, const float* a, const float* b, float* d) {
+    std::string err;
+    const int rc = umma_selftest(n, k, a, b, d, err);
+    if (rc) g_err = err;
     return rc;
 }
 

@@ -147,10 +147,12 @@ __device__ __forceinline__ float fmin_img(float d, float l, float li, int period
     return periodic ? d - l * rintf(d * li) : d;
 }
 
-// One thread per head: scan neighbouring cells, keep partners j > i.
+// One warp per head: the warp walks the neighbouring cells, lanes test 32 candidates at a time
+// and the kept partners (j > i) are appended in order with a ballot.
 __global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* cpos, const double4* hpos) {
     if (!v.status[ST_REBUILD]) return;
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (h >= v.nheads) return;
     const int ia = v.head_atom[h];
     const double4 pw = hpos[h];
@@ -173,30 +175,42 @@ __global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* 
             for (int dx = -rx; dx <= rx; ++dx) {
                 const int xx = (cx + dx + g.nc[0]) % g.nc[0];
                 const int c = (zz * g.nc[1] + yy) * g.nc[0] + xx;
-                for (int s = cell_start[c]; s < cell_start[c + 1]; ++s) {
-                    const float4 q = cpos[s];
-                    const int ja = __float_as_int(q.w);
-                    if (ja <= ia) continue;
-                    float ddx = fmin_img(px - q.x, lxf, lxif, 1);
-                    float ddy = fmin_img(py - q.y, lyf, lyif, 1);
-                    float ddz = fmin_img(pz - q.z, lzf, lzif, g.periodic[2]);
-                    if (ddx * ddx + ddy * ddy + ddz * ddz > lim) continue;
-                    if (surf_i && ja >= v.nliqa && excluded(v, ia, ja)) continue;
-                    if (!keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja])) continue;
-                    if (cnt < v.maxnb) out[cnt] = ja;
-                    ++cnt;
+                const int s1 = cell_start[c + 1];
+                for (int base = cell_start[c]; base < s1; base += 32) {
+                    const int s = base + lane;
+                    bool keep = false;
+                    int ja = 0;
+                    if (s < s1) {
+                        const float4 q = cpos[s];
+                        ja = __float_as_int(q.w);
+                        if (ja > ia) {
+                            const float ddx = fmin_img(px - q.x, lxf, lxif, 1);
+                            const float ddy = fmin_img(py - q.y, lyf, lyif, 1);
+                            const float ddz = fmin_img(pz - q.z, lzf, lzif, g.periodic[2]);
+                            keep = ddx * ddx + ddy * ddy + ddz * ddz <= lim;
+                            if (keep && surf_i && ja >= v.nliqa && excluded(v, ia, ja)) keep = false;
+                            if (keep) keep = keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja]);
+                        }
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, keep);
+                    const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                    if (keep && pos < v.maxnb) out[pos] = ja;
+                    cnt += __popc(m);
                 }
             }
         }
     }
-    if (cnt > v.maxnb) atomicMax(&v.status[ST_LIST_OVF], cnt);
-    v.nbcnt[h] = min(cnt, v.maxnb);
+    if (lane == 0) {
+        if (cnt > v.maxnb) atomicMax(&v.status[ST_LIST_OVF], cnt);
+        v.nbcnt[h] = min(cnt, v.maxnb);
+    }
 }
 
-// One thread per head: all wall atoms within rskin (src/nnlist.f90:143-161).
+// One warp per head: all wall atoms within rskin (src/nnlist.f90:143-161).
 __global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4* wpos, const double4* hpos) {
     if (!v.status[ST_REBUILD]) return;
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (h >= v.nheads) return;
     const int ia = v.head_atom[h];
     const double xi = v.x[ia], yi = v.y[ia], zi = v.z[ia];
@@ -220,23 +234,33 @@ __global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4*
             for (int dx = -rx; dx <= rx; ++dx) {
                 const int xx = (cx + dx + g.nc[0]) % g.nc[0];
                 const int c = (zz * g.nc[1] + yy) * g.nc[0] + xx;
-                for (int s = wcell_start[c]; s < wcell_start[c + 1]; ++s) {
-                    const float4 q = wpos[s];
-                    const int ja = __float_as_int(q.w);
-                    float ddx = fmin_img(px - q.x, lxf, lxif, 1);
-                    float ddy = fmin_img(py - q.y, lyf, lyif, 1);
-                    float ddz = fmin_img(pz - q.z, lzf, lzif, g.periodic[2]);
-                    if (ddx * ddx + ddy * ddy + ddz * ddz > lim) continue;
-                    if (surf_i && excluded(v, ia, ja)) continue;
-                    if (!keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja])) continue;
-                    if (cnt < v.maxwnb) out[cnt] = ja;
-                    ++cnt;
+                const int s1 = wcell_start[c + 1];
+                for (int base = wcell_start[c]; base < s1; base += 32) {
+                    const int s = base + lane;
+                    bool keep = false;
+                    int ja = 0;
+                    if (s < s1) {
+                        const float4 q = wpos[s];
+                        ja = __float_as_int(q.w);
+                        const float ddx = fmin_img(px - q.x, lxf, lxif, 1);
+                        const float ddy = fmin_img(py - q.y, lyf, lyif, 1);
+                        const float ddz = fmin_img(pz - q.z, lzf, lzif, g.periodic[2]);
+                        keep = ddx * ddx + ddy * ddy + ddz * ddz <= lim;
+                        if (keep && surf_i && excluded(v, ia, ja)) keep = false;
+                        if (keep) keep = keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja]);
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, keep);
+                    const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                    if (keep && pos < v.maxwnb) out[pos] = ja;
+                    cnt += __popc(m);
                 }
             }
         }
     }
-    if (cnt > v.maxwnb) atomicMax(&v.status[ST_WLIST_OVF], cnt);
-    v.wnbcnt[h] = min(cnt, v.maxwnb);
+    if (lane == 0) {
+        if (cnt > v.maxwnb) atomicMax(&v.status[ST_WLIST_OVF], cnt);
+        v.wnbcnt[h] = min(cnt, v.maxwnb);
+    }
 }
 
 Grid make_grid(double lx, double ly, double lz, double rs, int pz, double zlo, double zhi) {
@@ -342,9 +366,8 @@ void nnlist_build(Ctx& c) {
     k_scan_cells<<<1, kNT, 0, c.stream>>>(v, g.ncell, c.d_cell_count, c.d_cell_start);
     k_scatter_heads<<<(nh + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, c.d_head_cell, c.d_cell_count, c.d_cell_start,
                                                                  c.d_hpos, c.d_cpos);
-    k_build_hh<<<(nh + 127) / 128, 128, 0, c.stream>>>(v, g, c.d_cell_start, c.d_cpos, c.d_hpos);
-    if (v.nwall > 0)
-        k_build_hw<<<(nh + 127) / 128, 128, 0, c.stream>>>(v, c.wgrid, c.d_wcell_start, c.d_wpos, c.d_hpos);
+    k_build_hh<<<(nh + 3) / 4, 128, 0, c.stream>>>(v, g, c.d_cell_start, c.d_cpos, c.d_hpos);
+    if (v.nwall > 0) k_build_hw<<<(nh + 3) / 4, 128, 0, c.stream>>>(v, c.wgrid, c.d_wcell_start, c.d_wpos, c.d_hpos);
 }
 
 }  // namespace mdg

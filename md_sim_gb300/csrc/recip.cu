@@ -334,6 +334,11 @@ int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const 
     return MDG_OK;
 }
 
+void recip_energy_launch(Ctx& c) {
+    KSet& ks = c.ks;
+    k_kenergy<<<std::min((ks.nk + 255) / 256, 256), 256, 0, c.stream>>>(c.v, ks.nk, ks.ak, ks.s, ks.qw, ks.c);
+}
+
 void recip_fp64(Ctx& c) {
     const View& v = c.v;
     KSet& ks = c.ks;
