@@ -268,28 +268,26 @@ def gpu_arm(args):
     ctx = abi.Context(lib, s, prm)
     ctx.set_stream(stream.cuda_stream)
     configs.equilibrate(ctx, s, steps=args.equil, every=20)
+    s_start = s.copy()
     ctx.set_state(s)
     ctx.run(args.warmup)
-    rep0 = ctx.run(1)
     K = args.steps
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    torch.cuda.synchronize()
     with ClockSampler() as clk:
-        with torch.cuda.stream(stream):
-            for k in range(K):
-                flush.zero_()
-                ev[k][0].record(stream)
-                ctx.run_async(1)
-                ev[k][1].record(stream)
-        stream.synchronize()
+        per_step = time_resident(ctx, K, stream, flush, torch)
     rep = ctx.check()
-    per_step = [a.elapsed_time(b) for a, b in ev]
     t_step = float(np.sum(per_step)) / K * 1e-3
     value = ns_per_day(t_step, s.dt)
     kps = ctx.kernels_per_step()
     ctx.get_state(s)
     pk = peaks()
     roof, roof_recip = roofline(ctx, s, prm, precision, pk)
+    ctx.close()
+
+    # ---------------- the plain FP64 GPU form on the same start, and the force error against it
+    cmp64 = None
+    if precision == MDG_MIXED and args.fp64_steps > 0:
+        cmp64 = fp64_compare(lib, s_start, prm, args, stream, flush, torch)
+        cmp64["speedup"] = value / cmp64["value"]
 
     # ---------------- e2e through the drop-in ABI with pinned host buffers
     e2e = e2e_arm(lib, s, prm, args, torch)
@@ -310,12 +308,64 @@ def gpu_arm(args):
         "step_report": {k: rep[k] for k in ("tempnow", "htot", "uconf", "rebuilds", "steps")},
         "step_ms_min_median_max": [min(per_step), float(np.median(per_step)), max(per_step)],
     }
+    if cmp64 is not None:
+        out["fp64_gpu"] = cmp64
     if args.cpu_baseline:
         v, dt, n = cpu_reference(s, prm, args.cpu_steps)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                "sample": f"{n} MD steps of the same workload after one untimed step "
                                          f"({dt * 1e3:.2f} ms/step), OpenMP over all host cores"}
     return out
+
+
+def time_resident(ctx, K, stream, flush, torch):
+    """K resident steps, each bracketed by CUDA events on the library stream, L2 flushed between."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(K):
+            flush.zero_()
+            ev[k][0].record(stream)
+            ctx.run_async(1)
+            ev[k][1].record(stream)
+    stream.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def fp64_compare(lib, s_start, prm, args, stream, flush, torch):
+    """Plain FP64 GPU form from the same equilibrated start (same step count, same timing), and
+    the mixed form's force / energy / virial error against FP64 on that configuration."""
+    import dataclasses
+
+    from md_sim_gb300 import abi
+    from md_sim_gb300.abi import MDG_FP64
+
+    p64 = dataclasses.replace(prm, precision=MDG_FP64)
+    # force error on the equilibrated configuration (site forces of all moving atoms)
+    fm = abi.Context(lib, s_start.copy(), prm)
+    f64 = abi.Context(lib, s_start.copy(), p64)
+    em, e64 = fm.force_get(s_start.copy()), f64.force_get(s_start.copy())
+    fm.close()
+    f64.close()
+    d = em["f"] - e64["f"]
+    err = {
+        "dF_rms_rel": float(np.linalg.norm(d) / np.linalg.norm(e64["f"])),
+        "dF_max_abs": float(np.abs(d).max()),
+        "uconf_rel": float(abs(em["uconf"] - e64["uconf"]) / abs(e64["uconf"])),
+        "uewa_rel": float(abs(em["uewa"] - e64["uewa"]) / max(abs(e64["uewa"]), 1e-300)),
+        "vir_rel": float(abs(em["vir"] - e64["vir"]) / max(abs(e64["vir"]), 1e-300)),
+    }
+    s = s_start.copy()
+    ctx = abi.Context(lib, s, p64)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_state(s)
+    ctx.run(args.warmup)
+    K = min(args.steps, args.fp64_steps)
+    per_step = time_resident(ctx, K, stream, flush, torch)
+    ctx.close()
+    t = float(np.sum(per_step)) / K * 1e-3
+    return {"value": ns_per_day(t, s.dt), "unit": UNIT, "ms_per_step": t * 1e3, "steps": K,
+            "error_vs_fp64": err}
 
 
 def e2e_arm(lib, s, prm, args, torch):
@@ -430,11 +480,13 @@ def profile_run(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="slab2048", choices=["slab2048", "bulk256", "bulk32k", "shake8k"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--fp64-steps", type=int, default=200,
+                    help="steps of the plain FP64 GPU comparison arm (0 = skip)")
     ap.add_argument("--equil", type=int, default=200)
     ap.add_argument("--e2e-steps", type=int, default=60)
     ap.add_argument("--cpu-steps", type=int, default=3)

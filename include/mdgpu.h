@@ -255,6 +255,29 @@ int mdg_set_stream(mdg_ctx* ctx, void* stream);
 #define MDG_NPHASE 7
 int mdg_phase_times(mdg_ctx* ctx, int reps, double* ms);
 
+/* ---------------------------------------------------------------------------------------------
+ * Learned SHAKE seed.  A small network (9 -> 64 -> 64 -> 3, SiLU) maps rotation-invariant features
+ * of a 3-constraint molecule's unconstrained and previous bond vectors to the multipliers that
+ * SHAKE accumulates for it; the prediction is applied as one SHAKE-type correction before the
+ * sweeps, which then iterate to the unchanged tolerance.  Parameters are a float blob of
+ * mdg_mlp_nw() values (weights used rounded to BF16, FP32 accumulation).
+ * ------------------------------------------------------------------------------------------- */
+int mdg_mlp_nw(void);
+/* Seeds every later SHAKE step of the context with the network w (n = mdg_mlp_nw()); n = 0 stops. */
+int mdg_shake_set_model(mdg_ctx* ctx, const float* w, int64_t n);
+/* enable != 0: each SHAKE step records per constrained molecule 16 floats: 9 features, the 3
+ * accumulated multipliers (scaled by the summed inverse masses of each constraint), the sweeps
+ * it took, 3 zeros; mdg_shake_samples copies the last step's ncons x 16. */
+int mdg_shake_record(mdg_ctx* ctx, int enable);
+int mdg_shake_samples(mdg_ctx* ctx, float* out);
+/* Network training and evaluation on the GPU (host arrays in and out): x is n x 9, y is n x 3.
+ * mdg_mlp_train runs Adam (cosine learning-rate decay) from a seeded start and returns the blob
+ * (with the input/output normalisation it computed) and the mean loss of each epoch. */
+int mdg_mlp_forward(const float* w, const float* x, int64_t n, float* y);
+int mdg_mlp_grad(const float* w, const float* x, const float* y, int64_t n, float* grad, float* loss);
+int mdg_mlp_train(const float* x, const float* y, int64_t n, int epochs, int batch, float lr, uint64_t seed,
+                  float* w_out, float* loss_out);
+
 /* Diagnostic: one tcgen05 BF16 matrix product D (128 x n) = A (128 x k) . B^T (n x k) on the
  * device with the shared-memory operand layout of the tensor-core reciprocal sum (host arrays,
  * row-major floats rounded to BF16).  Lets a caller check the tensor-core path on its GPU. */

@@ -170,6 +170,15 @@ class Lib:
             g("run_async", C.c_int, [C.c_void_p, C.c_int64])
             g("check", C.c_int, [C.c_void_p, C.POINTER(Report)])
             g("kernels_per_step", C.c_int64, [C.c_void_p])
+        if self.has("mlp_nw"):
+            FP = C.POINTER(C.c_float)
+            g("mlp_nw", C.c_int, [])
+            g("shake_set_model", C.c_int, [C.c_void_p, FP, C.c_int64])
+            g("shake_record", C.c_int, [C.c_void_p, C.c_int])
+            g("shake_samples", C.c_int, [C.c_void_p, FP])
+            g("mlp_forward", C.c_int, [FP, FP, C.c_int64, FP])
+            g("mlp_grad", C.c_int, [FP, FP, FP, C.c_int64, FP, FP])
+            g("mlp_train", C.c_int, [FP, FP, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, FP, FP])
         if self.has("run"):
             g("set_state", C.c_int, [C.c_void_p, C.POINTER(Rigid), C.POINTER(State)])
             g("get_state", C.c_int, [C.c_void_p, C.POINTER(State)])
@@ -412,3 +421,32 @@ def _ctx_kernels_per_step(self) -> int:
 Context.run_async = _ctx_run_async
 Context.check = _ctx_check
 Context.kernels_per_step = _ctx_kernels_per_step
+
+
+def _fp(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _ctx_set_shake_model(self, w: Optional[np.ndarray]):
+    """Seed SHAKE with the network blob w (float32, mdg_mlp_nw() values); None stops seeding."""
+    if w is None:
+        self._check(self.lib.shake_set_model(self.h, None, 0))
+        return
+    self._mlpw = np.ascontiguousarray(w, dtype=np.float32)
+    self._check(self.lib.shake_set_model(self.h, _fp(self._mlpw), self._mlpw.size))
+
+
+def _ctx_shake_record(self, enable: bool = True):
+    self._check(self.lib.shake_record(self.h, 1 if enable else 0))
+
+
+def _ctx_shake_samples(self) -> np.ndarray:
+    """(ncons, 16) float32: features[9], multipliers[3], sweeps, 0, 0, 0 of the last SHAKE step."""
+    out = np.zeros((max(self.sys.ncons, 1), 16), np.float32)
+    self._check(self.lib.shake_samples(self.h, _fp(out)))
+    return out[: self.sys.ncons]
+
+
+Context.set_shake_model = _ctx_set_shake_model
+Context.shake_record = _ctx_shake_record
+Context.shake_samples = _ctx_shake_samples

@@ -105,6 +105,16 @@ struct KSet {
     int nwork = 0, tile = 0, splits = 1, atoms_per_split = 0, sfac_smem = 0, force_smem = 0;
 };
 
+// Per-step packed atom records of the mixed-precision real-space kernels (pair_mx.cu).
+struct Pk {
+    uint4* P = nullptr;     // fixed-point x, y (z if periodic) | FP32 z hi; w = type | sign(z) << 31
+    float4* Q = nullptr;    // rs offset, charge
+    float* zlo = nullptr;   // z - z_hi when z is not periodic
+    float4* F = nullptr;    // j-side force accumulator (moving atoms)
+    float sx = 0, sy = 0, sz = 0;  // box edge / 2^32
+    int zper = 0;
+};
+
 // Launch plan of the tensor-core reciprocal sum (recip_tc.cu).
 struct TcPlan {
     bool ready = false;
@@ -118,6 +128,7 @@ struct Ctx {
     Grid grid{}, wgrid{};
     KSet ks;
     TcPlan tcp;
+    Pk pk;
     uint4* d_tc_atoms = nullptr;        // fixed-point phases + charge per moving atom
     unsigned char* d_tc_img = nullptr;  // packed C(k) operand chunks
     float* d_tc_cmax = nullptr;         // scale of the packed C(k) operand
@@ -149,6 +160,9 @@ struct Ctx {
     double* d_ft_in = nullptr;    // 3 x (nmove - nriga) forces handed to SHAKE
     int* d_sweeps = nullptr;      // [0] sweeps, [1] done
     int* d_seq_flags = nullptr;   // moving/moved of the sequential SHAKE
+    float* d_mlpw = nullptr;      // SHAKE-seeding network parameters
+    float* d_shake_rec = nullptr; // ncons x 12 recorded features / multipliers
+    bool shake_model = false, shake_record = false;
     int64_t nfreed = 0;
     // angles
     int nang_terms = 0;
@@ -184,8 +198,10 @@ void pair_forces_fp64(Ctx& c);
 void wall_forces_fp64(Ctx& c);
 void surf_partition(Ctx& c);
 void lr_tail(Ctx& c);
-void pair_forces_fp32(Ctx& c);
-void wall_forces_fp32(Ctx& c);
+// pair_mx.cu
+void pack_setup(Ctx& c);
+void real_space_mixed(Ctx& c);   // pack, head-head pairs, j-side merge
+void wall_forces_mixed(Ctx& c);
 // recip.cu
 int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const double* z0);
 void recip_fp64(Ctx& c);
@@ -198,6 +214,12 @@ void recip_energy_launch(Ctx& c);
 int recip_tc_setup(Ctx& c);
 void recip_tc(Ctx& c);
 int umma_selftest(int n, int k, const float* a, const float* b, float* d, std::string& err);
+// mlp.cu
+int mlp_nw();
+int mlp_forward_host(const float* w, const float* X, int64_t n, float* Y, std::string& err);
+int mlp_grad_host(const float* w, const float* X, const float* Y, int64_t n, float* grad, float* loss, std::string& err);
+int mlp_train_host(const float* X, const float* Y, int64_t n, int epochs, int batch, float lr, uint64_t seed,
+                   float* w_out, float* loss_out, std::string& err);
 // epilogue.cu
 void dipole_correction(Ctx& c);
 void angle_forces(Ctx& c);

@@ -15,7 +15,7 @@ namespace mdg {
 
 namespace {
 
-constexpr int kNT = 256;
+constexpr int kNT = 64;
 
 __global__ void k_dipz(View v) {
     double s = 0.0;
@@ -114,7 +114,7 @@ void dipole_correction(Ctx& c) {
     if (c.variant != MDG_SLAB || v.nmove == 0) return;
     const double pi_r = (double)3.1415926535898f;
     const double crf0 = -2.0 * pi_r * v.lzi * v.lxi * v.lyi;
-    const int nb = std::min((v.nmove + kNT - 1) / kNT, 152);
+    const int nb = std::min((v.nmove + kNT - 1) / kNT, 152 * 8);
     k_dipz<<<nb, kNT, 0, c.stream>>>(v);
     k_dipforce<<<nb, kNT, 0, c.stream>>>(v, crf0);
 }
@@ -129,7 +129,7 @@ void angle_forces(Ctx& c) {
 void force_sum(Ctx& c, double* d_ft, double* d_fc, double* d_tq) {
     const View& v = c.v;
     const int n = std::max(v.nmove, v.nrig);
-    const int nb = std::max(1, std::min((n + kNT - 1) / kNT, 152 * 2));
+    const int nb = std::max(1, std::min((n + kNT - 1) / kNT, 152 * 8));
     k_force_sum<<<nb, kNT, 0, c.stream>>>(v, d_ft, d_fc, d_tq);
 }
 

@@ -19,7 +19,7 @@ namespace mdg {
 
 namespace {
 
-constexpr int kNT = 256;
+constexpr int kNT = 32;
 
 constexpr double Gf01 = F32D(0.348611111), Gf11 = 1.0, Gf21 = F32D(0.916666667), Gf31 = F32D(0.333333333),
                  Gf41 = F32D(0.041666667);
@@ -313,7 +313,7 @@ Dyn dyn_of(Ctx& c) {
     return D;
 }
 
-int nblk(int n) { return std::max(1, std::min((n + kNT - 1) / kNT, 152 * 4)); }
+int nblk(int n) { return std::max(1, std::min((n + kNT - 1) / kNT, 152 * 16)); }
 
 }  // namespace
 

@@ -229,9 +229,9 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
     PHASE(nnlist_trigger(c, force_rebuild), "trigger");
     PHASE(nnlist_build(c), "nnlist");
     if (c.precision == MDG_MIXED) {
-        PHASE(pair_forces_fp32(c), "pairs");
+        PHASE(real_space_mixed(c), "pairs");
         PHASE(surf_partition(c), "surf_partition");
-        PHASE(wall_forces_fp32(c), "walls");
+        PHASE(wall_forces_mixed(c), "walls");
     } else {
         PHASE(pair_forces_fp64(c), "pairs");
         PHASE(surf_partition(c), "surf_partition");
@@ -473,6 +473,7 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
     if (c.precision == MDG_MIXED) {
         rc = recip_tc_setup(c);
         if (rc) return bail(rc);
+        pack_setup(c);
     }
     rc = nnlist_setup(c, x0, y0, z0);
     if (rc) return bail(rc);
@@ -1084,11 +1085,11 @@ int mdg_phase_times(mdg_ctx* cp, int reps, double* ms) {
         nnlist_trigger(c, true);
         nnlist_build(c);
         cudaEventRecord(ev[1], c.stream);
-        if (c.precision == MDG_MIXED) pair_forces_fp32(c);
+        if (c.precision == MDG_MIXED) real_space_mixed(c);
         else pair_forces_fp64(c);
         surf_partition(c);
         cudaEventRecord(ev[2], c.stream);
-        if (c.precision == MDG_MIXED) wall_forces_fp32(c);
+        if (c.precision == MDG_MIXED) wall_forces_mixed(c);
         else wall_forces_fp64(c);
         cudaEventRecord(ev[3], c.stream);
         if (c.precision == MDG_MIXED) recip_tc(c);
@@ -1130,6 +1131,72 @@ int mdg_recip_forces_noalloc(const double* x, const double* y, const double* z, 
 int mdg_selftest_umma(int n, int k, const float* a, const float* b, float* d) {
     std::string err;
     const int rc = umma_selftest(n, k, a, b, d, err);
+    if (rc) g_err = err;
+    return rc;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Learned SHAKE seed
+// ---------------------------------------------------------------------------------------------
+int mdg_mlp_nw(void) { return mlp_nw(); }
+
+int mdg_shake_set_model(mdg_ctx* cp, const float* w, int64_t n) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    if (n == 0 || !w) {
+        c.shake_model = false;
+    } else {
+        if (n != mlp_nw()) return set_err(&c, MDG_E_ARG, "mdg_shake_set_model: parameter count differs from mdg_mlp_nw()");
+        MDG_CUDA(cudaStreamSynchronize(c.stream));
+        MDG_CUDA(cudaMemcpy(c.d_mlpw, w, sizeof(float) * n, cudaMemcpyHostToDevice));
+        c.shake_model = true;
+    }
+    if (c.graph_exec) {
+        cudaGraphExecDestroy(c.graph_exec);
+        c.graph_exec = nullptr;
+    }
+    return MDG_OK;
+}
+
+int mdg_shake_record(mdg_ctx* cp, int enable) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    c.shake_record = enable != 0;
+    if (c.graph_exec) {
+        cudaGraphExecDestroy(c.graph_exec);
+        c.graph_exec = nullptr;
+    }
+    return MDG_OK;
+}
+
+int mdg_shake_samples(mdg_ctx* cp, float* out) {
+    if (!cp || !out) return set_err(cp, MDG_E_ARG, "null argument");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    MDG_CUDA(cudaMemcpy(out, c.d_shake_rec, sizeof(float) * 16 * c.ncons, cudaMemcpyDeviceToHost));
+    return MDG_OK;
+}
+
+int mdg_mlp_forward(const float* w, const float* x, int64_t n, float* y) {
+    std::string err;
+    const int rc = mlp_forward_host(w, x, n, y, err);
+    if (rc) g_err = err;
+    return rc;
+}
+
+int mdg_mlp_grad(const float* w, const float* x, const float* y, int64_t n, float* grad, float* loss) {
+    std::string err;
+    const int rc = mlp_grad_host(w, x, y, n, grad, loss, err);
+    if (rc) g_err = err;
+    return rc;
+}
+
+int mdg_mlp_train(const float* x, const float* y, int64_t n, int epochs, int batch, float lr, uint64_t seed,
+                  float* w_out, float* loss_out) {
+    std::string err;
+    const int rc = mlp_train_host(x, y, n, epochs, batch, lr, seed, w_out, loss_out, err);
     if (rc) g_err = err;
     return rc;
 }

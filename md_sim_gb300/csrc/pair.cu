@@ -287,7 +287,9 @@ __global__ void k_surf_part(View v) {
     block_atomic_sum<kNT>(hi, &v.acc[2 * v.nijt + ACC_FWS + 6 + 2]);
 }
 
-// Wall long-range tail, src/forcem.f90:509-543.  lr: [9][nit] tables.
+// Wall long-range tail, src/forcem.f90:509-543.  lr: [9][nit] tables.  Small blocks: the
+// per-atom FP64 work is spread over as many SMs as the atom count allows.
+constexpr int kLrNT = 64;
 __global__ void k_lr_tail(View v, const double* lr) {
     double ulr = 0.0, fw[2] = {0.0, 0.0};
     const int nit = v.nit;
@@ -320,264 +322,9 @@ __global__ void k_lr_tail(View v, const double* lr) {
         }
         v.fz[i] = fz;
     }
-    block_atomic_sum<kNT>(ulr, &v.acc[2 * v.nijt + ACC_ULR]);
-    block_atomic_sum<kNT>(fw[0], &v.acc[2 * v.nijt + ACC_FWS + 6 + 0]);
-    block_atomic_sum<kNT>(fw[1], &v.acc[2 * v.nijt + ACC_FWS + 6 + 2]);
-}
-
-// ---------------------------------------------------------------------------------------------
-// Mixed precision (FP32 arithmetic, FP64 accumulation).  The head-head vector is formed in FP64
-// from the unwrapped coordinates (up to ~100 A) and only then rounded to FP32; erfc, exp and the
-// site sub-loop run in FP32 with fast intrinsics; i-side sums are Kahan-compensated FP32 in
-// registers, j-side contributions go to the FP64 force arrays by atomics.
-// ---------------------------------------------------------------------------------------------
-constexpr float kA1f = 0.254829592f, kA2f = -0.284496736f, kA3f = 1.421413741f, kA4f = -1.453152027f,
-                kA5f = 1.061405429f, kPf = 0.3275911f;
-
-struct Kahan {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float x) {
-        const float y = x - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-
-__device__ __forceinline__ float ewald_erfc_f(float alfar, float* ff, float spii) {
-    const float t = __frcp_rn(1.0f + kPf * alfar);
-    const float exp2a = __expf(-alfar * alfar);
-    const float erfx = ((((kA5f * t + kA4f) * t + kA3f) * t + kA2f) * t + kA1f) * t * exp2a;
-    *ff = spii * alfar * exp2a + erfx;
-    return erfx;
-}
-
-__global__ void __launch_bounds__(kNT) k_pair_fp32(View v) {
-    extern __shared__ double s_e[];
-    for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x) s_e[k] = 0.0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const int nwarps = gridDim.x * kWarps;
-    const float alfa = (float)v.alfa, spii = (float)v.spii, facq = (float)v.facq, rcutsq = (float)v.rcutsq;
-    EAcc e;
-    for (int h = warp; h < v.nheads; h += nwarps) {
-        const int i = v.head_atom[h];
-        const int it = v.type[i];
-        const int nsi_i = v.nsi[it];
-        const double xi0 = v.x[i], yi0 = v.y[i], zi0 = v.z[i];
-        float rix[3], riy[3], riz[3], qi[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const bool ok = a < nsi_i;
-            rix[a] = ok ? (float)v.rsx[i + a] : 0.f;
-            riy[a] = ok ? (float)v.rsy[i + a] : 0.f;
-            riz[a] = ok ? (float)v.rsz[i + a] : 0.f;
-            qi[a] = ok ? (float)v.q[i + a] : 0.f;
-        }
-        Kahan fix[3], fiy[3], fiz[3];
-        const int n = v.nbcnt[h];
-        const int* nb = v.nb + (size_t)h * v.maxnb;
-        for (int k = lane; k < n; k += 32) {
-            const int j = nb[k];
-            const float xio = (float)minimg(xi0 - v.x[j], v.lx, v.lxi);
-            const float yio = (float)minimg(yi0 - v.y[j], v.ly, v.lyi);
-            double zd64 = zi0 - v.z[j];
-            if (v.bulk) zd64 = minimg(zd64, v.lz, v.lzi);
-            const float zio = (float)zd64;
-            const float rsq = xio * xio + yio * yio + zio * zio;
-            if (rsq > rcutsq) continue;
-            const int jt = v.type[j];
-            const int ijt = v.ijt[it * v.nit + jt];
-            const int nsi_j = v.nsi[jt];
-            const float rinv = rsqrtf(rsq);
-            const float rsqi = rinv * rinv;
-            const float rij = rsq * rinv;
-            float fij = 0.f, elj = 0.f;
-            const int vk = v.vdw[ijt];
-            if (vk == 1) {
-                const float r6 = (float)v.sig[ijt] * (rsqi * rsqi * rsqi);
-                const float ep = (float)v.eps[ijt];
-                elj = ep * r6 * (r6 - 1.0f);
-                fij = 6.0f * rsqi * ep * r6 * (2.0f * r6 - 1.0f);
-            } else if (vk == 2) {
-                const float r6 = (float)v.cc[ijt] * (rsqi * rsqi * rsqi);
-                const float rh = (float)v.rhoi[ijt];
-                const float aux = (float)v.aa[ijt] * __expf(-rij * rh);
-                elj = aux - r6;
-                fij = aux * rh * rinv - 6.0f * rsqi * r6;
-            }
-            float ff;
-            const float auxq = facq * qi[0] * (float)v.q[j] * rinv;
-            const float erfx = ewald_erfc_f(alfa * rij, &ff, spii);
-            float eqq = erfx * auxq;
-            fij = fij + ff * auxq * rsqi;
-            float fjx[3], fjy[3], fjz[3];
-            fix[0].add(xio * fij); fiy[0].add(yio * fij); fiz[0].add(zio * fij);
-            fjx[0] = -xio * fij; fjy[0] = -yio * fij; fjz[0] = -zio * fij;
-            float rjx[3], rjy[3], rjz[3], qj[3];
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                if (b > 0) fjx[b] = fjy[b] = fjz[b] = 0.f;
-                const bool ok = b < nsi_j;
-                rjx[b] = ok ? (float)v.rsx[j + b] : 0.f;
-                rjy[b] = ok ? (float)v.rsy[j + b] : 0.f;
-                rjz[b] = ok ? (float)v.rsz[j + b] : 0.f;
-                qj[b] = ok ? (float)v.q[j + b] : 0.f;
-            }
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                if (a >= nsi_i) break;
-                const float xa = xio + rix[a], ya = yio + riy[a], za = zio + riz[a];
-                const float qx = facq * qi[a];
-#pragma unroll
-                for (int b = 0; b < 3; ++b) {
-                    if (b >= nsi_j) break;
-                    if (a == 0 && b == 0) continue;
-                    const float xd = xa - rjx[b], yd = ya - rjy[b], zd = za - rjz[b];
-                    const float r2 = xd * xd + yd * yd + zd * zd;
-                    const float ri = rsqrtf(r2);
-                    const float rr = r2 * ri;
-                    const float au = qx * qj[b] * ri;
-                    float fq;
-                    const float ef = ewald_erfc_f(alfa * rr, &fq, spii);
-                    eqq += ef * au;
-                    const float fs = fq * au * (ri * ri);
-                    fix[a].add(xd * fs); fiy[a].add(yd * fs); fiz[a].add(zd * fs);
-                    fjx[b] -= xd * fs; fjy[b] -= yd * fs; fjz[b] -= zd * fs;
-                }
-            }
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                if (b >= nsi_j) break;
-                atomicAdd(&v.fx[j + b], (double)fjx[b]);
-                atomicAdd(&v.fy[j + b], (double)fjy[b]);
-                atomicAdd(&v.fz[j + b], (double)fjz[b]);
-            }
-            e_add(e, ijt, (double)elj, (double)eqq, s_e, v.nijt);
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            if (a >= nsi_i) break;
-            const double sx = warp_sum(fix[a].value()), sy = warp_sum(fiy[a].value()), sz = warp_sum(fiz[a].value());
-            if (lane == 0) {
-                atomicAdd(&v.fx[i + a], sx);
-                atomicAdd(&v.fy[i + a], sy);
-                atomicAdd(&v.fz[i + a], sz);
-            }
-        }
-    }
-    e_flush(e, s_e, v.nijt);
-    __syncthreads();
-    for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x)
-        if (s_e[k] != 0.0) atomicAdd(&v.acc[k], s_e[k]);
-}
-
-__global__ void __launch_bounds__(kNT) k_wall_fp32(View v) {
-    extern __shared__ double s_e[];
-    for (int k = threadIdx.x; k < 2 * v.nijt + 6; k += blockDim.x) s_e[k] = 0.0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const int nwarps = gridDim.x * kWarps;
-    const float alfa = (float)v.alfa, spii = (float)v.spii, facq = (float)v.facq, rcutsq = (float)v.rcutsq;
-    EAcc e;
-    double ws[6] = {0, 0, 0, 0, 0, 0};
-    for (int h = warp; h < v.nheads; h += nwarps) {
-        const int i = v.head_atom[h];
-        const int it = v.type[i];
-        const int nsi_i = v.nsi[it];
-        const bool book = (it + 1) <= v.nltype;
-        const double xi0 = v.x[i], yi0 = v.y[i], zi0 = v.z[i];
-        float rix[3], riy[3], riz[3], qi[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const bool ok = a < nsi_i;
-            rix[a] = ok ? (float)v.rsx[i + a] : 0.f;
-            riy[a] = ok ? (float)v.rsy[i + a] : 0.f;
-            riz[a] = ok ? (float)v.rsz[i + a] : 0.f;
-            qi[a] = ok ? (float)v.q[i + a] : 0.f;
-        }
-        Kahan fix[3], fiy[3], fiz[3];
-        const int n = v.wnbcnt[h];
-        const int* nb = v.wnb + (size_t)h * v.maxwnb;
-        for (int k = lane; k < n; k += 32) {
-            const int j = nb[k];
-            const float xi = (float)minimg(xi0 - v.x[j], v.lx, v.lxi);
-            const float yi = (float)minimg(yi0 - v.y[j], v.ly, v.lyi);
-            double zd64 = zi0 - v.z[j];
-            if (v.bulk) zd64 = minimg(zd64, v.lz, v.lzi);
-            const float zi = (float)zd64;
-            const float rsq = xi * xi + yi * yi + zi * zi;
-            if (rsq > rcutsq) continue;
-            const int so = signbit(v.z[j]) ? 0 : 3;
-            const int ijt = v.ijt[it * v.nit + v.type[j]];
-            float fij = 0.f, elj = 0.f;
-            const int vk = v.vdw[ijt];
-            if (vk == 1) {
-                const float rsqi = 1.0f / rsq;
-                const float r6 = (float)v.sig[ijt] * (rsqi * rsqi * rsqi);
-                const float ep = (float)v.eps[ijt];
-                elj = ep * r6 * (r6 - 1.0f);
-                fij = 6.0f * rsqi * ep * r6 * (2.0f * r6 - 1.0f);
-            } else if (vk == 2) {
-                const float rinv = rsqrtf(rsq);
-                const float rsqi = rinv * rinv;
-                const float rij = rsq * rinv;
-                const float r6 = (float)v.cc[ijt] * (rsqi * rsqi * rsqi);
-                const float rh = (float)v.rhoi[ijt];
-                const float aux = (float)v.aa[ijt] * __expf(-rij * rh);
-                elj = aux - r6;
-                fij = aux * rh * rinv - 6.0f * rsqi * r6;
-            }
-            const float qx = facq * (float)v.q[j];
-            float eqq = 0.f;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                if (a >= nsi_i) break;
-                const float xd = xi + rix[a], yd = yi + riy[a], zd = zi + riz[a];
-                const float r2 = xd * xd + yd * yd + zd * zd;
-                const float ri = rsqrtf(r2);
-                const float rr = r2 * ri;
-                const float au = qx * qi[a] * ri;
-                float fq;
-                const float ef = ewald_erfc_f(alfa * rr, &fq, spii);
-                eqq += ef * au;
-                fij = fij + fq * au * (ri * ri);
-                fix[a].add(xd * fij); fiy[a].add(yd * fij); fiz[a].add(zd * fij);
-                if (book) {
-                    ws[so] -= (double)(xd * fij); ws[so + 1] -= (double)(yd * fij); ws[so + 2] -= (double)(zd * fij);
-                }
-                fij = 0.f;
-            }
-            e_add(e, ijt, (double)elj, (double)eqq, s_e, v.nijt);
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            if (a >= nsi_i) break;
-            const double sx = warp_sum(fix[a].value()), sy = warp_sum(fiy[a].value()), sz = warp_sum(fiz[a].value());
-            if (lane == 0) {
-                atomicAdd(&v.fx[i + a], sx);
-                atomicAdd(&v.fy[i + a], sy);
-                atomicAdd(&v.fz[i + a], sz);
-            }
-        }
-    }
-    e_flush(e, s_e, v.nijt);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const double s = warp_sum(ws[k]);
-        if (lane == 0 && s != 0.0) atomicAdd(&s_e[2 * v.nijt + k], s);
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x)
-        if (s_e[k] != 0.0) atomicAdd(&v.acc[k], s_e[k]);
-    if (threadIdx.x < 6) {
-        const int comp = threadIdx.x % 3, sg = threadIdx.x / 3;
-        const double s = s_e[2 * v.nijt + threadIdx.x];
-        if (s != 0.0) atomicAdd(&v.acc[2 * v.nijt + ACC_FWS + comp * 3 + (sg ? 2 : 0)], s);
-    }
+    block_atomic_sum<kLrNT>(ulr, &v.acc[2 * v.nijt + ACC_ULR]);
+    block_atomic_sum<kLrNT>(fw[0], &v.acc[2 * v.nijt + ACC_FWS + 6 + 0]);
+    block_atomic_sum<kLrNT>(fw[1], &v.acc[2 * v.nijt + ACC_FWS + 6 + 2]);
 }
 
 int pair_blocks(int nheads) {
@@ -598,18 +345,6 @@ void wall_forces_fp64(Ctx& c) {
     k_wall_fp64<<<pair_blocks(v.nheads), kNT, sizeof(double) * (2 * v.nijt + 6), c.stream>>>(v);
 }
 
-void pair_forces_fp32(Ctx& c) {
-    const View& v = c.v;
-    if (v.nheads == 0) return;
-    k_pair_fp32<<<pair_blocks(v.nheads), kNT, sizeof(double) * 2 * v.nijt, c.stream>>>(v);
-}
-
-void wall_forces_fp32(Ctx& c) {
-    const View& v = c.v;
-    if (v.nheads == 0 || v.nwall == 0) return;
-    k_wall_fp32<<<pair_blocks(v.nheads), kNT, sizeof(double) * (2 * v.nijt + 6), c.stream>>>(v);
-}
-
 void surf_partition(Ctx& c) {
     const View& v = c.v;
     if (v.nmove <= v.nliqa) return;
@@ -619,7 +354,7 @@ void surf_partition(Ctx& c) {
 void lr_tail(Ctx& c) {
     const View& v = c.v;
     if (c.variant != MDG_SLAB || v.nmove == 0) return;
-    k_lr_tail<<<std::min((v.nmove + kNT - 1) / kNT, 256), kNT, 0, c.stream>>>(v, c.d_lr);
+    k_lr_tail<<<std::min((v.nmove + kLrNT - 1) / kLrNT, 152 * 8), kLrNT, 0, c.stream>>>(v, c.d_lr);
 }
 
 }  // namespace mdg

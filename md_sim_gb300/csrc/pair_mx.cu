@@ -1,0 +1,396 @@
+// pair_mx.cu - mixed-precision real-space forces: the terms of force_real (src/forcem.f90:233-552)
+// in FP32 arithmetic with no FP64 work inside the pair loops.
+//
+// Each force evaluation first packs per-atom records (k_pack):
+//   P[a]   uint4  x and y (and z when z is periodic for the forces) as 32-bit fixed-point
+//                 fractions of the box edge, so the wrapped integer difference of two records IS
+//                 the minimum-image vector (src/forcem.f90:296-300, anint image) to 2^-32 of the
+//                 edge; a non-periodic z is the FP32 value z_hi (remainder in zlo[a]); w = site
+//                 type, bit 31 = sign of z (which wall a wall atom belongs to).
+//   Q[a]   float4 site offset rs(a) and charge q(a)
+//   F[a]   float4 j-side force accumulator, zeroed here
+// k_pair_mx walks the same per-head half lists as the FP64 kernel (one warp per head): i-side
+// site forces in compensated FP32 sums per lane, warp-reduced once per head; j-side site forces
+// per pair; both leave as one vector FP32 reduction (red.global.add.v4.f32) per site into F,
+// which k_merge_f adds into the FP64 forces (and clears) after the loop.  k_wall_mx does the
+// head-wall loop (src/forcem.f90:418-498) the same way, with the wall reaction sums in
+// compensated FP32.  Neither loop issues FP64 instructions (the FP64 pipe of GB300 is narrow).
+#include <algorithm>
+
+#include "common.cuh"
+#include "ctx.h"
+
+namespace mdg {
+
+namespace {
+
+constexpr int kWarps = 8;
+constexpr int kNT = kWarps * 32;
+constexpr float kPf = (float)kP, kA1f = (float)kA1, kA2f = (float)kA2, kA3f = (float)kA3, kA4f = (float)kA4,
+                kA5f = (float)kA5;
+
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    __device__ __forceinline__ float valuef() const { return s - c; }
+};
+
+__device__ __forceinline__ float warp_sumf(float x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// Energies of the current head type pair; flushed to shared FP64 sums when the pair type changes.
+struct EAcc {
+    int ijt = -1;
+    Kahan lj, qq;
+};
+
+__device__ __forceinline__ void e_flush(EAcc& e, double* s_e, int nijt) {
+    if (e.ijt >= 0) {
+        const double a = e.lj.value(), b = e.qq.value();
+        if (a != 0.0) atomicAdd(&s_e[e.ijt], a);
+        if (b != 0.0) atomicAdd(&s_e[nijt + e.ijt], b);
+    }
+    e.lj = Kahan();
+    e.qq = Kahan();
+}
+
+__device__ __forceinline__ void e_add(EAcc& e, int ijt, float lj, float qq, double* s_e, int nijt) {
+    if (ijt != e.ijt) {
+        e_flush(e, s_e, nijt);
+        e.ijt = ijt;
+    }
+    e.lj.add(lj);
+    e.qq.add(qq);
+}
+
+// Abramowitz-Stegun 7.1.26 erfc(alpha r) and the Ewald force factor (src/forcem.f90:334-340).
+__device__ __forceinline__ float erfc_as(float alfar, float* ff, float spii) {
+    const float t = __fdividef(1.0f, 1.0f + kPf * alfar);
+    const float exp2a = __expf(-alfar * alfar);
+    const float erfx = ((((kA5f * t + kA4f) * t + kA3f) * t + kA2f) * t + kA1f) * t * exp2a;
+    *ff = spii * alfar * exp2a + erfx;
+    return erfx;
+}
+
+__device__ __forceinline__ void red_v4(float4* p, float a, float b, float c) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(0.f)
+                 : "memory");
+}
+
+__device__ __forceinline__ uint32_t frac32(double t) {
+    const double f = t - floor(t);
+    return (uint32_t)(__double2ull_rn(f * 4294967296.0) & 0xffffffffull);
+}
+
+__global__ void k_pack(View v, Pk pk) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < v.ntota; a += gridDim.x * blockDim.x) {
+        const double x = v.x[a], y = v.y[a], z = v.z[a];
+        uint4 p;
+        p.x = frac32(x * v.lxi);
+        p.y = frac32(y * v.lyi);
+        if (pk.zper) {
+            p.z = frac32(z * v.lzi);
+        } else {
+            const float zh = (float)z;
+            p.z = __float_as_uint(zh);
+            pk.zlo[a] = (float)(z - (double)zh);
+        }
+        p.w = (uint32_t)v.type[a] | (signbit(z) ? 0x80000000u : 0u);
+        pk.P[a] = p;
+        float4 q = make_float4(0.f, 0.f, 0.f, (float)v.q[a]);
+        if (a < v.nmove) {
+            q.x = (float)v.rsx[a];
+            q.y = (float)v.rsy[a];
+            q.z = (float)v.rsz[a];
+            pk.F[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        pk.Q[a] = q;
+    }
+}
+
+// Pair-type tables in shared memory: per ijt {kind, sig, eps, aa, rhoi, cc}, ijt[it*nit+jt], nsi[it].
+struct Tables {
+    float* par;
+    int* ijt;
+    int* nsi;
+};
+
+__device__ __forceinline__ Tables load_tables(const View& v, double* s_e, int nextra) {
+    Tables t;
+    t.par = reinterpret_cast<float*>(s_e + 2 * v.nijt + nextra);
+    t.ijt = reinterpret_cast<int*>(t.par + 6 * v.nijt);
+    t.nsi = t.ijt + v.nit * v.nit;
+    for (int k = threadIdx.x; k < 2 * v.nijt + nextra; k += blockDim.x) s_e[k] = 0.0;
+    for (int k = threadIdx.x; k < v.nijt; k += blockDim.x) {
+        t.par[6 * k + 0] = __int_as_float(v.vdw[k]);
+        t.par[6 * k + 1] = (float)v.sig[k];
+        t.par[6 * k + 2] = (float)v.eps[k];
+        t.par[6 * k + 3] = (float)v.aa[k];
+        t.par[6 * k + 4] = (float)v.rhoi[k];
+        t.par[6 * k + 5] = (float)v.cc[k];
+    }
+    for (int k = threadIdx.x; k < v.nit * v.nit; k += blockDim.x) t.ijt[k] = v.ijt[k];
+    for (int k = threadIdx.x; k < v.nit; k += blockDim.x) t.nsi[k] = v.nsi[k];
+    __syncthreads();
+    return t;
+}
+
+// Head-head (or head-wall) separation from packed records.
+template <int ZPER>
+__device__ __forceinline__ void head_vec(const uint4& pi, float zli, const uint4& pj, const Pk& pk, int j, float& dx,
+                                         float& dy, float& dz) {
+    dx = __int2float_rn((int)(pi.x - pj.x)) * pk.sx;
+    dy = __int2float_rn((int)(pi.y - pj.y)) * pk.sy;
+    if (ZPER) dz = __int2float_rn((int)(pi.z - pj.z)) * pk.sz;
+    else dz = (__uint_as_float(pi.z) - __uint_as_float(pj.z)) + (zli - pk.zlo[j]);
+}
+
+// vdW between heads (src/forcem.f90:303-327): returns the energy, adds f/r to *fij.
+__device__ __forceinline__ float vdw_term(const float* par, float rsqi, float rinv, float rij, float* fij) {
+    const int vk = __float_as_int(par[0]);
+    if (vk == 1) {
+        const float r6 = par[1] * (rsqi * rsqi * rsqi);
+        const float ep = par[2];
+        *fij = 6.0f * rsqi * ep * r6 * (2.0f * r6 - 1.0f);
+        return ep * r6 * (r6 - 1.0f);
+    }
+    if (vk == 2) {
+        const float r6 = par[5] * (rsqi * rsqi * rsqi);
+        const float rh = par[4];
+        const float aux = par[3] * __expf(-rij * rh);
+        *fij = aux * rh * rinv - 6.0f * rsqi * r6;
+        return aux - r6;
+    }
+    *fij = 0.f;
+    return 0.f;
+}
+
+template <int ZPER>
+__global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
+    extern __shared__ double s_e[];
+    const Tables T = load_tables(v, s_e, 0);
+    const int lane = threadIdx.x & 31;
+    const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * kWarps;
+    const float alfa = (float)v.alfa, spii = (float)v.spii, facq = (float)v.facq, rcutsq = (float)v.rcutsq;
+    EAcc e;
+    for (int h = warp; h < v.nheads; h += nwarps) {
+        const int i = v.head_atom[h];
+        const uint4 pi = pk.P[i];
+        const int it = (int)(pi.w & 0x7fffffffu);
+        const int nsi_i = T.nsi[it];
+        const float zli = ZPER ? 0.f : pk.zlo[i];
+        float4 si[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) si[a] = a < nsi_i ? pk.Q[i + a] : make_float4(0.f, 0.f, 0.f, 0.f);
+        Kahan fix[3], fiy[3], fiz[3];
+        const int n = v.nbcnt[h];
+        const int* nb = v.nb + (size_t)h * v.maxnb;
+        for (int k = lane; k < n; k += 32) {
+            const int j = nb[k];
+            const uint4 pj = pk.P[j];
+            float xio, yio, zio;
+            head_vec<ZPER>(pi, zli, pj, pk, j, xio, yio, zio);
+            const float rsq = xio * xio + yio * yio + zio * zio;
+            if (rsq > rcutsq) continue;
+            const int jt = (int)(pj.w & 0x7fffffffu);
+            const int ijt = T.ijt[it * v.nit + jt];
+            const int nsi_j = T.nsi[jt];
+            const float rinv = rsqrtf(rsq);
+            const float rsqi = rinv * rinv;
+            const float rij = rsq * rinv;
+            float fij;
+            const float elj = vdw_term(T.par + 6 * ijt, rsqi, rinv, rij, &fij);
+            float4 sj[3];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) sj[b] = b < nsi_j ? pk.Q[j + b] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float ff;
+            const float auxq = facq * si[0].w * sj[0].w * rinv;
+            float eqq = erfc_as(alfa * rij, &ff, spii) * auxq;
+            fij = fij + ff * auxq * rsqi;
+            float fjx[3], fjy[3], fjz[3];
+            fix[0].add(xio * fij); fiy[0].add(yio * fij); fiz[0].add(zio * fij);
+            fjx[0] = -xio * fij; fjy[0] = -yio * fij; fjz[0] = -zio * fij;
+#pragma unroll
+            for (int b = 1; b < 3; ++b) fjx[b] = fjy[b] = fjz[b] = 0.f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (a >= nsi_i) break;
+                const float xa = xio + si[a].x, ya = yio + si[a].y, za = zio + si[a].z;
+                const float qx = facq * si[a].w;
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    if (b >= nsi_j) break;
+                    if (a == 0 && b == 0) continue;
+                    const float xd = xa - sj[b].x, yd = ya - sj[b].y, zd = za - sj[b].z;
+                    const float r2 = xd * xd + yd * yd + zd * zd;
+                    const float ri = rsqrtf(r2);
+                    const float rr = r2 * ri;
+                    const float au = qx * sj[b].w * ri;
+                    float fq;
+                    eqq += erfc_as(alfa * rr, &fq, spii) * au;
+                    const float fs = fq * au * (ri * ri);
+                    fix[a].add(xd * fs); fiy[a].add(yd * fs); fiz[a].add(zd * fs);
+                    fjx[b] -= xd * fs; fjy[b] -= yd * fs; fjz[b] -= zd * fs;
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                if (b >= nsi_j) break;
+                red_v4(&pk.F[j + b], fjx[b], fjy[b], fjz[b]);
+            }
+            e_add(e, ijt, elj, eqq, s_e, v.nijt);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (a >= nsi_i) break;
+            const float sx = warp_sumf(fix[a].valuef()), sy = warp_sumf(fiy[a].valuef()), sz = warp_sumf(fiz[a].valuef());
+            if (lane == 0) red_v4(&pk.F[i + a], sx, sy, sz);
+        }
+    }
+    e_flush(e, s_e, v.nijt);
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x)
+        if (s_e[k] != 0.0) atomicAdd(&v.acc[k], s_e[k]);
+}
+
+template <int ZPER>
+__global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
+    extern __shared__ double s_e[];
+    const Tables T = load_tables(v, s_e, 6);
+    const int lane = threadIdx.x & 31;
+    const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * kWarps;
+    const float alfa = (float)v.alfa, spii = (float)v.spii, facq = (float)v.facq, rcutsq = (float)v.rcutsq;
+    EAcc e;
+    Kahan ws[6];
+    for (int h = warp; h < v.nheads; h += nwarps) {
+        const int i = v.head_atom[h];
+        const uint4 pi = pk.P[i];
+        const int it = (int)(pi.w & 0x7fffffffu);
+        const int nsi_i = T.nsi[it];
+        const bool book = (it + 1) <= v.nltype;
+        const float zli = ZPER ? 0.f : pk.zlo[i];
+        float4 si[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) si[a] = a < nsi_i ? pk.Q[i + a] : make_float4(0.f, 0.f, 0.f, 0.f);
+        Kahan fix[3], fiy[3], fiz[3];
+        const int n = v.wnbcnt[h];
+        const int* nb = v.wnb + (size_t)h * v.maxwnb;
+        for (int k = lane; k < n; k += 32) {
+            const int j = nb[k];
+            const uint4 pj = pk.P[j];
+            float xi, yi, zi;
+            head_vec<ZPER>(pi, zli, pj, pk, j, xi, yi, zi);
+            const float rsq = xi * xi + yi * yi + zi * zi;
+            if (rsq > rcutsq) continue;
+            const int so = (pj.w & 0x80000000u) ? 0 : 3;
+            const int jt = (int)(pj.w & 0x7fffffffu);
+            const int ijt = T.ijt[it * v.nit + jt];
+            const float rinv = rsqrtf(rsq);
+            float fij;
+            const float elj = vdw_term(T.par + 6 * ijt, rinv * rinv, rinv, rsq * rinv, &fij);
+            const float qx = facq * pk.Q[j].w;
+            float eqq = 0.f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (a >= nsi_i) break;
+                const float xd = xi + si[a].x, yd = yi + si[a].y, zd = zi + si[a].z;
+                const float r2 = xd * xd + yd * yd + zd * zd;
+                const float ri = rsqrtf(r2);
+                const float rr = r2 * ri;
+                const float au = qx * si[a].w * ri;
+                float fq;
+                eqq += erfc_as(alfa * rr, &fq, spii) * au;
+                fij = fij + fq * au * (ri * ri);
+                fix[a].add(xd * fij); fiy[a].add(yd * fij); fiz[a].add(zd * fij);
+                if (book) {
+                    ws[so].add(-xd * fij); ws[so + 1].add(-yd * fij); ws[so + 2].add(-zd * fij);
+                }
+                fij = 0.f;
+            }
+            e_add(e, ijt, elj, eqq, s_e, v.nijt);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (a >= nsi_i) break;
+            const float sx = warp_sumf(fix[a].valuef()), sy = warp_sumf(fiy[a].valuef()), sz = warp_sumf(fiz[a].valuef());
+            if (lane == 0) red_v4(&pk.F[i + a], sx, sy, sz);
+        }
+    }
+    e_flush(e, s_e, v.nijt);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const double s = warp_sum(ws[k].value());
+        if (lane == 0 && s != 0.0) atomicAdd(&s_e[2 * v.nijt + k], s);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x)
+        if (s_e[k] != 0.0) atomicAdd(&v.acc[k], s_e[k]);
+    if (threadIdx.x < 6) {
+        const int comp = threadIdx.x % 3, sg = threadIdx.x / 3;
+        const double s = s_e[2 * v.nijt + threadIdx.x];
+        if (s != 0.0) atomicAdd(&v.acc[2 * v.nijt + ACC_FWS + comp * 3 + (sg ? 2 : 0)], s);
+    }
+}
+
+__global__ void k_merge_f(View v, Pk pk) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < v.nmove; a += gridDim.x * blockDim.x) {
+        const float4 f = pk.F[a];
+        v.fx[a] += (double)f.x;
+        v.fy[a] += (double)f.y;
+        v.fz[a] += (double)f.z;
+        pk.F[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+int blocks(int nheads) { return std::max(1, std::min((nheads + kWarps - 1) / kWarps, 152 * 16)); }
+
+size_t table_smem(const View& v, int nextra) {
+    return sizeof(double) * (2 * v.nijt + nextra) + sizeof(float) * 6 * v.nijt + sizeof(int) * (v.nit * v.nit + v.nit);
+}
+
+}  // namespace
+
+void pack_setup(Ctx& c) {
+    const View& v = c.v;
+    const int n = std::max(v.ntota, 1);
+    c.pk.P = (uint4*)dalloc(c, sizeof(uint4) * n);
+    c.pk.Q = (float4*)dalloc(c, sizeof(float4) * n);
+    c.pk.zlo = (float*)dalloc(c, sizeof(float) * n);
+    c.pk.F = (float4*)dalloc(c, sizeof(float4) * std::max(v.nmove, 1));
+    c.pk.zper = v.bulk ? 1 : 0;
+    c.pk.sx = (float)(v.lx / 4294967296.0);
+    c.pk.sy = (float)(v.ly / 4294967296.0);
+    c.pk.sz = (float)(v.lz / 4294967296.0);
+}
+
+void real_space_mixed(Ctx& c) {
+    const View& v = c.v;
+    if (v.ntota == 0) return;
+    k_pack<<<std::min((v.ntota + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
+    if (v.nheads > 0) {
+        if (c.pk.zper) k_pair_mx<1><<<blocks(v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
+        else k_pair_mx<0><<<blocks(v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
+        k_merge_f<<<std::min((v.nmove + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
+    }
+}
+
+void wall_forces_mixed(Ctx& c) {
+    const View& v = c.v;
+    if (v.nheads == 0 || v.nwall == 0) return;
+    if (c.pk.zper) k_wall_mx<1><<<blocks(v.nheads), kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
+    else k_wall_mx<0><<<blocks(v.nheads), kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
+    k_merge_f<<<std::min((v.nmove + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
+}
+
+}  // namespace mdg

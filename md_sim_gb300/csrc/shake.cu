@@ -17,6 +17,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "mlp.cuh"
 
 namespace mdg {
 
@@ -33,6 +34,8 @@ struct ShakeArgs {
     const int* cons_n;    // ncons
     double *xo, *yo, *zo; // xold(nliqa:ntota)
     int* sweeps_out;      // [0] sweeps decided, [1] done flag
+    const float* mlpw;    // seeding network (mlp.cuh blob) or nullptr
+    float* rec;           // ncons x 16: features, accumulated multipliers, sweeps of this call, or nullptr
 };
 
 __global__ void k_verlet(View v, const double* ft, double* xo, double* yo, double* zo, double* kps) {
@@ -87,7 +90,8 @@ __device__ void load_mol(const ShakeArgs& A, int ic, Mol& m) {
 // One sweep over the molecule; returns true when some constraint was corrected.
 // moved bit s = 1: atom in slot s was NOT moved in the previous sweep (reference `moved` = 1).
 __device__ bool sweep(const View& v, const ShakeArgs& A, const Mol& m, double* px, double* py, double* pz,
-                      const double* ox, const double* oy, const double* oz, unsigned& moved, int* fail) {
+                      const double* ox, const double* oy, const double* oz, unsigned& moved, int* fail,
+                      double* gacc = nullptr) {
     unsigned moving = (1u << kMaxAt) - 1u;
     bool upd = false;
     for (int s = 0; s < m.n; ++s) {
@@ -109,6 +113,7 @@ __device__ bool sweep(const View& v, const ShakeArgs& A, const Mol& m, double* p
             }
             double rma = v.mii[m.at[a]], rmb = v.mii[m.at[b]];
             const double aux = diffsq / (2.0 * (rma + rmb) * rpab);
+            if (gacc) gacc[s] += aux;
             rma = rma * aux;
             rmb = rmb * aux;
             px[a] = px[a] + rx * rma; py[a] = py[a] + ry * rma; pz[a] = pz[a] + rz * rma;
@@ -137,18 +142,63 @@ __device__ void gather(const View& v, const ShakeArgs& A, const Mol& m, double* 
     }
 }
 
+// Bonds of a 3-constraint molecule after the Verlet step (p) and before it (r), minimum-imaged.
+__device__ void bonds(const View& v, const Mol& m, const double* px, const double* py, const double* pz,
+                      const double* ox, const double* oy, const double* oz, double p[3][3], double r[3][3]) {
+    for (int c = 0; c < 3; ++c) {
+        const int a = m.ca[c], b = m.cb[c];
+        p[c][0] = minimg(px[a] - px[b], v.lx, v.lxi);
+        p[c][1] = minimg(py[a] - py[b], v.ly, v.lyi);
+        p[c][2] = minimg(pz[a] - pz[b], v.lz, v.lzi);
+        r[c][0] = minimg(ox[a] - ox[b], v.lx, v.lxi);
+        r[c][1] = minimg(oy[a] - oy[b], v.ly, v.lyi);
+        r[c][2] = minimg(oz[a] - oz[b], v.lz, v.lzi);
+    }
+}
+
+// Network seed: predicted accumulated multipliers applied along the old bonds, the same update as a
+// SHAKE correction (src/move.f90:498-510) with all three constraints at once.
+__device__ void seed_mol(const View& v, const Mol& m, const float* W, const float f[9], double* px, double* py,
+                         double* pz, const double r[3][3], double* gacc) {
+    float y[3];
+    mlp::forward(W, f, y);
+    for (int c = 0; c < 3; ++c) {
+        const int a = m.ca[c], b = m.cb[c];
+        const double ma = v.mii[m.at[a]], mb = v.mii[m.at[b]];
+        if (ma + mb <= 0.0) continue;
+        const double g = (double)y[c] / (ma + mb);
+        gacc[c] += g;
+        px[a] += r[c][0] * ma * g; py[a] += r[c][1] * ma * g; pz[a] += r[c][2] * ma * g;
+        px[b] -= r[c][0] * mb * g; py[b] -= r[c][1] * mb * g; pz[b] -= r[c][2] * mb * g;
+    }
+}
+
+__device__ void load_weights(const float* mlpw, float* W) {
+    for (int i = threadIdx.x; i < mlp::NW; i += blockDim.x) W[i] = i < mlp::NPARAM ? mlp::bf16r(mlpw[i]) : mlpw[i];
+}
+
 __global__ void k_shake_init(ShakeArgs A) {
     A.sweeps_out[0] = 0;
     A.sweeps_out[1] = 1;
 }
 
 __global__ void k_shake_last(View v, ShakeArgs A) {
+    __shared__ float W[mlp::NW];
+    if (A.mlpw) load_weights(A.mlpw, W);
+    __syncthreads();
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     Mol m;
     load_mol(A, A.ncons - 1, m);
     double px[kMaxAt], py[kMaxAt], pz[kMaxAt], ox[kMaxAt], oy[kMaxAt], oz[kMaxAt];
     unsigned moved;
     gather(v, A, m, px, py, pz, ox, oy, oz, moved);
+    if (A.mlpw && m.n == 3) {
+        double p[3][3], r[3][3], g[3] = {0, 0, 0};
+        float f[9];
+        bonds(v, m, px, py, pz, ox, oy, oz, p, r);
+        mlp::features(p, r, m.l2, f);
+        seed_mol(v, m, W, f, px, py, pz, r, g);
+    }
     int fail = 0, s = 0;
     bool done = false;
     while (!done && s <= A.maxit) {
@@ -161,6 +211,9 @@ __global__ void k_shake_last(View v, ShakeArgs A) {
 }
 
 __global__ void k_shake_mol(View v, ShakeArgs A) {
+    __shared__ float W[mlp::NW];
+    if (A.mlpw) load_weights(A.mlpw, W);
+    __syncthreads();
     const int ic = blockIdx.x * blockDim.x + threadIdx.x;
     if (ic >= A.ncons) return;
     Mol m;
@@ -168,12 +221,21 @@ __global__ void k_shake_mol(View v, ShakeArgs A) {
     double px[kMaxAt], py[kMaxAt], pz[kMaxAt], ox[kMaxAt], oy[kMaxAt], oz[kMaxAt];
     unsigned moved;
     gather(v, A, m, px, py, pz, ox, oy, oz, moved);
+    double gacc[3] = {0.0, 0.0, 0.0};
+    float feat[9];
+    const bool model = m.n == 3 && (A.mlpw || A.rec);
+    if (model) {
+        double p[3][3], r[3][3];
+        bonds(v, m, px, py, pz, ox, oy, oz, p, r);
+        mlp::features(p, r, m.l2, feat);
+        if (A.mlpw) seed_mol(v, m, W, feat, px, py, pz, r, gacc);
+    }
     int fail = 0;
     int s = 0;
     const int nsw = A.clean ? A.maxit + 1 : A.sweeps_out[0];
     bool converged = false;
     for (; s < nsw; ++s) {
-        const bool upd = sweep(v, A, m, px, py, pz, ox, oy, oz, moved, &fail);
+        const bool upd = sweep(v, A, m, px, py, pz, ox, oy, oz, moved, &fail, gacc);
         if (fail) {
             atomicCAS(&v.status[ST_SHAKE_RPTOL], 0, 1 + ic * 8 + 0);
             break;
@@ -192,6 +254,14 @@ __global__ void k_shake_mol(View v, ShakeArgs A) {
         if (a < A.nmove) {
             v.x[a] = px[t]; v.y[a] = py[t]; v.z[a] = pz[t];
         }
+    }
+    if (A.rec) {
+        float* o = A.rec + (size_t)ic * 16;
+        for (int k = 0; k < 9; ++k) o[k] = model ? feat[k] : 0.f;
+        for (int c = 0; c < 3; ++c)
+            o[9 + c] = model ? (float)(gacc[c] * (v.mii[m.at[m.ca[c]]] + v.mii[m.at[m.cb[c]]])) : 0.f;
+        o[12] = (float)(s + (converged && A.clean ? 1 : 0));
+        o[13] = o[14] = o[15] = 0.f;
     }
 }
 
@@ -268,6 +338,8 @@ int shake_setup(Ctx& c, const mdg_sysdesc* s) {
     c.d_ft_in = (double*)dalloc(c, sizeof(double) * 3 * std::max(v.nmove - v.nriga, 1));
     c.d_sweeps = (int*)dalloc(c, sizeof(int) * 2);
     c.d_seq_flags = (int*)dalloc(c, sizeof(int) * 2 * std::max(v.nmove - v.nliqa, 1));
+    c.d_mlpw = (float*)dalloc(c, sizeof(float) * mlp::NW);
+    c.d_shake_rec = (float*)dalloc(c, sizeof(float) * 16 * std::max<int64_t>(s->ncons, 1));
     if (c.ncons == 0) return MDG_OK;
     std::vector<int> cons(6 * c.ncons, -1), cn(c.ncons, 0);
     std::vector<double> l2(3 * c.ncons, 0.0);
@@ -318,7 +390,8 @@ void shake_launch(Ctx& c, const double* d_ft) {
     if (c.ncons == 0) return;
     const int clean = (c.quirks & MDG_QUIRK_CLEAN_SHAKE_DONE) ? 1 : 0;
     ShakeArgs A{c.ncons, c.maxit, clean, v.nliqa, v.nmove, c.tol2, c.rptol, c.d_cons, c.d_clen2,
-                c.d_cons_n, c.d_xold, c.d_yold, c.d_zold, c.d_sweeps};
+                c.d_cons_n, c.d_xold, c.d_yold, c.d_zold, c.d_sweeps, c.shake_model ? c.d_mlpw : nullptr,
+                c.shake_record ? c.d_shake_rec : nullptr};
     if (c.shake_seq) {
         k_shake_seq<<<1, 1, 0, c.stream>>>(v, A, c.d_seq_flags, c.d_seq_flags + std::max(nsurf, 1));
         k_shake_status<<<1, 1, 0, c.stream>>>(v, c.d_sweeps);
@@ -327,7 +400,7 @@ void shake_launch(Ctx& c, const double* d_ft) {
     if (clean) {
         k_shake_init<<<1, 1, 0, c.stream>>>(A);
     } else {
-        k_shake_last<<<1, 1, 0, c.stream>>>(v, A);
+        k_shake_last<<<1, 128, 0, c.stream>>>(v, A);
     }
     k_shake_mol<<<(c.ncons + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, A);
     k_shake_status<<<1, 1, 0, c.stream>>>(v, c.d_sweeps);

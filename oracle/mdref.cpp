@@ -7,8 +7,9 @@
 // Parity status: the reference (Fortran 90 + MPI) cannot be compiled in this environment (no
 // Fortran compiler) and ships no tests, golden vectors or known answers for this path, so this
 // restatement is "parity unpinned" against the reference's own outputs.  It is validated by
-// independent checks instead (finite-difference forces, Ewald vs direct lattice sums, Newton's
-// third law, invariances; see tests/test_oracle_physics.py).
+// independent checks instead (the NaCl Madelung constant from its Ewald sum, finite-difference
+// forces, independence of the total from the Ewald split, Newton's third law, translation
+// invariance; tests/test_oracle_physics.py).
 //
 // Each routine follows the reference loop by loop, in the same order, so that sums match to
 // rounding.  References are to files under src/ of the reference tree:
