@@ -111,6 +111,7 @@ struct Pk {
     float4* Q = nullptr;    // rs offset, charge
     float* zlo = nullptr;   // z - z_hi when z is not periodic
     float4* F = nullptr;    // j-side force accumulator (moving atoms)
+    uint4* tc = nullptr;    // reciprocal-sum records (moving atoms), or nullptr
     float sx = 0, sy = 0, sz = 0;  // box edge / 2^32
     int zper = 0;
 };
@@ -118,8 +119,8 @@ struct Pk {
 // Launch plan of the tensor-core reciprocal sum (recip_tc.cu).
 struct TcPlan {
     bool ready = false;
-    int KN = 0, NN = 0, NP = 0, KS = 0;
-    int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, smem1 = 0, smem2 = 0;
+    int KN = 0, NN = 0, NP = 0, KS = 0, KM = 0, NM = 0;
+    int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, grid1x = 0, rtot = 0, tpc1 = 0, smem1 = 0, smem2 = 0;
 };
 
 struct Ctx {
@@ -132,6 +133,7 @@ struct Ctx {
     uint4* d_tc_atoms = nullptr;        // fixed-point phases + charge per moving atom
     unsigned char* d_tc_img = nullptr;  // packed C(k) operand chunks
     float* d_tc_cmax = nullptr;         // scale of the packed C(k) operand
+    float* d_tc_part = nullptr;         // pass-1 partial sums [split][col][row]
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the context's stream while a caller's stream is in use
     int device = 0;

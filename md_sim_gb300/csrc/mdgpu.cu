@@ -474,6 +474,7 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
         rc = recip_tc_setup(c);
         if (rc) return bail(rc);
         pack_setup(c);
+        c.pk.tc = c.d_tc_atoms;
     }
     rc = nnlist_setup(c, x0, y0, z0);
     if (rc) return bail(rc);

@@ -160,7 +160,11 @@ __global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* 
     const double xi = v.x[ia], yi = v.y[ia], zi = v.z[ia];
     const float lxf = (float)v.lx, lyf = (float)v.ly, lzf = (float)v.lz;
     const float lxif = 1.0f / lxf, lyif = 1.0f / lyf, lzif = 1.0f / lzf;
-    const float lim = (float)v.rskinsq * 1.0001f + 0.05f;  // conservative: FP32 errors are ~1e-4 A^2
+    // FP32 distances of the binned positions are within ~1e-3 A^2 of the FP64 ones; only pairs
+    // inside the shell [lim_lo, lim_hi] around rskinsq need the exact FP64 test (the FP64 pipe
+    // is narrow on this part, so it is kept off the bulk of the candidates)
+    const float lim_hi = (float)v.rskinsq * 1.0001f + 0.05f;
+    const float lim_lo = (float)v.rskinsq * 0.9999f - 0.05f;
     const int cx = cell_coord(pw.x, 0, g), cy = cell_coord(pw.y, 1, g), cz = cell_coord(pw.z, 2, g);
     const bool surf_i = ia >= v.nliqa;
     int cnt = 0;
@@ -187,9 +191,10 @@ __global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* 
                             const float ddx = fmin_img(px - q.x, lxf, lxif, 1);
                             const float ddy = fmin_img(py - q.y, lyf, lyif, 1);
                             const float ddz = fmin_img(pz - q.z, lzf, lzif, g.periodic[2]);
-                            keep = ddx * ddx + ddy * ddy + ddz * ddz <= lim;
+                            const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                            keep = d2 <= lim_hi;
                             if (keep && surf_i && ja >= v.nliqa && excluded(v, ia, ja)) keep = false;
-                            if (keep) keep = keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja]);
+                            if (keep && d2 >= lim_lo) keep = keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja]);
                         }
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -218,7 +223,8 @@ __global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4*
     const float px = (float)pw.x, py = (float)pw.y, pz = (float)pw.z;
     const float lxf = (float)v.lx, lyf = (float)v.ly, lzf = (float)v.lz;
     const float lxif = 1.0f / lxf, lyif = 1.0f / lyf, lzif = 1.0f / lzf;
-    const float lim = (float)v.rskinsq * 1.0001f + 0.05f;
+    const float lim_hi = (float)v.rskinsq * 1.0001f + 0.05f;
+    const float lim_lo = (float)v.rskinsq * 0.9999f - 0.05f;
     const double wz = wrap(zi, v.lz, g.periodic[2]);
     const int cx = cell_coord(pw.x, 0, g), cy = cell_coord(pw.y, 1, g), cz = cell_coord(wz, 2, g);
     const bool surf_i = ia >= v.nliqa;
@@ -245,9 +251,10 @@ __global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4*
                         const float ddx = fmin_img(px - q.x, lxf, lxif, 1);
                         const float ddy = fmin_img(py - q.y, lyf, lyif, 1);
                         const float ddz = fmin_img(pz - q.z, lzf, lzif, g.periodic[2]);
-                        keep = ddx * ddx + ddy * ddy + ddz * ddz <= lim;
+                        const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                        keep = d2 <= lim_hi;
                         if (keep && surf_i && excluded(v, ia, ja)) keep = false;
-                        if (keep) keep = keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja]);
+                        if (keep && d2 >= lim_lo) keep = keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja]);
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, keep);
                     const int pos = cnt + __popc(m & ((1u << lane) - 1u));

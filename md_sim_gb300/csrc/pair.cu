@@ -36,6 +36,21 @@ __device__ __forceinline__ void e_flush(EAcc& e, double* s_e, int nijt) {
     e.lj = e.qq = 0.0;
 }
 
+// End of the loops: lanes holding the warp's (largest) pair type reduce with shuffles, one shared
+// atomic per warp; lanes left with another type flush one by one.
+__device__ __forceinline__ void e_final(EAcc& e, double* s_e, int nijt) {
+    const int ij0 = __reduce_max_sync(0xffffffffu, e.ijt);
+    if (ij0 < 0) return;
+    const bool mine = e.ijt == ij0;
+    const double lj = warp_sum(mine ? e.lj : 0.0);
+    const double qq = warp_sum(mine ? e.qq : 0.0);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&s_e[ij0], lj);
+        atomicAdd(&s_e[nijt + ij0], qq);
+    }
+    if (!mine) e_flush(e, s_e, nijt);
+}
+
 __device__ __forceinline__ void e_add(EAcc& e, int ijt, double lj, double qq, double* s_e, int nijt) {
     if (ijt != e.ijt) {
         e_flush(e, s_e, nijt);
@@ -168,7 +183,7 @@ __global__ void __launch_bounds__(kNT) k_pair_fp64(View v) {
             }
         }
     }
-    e_flush(e, s_e, v.nijt);
+    e_final(e, s_e, v.nijt);
     __syncthreads();
     for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x)
         if (s_e[k] != 0.0) atomicAdd(&v.acc[k], s_e[k]);
@@ -259,7 +274,7 @@ __global__ void __launch_bounds__(kNT) k_wall_fp64(View v) {
             }
         }
     }
-    e_flush(e, s_e, v.nijt);
+    e_final(e, s_e, v.nijt);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const double s = warp_sum(ws[k]);

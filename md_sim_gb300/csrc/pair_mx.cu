@@ -9,6 +9,8 @@
 //                 type, bit 31 = sign of z (which wall a wall atom belongs to).
 //   Q[a]   float4 site offset rs(a) and charge q(a)
 //   F[a]   float4 j-side force accumulator, zeroed here
+//   tc[a]  uint4  fixed-point fractions of x, y, z and the charge, for the tensor-core reciprocal
+//                 sum of the same evaluation (recip_tc.cu)
 // k_pair_mx walks the same per-head half lists as the FP64 kernel (one warp per head): i-side
 // site forces in compensated FP32 sums per lane, warp-reduced once per head; j-side site forces
 // per pair; both leave as one vector FP32 reduction (red.global.add.v4.f32) per site into F,
@@ -63,6 +65,21 @@ __device__ __forceinline__ void e_flush(EAcc& e, double* s_e, int nijt) {
     e.qq = Kahan();
 }
 
+// End of the loops: lanes holding the warp's (largest) pair type reduce with shuffles, one shared
+// atomic per warp; lanes left with another type (mixed-type systems) flush one by one.
+__device__ __forceinline__ void e_final(EAcc& e, double* s_e, int nijt) {
+    const int ij0 = __reduce_max_sync(0xffffffffu, e.ijt);
+    if (ij0 < 0) return;
+    const bool mine = e.ijt == ij0;
+    const float lj = warp_sumf(mine ? e.lj.valuef() : 0.f);
+    const float qq = warp_sumf(mine ? e.qq.valuef() : 0.f);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&s_e[ij0], (double)lj);
+        atomicAdd(&s_e[nijt + ij0], (double)qq);
+    }
+    if (!mine) e_flush(e, s_e, nijt);
+}
+
 __device__ __forceinline__ void e_add(EAcc& e, int ijt, float lj, float qq, double* s_e, int nijt) {
     if (ijt != e.ijt) {
         e_flush(e, s_e, nijt);
@@ -86,9 +103,11 @@ __device__ __forceinline__ void red_v4(float4* p, float a, float b, float c) {
                  : "memory");
 }
 
+// round(t 2^32) mod 2^32 for |t| < 2^19: t + 1.5 2^20 lies in [2^20, 2^21), where the spacing of
+// doubles is 2^-32, so the low 32 bits of its significand are the rounded fraction (two FP64
+// operations per coordinate; the FP64 pipe is narrow on this part).
 __device__ __forceinline__ uint32_t frac32(double t) {
-    const double f = t - floor(t);
-    return (uint32_t)(__double2ull_rn(f * 4294967296.0) & 0xffffffffull);
+    return (uint32_t)__double_as_longlong(t + 1572864.0);
 }
 
 __global__ void k_pack(View v, Pk pk) {
@@ -97,8 +116,9 @@ __global__ void k_pack(View v, Pk pk) {
         uint4 p;
         p.x = frac32(x * v.lxi);
         p.y = frac32(y * v.lyi);
+        const uint32_t uz = frac32(z * v.lzi);
         if (pk.zper) {
-            p.z = frac32(z * v.lzi);
+            p.z = uz;
         } else {
             const float zh = (float)z;
             p.z = __float_as_uint(zh);
@@ -112,6 +132,8 @@ __global__ void k_pack(View v, Pk pk) {
             q.y = (float)v.rsy[a];
             q.z = (float)v.rsz[a];
             pk.F[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+            // the reciprocal sum's record: periodic fractions on all three axes and the charge
+            if (pk.tc) pk.tc[a] = make_uint4(p.x, p.y, uz, __float_as_uint(q.w));
         }
         pk.Q[a] = q;
     }
@@ -257,7 +279,7 @@ __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
             if (lane == 0) red_v4(&pk.F[i + a], sx, sy, sz);
         }
     }
-    e_flush(e, s_e, v.nijt);
+    e_final(e, s_e, v.nijt);
     __syncthreads();
     for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x)
         if (s_e[k] != 0.0) atomicAdd(&v.acc[k], s_e[k]);
@@ -327,7 +349,7 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
             if (lane == 0) red_v4(&pk.F[i + a], sx, sy, sz);
         }
     }
-    e_flush(e, s_e, v.nijt);
+    e_final(e, s_e, v.nijt);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const double s = warp_sum(ws[k].value());

@@ -27,7 +27,6 @@ namespace mdg {
 
 namespace {
 
-constexpr int kG1 = 32;      // atoms per pass-1 group (two K steps)
 constexpr int kT = 256;      // threads per CTA
 constexpr float kPhase = 1.4629180792671596e-09f;  // 2 pi / 2^32
 
@@ -54,193 +53,264 @@ __device__ __forceinline__ uint32_t pack2(elem_t a, elem_t b) {
     return (uint32_t)ebits(a) | ((uint32_t)ebits(b) << 16);
 }
 
-// 32-bit fixed-point box fractions and the charge of each moving atom
-__global__ void k_tc_prep_atoms(View v, uint4* out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.nmove) return;
-    double f[3] = {v.x[i] * v.lxi, v.y[i] * v.lyi, v.z[i] * v.lzi};
-    uint32_t u[3];
-    for (int d = 0; d < 3; ++d) {
-        const double fr = f[d] - floor(f[d]);
-        u[d] = (uint32_t)(unsigned long long)llrint(fr * 4294967296.0);
-    }
-    out[i] = make_uint4(u[0], u[1], u[2], __float_as_uint((float)v.q[i]));
-}
-
 // ---------------------------------------------------------------------------------------------
 // pass 1: structure factor
+//
+// One CTA owns TPC row tiles (TPC * 128 (l, m) rows; TPC = 4 when the accumulators fit TMEM) and a
+// contiguous chunk of atoms, walked in groups of kGA = 16 atoms (one K step) through a 2-3 deep
+// shared-memory ring:
+//   producer warps (one thread per row): per group, phase tables e^{i m ty_j} (all m) and q_j e^{i l tx_j}
+//       (the l values of the CTA's rows) by __sincosf of exact fixed-point phases, the B tiles
+//       e^{i n tz_j} in the 2x2 real block form, then each thread its row's A entries
+//       q_j e^{i l tx_j} e^{i m ty_j} = table products, split hi/lo and stored in the UMMA
+//       canonical layout; arrive on full[s];
+//   last warp, lane 0 (issuer): waits full[s], issues 3 (hi/lo) x 2 (re/im part) MMAs per tile,
+//       commits to empty[s], which frees the stage for the producers.
+// The accumulators (one per tile, N = NP columns) are written once, as FP32 partial sums per
+// atom chunk, to part[split][col][row]; k_tc_sreduce adds the chunks in compensated FP32 and
+// forms S(k), the energy terms, C(k) and the scale of the pass-2 operand (src/forcem.f90:879-917).
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kT, 1) k_tc_sfac(View v, const uint4* __restrict__ atoms, int chunk,
-                                                   const int4* __restrict__ rows, const int* __restrict__ nlen,
-                                                   TcDims d, double2* S, uint32_t ncols) {
+constexpr int kGA = 16;                  // atoms per group (one K step)
+constexpr int kMaxNL = 64;               // l values per CTA (table width; the last slot stays 0)
+constexpr int kMaxItems = 4;             // table entries per producer thread and group
+
+template <int TPC>
+struct P1 {
+    static constexpr int kProd = 128 * TPC;      // producer threads: one per CTA row
+    static constexpr int kThreads = kProd + 32;  // + issuer warp
+    static constexpr int kS = TPC >= 4 ? 2 : 3;  // ring depth
+};
+
+struct P1Layout {
+    uint32_t a_bytes, b_tile, stage, tab_m, tab_l, off_stage, off_tab, total;
+};
+
+// tables: e^{i m ty} as float2 [atom][NM + 1] (slot NM = 0), q e^{i l tx} as float2 [atom][kMaxNL]
+__host__ __device__ inline P1Layout p1_layout(int tpc, int stages, int NP, int NM) {
+    P1Layout L;
+    L.a_bytes = tpc * 4 * 4096;                         // [tile][p][h] 128 x 16 halves
+    L.b_tile = (uint32_t)NP * 32;                       // NP x 16 halves
+    L.stage = L.a_bytes + 4 * L.b_tile;                 // + [p][h] B tiles
+    L.tab_m = (uint32_t)kGA * (NM + 1) * 8;
+    L.tab_l = (uint32_t)kGA * kMaxNL * 8;
+    L.off_stage = 1024;
+    L.off_tab = L.off_stage + stages * L.stage;
+    L.total = L.off_tab + 2 * (L.tab_m + L.tab_l);
+    return L;
+}
+
+// Named barrier 1 over the producer warps with an AND of their flags (every producer reaches it on
+// every group, so a timeout seen by one producer stops all of them together).
+template <int NPROD>
+__device__ __forceinline__ bool producers_all(bool ok) {
+    uint32_t res;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, 1, %2, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(res)
+        : "r"((uint32_t)ok), "n"(NPROD)
+        : "memory");
+    return res != 0;
+}
+
+__device__ __forceinline__ uint32_t pack_h2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// hi/lo FP16 split of two floats into packed halves
+__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = pack_h2(a - hf.x, b - hf.y);
+}
+
+template <int TPC>
+__global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
+    k_tc_sfac(View v, const uint4* __restrict__ atoms, int chunk, const int4* __restrict__ rows, TcDims d, int NM,
+              int KM, float* __restrict__ part, int rtot, uint32_t ncols) {
+    constexpr int kProd = P1<TPC>::kProd, kS = P1<TPC>::kS;
     extern __shared__ __align__(1024) unsigned char sm[];
+    const P1Layout L = p1_layout(TPC, kS, d.NP, NM);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const uint32_t aBytes = 8 * 4096;                 // [p][h][ks] 128 x 16 tiles
-    const uint32_t bTile = (uint32_t)d.NP * 32;       // NP x 16 tile
-    const uint32_t stBytes = aBytes + 8 * bTile;
-    unsigned char* stage0 = sm + 1024;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm);  // mma_done[2]
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 64);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm);
+    uint64_t* empty = full + kS;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     int* err = &v.status[ST_TC_TIMEOUT];
     const int a0 = blockIdx.y * chunk, a1 = min(v.nmove, a0 + chunk);
-    const int ngroup = (a1 > a0) ? (a1 - a0 + kG1 - 1) / kG1 : 0;
-    const int row_base = blockIdx.x * 128;
+    const int ngroup = a1 > a0 ? (a1 - a0 + kGA - 1) / kGA : 0;
+    const int row0 = blockIdx.x * (TPC * 128);
+    const int rlast = min(row0 + TPC * 128, d.nrow) - 1;
+    const int l_lo = rows[row0].x, nl = min(rows[rlast].x - l_lo + 1, kMaxNL - 1);
+    const int NM1 = NM + 1;
     if (t == 0) {
-        tc::mbar_init(tc::smem_u32(&bars[0]), 1);
-        tc::mbar_init(tc::smem_u32(&bars[1]), 1);
+        for (int i = 0; i < kS; ++i) {
+            tc::mbar_init(tc::smem_u32(&full[i]), kProd);
+            tc::mbar_init(tc::smem_u32(&empty[i]), 1);
+        }
         tc::mbar_fence_init();
     }
-    // zero both stages once (padding rows of B stay zero)
-    for (uint32_t o = t * 16; o < 2 * stBytes; o += kT * 16) *reinterpret_cast<uint4*>(stage0 + o) = make_uint4(0, 0, 0, 0);
+    // zero the ring (B rows beyond 2 NN stay zero) and both table buffers (padding slots stay zero)
+    for (uint32_t o = t * 16; o < L.total - L.off_stage; o += P1<TPC>::kThreads * 16)
+        *reinterpret_cast<uint4*>(sm + L.off_stage + o) = make_uint4(0, 0, 0, 0);
     if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), ncols);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t idesc = idesc_e(128, d.NP);
-    // this thread's row for the A operand
-    const int r = t & 127, ksA = t >> 7;
-    const int row = row_base + r;
-    int l = 0, m = 0;
-    const bool row_ok = row < d.nrow;
-    if (row_ok) {
-        const int4 rw = rows[row];
-        l = rw.x;
-        m = rw.y;
-    }
+    const uint32_t tcols = ncols / TPC;
     bool alive = true;
-    for (int g = 0; g < ngroup && alive; ++g) {
-        const int s = g & 1;
-        unsigned char* st = stage0 + s * stBytes;
-        if (g >= 2) alive = tc::mbar_wait(tc::smem_u32(&bars[s]), ((g >> 1) - 1) & 1, err, 11);
-        if (!alive) break;
-        const int gbase = a0 + g * kG1;
-        // A: row r, atoms ksA*16 .. +15, parts re/im, hi/lo
-        {
-            uint32_t w[4][8];  // [p*2+h][pair]
+    if (warp == kProd / 32) {
+        // ---------------- issuer
+        if (lane == 0) {
+            const uint32_t idesc = idesc_e(128, d.NP);
+            int committed = -1;
+            for (int g = 0; g < ngroup && alive; ++g) {
+                const int s = g % kS;
+                alive = tc::mbar_wait(tc::smem_u32(&full[s]), (g / kS) & 1, err, 11);
+                if (!alive) break;
+                tc::fence_after();
+                const uint32_t st = tc::smem_u32(sm + L.off_stage + s * L.stage);
+                const uint32_t bb = st + L.a_bytes;
 #pragma unroll
-            for (int i = 0; i < 16; i += 2) {
-                float ar[2], ai[2];
+                for (int p = 0; p < 2; ++p) {
+                    const uint64_t bh = tc::desc(bb + (p * 2 + 0) * L.b_tile);
+                    const uint64_t bl = tc::desc(bb + (p * 2 + 1) * L.b_tile);
 #pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const int at = gbase + ksA * 16 + i + e;
-                    ar[e] = ai[e] = 0.f;
-                    if (row_ok && at < a1) {
-                        const uint4 rec = atoms[at];
-                        float c, sn;
-                        phase((uint32_t)l * rec.x + (uint32_t)m * rec.y, c, sn);
-                        const float q = __uint_as_float(rec.w);
-                        ar[e] = q * c;
-                        ai[e] = q * sn;
+                    for (int tile = 0; tile < TPC; ++tile) {
+                        const uint64_t ah = tc::desc(st + ((tile * 2 + p) * 2 + 0) * 4096);
+                        const uint64_t al = tc::desc(st + ((tile * 2 + p) * 2 + 1) * 4096);
+                        const uint32_t dcol = tmem + tile * tcols;
+                        tc::mma_bf16(dcol, ah, bh, idesc, (g > 0 || p > 0) ? 1u : 0u);
+                        tc::mma_bf16(dcol, ah, bl, idesc, 1u);
+                        tc::mma_bf16(dcol, al, bh, idesc, 1u);
                     }
                 }
-                elem_t h0, l0, h1, l1;
-                tc::split(ar[0], h0, l0);
-                tc::split(ar[1], h1, l1);
-                w[0][i >> 1] = pack2(h0, h1);
-                w[1][i >> 1] = pack2(l0, l1);
-                tc::split(ai[0], h0, l0);
-                tc::split(ai[1], h1, l1);
-                w[2][i >> 1] = pack2(h0, h1);
-                w[3][i >> 1] = pack2(l0, l1);
+                tc::commit(tc::smem_u32(&empty[s]));
+                committed = g;
             }
-#pragma unroll
-            for (int ph = 0; ph < 4; ++ph) {
-                unsigned char* tile = st + (ph * 2 + ksA) * 4096;  // [p][h][ks]
-                *reinterpret_cast<uint4*>(tile + tc::tile_off(r, 0)) = make_uint4(w[ph][0], w[ph][1], w[ph][2], w[ph][3]);
-                *reinterpret_cast<uint4*>(tile + tc::tile_off(r, 8)) = make_uint4(w[ph][4], w[ph][5], w[ph][6], w[ph][7]);
-            }
+            // on a timeout, let the issued MMAs drain (bounded) before the block frees its TMEM
+            if (!alive && committed >= 0)
+                tc::mbar_wait(tc::smem_u32(&empty[committed % kS]), (committed / kS) & 1, nullptr, 0);
         }
-        // B: rows (re, n) and (im, n) for 16 atoms of one K step
-        if (t < 2 * d.NN) {
-            const int ni = t % d.NN, ks = t / d.NN;
-            const int n = ni - d.KN;
-            uint32_t wc[2][8], wsn[2][8], wns[2][8];  // [h][pair]: cos, sin, -sin
-#pragma unroll
-            for (int i = 0; i < 16; i += 2) {
-                float c2[2], s2[2];
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const int at = gbase + ks * 16 + i + e;
-                    c2[e] = s2[e] = 0.f;
-                    if (at < a1) phase((uint32_t)n * atoms[at].z, c2[e], s2[e]);
-                }
-                elem_t hc0, lc0, hc1, lc1, hs0, ls0, hs1, ls1;
-                tc::split(c2[0], hc0, lc0);
-                tc::split(c2[1], hc1, lc1);
-                tc::split(s2[0], hs0, ls0);
-                tc::split(s2[1], hs1, ls1);
-                wc[0][i >> 1] = pack2(hc0, hc1);
-                wc[1][i >> 1] = pack2(lc0, lc1);
-                wsn[0][i >> 1] = pack2(hs0, hs1);
-                wsn[1][i >> 1] = pack2(ls0, ls1);
-                wns[0][i >> 1] = pack2(eneg(hs0), eneg(hs1));
-                wns[1][i >> 1] = pack2(eneg(ls0), eneg(ls1));
-            }
-            unsigned char* bb = st + aBytes;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                // part 0: re row <- cos, im row <- sin ; part 1: re row <- -sin, im row <- cos
-                unsigned char* t0 = bb + ((0 * 2 + h) * 2 + ks) * bTile;
-                unsigned char* t1 = bb + ((1 * 2 + h) * 2 + ks) * bTile;
-                const int rre = ni, rim = d.NN + ni;
-                *reinterpret_cast<uint4*>(t0 + tc::tile_off(rre, 0)) = make_uint4(wc[h][0], wc[h][1], wc[h][2], wc[h][3]);
-                *reinterpret_cast<uint4*>(t0 + tc::tile_off(rre, 8)) = make_uint4(wc[h][4], wc[h][5], wc[h][6], wc[h][7]);
-                *reinterpret_cast<uint4*>(t0 + tc::tile_off(rim, 0)) = make_uint4(wsn[h][0], wsn[h][1], wsn[h][2], wsn[h][3]);
-                *reinterpret_cast<uint4*>(t0 + tc::tile_off(rim, 8)) = make_uint4(wsn[h][4], wsn[h][5], wsn[h][6], wsn[h][7]);
-                *reinterpret_cast<uint4*>(t1 + tc::tile_off(rre, 0)) = make_uint4(wns[h][0], wns[h][1], wns[h][2], wns[h][3]);
-                *reinterpret_cast<uint4*>(t1 + tc::tile_off(rre, 8)) = make_uint4(wns[h][4], wns[h][5], wns[h][6], wns[h][7]);
-                *reinterpret_cast<uint4*>(t1 + tc::tile_off(rim, 0)) = make_uint4(wc[h][0], wc[h][1], wc[h][2], wc[h][3]);
-                *reinterpret_cast<uint4*>(t1 + tc::tile_off(rim, 8)) = make_uint4(wc[h][4], wc[h][5], wc[h][6], wc[h][7]);
-            }
-        }
-        tc::fence_async_smem();
-        __syncthreads();
-        if (t == 0) {
-            tc::fence_after();
-            const uint32_t sbase = tc::smem_u32(st);
-#pragma unroll
-            for (int p = 0; p < 2; ++p)
-#pragma unroll
-                for (int ks = 0; ks < 2; ++ks) {
-                    const uint64_t ah = tc::desc(sbase + ((p * 2 + 0) * 2 + ks) * 4096);
-                    const uint64_t al = tc::desc(sbase + ((p * 2 + 1) * 2 + ks) * 4096);
-                    const uint64_t bh = tc::desc(sbase + aBytes + ((p * 2 + 0) * 2 + ks) * bTile);
-                    const uint64_t bl = tc::desc(sbase + aBytes + ((p * 2 + 1) * 2 + ks) * bTile);
-                    const uint32_t first = (g == 0 && p == 0 && ks == 0) ? 0u : 1u;
-                    tc::mma_bf16(tmem, ah, bh, idesc, first);
-                    tc::mma_bf16(tmem, ah, bl, idesc, 1u);
-                    tc::mma_bf16(tmem, al, bh, idesc, 1u);
-                }
-            tc::commit(tc::smem_u32(&bars[s]));
-        }
-    }
-    // all MMAs of this block done
-    if (ngroup > 0 && alive) alive = tc::mbar_wait(tc::smem_u32(&bars[(ngroup - 1) & 1]), ((ngroup - 1) >> 1) & 1, err, 12);
-    __syncthreads();
-    if (ngroup > 0 && t < 128) {
-        tc::fence_after();
-        int nf = 0, kf = 0, nl = 0;
-        if (row_ok) {
+    } else {
+        // ---------------- producers
+        const int r = t;                                 // CTA row (tile = r / 128)
+        const int row = row0 + r;
+        int li = kMaxNL - 1, mi = NM;                    // zero slots for padding rows
+        if (row < d.nrow) {
             const int4 rw = rows[row];
-            nf = rw.z;
-            kf = rw.w;
-            nl = nlen[row];
+            li = min(rw.x - l_lo, kMaxNL - 2);
+            mi = rw.y + KM;
         }
+        const int tile = r >> 7, rr = r & 127;
+        // this thread's table entries (the same every group): e^{i m ty} items, q e^{i l tx} items,
+        // and B items (n, atom pair)
+        const int nm_items = kGA * NM, nl_items = kGA * nl, nb_items = d.NN * (kGA / 2);
+        int im_j[kMaxItems], im_m[kMaxItems], il_j[kMaxItems], il_l[kMaxItems], ib_n[kMaxItems], ib_j[kMaxItems];
+#pragma unroll
+        for (int k = 0; k < kMaxItems; ++k) {
+            const int e = t + k * kProd;
+            im_j[k] = e < nm_items ? e / NM : -1;
+            im_m[k] = e < nm_items ? e % NM : 0;
+            il_j[k] = e < nl_items ? e / nl : -1;
+            il_l[k] = e < nl_items ? e % nl : 0;
+            ib_j[k] = e < nb_items ? (e / d.NN) * 2 : -1;
+            ib_n[k] = e < nb_items ? e % d.NN : 0;
+        }
+        for (int g = 0; g < ngroup; ++g) {
+            const int s = g % kS;
+            const int gb = a0 + g * kGA;
+            float2* tm = reinterpret_cast<float2*>(sm + L.off_tab + (g & 1) * (L.tab_m + L.tab_l));
+            float2* tl = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(tm) + L.tab_m);
+            bool ok = true;
+            if (g >= kS) ok = tc::mbar_wait(tc::smem_u32(&empty[s]), ((g / kS) - 1) & 1, err, 12);
+            unsigned char* st = sm + L.off_stage + s * L.stage;
+            unsigned char* bb = st + L.a_bytes;
+            if (ok) {
+#pragma unroll
+                for (int k = 0; k < kMaxItems; ++k) {
+                    if (im_j[k] >= 0) {
+                        const int at = gb + im_j[k];
+                        float c = 0.f, sn = 0.f;
+                        if (at < a1) phase((uint32_t)(im_m[k] - KM) * __ldg(&atoms[at].y), c, sn);
+                        tm[im_j[k] * NM1 + im_m[k]] = make_float2(c, sn);
+                    }
+                    if (il_j[k] >= 0) {
+                        const int at = gb + il_j[k];
+                        float c = 0.f, sn = 0.f;
+                        if (at < a1) {
+                            const uint4 rec = __ldg(&atoms[at]);
+                            phase((uint32_t)(il_l[k] + l_lo) * rec.x, c, sn);
+                            const float q = __uint_as_float(rec.w);
+                            c *= q;
+                            sn *= q;
+                        }
+                        tl[il_j[k] * kMaxNL + il_l[k]] = make_float2(c, sn);
+                    }
+                    if (ib_j[k] >= 0) {
+                        const int jp = ib_j[k], ni = ib_n[k];
+                        const uint32_t n = (uint32_t)(ni - d.KN);
+                        float c0 = 0.f, s0 = 0.f, c1 = 0.f, s1 = 0.f;
+                        if (gb + jp < a1) phase(n * __ldg(&atoms[gb + jp].z), c0, s0);
+                        if (gb + jp + 1 < a1) phase(n * __ldg(&atoms[gb + jp + 1].z), c1, s1);
+                        uint32_t ch, cl, sh, sl;
+                        split2(c0, c1, ch, cl);
+                        split2(s0, s1, sh, sl);
+                        const uint32_t ore = tc::tile_off(ni, jp), oim = tc::tile_off(d.NN + ni, jp);
+                        // part 0: re row <- cos, im row <- sin ; part 1: re row <- -sin, im row <- cos
+                        *reinterpret_cast<uint32_t*>(bb + 0 * L.b_tile + ore) = ch;
+                        *reinterpret_cast<uint32_t*>(bb + 1 * L.b_tile + ore) = cl;
+                        *reinterpret_cast<uint32_t*>(bb + 0 * L.b_tile + oim) = sh;
+                        *reinterpret_cast<uint32_t*>(bb + 1 * L.b_tile + oim) = sl;
+                        *reinterpret_cast<uint32_t*>(bb + 2 * L.b_tile + ore) = sh ^ 0x80008000u;
+                        *reinterpret_cast<uint32_t*>(bb + 3 * L.b_tile + ore) = sl ^ 0x80008000u;
+                        *reinterpret_cast<uint32_t*>(bb + 2 * L.b_tile + oim) = ch;
+                        *reinterpret_cast<uint32_t*>(bb + 3 * L.b_tile + oim) = cl;
+                    }
+                }
+            }
+            if (!producers_all<kProd>(ok)) {
+                alive = false;
+                break;
+            }
+            // A: this row's 16 entries q e^{i l tx} e^{i m ty} (zero for padding rows)
+            uint32_t wrh[8], wrl[8], wih[8], wil[8];
+#pragma unroll
+            for (int j = 0; j < kGA; j += 2) {
+                const float2 el0 = tl[j * kMaxNL + li], em0 = tm[j * NM1 + mi];
+                const float2 el1 = tl[(j + 1) * kMaxNL + li], em1 = tm[(j + 1) * NM1 + mi];
+                const float re0 = el0.x * em0.x - el0.y * em0.y, im0 = el0.x * em0.y + el0.y * em0.x;
+                const float re1 = el1.x * em1.x - el1.y * em1.y, im1 = el1.x * em1.y + el1.y * em1.x;
+                split2(re0, re1, wrh[j >> 1], wrl[j >> 1]);
+                split2(im0, im1, wih[j >> 1], wil[j >> 1]);
+            }
+            unsigned char* ta = st + (tile * 2) * 2 * 4096;   // [tile][p][h]
+            const uint32_t o0 = tc::tile_off(rr, 0), o8 = tc::tile_off(rr, 8);
+            *reinterpret_cast<uint4*>(ta + 0 * 4096 + o0) = make_uint4(wrh[0], wrh[1], wrh[2], wrh[3]);
+            *reinterpret_cast<uint4*>(ta + 0 * 4096 + o8) = make_uint4(wrh[4], wrh[5], wrh[6], wrh[7]);
+            *reinterpret_cast<uint4*>(ta + 1 * 4096 + o0) = make_uint4(wrl[0], wrl[1], wrl[2], wrl[3]);
+            *reinterpret_cast<uint4*>(ta + 1 * 4096 + o8) = make_uint4(wrl[4], wrl[5], wrl[6], wrl[7]);
+            *reinterpret_cast<uint4*>(ta + 2 * 4096 + o0) = make_uint4(wih[0], wih[1], wih[2], wih[3]);
+            *reinterpret_cast<uint4*>(ta + 2 * 4096 + o8) = make_uint4(wih[4], wih[5], wih[6], wih[7]);
+            *reinterpret_cast<uint4*>(ta + 3 * 4096 + o0) = make_uint4(wil[0], wil[1], wil[2], wil[3]);
+            *reinterpret_cast<uint4*>(ta + 3 * 4096 + o8) = make_uint4(wil[4], wil[5], wil[6], wil[7]);
+            tc::fence_async_smem();
+            tc::mbar_arrive(tc::smem_u32(&full[s]));
+        }
+        // all MMAs done -> accumulators to the partial-sum buffer
+        if (ngroup > 0 && alive)
+            alive = tc::mbar_wait(tc::smem_u32(&empty[(ngroup - 1) % kS]), ((ngroup - 1) / kS) & 1, err, 13);
+        tc::fence_after();
+        const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + tile * tcols;
+        float* dst = part + (size_t)blockIdx.y * d.NP * rtot;
         for (int cc = 0; cc < d.NP / 16; ++cc) {
             float val[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + cc * 16, val);
-            if (!row_ok || !alive) continue;
+            tc::tmem_ld16(tbase + cc * 16, val);
+            if (!alive) continue;
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                const int col = cc * 16 + c;
-                if (col >= 2 * d.NN) continue;
-                const int comp = col >= d.NN ? 1 : 0;
-                const int n = (comp ? col - d.NN : col) - d.KN;
-                if (n < nf || n >= nf + nl) continue;
-                double* dst = comp ? &S[kf + n - nf].y : &S[kf + n - nf].x;
-                atomicAdd(dst, (double)val[c]);
-            }
+            for (int c = 0; c < 16; ++c) dst[(size_t)(cc * 16 + c) * rtot + row] = ngroup > 0 ? val[c] : 0.f;
         }
         tc::fence_before();
     }
@@ -249,25 +319,56 @@ __global__ void __launch_bounds__(kT, 1) k_tc_sfac(View v, const uint4* __restri
         tc::fence_after();
         tc::tmem_dealloc(tmem, ncols);
     }
-    (void)lane;
+}
+
+// Split-K reduction of pass 1 fused with the energy (src/forcem.f90:880-885,917), C(k) = Ak
+// conj(S + S_wall) and the scale max |C| max(1, |n|) of the pass-2 operand.  One thread per
+// (row, n); partial sums added in compensated FP32 (nsplit values), the result kept in FP64.
+__global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit, int rtot, TcDims d,
+                             const int4* __restrict__ rows, const int* __restrict__ nlen, const double* __restrict__ ak,
+                             const double2* __restrict__ qw, double2* S, double2* C, float* cmax) {
+    double ew = 0.0, ll = 0.0;
+    float mx = 0.f;
+    const long total = (long)d.nrow * d.NN;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+        const int row = (int)(e % d.nrow), ni = (int)(e / d.nrow);
+        const int4 rw = rows[row];
+        const int n = ni - d.KN;
+        if (n < rw.z || n >= rw.z + nlen[row]) continue;
+        float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+        for (int sp = 0; sp < nsplit; ++sp) {
+            const float* pp = part + (size_t)sp * d.NP * rtot;
+            const float xr = pp[(size_t)ni * rtot + row] - cr;
+            const float tr = sr + xr;
+            cr = (tr - sr) - xr;
+            sr = tr;
+            const float xi = pp[(size_t)(d.NN + ni) * rtot + row] - ci;
+            const float ti = si + xi;
+            ci = (ti - si) - xi;
+            si = ti;
+        }
+        const int k = rw.w + n - rw.z;
+        const double2 sv = make_double2((double)sr - (double)cr, (double)si - (double)ci);
+        S[k] = sv;
+        const double2 st = make_double2(sv.x + qw[k].x, sv.y + qw[k].y);
+        const double a = ak[k];
+        ll += a * (sv.x * sv.x + sv.y * sv.y);
+        ew += a * (st.x * st.x + st.y * st.y);
+        const double2 cv = make_double2(a * st.x, -a * st.y);
+        C[k] = cv;
+        const float w = (float)max(1, abs(n));
+        mx = fmaxf(mx, fmaxf(fabsf((float)cv.x), fabsf((float)cv.y)) * w);
+    }
+    block_atomic_sum<256>(ew, &v.acc[2 * v.nijt + ACC_UEWA]);
+    block_atomic_sum<256>(ll, &v.acc[2 * v.nijt + ACC_EWQLL]);
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned int*>(cmax), __float_as_uint(mx));
 }
 
 // ---------------------------------------------------------------------------------------------
 // C(k) packed as the pass-2 B operand: chunk c holds rows 32c..32c+31, columns
 // col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part.
 // ---------------------------------------------------------------------------------------------
-// max |C| * max(1, |n|) over the k set (non-negative floats order like their bits)
-__global__ void k_tc_cmax(const double2* __restrict__ C, const int3* __restrict__ kv, int nk, float* cmax) {
-    float m = 0.f;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nk; k += gridDim.x * blockDim.x) {
-        const double2 c = C[k];
-        const double w = fmax(1.0, fabs((double)kv[k].z));
-        m = fmaxf(m, (float)(fmax(fabs(c.x), fabs(c.y)) * w));
-    }
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned int*>(cmax), __float_as_uint(m));
-}
-
 __global__ void k_tc_prep_c(const double2* __restrict__ C, const int4* __restrict__ rows,
                             const int* __restrict__ nlen, TcDims d, unsigned char* img, const float* cmax) {
     const double inv = cmax[0] > 0.f ? 1.0 / (double)cmax[0] : 1.0;
@@ -504,22 +605,34 @@ int recip_tc_setup(Ctx& c) {
     p.NN = 2 * ks.knmax + 1;
     p.NP = (2 * p.NN + 15) / 16 * 16;
     p.KS = (2 * p.NN + 15) / 16;
+    p.KM = ks.kmmax;
+    p.NM = 2 * ks.kmmax + 1;
     if (p.NP > 256) return set_err(&c, MDG_E_UNSUPPORTED, "knmax too large for the tensor-core reciprocal sum");
-    p.ncols1 = p.NP <= 128 ? 128 : 256;
+    if (ks.klmax + 1 > kMaxNL - 1) return set_err(&c, MDG_E_UNSUPPORTED, "klmax too large for the tensor-core reciprocal sum");
+    p.tpc1 = p.NP <= 128 ? 4 : 2;
+    p.ncols1 = p.tpc1 * (p.NP <= 128 ? 128 : 256);
+    p.grid1x = (ks.nrow + p.tpc1 * 128 - 1) / (p.tpc1 * 128);
+    p.rtot = p.grid1x * p.tpc1 * 128;
+    p.nsplit1 = std::max(1, std::min(152 / p.grid1x, (v.nmove + 127) / 128));
+    p.chunk1 = (v.nmove + p.nsplit1 - 1) / p.nsplit1;
+    p.chunk1 = std::max(kGA, (p.chunk1 + kGA - 1) / kGA * kGA);
+    p.nsplit1 = std::max(1, (v.nmove + p.chunk1 - 1) / p.chunk1);
+    if (kGA * p.NM > kMaxItems * 128 * p.tpc1 || kGA * (kMaxNL - 1) > kMaxItems * 128 * p.tpc1 ||
+        p.NN * (kGA / 2) > kMaxItems * 128 * p.tpc1)
+        return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core table fill");
     p.mtiles = (ks.nrow + 127) / 128;
     p.nchunk2 = (ks.nrow + 31) / 32;
-    const long want = (long)v.nmove * p.mtiles / (2 * 152);
-    p.chunk1 = (int)std::max<long>(kG1, (want + kG1 - 1) / kG1 * kG1);
-    p.nsplit1 = (v.nmove + p.chunk1 - 1) / p.chunk1;
-    p.smem1 = 1024 + 2 * (8 * 4096 + 8 * p.NP * 32);
+    p.smem1 = (int)(p.tpc1 == 4 ? p1_layout(4, P1<4>::kS, p.NP, p.NM).total : p1_layout(2, P1<2>::kS, p.NP, p.NM).total);
     p.smem2 = 1024 + 3 * 2 * p.KS * 4096;
     if (p.smem1 > 227 * 1024 || p.smem2 > 227 * 1024)
-        return set_err(&c, MDG_E_UNSUPPORTED, "knmax too large for the tensor-core shared-memory tiles");
+        return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
     c.d_tc_atoms = (uint4*)dalloc(c, sizeof(uint4) * std::max(v.nmove, 1));
     c.d_tc_img = (unsigned char*)dalloc(c, (size_t)std::max(p.nchunk2, 1) * 2 * p.KS * 4096);
     c.d_tc_cmax = (float*)dalloc(c, sizeof(float) * 4);
+    c.d_tc_part = (float*)dalloc(c, sizeof(float) * (size_t)p.nsplit1 * p.NP * p.rtot);
     if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
-    MDG_CUDA(cudaFuncSetAttribute(k_tc_sfac, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem1));
+    MDG_CUDA(cudaFuncSetAttribute(k_tc_sfac<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem1));
+    MDG_CUDA(cudaFuncSetAttribute(k_tc_sfac<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem1));
     MDG_CUDA(cudaFuncSetAttribute(k_tc_force, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem2));
     p.ready = true;
     return MDG_OK;
@@ -531,13 +644,17 @@ void recip_tc(Ctx& c) {
     const TcPlan& p = c.tcp;
     if (ks.nk == 0 || v.nmove == 0) return;
     TcDims d{p.KN, p.NN, p.NP, p.KS, ks.nrow, p.nchunk2, (float)ks.pipix, (float)ks.pipiy, (float)ks.pipiz};
-    k_tc_prep_atoms<<<(v.nmove + 255) / 256, 256, 0, c.stream>>>(v, c.d_tc_atoms);
-    cudaMemsetAsync(ks.s, 0, sizeof(double2) * ks.nk, c.stream);
-    k_tc_sfac<<<dim3(p.mtiles, p.nsplit1), kT, p.smem1, c.stream>>>(v, c.d_tc_atoms, p.chunk1, ks.row, ks.row_nlen, d,
-                                                                    ks.s, (uint32_t)p.ncols1);
-    recip_energy_launch(c);
+    // c.d_tc_atoms was filled by the packing kernel of the real-space phase of this evaluation
     cudaMemsetAsync(c.d_tc_cmax, 0, sizeof(float), c.stream);
-    k_tc_cmax<<<std::min((ks.nk + 255) / 256, 152), 256, 0, c.stream>>>(ks.c, ks.kvec, ks.nk, c.d_tc_cmax);
+    if (p.tpc1 == 4)
+        k_tc_sfac<4><<<dim3(p.grid1x, p.nsplit1), P1<4>::kThreads, p.smem1, c.stream>>>(
+            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1);
+    else
+        k_tc_sfac<2><<<dim3(p.grid1x, p.nsplit1), P1<2>::kThreads, p.smem1, c.stream>>>(
+            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1);
+    const long nred = (long)ks.nrow * p.NN;
+    k_tc_sreduce<<<(int)std::min<long>((nred + 255) / 256, 152 * 4), 256, 0, c.stream>>>(
+        v, c.d_tc_part, p.nsplit1, p.rtot, d, ks.row, ks.row_nlen, ks.ak, ks.qw, ks.s, ks.c, c.d_tc_cmax);
     const long total = (long)p.nchunk2 * p.KS * 128 * 16;
     k_tc_prep_c<<<(int)std::min<long>((total + 255) / 256, 152 * 8), 256, 0, c.stream>>>(ks.c, ks.row, ks.row_nlen, d,
                                                                                          c.d_tc_img, c.d_tc_cmax);
