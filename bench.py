@@ -504,7 +504,7 @@ def main():
         print(json.dumps(reference_arm(args)))
         return
     if args.gpus > 1 or int(os.environ.get("WORLD_SIZE", "1")) > 1:
-        # replicas only: every rank runs its own system; rank 0 reports its own
+        # replicas only: every rank runs its own independent system; rank 0 reports its own
         pass
     out = gpu_arm(args)
     if rank == 0:

@@ -121,6 +121,7 @@ struct TcPlan {
     bool ready = false;
     int KN = 0, NN = 0, NP = 0, KS = 0, KM = 0, NM = 0;
     int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, grid1x = 0, rtot = 0, tpc1 = 0, smem1 = 0, smem2 = 0;
+    int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0;
 };
 
 struct Ctx {
@@ -134,6 +135,7 @@ struct Ctx {
     unsigned char* d_tc_img = nullptr;  // packed C(k) operand chunks
     float* d_tc_cmax = nullptr;         // scale of the packed C(k) operand
     float* d_tc_part = nullptr;         // pass-1 partial sums [split][col][row]
+    float2* d_tc_cf = nullptr;          // C(k) in FP32 for the pass-2 operand
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the context's stream while a caller's stream is in use
     int device = 0;

@@ -27,15 +27,11 @@ namespace mdg {
 
 namespace {
 
-constexpr int kT = 256;      // threads per CTA
 constexpr float kPhase = 1.4629180792671596e-09f;  // 2 pi / 2^32
 
-// Operand type of the hi/lo split.  FP16 keeps 11 + 11 significant bits (BF16: 8 + 8); all
-// operands are O(1) (phase factors, charges, and C(k) scaled by the step's max |n C|).
-typedef __half elem_t;
+// Operands are FP16 hi/lo splits (11 + 11 significant bits; BF16 would give 8 + 8); all are O(1)
+// (phase factors, charges, and C(k) scaled by the step's max |n C|).
 __device__ __forceinline__ uint32_t idesc_e(int M, int N) { return tc::idesc_f16(M, N); }
-__device__ __forceinline__ uint16_t ebits(elem_t h) { return __half_as_ushort(h); }
-__device__ __forceinline__ elem_t eneg(elem_t h) { return __hneg(h); }
 
 struct TcDims {
     int KN, NN;      // n range -KN..KN, NN = 2 KN + 1
@@ -49,9 +45,6 @@ __device__ __forceinline__ void phase(uint32_t u, float& c, float& s) {
     __sincosf((float)(int32_t)u * kPhase, &s, &c);
 }
 
-__device__ __forceinline__ uint32_t pack2(elem_t a, elem_t b) {
-    return (uint32_t)ebits(a) | ((uint32_t)ebits(b) << 16);
-}
 
 // ---------------------------------------------------------------------------------------------
 // pass 1: structure factor
@@ -165,22 +158,23 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
         // ---------------- issuer
         if (lane == 0) {
             const uint32_t idesc = idesc_e(128, d.NP);
+            const uint64_t dS0 = tc::desc(tc::smem_u32(sm + L.off_stage));
             int committed = -1;
             for (int g = 0; g < ngroup && alive; ++g) {
                 const int s = g % kS;
                 alive = tc::mbar_wait(tc::smem_u32(&full[s]), (g / kS) & 1, err, 11);
                 if (!alive) break;
                 tc::fence_after();
-                const uint32_t st = tc::smem_u32(sm + L.off_stage + s * L.stage);
-                const uint32_t bb = st + L.a_bytes;
+                const uint64_t ds = dS0 + (uint64_t)((s * L.stage) >> 4);
+                const uint64_t db = ds + (uint64_t)(L.a_bytes >> 4);
 #pragma unroll
                 for (int p = 0; p < 2; ++p) {
-                    const uint64_t bh = tc::desc(bb + (p * 2 + 0) * L.b_tile);
-                    const uint64_t bl = tc::desc(bb + (p * 2 + 1) * L.b_tile);
+                    const uint64_t bh = db + (uint64_t)(((p * 2 + 0) * L.b_tile) >> 4);
+                    const uint64_t bl = db + (uint64_t)(((p * 2 + 1) * L.b_tile) >> 4);
 #pragma unroll
                     for (int tile = 0; tile < TPC; ++tile) {
-                        const uint64_t ah = tc::desc(st + ((tile * 2 + p) * 2 + 0) * 4096);
-                        const uint64_t al = tc::desc(st + ((tile * 2 + p) * 2 + 1) * 4096);
+                        const uint64_t ah = ds + (uint64_t)(((tile * 2 + p) * 2 + 0) * 256);
+                        const uint64_t al = ds + (uint64_t)(((tile * 2 + p) * 2 + 1) * 256);
                         const uint32_t dcol = tmem + tile * tcols;
                         tc::mma_bf16(dcol, ah, bh, idesc, (g > 0 || p > 0) ? 1u : 0u);
                         tc::mma_bf16(dcol, ah, bl, idesc, 1u);
@@ -326,7 +320,7 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
 // (row, n); partial sums added in compensated FP32 (nsplit values), the result kept in FP64.
 __global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit, int rtot, TcDims d,
                              const int4* __restrict__ rows, const int* __restrict__ nlen, const double* __restrict__ ak,
-                             const double2* __restrict__ qw, double2* S, double2* C, float* cmax) {
+                             const double2* __restrict__ qw, double2* S, double2* C, float2* Cf, float* cmax) {
     double ew = 0.0, ll = 0.0;
     float mx = 0.f;
     const long total = (long)d.nrow * d.NN;
@@ -356,6 +350,7 @@ __global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit,
         ew += a * (st.x * st.x + st.y * st.y);
         const double2 cv = make_double2(a * st.x, -a * st.y);
         C[k] = cv;
+        Cf[k] = make_float2((float)cv.x, (float)cv.y);
         const float w = (float)max(1, abs(n));
         mx = fmaxf(mx, fmaxf(fabsf((float)cv.x), fabsf((float)cv.y)) * w);
     }
@@ -366,176 +361,320 @@ __global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit,
 }
 
 // ---------------------------------------------------------------------------------------------
-// C(k) packed as the pass-2 B operand: chunk c holds rows 32c..32c+31, columns
-// col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part.
+// C(k) packed as the pass-2 B operand: chunk c holds rows kRC c .. kRC c + kRC - 1, columns
+// col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part; one thread
+// per (chunk, K step, column, n) writes the (part 0, part 1) half pairs of hi and lo.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_tc_prep_c(const double2* __restrict__ C, const int4* __restrict__ rows,
+constexpr int kRC = 16;                 // rows per pass-2 chunk
+constexpr int kNC2 = 4 * kRC;           // pass-2 MMA N
+constexpr uint32_t kTile2 = kNC2 * 32;  // one N x 16 B tile (bytes)
+
+__global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restrict__ rows,
                             const int* __restrict__ nlen, TcDims d, unsigned char* img, const float* cmax) {
-    const double inv = cmax[0] > 0.f ? 1.0 / (double)cmax[0] : 1.0;
-    const long total = (long)d.nchunk2 * d.KS * 128 * 16;
-    const long chunkBytes = 2L * d.KS * 4096;
+    const float inv = cmax[0] > 0.f ? 1.0f / cmax[0] : 1.0f;
+    const long total = (long)d.nchunk2 * d.KS * kNC2 * 8;
+    const long chunkBytes = 2L * d.KS * kTile2;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-        const int kk = e & 15;
-        const int col = (e >> 4) & 127;
-        const long rest = e >> 11;
+        const int i8 = (int)(e & 7);
+        const int col = (int)((e >> 3) % kNC2);
+        const long rest = (e >> 3) / kNC2;
         const int ks = (int)(rest % d.KS);
         const int c = (int)(rest / d.KS);
-        const int row = c * 32 + (col >> 2), tt = (col >> 1) & 1, comp = col & 1;
-        const int k2 = ks * 16 + kk, ni = k2 >> 1, part = k2 & 1;
-        float val = 0.f;
+        const int row = c * kRC + (col >> 2), tt = (col >> 1) & 1, comp = col & 1;
+        const int ni = ks * 8 + i8;
+        float v0 = 0.f, v1 = 0.f;
         if (row < d.nrow && ni < d.NN) {
             const int4 rw = rows[row];
             const int n = ni - d.KN;
             if (n >= rw.z && n < rw.z + nlen[row]) {
-                const double2 cv = C[rw.w + n - rw.z];
-                const double sc = (tt ? (double)n : 1.0) * inv;
-                const double cr = cv.x * sc, ci = cv.y * sc;
-                const double vv = comp == 0 ? (part == 0 ? cr : -ci) : (part == 0 ? ci : cr);
-                val = (float)vv;
+                const float2 cv = Cf[rw.w + n - rw.z];
+                const float sc = (tt ? (float)n : 1.0f) * inv;
+                const float cr = cv.x * sc, ci = cv.y * sc;
+                v0 = comp == 0 ? cr : ci;   // part 0
+                v1 = comp == 0 ? -ci : cr;  // part 1
             }
         }
-        elem_t h, lo;
-        tc::split(val, h, lo);
+        uint32_t hi, lo;
+        split2(v0, v1, hi, lo);
         unsigned char* base = img + c * chunkBytes;
-        const uint32_t off = tc::tile_off(col, kk);
-        *reinterpret_cast<elem_t*>(base + (0 * d.KS + ks) * 4096 + off) = h;
-        *reinterpret_cast<elem_t*>(base + (1 * d.KS + ks) * 4096 + off) = lo;
+        const uint32_t off = tc::tile_off(col, 2 * i8);
+        *reinterpret_cast<uint32_t*>(base + (0 * d.KS + ks) * kTile2 + off) = hi;
+        *reinterpret_cast<uint32_t*>(base + (1 * d.KS + ks) * kTile2 + off) = lo;
     }
 }
 
 // ---------------------------------------------------------------------------------------------
 // pass 2: forces
+//
+// Work items (a tile of 256 atoms, a range of row chunks) are spread over a persistent grid.
+// Per item the epilogue warps build A = e^{i n tz} of the tile's atoms (two M = 128 operands,
+// K = 2 (n + KN) + part); the issuer thread streams the chunk images of C through a 3-deep ring
+// with cp.async.bulk and, per chunk, issues 3 (hi/lo) products per K step for both operands into
+// a 4-deep ring of TMEM accumulator pairs (N = 64: T and T' of 16 rows).  Two epilogue threads
+// own each atom, one per half of a chunk's rows: per row a thread forms Im(e^{i(l tx + m ty)} T)
+// with the row phase advanced along m by a complex multiply (recomputed by __sincosf at the first
+// of its 8 rows and at each change of l), and sums the force components; forces are added once
+// per item.
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kT, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
-                                                    const unsigned char* __restrict__ img,
-                                                    const int4* __restrict__ rows, TcDims d, const float* cmax) {
+constexpr int kMT2 = 2;                 // M tiles per item (256 atoms)
+constexpr int kS2 = 3;                  // B ring depth
+constexpr int kAB2 = 4;                 // TMEM accumulator ring depth (kAB2 x kMT2 x 64 columns)
+constexpr int kEW2 = kMT2 * 4 * 2;      // epilogue warps: (M tile, lane quadrant, row half)
+constexpr int kT2 = kEW2 * 32 + 32;     // + issuer warp
+
+// j-th chunk of an item: every item walks its chunk range from a different starting point, so
+// that the CTAs do not all read the same chunk image (the same L2 lines) at the same time
+__device__ __forceinline__ int item_chunk(int it, int j, int c0, int cnt) {
+    return c0 + (int)((j + (unsigned)it * 7919u % (unsigned)cnt) % (unsigned)cnt);
+}
+
+struct P2Layout {
+    uint32_t a_bytes, img, off_a, off_b, off_rows, total;
+};
+
+__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad) {
+    P2Layout L;
+    L.a_bytes = kMT2 * 2 * KS * 4096;        // [mt][h][ks] 128 x 16
+    L.img = 2 * KS * kTile2;                 // [h][ks] 64 x 16
+    L.off_a = 1024;
+    L.off_b = L.off_a + L.a_bytes;
+    L.off_rows = L.off_b + kS2 * L.img;
+    L.total = L.off_rows + nrow_pad * 8;     // (l, m) per row
+    return L;
+}
+
+__global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
+                                                     const unsigned char* __restrict__ img,
+                                                     const int4* __restrict__ rows, TcDims d, const float* cmax,
+                                                     int ntile, int nparts, int cper) {
     extern __shared__ __align__(1024) unsigned char sm[];
+    const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const uint32_t tileB = 4096;
-    const uint32_t halfBytes = d.KS * tileB;   // one of hi / lo
-    const uint32_t imgBytes = 2 * halfBytes;   // a chunk image
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm);  // full[2], mma_done[2], acc_free[2]
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 64);
-    unsigned char* Asm = sm + 1024;            // [h][ks] 128 x 16
-    unsigned char* Bsm = Asm + imgBytes;       // [s][h][ks]
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm);      // [kS2] chunk image landed
+    uint64_t* bfree = full + kS2;                           // [kS2] MMAs of the stage done
+    uint64_t* accf = bfree + kS2;                           // [kAB2] accumulator ready
+    uint64_t* acce = accf + kAB2;                           // [kAB2] accumulator drained (epilogue warps)
+    uint64_t* afree = acce + kAB2;                          // MMAs of the item done
+    uint64_t* aready = afree + 1;                           // A built (epilogue threads)
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
+    int2* rlm = reinterpret_cast<int2*>(sm + L.off_rows);
     int* err = &v.status[ST_TC_TIMEOUT];
-    const int atom0 = blockIdx.x * 128;
+    const int NC = d.nchunk2;
+    const int nitem = ntile * nparts;
     if (t == 0) {
-        for (int b = 0; b < 6; ++b) tc::mbar_init(tc::smem_u32(&bars[b]), b >= 4 ? 4 : 1);
+        for (int i = 0; i < kS2; ++i) {
+            tc::mbar_init(tc::smem_u32(&full[i]), 1);
+            tc::mbar_init(tc::smem_u32(&bfree[i]), 1);
+        }
+        for (int i = 0; i < kAB2; ++i) {
+            tc::mbar_init(tc::smem_u32(&accf[i]), 1);
+            tc::mbar_init(tc::smem_u32(&acce[i]), kEW2);
+        }
+        tc::mbar_init(tc::smem_u32(afree), 1);
+        tc::mbar_init(tc::smem_u32(aready), kEW2 * 32);
         tc::mbar_fence_init();
     }
-    if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 256);
-    // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part
-    {
-        const int mrow = t & 127, half = t >> 7;
-        const int at = atom0 + mrow;
-        const uint32_t uz = at < v.nmove ? atoms[at].z : 0u;
-        const int ksplit = (d.KS + 1) / 2;
-        const int ks0 = half ? ksplit : 0, ks1 = half ? d.KS : ksplit;
-        for (int ks = ks0; ks < ks1; ++ks) {
-            uint32_t wh[8], wl[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int ni = ks * 8 + i;
-                float c = 0.f, s = 0.f;
-                if (at < v.nmove && ni < d.NN) phase((uint32_t)(ni - d.KN) * uz, c, s);
-                elem_t hc, lc, hs, ls;
-                tc::split(c, hc, lc);
-                tc::split(s, hs, ls);
-                wh[i] = pack2(hc, hs);
-                wl[i] = pack2(lc, ls);
-            }
-            unsigned char* th = Asm + (0 * d.KS + ks) * tileB;
-            unsigned char* tl = Asm + (1 * d.KS + ks) * tileB;
-            *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 0)) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
-            *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 8)) = make_uint4(wh[4], wh[5], wh[6], wh[7]);
-            *reinterpret_cast<uint4*>(tl + tc::tile_off(mrow, 0)) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
-            *reinterpret_cast<uint4*>(tl + tc::tile_off(mrow, 8)) = make_uint4(wl[4], wl[5], wl[6], wl[7]);
-        }
+    for (int r = t; r < NC * kRC; r += kT2) {
+        const int4 rw = r < d.nrow ? rows[r] : make_int4(0, 0, 0, 0);
+        rlm[r] = make_int2(rw.x, rw.y);
     }
-    tc::fence_async_smem();
+    if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 512);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t idesc = idesc_e(128, 128);
-    const int NC = d.nchunk2;
-    if (warp == 4) {
+    const uint32_t imgBytes = L.img, halfBytes = L.img / 2;
+    if (warp == kEW2) {
+        // ---------------- issuer: copies and MMAs over the flat (item, chunk) sequence
         if (lane == 0) {
-            const uint32_t abase = tc::smem_u32(Asm), bbase = tc::smem_u32(Bsm);
+            const uint32_t idesc = idesc_e(128, kNC2);
+            const uint32_t abase = tc::smem_u32(sm + L.off_a), bbase = tc::smem_u32(sm + L.off_b);
+            const uint64_t dA0 = tc::desc(abase), dB0 = tc::desc(bbase);
             bool alive = true;
-            for (int c = 0; c < NC && alive; ++c) {
-                const int s = c & 1;
-                if (c >= 2) alive = tc::mbar_wait(tc::smem_u32(&bars[2 + s]), ((c >> 1) - 1) & 1, err, 21);
+            long seq = 0, copied = 0, last_commit = -1;
+            int nitems_done = 0;
+            // the flat list of chunks this CTA processes
+            auto chunk_of = [&](long q, int& item_out) -> int {
+                // q-th chunk of this CTA: items blockIdx.x, blockIdx.x + gridDim.x, ...
+                int it = blockIdx.x;
+                long left = q;
+                while (it < nitem) {
+                    const int part = it % nparts;
+                    const int c0 = part * cper, c1 = min(NC, c0 + cper);
+                    const int cnt = max(0, c1 - c0);
+                    if (left < cnt) {
+                        item_out = it;
+                        return item_chunk(it, (int)left, c0, cnt);
+                    }
+                    left -= cnt;
+                    it += gridDim.x;
+                }
+                item_out = -1;
+                return -1;
+            };
+            auto issue_copy = [&](long q) {
+                int it;
+                const int c = chunk_of(q, it);
+                if (c < 0) return false;
+                const int s = (int)(q % kS2);
+                if (q >= kS2) {
+                    if (!tc::mbar_wait(tc::smem_u32(&bfree[s]), (int)((q / kS2) - 1) & 1, err, 21)) return false;
+                }
+                const uint32_t fb = tc::smem_u32(&full[s]);
+                tc::mbar_expect_tx(fb, imgBytes);
+                tc::bulk_g2s(bbase + s * imgBytes, img + (size_t)c * imgBytes, halfBytes, fb);
+                tc::bulk_g2s(bbase + s * imgBytes + halfBytes, img + (size_t)c * imgBytes + halfBytes, halfBytes, fb);
+                return true;
+            };
+            for (; copied < kS2; ++copied)
+                if (!issue_copy(copied)) break;
+            int cur_item = -1;
+            for (;; ++seq) {
+                int it;
+                const int c = chunk_of(seq, it);
+                if (c < 0) break;
+                if (it != cur_item) {
+                    // a new item: its A operand must be built (after the previous item's MMAs)
+                    if (cur_item >= 0) {
+                        tc::commit(tc::smem_u32(afree));
+                        ++nitems_done;
+                    }
+                    cur_item = it;
+                    alive = tc::mbar_wait(tc::smem_u32(aready), (nitems_done & 1), err, 22);
+                    if (!alive) break;
+                }
+                const int s = (int)(seq % kS2);
+                alive = tc::mbar_wait(tc::smem_u32(&full[s]), (int)(seq / kS2) & 1, err, 23);
                 if (!alive) break;
-                const uint32_t full = tc::smem_u32(&bars[s]);
-                tc::mbar_expect_tx(full, imgBytes);
-                tc::bulk_g2s(bbase + s * imgBytes, img + (size_t)c * imgBytes, halfBytes, full);
-                tc::bulk_g2s(bbase + s * imgBytes + halfBytes, img + (size_t)c * imgBytes + halfBytes, halfBytes, full);
-                alive = tc::mbar_wait(full, (c >> 1) & 1, err, 22);
-                if (!alive) break;
-                if (c >= 2) alive = tc::mbar_wait(tc::smem_u32(&bars[4 + s]), ((c >> 1) - 1) & 1, err, 23);
+                const int ab = (int)(seq % kAB2);
+                if (seq >= kAB2) alive = tc::mbar_wait(tc::smem_u32(&acce[ab]), (int)((seq / kAB2) - 1) & 1, err, 24);
                 if (!alive) break;
                 tc::fence_after();
-                const uint32_t dcol = tmem + s * 128;
-                for (int ks = 0; ks < d.KS; ++ks) {
-                    const uint64_t ah = tc::desc(abase + (0 * d.KS + ks) * tileB);
-                    const uint64_t al = tc::desc(abase + (1 * d.KS + ks) * tileB);
-                    const uint64_t bh = tc::desc(bbase + s * imgBytes + (0 * d.KS + ks) * tileB);
-                    const uint64_t bl = tc::desc(bbase + s * imgBytes + (1 * d.KS + ks) * tileB);
-                    tc::mma_bf16(dcol, ah, bh, idesc, ks > 0 ? 1u : 0u);
-                    tc::mma_bf16(dcol, ah, bl, idesc, 1u);
-                    tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                // descriptors advance linearly with the shared address (16-byte units)
+                const uint64_t dB = dB0 + (uint64_t)((s * imgBytes) >> 4);
+#pragma unroll
+                for (int mt = 0; mt < kMT2; ++mt) {
+                    const uint32_t dcol = tmem + ab * (kMT2 * kNC2) + mt * kNC2;
+                    const uint64_t dAh = dA0 + (uint64_t)((mt * 2 + 0) * d.KS * 256);
+                    const uint64_t dAl = dA0 + (uint64_t)((mt * 2 + 1) * d.KS * 256);
+                    const uint64_t dBl = dB + (uint64_t)(d.KS * (kTile2 >> 4));
+                    for (int ks = 0; ks < d.KS; ++ks) {
+                        const uint64_t ah = dAh + (uint64_t)(ks * 256), al = dAl + (uint64_t)(ks * 256);
+                        const uint64_t bh = dB + (uint64_t)(ks * (kTile2 >> 4)), bl = dBl + (uint64_t)(ks * (kTile2 >> 4));
+                        tc::mma_bf16(dcol, ah, bh, idesc, ks > 0 ? 1u : 0u);
+                        tc::mma_bf16(dcol, ah, bl, idesc, 1u);
+                        tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                    }
                 }
-                tc::commit(tc::smem_u32(&bars[2 + s]));
+                tc::commit(tc::smem_u32(&bfree[s]));
+                tc::commit(tc::smem_u32(&accf[ab]));
+                last_commit = seq;
+                // prefetch two chunks ahead: the stage of chunk seq - 1, whose MMAs precede these
+                while (copied <= seq + kS2 - 1) {
+                    if (!issue_copy(copied)) break;
+                    ++copied;
+                }
             }
-            // on a timeout, let issued work drain (bounded) before the block frees its TMEM
-            if (!alive && NC > 0) tc::mbar_wait(tc::smem_u32(&bars[2 + ((NC - 1) & 1)]), ((NC - 1) >> 1) & 1, nullptr, 0);
+            if (alive && cur_item >= 0) tc::commit(tc::smem_u32(afree));
+            // on a timeout, let the issued MMAs drain (bounded) before the block frees its TMEM
+            if (!alive && last_commit >= 0)
+                tc::mbar_wait(tc::smem_u32(&bfree[last_commit % kS2]), (int)(last_commit / kS2) & 1, nullptr, 0);
         }
-    } else if (warp < 4) {
-        const int at = atom0 + t;
-        const bool ok = at < v.nmove;
-        uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
-        float fx = 0.f, fy = 0.f, fz = 0.f;
+    } else {
+        // ---------------- epilogue: two threads per atom (row halves of each chunk)
+        const int q4 = warp & 3, mt = (warp >> 2) & 1, rh = warp >> 3;
+        const uint32_t tl_base = tmem + ((uint32_t)(q4 * 32) << 16) + mt * kNC2 + rh * (kNC2 / 2);
+        const float px = d.px, py = d.py, pz = d.pz;
+        const double scale = (double)cmax[0];
+        const int mrow = t & 127;
+        const int ksh = (d.KS + 1) / 2, ks0 = rh ? ksh : 0, ks1 = rh ? d.KS : ksh;
         bool alive = true;
-        for (int c = 0; c < NC && alive; ++c) {
-            const int s = c & 1;
-            alive = tc::mbar_wait(tc::smem_u32(&bars[2 + s]), (c >> 1) & 1, err, 24);
+        long seq = 0;
+        int nitems_done = 0;
+        for (int it = blockIdx.x; it < nitem && alive; it += gridDim.x) {
+            const int tile = it / nparts, part = it % nparts;
+            const int c0 = part * cper, c1 = min(NC, c0 + cper);
+            if (c1 <= c0) continue;
+            const int at = tile * (kMT2 * 128) + mt * 128 + mrow;
+            const bool ok = at < v.nmove;
+            const uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
+            // A for this item (each row half builds half of the K steps), after the previous
+            // item's MMAs finished
+            if (nitems_done > 0) alive = tc::mbar_wait(tc::smem_u32(afree), (nitems_done - 1) & 1, err, 25);
+            alive = __all_sync(0xffffffffu, alive);
             if (!alive) break;
-            tc::fence_after();
-            for (int half = 0; half < 2; ++half) {
-                float val[64];
+            for (int ks = ks0; ks < ks1; ++ks) {
+                uint32_t wh[8], wl[8];
 #pragma unroll
-                for (int cc = 0; cc < 4; ++cc)
-                    tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + s * 128 + half * 64 + cc * 16, val + cc * 16);
+                for (int i = 0; i < 8; ++i) {
+                    const int ni = ks * 8 + i;
+                    float c = 0.f, s = 0.f;
+                    if (ok && ni < d.NN) phase((uint32_t)(ni - d.KN) * rec.z, c, s);
+                    split2(c, s, wh[i], wl[i]);
+                }
+                unsigned char* th = sm + L.off_a + ((mt * 2 + 0) * d.KS + ks) * 4096;
+                unsigned char* tlo = sm + L.off_a + ((mt * 2 + 1) * d.KS + ks) * 4096;
+                *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 0)) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+                *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 8)) = make_uint4(wh[4], wh[5], wh[6], wh[7]);
+                *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 0)) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+                *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 8)) = make_uint4(wl[4], wl[5], wl[6], wl[7]);
+            }
+            tc::fence_async_smem();
+            tc::mbar_arrive(tc::smem_u32(aready));
+            ++nitems_done;
+            // per-atom step of the row phase along m
+            float dyc, dys;
+            phase(rec.y, dyc, dys);
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+            for (int j = 0; j < c1 - c0; ++j, ++seq) {
+                const int c = item_chunk(it, j, c0, c1 - c0);
+                const int ab = (int)(seq % kAB2);
+                alive = tc::mbar_wait(tc::smem_u32(&accf[ab]), (int)(seq / kAB2) & 1, err, 26);
+                alive = __all_sync(0xffffffffu, alive);
+                if (!alive) break;
+                tc::fence_after();
+                uint32_t raw[kNC2 / 2];
+                tc::tmem_ld16_nw(tl_base + ab * (kMT2 * kNC2), raw);
+                tc::tmem_ld16_nw(tl_base + ab * (kMT2 * kNC2) + 16, raw + 16);
+                tc::tmem_wait_ld();
+                tc::fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(tc::smem_u32(&acce[ab]));
+                float ec = 0.f, es = 0.f;
+                int pl = -1 << 30, pm = 0;
 #pragma unroll
-                for (int rr = 0; rr < 16; ++rr) {
-                    const int row = c * 32 + half * 16 + rr;
-                    const int4 rw = row < d.nrow ? rows[row] : make_int4(0, 0, 0, 0);
-                    float ec, es;
-                    phase((uint32_t)rw.x * rec.x + (uint32_t)rw.y * rec.y, ec, es);
-                    const float s0 = ec * val[rr * 4 + 1] + es * val[rr * 4 + 0];
-                    const float s1 = ec * val[rr * 4 + 3] + es * val[rr * 4 + 2];
-                    fx += (d.px * (float)rw.x) * s0;
-                    fy += (d.py * (float)rw.y) * s0;
+                for (int rr = 0; rr < kRC / 2; ++rr) {
+                    const int2 lm = rlm[c * kRC + rh * (kRC / 2) + rr];
+                    if (rr == 0 || lm.x != pl || lm.y != pm + 1) {
+                        phase((uint32_t)lm.x * rec.x + (uint32_t)lm.y * rec.y, ec, es);
+                    } else {
+                        const float nc = ec * dyc - es * dys;
+                        es = ec * dys + es * dyc;
+                        ec = nc;
+                    }
+                    pl = lm.x;
+                    pm = lm.y;
+                    const float v0 = __uint_as_float(raw[rr * 4 + 0]), v1 = __uint_as_float(raw[rr * 4 + 1]);
+                    const float v2 = __uint_as_float(raw[rr * 4 + 2]), v3 = __uint_as_float(raw[rr * 4 + 3]);
+                    const float s0 = ec * v1 + es * v0;
+                    const float s1 = ec * v3 + es * v2;
+                    fx += (px * (float)lm.x) * s0;
+                    fy += (py * (float)lm.y) * s0;
                     fz += s1;
                 }
             }
-            tc::fence_before();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(tc::smem_u32(&bars[4 + s]));
-        }
-        if (ok && alive) {
-            const double q = (double)__uint_as_float(rec.w) * (double)cmax[0];
-            v.fx[at] += q * (double)fx;
-            v.fy[at] += q * (double)fy;
-            v.fz[at] += q * (double)d.pz * (double)fz;
+            if (ok && alive) {
+                const double q = (double)__uint_as_float(rec.w) * scale;
+                atomicAdd(&v.fx[at], q * (double)fx);
+                atomicAdd(&v.fy[at], q * (double)fy);
+                atomicAdd(&v.fz[at], q * (double)pz * (double)fz);
+            }
         }
     }
     __syncthreads();
     if (warp == 0) {
         tc::fence_after();
-        tc::tmem_dealloc(tmem, 256);
+        tc::tmem_dealloc(tmem, 512);
     }
 }
 
@@ -621,15 +760,35 @@ int recip_tc_setup(Ctx& c) {
         p.NN * (kGA / 2) > kMaxItems * 128 * p.tpc1)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core table fill");
     p.mtiles = (ks.nrow + 127) / 128;
-    p.nchunk2 = (ks.nrow + 31) / 32;
+    p.nchunk2 = (ks.nrow + kRC - 1) / kRC;
     p.smem1 = (int)(p.tpc1 == 4 ? p1_layout(4, P1<4>::kS, p.NP, p.NM).total : p1_layout(2, P1<2>::kS, p.NP, p.NM).total);
-    p.smem2 = 1024 + 3 * 2 * p.KS * 4096;
+    p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC).total;
     if (p.smem1 > 227 * 1024 || p.smem2 > 227 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
+    // pass-2 work items: atom tiles x chunk ranges, spread so the last wave of 152 SMs is full
+    p.ntile2 = (v.nmove + kMT2 * 128 - 1) / (kMT2 * 128);
+    {
+        int best = 1;
+        double beff = -1.0;
+        for (int np = 1; np <= 8 && np <= p.nchunk2; ++np) {
+            const long items = (long)p.ntile2 * np;
+            const long waves = (items + 151) / 152;
+            const double eff = (double)items / (double)(waves * 152) - 0.01 * np;  // A rebuild per item
+            if (eff > beff + 1e-9) {
+                beff = eff;
+                best = np;
+            }
+        }
+        p.nparts2 = best;
+    }
+    p.cper2 = (p.nchunk2 + p.nparts2 - 1) / p.nparts2;
+    p.nparts2 = (p.nchunk2 + p.cper2 - 1) / p.cper2;
+    p.grid2 = std::min(152, p.ntile2 * p.nparts2);
     c.d_tc_atoms = (uint4*)dalloc(c, sizeof(uint4) * std::max(v.nmove, 1));
-    c.d_tc_img = (unsigned char*)dalloc(c, (size_t)std::max(p.nchunk2, 1) * 2 * p.KS * 4096);
+    c.d_tc_img = (unsigned char*)dalloc(c, (size_t)std::max(p.nchunk2, 1) * 2 * p.KS * kTile2);
     c.d_tc_cmax = (float*)dalloc(c, sizeof(float) * 4);
     c.d_tc_part = (float*)dalloc(c, sizeof(float) * (size_t)p.nsplit1 * p.NP * p.rtot);
+    c.d_tc_cf = (float2*)dalloc(c, sizeof(float2) * std::max(ks.nk, 1));
     if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
     MDG_CUDA(cudaFuncSetAttribute(k_tc_sfac<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem1));
     MDG_CUDA(cudaFuncSetAttribute(k_tc_sfac<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem1));
@@ -654,11 +813,12 @@ void recip_tc(Ctx& c) {
             v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1);
     const long nred = (long)ks.nrow * p.NN;
     k_tc_sreduce<<<(int)std::min<long>((nred + 255) / 256, 152 * 4), 256, 0, c.stream>>>(
-        v, c.d_tc_part, p.nsplit1, p.rtot, d, ks.row, ks.row_nlen, ks.ak, ks.qw, ks.s, ks.c, c.d_tc_cmax);
-    const long total = (long)p.nchunk2 * p.KS * 128 * 16;
-    k_tc_prep_c<<<(int)std::min<long>((total + 255) / 256, 152 * 8), 256, 0, c.stream>>>(ks.c, ks.row, ks.row_nlen, d,
-                                                                                         c.d_tc_img, c.d_tc_cmax);
-    k_tc_force<<<(v.nmove + 127) / 128, kT, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, ks.row, d, c.d_tc_cmax);
+        v, c.d_tc_part, p.nsplit1, p.rtot, d, ks.row, ks.row_nlen, ks.ak, ks.qw, ks.s, ks.c, c.d_tc_cf, c.d_tc_cmax);
+    const long total = (long)p.nchunk2 * p.KS * kNC2 * 8;
+    k_tc_prep_c<<<(int)std::min<long>((total + 255) / 256, 152 * 8), 256, 0, c.stream>>>(c.d_tc_cf, ks.row, ks.row_nlen,
+                                                                                         d, c.d_tc_img, c.d_tc_cmax);
+    k_tc_force<<<p.grid2, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, ks.row, d, c.d_tc_cmax, p.ntile2,
+                                                    p.nparts2, p.cper2);
 }
 
 int umma_selftest(int n, int k, const float* a, const float* b, float* dout, std::string& err) {
