@@ -281,6 +281,41 @@ def gpu_arm(args):
     ctx.get_state(s)
     pk = peaks()
     roof, roof_recip = roofline(ctx, s, prm, precision, pk)
+
+    # ---------------- learned SHAKE seed (workloads with SHAKE-constrained molecules): the same
+    # start and step count with the seed network active; the headline value is then this run
+    learned_rep = None
+    if s.ncons > 0 and args.learned and precision == MDG_MIXED:
+        from md_sim_gb300 import learned
+
+        t0 = time.perf_counter()
+        w, how = learned.load_or_train(lib, ctx, s_start)
+        t_model = time.perf_counter() - t0
+        ctx.set_state(s_start.copy())
+        sw_plain = learned.sweep_stats(ctx, 20)
+        ctx.set_state(s_start.copy())
+        ctx.set_shake_model(w)
+        sw_seed = learned.sweep_stats(ctx, 20)
+        ctx.set_state(s_start.copy())
+        ctx.run(args.warmup)
+        per_seed = time_resident(ctx, K, stream, flush, torch)
+        ph_seed = ctx.phase_times(reps=5)
+        ctx.set_shake_model(None)
+        ph_plain = ctx.phase_times(reps=5)
+        t_seed = float(np.sum(per_seed)) / K * 1e-3
+        learned_rep = {
+            "model": how, "model_s": t_model,
+            "value_plain_shake": value, "ms_per_step_plain_shake": t_step * 1e3,
+            "value_seeded": ns_per_day(t_seed, s.dt), "ms_per_step_seeded": t_seed * 1e3,
+            "sweeps_per_molecule_plain": sw_plain.mean_sweeps, "sweeps_per_molecule_seeded": sw_seed.mean_sweeps,
+            "max_sweeps_plain": sw_plain.max_sweeps, "max_sweeps_seeded": sw_seed.max_sweeps,
+            "shake_ms_plain": ph_plain["shake"], "shake_ms_seeded": ph_seed["shake"],
+            "tolerance": prm.shake_tol2,
+        }
+        value, t_step, per_step = learned_rep["value_seeded"], t_seed, per_seed
+    drift = None
+    if args.drift > 0:
+        drift = nve_drift(ctx, s, args.drift)
     ctx.close()
 
     # ---------------- the plain FP64 GPU form on the same start, and the force error against it
@@ -295,7 +330,8 @@ def gpu_arm(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup,
         "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if precision == MDG_FP64 else "f32+bf16x3 (f64 state)", "data": "synthetic (seeded)",
+        "dtype": "f64" if precision == MDG_FP64 else "f32 pairs + f16x3 tensor reciprocal (f64 state)",
+        "data": "synthetic (seeded)",
         "config": {"workload": desc, "precision": args.precision, "config": args.config,
                    "l2": "flushed (256 MB write) between timed steps", "equilibration_steps": args.equil,
                    "ensemble": "NVE" if s.temper == -1.0 else f"NVT {s.temper} K"},
@@ -310,12 +346,36 @@ def gpu_arm(args):
     }
     if cmp64 is not None:
         out["fp64_gpu"] = cmp64
+        out["fp64_gpu"]["speedup"] = value / cmp64["value"]
+    if learned_rep is not None:
+        out["learned_shake"] = learned_rep
+    if drift is not None:
+        out["nve_drift"] = drift
     if args.cpu_baseline:
         v, dt, n = cpu_reference(s, prm, args.cpu_steps)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                "sample": f"{n} MD steps of the same workload after one untimed step "
                                          f"({dt * 1e3:.2f} ms/step), OpenMP over all host cores"}
     return out
+
+
+def nve_drift(ctx, s, nsteps, every=100):
+    """Total energy htot (src/move.f90 bookkeeping) sampled every `every` resident steps over
+    nsteps: relative change and least-squares slope per ns."""
+    h = []
+    done = 0
+    while done < nsteps:
+        rep = ctx.run(min(every, nsteps - done))
+        done += min(every, nsteps - done)
+        h.append((done, rep["htot"], rep["tempnow"]))
+    t = np.array([x[0] for x in h], float) * s.dt * 1e-6  # ns
+    e = np.array([x[1] for x in h], float)
+    slope = float(np.polyfit(t, e, 1)[0]) if len(t) > 1 else 0.0
+    return {"steps": int(nsteps), "dt_fs": s.dt, "htot_first": float(e[0]), "htot_last": float(e[-1]),
+            "rel_change": float((e[-1] - e[0]) / abs(e[0])), "slope_per_ns": slope,
+            "slope_per_ns_per_molecule": slope / max(s.nrig + s.ncons, 1),
+            "temp_first": float(h[0][2]), "temp_last": float(h[-1][2]),
+            "unit": "htot in the reference's energy unit (kJ/mol)"}
 
 
 def time_resident(ctx, K, stream, flush, torch):
@@ -488,6 +548,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=200,
                     help="steps of the plain FP64 GPU comparison arm (0 = skip)")
     ap.add_argument("--equil", type=int, default=200)
+    ap.add_argument("--drift", type=int, default=0, help="NVE energy drift over this many extra resident steps")
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="skip the learned SHAKE seed arm (workloads with SHAKE only)")
     ap.add_argument("--e2e-steps", type=int, default=60)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")

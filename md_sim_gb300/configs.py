@@ -251,7 +251,12 @@ def shake_water(nwat: int = 8192, cells: int = 19, a: float = 4.21, seed: int = 
     crys = _crystal(len(wpos), a, lw)
     names = ["O", "H", "Mg", "Ox"]
     buck = ("Buck", 1000.0 * EV, 0.30, 10.0 * EV)
-    vdw = _vdw_table(names, {(1, 1): ("LeJo", SIG_OO, EPS_OO), (1, 3): buck, (1, 4): buck})
+    # H carries a bare charge; against the wall anions (-1.2 e) that is an unbounded attraction
+    # which pulls the SHAKE-constrained molecule into the O-wall Buckingham collapse region within
+    # a few hundred steps.  A short-range H-wall repulsion (A e^{-r/rho}, no dispersion) bounds it.
+    hwall = ("Buck", 100.0 * EV, 0.25, 0.0)
+    vdw = _vdw_table(names, {(1, 1): ("LeJo", SIG_OO, EPS_OO), (1, 3): buck, (1, 4): buck,
+                             (2, 3): hwall, (2, 4): hwall})
     fld = S.FieldFile([wat, crys], vdw)
     constr = [[(3 * i + 1, 3 * i + 2), (3 * i + 1, 3 * i + 3), (3 * i + 2, 3 * i + 3)] for i in range(nwat)]
     top = S.TopFile(constr, [1] * nwat, [], [])
@@ -263,6 +268,7 @@ def shake_water(nwat: int = 8192, cells: int = 19, a: float = 4.21, seed: int = 
     body[2, 0] = -hh / 2.0
     body[1, 1] = body[2, 1] = math.sqrt(R_OH ** 2 - (hh / 2.0) ** 2)
     qrot = _random_quaternions(np.random.default_rng(seed + 1), nwat)
+    qrot = _relax_orientations(np.random.default_rng(seed + 3), opos, qrot, body, L, lz, wpos)
     q1, q2, q3, q4 = qrot
     amat = np.empty((3, 3, nwat))
     amat[0, 0] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4
@@ -286,7 +292,7 @@ def shake_water(nwat: int = 8192, cells: int = 19, a: float = 4.21, seed: int = 
     kT = KB * T
     mtot = (M_O + 2 * M_H) * v_unit ** 2 / 1000.0
     vcom = rngv.normal(0.0, math.sqrt(kT / mtot), size=(nwat, 3))
-    omega = rngv.normal(0.0, 0.02, size=(nwat, 3))
+    omega = rngv.normal(0.0, 0.012, size=(nwat, 3))  # ~ sqrt(kT / I) of water at 300 K, rad/fs
     nm = s.nmove
     xyz = np.stack([s.x0[:nm], s.y0[:nm], s.z0[:nm]], 1).reshape(nwat, 3, 3)
     ctr = xyz.mean(axis=1, keepdims=True)
@@ -307,6 +313,60 @@ def shake_water(nwat: int = 8192, cells: int = 19, a: float = 4.21, seed: int = 
     return s, prm
 
 
+def _water_sites(opos, q, body):
+    """(n, 3, 3) site positions of waters with head positions opos and quaternions q (the
+    rotation of config_quatsite, src/config.f90:303-329)."""
+    q1, q2, q3, q4 = q
+    a = np.empty((3, 3, len(opos)))
+    a[0, 0] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4
+    a[0, 1] = 2.0 * (q3 * q4 - q1 * q2)
+    a[0, 2] = 2.0 * (q2 * q3 + q1 * q4)
+    a[1, 0] = -2.0 * (q1 * q2 + q3 * q4)
+    a[1, 1] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4
+    a[1, 2] = 2.0 * (q2 * q4 - q1 * q3)
+    a[2, 0] = 2.0 * (q2 * q3 - q1 * q4)
+    a[2, 1] = -2.0 * (q1 * q3 + q4 * q2)
+    a[2, 2] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4
+    out = np.empty((len(opos), 3, 3))
+    for j in range(3):
+        for d in range(3):
+            out[:, j, d] = opos[:, d] + a[0, d] * body[j, 0] + a[1, d] * body[j, 1] + a[2, d] * body[j, 2]
+    return out
+
+
+def _relax_orientations(rng, opos, q, body, L, lz, walls, dmin=1.7, iters=200):
+    """Re-draws the orientation of every water with a site closer than dmin to a site of another
+    molecule or to a wall atom (x, y periodic), until none is left: a random-orientation start
+    with only O-O spacing enforced puts H atoms on top of neighbours, and the resulting forces
+    break SHAKE in the first steps."""
+    from scipy.spatial import cKDTree
+
+    q = q.copy()
+    n = len(opos)
+    shift = np.array([0.0, 0.0, 4.0 * lz])
+    box = np.array([L, L, 16.0 * lz])
+    wtree = cKDTree(np.mod(np.asarray(walls) + shift, box), boxsize=box) if len(walls) else None
+    for _ in range(iters):
+        sites = np.mod(_water_sites(opos, q, body).reshape(-1, 3) + shift, box)
+        tree = cKDTree(sites, boxsize=box)
+        pairs = tree.query_pairs(dmin, output_type="ndarray")
+        bad = set()
+        if len(pairs):
+            mi, mj = pairs[:, 0] // 3, pairs[:, 1] // 3
+            sel = mi != mj
+            bad.update(mi[sel].tolist())
+            bad.update(mj[sel].tolist())
+        if wtree is not None:
+            for i, lst in enumerate(tree.query_ball_tree(wtree, dmin)):
+                if lst:
+                    bad.add(i // 3)
+        if not bad:
+            return q
+        idx = np.array(sorted(bad))
+        q[:, idx] = _random_quaternions(rng, len(idx))
+    return q
+
+
 def rescale_velocities(s: S.System, T: float) -> float:
     """Scales the velocity-like Gear derivatives of the rigid molecules and ions to temperature T
     (kinetic energy as in move_predict: ke = kp + kw, tempnow = ke*1000/(3 R (nfree + 2 nrig)),
@@ -318,6 +378,7 @@ def rescale_velocities(s: S.System, T: float) -> float:
             s.inzz * float((s.w[0, 2] ** 2).sum())
     else:
         kw = 0.0
+    _rescale_shake_atoms(s, T)
     ndf = (s.nliqa - s.nriga) + 2 * s.nrig
     if ndf == 0 or kp + kw <= 0:
         return 1.0
@@ -328,6 +389,26 @@ def rescale_velocities(s: S.System, T: float) -> float:
         s.c[1:] *= lam
         s.w *= lam
         s.q[1:] *= lam
+    return lam
+
+
+def _rescale_shake_atoms(s: S.System, T: float) -> float:
+    """Verlet (SHAKE) atoms carry their velocity as the displacement x - xold: scale it to the
+    temperature tkps = sum m d^2 1000 / (R nfreed) of move_shake (src/move.f90:416-439)."""
+    lo, hi = s.nliqa, s.nmove
+    if hi <= lo:
+        return 1.0
+    d = [s.x0[lo:hi] - s.xold[lo:hi], s.y0[lo:hi] - s.yold[lo:hi], s.z0[lo:hi] - s.zold[lo:hi]]
+    d[0] -= s.lx * np.rint(d[0] / s.lx)
+    d[1] -= s.ly * np.rint(d[1] / s.ly)
+    k = float((s.mi[lo:hi] * (d[0] ** 2 + d[1] ** 2 + d[2] ** 2)).sum())
+    nfreed = 3 * (hi - lo) - sum(int(s.nt[it]) * int(s.nconst[it]) for it in range(s.ntype) if s.moltypen[it] == 2)
+    if nfreed <= 0 or k <= 0:
+        return 1.0
+    lam = math.sqrt(T / (k * 1000.0 / (S.PH_R * nfreed)))
+    s.xold[lo:hi] = s.x0[lo:hi] - lam * d[0]
+    s.yold[lo:hi] = s.y0[lo:hi] - lam * d[1]
+    s.zold[lo:hi] = s.z0[lo:hi] - lam * d[2]
     return lam
 
 

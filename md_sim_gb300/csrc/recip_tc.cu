@@ -167,15 +167,17 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
                 tc::fence_after();
                 const uint64_t ds = dS0 + (uint64_t)((s * L.stage) >> 4);
                 const uint64_t db = ds + (uint64_t)(L.a_bytes >> 4);
+                // all products of one accumulator back to back: switching the accumulator between
+                // consecutive MMAs roughly halves the issue rate
 #pragma unroll
-                for (int p = 0; p < 2; ++p) {
-                    const uint64_t bh = db + (uint64_t)(((p * 2 + 0) * L.b_tile) >> 4);
-                    const uint64_t bl = db + (uint64_t)(((p * 2 + 1) * L.b_tile) >> 4);
+                for (int tile = 0; tile < TPC; ++tile) {
+                    const uint32_t dcol = tmem + tile * tcols;
 #pragma unroll
-                    for (int tile = 0; tile < TPC; ++tile) {
+                    for (int p = 0; p < 2; ++p) {
+                        const uint64_t bh = db + (uint64_t)(((p * 2 + 0) * L.b_tile) >> 4);
+                        const uint64_t bl = db + (uint64_t)(((p * 2 + 1) * L.b_tile) >> 4);
                         const uint64_t ah = ds + (uint64_t)(((tile * 2 + p) * 2 + 0) * 256);
                         const uint64_t al = ds + (uint64_t)(((tile * 2 + p) * 2 + 1) * 256);
-                        const uint32_t dcol = tmem + tile * tcols;
                         tc::mma_bf16(dcol, ah, bh, idesc, (g > 0 || p > 0) ? 1u : 0u);
                         tc::mma_bf16(dcol, ah, bl, idesc, 1u);
                         tc::mma_bf16(dcol, al, bh, idesc, 1u);
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
             float2* tm = reinterpret_cast<float2*>(sm + L.off_tab + (g & 1) * (L.tab_m + L.tab_l));
             float2* tl = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(tm) + L.tab_m);
             bool ok = true;
-            if (g >= kS) ok = tc::mbar_wait(tc::smem_u32(&empty[s]), ((g / kS) - 1) & 1, err, 12);
+            if (g >= kS) ok = tc::mbar_wait_warp(tc::smem_u32(&empty[s]), ((g / kS) - 1) & 1, err, 12);
             unsigned char* st = sm + L.off_stage + s * L.stage;
             unsigned char* bb = st + L.a_bytes;
             if (ok) {
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
         }
         // all MMAs done -> accumulators to the partial-sum buffer
         if (ngroup > 0 && alive)
-            alive = tc::mbar_wait(tc::smem_u32(&empty[(ngroup - 1) % kS]), ((ngroup - 1) / kS) & 1, err, 13);
+            alive = tc::mbar_wait_warp(tc::smem_u32(&empty[(ngroup - 1) % kS]), ((ngroup - 1) / kS) & 1, err, 13);
         tc::fence_after();
         const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + tile * tcols;
         float* dst = part + (size_t)blockIdx.y * d.NP * rtot;
@@ -365,7 +367,7 @@ __global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit,
 // col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part; one thread
 // per (chunk, K step, column, n) writes the (part 0, part 1) half pairs of hi and lo.
 // ---------------------------------------------------------------------------------------------
-constexpr int kRC = 16;                 // rows per pass-2 chunk
+constexpr int kRC = 64;                 // rows per pass-2 chunk
 constexpr int kNC2 = 4 * kRC;           // pass-2 MMA N
 constexpr uint32_t kTile2 = kNC2 * 32;  // one N x 16 B tile (bytes)
 
@@ -406,41 +408,57 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
 // ---------------------------------------------------------------------------------------------
 // pass 2: forces
 //
-// Work items (a tile of 256 atoms, a range of row chunks) are spread over a persistent grid.
-// Per item the epilogue warps build A = e^{i n tz} of the tile's atoms (two M = 128 operands,
-// K = 2 (n + KN) + part); the issuer thread streams the chunk images of C through a 3-deep ring
-// with cp.async.bulk and, per chunk, issues 3 (hi/lo) products per K step for both operands into
-// a 4-deep ring of TMEM accumulator pairs (N = 64: T and T' of 16 rows).  Two epilogue threads
-// own each atom, one per half of a chunk's rows: per row a thread forms Im(e^{i(l tx + m ty)} T)
-// with the row phase advanced along m by a complex multiply (recomputed by __sincosf at the first
-// of its 8 rows and at each change of l), and sums the force components; forces are added once
-// per item.
+// Work items (a tile of 128 atoms, a range of row chunks) are spread over a persistent grid.
+// Per item the epilogue warps build A = e^{i n tz} of the tile's atoms (K = 2 (n + KN) + part).
+// One MMA is M = 128 atoms x N = 256 (T and T' x re/im of 64 rows) x K = 16: the largest N of a
+// single-CTA MMA, since an MMA costs about the same issue time for any N up to 128.  The issuer
+// streams the chunk images as K-step tiles (hi part of C, then lo part; 4 tiles per ring stage,
+// 4 stages) with cp.async.bulk: per hi tile ah*bh and al*bh, per lo tile ah*bl, all into one
+// accumulator (consecutive MMAs on one accumulator issue fastest).  Accumulators are
+// double-buffered in TMEM against the epilogue, where four threads own each atom (16 rows each):
+// per row they form Im(e^{i(l tx + m ty)} T) with the row phase advanced along m by a complex
+// multiply (recomputed by __sincosf at the first of the 16 rows and at each change of l).
 // ---------------------------------------------------------------------------------------------
-constexpr int kMT2 = 2;                 // M tiles per item (256 atoms)
-constexpr int kS2 = 3;                  // B ring depth
-constexpr int kAB2 = 4;                 // TMEM accumulator ring depth (kAB2 x kMT2 x 64 columns)
-constexpr int kEW2 = kMT2 * 4 * 2;      // epilogue warps: (M tile, lane quadrant, row half)
-constexpr int kT2 = kEW2 * 32 + 32;     // + issuer warp
-
 // j-th chunk of an item: every item walks its chunk range from a different starting point, so
 // that the CTAs do not all read the same chunk image (the same L2 lines) at the same time
 __device__ __forceinline__ int item_chunk(int it, int j, int c0, int cnt) {
     return c0 + (int)((j + (unsigned)it * 7919u % (unsigned)cnt) % (unsigned)cnt);
 }
 
+constexpr int kRQ = 4;                  // row quarters of a chunk (threads per atom)
+constexpr int kEW2 = 4 * kRQ;           // epilogue warps: (lane quadrant, row quarter)
+constexpr int kT2 = kEW2 * 32 + 32;     // + issuer warp
+
+constexpr int kTPS2 = 4;                // K-step tiles (256 x 16 halves, 8 KB) per ring stage
+constexpr int kNS2 = 4;                 // ring stages
+
 struct P2Layout {
-    uint32_t a_bytes, img, off_a, off_b, off_rows, total;
+    uint32_t a_bytes, off_a, off_b, off_rows, off_red, total;
 };
 
 __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad) {
     P2Layout L;
-    L.a_bytes = kMT2 * 2 * KS * 4096;        // [mt][h][ks] 128 x 16
-    L.img = 2 * KS * kTile2;                 // [h][ks] 64 x 16
+    L.a_bytes = 2 * KS * 4096;               // [h][ks] 128 x 16
     L.off_a = 1024;
     L.off_b = L.off_a + L.a_bytes;
-    L.off_rows = L.off_b + kS2 * L.img;
-    L.total = L.off_rows + nrow_pad * 8;     // (l, m) per row
+    L.off_rows = L.off_b + kNS2 * kTPS2 * kTile2;  // ring of stages of K-step tiles
+    L.off_red = L.off_rows + nrow_pad * 8;   // (l, m) per row
+    L.total = L.off_red + kRQ * 128 * 3 * 4; // per-item force partials
     return L;
+}
+
+// Named barrier 2 over the epilogue warps; the _all form returns the AND of the threads' flags, so
+// that a timeout seen by one warp stops every epilogue warp at the same point.
+__device__ __forceinline__ void epilogue_sync() { asm volatile("bar.sync 2, %0;" ::"n"(kEW2 * 32) : "memory"); }
+__device__ __forceinline__ bool epilogue_all(bool ok) {
+    uint32_t res;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, 2, %2, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(res)
+        : "r"((uint32_t)ok), "n"(kEW2 * 32)
+        : "memory");
+    return res != 0;
 }
 
 __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
@@ -450,23 +468,24 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     extern __shared__ __align__(1024) unsigned char sm[];
     const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm);      // [kS2] chunk image landed
-    uint64_t* bfree = full + kS2;                           // [kS2] MMAs of the stage done
-    uint64_t* accf = bfree + kS2;                           // [kAB2] accumulator ready
-    uint64_t* acce = accf + kAB2;                           // [kAB2] accumulator drained (epilogue warps)
-    uint64_t* afree = acce + kAB2;                          // MMAs of the item done
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm);      // [kNS2] stage landed
+    uint64_t* bfree = full + kNS2;                          // [kNS2] MMAs reading the stage done
+    uint64_t* accf = bfree + kNS2;                          // [2] accumulator ready
+    uint64_t* acce = accf + 2;                              // [2] accumulator drained (epilogue warps)
+    uint64_t* afree = acce + 2;                             // MMAs of the item done
     uint64_t* aready = afree + 1;                           // A built (epilogue threads)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     int2* rlm = reinterpret_cast<int2*>(sm + L.off_rows);
+    float* red = reinterpret_cast<float*>(sm + L.off_red);
     int* err = &v.status[ST_TC_TIMEOUT];
     const int NC = d.nchunk2;
     const int nitem = ntile * nparts;
     if (t == 0) {
-        for (int i = 0; i < kS2; ++i) {
+        for (int i = 0; i < kNS2; ++i) {
             tc::mbar_init(tc::smem_u32(&full[i]), 1);
             tc::mbar_init(tc::smem_u32(&bfree[i]), 1);
         }
-        for (int i = 0; i < kAB2; ++i) {
+        for (int i = 0; i < 2; ++i) {
             tc::mbar_init(tc::smem_u32(&accf[i]), 1);
             tc::mbar_init(tc::smem_u32(&acce[i]), kEW2);
         }
@@ -483,127 +502,143 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t imgBytes = L.img, halfBytes = L.img / 2;
     if (warp == kEW2) {
-        // ---------------- issuer: copies and MMAs over the flat (item, chunk) sequence
+        // ---------------- issuer: K-step tile copies and MMAs over the CTA's (item, chunk) sequence
         if (lane == 0) {
             const uint32_t idesc = idesc_e(128, kNC2);
             const uint32_t abase = tc::smem_u32(sm + L.off_a), bbase = tc::smem_u32(sm + L.off_b);
             const uint64_t dA0 = tc::desc(abase), dB0 = tc::desc(bbase);
+            const int TPCH = 2 * d.KS;  // tiles per chunk: hi K steps, then lo K steps
             bool alive = true;
-            long seq = 0, copied = 0, last_commit = -1;
-            int nitems_done = 0;
-            // the flat list of chunks this CTA processes
-            auto chunk_of = [&](long q, int& item_out) -> int {
-                // q-th chunk of this CTA: items blockIdx.x, blockIdx.x + gridDim.x, ...
-                int it = blockIdx.x;
-                long left = q;
+            // chunk sequence of this CTA: items blockIdx.x, blockIdx.x + gridDim.x, ... (empty
+            // items skipped); (cit, cj, ck) walks it tile by tile for the copies
+            auto range = [&](int it, int& c0, int& cnt) {
+                const int part = it % nparts;
+                c0 = part * cper;
+                cnt = max(0, min(NC, c0 + cper) - c0);
+            };
+            auto skip_empty = [&](int& it, int& j) {
+                int c0, cnt;
                 while (it < nitem) {
-                    const int part = it % nparts;
-                    const int c0 = part * cper, c1 = min(NC, c0 + cper);
-                    const int cnt = max(0, c1 - c0);
-                    if (left < cnt) {
-                        item_out = it;
-                        return item_chunk(it, (int)left, c0, cnt);
-                    }
-                    left -= cnt;
+                    range(it, c0, cnt);
+                    if (j < cnt) return;
                     it += gridDim.x;
+                    j = 0;
                 }
-                item_out = -1;
-                return -1;
             };
-            auto issue_copy = [&](long q) {
-                int it;
-                const int c = chunk_of(q, it);
-                if (c < 0) return false;
-                const int s = (int)(q % kS2);
-                if (q >= kS2) {
-                    if (!tc::mbar_wait(tc::smem_u32(&bfree[s]), (int)((q / kS2) - 1) & 1, err, 21)) return false;
+            int cit = blockIdx.x, cj = 0, ck = 0;
+            skip_empty(cit, cj);
+            long w_copy = 0;  // stages copied
+            auto issue_stage = [&]() {
+                // the next kTPS2 tiles of the copy sequence (fewer at its end) into slot w_copy % kNS2
+                if (cit >= nitem) return;
+                const int slot = (int)(w_copy % kNS2);
+                const uint32_t fb = tc::smem_u32(&full[slot]);
+                const uint32_t dst0 = bbase + slot * (kTPS2 * kTile2);
+                int n = 0;
+                const unsigned char* src[kTPS2];
+                while (n < kTPS2 && cit < nitem) {
+                    int c0, cnt;
+                    range(cit, c0, cnt);
+                    const int c = item_chunk(cit, cj, c0, cnt);
+                    src[n++] = img + ((size_t)c * TPCH + ck) * kTile2;
+                    if (++ck == TPCH) {
+                        ck = 0;
+                        ++cj;
+                        skip_empty(cit, cj);
+                    }
                 }
-                const uint32_t fb = tc::smem_u32(&full[s]);
-                tc::mbar_expect_tx(fb, imgBytes);
-                tc::bulk_g2s(bbase + s * imgBytes, img + (size_t)c * imgBytes, halfBytes, fb);
-                tc::bulk_g2s(bbase + s * imgBytes + halfBytes, img + (size_t)c * imgBytes + halfBytes, halfBytes, fb);
-                return true;
+                tc::mbar_expect_tx(fb, (uint32_t)n * kTile2);
+                for (int i = 0; i < n; ++i) tc::bulk_g2s(dst0 + i * kTile2, src[i], kTile2, fb);
+                ++w_copy;
             };
-            for (; copied < kS2; ++copied)
-                if (!issue_copy(copied)) break;
-            int cur_item = -1;
-            for (;; ++seq) {
-                int it;
-                const int c = chunk_of(seq, it);
-                if (c < 0) break;
-                if (it != cur_item) {
-                    // a new item: its A operand must be built (after the previous item's MMAs)
+            for (int i = 0; i < kNS2 - 1; ++i) issue_stage();
+            int mit = blockIdx.x, mj = 0;
+            skip_empty(mit, mj);
+            long u = 0, seq = 0;
+            int cur_item = -1, nitems_done = 0;
+            long last_commit = -1;  // last committed stage
+            while (alive && mit < nitem) {
+                const int ab = (int)(seq & 1);
+                if (mit != cur_item) {
                     if (cur_item >= 0) {
                         tc::commit(tc::smem_u32(afree));
                         ++nitems_done;
                     }
-                    cur_item = it;
-                    alive = tc::mbar_wait(tc::smem_u32(aready), (nitems_done & 1), err, 22);
+                    cur_item = mit;
+                    alive = tc::mbar_wait(tc::smem_u32(aready), nitems_done & 1, err, 22);
                     if (!alive) break;
                 }
-                const int s = (int)(seq % kS2);
-                alive = tc::mbar_wait(tc::smem_u32(&full[s]), (int)(seq / kS2) & 1, err, 23);
+                if (seq >= 2) alive = tc::mbar_wait(tc::smem_u32(&acce[ab]), (int)((seq >> 1) - 1) & 1, err, 24);
                 if (!alive) break;
-                const int ab = (int)(seq % kAB2);
-                if (seq >= kAB2) alive = tc::mbar_wait(tc::smem_u32(&acce[ab]), (int)((seq / kAB2) - 1) & 1, err, 24);
-                if (!alive) break;
-                tc::fence_after();
-                // descriptors advance linearly with the shared address (16-byte units)
-                const uint64_t dB = dB0 + (uint64_t)((s * imgBytes) >> 4);
-#pragma unroll
-                for (int mt = 0; mt < kMT2; ++mt) {
-                    const uint32_t dcol = tmem + ab * (kMT2 * kNC2) + mt * kNC2;
-                    const uint64_t dAh = dA0 + (uint64_t)((mt * 2 + 0) * d.KS * 256);
-                    const uint64_t dAl = dA0 + (uint64_t)((mt * 2 + 1) * d.KS * 256);
-                    const uint64_t dBl = dB + (uint64_t)(d.KS * (kTile2 >> 4));
-                    for (int ks = 0; ks < d.KS; ++ks) {
-                        const uint64_t ah = dAh + (uint64_t)(ks * 256), al = dAl + (uint64_t)(ks * 256);
-                        const uint64_t bh = dB + (uint64_t)(ks * (kTile2 >> 4)), bl = dBl + (uint64_t)(ks * (kTile2 >> 4));
-                        tc::mma_bf16(dcol, ah, bh, idesc, ks > 0 ? 1u : 0u);
-                        tc::mma_bf16(dcol, ah, bl, idesc, 1u);
-                        tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                const uint32_t dcol = tmem + ab * kNC2;
+                // is this the CTA's last chunk? (then its last tile closes a partial stage)
+                int nit2 = mit, nj2 = mj + 1;
+                skip_empty(nit2, nj2);
+                const bool last_chunk = nit2 >= nitem;
+                for (int k = 0; k < TPCH && alive; ++k, ++u) {
+                    const long w = u / kTPS2;
+                    const int slot = (int)(w % kNS2), pos = (int)(u % kTPS2);
+                    if (pos == 0) {
+                        alive = tc::mbar_wait(tc::smem_u32(&full[slot]), (int)(w / kNS2) & 1, err, 23);
+                        if (!alive) break;
+                        tc::fence_after();
+                    }
+                    const uint64_t b = dB0 + (uint64_t)((slot * kTPS2 + pos) * (kTile2 >> 4));
+                    const int ks = k < d.KS ? k : k - d.KS;
+                    const uint64_t ah = dA0 + (uint64_t)((0 * d.KS + ks) * 256);
+                    if (k < d.KS) {
+                        const uint64_t al = dA0 + (uint64_t)((1 * d.KS + ks) * 256);
+                        tc::mma_bf16(dcol, ah, b, idesc, k > 0 ? 1u : 0u);
+                        tc::mma_bf16(dcol, al, b, idesc, 1u);
+                    } else {
+                        tc::mma_bf16(dcol, ah, b, idesc, 1u);
+                    }
+                    if (pos == kTPS2 - 1 || (last_chunk && k == TPCH - 1)) {
+                        tc::commit(tc::smem_u32(&bfree[slot]));
+                        last_commit = w;
+                        // refill the slot of stage w - 1 (its MMAs precede the ones just issued)
+                        if (w >= 1) {
+                            alive = tc::mbar_wait(tc::smem_u32(&bfree[(w - 1) % kNS2]), (int)((w - 1) / kNS2) & 1, err, 21);
+                            if (!alive) break;
+                        }
+                        issue_stage();
                     }
                 }
-                tc::commit(tc::smem_u32(&bfree[s]));
+                if (!alive) break;
                 tc::commit(tc::smem_u32(&accf[ab]));
-                last_commit = seq;
-                // prefetch two chunks ahead: the stage of chunk seq - 1, whose MMAs precede these
-                while (copied <= seq + kS2 - 1) {
-                    if (!issue_copy(copied)) break;
-                    ++copied;
-                }
+                ++seq;
+                mit = nit2;
+                mj = nj2;
             }
             if (alive && cur_item >= 0) tc::commit(tc::smem_u32(afree));
             // on a timeout, let the issued MMAs drain (bounded) before the block frees its TMEM
             if (!alive && last_commit >= 0)
-                tc::mbar_wait(tc::smem_u32(&bfree[last_commit % kS2]), (int)(last_commit / kS2) & 1, nullptr, 0);
+                tc::mbar_wait(tc::smem_u32(&bfree[last_commit % kNS2]), (int)(last_commit / kNS2) & 1, nullptr, 0);
         }
     } else {
-        // ---------------- epilogue: two threads per atom (row halves of each chunk)
-        const int q4 = warp & 3, mt = (warp >> 2) & 1, rh = warp >> 3;
-        const uint32_t tl_base = tmem + ((uint32_t)(q4 * 32) << 16) + mt * kNC2 + rh * (kNC2 / 2);
+        // ---------------- epilogue: four threads per atom (row quarters of each chunk)
+        const int q4 = warp & 3, rq = warp >> 2;
+        const uint32_t tl_base = tmem + ((uint32_t)(q4 * 32) << 16) + rq * (kNC2 / kRQ);
         const float px = d.px, py = d.py, pz = d.pz;
         const double scale = (double)cmax[0];
         const int mrow = t & 127;
-        const int ksh = (d.KS + 1) / 2, ks0 = rh ? ksh : 0, ks1 = rh ? d.KS : ksh;
         bool alive = true;
         long seq = 0;
         int nitems_done = 0;
         for (int it = blockIdx.x; it < nitem && alive; it += gridDim.x) {
             const int tile = it / nparts, part = it % nparts;
-            const int c0 = part * cper, c1 = min(NC, c0 + cper);
-            if (c1 <= c0) continue;
-            const int at = tile * (kMT2 * 128) + mt * 128 + mrow;
+            const int c0 = part * cper, cnt = max(0, min(NC, c0 + cper) - c0);
+            if (cnt == 0) continue;
+            const int at = tile * 128 + mrow;
             const bool ok = at < v.nmove;
             const uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
-            // A for this item (each row half builds half of the K steps), after the previous
+            // A for this item (row quarter rq builds K steps rq, rq + 4, ...), after the previous
             // item's MMAs finished
-            if (nitems_done > 0) alive = tc::mbar_wait(tc::smem_u32(afree), (nitems_done - 1) & 1, err, 25);
-            alive = __all_sync(0xffffffffu, alive);
+            if (nitems_done > 0) alive = tc::mbar_wait_warp(tc::smem_u32(afree), (nitems_done - 1) & 1, err, 25);
+            alive = epilogue_all(alive);
             if (!alive) break;
-            for (int ks = ks0; ks < ks1; ++ks) {
+            for (int ks = rq; ks < d.KS; ks += kRQ) {
                 uint32_t wh[8], wl[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
@@ -612,8 +647,8 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                     if (ok && ni < d.NN) phase((uint32_t)(ni - d.KN) * rec.z, c, s);
                     split2(c, s, wh[i], wl[i]);
                 }
-                unsigned char* th = sm + L.off_a + ((mt * 2 + 0) * d.KS + ks) * 4096;
-                unsigned char* tlo = sm + L.off_a + ((mt * 2 + 1) * d.KS + ks) * 4096;
+                unsigned char* th = sm + L.off_a + (0 * d.KS + ks) * 4096;
+                unsigned char* tlo = sm + L.off_a + (1 * d.KS + ks) * 4096;
                 *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 0)) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
                 *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 8)) = make_uint4(wh[4], wh[5], wh[6], wh[7]);
                 *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 0)) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
@@ -626,16 +661,16 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             float dyc, dys;
             phase(rec.y, dyc, dys);
             float fx = 0.f, fy = 0.f, fz = 0.f;
-            for (int j = 0; j < c1 - c0; ++j, ++seq) {
-                const int c = item_chunk(it, j, c0, c1 - c0);
-                const int ab = (int)(seq % kAB2);
-                alive = tc::mbar_wait(tc::smem_u32(&accf[ab]), (int)(seq / kAB2) & 1, err, 26);
-                alive = __all_sync(0xffffffffu, alive);
+            for (int j = 0; j < cnt; ++j, ++seq) {
+                const int c = item_chunk(it, j, c0, cnt);
+                const int ab = (int)(seq & 1);
+                alive = tc::mbar_wait_warp(tc::smem_u32(&accf[ab]), (int)(seq >> 1) & 1, err, 26);
                 if (!alive) break;
                 tc::fence_after();
-                uint32_t raw[kNC2 / 2];
-                tc::tmem_ld16_nw(tl_base + ab * (kMT2 * kNC2), raw);
-                tc::tmem_ld16_nw(tl_base + ab * (kMT2 * kNC2) + 16, raw + 16);
+                uint32_t raw[kNC2 / kRQ];
+#pragma unroll
+                for (int cc = 0; cc < kNC2 / kRQ / 16; ++cc)
+                    tc::tmem_ld16_nw(tl_base + ab * kNC2 + cc * 16, raw + cc * 16);
                 tc::tmem_wait_ld();
                 tc::fence_before();
                 __syncwarp();
@@ -643,8 +678,8 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 float ec = 0.f, es = 0.f;
                 int pl = -1 << 30, pm = 0;
 #pragma unroll
-                for (int rr = 0; rr < kRC / 2; ++rr) {
-                    const int2 lm = rlm[c * kRC + rh * (kRC / 2) + rr];
+                for (int rr = 0; rr < kRC / kRQ; ++rr) {
+                    const int2 lm = rlm[c * kRC + rq * (kRC / kRQ) + rr];
                     if (rr == 0 || lm.x != pl || lm.y != pm + 1) {
                         phase((uint32_t)lm.x * rec.x + (uint32_t)lm.y * rec.y, ec, es);
                     } else {
@@ -663,12 +698,27 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                     fz += s1;
                 }
             }
-            if (ok && alive) {
-                const double q = (double)__uint_as_float(rec.w) * scale;
-                atomicAdd(&v.fx[at], q * (double)fx);
-                atomicAdd(&v.fy[at], q * (double)fy);
-                atomicAdd(&v.fz[at], q * (double)pz * (double)fz);
+            // the four row quarters of each atom meet in shared memory; every epilogue thread
+            // reaches these barriers on every item (a timeout only shortens the chunk loop, and
+            // the flag is combined over all epilogue warps before anyone leaves the item loop)
+            red[(rq * 128 + mrow) * 3 + 0] = fx;
+            red[(rq * 128 + mrow) * 3 + 1] = fy;
+            red[(rq * 128 + mrow) * 3 + 2] = fz;
+            alive = epilogue_all(alive);
+            if (rq == 0 && ok && alive) {
+                float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                for (int k = 0; k < kRQ; ++k) {
+                    sx += red[(k * 128 + mrow) * 3 + 0];
+                    sy += red[(k * 128 + mrow) * 3 + 1];
+                    sz += red[(k * 128 + mrow) * 3 + 2];
+                }
+                const double qq = (double)__uint_as_float(rec.w) * scale;
+                atomicAdd(&v.fx[at], qq * (double)sx);
+                atomicAdd(&v.fy[at], qq * (double)sy);
+                atomicAdd(&v.fz[at], qq * (double)pz * (double)sz);
             }
+            epilogue_sync();
         }
     }
     __syncthreads();
@@ -766,14 +816,14 @@ int recip_tc_setup(Ctx& c) {
     if (p.smem1 > 227 * 1024 || p.smem2 > 227 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
     // pass-2 work items: atom tiles x chunk ranges, spread so the last wave of 152 SMs is full
-    p.ntile2 = (v.nmove + kMT2 * 128 - 1) / (kMT2 * 128);
+    p.ntile2 = (v.nmove + 127) / 128;
     {
         int best = 1;
         double beff = -1.0;
         for (int np = 1; np <= 8 && np <= p.nchunk2; ++np) {
             const long items = (long)p.ntile2 * np;
             const long waves = (items + 151) / 152;
-            const double eff = (double)items / (double)(waves * 152) - 0.01 * np;  // A rebuild per item
+            const double eff = (double)items / (double)(waves * 152) - 0.005 * np;  // A rebuild per item
             if (eff > beff + 1e-9) {
                 beff = eff;
                 best = np;

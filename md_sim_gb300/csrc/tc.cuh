@@ -125,6 +125,32 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, int* e
     return false;
 }
 
+// Bounded wait for a whole warp: lane 0 polls (backing off with __nanosleep, so that many waiting
+// warps do not flood the shared-memory pipe that also carries the issuing thread's MMA and
+// bulk-copy instructions), the other lanes wait at __syncwarp; the result is warp-uniform.
+__device__ __forceinline__ bool mbar_wait_warp(uint32_t addr, uint32_t parity, int* err, int tag) {
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0) {
+        ok = 0;
+        for (int it = 0; it < (1 << 22); ++it) {
+            uint32_t done;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+                : "=r"(done)
+                : "r"(addr), "r"(parity)
+                : "memory");
+            if (done) {
+                ok = 1;
+                break;
+            }
+            __nanosleep(it < 16 ? 32 : 256);
+        }
+        if (!ok && err) atomicCAS(err, 0, tag);
+    }
+    __syncwarp();
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
 // 1-D bulk copy global -> shared, completion counted on an mbarrier (bytes multiple of 16).
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),

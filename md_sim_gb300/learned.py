@@ -15,6 +15,7 @@ All arrays cross the C ABI (mdg_mlp_*, mdg_shake_set_model / _record / _samples)
 from __future__ import annotations
 
 import ctypes as C
+import os
 import time
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional
@@ -133,3 +134,69 @@ def evaluate(ctx: Context, w: np.ndarray, steps: int = 50, phase_reps: int = 20)
         "shake_ms_plain": t_plain, "shake_ms_seeded": t_seed,
         "shake_ms_saved": t_plain - t_seed,
     }
+
+
+DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "shake_seed.npy")
+
+
+def load_or_train(lib: Lib, ctx: Context, s_start, path: str = DEFAULT_MODEL, steps: int = 30, epochs: int = 20):
+    """The stored seed network if it exists (and matches this build's parameter count), else a
+    quick one trained on `steps` plain SHAKE steps from s_start.  Returns (blob, description)."""
+    if os.path.exists(path):
+        w = np.load(path).astype(np.float32)
+        if w.size == nw(lib):
+            return w, f"stored ({os.path.basename(path)})"
+    ctx.set_state(s_start.copy())
+    X, Y, _ = collect(ctx, steps)
+    w, losses = train(lib, X, Y, epochs=epochs, batch=4096, lr=2e-3, seed=9)
+    return w, f"trained here on {X.shape[0]} samples, {epochs} epochs, loss {losses[0]:.3g} -> {losses[-1]:.3g}"
+
+
+def main(argv=None):
+    """Collect multipliers from plain SHAKE on the 8192-water SHAKE config, train the seed network
+    on the GPU, evaluate it from a fresh start and save the parameter blob (float32 .npy)."""
+    import argparse
+    import json
+
+    import md_sim_gb300
+    from . import configs
+    from .abi import MDG_MIXED
+
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--nwat", type=int, default=8192)
+    ap.add_argument("--cells", type=int, default=19)
+    ap.add_argument("--samples", type=int, default=1_000_000)
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--seed", type=int, default=9)
+    ap.add_argument("--eval-steps", type=int, default=100)
+    ap.add_argument("--equil", type=int, default=300)
+    ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
+                                                  "shake_seed.npy"))
+    args = ap.parse_args(argv)
+    lib = md_sim_gb300.load()
+    s, prm = configs.shake_water(nwat=args.nwat, cells=args.cells)
+    prm.precision = MDG_MIXED
+    ctx = Context(lib, s, prm)
+    configs.equilibrate(ctx, s, steps=args.equil, every=10)   # leave the start-up transient at 300 K
+    ctx.set_state(s)
+    steps = max(1, (args.samples + s.ncons - 1) // s.ncons)
+    t0 = time.perf_counter()
+    X, Y, sw = collect(ctx, steps)
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    w, losses = train(lib, X, Y, epochs=args.epochs, batch=args.batch, lr=args.lr, seed=args.seed)
+    t_train = time.perf_counter() - t0
+    ev = evaluate(ctx, w, steps=args.eval_steps)
+    os.makedirs(os.path.dirname(args.out), exist_ok=True)
+    np.save(args.out, w)
+    rep = {"samples": int(X.shape[0]), "collect_s": t_collect, "train_s": t_train, "epochs": args.epochs,
+           "loss_first": float(losses[0]), "loss_last": float(losses[-1]), "plain_sweeps_in_data": float(sw.mean()),
+           **ev, "out": args.out}
+    print(json.dumps(rep))
+    return rep
+
+
+if __name__ == "__main__":
+    main()

@@ -136,7 +136,10 @@ def test_shake_parity(clean, oracle, gpulib):
 
     sg, sr, g, r = _both("shake256", oracle, gpulib, mut)
     og, orf = g.force_get(sg), r.force_get(sr)
-    a = g.shake(sg, og["ft"])
+    assert np.abs(og["ft"] - orf["ft"]).max() <= 1e-11 * np.abs(orf["ft"]).max()
+    # the same forces into both SHAKEs: the sweep count of the reference stop rule depends on the
+    # last bits of one molecule's iteration, so force rounding is kept out of this comparison
+    a = g.shake(sg, orf["ft"])
     b = r.shake(sr, orf["ft"])
     assert a["sweeps"] == b["sweeps"]
     for u, w in ((sg.x0, sr.x0), (sg.y0, sr.y0), (sg.z0, sr.z0), (sg.xold, sr.xold)):
@@ -153,7 +156,7 @@ def test_shake_reference_stop_rule(oracle, gpulib):
 
     sg, sr, g, r = _both("shake256", oracle, gpulib, mut)
     og, orf = g.force_get(sg), r.force_get(sr)
-    a, b = g.shake(sg, og["ft"]), r.shake(sr, orf["ft"])
+    a, b = g.shake(sg, orf["ft"]), r.shake(sr, orf["ft"])
     assert a["sweeps"] == b["sweeps"]
     assert np.abs(sg.x0 - sr.x0).max() < 1e-12 * sg.lx
 
