@@ -121,7 +121,7 @@ struct TcPlan {
     bool ready = false;
     int KN = 0, NN = 0, NP = 0, KS = 0, KM = 0, NM = 0;
     int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, grid1x = 0, rtot = 0, tpc1 = 0, smem1 = 0, smem2 = 0;
-    int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0;
+    int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0, nlist2 = 0;
 };
 
 struct Ctx {

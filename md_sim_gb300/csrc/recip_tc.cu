@@ -427,23 +427,25 @@ __device__ __forceinline__ int item_chunk(int it, int j, int c0, int cnt) {
 
 constexpr int kRQ = 4;                  // row quarters of a chunk (threads per atom)
 constexpr int kEW2 = 4 * kRQ;           // epilogue warps: (lane quadrant, row quarter)
-constexpr int kT2 = kEW2 * 32 + 32;     // + issuer warp
+constexpr int kT2 = kEW2 * 32 + 64;     // + MMA warp + copy warp
 
-constexpr int kTPS2 = 4;                // K-step tiles (256 x 16 halves, 8 KB) per ring stage
-constexpr int kNS2 = 4;                 // ring stages
+constexpr int kTPS2 = 2;                // K-step tiles (256 x 16 halves, 8 KB) per ring stage
+constexpr int kNS2 = 8;                 // ring stages
 
 struct P2Layout {
-    uint32_t a_bytes, off_a, off_b, off_rows, off_red, total;
+    uint32_t a_bytes, off_a, off_b, off_rows, off_red, off_list, total;
 };
 
-__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad) {
+// nlist: chunks this CTA processes (its work list, filled at kernel start)
+__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nlist) {
     P2Layout L;
     L.a_bytes = 2 * KS * 4096;               // [h][ks] 128 x 16
     L.off_a = 1024;
     L.off_b = L.off_a + L.a_bytes;
     L.off_rows = L.off_b + kNS2 * kTPS2 * kTile2;  // ring of stages of K-step tiles
-    L.off_red = L.off_rows + nrow_pad * 8;   // (l, m) per row
-    L.total = L.off_red + kRQ * 128 * 3 * 4; // per-item force partials
+    L.off_red = L.off_rows + nrow_pad * 16;  // row records (float l, float m, l | restart << 31, m)
+    L.off_list = L.off_red + kRQ * 128 * 3 * 4;    // per-item force partials
+    L.total = L.off_list + nlist * 8;        // (chunk, item) per list entry
     return L;
 }
 
@@ -464,9 +466,9 @@ __device__ __forceinline__ bool epilogue_all(bool ok) {
 __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
                                                      const unsigned char* __restrict__ img,
                                                      const int4* __restrict__ rows, TcDims d, const float* cmax,
-                                                     int ntile, int nparts, int cper) {
+                                                     int ntile, int nparts, int cper, int nlist_max) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC);
+    const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC, nlist_max);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     uint64_t* full = reinterpret_cast<uint64_t*>(sm);      // [kNS2] stage landed
     uint64_t* bfree = full + kNS2;                          // [kNS2] MMAs reading the stage done
@@ -475,11 +477,13 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     uint64_t* afree = acce + 2;                             // MMAs of the item done
     uint64_t* aready = afree + 1;                           // A built (epilogue threads)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
-    int2* rlm = reinterpret_cast<int2*>(sm + L.off_rows);
+    float4* rlm = reinterpret_cast<float4*>(sm + L.off_rows);
     float* red = reinterpret_cast<float*>(sm + L.off_red);
+    int2* clist = reinterpret_cast<int2*>(sm + L.off_list);
     int* err = &v.status[ST_TC_TIMEOUT];
     const int NC = d.nchunk2;
     const int nitem = ntile * nparts;
+    int& s_nlist = *reinterpret_cast<int*>(sm + 516);
     if (t == 0) {
         for (int i = 0; i < kNS2; ++i) {
             tc::mbar_init(tc::smem_u32(&full[i]), 1);
@@ -495,88 +499,77 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     }
     for (int r = t; r < NC * kRC; r += kT2) {
         const int4 rw = r < d.nrow ? rows[r] : make_int4(0, 0, 0, 0);
-        rlm[r] = make_int2(rw.x, rw.y);
+        // restart the phase recurrence at the first row of each row quarter and wherever the
+        // row does not continue the previous one along m
+        int restart = (r % (kRC / kRQ)) == 0 || r >= d.nrow;
+        if (!restart) {
+            const int4 pw = rows[r - 1];  // 0 < r < nrow here
+            restart = pw.x != rw.x || pw.y + 1 != rw.y;
+        }
+        rlm[r] = make_float4((float)rw.x, (float)rw.y, __int_as_float(rw.x | (restart << 31)), __int_as_float(rw.y));
+    }
+    if (t == 0) {
+        // this CTA's flat work list: items blockIdx.x, blockIdx.x + gridDim.x, ..., each a chunk
+        // range walked from an item-dependent start
+        int n = 0;
+        for (int it = blockIdx.x; it < nitem; it += gridDim.x) {
+            const int c0 = (it % nparts) * cper, cnt = max(0, min(NC, c0 + cper) - c0);
+            for (int j = 0; j < cnt && n < nlist_max; ++j) clist[n++] = make_int2(item_chunk(it, j, c0, cnt), it);
+        }
+        s_nlist = n;
     }
     if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 512);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    if (warp == kEW2) {
-        // ---------------- issuer: K-step tile copies and MMAs over the CTA's (item, chunk) sequence
+    const int nlist = s_nlist;
+    const int TPCH = 2 * d.KS;  // tiles per chunk: hi K steps, then lo K steps
+    const long ntiles = (long)nlist * TPCH;
+    const long nstages = (ntiles + kTPS2 - 1) / kTPS2;
+    if (warp == kEW2 + 1) {
+        // ---------------- copy warp: K-step tiles of the work list into the stage ring
+        if (lane == 0) {
+            const uint32_t bbase = tc::smem_u32(sm + L.off_b);
+            for (long w = 0; w < nstages; ++w) {
+                const int slot = (int)(w % kNS2);
+                if (w >= kNS2 && !tc::mbar_wait(tc::smem_u32(&bfree[slot]), (int)((w / kNS2) - 1) & 1, err, 21)) break;
+                const long u0 = w * kTPS2;
+                const int n = (int)min((long)kTPS2, ntiles - u0);
+                const uint32_t fb = tc::smem_u32(&full[slot]);
+                tc::mbar_expect_tx(fb, (uint32_t)n * kTile2);
+                for (int i = 0; i < n; ++i) {
+                    const long u = u0 + i;
+                    const int c = clist[u / TPCH].x, k = (int)(u % TPCH);
+                    tc::bulk_g2s(bbase + (slot * kTPS2 + i) * kTile2, img + ((size_t)c * TPCH + k) * kTile2, kTile2, fb);
+                }
+            }
+        }
+    } else if (warp == kEW2) {
+        // ---------------- MMA warp
         if (lane == 0) {
             const uint32_t idesc = idesc_e(128, kNC2);
-            const uint32_t abase = tc::smem_u32(sm + L.off_a), bbase = tc::smem_u32(sm + L.off_b);
-            const uint64_t dA0 = tc::desc(abase), dB0 = tc::desc(bbase);
-            const int TPCH = 2 * d.KS;  // tiles per chunk: hi K steps, then lo K steps
+            const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(tc::smem_u32(sm + L.off_b));
             bool alive = true;
-            // chunk sequence of this CTA: items blockIdx.x, blockIdx.x + gridDim.x, ... (empty
-            // items skipped); (cit, cj, ck) walks it tile by tile for the copies
-            auto range = [&](int it, int& c0, int& cnt) {
-                const int part = it % nparts;
-                c0 = part * cper;
-                cnt = max(0, min(NC, c0 + cper) - c0);
-            };
-            auto skip_empty = [&](int& it, int& j) {
-                int c0, cnt;
-                while (it < nitem) {
-                    range(it, c0, cnt);
-                    if (j < cnt) return;
-                    it += gridDim.x;
-                    j = 0;
-                }
-            };
-            int cit = blockIdx.x, cj = 0, ck = 0;
-            skip_empty(cit, cj);
-            long w_copy = 0;  // stages copied
-            auto issue_stage = [&]() {
-                // the next kTPS2 tiles of the copy sequence (fewer at its end) into slot w_copy % kNS2
-                if (cit >= nitem) return;
-                const int slot = (int)(w_copy % kNS2);
-                const uint32_t fb = tc::smem_u32(&full[slot]);
-                const uint32_t dst0 = bbase + slot * (kTPS2 * kTile2);
-                int n = 0;
-                const unsigned char* src[kTPS2];
-                while (n < kTPS2 && cit < nitem) {
-                    int c0, cnt;
-                    range(cit, c0, cnt);
-                    const int c = item_chunk(cit, cj, c0, cnt);
-                    src[n++] = img + ((size_t)c * TPCH + ck) * kTile2;
-                    if (++ck == TPCH) {
-                        ck = 0;
-                        ++cj;
-                        skip_empty(cit, cj);
-                    }
-                }
-                tc::mbar_expect_tx(fb, (uint32_t)n * kTile2);
-                for (int i = 0; i < n; ++i) tc::bulk_g2s(dst0 + i * kTile2, src[i], kTile2, fb);
-                ++w_copy;
-            };
-            for (int i = 0; i < kNS2 - 1; ++i) issue_stage();
-            int mit = blockIdx.x, mj = 0;
-            skip_empty(mit, mj);
-            long u = 0, seq = 0;
             int cur_item = -1, nitems_done = 0;
-            long last_commit = -1;  // last committed stage
-            while (alive && mit < nitem) {
-                const int ab = (int)(seq & 1);
-                if (mit != cur_item) {
+            long last_stage = -1;
+            long u = 0;
+            for (int q = 0; q < nlist && alive; ++q) {
+                const int it = clist[q].y;
+                const int ab = q & 1;
+                if (it != cur_item) {
                     if (cur_item >= 0) {
                         tc::commit(tc::smem_u32(afree));
                         ++nitems_done;
                     }
-                    cur_item = mit;
+                    cur_item = it;
                     alive = tc::mbar_wait(tc::smem_u32(aready), nitems_done & 1, err, 22);
                     if (!alive) break;
                 }
-                if (seq >= 2) alive = tc::mbar_wait(tc::smem_u32(&acce[ab]), (int)((seq >> 1) - 1) & 1, err, 24);
+                if (q >= 2) alive = tc::mbar_wait(tc::smem_u32(&acce[ab]), ((q >> 1) - 1) & 1, err, 24);
                 if (!alive) break;
                 const uint32_t dcol = tmem + ab * kNC2;
-                // is this the CTA's last chunk? (then its last tile closes a partial stage)
-                int nit2 = mit, nj2 = mj + 1;
-                skip_empty(nit2, nj2);
-                const bool last_chunk = nit2 >= nitem;
-                for (int k = 0; k < TPCH && alive; ++k, ++u) {
+                for (int k = 0; k < TPCH; ++k, ++u) {
                     const long w = u / kTPS2;
                     const int slot = (int)(w % kNS2), pos = (int)(u % kTPS2);
                     if (pos == 0) {
@@ -585,36 +578,24 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                         tc::fence_after();
                     }
                     const uint64_t b = dB0 + (uint64_t)((slot * kTPS2 + pos) * (kTile2 >> 4));
-                    const int ks = k < d.KS ? k : k - d.KS;
-                    const uint64_t ah = dA0 + (uint64_t)((0 * d.KS + ks) * 256);
                     if (k < d.KS) {
-                        const uint64_t al = dA0 + (uint64_t)((1 * d.KS + ks) * 256);
-                        tc::mma_bf16(dcol, ah, b, idesc, k > 0 ? 1u : 0u);
-                        tc::mma_bf16(dcol, al, b, idesc, 1u);
+                        tc::mma_bf16(dcol, dA0 + (uint64_t)(k * 256), b, idesc, k > 0 ? 1u : 0u);
+                        tc::mma_bf16(dcol, dA0 + (uint64_t)((d.KS + k) * 256), b, idesc, 1u);
                     } else {
-                        tc::mma_bf16(dcol, ah, b, idesc, 1u);
+                        tc::mma_bf16(dcol, dA0 + (uint64_t)((k - d.KS) * 256), b, idesc, 1u);
                     }
-                    if (pos == kTPS2 - 1 || (last_chunk && k == TPCH - 1)) {
+                    if (pos == kTPS2 - 1 || u == ntiles - 1) {
                         tc::commit(tc::smem_u32(&bfree[slot]));
-                        last_commit = w;
-                        // refill the slot of stage w - 1 (its MMAs precede the ones just issued)
-                        if (w >= 1) {
-                            alive = tc::mbar_wait(tc::smem_u32(&bfree[(w - 1) % kNS2]), (int)((w - 1) / kNS2) & 1, err, 21);
-                            if (!alive) break;
-                        }
-                        issue_stage();
+                        last_stage = w;
                     }
                 }
                 if (!alive) break;
                 tc::commit(tc::smem_u32(&accf[ab]));
-                ++seq;
-                mit = nit2;
-                mj = nj2;
             }
             if (alive && cur_item >= 0) tc::commit(tc::smem_u32(afree));
             // on a timeout, let the issued MMAs drain (bounded) before the block frees its TMEM
-            if (!alive && last_commit >= 0)
-                tc::mbar_wait(tc::smem_u32(&bfree[last_commit % kNS2]), (int)(last_commit / kNS2) & 1, nullptr, 0);
+            if (!alive && last_stage >= 0)
+                tc::mbar_wait(tc::smem_u32(&bfree[last_stage % kNS2]), (int)(last_stage / kNS2) & 1, nullptr, 0);
         }
     } else {
         // ---------------- epilogue: four threads per atom (row quarters of each chunk)
@@ -624,12 +605,12 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
         const double scale = (double)cmax[0];
         const int mrow = t & 127;
         bool alive = true;
-        long seq = 0;
         int nitems_done = 0;
-        for (int it = blockIdx.x; it < nitem && alive; it += gridDim.x) {
-            const int tile = it / nparts, part = it % nparts;
-            const int c0 = part * cper, cnt = max(0, min(NC, c0 + cper) - c0);
-            if (cnt == 0) continue;
+        for (int q0 = 0; q0 < nlist && alive;) {
+            const int it = clist[q0].y;
+            int q1 = q0 + 1;
+            while (q1 < nlist && clist[q1].y == it) ++q1;   // this item's entries: [q0, q1)
+            const int tile = it / nparts;
             const int at = tile * 128 + mrow;
             const bool ok = at < v.nmove;
             const uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
@@ -661,10 +642,10 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             float dyc, dys;
             phase(rec.y, dyc, dys);
             float fx = 0.f, fy = 0.f, fz = 0.f;
-            for (int j = 0; j < cnt; ++j, ++seq) {
-                const int c = item_chunk(it, j, c0, cnt);
-                const int ab = (int)(seq & 1);
-                alive = tc::mbar_wait_warp(tc::smem_u32(&accf[ab]), (int)(seq >> 1) & 1, err, 26);
+            for (int q = q0; q < q1; ++q) {
+                const int c = clist[q].x;
+                const int ab = q & 1;
+                alive = tc::mbar_wait_warp(tc::smem_u32(&accf[ab]), (q >> 1) & 1, err, 26);
                 if (!alive) break;
                 tc::fence_after();
                 uint32_t raw[kNC2 / kRQ];
@@ -676,26 +657,23 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(tc::smem_u32(&acce[ab]));
                 float ec = 0.f, es = 0.f;
-                int pl = -1 << 30, pm = 0;
 #pragma unroll
                 for (int rr = 0; rr < kRC / kRQ; ++rr) {
-                    const int2 lm = rlm[c * kRC + rq * (kRC / kRQ) + rr];
-                    if (rr == 0 || lm.x != pl || lm.y != pm + 1) {
-                        phase((uint32_t)lm.x * rec.x + (uint32_t)lm.y * rec.y, ec, es);
+                    const float4 lm = rlm[c * kRC + rq * (kRC / kRQ) + rr];
+                    const int lb = __float_as_int(lm.z);
+                    if (lb < 0) {
+                        phase((uint32_t)(lb & 0x7fffffff) * rec.x + (uint32_t)__float_as_int(lm.w) * rec.y, ec, es);
                     } else {
                         const float nc = ec * dyc - es * dys;
                         es = ec * dys + es * dyc;
                         ec = nc;
                     }
-                    pl = lm.x;
-                    pm = lm.y;
                     const float v0 = __uint_as_float(raw[rr * 4 + 0]), v1 = __uint_as_float(raw[rr * 4 + 1]);
                     const float v2 = __uint_as_float(raw[rr * 4 + 2]), v3 = __uint_as_float(raw[rr * 4 + 3]);
                     const float s0 = ec * v1 + es * v0;
-                    const float s1 = ec * v3 + es * v2;
-                    fx += (px * (float)lm.x) * s0;
-                    fy += (py * (float)lm.y) * s0;
-                    fz += s1;
+                    fx = fmaf(lm.x, s0, fx);
+                    fy = fmaf(lm.y, s0, fy);
+                    fz += ec * v3 + es * v2;
                 }
             }
             // the four row quarters of each atom meet in shared memory; every epilogue thread
@@ -714,11 +692,12 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                     sz += red[(k * 128 + mrow) * 3 + 2];
                 }
                 const double qq = (double)__uint_as_float(rec.w) * scale;
-                atomicAdd(&v.fx[at], qq * (double)sx);
-                atomicAdd(&v.fy[at], qq * (double)sy);
+                atomicAdd(&v.fx[at], qq * (double)px * (double)sx);
+                atomicAdd(&v.fy[at], qq * (double)py * (double)sy);
                 atomicAdd(&v.fz[at], qq * (double)pz * (double)sz);
             }
             epilogue_sync();
+            q0 = q1;
         }
     }
     __syncthreads();
@@ -812,7 +791,7 @@ int recip_tc_setup(Ctx& c) {
     p.mtiles = (ks.nrow + 127) / 128;
     p.nchunk2 = (ks.nrow + kRC - 1) / kRC;
     p.smem1 = (int)(p.tpc1 == 4 ? p1_layout(4, P1<4>::kS, p.NP, p.NM).total : p1_layout(2, P1<2>::kS, p.NP, p.NM).total);
-    p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC).total;
+    p.smem2 = 0;  // set with the work split below
     if (p.smem1 > 227 * 1024 || p.smem2 > 227 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
     // pass-2 work items: atom tiles x chunk ranges, spread so the last wave of 152 SMs is full
@@ -834,6 +813,10 @@ int recip_tc_setup(Ctx& c) {
     p.cper2 = (p.nchunk2 + p.nparts2 - 1) / p.nparts2;
     p.nparts2 = (p.nchunk2 + p.cper2 - 1) / p.cper2;
     p.grid2 = std::min(152, p.ntile2 * p.nparts2);
+    p.nlist2 = ((p.ntile2 * p.nparts2 + p.grid2 - 1) / p.grid2) * p.cper2;
+    p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC, p.nlist2).total;
+    if (p.smem2 > 227 * 1024)
+        return set_err(&c, MDG_E_UNSUPPORTED, "work list too long for the tensor-core force pass");
     c.d_tc_atoms = (uint4*)dalloc(c, sizeof(uint4) * std::max(v.nmove, 1));
     c.d_tc_img = (unsigned char*)dalloc(c, (size_t)std::max(p.nchunk2, 1) * 2 * p.KS * kTile2);
     c.d_tc_cmax = (float*)dalloc(c, sizeof(float) * 4);
@@ -868,7 +851,7 @@ void recip_tc(Ctx& c) {
     k_tc_prep_c<<<(int)std::min<long>((total + 255) / 256, 152 * 8), 256, 0, c.stream>>>(c.d_tc_cf, ks.row, ks.row_nlen,
                                                                                          d, c.d_tc_img, c.d_tc_cmax);
     k_tc_force<<<p.grid2, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, ks.row, d, c.d_tc_cmax, p.ntile2,
-                                                    p.nparts2, p.cper2);
+                                                    p.nparts2, p.cper2, p.nlist2);
 }
 
 int umma_selftest(int n, int k, const float* a, const float* b, float* dout, std::string& err) {
