@@ -367,7 +367,7 @@ __global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit,
 // col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part; one thread
 // per (chunk, K step, column, n) writes the (part 0, part 1) half pairs of hi and lo.
 // ---------------------------------------------------------------------------------------------
-constexpr int kRC = 64;                 // rows per pass-2 chunk
+constexpr int kRC = 32;                 // rows per pass-2 chunk
 constexpr int kNC2 = 4 * kRC;           // pass-2 MMA N
 constexpr uint32_t kTile2 = kNC2 * 32;  // one N x 16 B tile (bytes)
 
@@ -408,260 +408,166 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
 // ---------------------------------------------------------------------------------------------
 // pass 2: forces
 //
-// Work items (a tile of 128 atoms, a range of row chunks) are spread over a persistent grid.
-// Per item the epilogue warps build A = e^{i n tz} of the tile's atoms (K = 2 (n + KN) + part).
-// One MMA is M = 128 atoms x N = 256 (T and T' x re/im of 64 rows) x K = 16: the largest N of a
-// single-CTA MMA, since an MMA costs about the same issue time for any N up to 128.  The issuer
-// streams the chunk images as K-step tiles (hi part of C, then lo part; 4 tiles per ring stage,
-// 4 stages) with cp.async.bulk: per hi tile ah*bh and al*bh, per lo tile ah*bl, all into one
-// accumulator (consecutive MMAs on one accumulator issue fastest).  Accumulators are
-// double-buffered in TMEM against the epilogue, where four threads own each atom (16 rows each):
-// per row they form Im(e^{i(l tx + m ty)} T) with the row phase advanced along m by a complex
-// multiply (recomputed by __sincosf at the first of the 16 rows and at each change of l).
+// One CTA per 128 atoms.  The CTA builds A = e^{i n tz} of its atoms (K = 2 (n + KN) + part) and
+// walks the chunk images of C (32 rows each: N = 128 columns = T and T' x re/im), double-buffered:
+// the issuer thread starts the copy of chunk c + 1 as soon as the MMAs of chunk c are issued (its
+// stage is free once the MMAs of chunk c - 1 are done), so the copy overlaps the MMAs; per chunk
+// 3 (hi/lo) products per K step accumulate into one of two TMEM accumulators, which the four
+// epilogue warps (one thread per atom) drain while the next chunk runs.  Per row the epilogue
+// forms Im(e^{i(l tx + m ty)} T) with the row phase advanced along m by a complex multiply
+// (recomputed by __sincosf at rows flagged in the shared row table: every 8th row and each change
+// of l).
 // ---------------------------------------------------------------------------------------------
-// j-th chunk of an item: every item walks its chunk range from a different starting point, so
-// that the CTAs do not all read the same chunk image (the same L2 lines) at the same time
-__device__ __forceinline__ int item_chunk(int it, int j, int c0, int cnt) {
-    return c0 + (int)((j + (unsigned)it * 7919u % (unsigned)cnt) % (unsigned)cnt);
-}
-
-constexpr int kRQ = 4;                  // row quarters of a chunk (threads per atom)
-constexpr int kEW2 = 4 * kRQ;           // epilogue warps: (lane quadrant, row quarter)
-constexpr int kT2 = kEW2 * 32 + 64;     // + MMA warp + copy warp
-
-constexpr int kTPS2 = 2;                // K-step tiles (256 x 16 halves, 8 KB) per ring stage
-constexpr int kNS2 = 8;                 // ring stages
+constexpr int kT2 = 256;  // epilogue warps 0-3, issuer warp 4, warps 5-7 help build A
 
 struct P2Layout {
-    uint32_t a_bytes, off_a, off_b, off_rows, off_red, off_list, total;
+    uint32_t a_bytes, img, off_a, off_b, off_rows, total;
 };
 
-// nlist: chunks this CTA processes (its work list, filled at kernel start)
-__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nlist) {
+__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad) {
     P2Layout L;
-    L.a_bytes = 2 * KS * 4096;               // [h][ks] 128 x 16
+    L.a_bytes = 2 * KS * 4096;                 // [h][ks] 128 x 16
+    L.img = 2 * KS * kTile2;                   // a chunk image [h][ks] 128 x 16
     L.off_a = 1024;
     L.off_b = L.off_a + L.a_bytes;
-    L.off_rows = L.off_b + kNS2 * kTPS2 * kTile2;  // ring of stages of K-step tiles
-    L.off_red = L.off_rows + nrow_pad * 16;  // row records (float l, float m, l | restart << 31, m)
-    L.off_list = L.off_red + kRQ * 128 * 3 * 4;    // per-item force partials
-    L.total = L.off_list + nlist * 8;        // (chunk, item) per list entry
+    L.off_rows = L.off_b + 2 * L.img;
+    L.total = L.off_rows + nrow_pad * 16;      // (float l, float m, l | restart << 31, m)
     return L;
-}
-
-// Named barrier 2 over the epilogue warps; the _all form returns the AND of the threads' flags, so
-// that a timeout seen by one warp stops every epilogue warp at the same point.
-__device__ __forceinline__ void epilogue_sync() { asm volatile("bar.sync 2, %0;" ::"n"(kEW2 * 32) : "memory"); }
-__device__ __forceinline__ bool epilogue_all(bool ok) {
-    uint32_t res;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, 2, %2, q;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(res)
-        : "r"((uint32_t)ok), "n"(kEW2 * 32)
-        : "memory");
-    return res != 0;
 }
 
 __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
                                                      const unsigned char* __restrict__ img,
-                                                     const int4* __restrict__ rows, TcDims d, const float* cmax,
-                                                     int ntile, int nparts, int cper, int nlist_max) {
+                                                     const int4* __restrict__ rows, TcDims d, const float* cmax) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC, nlist_max);
+    const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm);      // [kNS2] stage landed
-    uint64_t* bfree = full + kNS2;                          // [kNS2] MMAs reading the stage done
-    uint64_t* accf = bfree + kNS2;                          // [2] accumulator ready
-    uint64_t* acce = accf + 2;                              // [2] accumulator drained (epilogue warps)
-    uint64_t* afree = acce + 2;                             // MMAs of the item done
-    uint64_t* aready = afree + 1;                           // A built (epilogue threads)
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm);   // [2] chunk image landed
+    uint64_t* mdone = full + 2;                          // [2] MMAs of the chunk done (accumulator ready)
+    uint64_t* afree = mdone + 2;                         // [2] accumulator drained (4 epilogue warps)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     float4* rlm = reinterpret_cast<float4*>(sm + L.off_rows);
-    float* red = reinterpret_cast<float*>(sm + L.off_red);
-    int2* clist = reinterpret_cast<int2*>(sm + L.off_list);
     int* err = &v.status[ST_TC_TIMEOUT];
+    const int atom0 = blockIdx.x * 128;
     const int NC = d.nchunk2;
-    const int nitem = ntile * nparts;
-    int& s_nlist = *reinterpret_cast<int*>(sm + 516);
     if (t == 0) {
-        for (int i = 0; i < kNS2; ++i) {
-            tc::mbar_init(tc::smem_u32(&full[i]), 1);
-            tc::mbar_init(tc::smem_u32(&bfree[i]), 1);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(tc::smem_u32(&full[b]), 1);
+            tc::mbar_init(tc::smem_u32(&mdone[b]), 1);
+            tc::mbar_init(tc::smem_u32(&afree[b]), 4);
         }
-        for (int i = 0; i < 2; ++i) {
-            tc::mbar_init(tc::smem_u32(&accf[i]), 1);
-            tc::mbar_init(tc::smem_u32(&acce[i]), kEW2);
-        }
-        tc::mbar_init(tc::smem_u32(afree), 1);
-        tc::mbar_init(tc::smem_u32(aready), kEW2 * 32);
         tc::mbar_fence_init();
     }
     for (int r = t; r < NC * kRC; r += kT2) {
         const int4 rw = r < d.nrow ? rows[r] : make_int4(0, 0, 0, 0);
-        // restart the phase recurrence at the first row of each row quarter and wherever the
-        // row does not continue the previous one along m
-        int restart = (r % (kRC / kRQ)) == 0 || r >= d.nrow;
+        int restart = (r & 7) == 0 || r >= d.nrow;
         if (!restart) {
             const int4 pw = rows[r - 1];  // 0 < r < nrow here
             restart = pw.x != rw.x || pw.y + 1 != rw.y;
         }
         rlm[r] = make_float4((float)rw.x, (float)rw.y, __int_as_float(rw.x | (restart << 31)), __int_as_float(rw.y));
     }
-    if (t == 0) {
-        // this CTA's flat work list: items blockIdx.x, blockIdx.x + gridDim.x, ..., each a chunk
-        // range walked from an item-dependent start
-        int n = 0;
-        for (int it = blockIdx.x; it < nitem; it += gridDim.x) {
-            const int c0 = (it % nparts) * cper, cnt = max(0, min(NC, c0 + cper) - c0);
-            for (int j = 0; j < cnt && n < nlist_max; ++j) clist[n++] = make_int2(item_chunk(it, j, c0, cnt), it);
+    if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 256);
+    // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part
+    {
+        const int mrow = t & 127, half = t >> 7;
+        const int at = atom0 + mrow;
+        const uint32_t uz = at < v.nmove ? atoms[at].z : 0u;
+        const int ksplit = (d.KS + 1) / 2;
+        const int ks0 = half ? ksplit : 0, ks1 = half ? d.KS : ksplit;
+        for (int ks = ks0; ks < ks1; ++ks) {
+            uint32_t wh[8], wl[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int ni = ks * 8 + i;
+                float c = 0.f, s = 0.f;
+                if (at < v.nmove && ni < d.NN) phase((uint32_t)(ni - d.KN) * uz, c, s);
+                split2(c, s, wh[i], wl[i]);
+            }
+            unsigned char* th = sm + L.off_a + (0 * d.KS + ks) * 4096;
+            unsigned char* tlo = sm + L.off_a + (1 * d.KS + ks) * 4096;
+            *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 0)) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+            *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 8)) = make_uint4(wh[4], wh[5], wh[6], wh[7]);
+            *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 0)) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+            *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 8)) = make_uint4(wl[4], wl[5], wl[6], wl[7]);
         }
-        s_nlist = n;
     }
-    if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 512);
+    tc::fence_async_smem();
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    const int nlist = s_nlist;
-    const int TPCH = 2 * d.KS;  // tiles per chunk: hi K steps, then lo K steps
-    const long ntiles = (long)nlist * TPCH;
-    const long nstages = (ntiles + kTPS2 - 1) / kTPS2;
-    if (warp == kEW2 + 1) {
-        // ---------------- copy warp: K-step tiles of the work list into the stage ring
-        if (lane == 0) {
-            const uint32_t bbase = tc::smem_u32(sm + L.off_b);
-            for (long w = 0; w < nstages; ++w) {
-                const int slot = (int)(w % kNS2);
-                if (w >= kNS2 && !tc::mbar_wait(tc::smem_u32(&bfree[slot]), (int)((w / kNS2) - 1) & 1, err, 21)) break;
-                const long u0 = w * kTPS2;
-                const int n = (int)min((long)kTPS2, ntiles - u0);
-                const uint32_t fb = tc::smem_u32(&full[slot]);
-                tc::mbar_expect_tx(fb, (uint32_t)n * kTile2);
-                for (int i = 0; i < n; ++i) {
-                    const long u = u0 + i;
-                    const int c = clist[u / TPCH].x, k = (int)(u % TPCH);
-                    tc::bulk_g2s(bbase + (slot * kTPS2 + i) * kTile2, img + ((size_t)c * TPCH + k) * kTile2, kTile2, fb);
-                }
-            }
-        }
-    } else if (warp == kEW2) {
-        // ---------------- MMA warp
+    if (warp == 4) {
         if (lane == 0) {
             const uint32_t idesc = idesc_e(128, kNC2);
-            const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(tc::smem_u32(sm + L.off_b));
+            const uint32_t bbase = tc::smem_u32(sm + L.off_b);
+            const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(bbase);
+            const uint32_t half = L.img / 2;
+            auto copy = [&](int c) {
+                const int s = c & 1;
+                const uint32_t fb = tc::smem_u32(&full[s]);
+                tc::mbar_expect_tx(fb, L.img);
+                tc::bulk_g2s(bbase + s * L.img, img + (size_t)c * L.img, half, fb);
+                tc::bulk_g2s(bbase + s * L.img + half, img + (size_t)c * L.img + half, half, fb);
+            };
             bool alive = true;
-            int cur_item = -1, nitems_done = 0;
-            long last_stage = -1;
-            long u = 0;
-            for (int q = 0; q < nlist && alive; ++q) {
-                const int it = clist[q].y;
-                const int ab = q & 1;
-                if (it != cur_item) {
-                    if (cur_item >= 0) {
-                        tc::commit(tc::smem_u32(afree));
-                        ++nitems_done;
-                    }
-                    cur_item = it;
-                    alive = tc::mbar_wait(tc::smem_u32(aready), nitems_done & 1, err, 22);
-                    if (!alive) break;
-                }
-                if (q >= 2) alive = tc::mbar_wait(tc::smem_u32(&acce[ab]), ((q >> 1) - 1) & 1, err, 24);
+            if (NC > 0) copy(0);
+            for (int c = 0; c < NC && alive; ++c) {
+                const int s = c & 1;
+                alive = tc::mbar_wait(tc::smem_u32(&full[s]), (c >> 1) & 1, err, 22);
                 if (!alive) break;
-                const uint32_t dcol = tmem + ab * kNC2;
-                for (int k = 0; k < TPCH; ++k, ++u) {
-                    const long w = u / kTPS2;
-                    const int slot = (int)(w % kNS2), pos = (int)(u % kTPS2);
-                    if (pos == 0) {
-                        alive = tc::mbar_wait(tc::smem_u32(&full[slot]), (int)(w / kNS2) & 1, err, 23);
-                        if (!alive) break;
-                        tc::fence_after();
-                    }
-                    const uint64_t b = dB0 + (uint64_t)((slot * kTPS2 + pos) * (kTile2 >> 4));
-                    if (k < d.KS) {
-                        tc::mma_bf16(dcol, dA0 + (uint64_t)(k * 256), b, idesc, k > 0 ? 1u : 0u);
-                        tc::mma_bf16(dcol, dA0 + (uint64_t)((d.KS + k) * 256), b, idesc, 1u);
-                    } else {
-                        tc::mma_bf16(dcol, dA0 + (uint64_t)((k - d.KS) * 256), b, idesc, 1u);
-                    }
-                    if (pos == kTPS2 - 1 || u == ntiles - 1) {
-                        tc::commit(tc::smem_u32(&bfree[slot]));
-                        last_stage = w;
-                    }
-                }
-                if (!alive) break;
-                tc::commit(tc::smem_u32(&accf[ab]));
-            }
-            if (alive && cur_item >= 0) tc::commit(tc::smem_u32(afree));
-            // on a timeout, let the issued MMAs drain (bounded) before the block frees its TMEM
-            if (!alive && last_stage >= 0)
-                tc::mbar_wait(tc::smem_u32(&bfree[last_stage % kNS2]), (int)(last_stage / kNS2) & 1, nullptr, 0);
-        }
-    } else {
-        // ---------------- epilogue: four threads per atom (row quarters of each chunk)
-        const int q4 = warp & 3, rq = warp >> 2;
-        const uint32_t tl_base = tmem + ((uint32_t)(q4 * 32) << 16) + rq * (kNC2 / kRQ);
-        const float px = d.px, py = d.py, pz = d.pz;
-        const double scale = (double)cmax[0];
-        const int mrow = t & 127;
-        bool alive = true;
-        int nitems_done = 0;
-        for (int q0 = 0; q0 < nlist && alive;) {
-            const int it = clist[q0].y;
-            int q1 = q0 + 1;
-            while (q1 < nlist && clist[q1].y == it) ++q1;   // this item's entries: [q0, q1)
-            const int tile = it / nparts;
-            const int at = tile * 128 + mrow;
-            const bool ok = at < v.nmove;
-            const uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
-            // A for this item (row quarter rq builds K steps rq, rq + 4, ...), after the previous
-            // item's MMAs finished
-            if (nitems_done > 0) alive = tc::mbar_wait_warp(tc::smem_u32(afree), (nitems_done - 1) & 1, err, 25);
-            alive = epilogue_all(alive);
-            if (!alive) break;
-            for (int ks = rq; ks < d.KS; ks += kRQ) {
-                uint32_t wh[8], wl[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int ni = ks * 8 + i;
-                    float c = 0.f, s = 0.f;
-                    if (ok && ni < d.NN) phase((uint32_t)(ni - d.KN) * rec.z, c, s);
-                    split2(c, s, wh[i], wl[i]);
-                }
-                unsigned char* th = sm + L.off_a + (0 * d.KS + ks) * 4096;
-                unsigned char* tlo = sm + L.off_a + (1 * d.KS + ks) * 4096;
-                *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 0)) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
-                *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 8)) = make_uint4(wh[4], wh[5], wh[6], wh[7]);
-                *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 0)) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
-                *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 8)) = make_uint4(wl[4], wl[5], wl[6], wl[7]);
-            }
-            tc::fence_async_smem();
-            tc::mbar_arrive(tc::smem_u32(aready));
-            ++nitems_done;
-            // per-atom step of the row phase along m
-            float dyc, dys;
-            phase(rec.y, dyc, dys);
-            float fx = 0.f, fy = 0.f, fz = 0.f;
-            for (int q = q0; q < q1; ++q) {
-                const int c = clist[q].x;
-                const int ab = q & 1;
-                alive = tc::mbar_wait_warp(tc::smem_u32(&accf[ab]), (q >> 1) & 1, err, 26);
+                if (c >= 2) alive = tc::mbar_wait(tc::smem_u32(&afree[s]), ((c >> 1) - 1) & 1, err, 23);
                 if (!alive) break;
                 tc::fence_after();
-                uint32_t raw[kNC2 / kRQ];
+                const uint32_t dcol = tmem + s * kNC2;
+                const uint64_t dB = dB0 + (uint64_t)((s * L.img) >> 4);
+                for (int ks = 0; ks < d.KS; ++ks) {
+                    const uint64_t ah = dA0 + (uint64_t)(ks * 256), al = dA0 + (uint64_t)((d.KS + ks) * 256);
+                    const uint64_t bh = dB + (uint64_t)(ks * (kTile2 >> 4)), bl = dB + (uint64_t)((d.KS + ks) * (kTile2 >> 4));
+                    tc::mma_bf16(dcol, ah, bh, idesc, ks > 0 ? 1u : 0u);
+                    tc::mma_bf16(dcol, ah, bl, idesc, 1u);
+                    tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                }
+                tc::commit(tc::smem_u32(&mdone[s]));
+                // next chunk's copy into the other stage, free once the MMAs of chunk c - 1 are done
+                if (c + 1 < NC) {
+                    if (c >= 1) alive = tc::mbar_wait(tc::smem_u32(&mdone[s ^ 1]), ((c - 1) >> 1) & 1, err, 21);
+                    if (!alive) break;
+                    copy(c + 1);
+                }
+            }
+            // on a timeout, let issued work drain (bounded) before the block frees its TMEM
+            if (!alive && NC > 0) tc::mbar_wait(tc::smem_u32(&mdone[(NC - 1) & 1]), ((NC - 1) >> 1) & 1, nullptr, 0);
+        }
+    } else if (warp < 4) {
+        const int at = atom0 + t;
+        const bool ok = at < v.nmove;
+        const uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
+        float dyc, dys;
+        phase(rec.y, dyc, dys);
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        bool alive = true;
+        for (int c = 0; c < NC && alive; ++c) {
+            const int s = c & 1;
+            alive = tc::mbar_wait_warp(tc::smem_u32(&mdone[s]), (c >> 1) & 1, err, 24);
+            if (!alive) break;
+            tc::fence_after();
+            for (int hf = 0; hf < 2; ++hf) {
+                uint32_t raw[64];
 #pragma unroll
-                for (int cc = 0; cc < kNC2 / kRQ / 16; ++cc)
-                    tc::tmem_ld16_nw(tl_base + ab * kNC2 + cc * 16, raw + cc * 16);
+                for (int cc = 0; cc < 4; ++cc)
+                    tc::tmem_ld16_nw(tmem + ((uint32_t)(warp * 32) << 16) + s * kNC2 + hf * 64 + cc * 16, raw + cc * 16);
                 tc::tmem_wait_ld();
-                tc::fence_before();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(tc::smem_u32(&acce[ab]));
+                if (hf == 1) {
+                    tc::fence_before();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(tc::smem_u32(&afree[s]));
+                }
                 float ec = 0.f, es = 0.f;
 #pragma unroll
-                for (int rr = 0; rr < kRC / kRQ; ++rr) {
-                    const float4 lm = rlm[c * kRC + rq * (kRC / kRQ) + rr];
+                for (int rr = 0; rr < 16; ++rr) {
+                    const float4 lm = rlm[c * kRC + hf * 16 + rr];
                     const int lb = __float_as_int(lm.z);
-                    if (lb < 0) {
+                    if (rr == 0 || lb < 0) {
                         phase((uint32_t)(lb & 0x7fffffff) * rec.x + (uint32_t)__float_as_int(lm.w) * rec.y, ec, es);
                     } else {
                         const float nc = ec * dyc - es * dys;
@@ -676,34 +582,18 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                     fz += ec * v3 + es * v2;
                 }
             }
-            // the four row quarters of each atom meet in shared memory; every epilogue thread
-            // reaches these barriers on every item (a timeout only shortens the chunk loop, and
-            // the flag is combined over all epilogue warps before anyone leaves the item loop)
-            red[(rq * 128 + mrow) * 3 + 0] = fx;
-            red[(rq * 128 + mrow) * 3 + 1] = fy;
-            red[(rq * 128 + mrow) * 3 + 2] = fz;
-            alive = epilogue_all(alive);
-            if (rq == 0 && ok && alive) {
-                float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll
-                for (int k = 0; k < kRQ; ++k) {
-                    sx += red[(k * 128 + mrow) * 3 + 0];
-                    sy += red[(k * 128 + mrow) * 3 + 1];
-                    sz += red[(k * 128 + mrow) * 3 + 2];
-                }
-                const double qq = (double)__uint_as_float(rec.w) * scale;
-                atomicAdd(&v.fx[at], qq * (double)px * (double)sx);
-                atomicAdd(&v.fy[at], qq * (double)py * (double)sy);
-                atomicAdd(&v.fz[at], qq * (double)pz * (double)sz);
-            }
-            epilogue_sync();
-            q0 = q1;
+        }
+        if (ok && alive) {
+            const double q = (double)__uint_as_float(rec.w) * (double)cmax[0];
+            v.fx[at] += q * (double)d.px * (double)fx;
+            v.fy[at] += q * (double)d.py * (double)fy;
+            v.fz[at] += q * (double)d.pz * (double)fz;
         }
     }
     __syncthreads();
     if (warp == 0) {
         tc::fence_after();
-        tc::tmem_dealloc(tmem, 512);
+        tc::tmem_dealloc(tmem, 256);
     }
 }
 
@@ -791,32 +681,9 @@ int recip_tc_setup(Ctx& c) {
     p.mtiles = (ks.nrow + 127) / 128;
     p.nchunk2 = (ks.nrow + kRC - 1) / kRC;
     p.smem1 = (int)(p.tpc1 == 4 ? p1_layout(4, P1<4>::kS, p.NP, p.NM).total : p1_layout(2, P1<2>::kS, p.NP, p.NM).total);
-    p.smem2 = 0;  // set with the work split below
+    p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC).total;
     if (p.smem1 > 227 * 1024 || p.smem2 > 227 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
-    // pass-2 work items: atom tiles x chunk ranges, spread so the last wave of 152 SMs is full
-    p.ntile2 = (v.nmove + 127) / 128;
-    {
-        int best = 1;
-        double beff = -1.0;
-        for (int np = 1; np <= 8 && np <= p.nchunk2; ++np) {
-            const long items = (long)p.ntile2 * np;
-            const long waves = (items + 151) / 152;
-            const double eff = (double)items / (double)(waves * 152) - 0.005 * np;  // A rebuild per item
-            if (eff > beff + 1e-9) {
-                beff = eff;
-                best = np;
-            }
-        }
-        p.nparts2 = best;
-    }
-    p.cper2 = (p.nchunk2 + p.nparts2 - 1) / p.nparts2;
-    p.nparts2 = (p.nchunk2 + p.cper2 - 1) / p.cper2;
-    p.grid2 = std::min(152, p.ntile2 * p.nparts2);
-    p.nlist2 = ((p.ntile2 * p.nparts2 + p.grid2 - 1) / p.grid2) * p.cper2;
-    p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC, p.nlist2).total;
-    if (p.smem2 > 227 * 1024)
-        return set_err(&c, MDG_E_UNSUPPORTED, "work list too long for the tensor-core force pass");
     c.d_tc_atoms = (uint4*)dalloc(c, sizeof(uint4) * std::max(v.nmove, 1));
     c.d_tc_img = (unsigned char*)dalloc(c, (size_t)std::max(p.nchunk2, 1) * 2 * p.KS * kTile2);
     c.d_tc_cmax = (float*)dalloc(c, sizeof(float) * 4);
@@ -850,8 +717,7 @@ void recip_tc(Ctx& c) {
     const long total = (long)p.nchunk2 * p.KS * kNC2 * 8;
     k_tc_prep_c<<<(int)std::min<long>((total + 255) / 256, 152 * 8), 256, 0, c.stream>>>(c.d_tc_cf, ks.row, ks.row_nlen,
                                                                                          d, c.d_tc_img, c.d_tc_cmax);
-    k_tc_force<<<p.grid2, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, ks.row, d, c.d_tc_cmax, p.ntile2,
-                                                    p.nparts2, p.cper2, p.nlist2);
+    k_tc_force<<<(v.nmove + 127) / 128, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, ks.row, d, c.d_tc_cmax);
 }
 
 int umma_selftest(int n, int k, const float* a, const float* b, float* dout, std::string& err) {
