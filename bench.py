@@ -59,6 +59,9 @@ def make_workload(name):
         s, prm = configs.shake_water()
         desc = ("8192 SHAKE-constrained 3-site waters on rocksalt walls (19x19 cells, 11552 sites), "
                 "tol 1e-10")
+    elif name == "replicas64":
+        s, prm = configs.replica_slabs(n=64)[0]
+        desc = "first of the 64 uneven interfacial replicas (the CPU arm times one replica)"
     else:
         raise SystemExit(f"unknown config {name}")
     return s, prm, desc
@@ -155,7 +158,7 @@ def fp32_nominal_tflops():
     return 152 * 128 * 2 * mhz * 1e6 / 1e12
 
 
-def roofline(ctx, s, prm, precision, pk):
+def roofline(ctx, s, prm, precision, pk, config_name=""):
     """Roofline of the dominant force phase (and of the reciprocal phase), from CUDA-event phase
     times of mdg_phase_times and the algorithmic work per unit:
       pair phases   45 flops per accepted site pair (FP64 pipe, or FP32 + MUFU when mixed)
@@ -188,14 +191,17 @@ def roofline(ctx, s, prm, precision, pk):
                 bound, peak, src = "fp64", FP64_NOMINAL_TFLOPS, "nominal (no measured FP64 peak)"
         achieved = flops / max(t, 1e-12) / 1e12
         return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": traffic_tab.get(f"{kind}:{'mixed' if mixed else 'fp64'}"), "kernel": kind,
+                "traffic": traffic_tab.get(f"{kind}:{'mixed' if mixed else 'fp64'}:{config_name}"),
+                "traffic_unit": "DRAM bytes per launch (profiles/traffic.json, ncu)", "kernel": kind,
                 "ms_per_launch": ph[kind], "units_per_launch": int(units), "flops_per_unit": flops / max(units, 1),
                 "peak_source": src}
 
     dom = max(("pairs", "walls", "reciprocal"), key=lambda k: ph[k])
     out = one(dom)
     out["phase_ms"] = ph
-    return out, one("reciprocal")
+    pairs = one("pairs")
+    pairs["site_pairs_per_s"] = pairs["units_per_launch"] / max(ph["pairs"] * 1e-3, 1e-12)
+    return out, one("reciprocal"), pairs
 
 
 def ctx_nk(s, prm):
@@ -280,7 +286,7 @@ def gpu_arm(args):
     kps = ctx.kernels_per_step()
     ctx.get_state(s)
     pk = peaks()
-    roof, roof_recip = roofline(ctx, s, prm, precision, pk)
+    roof, roof_recip, roof_pairs = roofline(ctx, s, prm, precision, pk, args.config)
 
     # ---------------- learned SHAKE seed (workloads with SHAKE-constrained molecules): the same
     # start and step count with the seed network active; the headline value is then this run
@@ -340,6 +346,7 @@ def gpu_arm(args):
         "kernels_per_step": kps,
         "roofline": roof,
         "roofline_reciprocal": roof_recip,
+        "roofline_pairs": roof_pairs,
         "clocks": clk.summary(),
         "step_report": {k: rep[k] for k in ("tempnow", "htot", "uconf", "rebuilds", "steps")},
         "step_ms_min_median_max": [min(per_step), float(np.median(per_step)), max(per_step)],
@@ -357,6 +364,95 @@ def gpu_arm(args):
                                "sample": f"{n} MD steps of the same workload after one untimed step "
                                          f"({dt * 1e3:.2f} ms/step), OpenMP over all host cores"}
     return out
+
+
+def replicas_arm(args):
+    """Config 4: uneven interfacial replicas stepped together by one graph launch per batch step
+    (mdg_batch), timed with CUDA events on the batch stream; against the same replicas stepped one
+    after another with their own graphs."""
+    import torch
+
+    import md_sim_gb300
+    from md_sim_gb300 import abi, configs
+    from md_sim_gb300.abi import MDG_FP64, MDG_MIXED
+
+    lib = md_sim_gb300.load()
+    n = args.replicas
+    t0 = time.perf_counter()
+    systems = configs.replica_slabs(n=n)
+    t_build = time.perf_counter() - t0
+    precision = MDG_MIXED if args.precision == "mixed" else MDG_FP64
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    ctxs = []
+    t0 = time.perf_counter()
+    for s, prm in systems:
+        prm.precision = precision
+        c = abi.Context(lib, s, prm)
+        c.set_state(s)
+        ctxs.append(c)
+    t_create = time.perf_counter() - t0
+    batch = abi.Batch(lib, ctxs)
+    batch.set_stream(stream.cuda_stream)
+    batch.run(args.equil)                 # untimed: start-up transient and graph build
+    batch.run(args.warmup)
+    K = args.steps
+    with ClockSampler() as clk:
+        per_step = []
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for k in range(K):
+                flush.zero_()
+                ev[k][0].record(stream)
+                batch.run_async(1)
+                ev[k][1].record(stream)
+        stream.synchronize()
+        per_step = [a.elapsed_time(b) for a, b in ev]
+    for c in ctxs:
+        c.check()
+    t_batch = float(np.sum(per_step)) / K * 1e-3
+    # the same replicas one after another, each with its own graph, on the same stream
+    for c in ctxs:
+        c.set_stream(stream.cuda_stream)
+        c.run_async(1)
+    torch.cuda.synchronize()
+    Ks = max(5, K // 10)
+    a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        flush.zero_()
+        a_.record(stream)
+        for _ in range(Ks):
+            for c in ctxs:
+                c.run_async(1)
+        b_.record(stream)
+    stream.synchronize()
+    t_seq = a_.elapsed_time(b_) * 1e-3 / Ks
+    for c in ctxs:
+        c.check()
+    batch.close()
+    atoms = int(sum(s.ntota for s, _ in systems))
+    waters = int(sum(s.nrig for s, _ in systems))
+    dt = systems[0][0].dt
+    value = ns_per_day(t_batch, dt) * n
+    return {
+        "metric": METRIC + " (config 4: replica batch)", "value": value, "unit": "replica-ns/day",
+        "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": t_batch * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if precision == MDG_FP64 else "f32 pairs + f16x3 tensor reciprocal (f64 state)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"{n} interfacial replicas, waters U{{500..4000}} (total {waters}), walls 7-14+ cells, "
+                               f"{atoms} sites in all, one graph launch per batch step",
+                   "config": "replicas64", "precision": args.precision, "l2": "flushed (256 MB write) between timed steps"},
+        "per_replica_ns_per_day": ns_per_day(t_batch, dt),
+        "sequential": {"ms_per_step": t_seq * 1e3, "value": ns_per_day(t_seq, dt) * n, "unit": "replica-ns/day",
+                       "how": "each replica's own graph, one after another on one stream"},
+        "batch_speedup_vs_sequential": t_seq / t_batch,
+        "setup_s": {"build": t_build, "create": t_create},
+        "clocks": clk.summary(),
+        "step_ms_min_median_max": [min(per_step), float(np.median(per_step)), max(per_step)],
+    }
 
 
 def nve_drift(ctx, s, nsteps, every=100):
@@ -543,7 +639,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="slab2048", choices=["slab2048", "bulk256", "bulk32k", "shake8k"])
+    ap.add_argument("--config", default="slab2048", choices=["slab2048", "bulk256", "bulk32k", "shake8k", "replicas64"])
+    ap.add_argument("--replicas", type=int, default=64)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--fp64-steps", type=int, default=200,
                     help="steps of the plain FP64 GPU comparison arm (0 = skip)")
@@ -569,7 +666,7 @@ def main():
     if args.gpus > 1 or int(os.environ.get("WORLD_SIZE", "1")) > 1:
         # replicas only: every rank runs its own independent system; rank 0 reports its own
         pass
-    out = gpu_arm(args)
+    out = replicas_arm(args) if args.config == "replicas64" else gpu_arm(args)
     if rank == 0:
         print(json.dumps(out))
 

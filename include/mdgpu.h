@@ -256,6 +256,24 @@ int mdg_set_stream(mdg_ctx* ctx, void* stream);
 int mdg_phase_times(mdg_ctx* ctx, int reps, double* ms);
 
 /* ---------------------------------------------------------------------------------------------
+ * Replica batches (no reference counterpart; the reference runs one system per MPI job).
+ * Independent contexts in resident mode, stepped together by one CUDA graph whose per-replica
+ * step graphs are parallel branches, so that many small systems share the GPU in one launch.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct mdg_batch mdg_batch;
+/* ctxs: n contexts on one device, each after mdg_set_state; they stay owned by the caller and
+ * must outlive the batch. */
+int mdg_batch_create(mdg_ctx* const* ctxs, int n, mdg_batch** out);
+void mdg_batch_destroy(mdg_batch* b);
+const char* mdg_batch_last_error(const mdg_batch* b);
+int mdg_batch_set_stream(mdg_batch* b, void* stream);
+/* nsteps batch steps (every replica one MD step each), checked every 64 steps; a replica whose
+ * neighbour list overflows redoes its chunk alone with larger lists.  reps: n reports or NULL. */
+int mdg_batch_run(mdg_batch* b, int64_t nsteps, mdg_report* reps);
+/* nsteps graph launches on the batch stream, no checks (for timing; then mdg_check per context) */
+int mdg_batch_run_async(mdg_batch* b, int64_t nsteps);
+
+/* ---------------------------------------------------------------------------------------------
  * Learned SHAKE seed.  A small network (9 -> 64 -> 64 -> 3, SiLU) maps rotation-invariant features
  * of a 3-constraint molecule's unconstrained and previous bond vectors to the multipliers that
  * SHAKE accumulates for it; the prediction is applied as one SHAKE-type correction before the

@@ -179,6 +179,13 @@ class Lib:
             g("mlp_forward", C.c_int, [FP, FP, C.c_int64, FP])
             g("mlp_grad", C.c_int, [FP, FP, FP, C.c_int64, FP, FP])
             g("mlp_train", C.c_int, [FP, FP, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, FP, FP])
+        if self.has("batch_create"):
+            g("batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)])
+            g("batch_destroy", None, [C.c_void_p])
+            g("batch_last_error", C.c_char_p, [C.c_void_p])
+            g("batch_set_stream", C.c_int, [C.c_void_p, C.c_void_p])
+            g("batch_run", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p])
+            g("batch_run_async", C.c_int, [C.c_void_p, C.c_int64])
         if self.has("run"):
             g("set_state", C.c_int, [C.c_void_p, C.POINTER(Rigid), C.POINTER(State)])
             g("get_state", C.c_int, [C.c_void_p, C.POINTER(State)])
@@ -450,3 +457,42 @@ def _ctx_shake_samples(self) -> np.ndarray:
 Context.set_shake_model = _ctx_set_shake_model
 Context.shake_record = _ctx_shake_record
 Context.shake_samples = _ctx_shake_samples
+
+
+class Batch:
+    """Replica batch over resident contexts (mdg_batch_*): one graph launch steps all of them."""
+
+    def __init__(self, lib: Lib, ctxs):
+        self.lib, self.ctxs = lib, list(ctxs)
+        arr = (C.c_void_p * len(self.ctxs))(*[c.h.value if hasattr(c.h, "value") else c.h for c in self.ctxs])
+        h = C.c_void_p()
+        rc = lib.batch_create(arr, len(self.ctxs), C.byref(h))
+        if rc != MDG_OK:
+            raise MdgError(rc, (lib.batch_last_error(None) or b"").decode())
+        self.h = h
+
+    def _check(self, rc):
+        if rc != MDG_OK:
+            raise MdgError(rc, (self.lib.batch_last_error(self.h) or b"").decode())
+
+    def set_stream(self, stream_handle: int):
+        self._check(self.lib.batch_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    def run(self, nsteps: int):
+        reps = (Report * len(self.ctxs))()
+        self._check(self.lib.batch_run(self.h, int(nsteps), C.cast(reps, C.c_void_p)))
+        return [{f: getattr(r, f) for f, _ in Report._fields_} for r in reps]
+
+    def run_async(self, nsteps: int):
+        self._check(self.lib.batch_run_async(self.h, int(nsteps)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

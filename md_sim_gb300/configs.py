@@ -11,7 +11,7 @@ field file) and can be written out in the reference formats with system.write_fl
 from __future__ import annotations
 
 import math
-from typing import Optional, Tuple
+from typing import List, Optional, Tuple
 
 import numpy as np
 
@@ -154,6 +154,27 @@ def _rocksalt_walls(cells: int, a: float, lwh: float, layers: int = 4):
     return np.array(pos), np.array(typ, dtype=np.int64)
 
 
+def _lattice_waters(rng, nwat, L, zlo, zhi, jitter=0.2):
+    """nwat O positions on a random subset of a simple cubic lattice filling the film (x, y
+    periodic), jittered: O-O >= spacing - 2 jitter.  Vectorised stand-in for random sequential
+    placement when many systems are built."""
+    h = zhi - zlo
+    sp = (L * L * h / nwat) ** (1.0 / 3.0)
+    while True:
+        nx = max(1, int(L // sp))
+        nz = max(1, int(h // sp) + 1)
+        if nx * nx * nz >= nwat:
+            break
+        sp *= 0.98
+    g = np.stack(np.meshgrid(np.arange(nx), np.arange(nx), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    pick = rng.choice(len(g), size=nwat, replace=False)
+    dz = (h / max(nz - 1, 1)) if nz > 1 else 0.0
+    pos = np.stack([g[pick, 0] * (L / nx), g[pick, 1] * (L / nx), zlo + g[pick, 2] * dz], 1)
+    pos += rng.uniform(-jitter, jitter, size=pos.shape)
+    pos[:, 2] = np.clip(pos[:, 2], zlo, zhi)
+    return pos
+
+
 def _place_waters(rng, nwat, L, zlo, zhi, walls, dmin_oo=2.5, dmin_ow=2.2, max_tries=200000):
     """Random sequential placement of O positions with overlap rejection (cell hashed)."""
     cs = 2.5
@@ -202,7 +223,8 @@ def _place_waters(rng, nwat, L, zlo, zhi, walls, dmin_oo=2.5, dmin_ow=2.2, max_t
 
 def slab_water(nwat: int = 2048, cells: int = 10, a: float = 4.21, lz: Optional[float] = None,
                seed: int = 4, T: float = 300.0, rcut: float = 10.0, skin: float = 1.0,
-               alpha: float = 0.30, kmax: int = 10, nvt: bool = False) -> Tuple[S.System, RunParams]:
+               alpha: float = 0.30, kmax: int = 10, nvt: bool = False,
+               placement: str = "rsa") -> Tuple[S.System, RunParams]:
     """Rigid waters between two rocksalt walls (4 layers, q +-1.2, Buckingham wall-O).
     NVE by default (T sets the initial velocities); nvt=True selects the reference's thermostat."""
     L = cells * a
@@ -213,7 +235,10 @@ def slab_water(nwat: int = 2048, cells: int = 10, a: float = 4.21, lz: Optional[
     lz = lz if lz is not None else 2.0 * L
     wpos, wtyp = _rocksalt_walls(cells, a, lwh)
     rng = np.random.default_rng(seed)
-    com = _place_waters(rng, nwat, L, -lwh + 1.4, lwh - 1.4, wpos)
+    if placement == "lattice":
+        com = _lattice_waters(rng, nwat, L, -lwh + 2.2, lwh - 2.2)
+    else:
+        com = _place_waters(rng, nwat, L, -lwh + 1.4, lwh - 1.4, wpos)
     wat = _water_moltype("rigmol", nwat)
     crys = _crystal(len(wpos), a, lw)
     names = ["O", "H", "Mg", "Ox"]
@@ -233,6 +258,29 @@ def slab_water(nwat: int = 2048, cells: int = 10, a: float = 4.21, lz: Optional[
 
 
 # ----------------------------------------------------------------------------------------------
+def replica_slabs(n: int = 64, seed: int = 8, nmin: int = 500, nmax: int = 4000, cmin: int = 7, cmax: int = 14,
+                  a: float = 4.21) -> List[Tuple[S.System, RunParams]]:
+    """Uneven interfacial replicas: water counts ~U{nmin..nmax} and wall cells ~U{cmin..cmax}
+    (seeded), the slab-2048 walls and Buckingham parameters, alpha 0.30, rcut 10, kmax scaled to
+    the box (nint(10 Lx / 42.1)).  A replica whose water film would be thicker than 95 A gets the
+    smallest wider wall that brings it under (so that the z range of the reciprocal sum stays
+    within the tensor-core tiles); Lz = max(2 Lx, film + 35 A)."""
+    rng = np.random.default_rng(seed)
+    nws = rng.integers(nmin, nmax + 1, size=n)
+    cls = rng.integers(cmin, cmax + 1, size=n)
+    dens = 0.033427
+    out = []
+    for i, (nw, cells) in enumerate(zip(nws.tolist(), cls.tolist())):
+        while nw / ((cells * a) ** 2 * dens) > 95.0:
+            cells += 1
+        L = cells * a
+        thick = nw / (L * L * dens)
+        lz = max(2.0 * L, thick + 35.0)
+        kmax = int(round(10.0 * L / 42.1))
+        out.append(slab_water(nwat=nw, cells=cells, a=a, lz=lz, seed=seed * 1000 + i, kmax=kmax, placement="lattice"))
+    return out
+
+
 def shake_water(nwat: int = 8192, cells: int = 19, a: float = 4.21, seed: int = 9, T: float = 300.0,
                 rcut: float = 10.0, skin: float = 1.0, alpha: float = 0.30,
                 kmax: Optional[int] = None, tol2: float = 1e-10, maxit: int = 100,

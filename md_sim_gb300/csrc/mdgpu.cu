@@ -919,6 +919,16 @@ int mdg_get_state(mdg_ctx* cp, mdg_state* st) {
     return MDG_OK;
 }
 
+// One resident step captured as a graph (not instantiated); the caller owns *out.
+static int capture_step_graph(Ctx& c, cudaGraph_t* out) {
+    MDG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = step_launch(c);
+    const cudaError_t e = cudaStreamEndCapture(c.stream, out);
+    if (rc) return rc;
+    if (e != cudaSuccess) return set_err(&c, MDG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    return MDG_OK;
+}
+
 static int ensure_graph(Ctx& c, int nstep) {
     if (c.graph_exec) return MDG_OK;
     cudaGraph_t g;
@@ -1200,6 +1210,158 @@ int mdg_mlp_train(const float* x, const float* y, int64_t n, int epochs, int bat
     const int rc = mlp_train_host(x, y, n, epochs, batch, lr, seed, w_out, loss_out, err);
     if (rc) g_err = err;
     return rc;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Replica batches: independent contexts stepped by one graph launch (their per-step graphs are
+// parallel child graphs of one graph, so the kernels of small systems fill the GPU together).
+// ---------------------------------------------------------------------------------------------
+struct mdg_batch {
+    std::vector<mdg_ctx*> ctx;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int device = 0;
+    std::string err;
+};
+
+static int batch_err(mdg_batch* b, int code, const std::string& m) {
+    if (b) b->err = m;
+    g_err = m;
+    return code;
+}
+
+static int batch_graph(mdg_batch* b) {
+    if (b->exec) return MDG_OK;
+    cudaGraph_t g;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return batch_err(b, MDG_E_CUDA, "cudaGraphCreate failed");
+    for (size_t i = 0; i < b->ctx.size(); ++i) {
+        Ctx& c = *b->ctx[i];
+        cudaGraph_t child;
+        int rc = capture_step_graph(c, &child);
+        if (rc) {
+            cudaGraphDestroy(g);
+            return batch_err(b, rc, "replica " + std::to_string(i) + ": " + c.err);
+        }
+        cudaGraphNode_t node;
+        const cudaError_t e = cudaGraphAddChildGraphNode(&node, g, nullptr, 0, child);
+        cudaGraphDestroy(child);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return batch_err(b, MDG_E_CUDA, std::string("child graph: ") + cudaGetErrorString(e));
+        }
+    }
+    const cudaError_t e = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return batch_err(b, MDG_E_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
+    return MDG_OK;
+}
+
+int mdg_batch_create(mdg_ctx* const* ctxs, int n, mdg_batch** out) {
+    if (!ctxs || n < 1 || !out) return batch_err(nullptr, MDG_E_ARG, "mdg_batch_create: bad argument");
+    auto* b = new mdg_batch();
+    b->device = ctxs[0]->device;
+    for (int i = 0; i < n; ++i) {
+        if (!ctxs[i] || !ctxs[i]->resident || ctxs[i]->device != b->device) {
+            delete b;
+            return batch_err(nullptr, MDG_E_ARG, "mdg_batch_create: every context needs mdg_set_state, one device");
+        }
+        b->ctx.push_back(ctxs[i]);
+    }
+    cudaSetDevice(b->device);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        return batch_err(nullptr, MDG_E_CUDA, "mdg_batch_create: stream");
+    }
+    *out = b;
+    return MDG_OK;
+}
+
+void mdg_batch_destroy(mdg_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char* mdg_batch_last_error(const mdg_batch* b) { return b ? b->err.c_str() : g_err.c_str(); }
+
+int mdg_batch_set_stream(mdg_batch* b, void* stream) {
+    if (!b) return batch_err(nullptr, MDG_E_ARG, "null batch");
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    b->stream = stream ? (cudaStream_t)stream : b->stream;
+    return MDG_OK;
+}
+
+int mdg_batch_run_async(mdg_batch* b, int64_t nsteps) {
+    if (!b) return batch_err(nullptr, MDG_E_ARG, "null batch");
+    cudaSetDevice(b->device);
+    int rc = batch_graph(b);
+    if (rc) return rc;
+    for (int64_t k = 0; k < nsteps; ++k)
+        if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess) return batch_err(b, MDG_E_CUDA, "batch graph launch");
+    return MDG_OK;
+}
+
+// Steps every replica nsteps times.  Status is checked every 64 steps; a replica whose neighbour
+// list overflowed in a chunk is rolled back and redoes that chunk alone with larger lists
+// (mdg_run), after which the batch graph is rebuilt.  reps: n reports or NULL.
+int mdg_batch_run(mdg_batch* b, int64_t nsteps, mdg_report* reps) {
+    if (!b) return batch_err(nullptr, MDG_E_ARG, "null batch");
+    cudaSetDevice(b->device);
+    const int64_t kChunk = 64;
+    int64_t done = 0;
+    while (done < nsteps) {
+        const int64_t chunk = std::min<int64_t>(kChunk, nsteps - done);
+        for (auto* cp : b->ctx) {
+            snapshot(*cp, false);
+            cudaMemsetAsync(cp->v.status, 0, sizeof(int) * 4, cp->stream);
+        }
+        for (auto* cp : b->ctx) cudaStreamSynchronize(cp->stream);
+        int rc = mdg_batch_run_async(b, chunk);
+        if (rc) return rc;
+        if (cudaStreamSynchronize(b->stream) != cudaSuccess) return batch_err(b, MDG_E_CUDA, "batch step failed");
+        bool rebuild = false;
+        for (size_t i = 0; i < b->ctx.size(); ++i) {
+            Ctx& c = *b->ctx[i];
+            rc = read_status(c);
+            if (rc) return batch_err(b, rc, "replica " + std::to_string(i) + ": " + c.err);
+            const int ovf = c.h_status[ST_LIST_OVF], wovf = c.h_status[ST_WLIST_OVF];
+            if (ovf || wovf) {
+                rc = alloc_lists(c, ovf ? ovf + ovf / 4 + 32 : c.v.maxnb, wovf ? wovf + wovf / 4 + 32 : c.v.maxwnb);
+                if (rc) return batch_err(b, rc, "replica " + std::to_string(i) + ": " + c.err);
+                snapshot(c, true);
+                const int one = 1;
+                cudaMemcpyAsync(c.v.status + ST_FORCE_RB, &one, sizeof(int), cudaMemcpyHostToDevice, c.stream);
+                cudaStreamSynchronize(c.stream);
+                rc = mdg_run(b->ctx[i], chunk, nullptr);
+                if (rc) return batch_err(b, rc, "replica " + std::to_string(i) + ": " + c.err);
+                rebuild = true;
+                continue;
+            }
+            if (c.h_status[ST_SHAKE_RPTOL])
+                return batch_err(b, MDG_E_SHAKE_RPTOL, "replica " + std::to_string(i) + ": Constraint failure");
+            if (c.h_status[ST_SHAKE_MAXIT])
+                return batch_err(b, MDG_E_SHAKE_MAXIT, "replica " + std::to_string(i) + ": shake(): Too many constraint iterations!");
+        }
+        if (rebuild && b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+        done += chunk;
+    }
+    if (reps) {
+        for (size_t i = 0; i < b->ctx.size(); ++i) {
+            Ctx& c = *b->ctx[i];
+            double th[TH_N];
+            if (cudaMemcpy(th, c.d_thermo, sizeof(th), cudaMemcpyDeviceToHost) != cudaSuccess)
+                return batch_err(b, MDG_E_CUDA, "batch report");
+            fill_report(c, th, &reps[i]);
+        }
+    }
+    return MDG_OK;
 }
 
 }  // extern "C"

@@ -229,7 +229,7 @@ int mlp_grad_host(const float* w, const float* X, const float* Y, int64_t n, flo
     cudaMemcpy(di, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
     cudaMemset(dg, 0, sizeof(float) * NPARAM);
     cudaMemset(dl, 0, sizeof(float));
-    if (cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem)) != cudaSuccess)
+    if (allow_max_smem(k_mlp_grad) != cudaSuccess)
         return err = "mlp: attribute", MDG_E_CUDA;
     k_mlp_round<<<20, 256>>>(dw, dwr, NW);
     k_mlp_grad<<<(int)((n + kB - 1) / kB), kB, sizeof(GradSmem)>>>(dwr, dx, dy, di, 0, (int)n, 1.0f / (float)n, dg, dl);
@@ -273,7 +273,7 @@ int mlp_train_host(const float* X, const float* Y, int64_t n, int epochs, int ba
     cudaMemset(dm, 0, sizeof(float) * NPARAM);
     cudaMemset(dv, 0, sizeof(float) * NPARAM);
     cudaMemset(dg, 0, sizeof(float) * NPARAM);
-    if (cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem)) != cudaSuccess)
+    if (allow_max_smem(k_mlp_grad) != cudaSuccess)
         return err = "mlp_train: attribute", MDG_E_CUDA;
     std::vector<int> idx(n);
     for (int64_t k = 0; k < n; ++k) idx[k] = (int)k;

@@ -147,6 +147,32 @@ __device__ __forceinline__ float fmin_img(float d, float l, float li, int period
     return periodic ? d - l * rintf(d * li) : d;
 }
 
+// Kept partners of one warp, staged in shared memory and written out in whole 128-byte lines
+// (appending a few entries per ballot straight to global memory wrote partial lines).
+constexpr int kStage = 128;
+
+struct WarpOut {
+    int* buf;  // kStage entries of shared memory
+    int nbuf = 0, flushed = 0;
+    __device__ __forceinline__ void flush(int* out, int cap, int lane) {
+        for (int k = lane; k < nbuf; k += 32) {
+            const int pos = flushed + k;
+            if (pos < cap) out[pos] = buf[k];
+        }
+        flushed += nbuf;
+        nbuf = 0;
+        __syncwarp();
+    }
+    __device__ __forceinline__ void push(bool keep, int ja, unsigned m, int* out, int cap, int lane) {
+        const int np = __popc(m);
+        if (nbuf + np > kStage) flush(out, cap, lane);
+        if (keep) buf[nbuf + __popc(m & ((1u << lane) - 1u))] = ja;
+        nbuf += np;
+        __syncwarp();
+    }
+    __device__ __forceinline__ int total() const { return flushed + nbuf; }
+};
+
 // One warp per head: the warp walks the neighbouring cells, lanes test 32 candidates at a time
 // and the kept partners (j > i) are appended in order with a ballot.
 __global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* cpos, const double4* hpos) {
@@ -167,7 +193,9 @@ __global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* 
     const float lim_lo = (float)v.rskinsq * 0.9999f - 0.05f;
     const int cx = cell_coord(pw.x, 0, g), cy = cell_coord(pw.y, 1, g), cz = cell_coord(pw.z, 2, g);
     const bool surf_i = ia >= v.nliqa;
-    int cnt = 0;
+    __shared__ int stage[4][kStage];
+    WarpOut wo;
+    wo.buf = stage[(threadIdx.x >> 5) & 3];
     int* out = v.nb + (size_t)h * v.maxnb;
     const int rz = g.nc[2] >= 3 ? 1 : 0, ry = g.nc[1] >= 3 ? 1 : 0, rx = g.nc[0] >= 3 ? 1 : 0;
     for (int dz = -rz; dz <= rz; ++dz) {
@@ -198,13 +226,13 @@ __global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* 
                         }
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, keep);
-                    const int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                    if (keep && pos < v.maxnb) out[pos] = ja;
-                    cnt += __popc(m);
+                    wo.push(keep, ja, m, out, v.maxnb, lane);
                 }
             }
         }
     }
+    wo.flush(out, v.maxnb, lane);
+    const int cnt = wo.total();
     if (lane == 0) {
         if (cnt > v.maxnb) atomicMax(&v.status[ST_LIST_OVF], cnt);
         v.nbcnt[h] = min(cnt, v.maxnb);
@@ -228,7 +256,9 @@ __global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4*
     const double wz = wrap(zi, v.lz, g.periodic[2]);
     const int cx = cell_coord(pw.x, 0, g), cy = cell_coord(pw.y, 1, g), cz = cell_coord(wz, 2, g);
     const bool surf_i = ia >= v.nliqa;
-    int cnt = 0;
+    __shared__ int stage[4][kStage];
+    WarpOut wo;
+    wo.buf = stage[(threadIdx.x >> 5) & 3];
     int* out = v.wnb + (size_t)h * v.maxwnb;
     const int rz = g.nc[2] >= 3 ? 1 : 0, ry = g.nc[1] >= 3 ? 1 : 0, rx = g.nc[0] >= 3 ? 1 : 0;
     for (int dz = -rz; dz <= rz; ++dz) {
@@ -257,13 +287,13 @@ __global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4*
                         if (keep && d2 >= lim_lo) keep = keep_pair(v, xi, yi, zi, v.x[ja], v.y[ja], v.z[ja]);
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, keep);
-                    const int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                    if (keep && pos < v.maxwnb) out[pos] = ja;
-                    cnt += __popc(m);
+                    wo.push(keep, ja, m, out, v.maxwnb, lane);
                 }
             }
         }
     }
+    wo.flush(out, v.maxwnb, lane);
+    const int cnt = wo.total();
     if (lane == 0) {
         if (cnt > v.maxwnb) atomicMax(&v.status[ST_WLIST_OVF], cnt);
         v.wnbcnt[h] = min(cnt, v.maxwnb);

@@ -28,6 +28,7 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kNT = kWarps * 32;
+constexpr int kWSeg = 64;  // wall partners per work item of the head-wall loop
 constexpr float kPf = (float)kP, kA1f = (float)kA1, kA2f = (float)kA2, kA3f = (float)kA3, kA4f = (float)kA4,
                 kA5f = (float)kA5;
 
@@ -295,7 +296,14 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
     const float alfa = (float)v.alfa, spii = (float)v.spii, facq = (float)v.facq, rcutsq = (float)v.rcutsq;
     EAcc e;
     Kahan ws[6];
-    for (int h = warp; h < v.nheads; h += nwarps) {
+    // work items: (head, segment of kWSeg wall partners), so that the few heads next to a wall
+    // with hundreds of partners are shared by several warps
+    const int nseg = (v.maxwnb + kWSeg - 1) / kWSeg;
+    const long nitems = (long)v.nheads * nseg;
+    for (long item = warp; item < nitems; item += nwarps) {
+        const int h = (int)(item / nseg), seg = (int)(item % nseg);
+        const int n = min(v.wnbcnt[h], (seg + 1) * kWSeg);
+        if (seg * kWSeg >= n) continue;
         const int i = v.head_atom[h];
         const uint4 pi = pk.P[i];
         const int it = (int)(pi.w & 0x7fffffffu);
@@ -306,9 +314,8 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) si[a] = a < nsi_i ? pk.Q[i + a] : make_float4(0.f, 0.f, 0.f, 0.f);
         Kahan fix[3], fiy[3], fiz[3];
-        const int n = v.wnbcnt[h];
         const int* nb = v.wnb + (size_t)h * v.maxwnb;
-        for (int k = lane; k < n; k += 32) {
+        for (int k = seg * kWSeg + lane; k < n; k += 32) {
             const int j = nb[k];
             const uint4 pj = pk.P[j];
             float xi, yi, zi;

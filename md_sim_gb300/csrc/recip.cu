@@ -327,8 +327,8 @@ int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const 
     ks.splits = splits;
     ks.sfac_smem = ks.tile * ((KL + 1 + KM + 1 + KN + 1) * (int)sizeof(double2) + (int)sizeof(double));
     ks.force_smem = kForceNT * (KM + 1 + KN + 1) * (int)sizeof(double2);
-    MDG_CUDA(cudaFuncSetAttribute(k_sfac, cudaFuncAttributeMaxDynamicSharedMemorySize, ks.sfac_smem));
-    MDG_CUDA(cudaFuncSetAttribute(k_kforce, cudaFuncAttributeMaxDynamicSharedMemorySize, ks.force_smem));
+    MDG_CUDA(allow_max_smem(k_sfac));
+    MDG_CUDA(allow_max_smem(k_kforce));
     if (ks.force_smem > 200 * 1024 || ks.sfac_smem > 200 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "kmax too large for the shared-memory phase tables");
     return MDG_OK;
@@ -482,8 +482,8 @@ int recip_forces_noalloc(const double* x, const double* y, const double* z, cons
     if (smem1 > 200 * 1024 || smem2 > 200 * 1024)
         return na_fail(MDG_E_UNSUPPORTED, "mdg_recip_forces_noalloc: kmax too large for the phase tables");
     auto ck = [](cudaError_t e) { return e == cudaSuccess; };
-    if (!ck(cudaFuncSetAttribute(k_sfac, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1)) ||
-        !ck(cudaFuncSetAttribute(k_kforce, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2)))
+    if (!ck(allow_max_smem(k_sfac)) ||
+        !ck(allow_max_smem(k_kforce)))
         return na_fail(MDG_E_CUDA, "mdg_recip_forces_noalloc: cudaFuncSetAttribute failed");
     double2* S = reinterpret_cast<double2*>(base + kNaS);
     double2* C = reinterpret_cast<double2*>(base + kNaC);

@@ -690,9 +690,9 @@ int recip_tc_setup(Ctx& c) {
     c.d_tc_part = (float*)dalloc(c, sizeof(float) * (size_t)p.nsplit1 * p.NP * p.rtot);
     c.d_tc_cf = (float2*)dalloc(c, sizeof(float2) * std::max(ks.nk, 1));
     if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
-    MDG_CUDA(cudaFuncSetAttribute(k_tc_sfac<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem1));
-    MDG_CUDA(cudaFuncSetAttribute(k_tc_sfac<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem1));
-    MDG_CUDA(cudaFuncSetAttribute(k_tc_force, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem2));
+    MDG_CUDA(allow_max_smem(k_tc_sfac<4>));
+    MDG_CUDA(allow_max_smem(k_tc_sfac<2>));
+    MDG_CUDA(allow_max_smem(k_tc_force));
     p.ready = true;
     return MDG_OK;
 }
@@ -742,7 +742,7 @@ int umma_selftest(int n, int k, const float* a, const float* b, float* dout, std
     cudaMemcpy(db, b, sizeof(float) * n * k, cudaMemcpyHostToDevice);
     cudaMemset(de, 0, sizeof(int));
     const int smem = 1024 + 4096 + 256 * 32;
-    if (cudaFuncSetAttribute(k_umma_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (allow_max_smem(k_umma_selftest) != cudaSuccess)
         return fin(MDG_E_CUDA, "selftest: attribute");
     k_umma_selftest<<<1, 128, smem>>>(da, db, dd, n, k, de);
     if (cudaDeviceSynchronize() != cudaSuccess) return fin(MDG_E_CUDA, "selftest: kernel failed");
