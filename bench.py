@@ -276,6 +276,7 @@ def gpu_arm(args):
     configs.equilibrate(ctx, s, steps=args.equil, every=20)
     s_start = s.copy()
     ctx.set_state(s)
+    tuning = ctx.autotune(5) if args.autotune else None
     ctx.run(args.warmup)
     K = args.steps
     with ClockSampler() as clk:
@@ -343,6 +344,7 @@ def gpu_arm(args):
                    "ensemble": "NVE" if s.temper == -1.0 else f"NVT {s.temper} K"},
         "e2e": e2e,
         "gpu_launches": int(kps * K),
+        "tuning": tuning,
         "kernels_per_step": kps,
         "roofline": roof,
         "roofline_reciprocal": roof_recip,
@@ -393,6 +395,9 @@ def replicas_arm(args):
         c.set_state(s)
         ctxs.append(c)
     t_create = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tunings = [c.autotune(3) for c in ctxs] if args.autotune else []
+    t_tune = time.perf_counter() - t0
     batch = abi.Batch(lib, ctxs)
     batch.set_stream(stream.cuda_stream)
     batch.run(args.equil)                 # untimed: start-up transient and graph build
@@ -449,10 +454,24 @@ def replicas_arm(args):
         "sequential": {"ms_per_step": t_seq * 1e3, "value": ns_per_day(t_seq, dt) * n, "unit": "replica-ns/day",
                        "how": "each replica's own graph, one after another on one stream"},
         "batch_speedup_vs_sequential": t_seq / t_batch,
-        "setup_s": {"build": t_build, "create": t_create},
+        "setup_s": {"build": t_build, "create": t_create, "autotune": t_tune},
+        "tuning": _tuning_summary(tunings),
         "clocks": clk.summary(),
         "step_ms_min_median_max": [min(per_step), float(np.median(per_step)), max(per_step)],
     }
+
+
+def _tuning_summary(tunings):
+    """Per-replica autotuner choices folded into counts, with the summed force time before/after."""
+    if not tunings:
+        return None
+    keys = ("pair_blocks", "tc_rows_per_cta", "tc_atom_splits")
+    choice = {}
+    for t in tunings:
+        k = ",".join(f"{x}={t[x]}" for x in keys)
+        choice[k] = choice.get(k, 0) + 1
+    return {"choices": choice, "force_ms_sum_before": float(sum(t["ms_before"] for t in tunings)),
+            "force_ms_sum_after": float(sum(t["ms_after"] for t in tunings))}
 
 
 def nve_drift(ctx, s, nsteps, every=100):
@@ -555,6 +574,8 @@ def e2e_arm(lib, s, prm, args, torch):
     if s.nrig:
         s0.c[0] = np.stack([traj[0]["cx"], traj[0]["cy"], traj[0]["cz"]])
     dctx = abi.Context(lib, s0, prm)
+    if args.autotune:
+        dctx.autotune(3)
     nflex = nm - s.nriga
     outs = [pinned(max(nflex, 1)) for _ in range(3)] + [pinned(nrig) for _ in range(6)]
     elj, eqq = pinned(s.nijt), pinned(s.nijt)
@@ -648,6 +669,8 @@ def main():
     ap.add_argument("--drift", type=int, default=0, help="NVE energy drift over this many extra resident steps")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned SHAKE seed arm (workloads with SHAKE only)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default launch parameters instead of timing candidates (mdg_autotune)")
     ap.add_argument("--e2e-steps", type=int, default=60)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")

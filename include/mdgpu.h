@@ -256,6 +256,19 @@ int mdg_set_stream(mdg_ctx* ctx, void* stream);
 int mdg_phase_times(mdg_ctx* ctx, int reps, double* ms);
 
 /* ---------------------------------------------------------------------------------------------
+ * Autotuner (no reference counterpart): times whole force evaluations of the context's current
+ * configuration for candidate launch parameters (real-space grid size; structure-factor row
+ * tiles per CTA and atom splits) and keeps the fastest.  reps evaluations per candidate.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct mdg_tuning {
+    int32_t pair_blocks;      /* real-space blocks (0: one warp per head) */
+    int32_t tc_rows_per_cta;  /* structure-factor (l, m) rows per CTA (mixed precision) */
+    int32_t tc_atom_splits;   /* structure-factor atom chunks */
+    float ms_before, ms_after;
+} mdg_tuning;
+int mdg_autotune(mdg_ctx* ctx, int32_t reps, mdg_tuning* out);
+
+/* ---------------------------------------------------------------------------------------------
  * Replica batches (no reference counterpart; the reference runs one system per MPI job).
  * Independent contexts in resident mode, stepped together by one CUDA graph whose per-replica
  * step graphs are parallel branches, so that many small systems share the GPU in one launch.

@@ -179,6 +179,8 @@ class Lib:
             g("mlp_forward", C.c_int, [FP, FP, C.c_int64, FP])
             g("mlp_grad", C.c_int, [FP, FP, FP, C.c_int64, FP, FP])
             g("mlp_train", C.c_int, [FP, FP, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, FP, FP])
+        if self.has("autotune"):
+            g("autotune", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p])
         if self.has("batch_create"):
             g("batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)])
             g("batch_destroy", None, [C.c_void_p])
@@ -496,3 +498,19 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Tuning(C.Structure):
+    _fields_ = [("pair_blocks", C.c_int32), ("tc_rows_per_cta", C.c_int32), ("tc_atom_splits", C.c_int32),
+                ("ms_before", C.c_float), ("ms_after", C.c_float)]
+
+
+def _ctx_autotune(self, reps: int = 5) -> Dict[str, float]:
+    """mdg_autotune: pick launch parameters for this system; returns the choice and the force
+    evaluation time before and after (ms)."""
+    t = Tuning()
+    self._check(self.lib.autotune(self.h, int(reps), C.byref(t)))
+    return {f: getattr(t, f) for f, _ in Tuning._fields_}
+
+
+Context.autotune = _ctx_autotune

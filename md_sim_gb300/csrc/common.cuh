@@ -54,10 +54,18 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// Block-wide sum into *dst with one atomic per block; all threads must call.
+// Block-wide sum into *dst with one atomic per block; all threads must call.  Blocks smaller than
+// a warp (used to spread FP64-heavy per-molecule work over more SMs) reduce within their lanes.
 template <int NT>
 __device__ __forceinline__ void block_atomic_sum(double v, double* dst) {
-    __shared__ double red[NT / 32];
+    if constexpr (NT < 32) {
+        constexpr unsigned mask = (1u << NT) - 1u;
+#pragma unroll
+        for (int o = NT / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+        if (threadIdx.x == 0) atomicAdd(dst, v);
+        return;
+    }
+    __shared__ double red[NT >= 32 ? NT / 32 : 1];
     v = warp_sum(v);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();

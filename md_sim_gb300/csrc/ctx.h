@@ -121,7 +121,7 @@ struct TcPlan {
     bool ready = false;
     int KN = 0, NN = 0, NP = 0, KS = 0, KM = 0, NM = 0;
     int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, grid1x = 0, rtot = 0, tpc1 = 0, smem1 = 0, smem2 = 0;
-    int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0, nlist2 = 0;
+    int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0, nlist2 = 0, mult1 = 2;
 };
 
 struct Ctx {
@@ -167,6 +167,7 @@ struct Ctx {
     float* d_mlpw = nullptr;      // SHAKE-seeding network parameters
     float* d_shake_rec = nullptr; // ncons x 12 recorded features / multipliers
     bool shake_model = false, shake_record = false;
+    int pair_blocks = 0;          // blocks of the real-space loops (0: by head count); autotuned
     int64_t nfreed = 0;
     // angles
     int nang_terms = 0;
@@ -216,6 +217,7 @@ const char* recip_noalloc_error();
 void recip_energy_launch(Ctx& c);
 // recip_tc.cu
 int recip_tc_setup(Ctx& c);
+int tc_plan_pass1(Ctx& c, int tpc, int mult);
 void recip_tc(Ctx& c);
 int umma_selftest(int n, int k, const float* a, const float* b, float* d, std::string& err);
 // mlp.cu

@@ -19,7 +19,7 @@ namespace mdg {
 
 namespace {
 
-constexpr int kNT = 32;
+constexpr int kNT = 16;
 
 constexpr double Gf01 = F32D(0.348611111), Gf11 = 1.0, Gf21 = F32D(0.916666667), Gf31 = F32D(0.333333333),
                  Gf41 = F32D(0.041666667);

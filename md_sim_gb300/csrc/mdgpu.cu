@@ -1364,4 +1364,75 @@ int mdg_batch_run(mdg_batch* b, int64_t nsteps, mdg_report* reps) {
     return MDG_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Autotuner: launch parameters of the force phases timed on this context's own system
+// ---------------------------------------------------------------------------------------------
+static float time_force(Ctx& c, int reps) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    launch_force(c, false, true);
+    cudaEventRecord(a, c.stream);
+    for (int r = 0; r < reps; ++r) launch_force(c, false, true);
+    cudaEventRecord(b, c.stream);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms / std::max(reps, 1);
+}
+
+int mdg_autotune(mdg_ctx* cp, int32_t reps, mdg_tuning* out) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    reps = std::max(reps, 1);
+    const float t0 = time_force(c, reps);
+    // real-space grid (blocks of 8 warps; 0 = one warp per head up to 16 blocks per SM)
+    int best_pb = c.pair_blocks;
+    float best = t0;
+    for (int pb : {0, 152 * 2, 152 * 4, 152 * 8}) {
+        c.pair_blocks = pb;
+        const float t = time_force(c, reps);
+        if (t < best) {
+            best = t;
+            best_pb = pb;
+        }
+    }
+    c.pair_blocks = best_pb;
+    // structure-factor split: row tiles per CTA x atom splits
+    int best_tpc = c.tcp.tpc1, best_mult = c.tcp.mult1;
+    if (c.precision == MDG_MIXED && c.tcp.ready) {
+        best = time_force(c, reps);
+        for (int tpc : {4, 2})
+            for (int m : {1, 2, 4}) {
+                if (tc_plan_pass1(c, tpc, m)) continue;
+                const float t = time_force(c, reps);
+                if (t < best) {
+                    best = t;
+                    best_tpc = tpc;
+                    best_mult = m;
+                }
+            }
+        tc_plan_pass1(c, best_tpc, best_mult);
+    }
+    if (c.graph_exec) {
+        cudaGraphExecDestroy(c.graph_exec);
+        c.graph_exec = nullptr;
+    }
+    const float t1 = time_force(c, reps);
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    int rc = read_status(c);
+    if (rc) return rc;
+    if (out) {
+        out->pair_blocks = best_pb;
+        out->tc_rows_per_cta = 128 * best_tpc;
+        out->tc_atom_splits = c.tcp.nsplit1;
+        out->ms_before = t0;
+        out->ms_after = t1;
+    }
+    return MDG_OK;
+}
+
 }  // extern "C"

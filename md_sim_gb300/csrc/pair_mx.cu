@@ -382,7 +382,10 @@ __global__ void k_merge_f(View v, Pk pk) {
     }
 }
 
-int blocks(int nheads) { return std::max(1, std::min((nheads + kWarps - 1) / kWarps, 152 * 16)); }
+int blocks(const Ctx& c, int nheads) {
+    const int b = std::max(1, std::min((nheads + kWarps - 1) / kWarps, 152 * 16));
+    return c.pair_blocks > 0 ? std::min(b, c.pair_blocks) : b;
+}
 
 size_t table_smem(const View& v, int nextra) {
     return sizeof(double) * (2 * v.nijt + nextra) + sizeof(float) * 6 * v.nijt + sizeof(int) * (v.nit * v.nit + v.nit);
@@ -408,8 +411,8 @@ void real_space_mixed(Ctx& c) {
     if (v.ntota == 0) return;
     k_pack<<<std::min((v.ntota + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
     if (v.nheads > 0) {
-        if (c.pk.zper) k_pair_mx<1><<<blocks(v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
-        else k_pair_mx<0><<<blocks(v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
+        if (c.pk.zper) k_pair_mx<1><<<blocks(c, v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
+        else k_pair_mx<0><<<blocks(c, v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
         k_merge_f<<<std::min((v.nmove + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
     }
 }
@@ -417,8 +420,8 @@ void real_space_mixed(Ctx& c) {
 void wall_forces_mixed(Ctx& c) {
     const View& v = c.v;
     if (v.nheads == 0 || v.nwall == 0) return;
-    if (c.pk.zper) k_wall_mx<1><<<blocks(v.nheads), kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
-    else k_wall_mx<0><<<blocks(v.nheads), kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
+    if (c.pk.zper) k_wall_mx<1><<<blocks(c, v.nheads), kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
+    else k_wall_mx<0><<<blocks(c, v.nheads), kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
     k_merge_f<<<std::min((v.nmove + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
 }
 

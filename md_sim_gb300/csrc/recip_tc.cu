@@ -655,6 +655,29 @@ __global__ void __launch_bounds__(128, 1) k_umma_selftest(const float* A, const 
 
 }  // namespace
 
+// Pass-1 launch plan: tpc row tiles per CTA (2 or 4) and mult x (152 / row-tile groups) atom
+// splits (mult 2 is the default; the autotuner tries the others).  Returns nonzero when the
+// combination does not fit (TMEM columns or table capacity).
+int tc_plan_pass1(Ctx& c, int tpc, int mult) {
+    View& v = c.v;
+    KSet& ks = c.ks;
+    TcPlan& p = c.tcp;
+    if (tpc == 4 && p.NP > 128) return 1;
+    if (kGA * p.NM > kMaxItems * 128 * tpc || kGA * (kMaxNL - 1) > kMaxItems * 128 * tpc ||
+        p.NN * (kGA / 2) > kMaxItems * 128 * tpc)
+        return 1;
+    p.tpc1 = tpc;
+    p.ncols1 = tpc * (p.NP <= 128 ? 128 : 256);
+    p.grid1x = (ks.nrow + tpc * 128 - 1) / (tpc * 128);
+    p.rtot = p.grid1x * tpc * 128;
+    p.nsplit1 = std::max(1, std::min(std::max(1, 76 * mult / p.grid1x), (v.nmove + 127) / 128));
+    p.chunk1 = (v.nmove + p.nsplit1 - 1) / p.nsplit1;
+    p.chunk1 = std::max(kGA, (p.chunk1 + kGA - 1) / kGA * kGA);
+    p.nsplit1 = std::max(1, (v.nmove + p.chunk1 - 1) / p.chunk1);
+    p.mult1 = mult;
+    return 0;
+}
+
 int recip_tc_setup(Ctx& c) {
     View& v = c.v;
     KSet& ks = c.ks;
@@ -667,27 +690,23 @@ int recip_tc_setup(Ctx& c) {
     p.NM = 2 * ks.kmmax + 1;
     if (p.NP > 256) return set_err(&c, MDG_E_UNSUPPORTED, "knmax too large for the tensor-core reciprocal sum");
     if (ks.klmax + 1 > kMaxNL - 1) return set_err(&c, MDG_E_UNSUPPORTED, "klmax too large for the tensor-core reciprocal sum");
-    p.tpc1 = p.NP <= 128 ? 4 : 2;
-    p.ncols1 = p.tpc1 * (p.NP <= 128 ? 128 : 256);
-    p.grid1x = (ks.nrow + p.tpc1 * 128 - 1) / (p.tpc1 * 128);
-    p.rtot = p.grid1x * p.tpc1 * 128;
-    p.nsplit1 = std::max(1, std::min(152 / p.grid1x, (v.nmove + 127) / 128));
-    p.chunk1 = (v.nmove + p.nsplit1 - 1) / p.nsplit1;
-    p.chunk1 = std::max(kGA, (p.chunk1 + kGA - 1) / kGA * kGA);
-    p.nsplit1 = std::max(1, (v.nmove + p.chunk1 - 1) / p.chunk1);
-    if (kGA * p.NM > kMaxItems * 128 * p.tpc1 || kGA * (kMaxNL - 1) > kMaxItems * 128 * p.tpc1 ||
-        p.NN * (kGA / 2) > kMaxItems * 128 * p.tpc1)
-        return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core table fill");
+    if (tc_plan_pass1(c, p.NP <= 128 ? 4 : 2, 2)) return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core table fill");
+    // the partial-sum buffer is sized for the largest split the autotuner may choose
+    size_t part_max = 0;
+    for (int tpc : {2, 4})
+        for (int m = 1; m <= 4; m *= 2)
+            if (!tc_plan_pass1(c, tpc, m)) part_max = std::max(part_max, (size_t)p.nsplit1 * p.NP * p.rtot);
+    if (tc_plan_pass1(c, p.NP <= 128 ? 4 : 2, 2)) return set_err(&c, MDG_E_UNSUPPORTED, "tensor-core plan");
     p.mtiles = (ks.nrow + 127) / 128;
     p.nchunk2 = (ks.nrow + kRC - 1) / kRC;
-    p.smem1 = (int)(p.tpc1 == 4 ? p1_layout(4, P1<4>::kS, p.NP, p.NM).total : p1_layout(2, P1<2>::kS, p.NP, p.NM).total);
+    p.smem1 = (int)std::max(p1_layout(4, P1<4>::kS, p.NP, p.NM).total, p1_layout(2, P1<2>::kS, p.NP, p.NM).total);
     p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC).total;
     if (p.smem1 > 227 * 1024 || p.smem2 > 227 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
     c.d_tc_atoms = (uint4*)dalloc(c, sizeof(uint4) * std::max(v.nmove, 1));
     c.d_tc_img = (unsigned char*)dalloc(c, (size_t)std::max(p.nchunk2, 1) * 2 * p.KS * kTile2);
     c.d_tc_cmax = (float*)dalloc(c, sizeof(float) * 4);
-    c.d_tc_part = (float*)dalloc(c, sizeof(float) * (size_t)p.nsplit1 * p.NP * p.rtot);
+    c.d_tc_part = (float*)dalloc(c, sizeof(float) * std::max<size_t>(part_max, 1));
     c.d_tc_cf = (float2*)dalloc(c, sizeof(float2) * std::max(ks.nk, 1));
     if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
     MDG_CUDA(allow_max_smem(k_tc_sfac<4>));

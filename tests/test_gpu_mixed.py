@@ -32,3 +32,26 @@ def test_mixed_forces_vs_fp64(name, gpulib):
     assert rel <= MIXED_FORCE_RTOL, rel
     scale = np.abs(a["elj"]).sum() + np.abs(a["eqq"]).sum() + abs(a["uewa"]) + 1.0
     assert abs(b["uconf"] - a["uconf"]) <= 1e-5 * scale
+
+
+@pytest.mark.parametrize("name", ["slab512", "bulk256"])
+def test_autotune_keeps_forces(name, gpulib):
+    """mdg_autotune only changes launch shapes: the chosen grid and structure-factor split give
+    the same forces (mixed tolerance against FP64) as the defaults."""
+    s, prm = CASES[name]()
+    s64, s32 = s.copy(), s.copy()
+    p64 = abi.RunParams(**{**prm.__dict__, "precision": abi.MDG_FP64})
+    p32 = abi.RunParams(**{**prm.__dict__, "precision": abi.MDG_MIXED})
+    a = abi.Context(gpulib, s64, p64).force_get(s64)
+    ctx = abi.Context(gpulib, s32, p32)
+    ctx.set_state(s32)
+    t = ctx.autotune(2)
+    assert t["pair_blocks"] in (0, 304, 608, 1216)
+    assert t["tc_rows_per_cta"] in (256, 512)
+    assert t["tc_atom_splits"] >= 1
+    assert t["ms_after"] > 0 and t["ms_before"] > 0
+    b = ctx.force_get(s32)
+    rel = np.linalg.norm(b["f"] - a["f"]) / np.linalg.norm(a["f"])
+    assert rel <= MIXED_FORCE_RTOL, rel
+    rep = ctx.run(5)
+    assert np.isfinite(rep["htot"])
