@@ -465,12 +465,14 @@ def _tuning_summary(tunings):
     """Per-replica autotuner choices folded into counts, with the summed force time before/after."""
     if not tunings:
         return None
-    keys = ("pair_blocks", "tc_rows_per_cta", "tc_atom_splits")
     choice = {}
-    for t in tunings:
-        k = ",".join(f"{x}={t[x]}" for x in keys)
-        choice[k] = choice.get(k, 0) + 1
-    return {"choices": choice, "force_ms_sum_before": float(sum(t["ms_before"] for t in tunings)),
+    for key in ("pair_blocks", "tc_rows_per_cta"):
+        for t in tunings:
+            k = f"{key}={t[key]}"
+            choice[k] = choice.get(k, 0) + 1
+    splits = [t["tc_atom_splits"] for t in tunings]
+    return {"choices": choice, "tc_atom_splits_min_max": [min(splits), max(splits)],
+            "force_ms_sum_before": float(sum(t["ms_before"] for t in tunings)),
             "force_ms_sum_after": float(sum(t["ms_after"] for t in tunings))}
 
 

@@ -309,6 +309,71 @@ int mdg_mlp_grad(const float* w, const float* x, const float* y, int64_t n, floa
 int mdg_mlp_train(const float* x, const float* y, int64_t n, int epochs, int batch, float lr, uint64_t seed,
                   float* w_out, float* loss_out);
 
+/* ---------------------------------------------------------------------------------------------
+ * Measurement histograms.  The reference's force loops fill histograms as a side output, and
+ * measure_do (src/measure.f90:270-454) adds z-profiles after every production step:
+ *   ngc(nijt, 0:lmax)      site-wall pair distances, src/forcem.f90:493-495; the bulk variant
+ *                          also counts the moving pairs, src/forcem_back.f90:348-349,380-382
+ *   efipos(2, 0:lmax)      z force on Li/Cl-type ions (site types 3, 4) by their z bin: pair terms
+ *                          src/forcem.f90:347-354,388-395, wall terms :486-489, and the whole fz of
+ *                          the liquid ions after force_fouri :930-934 (slab variant only)
+ *   tefipos, nefipos       final ftz of the liquid ions and their count by z bin, :1094-1098
+ *   ngang(nit-2, 0:201)    bend-angle cosines by molecule type, :617-625
+ *   ngz(nit-2, 0:lmax)     site z-profile; ndipx/y/z/sq(0:lmax) water dipole profile; ng2d1/2 the
+ *                          near-wall 2-D maps; ftotx/y/z(-1:1) summed wall forces (measure_do)
+ * measure_init (src/measure.f90:66-176) sizes the arrays from rdel and the slab width lw:
+ * lmax = int(lw/rdel + 0.5) + 1.  The arrays stay on the device and accumulate until
+ * mdg_measure_zero (measure_zero, :178-262).  The reference indexes without bounds checks; here a
+ * sample whose bin falls outside its array is dropped and counted in out_of_range.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct mdg_measure_params {
+    double rdel;         /* bin width, A (tot.inp "rdel") */
+    int32_t force_hist;  /* 1: every force evaluation adds to ngc, efipos, tefipos/nefipos, ngang */
+    int32_t profiles;    /* 1: every resident step (mdg_run) ends with measure_do */
+    int32_t l2d;         /* 1: measure_do also fills the near-wall 2-D maps (tot.inp "l2d") */
+    int32_t pad;
+    double rfrst, rscnd; /* wall distance bounds of the first and second layer of the 2-D maps */
+} mdg_measure_params;
+
+typedef struct mdg_measure_dims {
+    int64_t lmax;            /* bins 0..lmax of ngc, efipos, tefipos, nefipos, ngz, ndip* */
+    int64_t nijt;            /* rows of ngc */
+    int64_t ntz;             /* rows of ngz, ngang, ng2d* (nit - 2) */
+    int64_t langmax;         /* bins 0..langmax of ngang (201) */
+    int64_t lgxmax, lgymax;  /* ng2d* bins 0..lgxmax by 0..lgymax */
+} mdg_measure_dims;
+
+/* Caller arrays, column-major as the Fortran module holds them (first index fastest); any may
+ * be NULL.  The scalars are filled in always. */
+typedef struct mdg_measure_out {
+    int64_t* ngc;      /* nijt x (lmax+1) */
+    double* efipos;    /* 2 x (lmax+1) */
+    double* tefipos;   /* 2 x (lmax+1) */
+    int64_t* nefipos;  /* 2 x (lmax+1) */
+    int64_t* ngang;    /* ntz x (langmax+1) */
+    int64_t* ngz;      /* ntz x (lmax+1) */
+    double* ndipx;     /* lmax+1 each */
+    double* ndipy;
+    double* ndipz;
+    double* ndipsq;
+    int64_t* ng2d1;    /* ntz x (lgxmax+1) x (lgymax+1) */
+    int64_t* ng2d2;
+    double ftot[3][3]; /* ftotx, ftoty, ftotz (-1:1) */
+    int64_t calls_force;   /* force evaluations accumulated */
+    int64_t calls_do;      /* measure_do calls accumulated */
+    int64_t out_of_range;  /* samples dropped because their bin was outside the array */
+} mdg_measure_out;
+
+/* measure_init: allocates and zeroes the arrays; dims may be NULL. */
+int mdg_measure_init(mdg_ctx* ctx, const mdg_measure_params* prm, mdg_measure_dims* dims);
+/* Switches the force-side histograms and the per-step profiles on or off without clearing. */
+int mdg_measure_enable(mdg_ctx* ctx, int force_hist, int profiles);
+int mdg_measure_zero(mdg_ctx* ctx);
+/* measure_do on positions x0, y0, z0 (nmove moving atoms; NULL: the context's resident state)
+ * with the wall forces of the last force evaluation. */
+int mdg_measure_do(mdg_ctx* ctx, const double* x0, const double* y0, const double* z0);
+int mdg_measure_get(mdg_ctx* ctx, mdg_measure_out* out);
+
 /* Diagnostic: one tcgen05 BF16 matrix product D (128 x n) = A (128 x k) . B^T (n x k) on the
  * device with the shared-memory operand layout of the tensor-core reciprocal sum (host arrays,
  * row-major floats rounded to BF16).  Lets a caller check the tensor-core path on its GPU. */

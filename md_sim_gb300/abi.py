@@ -148,6 +148,23 @@ def make_sysdesc(s: System):
     return d, keep
 
 
+class MeasureParams(C.Structure):
+    _fields_ = [("rdel", C.c_double), ("force_hist", C.c_int32), ("profiles", C.c_int32), ("l2d", C.c_int32),
+                ("pad", C.c_int32), ("rfrst", C.c_double), ("rscnd", C.c_double)]
+
+
+class MeasureDims(C.Structure):
+    _fields_ = [("lmax", C.c_int64), ("nijt", C.c_int64), ("ntz", C.c_int64), ("langmax", C.c_int64),
+                ("lgxmax", C.c_int64), ("lgymax", C.c_int64)]
+
+
+class MeasureOut(C.Structure):
+    _fields_ = [("ngc", I64P), ("efipos", DP), ("tefipos", DP), ("nefipos", I64P), ("ngang", I64P),
+                ("ngz", I64P), ("ndipx", DP), ("ndipy", DP), ("ndipz", DP), ("ndipsq", DP),
+                ("ng2d1", I64P), ("ng2d2", I64P), ("ftot", (C.c_double * 3) * 3), ("calls_force", C.c_int64),
+                ("calls_do", C.c_int64), ("out_of_range", C.c_int64)]
+
+
 class Lib:
     """Binds the entry points of one shared library (`prefix` = 'mdg_' for the product)."""
 
@@ -188,6 +205,12 @@ class Lib:
             g("batch_set_stream", C.c_int, [C.c_void_p, C.c_void_p])
             g("batch_run", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p])
             g("batch_run_async", C.c_int, [C.c_void_p, C.c_int64])
+        if self.has("measure_init"):
+            g("measure_init", C.c_int, [C.c_void_p, C.POINTER(MeasureParams), C.POINTER(MeasureDims)])
+            g("measure_enable", C.c_int, [C.c_void_p, C.c_int, C.c_int])
+            g("measure_zero", C.c_int, [C.c_void_p])
+            g("measure_do", C.c_int, [C.c_void_p, DP, DP, DP])
+            g("measure_get", C.c_int, [C.c_void_p, C.POINTER(MeasureOut)])
         if self.has("run"):
             g("set_state", C.c_int, [C.c_void_p, C.POINTER(Rigid), C.POINTER(State)])
             g("get_state", C.c_int, [C.c_void_p, C.POINTER(State)])
@@ -514,3 +537,64 @@ def _ctx_autotune(self, reps: int = 5) -> Dict[str, float]:
 
 
 Context.autotune = _ctx_autotune
+
+
+# ---------------------------------------------------------------------------------------------
+# Measurement histograms (mdg_measure_*): measure_init / measure_zero / measure_do and the
+# force-loop side outputs, src/measure.f90:66-454 and src/forcem.f90:347-354,388-395,486-495,
+# 617-625,930-934,1094-1098.  Arrays come back column-major as the Fortran module holds them,
+# reshaped to (rows, bins) numpy arrays.
+# ---------------------------------------------------------------------------------------------
+def _ctx_measure_init(self, rdel: float, force_hist: bool = True, profiles: bool = False, l2d: bool = False,
+                      rfrst: float = 0.0, rscnd: float = 0.0) -> Dict[str, int]:
+    p = MeasureParams(float(rdel), int(force_hist), int(profiles), int(l2d), 0, float(rfrst), float(rscnd))
+    d = MeasureDims()
+    self._check(self.lib.measure_init(self.h, C.byref(p), C.byref(d)))
+    self._mdims = {f: int(getattr(d, f)) for f, _ in MeasureDims._fields_}
+    return dict(self._mdims)
+
+
+def _ctx_measure_enable(self, force_hist: bool, profiles: bool) -> None:
+    self._check(self.lib.measure_enable(self.h, int(force_hist), int(profiles)))
+
+
+def _ctx_measure_zero(self) -> None:
+    self._check(self.lib.measure_zero(self.h))
+
+
+def _ctx_measure_do(self, s: Optional[System] = None) -> None:
+    """measure_do on the moving atoms of s, or on the resident state when s is None."""
+    if s is None:
+        self._check(self.lib.measure_do(self.h, None, None, None))
+    else:
+        n = s.nmove
+        xs = [np.ascontiguousarray(a[:n]) for a in (s.x0, s.y0, s.z0)]
+        self._check(self.lib.measure_do(self.h, *[_dp(a) for a in xs]))
+
+
+def _ctx_measure_get(self) -> Dict[str, object]:
+    d = self._mdims
+    L, nijt, ntz, la = d["lmax"] + 1, d["nijt"], d["ntz"], d["langmax"] + 1
+    g2 = ntz * (d["lgxmax"] + 1) * (d["lgymax"] + 1)
+    arrs = {"ngc": np.zeros(nijt * L, np.int64), "efipos": np.zeros(2 * L), "tefipos": np.zeros(2 * L),
+            "nefipos": np.zeros(2 * L, np.int64), "ngang": np.zeros(ntz * la, np.int64),
+            "ngz": np.zeros(ntz * L, np.int64), "ndipx": np.zeros(L), "ndipy": np.zeros(L), "ndipz": np.zeros(L),
+            "ndipsq": np.zeros(L), "ng2d1": np.zeros(g2, np.int64), "ng2d2": np.zeros(g2, np.int64)}
+    o = MeasureOut()
+    for k, a in arrs.items():
+        setattr(o, k, a.ctypes.data_as(I64P if a.dtype == np.int64 else DP))
+    self._check(self.lib.measure_get(self.h, C.byref(o)))
+    shape = {"ngc": (nijt, L), "efipos": (2, L), "tefipos": (2, L), "nefipos": (2, L), "ngang": (ntz, la),
+             "ngz": (ntz, L), "ng2d1": (ntz, d["lgxmax"] + 1, d["lgymax"] + 1),
+             "ng2d2": (ntz, d["lgxmax"] + 1, d["lgymax"] + 1)}
+    out: Dict[str, object] = {k: (a.reshape(shape[k], order="F") if k in shape else a) for k, a in arrs.items()}
+    out["ftot"] = np.array([[o.ftot[c][k] for k in range(3)] for c in range(3)])
+    out["calls_force"], out["calls_do"], out["out_of_range"] = o.calls_force, o.calls_do, o.out_of_range
+    return out
+
+
+Context.measure_init = _ctx_measure_init
+Context.measure_enable = _ctx_measure_enable
+Context.measure_zero = _ctx_measure_zero
+Context.measure_do = _ctx_measure_do
+Context.measure_get = _ctx_measure_get

@@ -257,6 +257,44 @@ def slab_water(nwat: int = 2048, cells: int = 10, a: float = 4.21, lz: Optional[
     return _finish(s), prm
 
 
+def slab_electrolyte(nwat: int = 384, npair: int = 12, cells: int = 6, a: float = 4.21, seed: int = 31,
+                     T: float = 300.0, rcut: float = 9.0, skin: float = 1.0, alpha: float = 0.30,
+                     kmax: int = 6) -> Tuple[S.System, RunParams]:
+    """Rigid waters with npair Li+ / Cl- point ions (atmol site types 3 and 4, the numbering of the
+    reference's y.fld) between two rocksalt walls: the case in which the force loops fill the
+    ion field profiles (efipos, tefipos/nefipos).  Ions sit on free sites of the water lattice."""
+    L = cells * a
+    dens = 0.033427
+    thick = (nwat + 2 * npair) / (L * L * dens)
+    lw = thick + 3.0
+    lwh = 0.5 * lw
+    wpos, wtyp = _rocksalt_walls(cells, a, lwh)
+    rng = np.random.default_rng(seed)
+    pts = _lattice_waters(rng, nwat + 2 * npair, L, -lwh + 2.2, lwh - 2.2)
+    com, ions = pts[:nwat], pts[nwat:]
+    wat = _water_moltype("rigmol", nwat)
+    li = S.MolType("Li", "atmol", npair, ["Li"], [1], [6.941e-3], [1.0], ns=1)
+    cl = S.MolType("Cl", "atmol", npair, ["Cl"], [1], [35.453e-3], [-1.0], ns=1)
+    crys = _crystal(len(wpos), a, lw)
+    names = ["O", "H", "Li", "Cl", "Mg", "Ox"]
+    buck = ("Buck", 1000.0 * EV, 0.30, 10.0 * EV)
+    vdw = _vdw_table(names, {(1, 1): ("LeJo", SIG_OO, EPS_OO), (1, 3): ("LeJo", 2.34, 0.70),
+                             (1, 4): ("LeJo", 3.78, 0.52), (3, 4): ("LeJo", 2.70, 0.35),
+                             (3, 3): ("LeJo", 1.50, 0.70), (4, 4): ("LeJo", 4.40, 0.42),
+                             (1, 5): buck, (1, 6): buck, (3, 6): buck, (4, 5): buck, (4, 6): buck})
+    fld = S.FieldFile([wat, li, cl, crys], vdw)
+    s = S.System(fld, S.TopFile([], [], [], []), L, L, 2.0 * L, 1.0)
+    s.c[0] = com.T
+    s.q[0] = _random_quaternions(np.random.default_rng(seed + 100), nwat)
+    s.set_walls(wtyp, wpos)
+    n0 = s.nriga
+    s.x0[n0:n0 + 2 * npair], s.y0[n0:n0 + 2 * npair], s.z0[n0:n0 + 2 * npair] = ions.T
+    _rigid_velocities(s, T, seed + 200, seed + 300)
+    s.temper = -1.0
+    prm = RunParams(rcut=rcut, skin=skin, kmax=kmax, alpha=alpha, variant=MDG_SLAB)
+    return _finish(s), prm
+
+
 # ----------------------------------------------------------------------------------------------
 def replica_slabs(n: int = 64, seed: int = 8, nmin: int = 500, nmax: int = 4000, cmin: int = 7, cmax: int = 14,
                   a: float = 4.21) -> List[Tuple[S.System, RunParams]]:

@@ -65,6 +65,25 @@ const double A4 = F(-1.453152027f), A5 = F(1.061405429f), PP = F(0.3275911f);
 inline double anint(double x) { return std::round(x); }  // Fortran ANINT: half away from zero
 inline double fsign(double z) { return std::signbit(z) ? -1.0 : 1.0; }
 inline double pw3(double x) { return x * x * x; }
+// Fortran MODULO(a, p) for reals as gfortran evaluates it: the exact remainder fmod(a, p), moved
+// into p's sign range when it is non-zero and of the other sign.
+inline double fmodulo(double a, double p) {
+    double m = std::fmod(a, p);
+    if (m != 0.0 && ((m < 0.0) != (p < 0.0))) m += p;
+    return m;
+}
+
+// Measurement arrays of src/measure.f90:12-22 (column-major, bins from 0).
+struct Meas {
+    bool init = false, force_hist = false, profiles = false, l2d = false;
+    double rdeli = 0, rfrst = 0, rscnd = 0;
+    int64_t lmax = 0, ntz = 0, langmax = 201, lgxmax = 0, lgymax = 0;
+    std::vector<int64_t> ngc, nefipos, ngang, ngz, ng2d1, ng2d2;
+    std::vector<double> efipos, tefipos, ndipx, ndipy, ndipz, ndipsq;
+    double ftot[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double fws[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // wall forces of the last evaluation
+    int64_t calls_force = 0, calls_do = 0, oor = 0;
+};
 
 struct Ref {
     // sizes
@@ -89,6 +108,7 @@ struct Ref {
     std::vector<double> ocx0, ocy0, ocz0, ox0, oy0, oz0;
     std::vector<std::vector<int64_t>> excl;  // constrained partners of surface atoms
     // reciprocal
+    Meas ms;
     int64_t kmax, klmax, kmmax, knmax;
     double pipix, pipiy, pipiz;
     std::vector<int> kl_, km_, kn_;  // valid k in reference order
@@ -109,6 +129,9 @@ struct Ref {
     double kp = 0, kw = 0, ke = 0, htot = 0, sft = 0, sfr = 0, tempnow = 0, uconf = 0, tkps = 0, press = 0;
     int32_t last_sweeps = 0;
 
+    // l = int((z + lwh)*rdeli + 0.5) and l = int(r*rdeli + 0.5) (src/forcem.f90:348,493)
+    int64_t zbin(double z) const { return (int64_t)((z + lwh) * ms.rdeli + 0.5); }
+    int64_t rbin(double d) const { return (int64_t)(d * ms.rdeli + 0.5); }
     int ij(int64_t it, int64_t jt) const { return (int)ijtype[(it - 1) + nit * (jt - 1)] - 1; }
     double mx(double d) const { return d - lx * anint(d * lxi); }
     double my(double d) const { return d - ly * anint(d * lyi); }
@@ -119,6 +142,36 @@ struct Ref {
         for (int64_t p : excl[i])
             if (p == j) return true;
         return false;
+    }
+};
+
+// Thread-private efipos / ngc contributions of one force loop, added to the context's arrays
+// under the loop's merge lock.
+struct Hist {
+    Ref* r;
+    bool on;
+    std::vector<double> efi;
+    std::vector<int64_t> ngc;
+    int64_t oor = 0;
+    Hist(Ref* r_, bool on_) : r(r_), on(on_) {
+        if (on) {
+            efi.assign(2 * (r->ms.lmax + 1), 0.0);
+            ngc.assign(r->nijt * (r->ms.lmax + 1), 0);
+        }
+    }
+    void ef(int64_t t, int64_t l, double v) {
+        if (t >= 0 && t < 2 && l >= 0 && l <= r->ms.lmax) efi[t + 2 * l] += v;
+        else ++oor;
+    }
+    void gc(int64_t ijt0, int64_t l) {
+        if (l >= 0 && l <= r->ms.lmax) ++ngc[ijt0 + r->nijt * l];
+        else ++oor;
+    }
+    void merge() {
+        if (!on) return;
+        for (size_t k = 0; k < efi.size(); ++k) r->ms.efipos[k] += efi[k];
+        for (size_t k = 0; k < ngc.size(); ++k) r->ms.ngc[k] += ngc[k];
+        r->ms.oor += oor;
     }
 };
 
@@ -537,6 +590,7 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
     std::vector<double> elj(nijt, 0.0), eqq(nijt, 0.0);
     double fwsx[3] = {0, 0, 0}, fwsy[3] = {0, 0, 0}, fwsz[3] = {0, 0, 0};  // index sgn+1
     double uewa = 0.0, urf = 0.0, ulr = 0.0, uavex = 0.0;
+    const bool hist = r->ms.init && r->ms.force_hist;
 
     // ---- force_real: rebuild trigger (src/forcem.f90:245-250)
     {
@@ -564,6 +618,7 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
         std::vector<double> tfx(nmove, 0.0), tfy(nmove, 0.0), tfz(nmove, 0.0), telj(nijt, 0.0),
             teqq(nijt, 0.0);
         double tuav = 0.0;
+        Hist th(r, hist);
         // ---- moving-moving pairs (src/forcem.f90:288-403)
 #ifdef _OPENMP
 #pragma omp for schedule(static)
@@ -606,6 +661,14 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
             fij = fij + (spii * alfar * exp2a + erfx) * aux * rsqi;
             tfx[i] += xio * fij; tfy[i] += yio * fij; tfz[i] += zio * fij;
             tfx[j] -= xio * fij; tfy[j] -= yio * fij; tfz[j] -= zio * fij;
+            if (hist) {
+                if (r->variant == MDG_SLAB) {  // src/forcem.f90:347-354
+                    if (it == 3 || it == 4) th.ef(it - 3, r->zbin(z0[i]), zio * fij);
+                    if (jt == 3 || jt == 4) th.ef(jt - 3, r->zbin(z0[j]), -zio * fij);
+                } else {                       // src/forcem_back.f90:348-349
+                    th.gc(ijt, r->rbin(rij));
+                }
+            }
             int64_t jmin = j + 1;
             const int64_t nsi_i = r->nsi[it - 1], nsi_j = r->nsi[jt - 1];
             for (int64_t ix = i; ix < i + nsi_i; ++ix) {
@@ -626,6 +689,14 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
                     double fj = (spii * ar * e2 + ef) * au * rs2i;
                     tfx[ix] += xd * fj; tfy[ix] += yd * fj; tfz[ix] += zd * fj;
                     tfx[jx] -= xd * fj; tfy[jx] -= yd * fj; tfz[jx] -= zd * fj;
+                    if (hist) {
+                        if (r->variant == MDG_SLAB) {  // src/forcem.f90:388-395
+                            if (it == 3 || it == 4) th.ef(it - 3, r->zbin(z0[i]), zd * fj);
+                            if (jt == 3 || jt == 4) th.ef(jt - 3, r->zbin(z0[j]), -zd * fj);
+                        } else {                       // src/forcem_back.f90:380-382
+                            th.gc(r->ij(r->itype[ix], r->itype[jx]), r->rbin(rr));
+                        }
+                    }
                 }
                 jmin = j;
             }
@@ -641,6 +712,7 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
                 elj[k] += telj[k]; eqq[k] += teqq[k];
             }
             uavex += tuav;
+            th.merge();
         }
     }
 
@@ -655,6 +727,7 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
         std::vector<double> tfx(nmove, 0.0), tfy(nmove, 0.0), tfz(nmove, 0.0), telj(nijt, 0.0),
             teqq(nijt, 0.0);
         double tuav = 0.0, tws[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        Hist th(r, hist);
 #ifdef _OPENMP
 #pragma omp for schedule(static)
 #endif
@@ -707,7 +780,10 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
                 if (it <= r->nltype) {
                     tws[0][sg] -= xd * fij; tws[1][sg] -= yd * fij; tws[2][sg] -= zd * fij;
                 }
+                if (hist && r->variant == MDG_SLAB && (it == 3 || it == 4))  // src/forcem.f90:486-489
+                    th.ef(it - 3, r->zbin(z0[i]), zd * fij);
                 fij = 0.0;
+                if (hist) th.gc(r->ij(r->itype[ix], r->itype[j]), r->rbin(rr));  // :493-495
             }
         }
 #ifdef _OPENMP
@@ -724,6 +800,7 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
             for (int c = 0; c < 3; ++c) {
                 fwsx[c] += tws[0][c]; fwsy[c] += tws[1][c]; fwsz[c] += tws[2][c];
             }
+            th.merge();
         }
     }
 
@@ -836,6 +913,11 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
             urf = -crf * facq * dipz * dipz;
             crf = 2.0 * crf * facq * dipz;
             for (int64_t i = 0; i < nmove; ++i) fz[i] += crf * r->qs[i];
+            if (hist) {  // src/forcem.f90:930-934: whole fz of the liquid ions so far
+                Hist th(r, hist);
+                for (int64_t i = nriga; i < r->nliqa; ++i) th.ef(r->itype[i] - 3, r->zbin(z0[i]), fz[i]);
+                th.merge();
+            }
         }
     }
 
@@ -867,6 +949,12 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
             tmp = aa * az - bz;
             if (k < nmove) fz[k] += fij * tmp;
             if (j < nmove) fz[j] += fij * (bb * bz - az - tmp);
+            if (hist) {  // src/forcem.f90:617-625
+                const int64_t l = (int64_t)((cang + 1.0) * 100.0) + 1;
+                Meas& m = r->ms;
+                if (l >= 0 && l <= m.langmax && it < m.ntz) ++m.ngang[it + m.ntz * l];
+                else ++m.oor;
+            }
         }
     }
 
@@ -878,6 +966,23 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
             sx += fx[i]; sy += fy[i]; sz += fz[i];
         }
         fwsx[1] = sx; fwsy[1] = sy; fwsz[1] = sz;
+    }
+    for (int c = 0; c < 3; ++c) {
+        r->ms.fws[0][c] = fwsx[c]; r->ms.fws[1][c] = fwsy[c]; r->ms.fws[2][c] = fwsz[c];
+    }
+    if (hist) {
+        Meas& m = r->ms;
+        if (r->variant == MDG_SLAB)  // src/forcem.f90:1094-1098 (ftz = fz of the flexible atoms)
+            for (int64_t i = nriga; i < r->nliqa; ++i) {
+                const int64_t t = r->itype[i] - 3, l = r->zbin(z0[i]);
+                if (t >= 0 && t < 2 && l >= 0 && l <= m.lmax) {
+                    ++m.nefipos[t + 2 * l];
+                    m.tefipos[t + 2 * l] += fz[i];
+                } else {
+                    ++m.oor;
+                }
+            }
+        ++m.calls_force;
     }
     if (fxo)
         for (int64_t i = 0; i < nmove; ++i) {
@@ -1246,6 +1351,138 @@ int ref_get_state(RefCtx* r, mdg_state* st) {
     return MDG_OK;
 }
 
+// ---- measurement (src/measure.f90) ------------------------------------------------------------
+// measure_init (src/measure.f90:66-176): bins of width rdel over the slab, lmax = int(lw/rdel+0.5)+1.
+int ref_measure_init(RefCtx* r, const mdg_measure_params* p, mdg_measure_dims* d) {
+    if (!p || !(p->rdel > 0.0)) return fail(r, MDG_E_ARG, "measure: rdel must be positive");
+    Meas& m = r->ms;
+    m = Meas();
+    m.rdeli = 1.0 / p->rdel;
+    m.lmax = (int64_t)(r->lw * m.rdeli + 0.5) + 1;
+    m.ntz = std::max<int64_t>(r->nit - 2, 1);
+    m.langmax = 201;
+    m.l2d = p->l2d != 0;
+    m.rfrst = p->rfrst;
+    m.rscnd = p->rscnd;
+    m.lgxmax = (int64_t)(4.0 * r->cx * m.rdeli + 1.0);
+    m.lgymax = (int64_t)(2.0 * r->cy * m.rdeli + 1.0);
+    const int64_t L = m.lmax + 1;
+    m.ngc.assign(r->nijt * L, 0);
+    m.efipos.assign(2 * L, 0.0);
+    m.tefipos.assign(2 * L, 0.0);
+    m.nefipos.assign(2 * L, 0);
+    m.ngang.assign(m.ntz * (m.langmax + 1), 0);
+    m.ngz.assign(m.ntz * L, 0);
+    m.ndipx.assign(L, 0.0);
+    m.ndipy.assign(L, 0.0);
+    m.ndipz.assign(L, 0.0);
+    m.ndipsq.assign(L, 0.0);
+    if (m.l2d) {
+        m.ng2d1.assign(m.ntz * (m.lgxmax + 1) * (m.lgymax + 1), 0);
+        m.ng2d2.assign(m.ntz * (m.lgxmax + 1) * (m.lgymax + 1), 0);
+    }
+    m.force_hist = p->force_hist != 0;
+    m.profiles = p->profiles != 0;
+    m.init = true;
+    if (d) {
+        d->lmax = m.lmax; d->nijt = r->nijt; d->ntz = m.ntz; d->langmax = m.langmax;
+        d->lgxmax = m.lgxmax; d->lgymax = m.lgymax;
+    }
+    return MDG_OK;
+}
+
+int ref_measure_enable(RefCtx* r, int force_hist, int profiles) {
+    if (!r->ms.init) return fail(r, MDG_E_ARG, "measure: not initialised");
+    r->ms.force_hist = force_hist != 0;
+    r->ms.profiles = profiles != 0;
+    return MDG_OK;
+}
+
+// measure_zero (src/measure.f90:178-262), the arrays this library keeps
+int ref_measure_zero(RefCtx* r) {
+    Meas& m = r->ms;
+    if (!m.init) return fail(r, MDG_E_ARG, "measure: not initialised");
+    for (auto* v : {&m.ngc, &m.nefipos, &m.ngang, &m.ngz, &m.ng2d1, &m.ng2d2}) std::fill(v->begin(), v->end(), 0);
+    for (auto* v : {&m.efipos, &m.tefipos, &m.ndipx, &m.ndipy, &m.ndipz, &m.ndipsq})
+        std::fill(v->begin(), v->end(), 0.0);
+    for (int c = 0; c < 3; ++c)
+        for (int k = 0; k < 3; ++k) m.ftot[c][k] = 0.0;
+    m.calls_force = m.calls_do = m.oor = 0;
+    return MDG_OK;
+}
+
+// measure_do (src/measure.f90:270-312): summed wall forces, site z-profile, water dipole profile
+// and the near-wall 2-D maps, over the moving atoms.
+static void measure_do(Ref* r, const double* x0, const double* y0, const double* z0) {
+    Meas& m = r->ms;
+    for (int c = 0; c < 3; ++c)
+        for (int k = 0; k < 3; ++k) m.ftot[c][k] += m.fws[c][k];
+    const int64_t L = m.lmax + 1;
+    std::vector<double> mux(L, 0.0), muy(L, 0.0), muz(L, 0.0);
+    const double lxh = 0.5 * r->lx, lyh = 0.5 * r->ly;
+    for (int64_t i = 0; i < r->nmove; ++i) {
+        const int64_t it = r->itype[i];
+        double rij = z0[i] + r->lwh;
+        int64_t l = (int64_t)(rij * m.rdeli + 0.5);
+        if (l >= 0 && l <= m.lmax && it - 1 < m.ntz) {
+            ++m.ngz[(it - 1) + m.ntz * l];
+            if (it == 1) {
+                muz[l] += (z0[i] - 0.5 * (z0[i + 1] + z0[i + 2]));
+                mux[l] += (x0[i] - 0.5 * (x0[i + 1] + x0[i + 2]));
+                muy[l] += (y0[i] - 0.5 * (y0[i + 1] + y0[i + 2]));
+            }
+        } else {
+            ++m.oor;
+        }
+        rij = r->lwh - std::fabs(z0[i]);
+        if (m.l2d && rij < m.rscnd) {
+            const int64_t lx2 = (int64_t)(0.5 * fmodulo(x0[i] + lxh + 4.0 * r->cx, 4.0 * r->cx) * m.rdeli + 0.5);
+            const int64_t ky2 = (int64_t)(0.5 * fmodulo(y0[i] + lyh + 2.0 * r->cy, 2.0 * r->cy) * m.rdeli + 0.5);
+            if (lx2 >= 0 && ky2 >= 0 && lx2 <= m.lgxmax && ky2 <= m.lgymax && it - 1 < m.ntz) {
+                const int64_t k = (it - 1) + m.ntz * (lx2 + (m.lgxmax + 1) * ky2);
+                if (rij < m.rfrst) ++m.ng2d1[k];
+                else ++m.ng2d2[k];
+            } else {
+                ++m.oor;
+            }
+        }
+    }
+    for (int64_t l = 0; l < L; ++l) {
+        m.ndipx[l] += mux[l];
+        m.ndipy[l] += muy[l];
+        m.ndipz[l] += muz[l];
+        m.ndipsq[l] += mux[l] * mux[l] + muy[l] * muy[l] + muz[l] * muz[l];
+    }
+    ++m.calls_do;
+}
+
+int ref_measure_do(RefCtx* r, const double* x0, const double* y0, const double* z0) {
+    if (!r->ms.init) return fail(r, MDG_E_ARG, "measure: not initialised");
+    if (!x0) {
+        if (!r->have_state) return fail(r, MDG_E_ARG, "measure: no positions");
+        x0 = r->X[0].data(); y0 = r->X[1].data(); z0 = r->X[2].data();
+    }
+    measure_do(r, x0, y0, z0);
+    return MDG_OK;
+}
+
+int ref_measure_get(RefCtx* r, mdg_measure_out* o) {
+    const Meas& m = r->ms;
+    if (!m.init) return fail(r, MDG_E_ARG, "measure: not initialised");
+    auto cp = [](const auto& v, auto* p) {
+        if (p) std::copy(v.begin(), v.end(), p);
+    };
+    cp(m.ngc, o->ngc); cp(m.efipos, o->efipos); cp(m.tefipos, o->tefipos); cp(m.nefipos, o->nefipos);
+    cp(m.ngang, o->ngang); cp(m.ngz, o->ngz); cp(m.ndipx, o->ndipx); cp(m.ndipy, o->ndipy);
+    cp(m.ndipz, o->ndipz); cp(m.ndipsq, o->ndipsq); cp(m.ng2d1, o->ng2d1); cp(m.ng2d2, o->ng2d2);
+    for (int c = 0; c < 3; ++c)
+        for (int k = 0; k < 3; ++k) o->ftot[c][k] = m.ftot[c][k];
+    o->calls_force = m.calls_force;
+    o->calls_do = m.calls_do;
+    o->out_of_range = m.oor;
+    return MDG_OK;
+}
+
 int ref_run(RefCtx* r, int64_t nsteps, mdg_report* rep) {
     if (!r->have_state) return fail(r, MDG_E_ARG, "mdg_run before mdg_set_state");
     const int64_t nm = r->nmove, nflex = r->nmove - r->nriga, nrig = std::max<int64_t>(r->nrig, 1);
@@ -1281,6 +1518,7 @@ int ref_run(RefCtx* r, int64_t nsteps, mdg_report* rep) {
             r->last_sweeps = sw;
             r->tkps = tk;
         }
+        if (r->ms.init && r->ms.profiles) measure_do(r, r->X[0].data(), r->X[1].data(), r->X[2].data());
         const int64_t nfree = r->nliqa - r->nriga;
         r->tempnow = r->ke * 1000.0 / (3.0 * PH_R * (double)(float)(nfree + 2 * r->nrig));
     }
