@@ -116,6 +116,27 @@ struct Pk {
     int zper = 0;
 };
 
+// Measurement arrays on the device and their bin parameters (measure.cu), passed by value.
+struct MeasView {
+    double rdeli = 0, lwh = 0, rfrst = 0, rscnd = 0, lxh = 0, lyh = 0, cx4 = 0, cy2 = 0;
+    int lmax = 0, L = 0, ntz = 0, langmax = 201, lgx = 0, lgy = 0, l2d = 0, slab = 1;
+    unsigned long long *ngc = nullptr, *nefipos = nullptr, *ngang = nullptr, *ngz = nullptr;
+    unsigned long long *ng2d1 = nullptr, *ng2d2 = nullptr;
+    unsigned long long* cnt = nullptr;  // calls_force, calls_do, out_of_range
+    double *efipos = nullptr, *tefipos = nullptr;
+    double* ndip = nullptr;  // 4 x L: ndipx, ndipy, ndipz, ndipsq
+    double* mu = nullptr;    // 3 x L scratch of one measure_do call
+    double* ftot = nullptr;  // 9: ftotx(-1:1), ftoty(-1:1), ftotz(-1:1)
+    double* pos = nullptr;   // 3 x nmove positions handed to mdg_measure_do
+    const int* ang_mt = nullptr;  // molecule type (0-based) of each angle term
+};
+
+struct Meas {
+    bool init = false, force_hist = false, profiles = false;
+    int smem = 0;  // bytes of the per-block ngc/efipos histogram of the pair loops, 0 = global atomics
+    MeasView m;
+};
+
 // Launch plan of the tensor-core reciprocal sum (recip_tc.cu).
 struct TcPlan {
     bool ready = false;
@@ -168,6 +189,8 @@ struct Ctx {
     float* d_shake_rec = nullptr; // ncons x 12 recorded features / multipliers
     bool shake_model = false, shake_record = false;
     int pair_blocks = 0;          // blocks of the real-space loops (0: by head count); autotuned
+    Meas meas;                    // measurement histograms (measure.cu)
+    std::vector<int> h_ang_mt;    // molecule type of each angle term
     int64_t nfreed = 0;
     // angles
     int nang_terms = 0;
@@ -230,6 +253,15 @@ int mlp_train_host(const float* X, const float* Y, int64_t n, int epochs, int ba
 void dipole_correction(Ctx& c);
 void angle_forces(Ctx& c);
 void force_sum(Ctx& c, double* d_ft, double* d_fc, double* d_tq);
+// measure.cu
+int measure_init(Ctx& c, const mdg_measure_params* p, mdg_measure_dims* d);
+void measure_zero(Ctx& c);
+void measure_force_real(Ctx& c);   // after the real-space loops
+void measure_force_fouri(Ctx& c);  // after force_fouri's slab term
+void measure_force_intra(Ctx& c);  // after force_intra
+void measure_force_sum(Ctx& c);    // after force_sum
+void measure_do_launch(Ctx& c, const double* x, const double* y, const double* z);
+int measure_get(Ctx& c, mdg_measure_out* o);
 // shake.cu
 int shake_setup(Ctx& c, const mdg_sysdesc* s);
 void shake_launch(Ctx& c, const double* d_ft);

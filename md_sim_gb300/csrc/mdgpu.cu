@@ -244,8 +244,15 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
         PHASE(recip_fp64(c), "reciprocal");
     }
     PHASE(dipole_correction(c), "dipole");
+    const bool hist = c.meas.init && c.meas.force_hist;
+    if (hist) {
+        measure_force_real(c);
+        measure_force_fouri(c);
+    }
     PHASE(angle_forces(c), "angles");
+    if (hist) measure_force_intra(c);
     PHASE(force_sum(c, c.d_ft, c.d_fc, c.d_tq), "force_sum");
+    if (hist) measure_force_sum(c);
     return MDG_OK;
 }
 
@@ -494,6 +501,7 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
                     return bail(MDG_E_ARG);
                 }
                 terms.push_back(make_int4((int)a, (int)b, (int)d, (int)kt.size()));
+                c.h_ang_mt.push_back((int)it);
                 kt.push_back(s->kt[it + s->ntype * k]);
                 th.push_back(s->theta[it + s->ntype * k]);
             }
@@ -823,6 +831,7 @@ static int step_launch(Ctx& c) {
     correct_launch(c);
     if (c.v.nmove > c.v.nliqa) shake_launch(c, c.d_ft);
     thermo_finish_launch(c);
+    if (c.meas.init && c.meas.profiles) measure_do_launch(c, c.v.x, c.v.y, c.v.z);
     return MDG_OK;
 }
 
@@ -1433,6 +1442,83 @@ int mdg_autotune(mdg_ctx* cp, int32_t reps, mdg_tuning* out) {
         out->ms_after = t1;
     }
     return MDG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Measurement histograms (measure.cu)
+// ---------------------------------------------------------------------------------------------
+static void drop_graph(Ctx& c) {
+    if (c.graph_exec) {
+        cudaGraphExecDestroy(c.graph_exec);
+        c.graph_exec = nullptr;
+    }
+}
+
+int mdg_measure_init(mdg_ctx* cp, const mdg_measure_params* p, mdg_measure_dims* d) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    const int rc = measure_init(c, p, d);
+    if (rc) return rc;
+    drop_graph(c);
+    return MDG_OK;
+}
+
+int mdg_measure_enable(mdg_ctx* cp, int force_hist, int profiles) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    if (!c.meas.init) return set_err(&c, MDG_E_ARG, "measure: mdg_measure_init first");
+    if (c.meas.force_hist != (force_hist != 0) || c.meas.profiles != (profiles != 0)) {
+        cudaSetDevice(c.device);
+        MDG_CUDA(cudaStreamSynchronize(c.stream));
+        drop_graph(c);
+    }
+    c.meas.force_hist = force_hist != 0;
+    c.meas.profiles = profiles != 0;
+    return MDG_OK;
+}
+
+int mdg_measure_zero(mdg_ctx* cp) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    if (!c.meas.init) return set_err(&c, MDG_E_ARG, "measure: mdg_measure_init first");
+    cudaSetDevice(c.device);
+    measure_zero(c);
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    return MDG_OK;
+}
+
+int mdg_measure_do(mdg_ctx* cp, const double* x0, const double* y0, const double* z0) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    if (!c.meas.init) return set_err(&c, MDG_E_ARG, "measure: mdg_measure_init first");
+    if ((x0 == nullptr) != (y0 == nullptr) || (x0 == nullptr) != (z0 == nullptr))
+        return set_err(&c, MDG_E_ARG, "measure: give all of x0, y0, z0 or none");
+    cudaSetDevice(c.device);
+    const View& v = c.v;
+    if (x0) {
+        const size_t n = (size_t)std::max(v.nmove, 1);
+        double* pos = c.meas.m.pos;
+        MDG_CUDA(cudaMemcpyAsync(pos, x0, sizeof(double) * v.nmove, cudaMemcpyHostToDevice, c.stream));
+        MDG_CUDA(cudaMemcpyAsync(pos + n, y0, sizeof(double) * v.nmove, cudaMemcpyHostToDevice, c.stream));
+        MDG_CUDA(cudaMemcpyAsync(pos + 2 * n, z0, sizeof(double) * v.nmove, cudaMemcpyHostToDevice, c.stream));
+        measure_do_launch(c, pos, pos + n, pos + 2 * n);
+    } else {
+        if (!c.resident) return set_err(&c, MDG_E_ARG, "measure: no positions and no resident state");
+        measure_do_launch(c, v.x, v.y, v.z);
+    }
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    MDG_CUDA(cudaGetLastError());
+    return MDG_OK;
+}
+
+int mdg_measure_get(mdg_ctx* cp, mdg_measure_out* o) {
+    if (!cp || !o) return set_err(cp, MDG_E_ARG, "null argument");
+    Ctx& c = *cp;
+    if (!c.meas.init) return set_err(&c, MDG_E_ARG, "measure: mdg_measure_init first");
+    cudaSetDevice(c.device);
+    return measure_get(c, o);
 }
 
 }  // extern "C"

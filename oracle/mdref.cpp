@@ -1426,7 +1426,7 @@ static void measure_do(Ref* r, const double* x0, const double* y0, const double*
         int64_t l = (int64_t)(rij * m.rdeli + 0.5);
         if (l >= 0 && l <= m.lmax && it - 1 < m.ntz) {
             ++m.ngz[(it - 1) + m.ntz * l];
-            if (it == 1) {
+            if (it == 1 && i + 2 < r->nmove) {  // a water O and its two H (the reference assumes it)
                 muz[l] += (z0[i] - 0.5 * (z0[i + 1] + z0[i + 2]));
                 mux[l] += (x0[i] - 0.5 * (x0[i + 1] + x0[i + 2]));
                 muy[l] += (y0[i] - 0.5 * (y0[i + 1] + y0[i + 2]));
