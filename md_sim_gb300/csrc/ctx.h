@@ -142,7 +142,7 @@ struct TcPlan {
     bool ready = false;
     int KN = 0, NN = 0, NP = 0, KS = 0, KM = 0, NM = 0;
     int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, grid1x = 0, rtot = 0, tpc1 = 0, smem1 = 0, smem2 = 0;
-    int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0, nlist2 = 0, mult1 = 2;
+    int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0, nlist2 = 0, mult1 = 2, nst2 = 2;
 };
 
 struct Ctx {
@@ -157,6 +157,10 @@ struct Ctx {
     float* d_tc_cmax = nullptr;         // scale of the packed C(k) operand
     float* d_tc_part = nullptr;         // pass-1 partial sums [split][col][row]
     float2* d_tc_cf = nullptr;          // C(k) in FP32 for the pass-2 operand
+    double* d_frc = nullptr;            // 3 x nmove reciprocal forces of the tensor-core sum, merged after the join
+    cudaStream_t side = nullptr;        // second stream: the reciprocal sum runs beside the real-space loops
+    cudaStream_t side2 = nullptr;       // third stream: the head-wall loop beside the head-head loop
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the context's stream while a caller's stream is in use
     int device = 0;
@@ -205,6 +209,7 @@ struct Ctx {
     mdg_rigid body{};
     double *d_xd = nullptr, *d_c = nullptr, *d_q = nullptr, *d_w = nullptr, *d_a = nullptr;
     double *d_thermo = nullptr, *d_isum = nullptr;
+    unsigned* d_done = nullptr;   // block counters of the fused integrator kernels
     std::vector<std::pair<void*, size_t>> snap_regions;
     char* d_snap = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -228,8 +233,13 @@ void surf_partition(Ctx& c);
 void lr_tail(Ctx& c);
 // pair_mx.cu
 void pack_setup(Ctx& c);
-void real_space_mixed(Ctx& c);   // pack, head-head pairs, j-side merge
-void wall_forces_mixed(Ctx& c);
+// per-evaluation records of the real-space loops and the reciprocal sum; clears the FP64 forces
+// and sums the slab dipole M_z
+void pack_mixed(Ctx& c);
+void pairs_mixed(Ctx& c, bool merge);  // head-head pairs into F (then merged into the FP64 forces)
+void walls_mixed(Ctx& c);              // head-wall pairs into F
+// F (+ frc, + the slab dipole term) into the FP64 forces, F cleared
+void merge_mixed(Ctx& c, const double* frc, bool dipole);
 // recip.cu
 int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const double* z0);
 void recip_fp64(Ctx& c);
@@ -268,7 +278,6 @@ void shake_launch(Ctx& c, const double* d_ft);
 // integrate.cu
 void predict_launch(Ctx& c);
 void correct_launch(Ctx& c);
-void thermo_finish_launch(Ctx& c);
 
 int set_err(Ctx* c, int code, const std::string& msg);
 void* dalloc(Ctx& c, size_t bytes);

@@ -1,14 +1,17 @@
 // integrate.cu - the MD step around the force phases, on the device (resident mode).
 //
-//   k_pred_ions / k_pred_rigid / k_thermo_pred   move_predict, src/move.f90:48-217: 5-value Gear
-//       predictor for ions, centres of mass, angular velocities and quaternions; quaternion
-//       normalisation, rotation matrix, site rebuild and the H offsets rsx (:148-162); kinetic
-//       energies, Nose-like thermostat predictor, htot, sft/sfr.
-//   k_uconf                                       uconf and press of force_sum (:1055,1079,1081)
-//   k_corr_ions / k_corr_rigid / k_thermo_corr   move_correct, src/move.f90:220-383.
+//   k_pred   move_predict, src/move.f90:48-217: 5-value Gear predictor for ions, centres of mass,
+//            angular velocities and quaternions; quaternion normalisation, rotation matrix, site
+//            rebuild and the H offsets rsx (:148-162); the block that finishes last computes the
+//            kinetic energies, the Nose-like thermostat predictor, htot and sft/sfr.
+//   k_corr   move_correct, src/move.f90:220-383, for ions and rigid molecules; its last block adds
+//            uconf and press of force_sum (src/forcem.f90:1055,1079,1081) and the thermostat
+//            corrector.
 //
-// One thread per atom or molecule; kinetic sums go through block reductions into a small
-// accumulator array.  Gear coefficients are the reference's single-precision literals.
+// One thread per ion or molecule in small blocks (the FP64 work of one molecule is a long
+// dependent chain, so the molecules are spread over as many SMs as possible); kinetic sums go
+// through block reductions into a small accumulator array that the last block reads and clears.
+// Gear coefficients are the reference's single-precision literals.
 #include <algorithm>
 #include <cmath>
 
@@ -34,6 +37,7 @@ __device__ __forceinline__ void gpred(double& a0, double& a1, double& a2, double
 }
 
 struct Dyn {
+    unsigned* done;  // [2] blocks finished (k_pred, k_corr), reset by the last block
     double* xd;     // [4][3][nion]
     double* c;      // [5][3][nrig]
     double* q;      // [4][5][nrig]
@@ -48,35 +52,41 @@ struct Dyn {
     int nion;
 };
 
-__global__ void k_pred_ions(View v, Dyn D) {
-    double kp = 0.0;
+__device__ __forceinline__ double pred_ion(const View& v, const Dyn& D, int k) {
     const int n = D.nion;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int i = v.nriga + k;
-        double* X[3] = {v.x, v.y, v.z};
-        double s2 = 0.0;
-        for (int d = 0; d < 3; ++d) {
-            double* x1 = D.xd + (0 * 3 + d) * n;
-            double* x2 = D.xd + (1 * 3 + d) * n;
-            double* x3 = D.xd + (2 * 3 + d) * n;
-            double* x4 = D.xd + (3 * 3 + d) * n;
-            double a0 = X[d][i], a1 = x1[k], a2 = x2[k], a3 = x3[k];
-            gpred(a0, a1, a2, a3, x4[k]);
-            X[d][i] = a0;
-            x1[k] = a1;
-            x2[k] = a2;
-            x3[k] = a3;
-            s2 += a1 * a1;
-        }
-        kp += v.mi[i] * s2;
+    const int i = v.nriga + k;
+    double* X[3] = {v.x, v.y, v.z};
+    double s2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        double* x1 = D.xd + (0 * 3 + d) * n;
+        double* x2 = D.xd + (1 * 3 + d) * n;
+        double* x3 = D.xd + (2 * 3 + d) * n;
+        double* x4 = D.xd + (3 * 3 + d) * n;
+        double a0 = X[d][i], a1 = x1[k], a2 = x2[k], a3 = x3[k];
+        gpred(a0, a1, a2, a3, x4[k]);
+        X[d][i] = a0;
+        x1[k] = a1;
+        x2[k] = a2;
+        x3[k] = a3;
+        s2 += a1 * a1;
     }
-    block_atomic_sum<kNT>(kp, &D.isum[0]);
+    return v.mi[i] * s2;
 }
 
-__global__ void k_pred_rigid(View v, Dyn D) {
-    double sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
+// True in every thread of the block that finished last; each block's atomics are visible before
+// it counts itself done.
+__device__ __forceinline__ bool last_block(unsigned* done) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    return last;
+}
+
+__device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, double* sc, double* sw) {
     const int nr = v.nrig;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += gridDim.x * blockDim.x) {
+    {
         double cx[3];
         for (int d = 0; d < 3; ++d) {
             double a0 = D.c[(0 * 3 + d) * nr + i], a1 = D.c[(1 * 3 + d) * nr + i], a2 = D.c[(2 * 3 + d) * nr + i],
@@ -142,15 +152,16 @@ __global__ void k_pred_rigid(View v, Dyn D) {
             v.rsz[ix + j] = sz[j] - sz[0];
         }
     }
-    for (int d = 0; d < 3; ++d) block_atomic_sum<kNT>(sc[d], &D.isum[1 + d]);
-    for (int d = 0; d < 3; ++d) block_atomic_sum<kNT>(sw[d], &D.isum[4 + d]);
 }
 
-__global__ void k_thermo_pred(View v, Dyn D) {
+// thermostat predictor and kinetic energies from the summed isum[0..6] (one thread)
+__device__ void thermo_pred(const View& v, const Dyn& D) {
     double* th = D.th;
     const mdg_rigid& b = D.body;
-    const double kp = D.isum[0] + b.mw * (D.isum[1] + D.isum[2] + D.isum[3]);
-    const double kw = b.inxx * D.isum[4] + b.inyy * D.isum[5] + b.inzz * D.isum[6];
+    double is[7];
+    for (int k = 0; k < 7; ++k) is[k] = __ldcg(&D.isum[k]);
+    const double kp = is[0] + b.mw * (is[1] + is[2] + is[3]);
+    const double kw = b.inxx * is[4] + b.inyy * is[5] + b.inzz * is[6];
     double* s = th + TH_S;
     double* rs = th + TH_RS;
     if (b.temper == -1.0) {
@@ -171,11 +182,27 @@ __global__ void k_thermo_pred(View v, Dyn D) {
     th[TH_HTOT] = 0.5 * (kp + kw + qmass * s[0] * s[0] + rmass * rs[0] * rs[0]) + th[TH_UCONF];
     th[TH_SFT] = (kp - (double)(float)(3 * (nfree + v.nrig) - 2) * tstar) / qmass;
     th[TH_SFR] = (kw - (double)(float)(3 * v.nrig + 1) * tstar) / rmass;
+    for (int k = 0; k < 7; ++k) D.isum[k] = 0.0;  // ready for the next step
+}
+
+__global__ void k_pred(View v, Dyn D) {
+    double kp = 0.0, sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
+    const int nu = D.nion + v.nrig;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+        if (u < D.nion) kp += pred_ion(v, D, u);
+        else pred_rigid(v, D, u - D.nion, sc, sw);
+    }
+    block_atomic_sum<kNT>(kp, &D.isum[0]);
+    for (int d = 0; d < 3; ++d) block_atomic_sum<kNT>(sc[d], &D.isum[1 + d]);
+    for (int d = 0; d < 3; ++d) block_atomic_sum<kNT>(sw[d], &D.isum[4 + d]);
+    if (last_block(&D.done[0]) && threadIdx.x == 0) {
+        thermo_pred(v, D);
+        D.done[0] = 0u;
+    }
 }
 
 // uconf = sum(elj) + sum(eqq) + uewa + urf (src/forcem.f90:1055,1079) and the wall pressure.
-__global__ void k_uconf(View v, Dyn D, int slab) {
-    if (threadIdx.x != 0) return;
+__device__ void uconf(const View& v, const Dyn& D, int slab) {
     const double* a = v.acc;
     const double* sl = a + 2 * v.nijt;
     double slj = 0.0, sqq = 0.0;
@@ -193,11 +220,11 @@ __global__ void k_uconf(View v, Dyn D, int slab) {
                      (F32D(6.022045e23) * F32D(1e-30)) * F32D(1e-5);
 }
 
-__global__ void k_corr_ions(View v, Dyn D) {
+__device__ __forceinline__ void corr_ion(const View& v, const Dyn& D, int k) {
     const int n = D.nion;
     const double s0i = D.th[TH_S];
     const int nflex = v.nmove - v.nriga;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    {
         const int i = v.nriga + k;
         double* X[3] = {v.x, v.y, v.z};
         for (int d = 0; d < 3; ++d) {
@@ -215,13 +242,13 @@ __global__ void k_corr_ions(View v, Dyn D) {
     }
 }
 
-__global__ void k_corr_rigid(View v, Dyn D) {
+__device__ __forceinline__ void corr_rigid(const View& v, const Dyn& D, int i) {
     const int nr = v.nrig;
     const double s0i = D.th[TH_S], rs0i = D.th[TH_RS];
     const mdg_rigid& b = D.body;
     const double rcorr = 0.5 / b.mw;
     const double inxxi = 1.0 / b.inxx, inyyi = 1.0 / b.inyy, inzzi = 1.0 / b.inzz;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += gridDim.x * blockDim.x) {
+    {
         for (int d = 0; d < 3; ++d) {
             double* c0 = D.c + (0 * 3 + d) * nr;
             double* c1 = D.c + (1 * 3 + d) * nr;
@@ -272,7 +299,7 @@ __global__ void k_corr_rigid(View v, Dyn D) {
     }
 }
 
-__global__ void k_thermo_corr(View v, Dyn D) {
+__device__ void thermo_corr(const View& v, const Dyn& D) {
     double* th = D.th;
     if (D.body.temper != -1.0) {
         double* s = th + TH_S;
@@ -296,8 +323,24 @@ __global__ void k_thermo_corr(View v, Dyn D) {
     if (v.status[ST_REBUILD]) th[TH_REBUILDS] += 1.0;
 }
 
+// The correctors read the thermostat values of the predictor; the block that finishes last then
+// adds uconf/press and corrects the thermostat.
+__global__ void k_corr(View v, Dyn D, int slab) {
+    const int nu = D.nion + v.nrig;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+        if (u < D.nion) corr_ion(v, D, u);
+        else corr_rigid(v, D, u - D.nion);
+    }
+    if (last_block(&D.done[1]) && threadIdx.x == 0) {
+        uconf(v, D, slab);
+        thermo_corr(v, D);
+        D.done[1] = 0u;
+    }
+}
+
 Dyn dyn_of(Ctx& c) {
     Dyn D;
+    D.done = c.d_done;
     D.xd = c.d_xd;
     D.c = c.d_c;
     D.q = c.d_q;
@@ -320,23 +363,13 @@ int nblk(int n) { return std::max(1, std::min((n + kNT - 1) / kNT, 152 * 16)); }
 void predict_launch(Ctx& c) {
     const View& v = c.v;
     Dyn D = dyn_of(c);
-    cudaMemsetAsync(c.d_isum, 0, sizeof(double) * 8, c.stream);
-    if (D.nion > 0) k_pred_ions<<<nblk(D.nion), kNT, 0, c.stream>>>(v, D);
-    if (v.nrig > 0) k_pred_rigid<<<nblk(v.nrig), kNT, 0, c.stream>>>(v, D);
-    k_thermo_pred<<<1, 1, 0, c.stream>>>(v, D);
+    k_pred<<<nblk(D.nion + v.nrig), kNT, 0, c.stream>>>(v, D);
 }
 
 void correct_launch(Ctx& c) {
     const View& v = c.v;
     Dyn D = dyn_of(c);
-    k_uconf<<<1, 32, 0, c.stream>>>(v, D, c.variant == MDG_SLAB ? 1 : 0);
-    if (D.nion > 0) k_corr_ions<<<nblk(D.nion), kNT, 0, c.stream>>>(v, D);
-    if (v.nrig > 0) k_corr_rigid<<<nblk(v.nrig), kNT, 0, c.stream>>>(v, D);
-}
-
-void thermo_finish_launch(Ctx& c) {
-    Dyn D = dyn_of(c);
-    k_thermo_corr<<<1, 1, 0, c.stream>>>(c.v, D);
+    k_corr<<<nblk(D.nion + v.nrig), kNT, 0, c.stream>>>(v, D, c.variant == MDG_SLAB ? 1 : 0);
 }
 
 }  // namespace mdg

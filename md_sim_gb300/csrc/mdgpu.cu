@@ -221,29 +221,57 @@ int phase_check(Ctx& c, const char* name) {
 // Queues the force phases on device-resident positions (no synchronisation).
 int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
     View& v = c.v;
-    cudaMemsetAsync(v.fx, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
-    cudaMemsetAsync(v.fy, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
-    cudaMemsetAsync(v.fz, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
     cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
     if (reset_status) cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
-    PHASE(nnlist_trigger(c, force_rebuild), "trigger");
-    PHASE(nnlist_build(c), "nnlist");
     if (c.precision == MDG_MIXED) {
-        PHASE(real_space_mixed(c), "pairs");
-        PHASE(surf_partition(c), "surf_partition");
-        PHASE(wall_forces_mixed(c), "walls");
+        // The tensor-core reciprocal sum needs only the packed atom records: it runs on a side
+        // stream while the main stream does the list, the real-space loops and the wall tail.
+        // Without surface atoms (whose z forces after the head-head loop are booked to the walls,
+        // src/forcem.f90:408-413) the head-wall loop runs on a third stream beside the head-head
+        // loop; both add into F with vector reductions.  Fork and join go through events, so the
+        // same dependencies hold inside a captured graph.  The reciprocal forces (d_frc), F and the
+        // slab dipole term join the FP64 forces in one merge at the end.
+        PHASE(pack_mixed(c), "pack");
+        const cudaStream_t s0 = c.stream;
+        MDG_CUDA(cudaEventRecord(c.ev_fork, s0));
+        MDG_CUDA(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
+        c.stream = c.side;
+        recip_tc(c);
+        c.stream = s0;
+        MDG_CUDA(cudaEventRecord(c.ev_join, c.side));
+        PHASE(nnlist_trigger(c, force_rebuild), "trigger");
+        PHASE(nnlist_build(c), "nnlist");
+        if (v.nliqa == v.nmove && v.nwall > 0 && v.nheads > 0) {
+            MDG_CUDA(cudaEventRecord(c.ev_fork2, s0));
+            MDG_CUDA(cudaStreamWaitEvent(c.side2, c.ev_fork2, 0));
+            c.stream = c.side2;
+            walls_mixed(c);
+            c.stream = s0;
+            MDG_CUDA(cudaEventRecord(c.ev_join2, c.side2));
+            PHASE(pairs_mixed(c, false), "pairs");
+            PHASE(lr_tail(c), "lr_tail");
+            MDG_CUDA(cudaStreamWaitEvent(s0, c.ev_join2, 0));
+        } else {
+            PHASE(pairs_mixed(c, true), "pairs");
+            PHASE(surf_partition(c), "surf_partition");
+            PHASE(walls_mixed(c), "walls");
+            PHASE(lr_tail(c), "lr_tail");
+        }
+        MDG_CUDA(cudaStreamWaitEvent(s0, c.ev_join, 0));
+        PHASE(merge_mixed(c, c.d_frc, true), "merge");
     } else {
+        cudaMemsetAsync(v.fx, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+        cudaMemsetAsync(v.fy, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+        cudaMemsetAsync(v.fz, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
+        PHASE(nnlist_trigger(c, force_rebuild), "trigger");
+        PHASE(nnlist_build(c), "nnlist");
         PHASE(pair_forces_fp64(c), "pairs");
         PHASE(surf_partition(c), "surf_partition");
         PHASE(wall_forces_fp64(c), "walls");
-    }
-    PHASE(lr_tail(c), "lr_tail");
-    if (c.precision == MDG_MIXED) {
-        PHASE(recip_tc(c), "reciprocal");
-    } else {
+        PHASE(lr_tail(c), "lr_tail");
         PHASE(recip_fp64(c), "reciprocal");
+        PHASE(dipole_correction(c), "dipole");
     }
-    PHASE(dipole_correction(c), "dipole");
     const bool hist = c.meas.init && c.meas.force_hist;
     if (hist) {
         measure_force_real(c);
@@ -288,6 +316,8 @@ void mdg_destroy(mdg_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
+    if (c->side2) cudaStreamSynchronize(c->side2);
     for (void* p : c->owned)
         if (p) cudaFree(p);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
@@ -295,6 +325,10 @@ void mdg_destroy(mdg_ctx* c) {
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     else if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->side2) cudaStreamDestroy(c->side2);
+    for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_fork2, c->ev_join2})
+        if (e) cudaEventDestroy(e);
     delete c;
 }
 
@@ -336,7 +370,13 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
         mdg_destroy(cp);
         return set_err(nullptr, code, m.empty() ? "mdg_create failed" : m);
     };
-    if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c.side2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c.ev_fork2, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c.ev_join2, cudaEventDisableTiming) != cudaSuccess) {
         c.err = "cudaStreamCreate failed";
         return bail(MDG_E_CUDA);
     }
@@ -785,6 +825,7 @@ static int resident_alloc(Ctx& c) {
     c.d_a = (double*)dalloc(c, sizeof(double) * 9 * nr);
     c.d_thermo = (double*)dalloc(c, sizeof(double) * TH_N);
     c.d_isum = (double*)dalloc(c, sizeof(double) * 8);
+    c.d_done = (unsigned*)dalloc(c, sizeof(unsigned) * 4);
     if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the integrator state");
     // the centres of mass of the force phases become the first Gear slice
     v.cx = c.d_c;
@@ -830,7 +871,6 @@ static int step_launch(Ctx& c) {
     if (rc) return rc;
     correct_launch(c);
     if (c.v.nmove > c.v.nliqa) shake_launch(c, c.d_ft);
-    thermo_finish_launch(c);
     if (c.meas.init && c.meas.profiles) measure_do_launch(c, c.v.x, c.v.y, c.v.z);
     return MDG_OK;
 }
@@ -1105,25 +1145,36 @@ int mdg_phase_times(mdg_ctx* cp, int reps, double* ms) {
         nnlist_trigger(c, true);
         nnlist_build(c);
         cudaEventRecord(ev[1], c.stream);
-        if (c.precision == MDG_MIXED) real_space_mixed(c);
-        else pair_forces_fp64(c);
+        if (c.precision == MDG_MIXED) {
+            pack_mixed(c);
+            pairs_mixed(c, true);
+        } else {
+            pair_forces_fp64(c);
+        }
         surf_partition(c);
         cudaEventRecord(ev[2], c.stream);
-        if (c.precision == MDG_MIXED) wall_forces_mixed(c);
-        else wall_forces_fp64(c);
+        if (c.precision == MDG_MIXED) {
+            walls_mixed(c);
+            merge_mixed(c, nullptr, false);
+        } else {
+            wall_forces_fp64(c);
+        }
         cudaEventRecord(ev[3], c.stream);
-        if (c.precision == MDG_MIXED) recip_tc(c);
-        else recip_fp64(c);
+        if (c.precision == MDG_MIXED) {
+            recip_tc(c);
+            merge_mixed(c, c.d_frc, true);
+        } else {
+            recip_fp64(c);
+        }
         cudaEventRecord(ev[4], c.stream);
         lr_tail(c);
-        dipole_correction(c);
+        if (c.precision != MDG_MIXED) dipole_correction(c);
         angle_forces(c);
         force_sum(c, c.d_ft, c.d_fc, c.d_tq);
         cudaEventRecord(ev[5], c.stream);
         if (c.resident) {
             predict_launch(c);
             correct_launch(c);
-            thermo_finish_launch(c);
         }
         cudaEventRecord(ev[6], c.stream);
         if (v.nmove > v.nliqa && c.ncons > 0 && c.resident) shake_launch(c, c.d_ft);
@@ -1227,7 +1278,8 @@ int mdg_mlp_train(const float* x, const float* y, int64_t n, int epochs, int bat
 // ---------------------------------------------------------------------------------------------
 struct mdg_batch {
     std::vector<mdg_ctx*> ctx;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // stream the batch graph is launched on
+    cudaStream_t own_stream = nullptr;  // the batch's own stream (the only one it destroys)
     cudaGraphExec_t exec = nullptr;
     int device = 0;
     std::string err;
@@ -1277,10 +1329,11 @@ int mdg_batch_create(mdg_ctx* const* ctxs, int n, mdg_batch** out) {
         b->ctx.push_back(ctxs[i]);
     }
     cudaSetDevice(b->device);
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete b;
         return batch_err(nullptr, MDG_E_CUDA, "mdg_batch_create: stream");
     }
+    b->stream = b->own_stream;
     *out = b;
     return MDG_OK;
 }
@@ -1290,7 +1343,7 @@ void mdg_batch_destroy(mdg_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);  // a caller's stream stays the caller's
     delete b;
 }
 
@@ -1300,7 +1353,7 @@ int mdg_batch_set_stream(mdg_batch* b, void* stream) {
     if (!b) return batch_err(nullptr, MDG_E_ARG, "null batch");
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
-    b->stream = stream ? (cudaStream_t)stream : b->stream;
+    b->stream = stream ? (cudaStream_t)stream : b->own_stream;
     return MDG_OK;
 }
 

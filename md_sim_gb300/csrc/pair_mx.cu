@@ -111,7 +111,11 @@ __device__ __forceinline__ uint32_t frac32(double t) {
     return (uint32_t)__double_as_longlong(t + 1572864.0);
 }
 
-__global__ void k_pack(View v, Pk pk) {
+// Records of every atom for this evaluation; also clears the FP64 forces and, for the slab
+// variant, sums the dipole M_z = sum q z of the moving atoms (src/forcem.f90:924) into the
+// accumulator block, which the caller zeroed.
+__global__ void k_pack(View v, Pk pk, int dip) {
+    double mz = 0.0;
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < v.ntota; a += gridDim.x * blockDim.x) {
         const double x = v.x[a], y = v.y[a], z = v.z[a];
         uint4 p;
@@ -133,11 +137,16 @@ __global__ void k_pack(View v, Pk pk) {
             q.y = (float)v.rsy[a];
             q.z = (float)v.rsz[a];
             pk.F[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+            v.fx[a] = 0.0;
+            v.fy[a] = 0.0;
+            v.fz[a] = 0.0;
+            mz += v.q[a] * z;
             // the reciprocal sum's record: periodic fractions on all three axes and the charge
             if (pk.tc) pk.tc[a] = make_uint4(p.x, p.y, uz, __float_as_uint(q.w));
         }
         pk.Q[a] = q;
     }
+    if (dip) block_atomic_sum<256>(mz, &v.acc[2 * v.nijt + ACC_DIPZ]);
 }
 
 // Pair-type tables in shared memory: per ijt {kind, sig, eps, aa, rhoi, cc}, ijt[it*nit+jt], nsi[it].
@@ -372,12 +381,23 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
     }
 }
 
-__global__ void k_merge_f(View v, Pk pk) {
+// F (and the reciprocal forces frc, 3 x nmove, when given) into the FP64 forces; F cleared.
+// crf0 != 0 adds the slab term fz += 2 crf0 facq M_z q (src/forcem.f90:925-928) with M_z from
+// k_pack.
+__global__ void k_merge_f(View v, Pk pk, const double* __restrict__ frc, double crf0) {
+    const double crf = crf0 != 0.0 ? 2.0 * crf0 * v.facq * v.acc[2 * v.nijt + ACC_DIPZ] : 0.0;
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < v.nmove; a += gridDim.x * blockDim.x) {
         const float4 f = pk.F[a];
-        v.fx[a] += (double)f.x;
-        v.fy[a] += (double)f.y;
-        v.fz[a] += (double)f.z;
+        double gx = (double)f.x, gy = (double)f.y, gz = (double)f.z;
+        if (frc) {
+            gx += frc[a];
+            gy += frc[v.nmove + a];
+            gz += frc[2 * v.nmove + a];
+        }
+        if (crf0 != 0.0) gz += crf * v.q[a];
+        v.fx[a] += gx;
+        v.fy[a] += gy;
+        v.fz[a] += gz;
         pk.F[a] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
@@ -406,23 +426,37 @@ void pack_setup(Ctx& c) {
     c.pk.sz = (float)(v.lz / 4294967296.0);
 }
 
-void real_space_mixed(Ctx& c) {
-    const View& v = c.v;
-    if (v.ntota == 0) return;
-    k_pack<<<std::min((v.ntota + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
-    if (v.nheads > 0) {
-        if (c.pk.zper) k_pair_mx<1><<<blocks(c, v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
-        else k_pair_mx<0><<<blocks(c, v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
-        k_merge_f<<<std::min((v.nmove + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
-    }
+double slab_crf0(const Ctx& c) {
+    if (c.variant != MDG_SLAB) return 0.0;
+    return -2.0 * (double)3.1415926535898f * c.v.lzi * c.v.lxi * c.v.lyi;
 }
 
-void wall_forces_mixed(Ctx& c) {
+void pack_mixed(Ctx& c) {
+    const View& v = c.v;
+    if (v.ntota == 0) return;
+    k_pack<<<std::min((v.ntota + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk, c.variant == MDG_SLAB ? 1 : 0);
+}
+
+void merge_mixed(Ctx& c, const double* frc, bool dipole) {
+    const View& v = c.v;
+    if (v.nmove == 0) return;
+    k_merge_f<<<std::min((v.nmove + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk, frc,
+                                                                              dipole ? slab_crf0(c) : 0.0);
+}
+
+void pairs_mixed(Ctx& c, bool merge) {
+    const View& v = c.v;
+    if (v.nheads == 0) return;
+    if (c.pk.zper) k_pair_mx<1><<<blocks(c, v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
+    else k_pair_mx<0><<<blocks(c, v.nheads), kNT, table_smem(v, 0), c.stream>>>(v, c.pk);
+    if (merge) merge_mixed(c, nullptr, false);
+}
+
+void walls_mixed(Ctx& c) {
     const View& v = c.v;
     if (v.nheads == 0 || v.nwall == 0) return;
     if (c.pk.zper) k_wall_mx<1><<<blocks(c, v.nheads), kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
     else k_wall_mx<0><<<blocks(c, v.nheads), kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
-    k_merge_f<<<std::min((v.nmove + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk);
 }
 
 }  // namespace mdg

@@ -39,6 +39,7 @@ struct TcDims {
     int KS;          // pass-2 K steps (2 NN rounded up to 16, / 16)
     int nrow, nchunk2;
     float px, py, pz;
+    int nst2;        // pass-2 chunk image stages in shared memory (2; 1 when two do not fit)
 };
 
 __device__ __forceinline__ void phase(uint32_t u, float& c, float& s) {
@@ -424,22 +425,23 @@ struct P2Layout {
     uint32_t a_bytes, img, off_a, off_b, off_rows, total;
 };
 
-__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad) {
+__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
     P2Layout L;
     L.a_bytes = 2 * KS * 4096;                 // [h][ks] 128 x 16
     L.img = 2 * KS * kTile2;                   // a chunk image [h][ks] 128 x 16
     L.off_a = 1024;
     L.off_b = L.off_a + L.a_bytes;
-    L.off_rows = L.off_b + 2 * L.img;
+    L.off_rows = L.off_b + nst * L.img;
     L.total = L.off_rows + nrow_pad * 16;      // (float l, float m, l | restart << 31, m)
     return L;
 }
 
 __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
                                                      const unsigned char* __restrict__ img,
-                                                     const int4* __restrict__ rows, TcDims d, const float* cmax) {
+                                                     const int4* __restrict__ rows, TcDims d, const float* cmax,
+                                                     double* __restrict__ frc) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC);
+    const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC, d.nst2);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     uint64_t* full = reinterpret_cast<uint64_t*>(sm);   // [2] chunk image landed
     uint64_t* mdone = full + 2;                          // [2] MMAs of the chunk done (accumulator ready)
@@ -502,8 +504,9 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             const uint32_t bbase = tc::smem_u32(sm + L.off_b);
             const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(bbase);
             const uint32_t half = L.img / 2;
+            const bool two = d.nst2 == 2;
             auto copy = [&](int c) {
-                const int s = c & 1;
+                const int s = two ? (c & 1) : 0;
                 const uint32_t fb = tc::smem_u32(&full[s]);
                 tc::mbar_expect_tx(fb, L.img);
                 tc::bulk_g2s(bbase + s * L.img, img + (size_t)c * L.img, half, fb);
@@ -512,14 +515,15 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             bool alive = true;
             if (NC > 0) copy(0);
             for (int c = 0; c < NC && alive; ++c) {
-                const int s = c & 1;
-                alive = tc::mbar_wait(tc::smem_u32(&full[s]), (c >> 1) & 1, err, 22);
+                const int s = c & 1;              // accumulator
+                const int sb = two ? s : 0;       // chunk image stage
+                alive = tc::mbar_wait(tc::smem_u32(&full[sb]), two ? ((c >> 1) & 1) : (c & 1), err, 22);
                 if (!alive) break;
                 if (c >= 2) alive = tc::mbar_wait(tc::smem_u32(&afree[s]), ((c >> 1) - 1) & 1, err, 23);
                 if (!alive) break;
                 tc::fence_after();
                 const uint32_t dcol = tmem + s * kNC2;
-                const uint64_t dB = dB0 + (uint64_t)((s * L.img) >> 4);
+                const uint64_t dB = dB0 + (uint64_t)((sb * L.img) >> 4);
                 for (int ks = 0; ks < d.KS; ++ks) {
                     const uint64_t ah = dA0 + (uint64_t)(ks * 256), al = dA0 + (uint64_t)((d.KS + ks) * 256);
                     const uint64_t bh = dB + (uint64_t)(ks * (kTile2 >> 4)), bl = dB + (uint64_t)((d.KS + ks) * (kTile2 >> 4));
@@ -528,9 +532,11 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                     tc::mma_bf16(dcol, al, bh, idesc, 1u);
                 }
                 tc::commit(tc::smem_u32(&mdone[s]));
-                // next chunk's copy into the other stage, free once the MMAs of chunk c - 1 are done
+                // next chunk's copy: into the other stage once the MMAs of chunk c - 1 are done, or
+                // with one stage, into the same stage once those of chunk c are done
                 if (c + 1 < NC) {
-                    if (c >= 1) alive = tc::mbar_wait(tc::smem_u32(&mdone[s ^ 1]), ((c - 1) >> 1) & 1, err, 21);
+                    if (two && c >= 1) alive = tc::mbar_wait(tc::smem_u32(&mdone[s ^ 1]), ((c - 1) >> 1) & 1, err, 21);
+                    if (!two) alive = tc::mbar_wait(tc::smem_u32(&mdone[s]), (c >> 1) & 1, err, 21);
                     if (!alive) break;
                     copy(c + 1);
                 }
@@ -583,11 +589,11 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 }
             }
         }
-        if (ok && alive) {
-            const double q = (double)__uint_as_float(rec.w) * (double)cmax[0];
-            v.fx[at] += q * (double)d.px * (double)fx;
-            v.fy[at] += q * (double)d.py * (double)fy;
-            v.fz[at] += q * (double)d.pz * (double)fz;
+        if (ok) {  // each atom has one writer: plain stores (a timed-out block leaves zeros and its status)
+            const double q = alive ? (double)__uint_as_float(rec.w) * (double)cmax[0] : 0.0;
+            frc[at] = q * (double)d.px * (double)fx;
+            frc[v.nmove + at] = q * (double)d.py * (double)fy;
+            frc[2 * v.nmove + at] = q * (double)d.pz * (double)fz;
         }
     }
     __syncthreads();
@@ -666,6 +672,9 @@ int tc_plan_pass1(Ctx& c, int tpc, int mult) {
     if (kGA * p.NM > kMaxItems * 128 * tpc || kGA * (kMaxNL - 1) > kMaxItems * 128 * tpc ||
         p.NN * (kGA / 2) > kMaxItems * 128 * tpc)
         return 1;
+    const size_t smem = tpc == 4 ? p1_layout(4, P1<4>::kS, p.NP, p.NM).total : p1_layout(2, P1<2>::kS, p.NP, p.NM).total;
+    if (smem > 227 * 1024) return 1;
+    p.smem1 = (int)smem;
     p.tpc1 = tpc;
     p.ncols1 = tpc * (p.NP <= 128 ? 128 : 256);
     p.grid1x = (ks.nrow + tpc * 128 - 1) / (tpc * 128);
@@ -690,24 +699,27 @@ int recip_tc_setup(Ctx& c) {
     p.NM = 2 * ks.kmmax + 1;
     if (p.NP > 256) return set_err(&c, MDG_E_UNSUPPORTED, "knmax too large for the tensor-core reciprocal sum");
     if (ks.klmax + 1 > kMaxNL - 1) return set_err(&c, MDG_E_UNSUPPORTED, "klmax too large for the tensor-core reciprocal sum");
-    if (tc_plan_pass1(c, p.NP <= 128 ? 4 : 2, 2)) return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core table fill");
+    const int tpc0 = p.NP <= 128 ? 4 : 2;
+    if (tc_plan_pass1(c, tpc0, 2) && tc_plan_pass1(c, 2, 2))
+        return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core table fill");
     // the partial-sum buffer is sized for the largest split the autotuner may choose
     size_t part_max = 0;
     for (int tpc : {2, 4})
         for (int m = 1; m <= 4; m *= 2)
             if (!tc_plan_pass1(c, tpc, m)) part_max = std::max(part_max, (size_t)p.nsplit1 * p.NP * p.rtot);
-    if (tc_plan_pass1(c, p.NP <= 128 ? 4 : 2, 2)) return set_err(&c, MDG_E_UNSUPPORTED, "tensor-core plan");
+    if (tc_plan_pass1(c, tpc0, 2) && tc_plan_pass1(c, 2, 2)) return set_err(&c, MDG_E_UNSUPPORTED, "tensor-core plan");
     p.mtiles = (ks.nrow + 127) / 128;
     p.nchunk2 = (ks.nrow + kRC - 1) / kRC;
-    p.smem1 = (int)std::max(p1_layout(4, P1<4>::kS, p.NP, p.NM).total, p1_layout(2, P1<2>::kS, p.NP, p.NM).total);
-    p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC).total;
-    if (p.smem1 > 227 * 1024 || p.smem2 > 227 * 1024)
+    p.nst2 = p2_layout(p.KS, p.nchunk2 * kRC, 2).total <= 227 * 1024 ? 2 : 1;
+    p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC, p.nst2).total;
+    if (p.smem2 > 227 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
     c.d_tc_atoms = (uint4*)dalloc(c, sizeof(uint4) * std::max(v.nmove, 1));
     c.d_tc_img = (unsigned char*)dalloc(c, (size_t)std::max(p.nchunk2, 1) * 2 * p.KS * kTile2);
     c.d_tc_cmax = (float*)dalloc(c, sizeof(float) * 4);
     c.d_tc_part = (float*)dalloc(c, sizeof(float) * std::max<size_t>(part_max, 1));
     c.d_tc_cf = (float2*)dalloc(c, sizeof(float2) * std::max(ks.nk, 1));
+    c.d_frc = (double*)dalloc(c, sizeof(double) * 3 * std::max(v.nmove, 1));
     if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
     MDG_CUDA(allow_max_smem(k_tc_sfac<4>));
     MDG_CUDA(allow_max_smem(k_tc_sfac<2>));
@@ -721,7 +733,7 @@ void recip_tc(Ctx& c) {
     KSet& ks = c.ks;
     const TcPlan& p = c.tcp;
     if (ks.nk == 0 || v.nmove == 0) return;
-    TcDims d{p.KN, p.NN, p.NP, p.KS, ks.nrow, p.nchunk2, (float)ks.pipix, (float)ks.pipiy, (float)ks.pipiz};
+    TcDims d{p.KN, p.NN, p.NP, p.KS, ks.nrow, p.nchunk2, (float)ks.pipix, (float)ks.pipiy, (float)ks.pipiz, p.nst2};
     // c.d_tc_atoms was filled by the packing kernel of the real-space phase of this evaluation
     cudaMemsetAsync(c.d_tc_cmax, 0, sizeof(float), c.stream);
     if (p.tpc1 == 4)
@@ -736,7 +748,8 @@ void recip_tc(Ctx& c) {
     const long total = (long)p.nchunk2 * p.KS * kNC2 * 8;
     k_tc_prep_c<<<(int)std::min<long>((total + 255) / 256, 152 * 8), 256, 0, c.stream>>>(c.d_tc_cf, ks.row, ks.row_nlen,
                                                                                          d, c.d_tc_img, c.d_tc_cmax);
-    k_tc_force<<<(v.nmove + 127) / 128, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, ks.row, d, c.d_tc_cmax);
+    k_tc_force<<<(v.nmove + 127) / 128, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, ks.row, d, c.d_tc_cmax,
+                                                                  c.d_frc);
 }
 
 int umma_selftest(int n, int k, const float* a, const float* b, float* dout, std::string& err) {

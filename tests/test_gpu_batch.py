@@ -50,3 +50,25 @@ def test_batch_list_regrowth(gpulib):
     reps = batch.run(200)
     assert all(np.isfinite(r["htot"]) for r in reps)
     batch.close()
+
+
+def test_batch_leaves_caller_stream(gpulib):
+    """A batch launched on a caller's stream destroys only its own stream when closed."""
+    import torch
+
+    s, p = _systems()[0]
+    c = abi.Context(gpulib, s, p)
+    c.set_state(s)
+    st = torch.cuda.Stream()
+    b = abi.Batch(gpulib, [c])
+    b.set_stream(st.cuda_stream)
+    b.run(3)
+    b.close()
+    with torch.cuda.stream(st):
+        x = torch.ones(1024, device="cuda") * 2
+    st.synchronize()
+    assert float(x.sum()) == 2048.0
+    c.set_stream(st.cuda_stream)
+    c.run(2)
+    c.close()
+    st.synchronize()
