@@ -103,6 +103,8 @@ struct KSet {
     int* witem_row = nullptr;     // k_sfac work items: row
     int* witem_n0 = nullptr;      //                    n offset inside the row
     int nwork = 0, tile = 0, splits = 1, atoms_per_split = 0, sfac_smem = 0, force_smem = 0;
+    std::vector<int4> h_row;      // host copies of row and row_nlen
+    std::vector<int> h_nlen;
 };
 
 // Per-step packed atom records of the mixed-precision real-space kernels (pair_mx.cu).
@@ -143,6 +145,10 @@ struct TcPlan {
     int KN = 0, NN = 0, NP = 0, KS = 0, KM = 0, NM = 0;
     int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, grid1x = 0, rtot = 0, tpc1 = 0, smem1 = 0, smem2 = 0;
     int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0, nlist2 = 0, mult1 = 2, nst2 = 2;
+    int4* row2 = nullptr;    // pass-2 rows, sorted by their K-step range (nchunk2 x kRC, padded)
+    int* nlen2 = nullptr;
+    int4* chunk2 = nullptr;  // per pass-2 chunk: image byte offset, first K step, K steps
+    size_t img_bytes = 0;
 };
 
 struct Ctx {

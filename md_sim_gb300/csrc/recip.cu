@@ -308,6 +308,8 @@ int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const 
     ks.kvec = (int3*)dalloc(c, sizeof(int3) * nk1);
     ks.witem_row = (int*)dalloc(c, sizeof(int) * nw1);
     ks.witem_n0 = (int*)dalloc(c, sizeof(int) * nw1);
+    ks.h_row = rows;
+    ks.h_nlen = nlen;
     if (ks.nk > 0) {
         MDG_CUDA(cudaMemcpy(ks.row, rows.data(), sizeof(int4) * ks.nrow, cudaMemcpyHostToDevice));
         MDG_CUDA(cudaMemcpy(ks.row_nlen, nlen.data(), sizeof(int) * ks.nrow, cudaMemcpyHostToDevice));

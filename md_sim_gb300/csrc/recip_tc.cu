@@ -205,17 +205,39 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
         // this thread's table entries (the same every group): e^{i m ty} items, q e^{i l tx} items,
         // and B items (n, atom pair)
         const int nm_items = kGA * NM, nl_items = kGA * nl, nb_items = d.NN * (kGA / 2);
-        int im_j[kMaxItems], im_m[kMaxItems], il_j[kMaxItems], il_l[kMaxItems], ib_n[kMaxItems], ib_j[kMaxItems];
+        // items packed as (atom << 16) | index, -1 when the thread has no such item
+        int im_i[kMaxItems], il_i[kMaxItems], ib_i[kMaxItems];
 #pragma unroll
         for (int k = 0; k < kMaxItems; ++k) {
             const int e = t + k * kProd;
-            im_j[k] = e < nm_items ? e / NM : -1;
-            im_m[k] = e < nm_items ? e % NM : 0;
-            il_j[k] = e < nl_items ? e / nl : -1;
-            il_l[k] = e < nl_items ? e % nl : 0;
-            ib_j[k] = e < nb_items ? (e / d.NN) * 2 : -1;
-            ib_n[k] = e < nb_items ? e % d.NN : 0;
+            im_i[k] = e < nm_items ? ((e / NM) << 16) | (e % NM) : -1;
+            il_i[k] = e < nl_items ? ((e / nl) << 16) | (e % nl) : -1;
+            ib_i[k] = e < nb_items ? (((e / d.NN) * 2) << 16) | (e % d.NN) : -1;
         }
+#define IM_J(k) (im_i[k] >> 16)
+#define IM_M(k) (im_i[k] & 0xffff)
+#define IL_J(k) (il_i[k] >> 16)
+#define IL_L(k) (il_i[k] & 0xffff)
+#define IB_J(k) (ib_i[k] >> 16)
+#define IB_N(k) (ib_i[k] & 0xffff)
+        // the atom fractions this thread's items need, loaded one group ahead so that the global
+        // load latency overlaps the barrier and the A fill of the current group
+        uint32_t pm[kMaxItems], plx[kMaxItems], plq[kMaxItems], pb0[kMaxItems], pb1[kMaxItems];
+        auto prefetch = [&](int gb) {
+#pragma unroll
+            for (int k = 0; k < kMaxItems; ++k) {
+                pm[k] = (im_i[k] >= 0 && gb + IM_J(k) < a1) ? __ldg(&atoms[gb + IM_J(k)].y) : 0u;
+                plx[k] = plq[k] = 0u;
+                if (il_i[k] >= 0 && gb + IL_J(k) < a1) {
+                    const uint4 rec = __ldg(&atoms[gb + IL_J(k)]);
+                    plx[k] = rec.x;
+                    plq[k] = rec.w;
+                }
+                pb0[k] = (ib_i[k] >= 0 && gb + IB_J(k) < a1) ? __ldg(&atoms[gb + IB_J(k)].z) : 0u;
+                pb1[k] = (ib_i[k] >= 0 && gb + IB_J(k) + 1 < a1) ? __ldg(&atoms[gb + IB_J(k) + 1].z) : 0u;
+            }
+        };
+        if (ngroup > 0) prefetch(a0);
         for (int g = 0; g < ngroup; ++g) {
             const int s = g % kS;
             const int gb = a0 + g * kGA;
@@ -228,30 +250,29 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
             if (ok) {
 #pragma unroll
                 for (int k = 0; k < kMaxItems; ++k) {
-                    if (im_j[k] >= 0) {
-                        const int at = gb + im_j[k];
+                    if (im_i[k] >= 0) {
+                        const int at = gb + IM_J(k);
                         float c = 0.f, sn = 0.f;
-                        if (at < a1) phase((uint32_t)(im_m[k] - KM) * __ldg(&atoms[at].y), c, sn);
-                        tm[im_j[k] * NM1 + im_m[k]] = make_float2(c, sn);
+                        if (at < a1) phase((uint32_t)(IM_M(k) - KM) * pm[k], c, sn);
+                        tm[IM_J(k) * NM1 + IM_M(k)] = make_float2(c, sn);
                     }
-                    if (il_j[k] >= 0) {
-                        const int at = gb + il_j[k];
+                    if (il_i[k] >= 0) {
+                        const int at = gb + IL_J(k);
                         float c = 0.f, sn = 0.f;
                         if (at < a1) {
-                            const uint4 rec = __ldg(&atoms[at]);
-                            phase((uint32_t)(il_l[k] + l_lo) * rec.x, c, sn);
-                            const float q = __uint_as_float(rec.w);
+                            phase((uint32_t)(IL_L(k) + l_lo) * plx[k], c, sn);
+                            const float q = __uint_as_float(plq[k]);
                             c *= q;
                             sn *= q;
                         }
-                        tl[il_j[k] * kMaxNL + il_l[k]] = make_float2(c, sn);
+                        tl[IL_J(k) * kMaxNL + IL_L(k)] = make_float2(c, sn);
                     }
-                    if (ib_j[k] >= 0) {
-                        const int jp = ib_j[k], ni = ib_n[k];
+                    if (ib_i[k] >= 0) {
+                        const int jp = IB_J(k), ni = IB_N(k);
                         const uint32_t n = (uint32_t)(ni - d.KN);
                         float c0 = 0.f, s0 = 0.f, c1 = 0.f, s1 = 0.f;
-                        if (gb + jp < a1) phase(n * __ldg(&atoms[gb + jp].z), c0, s0);
-                        if (gb + jp + 1 < a1) phase(n * __ldg(&atoms[gb + jp + 1].z), c1, s1);
+                        if (gb + jp < a1) phase(n * pb0[k], c0, s0);
+                        if (gb + jp + 1 < a1) phase(n * pb1[k], c1, s1);
                         uint32_t ch, cl, sh, sl;
                         split2(c0, c1, ch, cl);
                         split2(s0, s1, sh, sl);
@@ -268,6 +289,7 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
                     }
                 }
             }
+            if (g + 1 < ngroup) prefetch(gb + kGA);
             if (!producers_all<kProd>(ok)) {
                 alive = false;
                 break;
@@ -296,6 +318,12 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
             tc::fence_async_smem();
             tc::mbar_arrive(tc::smem_u32(&full[s]));
         }
+#undef IM_J
+#undef IM_M
+#undef IL_J
+#undef IL_L
+#undef IB_J
+#undef IB_N
         // all MMAs done -> accumulators to the partial-sum buffer
         if (ngroup > 0 && alive)
             alive = tc::mbar_wait_warp(tc::smem_u32(&empty[(ngroup - 1) % kS]), ((ngroup - 1) / kS) & 1, err, 13);
@@ -364,32 +392,37 @@ __global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit,
 }
 
 // ---------------------------------------------------------------------------------------------
-// C(k) packed as the pass-2 B operand: chunk c holds rows kRC c .. kRC c + kRC - 1, columns
-// col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part; one thread
-// per (chunk, K step, column, n) writes the (part 0, part 1) half pairs of hi and lo.
+// C(k) packed as the pass-2 B operand.  Pass 2 takes the rows sorted by the K steps their n range
+// covers (row2, nlen2), so that chunk c (rows kRC c .. kRC c + kRC - 1 of that order) multiplies
+// only the K steps ks_lo .. ks_lo + nks - 1 its rows use (chunk2[c] = image byte offset, ks_lo,
+// nks).  Columns col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part;
+// the image of a chunk is [hi | lo][nks] tiles of N x 16.  One thread per (K step, column, n).
 // ---------------------------------------------------------------------------------------------
 constexpr int kRC = 32;                 // rows per pass-2 chunk
 constexpr int kNC2 = 4 * kRC;           // pass-2 MMA N
 constexpr uint32_t kTile2 = kNC2 * 32;  // one N x 16 B tile (bytes)
 
 __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restrict__ rows,
-                            const int* __restrict__ nlen, TcDims d, unsigned char* img, const float* cmax) {
+                            const int* __restrict__ nlen, const int4* __restrict__ chunks, TcDims d,
+                            unsigned char* img, const float* cmax) {
     const float inv = cmax[0] > 0.f ? 1.0f / cmax[0] : 1.0f;
-    const long total = (long)d.nchunk2 * d.KS * kNC2 * 8;
-    const long chunkBytes = 2L * d.KS * kTile2;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-        const int i8 = (int)(e & 7);
-        const int col = (int)((e >> 3) % kNC2);
-        const long rest = (e >> 3) / kNC2;
-        const int ks = (int)(rest % d.KS);
-        const int c = (int)(rest / d.KS);
+    const int c = blockIdx.y;
+    const int4 ch = chunks[c];
+    const int nks = ch.z;
+    const int total = nks * kNC2 * 8;
+    unsigned char* base = img + ch.x;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int i8 = e & 7;
+        const int col = (e >> 3) % kNC2;
+        const int ksl = (e >> 3) / kNC2;
         const int row = c * kRC + (col >> 2), tt = (col >> 1) & 1, comp = col & 1;
-        const int ni = ks * 8 + i8;
+        const int ni = (ch.y + ksl) * 8 + i8;
         float v0 = 0.f, v1 = 0.f;
-        if (row < d.nrow && ni < d.NN) {
+        const int nl = nlen[row];
+        if (nl > 0 && ni < d.NN) {
             const int4 rw = rows[row];
             const int n = ni - d.KN;
-            if (n >= rw.z && n < rw.z + nlen[row]) {
+            if (n >= rw.z && n < rw.z + nl) {
                 const float2 cv = Cf[rw.w + n - rw.z];
                 const float sc = (tt ? (float)n : 1.0f) * inv;
                 const float cr = cv.x * sc, ci = cv.y * sc;
@@ -399,10 +432,9 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
         }
         uint32_t hi, lo;
         split2(v0, v1, hi, lo);
-        unsigned char* base = img + c * chunkBytes;
         const uint32_t off = tc::tile_off(col, 2 * i8);
-        *reinterpret_cast<uint32_t*>(base + (0 * d.KS + ks) * kTile2 + off) = hi;
-        *reinterpret_cast<uint32_t*>(base + (1 * d.KS + ks) * kTile2 + off) = lo;
+        *reinterpret_cast<uint32_t*>(base + ksl * kTile2 + off) = hi;
+        *reinterpret_cast<uint32_t*>(base + (nks + ksl) * kTile2 + off) = lo;
     }
 }
 
@@ -419,10 +451,10 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
 // (recomputed by __sincosf at rows flagged in the shared row table: every 8th row and each change
 // of l).
 // ---------------------------------------------------------------------------------------------
-constexpr int kT2 = 256;  // epilogue warps 0-3, issuer warp 4, warps 5-7 help build A
+constexpr int kT2 = 288;  // epilogue warps 0-7 (two per TMEM lane quarter, one per half chunk), issuer warp 8
 
 struct P2Layout {
-    uint32_t a_bytes, img, off_a, off_b, off_rows, total;
+    uint32_t a_bytes, img, off_a, off_b, off_rows, off_red, total;
 };
 
 __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
@@ -432,14 +464,15 @@ __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
     L.off_a = 1024;
     L.off_b = L.off_a + L.a_bytes;
     L.off_rows = L.off_b + nst * L.img;
-    L.total = L.off_rows + nrow_pad * 16;      // (float l, float m, l | restart << 31, m)
+    L.off_red = L.off_rows + nrow_pad * 16;    // rows: (float l, float m, l | restart << 31, m)
+    L.total = L.off_red + 3 * 128 * 4;         // second-half force partials of the 128 atoms
     return L;
 }
 
 __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
                                                      const unsigned char* __restrict__ img,
-                                                     const int4* __restrict__ rows, TcDims d, const float* cmax,
-                                                     double* __restrict__ frc) {
+                                                     const int4* __restrict__ rows, const int4* __restrict__ chunks,
+                                                     TcDims d, const float* cmax, double* __restrict__ frc) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC, d.nst2);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -455,7 +488,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(tc::smem_u32(&full[b]), 1);
             tc::mbar_init(tc::smem_u32(&mdone[b]), 1);
-            tc::mbar_init(tc::smem_u32(&afree[b]), 4);
+            tc::mbar_init(tc::smem_u32(&afree[b]), 8);
         }
         tc::mbar_fence_init();
     }
@@ -469,8 +502,8 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
         rlm[r] = make_float4((float)rw.x, (float)rw.y, __int_as_float(rw.x | (restart << 31)), __int_as_float(rw.y));
     }
     if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 256);
-    // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part
-    {
+    // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part (warps 0-7, half of K each)
+    if (t < 256) {
         const int mrow = t & 127, half = t >> 7;
         const int at = atom0 + mrow;
         const uint32_t uz = at < v.nmove ? atoms[at].z : 0u;
@@ -498,19 +531,20 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    if (warp == 4) {
+    if (warp == 8) {
         if (lane == 0) {
             const uint32_t idesc = idesc_e(128, kNC2);
             const uint32_t bbase = tc::smem_u32(sm + L.off_b);
             const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(bbase);
-            const uint32_t half = L.img / 2;
             const bool two = d.nst2 == 2;
             auto copy = [&](int c) {
                 const int s = two ? (c & 1) : 0;
+                const int4 ch = chunks[c];
+                const uint32_t bytes = (uint32_t)ch.z * kTile2;  // hi half, then lo half
                 const uint32_t fb = tc::smem_u32(&full[s]);
-                tc::mbar_expect_tx(fb, L.img);
-                tc::bulk_g2s(bbase + s * L.img, img + (size_t)c * L.img, half, fb);
-                tc::bulk_g2s(bbase + s * L.img + half, img + (size_t)c * L.img + half, half, fb);
+                tc::mbar_expect_tx(fb, 2 * bytes);
+                tc::bulk_g2s(bbase + s * L.img, img + ch.x, bytes, fb);
+                tc::bulk_g2s(bbase + s * L.img + bytes, img + ch.x + bytes, bytes, fb);
             };
             bool alive = true;
             if (NC > 0) copy(0);
@@ -524,10 +558,12 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 tc::fence_after();
                 const uint32_t dcol = tmem + s * kNC2;
                 const uint64_t dB = dB0 + (uint64_t)((sb * L.img) >> 4);
-                for (int ks = 0; ks < d.KS; ++ks) {
+                const int4 ch = chunks[c];
+                for (int ksl = 0; ksl < ch.z; ++ksl) {
+                    const int ks = ch.y + ksl;
                     const uint64_t ah = dA0 + (uint64_t)(ks * 256), al = dA0 + (uint64_t)((d.KS + ks) * 256);
-                    const uint64_t bh = dB + (uint64_t)(ks * (kTile2 >> 4)), bl = dB + (uint64_t)((d.KS + ks) * (kTile2 >> 4));
-                    tc::mma_bf16(dcol, ah, bh, idesc, ks > 0 ? 1u : 0u);
+                    const uint64_t bh = dB + (uint64_t)(ksl * (kTile2 >> 4)), bl = dB + (uint64_t)((ch.z + ksl) * (kTile2 >> 4));
+                    tc::mma_bf16(dcol, ah, bh, idesc, ksl > 0 ? 1u : 0u);
                     tc::mma_bf16(dcol, ah, bl, idesc, 1u);
                     tc::mma_bf16(dcol, al, bh, idesc, 1u);
                 }
@@ -544,8 +580,10 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             // on a timeout, let issued work drain (bounded) before the block frees its TMEM
             if (!alive && NC > 0) tc::mbar_wait(tc::smem_u32(&mdone[(NC - 1) & 1]), ((NC - 1) >> 1) & 1, nullptr, 0);
         }
-    } else if (warp < 4) {
-        const int at = atom0 + t;
+    } else {
+        // warp w reads TMEM lanes 32 (w & 3) .. + 31 (its atoms) and the half chunk w >> 2 (16 rows)
+        const int quad = warp & 3, hf = warp >> 2;
+        const int at = atom0 + quad * 32 + lane;
         const bool ok = at < v.nmove;
         const uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
         float dyc, dys;
@@ -557,17 +595,15 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             alive = tc::mbar_wait_warp(tc::smem_u32(&mdone[s]), (c >> 1) & 1, err, 24);
             if (!alive) break;
             tc::fence_after();
-            for (int hf = 0; hf < 2; ++hf) {
+            {
                 uint32_t raw[64];
 #pragma unroll
                 for (int cc = 0; cc < 4; ++cc)
-                    tc::tmem_ld16_nw(tmem + ((uint32_t)(warp * 32) << 16) + s * kNC2 + hf * 64 + cc * 16, raw + cc * 16);
+                    tc::tmem_ld16_nw(tmem + ((uint32_t)(quad * 32) << 16) + s * kNC2 + hf * 64 + cc * 16, raw + cc * 16);
                 tc::tmem_wait_ld();
-                if (hf == 1) {
-                    tc::fence_before();
-                    __syncwarp();
-                    if (lane == 0) tc::mbar_arrive(tc::smem_u32(&afree[s]));
-                }
+                tc::fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(tc::smem_u32(&afree[s]));
                 float ec = 0.f, es = 0.f;
 #pragma unroll
                 for (int rr = 0; rr < 16; ++rr) {
@@ -589,7 +625,19 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 }
             }
         }
-        if (ok) {  // each atom has one writer: plain stores (a timed-out block leaves zeros and its status)
+        // the second-half warps hand their partial sums to the first-half warps through shared memory
+        float* red = reinterpret_cast<float*>(sm + L.off_red);
+        const int ra = quad * 32 + lane;
+        if (hf == 1) {
+            red[ra] = alive ? fx : 0.f;
+            red[128 + ra] = alive ? fy : 0.f;
+            red[256 + ra] = alive ? fz : 0.f;
+        }
+        tc::named_sync(1, 256);
+        if (hf == 0 && ok) {  // each atom has one writer: plain stores (a timed-out block leaves zeros and its status)
+            fx += red[ra];
+            fy += red[128 + ra];
+            fz += red[256 + ra];
             const double q = alive ? (double)__uint_as_float(rec.w) * (double)cmax[0] : 0.0;
             frc[at] = q * (double)d.px * (double)fx;
             frc[v.nmove + at] = q * (double)d.py * (double)fy;
@@ -714,8 +762,50 @@ int recip_tc_setup(Ctx& c) {
     p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC, p.nst2).total;
     if (p.smem2 > 227 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
+    // pass-2 row order: rows sorted by the K steps of their n range, so that a chunk of kRC rows
+    // runs only the K steps its rows need (the n range shrinks towards the edge of the k sphere)
+    {
+        const int nr = ks.nrow, nrp = p.nchunk2 * kRC;
+        std::vector<int> klo(nr), khi(nr), order(nr);
+        for (int r = 0; r < nr; ++r) {
+            const int n0 = ks.h_row[r].z, n1 = n0 + ks.h_nlen[r] - 1;
+            klo[r] = (2 * (n0 + p.KN)) / 16;
+            khi[r] = (2 * (n1 + p.KN) + 1) / 16;
+            order[r] = r;
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            const int wa = khi[a] - klo[a], wb = khi[b] - klo[b];
+            return wa != wb ? wa > wb : klo[a] < klo[b];
+        });
+        std::vector<int4> row2(nrp, make_int4(0, 0, 0, 0)), chunk2(p.nchunk2);
+        std::vector<int> nlen2(nrp, 0);
+        size_t off = 0;
+        for (int cc = 0; cc < p.nchunk2; ++cc) {
+            int lo = 1 << 30, hi = -1;
+            for (int k = cc * kRC; k < std::min(nr, (cc + 1) * kRC); ++k) {
+                const int r = order[k];
+                row2[k] = ks.h_row[r];
+                nlen2[k] = ks.h_nlen[r];
+                lo = std::min(lo, klo[r]);
+                hi = std::max(hi, khi[r]);
+            }
+            const int nks = hi - lo + 1;
+            chunk2[cc] = make_int4((int)off, lo, nks, 0);
+            off += (size_t)2 * nks * kTile2;
+        }
+        p.img_bytes = off;
+        p.row2 = (int4*)dalloc(c, sizeof(int4) * std::max(nrp, 1));
+        p.nlen2 = (int*)dalloc(c, sizeof(int) * std::max(nrp, 1));
+        p.chunk2 = (int4*)dalloc(c, sizeof(int4) * std::max(p.nchunk2, 1));
+        if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
+        if (nrp > 0) {
+            MDG_CUDA(cudaMemcpy(p.row2, row2.data(), sizeof(int4) * nrp, cudaMemcpyHostToDevice));
+            MDG_CUDA(cudaMemcpy(p.nlen2, nlen2.data(), sizeof(int) * nrp, cudaMemcpyHostToDevice));
+            MDG_CUDA(cudaMemcpy(p.chunk2, chunk2.data(), sizeof(int4) * p.nchunk2, cudaMemcpyHostToDevice));
+        }
+    }
     c.d_tc_atoms = (uint4*)dalloc(c, sizeof(uint4) * std::max(v.nmove, 1));
-    c.d_tc_img = (unsigned char*)dalloc(c, (size_t)std::max(p.nchunk2, 1) * 2 * p.KS * kTile2);
+    c.d_tc_img = (unsigned char*)dalloc(c, std::max<size_t>(p.img_bytes, 16));
     c.d_tc_cmax = (float*)dalloc(c, sizeof(float) * 4);
     c.d_tc_part = (float*)dalloc(c, sizeof(float) * std::max<size_t>(part_max, 1));
     c.d_tc_cf = (float2*)dalloc(c, sizeof(float2) * std::max(ks.nk, 1));
@@ -745,11 +835,11 @@ void recip_tc(Ctx& c) {
     const long nred = (long)ks.nrow * p.NN;
     k_tc_sreduce<<<(int)std::min<long>((nred + 255) / 256, 152 * 4), 256, 0, c.stream>>>(
         v, c.d_tc_part, p.nsplit1, p.rtot, d, ks.row, ks.row_nlen, ks.ak, ks.qw, ks.s, ks.c, c.d_tc_cf, c.d_tc_cmax);
-    const long total = (long)p.nchunk2 * p.KS * kNC2 * 8;
-    k_tc_prep_c<<<(int)std::min<long>((total + 255) / 256, 152 * 8), 256, 0, c.stream>>>(c.d_tc_cf, ks.row, ks.row_nlen,
-                                                                                         d, c.d_tc_img, c.d_tc_cmax);
-    k_tc_force<<<(v.nmove + 127) / 128, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, ks.row, d, c.d_tc_cmax,
-                                                                  c.d_frc);
+    const int per_chunk = p.KS * kNC2 * 8;  // elements of the widest chunk image
+    k_tc_prep_c<<<dim3((per_chunk + 255) / 256, p.nchunk2), 256, 0, c.stream>>>(c.d_tc_cf, p.row2, p.nlen2, p.chunk2, d,
+                                                                               c.d_tc_img, c.d_tc_cmax);
+    k_tc_force<<<(v.nmove + 127) / 128, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, p.row2, p.chunk2, d,
+                                                                  c.d_tc_cmax, c.d_frc);
 }
 
 int umma_selftest(int n, int k, const float* a, const float* b, float* dout, std::string& err) {

@@ -170,5 +170,10 @@ __device__ __forceinline__ void split(float x, __half& hi, __half& lo) {
     lo = __float2half_rn(x - __half2float(hi));
 }
 
+// bar.sync on a named barrier for the first n threads that use it (n a multiple of 32)
+__device__ __forceinline__ void named_sync(int id, int n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
 }  // namespace tc
 }  // namespace mdg
