@@ -332,7 +332,7 @@ def gpu_arm(args):
         cmp64["speedup"] = value / cmp64["value"]
 
     # ---------------- e2e through the drop-in ABI with pinned host buffers
-    e2e = e2e_arm(lib, s, prm, args, torch)
+    e2e = e2e_arm(lib, s_start, prm, args, torch)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup,

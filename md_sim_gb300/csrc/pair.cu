@@ -196,7 +196,9 @@ __global__ void __launch_bounds__(kNT) k_wall_fp64(View v) {
     const int lane = threadIdx.x & 31;
     const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * kWarps;
-    EAcc e;
+    // energy sums per wall site type (the last two site types alternate from partner to partner)
+    EAcc ew[2];
+    const int wt0 = v.nit - 2;
     double ws[6] = {0, 0, 0, 0, 0, 0};  // [sgn<0: x,y,z][sgn>0: x,y,z]
     for (int h = warp; h < v.nheads; h += nwarps) {
         const int i = v.head_atom[h];
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kNT) k_wall_fp64(View v) {
                 }
                 fij = 0.0;
             }
-            e_add(e, ijt, elj, eqq, s_e, v.nijt);
+            e_add(ew[min(max(v.type[j] - wt0, 0), 1)], ijt, elj, eqq, s_e, v.nijt);
         }
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -274,7 +276,8 @@ __global__ void __launch_bounds__(kNT) k_wall_fp64(View v) {
             }
         }
     }
-    e_final(e, s_e, v.nijt);
+    e_final(ew[0], s_e, v.nijt);
+    e_final(ew[1], s_e, v.nijt);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const double s = warp_sum(ws[k]);

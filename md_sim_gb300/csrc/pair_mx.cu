@@ -12,11 +12,13 @@
 //   tc[a]  uint4  fixed-point fractions of x, y, z and the charge, for the tensor-core reciprocal
 //                 sum of the same evaluation (recip_tc.cu)
 // k_pair_mx walks the same per-head half lists as the FP64 kernel (one warp per head): i-side
-// site forces in compensated FP32 sums per lane, warp-reduced once per head; j-side site forces
-// per pair; both leave as one vector FP32 reduction (red.global.add.v4.f32) per site into F,
-// which k_merge_f adds into the FP64 forces (and clears) after the loop.  k_wall_mx does the
-// head-wall loop (src/forcem.f90:418-498) the same way, with the wall reaction sums in
-// compensated FP32.  Neither loop issues FP64 instructions (the FP64 pipe of GB300 is narrow).
+// site forces in FP32 sums per lane (a lane holds ~n/32 partners), warp-reduced once per head;
+// j-side site forces per pair; both leave as one vector FP32 reduction (red.global.add.v4.f32)
+// per site into F, which k_merge_f adds into the FP64 forces (and clears) after the loops.
+// Energies per lane are compensated FP32 sums.  k_wall_mx does the head-wall loop
+// (src/forcem.f90:418-498) the same way over (head, segment) work items, with the wall reaction
+// sums of each item added into FP64 per lane.  The pair loops issue no FP64 instructions (the
+// FP64 pipe of GB300 is narrow).
 #include <algorithm>
 
 #include "common.cuh"
@@ -224,7 +226,8 @@ __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
         float4 si[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) si[a] = a < nsi_i ? pk.Q[i + a] : make_float4(0.f, 0.f, 0.f, 0.f);
-        Kahan fix[3], fiy[3], fiz[3];
+        // i-side sums: a lane holds about n / 32 partners of the head, few enough for plain FP32
+        float fix[3] = {0, 0, 0}, fiy[3] = {0, 0, 0}, fiz[3] = {0, 0, 0};
         const int n = v.nbcnt[h];
         const int* nb = v.nb + (size_t)h * v.maxnb;
         for (int k = lane; k < n; k += 32) {
@@ -250,7 +253,7 @@ __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
             float eqq = erfc_as(alfa * rij, &ff, spii) * auxq;
             fij = fij + ff * auxq * rsqi;
             float fjx[3], fjy[3], fjz[3];
-            fix[0].add(xio * fij); fiy[0].add(yio * fij); fiz[0].add(zio * fij);
+            fix[0] = fmaf(xio, fij, fix[0]); fiy[0] = fmaf(yio, fij, fiy[0]); fiz[0] = fmaf(zio, fij, fiz[0]);
             fjx[0] = -xio * fij; fjy[0] = -yio * fij; fjz[0] = -zio * fij;
 #pragma unroll
             for (int b = 1; b < 3; ++b) fjx[b] = fjy[b] = fjz[b] = 0.f;
@@ -271,7 +274,7 @@ __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
                     float fq;
                     eqq += erfc_as(alfa * rr, &fq, spii) * au;
                     const float fs = fq * au * (ri * ri);
-                    fix[a].add(xd * fs); fiy[a].add(yd * fs); fiz[a].add(zd * fs);
+                    fix[a] = fmaf(xd, fs, fix[a]); fiy[a] = fmaf(yd, fs, fiy[a]); fiz[a] = fmaf(zd, fs, fiz[a]);
                     fjx[b] -= xd * fs; fjy[b] -= yd * fs; fjz[b] -= zd * fs;
                 }
             }
@@ -285,7 +288,7 @@ __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             if (a >= nsi_i) break;
-            const float sx = warp_sumf(fix[a].valuef()), sy = warp_sumf(fiy[a].valuef()), sz = warp_sumf(fiz[a].valuef());
+            const float sx = warp_sumf(fix[a]), sy = warp_sumf(fiy[a]), sz = warp_sumf(fiz[a]);
             if (lane == 0) red_v4(&pk.F[i + a], sx, sy, sz);
         }
     }
@@ -303,10 +306,14 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
     const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * kWarps;
     const float alfa = (float)v.alfa, spii = (float)v.spii, facq = (float)v.facq, rcutsq = (float)v.rcutsq;
-    EAcc e;
-    Kahan ws[6];
+    // energy sums per wall site type (the last two site types): the two alternate from partner to
+    // partner, and one accumulator per type avoids a flush on every change
+    EAcc ew[2];
+    const int wt0 = v.nit - 2;
+    double ws[6] = {0, 0, 0, 0, 0, 0};  // wall reaction sums of this lane, added per work item
     // work items: (head, segment of kWSeg wall partners), so that the few heads next to a wall
-    // with hundreds of partners are shared by several warps
+    // with hundreds of partners are shared by several warps.  A lane sees at most kWSeg / 32
+    // partners per item, so its FP32 sums within an item are short and need no compensation.
     const int nseg = (v.maxwnb + kWSeg - 1) / kWSeg;
     const long nitems = (long)v.nheads * nseg;
     for (long item = warp; item < nitems; item += nwarps) {
@@ -322,7 +329,7 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
         float4 si[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) si[a] = a < nsi_i ? pk.Q[i + a] : make_float4(0.f, 0.f, 0.f, 0.f);
-        Kahan fix[3], fiy[3], fiz[3];
+        float fix[3] = {0, 0, 0}, fiy[3] = {0, 0, 0}, fiz[3] = {0, 0, 0}, wsi[6] = {0, 0, 0, 0, 0, 0};
         const int* nb = v.wnb + (size_t)h * v.maxwnb;
         for (int k = seg * kWSeg + lane; k < n; k += 32) {
             const int j = nb[k];
@@ -350,25 +357,31 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
                 float fq;
                 eqq += erfc_as(alfa * rr, &fq, spii) * au;
                 fij = fij + fq * au * (ri * ri);
-                fix[a].add(xd * fij); fiy[a].add(yd * fij); fiz[a].add(zd * fij);
+                fix[a] = fmaf(xd, fij, fix[a]);
+                fiy[a] = fmaf(yd, fij, fiy[a]);
+                fiz[a] = fmaf(zd, fij, fiz[a]);
                 if (book) {
-                    ws[so].add(-xd * fij); ws[so + 1].add(-yd * fij); ws[so + 2].add(-zd * fij);
+                    wsi[so] -= xd * fij; wsi[so + 1] -= yd * fij; wsi[so + 2] -= zd * fij;
                 }
                 fij = 0.f;
             }
-            e_add(e, ijt, elj, eqq, s_e, v.nijt);
+            e_add(ew[min(max(jt - wt0, 0), 1)], ijt, elj, eqq, s_e, v.nijt);
         }
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             if (a >= nsi_i) break;
-            const float sx = warp_sumf(fix[a].valuef()), sy = warp_sumf(fiy[a].valuef()), sz = warp_sumf(fiz[a].valuef());
+            const float sx = warp_sumf(fix[a]), sy = warp_sumf(fiy[a]), sz = warp_sumf(fiz[a]);
             if (lane == 0) red_v4(&pk.F[i + a], sx, sy, sz);
         }
+        if (book)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) ws[k] += (double)wsi[k];
     }
-    e_final(e, s_e, v.nijt);
+    e_final(ew[0], s_e, v.nijt);
+    e_final(ew[1], s_e, v.nijt);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        const double s = warp_sum(ws[k].value());
+        const double s = warp_sum(ws[k]);
         if (lane == 0 && s != 0.0) atomicAdd(&s_e[2 * v.nijt + k], s);
     }
     __syncthreads();
