@@ -347,21 +347,35 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
 }
 
 // Split-K reduction of pass 1 fused with the energy (src/forcem.f90:880-885,917), C(k) = Ak
-// conj(S + S_wall) and the scale max |C| max(1, |n|) of the pass-2 operand.  One thread per
-// (row, n); partial sums added in compensated FP32 (nsplit values), the result kept in FP64.
-__global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit, int rtot, TcDims d,
-                             const int4* __restrict__ rows, const int* __restrict__ nlen, const double* __restrict__ ak,
-                             const double2* __restrict__ qw, double2* S, double2* C, float2* Cf, float* cmax) {
-    double ew = 0.0, ll = 0.0;
-    float mx = 0.f;
+// conj(S + S_wall) and the scale max |C| max(1, |n|) of the pass-2 operand.  A block takes 32
+// consecutive (row, n) entries (row fastest, so each warp's loads are coalesced); warp g adds the
+// partial sums of splits g, g + 8, ... in compensated FP32, and the eight partials are combined
+// in a fixed order (deterministic), the result kept in FP64.
+constexpr int kRedG = 8;
+__global__ void __launch_bounds__(32 * kRedG) k_tc_sreduce(View v, const float* __restrict__ part, int nsplit,
+                                                          int rtot, TcDims d, const int4* __restrict__ rows,
+                                                          const int* __restrict__ nlen,
+                                                          const double* __restrict__ ak,
+                                                          const double2* __restrict__ qw, double2* S, double2* C,
+                                                          float2* Cf, float* cmax) {
+    __shared__ float4 sh[kRedG][32];
+    const int le = threadIdx.x & 31, g = threadIdx.x >> 5;
     const long total = (long)d.nrow * d.NN;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-        const int row = (int)(e % d.nrow), ni = (int)(e / d.nrow);
-        const int4 rw = rows[row];
-        const int n = ni - d.KN;
-        if (n < rw.z || n >= rw.z + nlen[row]) continue;
-        float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
-        for (int sp = 0; sp < nsplit; ++sp) {
+    const long e = (long)blockIdx.x * 32 + le;
+    bool valid = e < total;
+    int row = 0, ni = 0, n = 0;
+    int4 rw = make_int4(0, 0, 0, 0);
+    if (valid) {
+        row = (int)(e % d.nrow);
+        ni = (int)(e / d.nrow);
+        rw = rows[row];
+        n = ni - d.KN;
+        valid = n >= rw.z && n < rw.z + nlen[row];
+    }
+    float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+    if (valid) {
+#pragma unroll 4
+        for (int sp = g; sp < nsplit; sp += kRedG) {
             const float* pp = part + (size_t)sp * d.NP * rtot;
             const float xr = pp[(size_t)ni * rtot + row] - cr;
             const float tr = sr + xr;
@@ -372,23 +386,42 @@ __global__ void k_tc_sreduce(View v, const float* __restrict__ part, int nsplit,
             ci = (ti - si) - xi;
             si = ti;
         }
+    }
+    sh[g][le] = make_float4(sr, cr, si, ci);
+    __syncthreads();
+    double ew = 0.0, ll = 0.0;
+    float mx = 0.f;
+    if (g == 0 && valid) {
+        double dr = 0.0, di = 0.0;
+#pragma unroll
+        for (int q = 0; q < kRedG; ++q) {
+            const float4 p4 = sh[q][le];
+            dr += (double)p4.x - (double)p4.y;
+            di += (double)p4.z - (double)p4.w;
+        }
         const int k = rw.w + n - rw.z;
-        const double2 sv = make_double2((double)sr - (double)cr, (double)si - (double)ci);
+        const double2 sv = make_double2(dr, di);
         S[k] = sv;
         const double2 st = make_double2(sv.x + qw[k].x, sv.y + qw[k].y);
         const double a = ak[k];
-        ll += a * (sv.x * sv.x + sv.y * sv.y);
-        ew += a * (st.x * st.x + st.y * st.y);
+        ll = a * (sv.x * sv.x + sv.y * sv.y);
+        ew = a * (st.x * st.x + st.y * st.y);
         const double2 cv = make_double2(a * st.x, -a * st.y);
         C[k] = cv;
         Cf[k] = make_float2((float)cv.x, (float)cv.y);
         const float w = (float)max(1, abs(n));
-        mx = fmaxf(mx, fmaxf(fabsf((float)cv.x), fabsf((float)cv.y)) * w);
+        mx = fmaxf(fabsf((float)cv.x), fabsf((float)cv.y)) * w;
     }
-    block_atomic_sum<256>(ew, &v.acc[2 * v.nijt + ACC_UEWA]);
-    block_atomic_sum<256>(ll, &v.acc[2 * v.nijt + ACC_EWQLL]);
-    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned int*>(cmax), __float_as_uint(mx));
+    if (g == 0) {  // warp 0 holds the block's entries
+        ew = warp_sum(ew);
+        ll = warp_sum(ll);
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (le == 0) {
+            if (ew != 0.0) atomicAdd(&v.acc[2 * v.nijt + ACC_UEWA], ew);
+            if (ll != 0.0) atomicAdd(&v.acc[2 * v.nijt + ACC_EWQLL], ll);
+            atomicMax(reinterpret_cast<unsigned int*>(cmax), __float_as_uint(mx));
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -833,7 +866,7 @@ void recip_tc(Ctx& c) {
         k_tc_sfac<2><<<dim3(p.grid1x, p.nsplit1), P1<2>::kThreads, p.smem1, c.stream>>>(
             v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1);
     const long nred = (long)ks.nrow * p.NN;
-    k_tc_sreduce<<<(int)std::min<long>((nred + 255) / 256, 152 * 4), 256, 0, c.stream>>>(
+    k_tc_sreduce<<<(int)((nred + 31) / 32), 32 * kRedG, 0, c.stream>>>(
         v, c.d_tc_part, p.nsplit1, p.rtot, d, ks.row, ks.row_nlen, ks.ak, ks.qw, ks.s, ks.c, c.d_tc_cf, c.d_tc_cmax);
     const int per_chunk = p.KS * kNC2 * 8;  // elements of the widest chunk image
     k_tc_prep_c<<<dim3((per_chunk + 255) / 256, p.nchunk2), 256, 0, c.stream>>>(c.d_tc_cf, p.row2, p.nlen2, p.chunk2, d,
