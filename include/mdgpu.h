@@ -374,6 +374,42 @@ int mdg_measure_zero(mdg_ctx* ctx);
 int mdg_measure_do(mdg_ctx* ctx, const double* x0, const double* y0, const double* z0);
 int mdg_measure_get(mdg_ctx* ctx, mdg_measure_out* out);
 
+/* ---------------------------------------------------------------------------------------------
+ * Widom test-particle insertion of a water molecule (chempot, src/forcem.f90:1226-1507, set up by
+ * measure_init src/measure.f90:155-175).  Each insertion puts an O at a random point of the band
+ * lwmin < wall distance < lwmax (bin il of lchmax over the band), then tries 20 random
+ * orientations (1 when il <= ilmid) of the rigid 3-site probe (q -0.8476 / 0.4238, O-H 1 A,
+ * H-O-H from cos = -1/3) and adds exp(-u / RT) of each to pave(il), with u = real-space energy
+ * (vdW and Ewald erfc of the probe against every non-H-type site within rcut of the O) + the
+ * reciprocal term 0.5 Ak Re(sum_s q_s e^{ik.r_s} conj(S(k))) with S(k) of the last force
+ * evaluation + the wall long-range tail of the O.  inave(il) counts the tries.  Random numbers
+ * come from the reference's congruential generator (src/rndmod.f90:26-35), whose state *seed
+ * the call advances exactly as the reference does.
+ * Reference behaviour kept: an O position closer than 2.35 A to a water O (2 A to any other
+ * site) ends the whole call (src/forcem.f90:1342 exits the insertion loop), and the slab dipole
+ * term reads an uninitialised local (src/forcem.f90:1236,1477) and is left out.
+ * MDG_WIDOM_SKIP_OVERLAP skips such a position instead (its orientations still draw their random
+ * numbers, so the stream differs from the reference from that point on); MDG_WIDOM_EW3DC adds
+ * the slab dipole term -crf sum_s q_s z_s with crf of the last evaluation.  Slab variant only.
+ * ------------------------------------------------------------------------------------------- */
+#define MDG_WIDOM_SKIP_OVERLAP 1u
+#define MDG_WIDOM_EW3DC 2u
+typedef struct mdg_widom_params {
+    int64_t ichmax;   /* insertion positions per call */
+    double lwmin;     /* band of distances from the walls, A (tot.inp "lwmin lwmax") */
+    double lwmax;
+    int64_t lchmax;   /* bins over the band */
+    int64_t ilmid;    /* bins il > ilmid get 20 orientations, the others 1 */
+    double temper;    /* K; <= 0 selects 300 (src/measure.f90:169-174) */
+    uint32_t flags;   /* MDG_WIDOM_* */
+    int32_t pad;
+} mdg_widom_params;
+
+/* One chempot call on the positions and S(k) of the last force evaluation.  pave (lchmax) and
+ * inave (lchmax) are accumulated (+=); *seed is the generator state in and out; *done (may be
+ * NULL) receives the positions tried. */
+int mdg_widom(mdg_ctx* ctx, const mdg_widom_params* prm, double* seed, double* pave, int64_t* inave, int64_t* done);
+
 /* Diagnostic: one tcgen05 BF16 matrix product D (128 x n) = A (128 x k) . B^T (n x k) on the
  * device with the shared-memory operand layout of the tensor-core reciprocal sum (host arrays,
  * row-major floats rounded to BF16).  Lets a caller check the tensor-core path on its GPU. */

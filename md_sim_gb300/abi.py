@@ -165,6 +165,15 @@ class MeasureOut(C.Structure):
                 ("calls_do", C.c_int64), ("out_of_range", C.c_int64)]
 
 
+MDG_WIDOM_SKIP_OVERLAP = 1
+MDG_WIDOM_EW3DC = 2
+
+
+class WidomParams(C.Structure):
+    _fields_ = [("ichmax", C.c_int64), ("lwmin", C.c_double), ("lwmax", C.c_double), ("lchmax", C.c_int64),
+                ("ilmid", C.c_int64), ("temper", C.c_double), ("flags", C.c_uint32), ("pad", C.c_int32)]
+
+
 class Lib:
     """Binds the entry points of one shared library (`prefix` = 'mdg_' for the product)."""
 
@@ -211,6 +220,8 @@ class Lib:
             g("measure_zero", C.c_int, [C.c_void_p])
             g("measure_do", C.c_int, [C.c_void_p, DP, DP, DP])
             g("measure_get", C.c_int, [C.c_void_p, C.POINTER(MeasureOut)])
+        if self.has("widom"):
+            g("widom", C.c_int, [C.c_void_p, C.POINTER(WidomParams), DP, DP, I64P, I64P])
         if self.has("run"):
             g("set_state", C.c_int, [C.c_void_p, C.POINTER(Rigid), C.POINTER(State)])
             g("get_state", C.c_int, [C.c_void_p, C.POINTER(State)])
@@ -598,3 +609,24 @@ Context.measure_enable = _ctx_measure_enable
 Context.measure_zero = _ctx_measure_zero
 Context.measure_do = _ctx_measure_do
 Context.measure_get = _ctx_measure_get
+
+
+# ---------------------------------------------------------------------------------------------
+# Widom insertion (mdg_widom): chempot, src/forcem.f90:1226-1507.
+# ---------------------------------------------------------------------------------------------
+def _ctx_widom(self, ichmax: int, lwmin: float, lwmax: float, lchmax: int, ilmid: int, seed: float,
+               temper: float = 0.0, flags: int = 0, pave: Optional[np.ndarray] = None,
+               inave: Optional[np.ndarray] = None) -> Dict[str, object]:
+    """One chempot call on the last force evaluation; pave/inave accumulate (new zero arrays when
+    not given).  Returns the arrays, the generator state after the call and the positions tried."""
+    p = WidomParams(int(ichmax), float(lwmin), float(lwmax), int(lchmax), int(ilmid), float(temper), int(flags), 0)
+    pave = np.zeros(lchmax) if pave is None else pave
+    inave = np.zeros(lchmax, np.int64) if inave is None else inave
+    sd = C.c_double(float(seed))
+    done = C.c_int64(0)
+    self._check(self.lib.widom(self.h, C.byref(p), C.byref(sd), _dp(pave), inave.ctypes.data_as(I64P),
+                               C.byref(done)))
+    return {"pave": pave, "inave": inave, "seed": sd.value, "done": int(done.value)}
+
+
+Context.widom = _ctx_widom

@@ -86,13 +86,17 @@ __device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
 // The dynamic shared memory limit of a kernel is a property of the function, shared by every
 // context of the process: raise it to the device's opt-in maximum instead of one context's need,
 // so that a context created later with smaller tiles cannot lower it under an earlier one.
+// The kernel's static shared memory counts against the same limit.
 template <typename F>
 inline cudaError_t allow_max_smem(F* f) {
     int dev = 0, mx = 0;
     cudaGetDevice(&dev);
-    const cudaError_t e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaError_t e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, f);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - (int)fa.sharedSizeBytes);
 }
 
 }  // namespace mdg

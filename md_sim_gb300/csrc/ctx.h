@@ -200,6 +200,10 @@ struct Ctx {
     bool shake_model = false, shake_record = false;
     int pair_blocks = 0;          // blocks of the real-space loops (0: by head count); autotuned
     Meas meas;                    // measurement histograms (measure.cu)
+    int64_t widom_cap = 0;        // Widom insertion scratch (widom.cu)
+    double *d_widom_pos = nullptr, *d_widom_rot = nullptr, *d_widom_res = nullptr;
+    int* d_widom_n = nullptr;
+    bool widom_attr = false;
     std::vector<int> h_ang_mt;    // molecule type of each angle term
     int64_t nfreed = 0;
     // angles
@@ -278,6 +282,8 @@ void measure_force_intra(Ctx& c);  // after force_intra
 void measure_force_sum(Ctx& c);    // after force_sum
 void measure_do_launch(Ctx& c, const double* x, const double* y, const double* z);
 int measure_get(Ctx& c, mdg_measure_out* o);
+// widom.cu
+int widom(Ctx& c, const mdg_widom_params* p, double* seed, double* pave, int64_t* inave, int64_t* done);
 // shake.cu
 int shake_setup(Ctx& c, const mdg_sysdesc* s);
 void shake_launch(Ctx& c, const double* d_ft);

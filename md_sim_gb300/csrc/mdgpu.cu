@@ -1574,4 +1574,15 @@ int mdg_measure_get(mdg_ctx* cp, mdg_measure_out* o) {
     return measure_get(c, o);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Widom insertion (widom.cu)
+// ---------------------------------------------------------------------------------------------
+int mdg_widom(mdg_ctx* cp, const mdg_widom_params* prm, double* seed, double* pave, int64_t* inave, int64_t* done) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    MDG_CUDA(cudaStreamSynchronize(c.stream));
+    return widom(c, prm, seed, pave, inave, done);
+}
+
 }  // extern "C"

@@ -109,6 +109,10 @@ struct Ref {
     std::vector<std::vector<int64_t>> excl;  // constrained partners of surface atoms
     // reciprocal
     Meas ms;
+    // state of the last force evaluation that chempot reads (module arrays x0, rsx, Qsum)
+    std::vector<double> wx0, wy0, wz0, wrsx, wrsy, wrsz;
+    std::vector<cplx> wqsum;
+    double wdipz = 0.0;
     int64_t kmax, klmax, kmmax, knmax;
     double pipix, pipiy, pipiz;
     std::vector<int> kl_, km_, kn_;  // valid k in reference order
@@ -858,6 +862,7 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
             for (int64_t n = 1; n <= KN; ++n) EN(i, -n) = std::conj(EN(i, n));
         }
         const int64_t nk = (int64_t)r->Ak.size();
+        r->wqsum.assign(nk, cplx(0.0, 0.0));
         double ewqLL = 0.0;
 #ifdef _OPENMP
 #pragma omp parallel
@@ -879,6 +884,7 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
                     qll += elmn[i];
                 }
                 cplx qsum = qll + r->Qsumw1[k] + r->Qsumw2[k];
+                r->wqsum[k] = qsum;
                 const double akx = r->Ak[k];
                 tLL += (akx * qll * std::conj(qll)).real();
                 tew += akx * (qsum * std::conj(qsum)).real();
@@ -909,6 +915,7 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
         if (r->variant == MDG_SLAB) {  // EW3DC (src/forcem.f90:924-928)
             double dipz = 0.0;
             for (int64_t i = 0; i < nmove; ++i) dipz += r->qs[i] * z0[i];
+            r->wdipz = dipz;
             double crf = -2.0 * M_PI_R * r->lzi * r->lxi * r->lyi;
             urf = -crf * facq * dipz * dipz;
             crf = 2.0 * crf * facq * dipz;
@@ -1017,6 +1024,15 @@ int ref_force_get(RefCtx* r, const double* x0, const double* y0, const double* z
                     (rsx[2] * fy[j + 2] - rsy[2] * fx[j + 2]);
         }
     }
+    r->wx0.assign(x0, x0 + nmove);
+    r->wy0.assign(y0, y0 + nmove);
+    r->wz0.assign(z0, z0 + nmove);
+    r->wx0.insert(r->wx0.end(), r->wx.begin(), r->wx.end());
+    r->wy0.insert(r->wy0.end(), r->wy.begin(), r->wy.end());
+    r->wz0.insert(r->wz0.end(), r->wz.begin(), r->wz.end());
+    r->wrsx.assign(rsx, rsx + nmove);
+    r->wrsy.assign(rsy, rsy + nmove);
+    r->wrsz.assign(rsz, rsz + nmove);
     if (e) {
         double sumlj = 0.0, sumqq = 0.0;
         for (int64_t k = 0; k < nijt; ++k) {
@@ -1480,6 +1496,191 @@ int ref_measure_get(RefCtx* r, mdg_measure_out* o) {
     o->calls_force = m.calls_force;
     o->calls_do = m.calls_do;
     o->out_of_range = m.oor;
+    return MDG_OK;
+}
+
+// ---- chempot (src/forcem.f90:1226-1507) with the generator of src/rndmod.f90:26-35 ------------
+static double rnd(double& seed) {
+    seed = std::fmod(8192.0 * seed, 67099547.0);
+    return seed * 1.4903230270690e-8;
+}
+
+static double erfc_as(double alfar) {
+    const double t = 1.0 / (1.0 + PP * alfar);
+    const double exp2a = std::exp(-alfar * alfar);
+    return ((((A5 * t + A4) * t + A3) * t + A2) * t + A1) * t * exp2a;
+}
+
+int ref_widom(RefCtx* r, const mdg_widom_params* p, double* seed, double* pave, int64_t* inave, int64_t* done) {
+    if (r->variant != MDG_SLAB) return fail(r, MDG_E_UNSUPPORTED, "Widom insertion: slab variant only");
+    if (r->wx0.empty()) return fail(r, MDG_E_ARG, "Widom insertion: no force evaluation yet");
+    if (done) *done = 0;
+    // measure_init (src/measure.f90:151-155)
+    const double lwmin = r->lwh - p->lwmax, lwmax = r->lwh - p->lwmin;
+    const double facbin = 1.0 / (lwmax - lwmin) * (double)(float)p->lchmax;
+    const double chtemper = p->temper > 0.0 ? p->temper : 300.0;
+    const double aco = F(-0.333333f), asi = F(0.942809f);
+    const double rinsmin = 4.0, rwinsmin = (double)(2.35f * 2.35f);
+    const double qsw[3] = {F(-0.8476f), F(0.4238f), F(0.4238f)};
+    const double beta = 1000.0 / (PH_R * chtemper);
+    const double crf = (p->flags & MDG_WIDOM_EW3DC)
+                           ? 2.0 * (-2.0 * M_PI_R * r->lzi * r->lxi * r->lyi) * r->facq * r->wdipz : 0.0;
+    const std::vector<double>&x0 = r->wx0, &y0 = r->wy0, &z0 = r->wz0;
+    const int64_t ntota = r->ntota, KL = r->klmax, KM = r->kmmax, KN = r->knmax;
+    double sd = *seed;
+    int64_t n = 0;
+    std::vector<int64_t> iarr;
+    std::vector<double> xarr, yarr, zarr;
+    for (int64_t ic = 0; ic < p->ichmax; ++ic) {
+        const double oxr = (rnd(sd) - 0.5) * r->lx;
+        const double oyr = (rnd(sd) - 0.5) * r->ly;
+        double ozr;
+        do {
+            ozr = ((rnd(sd) - 0.5) * lwmax * 2.0);
+        } while (!(std::fabs(ozr) > lwmin));
+        const int64_t il = (int64_t)((std::fabs(ozr) - lwmin) * facbin) + 1;
+        if (il < 1 || il > p->lchmax) return fail(r, MDG_E_ARG, "Widom insertion: bin outside lchmax");
+        const int irot = il > p->ilmid ? 20 : 1;
+        inave[il - 1] += irot;
+        ++n;
+        // the O of the probe (src/forcem.f90:1278-1340)
+        double uchem = 0.0;
+        int pins = 1;
+        iarr.clear(); xarr.clear(); yarr.clear(); zarr.clear();
+        for (int64_t j = 0; j < ntota; ++j) {
+            if (r->itype[j] == 2) continue;
+            const double zio = ozr - z0[j];
+            if (std::fabs(zio) > r->rcut) continue;
+            const double xio = r->mx(oxr - x0[j]);
+            const double yio = r->my(oyr - y0[j]);
+            const double rsq = xio * xio + yio * yio + zio * zio;
+            if (rsq > r->rcutsq) continue;
+            const int64_t jt = r->itype[j];
+            const int ijt = r->ij(1, jt);
+            if (rsq < rwinsmin) {
+                if (jt == 1 || rsq < rinsmin) {
+                    pins = 0;
+                    break;
+                }
+            }
+            const double rsqi = 1.0 / rsq;
+            const double rij = std::sqrt(rsq);
+            if (r->vdwnum[ijt] == 1) {
+                const double r6 = r->sig[ijt] * pw3(rsqi);
+                uchem += r->eps[ijt] * r6 * (r6 - 1.0);
+            } else if (r->vdwnum[ijt] == 2) {
+                const double r6 = r->cc[ijt] * pw3(rsqi);
+                uchem += r->aa[ijt] * std::exp(-rij * r->rhoi[ijt]) - r6;
+            }
+            const double aux = r->facq * qsw[0] * r->qs[j] / rij;
+            uchem += erfc_as(r->alfa * rij) * aux;
+            iarr.push_back(j); xarr.push_back(xio); yarr.push_back(yio); zarr.push_back(zio);
+        }
+        const double uchemx = uchem;
+        if (pins == 0 && !(p->flags & MDG_WIDOM_SKIP_OVERLAP)) {
+            *seed = sd;
+            if (done) *done = n;
+            return MDG_OK;   // the reference leaves the insertion loop (src/forcem.f90:1342)
+        }
+        for (int ir = 0; ir < irot; ++ir) {
+            double h1[3], ri;
+            for (;;) {
+                h1[0] = rnd(sd) - 0.5;
+                h1[1] = rnd(sd) - 0.5;
+                h1[2] = rnd(sd) - 0.5;
+                ri = h1[0] * h1[0] + h1[1] * h1[1] + h1[2] * h1[2];
+                if (ri < 0.25 && ri > F(0.001f)) break;
+            }
+            ri = 1.0 / std::sqrt(ri);
+            for (double& hh : h1) hh = hh * ri;
+            ri = 1.0 / std::sqrt(h1[0] * h1[0] + h1[1] * h1[1]);
+            const double h2[3] = {-h1[1] * ri, h1[0] * ri, 0.0};
+            const double mr[3] = {h2[1] * h1[2] - h2[2] * h1[1], h2[2] * h1[0] - h2[0] * h1[2],
+                                  h2[0] * h1[1] - h2[1] * h1[0]};
+            const double alph = 2.0 * M_PI_R * rnd(sd);
+            const double cosa = std::cos(alph), sina = std::sin(alph);
+            double rins[3][3];
+            const double o[3] = {oxr, oyr, ozr};
+            for (int d = 0; d < 3; ++d) {
+                rins[0][d] = o[d];
+                rins[1][d] = o[d] + aco * h1[d] + asi * (cosa * h2[d] + sina * mr[d]);
+                rins[2][d] = o[d] + h1[d];
+            }
+            if (pins == 0) continue;  // skipped position: its orientations are drawn but not used
+            // real space (src/forcem.f90:1378-1423)
+            uchem = 0.0;
+            for (size_t k = 0; k < iarr.size(); ++k) {
+                const int64_t j = iarr[k];
+                const double xio = xarr[k], yio = yarr[k], zio = zarr[k];
+                const int64_t jt = r->itype[j];
+                if (jt == 1) {
+                    int64_t jmin = j + 1;
+                    for (int ix = 0; ix < 3; ++ix) {
+                        const double xi = xio + rins[ix][0] - oxr, yi = yio + rins[ix][1] - oyr,
+                                     zi = zio + rins[ix][2] - ozr;
+                        const double qx = r->facq * qsw[ix];
+                        for (int64_t jx = jmin; jx < j + r->nsi[jt - 1]; ++jx) {
+                            const double xd = xi - r->wrsx[jx], yd = yi - r->wrsy[jx], zd = zi - r->wrsz[jx];
+                            const double rsq = xd * xd + yd * yd + zd * zd;
+                            const double rij = std::sqrt(rsq);
+                            uchem += erfc_as(r->alfa * rij) * (qx * r->qs[jx] / rij);
+                        }
+                        jmin = j;
+                    }
+                } else {
+                    for (int ix = 1; ix < 3; ++ix) {
+                        const double xi = xio + rins[ix][0] - oxr, yi = yio + rins[ix][1] - oyr,
+                                     zi = zio + rins[ix][2] - ozr;
+                        const double qx = r->facq * qsw[ix];
+                        const double rsq = xi * xi + yi * yi + zi * zi;
+                        const double rij = std::sqrt(rsq);
+                        uchem += erfc_as(r->alfa * rij) * (qx * r->qs[j] / rij);
+                    }
+                }
+            }
+            uchem = uchem + uchemx;
+            // reciprocal space (src/forcem.f90:1428-1475)
+            std::vector<cplx> el(3 * (KL + 1)), em(3 * (2 * KM + 1)), en(3 * (2 * KN + 1));
+            auto EL = [&](int q, int64_t l) -> cplx& { return el[q * (KL + 1) + l]; };
+            auto EM = [&](int q, int64_t m) -> cplx& { return em[q * (2 * KM + 1) + m + KM]; };
+            auto EN = [&](int q, int64_t nn) -> cplx& { return en[q * (2 * KN + 1) + nn + KN]; };
+            for (int q = 0; q < 3; ++q) {
+                EL(q, 0) = EM(q, 0) = EN(q, 0) = cplx(1.0, 0.0);
+                EL(q, 1) = cplx(std::cos(r->pipix * rins[q][0]), std::sin(r->pipix * rins[q][0]));
+                EM(q, 1) = cplx(std::cos(r->pipiy * rins[q][1]), std::sin(r->pipiy * rins[q][1]));
+                EN(q, 1) = cplx(std::cos(r->pipiz * rins[q][2]), std::sin(r->pipiz * rins[q][2]));
+                for (int64_t l = 2; l <= KL; ++l) EL(q, l) = EL(q, l - 1) * EL(q, 1);
+                for (int64_t m = 2; m <= KM; ++m) EM(q, m) = EM(q, m - 1) * EM(q, 1);
+                for (int64_t m = 1; m <= KM; ++m) EM(q, -m) = std::conj(EM(q, m));
+                for (int64_t nn = 2; nn <= KN; ++nn) EN(q, nn) = EN(q, nn - 1) * EN(q, 1);
+                for (int64_t nn = 1; nn <= KN; ++nn) EN(q, -nn) = std::conj(EN(q, nn));
+            }
+            for (size_t k = 0; k < r->Ak.size(); ++k) {
+                const int kl = r->kl_[k], km = r->km_[k], kn = r->kn_[k];
+                cplx sum(0.0, 0.0);
+                for (int q = 0; q < 3; ++q) sum += (qsw[q] * EL(q, kl) * EM(q, km)) * EN(q, kn);
+                uchem += 0.5 * r->Ak[k] * (sum * std::conj(r->wqsum[k])).real();
+            }
+            uchem = uchem - crf * (qsw[0] * rins[0][2] + qsw[1] * rins[1][2] + qsw[2] * rins[2][2]);
+            // wall tail of the O (src/forcem.f90:1481-1494)
+            for (int j = -1; j <= 1; j += 2) {
+                const double dw = r->lwh - (double)j * rins[0][2];
+                if (dw < r->rcut) {
+                    uchem += r->ulr_w[0];
+                } else {
+                    uchem += r->ulr_l[0];
+                    const double dw3 = dw * dw * dw;
+                    uchem += (r->flr_lja[0] / (9.0 * (dw3 * dw3 * dw3)) - r->flr_ljc[0] / (3.0 * dw3));
+                    const double t = r->flr_bur[0];
+                    const double exp2a = r->flr_bua[0] * std::exp(-dw / t);
+                    uchem += (t * (2.0 * t + dw) * exp2a - r->flr_buc[0] / (3.0 * dw3));
+                }
+            }
+            pave[il - 1] += std::exp(-beta * uchem);
+        }
+    }
+    *seed = sd;
+    if (done) *done = n;
     return MDG_OK;
 }
 
