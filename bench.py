@@ -323,6 +323,7 @@ def gpu_arm(args):
     drift = None
     if args.drift > 0:
         drift = nve_drift(ctx, s, args.drift)
+    widom = widom_arm(ctx, s, args) if (args.widom > 0 and s.nwall > 0) else None
     ctx.close()
 
     # ---------------- the plain FP64 GPU form on the same start, and the force error against it
@@ -345,6 +346,7 @@ def gpu_arm(args):
         "e2e": e2e,
         "gpu_launches": int(kps * K),
         "tuning": tuning,
+        "widom": widom,
         "kernels_per_step": kps,
         "roofline": roof,
         "roofline_reciprocal": roof_recip,
@@ -474,6 +476,40 @@ def _tuning_summary(tunings):
     return {"choices": choice, "tc_atom_splits_min_max": [min(splits), max(splits)],
             "force_ms_sum_before": float(sum(t["ms_before"] for t in tunings)),
             "force_ms_sum_after": float(sum(t["ms_after"] for t in tunings))}
+
+
+def widom_arm(ctx, s, args):
+    """Widom insertions (chempot) on the context's last force evaluation: wall time per call on the
+    GPU (host clock around mdg_widom: generator on the host, one kernel, results back) and the CPU
+    restatement on a smaller count of the same positions."""
+    from md_sim_gb300 import abi
+
+    seed0 = 14135621772.0
+    band = (1.0, min(6.0, 0.45 * s.lw))
+    f = abi.MDG_WIDOM_SKIP_OVERLAP
+    ctx.widom(16, band[0], band[1], 8, 4, seed0, flags=f)  # warm-up: scratch and attributes
+    t0 = time.perf_counter()
+    r = ctx.widom(args.widom, band[0], band[1], 8, 4, seed0, flags=f)
+    t_gpu = time.perf_counter() - t0
+    out = {"insertions": args.widom, "band_A": list(band), "orientations": int(r["inave"].sum()),
+           "ms_per_call": t_gpu * 1e3, "orientations_per_s": r["inave"].sum() / t_gpu,
+           "flags": "skip overlapping positions"}
+    if args.cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import build as oracle_build
+
+        oracle_build.build()
+        lib = abi.Lib(oracle_build.path("libmdref_omp.so"), "ref_")
+        oc = abi.Context(lib, s.copy(), ctx.prm)
+        oc.force_get(s.copy())
+        n = max(8, args.widom // 50)
+        t0 = time.perf_counter()
+        rc = oc.widom(n, band[0], band[1], 8, 4, seed0, flags=f)
+        t_cpu = time.perf_counter() - t0
+        oc.close()
+        out["cpu_port"] = {"insertions": n, "orientations_per_s": rc["inave"].sum() / t_cpu, "threads": 1,
+                           "note": "the restatement of chempot is sequential, like the reference's"}
+    return out
 
 
 def nve_drift(ctx, s, nsteps, every=100):
@@ -671,6 +707,8 @@ def main():
     ap.add_argument("--drift", type=int, default=0, help="NVE energy drift over this many extra resident steps")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned SHAKE seed arm (workloads with SHAKE only)")
+    ap.add_argument("--widom", type=int, default=2000,
+                    help="Widom insertion positions timed on the final state (0 = skip; wall systems only)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch parameters instead of timing candidates (mdg_autotune)")
     ap.add_argument("--e2e-steps", type=int, default=60)
