@@ -84,73 +84,82 @@ __device__ __forceinline__ bool last_block(unsigned* done) {
     return last;
 }
 
+// All of a molecule's state is loaded before anything is stored: the arrays may alias as far as
+// the compiler knows, and loads issued back to back overlap their latency instead of queueing
+// behind the stores (the per-molecule work is short; memory latency, not FP64, bounds it).
 __device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, double* sc, double* sw) {
     const int nr = v.nrig;
-    {
-        double cx[3];
+    double C[5][3], W[5][3], Q[5][4];
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
-            double a0 = D.c[(0 * 3 + d) * nr + i], a1 = D.c[(1 * 3 + d) * nr + i], a2 = D.c[(2 * 3 + d) * nr + i],
-                   a3 = D.c[(3 * 3 + d) * nr + i];
-            gpred(a0, a1, a2, a3, D.c[(4 * 3 + d) * nr + i]);
-            D.c[(0 * 3 + d) * nr + i] = a0;
-            D.c[(1 * 3 + d) * nr + i] = a1;
-            D.c[(2 * 3 + d) * nr + i] = a2;
-            D.c[(3 * 3 + d) * nr + i] = a3;
-            sc[d] += a1 * a1;
-            cx[d] = a0;
+            C[k][d] = D.c[(k * 3 + d) * nr + i];
+            W[k][d] = D.w[(k * 3 + d) * nr + i];
         }
-        for (int d = 0; d < 3; ++d) {
-            double a0 = D.w[(0 * 3 + d) * nr + i], a1 = D.w[(1 * 3 + d) * nr + i], a2 = D.w[(2 * 3 + d) * nr + i],
-                   a3 = D.w[(3 * 3 + d) * nr + i];
-            gpred(a0, a1, a2, a3, D.w[(4 * 3 + d) * nr + i]);
-            D.w[(0 * 3 + d) * nr + i] = a0;
-            D.w[(1 * 3 + d) * nr + i] = a1;
-            D.w[(2 * 3 + d) * nr + i] = a2;
-            D.w[(3 * 3 + d) * nr + i] = a3;
-            sw[d] += a0 * a0;
-        }
-        double qq[4];
-        for (int cc = 0; cc < 4; ++cc) {
-            double* b = D.q + (cc * 5) * nr;
-            double a0 = b[i], a1 = b[nr + i], a2 = b[2 * nr + i], a3 = b[3 * nr + i];
-            gpred(a0, a1, a2, a3, b[4 * nr + i]);
-            b[nr + i] = a1;
-            b[2 * nr + i] = a2;
-            b[3 * nr + i] = a3;
-            qq[cc] = a0;
-        }
-        const double cr = 1.0 / sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
-        const double q1 = qq[0] * cr, q2 = qq[1] * cr, q3 = qq[2] * cr, q4 = qq[3] * cr;
-        D.q[(0 * 5) * nr + i] = q1;
-        D.q[(1 * 5) * nr + i] = q2;
-        D.q[(2 * 5) * nr + i] = q3;
-        D.q[(3 * 5) * nr + i] = q4;
-        double a[9];
-        a[0] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
-        a[1] = 2.0 * (q3 * q4 - q1 * q2);
-        a[2] = 2.0 * (q2 * q3 + q1 * q4);
-        a[3] = -2.0 * (q1 * q2 + q3 * q4);
-        a[4] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4;
-        a[5] = 2.0 * (q2 * q4 - q1 * q3);
-        a[6] = 2.0 * (q2 * q3 - q1 * q4);
-        a[7] = -2.0 * (q1 * q3 + q4 * q2);
-        a[8] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
-        for (int k = 0; k < 9; ++k) D.a[k * nr + i] = a[k];
-        const int ix = 3 * i;
-        double sx[3], sy[3], sz[3];
-        for (int j = 0; j < 3; ++j) {
-            sx[j] = cx[0] + a[0] * D.body.xbody[j] + a[3] * D.body.ybody[j] + a[6] * D.body.zbody[j];
-            sy[j] = cx[1] + a[1] * D.body.xbody[j] + a[4] * D.body.ybody[j] + a[7] * D.body.zbody[j];
-            sz[j] = cx[2] + a[2] * D.body.xbody[j] + a[5] * D.body.ybody[j] + a[8] * D.body.zbody[j];
-            v.x[ix + j] = sx[j];
-            v.y[ix + j] = sy[j];
-            v.z[ix + j] = sz[j];
-        }
-        for (int j = 1; j < 3; ++j) {
-            v.rsx[ix + j] = sx[j] - sx[0];
-            v.rsy[ix + j] = sy[j] - sy[0];
-            v.rsz[ix + j] = sz[j] - sz[0];
-        }
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) Q[k][cc] = D.q[(cc * 5 + k) * nr + i];
+    double cx[3], qq[4];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        gpred(C[0][d], C[1][d], C[2][d], C[3][d], C[4][d]);
+        sc[d] += C[1][d] * C[1][d];
+        cx[d] = C[0][d];
+        gpred(W[0][d], W[1][d], W[2][d], W[3][d], W[4][d]);
+        sw[d] += W[0][d] * W[0][d];
+    }
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+        gpred(Q[0][cc], Q[1][cc], Q[2][cc], Q[3][cc], Q[4][cc]);
+        qq[cc] = Q[0][cc];
+    }
+    const double cr = 1.0 / sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
+    const double q1 = qq[0] * cr, q2 = qq[1] * cr, q3 = qq[2] * cr, q4 = qq[3] * cr;
+    double a[9];
+    a[0] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
+    a[1] = 2.0 * (q3 * q4 - q1 * q2);
+    a[2] = 2.0 * (q2 * q3 + q1 * q4);
+    a[3] = -2.0 * (q1 * q2 + q3 * q4);
+    a[4] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4;
+    a[5] = 2.0 * (q2 * q4 - q1 * q3);
+    a[6] = 2.0 * (q2 * q3 - q1 * q4);
+    a[7] = -2.0 * (q1 * q3 + q4 * q2);
+    a[8] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) D.c[(k * 3 + d) * nr + i] = C[k][d];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) D.w[(k * 3 + d) * nr + i] = W[k][d];
+    }
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc)
+#pragma unroll
+        for (int k = 1; k < 4; ++k) D.q[(cc * 5 + k) * nr + i] = Q[k][cc];
+    D.q[(0 * 5) * nr + i] = q1;
+    D.q[(1 * 5) * nr + i] = q2;
+    D.q[(2 * 5) * nr + i] = q3;
+    D.q[(3 * 5) * nr + i] = q4;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) D.a[k * nr + i] = a[k];
+    const int ix = 3 * i;
+    double sx[3], sy[3], sz[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        sx[j] = cx[0] + a[0] * D.body.xbody[j] + a[3] * D.body.ybody[j] + a[6] * D.body.zbody[j];
+        sy[j] = cx[1] + a[1] * D.body.xbody[j] + a[4] * D.body.ybody[j] + a[7] * D.body.zbody[j];
+        sz[j] = cx[2] + a[2] * D.body.xbody[j] + a[5] * D.body.ybody[j] + a[8] * D.body.zbody[j];
+        v.x[ix + j] = sx[j];
+        v.y[ix + j] = sy[j];
+        v.z[ix + j] = sz[j];
+    }
+#pragma unroll
+    for (int j = 1; j < 3; ++j) {
+        v.rsx[ix + j] = sx[j] - sx[0];
+        v.rsy[ix + j] = sy[j] - sy[0];
+        v.rsz[ix + j] = sz[j] - sz[0];
     }
 }
 
@@ -248,55 +257,78 @@ __device__ __forceinline__ void corr_rigid(const View& v, const Dyn& D, int i) {
     const mdg_rigid& b = D.body;
     const double rcorr = 0.5 / b.mw;
     const double inxxi = 1.0 / b.inxx, inyyi = 1.0 / b.inyy, inzzi = 1.0 / b.inzz;
-    {
+    // loads first (see pred_rigid)
+    double C[5][3], W[5][3], Q[5][4], a[9], fc[3], tq[3];
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
-            double* c0 = D.c + (0 * 3 + d) * nr;
-            double* c1 = D.c + (1 * 3 + d) * nr;
-            double* c2 = D.c + (2 * 3 + d) * nr;
-            double* c3 = D.c + (3 * 3 + d) * nr;
-            double* c4 = D.c + (4 * 3 + d) * nr;
-            const double co = rcorr * D.fc[d * nr + i] - c1[i] * s0i - c2[i];
-            c0[i] = c0[i] + Gf02 * co;
-            c1[i] = c1[i] + Gf12 * co;
-            c2[i] = c2[i] + Gf22 * co;
-            c3[i] = c3[i] + Gf32 * co;
-            c4[i] = c4[i] + Gf42 * co;
+            C[k][d] = D.c[(k * 3 + d) * nr + i];
+            W[k][d] = D.w[(k * 3 + d) * nr + i];
         }
-        const double q1 = D.q[0 * 5 * nr + i], q2 = D.q[1 * 5 * nr + i], q3 = D.q[2 * 5 * nr + i],
-                     q4 = D.q[3 * 5 * nr + i];
-        const double wx = D.w[0 * nr + i], wy = D.w[1 * nr + i], wz = D.w[2 * nr + i];
-        double cq[4];
-        cq[0] = 0.5 * (-q3 * wx - q4 * wy + q2 * wz);
-        cq[1] = 0.5 * (q4 * wx - q3 * wy - q1 * wz);
-        cq[2] = 0.5 * (q1 * wx + q2 * wy + q4 * wz);
-        cq[3] = 0.5 * (-q2 * wx + q1 * wy - q3 * wz);
-        for (int cc = 0; cc < 4; ++cc) {
-            double* bq = D.q + (cc * 5) * nr;
-            const double co = cq[cc] - bq[nr + i];
-            bq[i] = bq[i] + Gf01 * co;
-            bq[nr + i] = bq[nr + i] + Gf11 * co;
-            bq[2 * nr + i] = bq[2 * nr + i] + Gf21 * co;
-            bq[3 * nr + i] = bq[3 * nr + i] + Gf31 * co;
-            bq[4 * nr + i] = bq[4 * nr + i] + Gf41 * co;
-        }
-        double a[9];
-        for (int k = 0; k < 9; ++k) a[k] = D.a[k * nr + i];
-        const double tx = D.tq[i], ty = D.tq[nr + i], tz = D.tq[2 * nr + i];
-        double c1 = a[0] * tx + a[1] * ty + a[2] * tz;
-        c1 = ((c1 * 1.0 + wy * wz * (b.inyy - b.inzz)) * inxxi) - D.w[(1 * 3 + 0) * nr + i] - rs0i * wx;
-        double c2 = a[3] * tx + a[4] * ty + a[5] * tz;
-        c2 = ((c2 * 1.0 + wz * wx * (b.inzz - b.inxx)) * inyyi) - D.w[(1 * 3 + 1) * nr + i] - rs0i * wy;
-        double c3 = a[6] * tx + a[7] * ty + a[8] * tz;
-        c3 = ((c3 * 1.0 + wx * wy * (b.inxx - b.inyy)) * inzzi) - D.w[(1 * 3 + 2) * nr + i] - rs0i * wz;
-        const double cw[3] = {c1, c2, c3};
-        for (int d = 0; d < 3; ++d) {
-            D.w[(0 * 3 + d) * nr + i] += Gf01 * cw[d];
-            D.w[(1 * 3 + d) * nr + i] += Gf11 * cw[d];
-            D.w[(2 * 3 + d) * nr + i] += Gf21 * cw[d];
-            D.w[(3 * 3 + d) * nr + i] += Gf31 * cw[d];
-            D.w[(4 * 3 + d) * nr + i] += Gf41 * cw[d];
-        }
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) Q[k][cc] = D.q[(cc * 5 + k) * nr + i];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a[k] = D.a[k * nr + i];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        fc[d] = D.fc[d * nr + i];
+        tq[d] = D.tq[d * nr + i];
     }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double co = rcorr * fc[d] - C[1][d] * s0i - C[2][d];
+        C[0][d] = C[0][d] + Gf02 * co;
+        C[1][d] = C[1][d] + Gf12 * co;
+        C[2][d] = C[2][d] + Gf22 * co;
+        C[3][d] = C[3][d] + Gf32 * co;
+        C[4][d] = C[4][d] + Gf42 * co;
+    }
+    const double q1 = Q[0][0], q2 = Q[0][1], q3 = Q[0][2], q4 = Q[0][3];
+    const double wx = W[0][0], wy = W[0][1], wz = W[0][2];
+    double cq[4];
+    cq[0] = 0.5 * (-q3 * wx - q4 * wy + q2 * wz);
+    cq[1] = 0.5 * (q4 * wx - q3 * wy - q1 * wz);
+    cq[2] = 0.5 * (q1 * wx + q2 * wy + q4 * wz);
+    cq[3] = 0.5 * (-q2 * wx + q1 * wy - q3 * wz);
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+        const double co = cq[cc] - Q[1][cc];
+        Q[0][cc] = Q[0][cc] + Gf01 * co;
+        Q[1][cc] = Q[1][cc] + Gf11 * co;
+        Q[2][cc] = Q[2][cc] + Gf21 * co;
+        Q[3][cc] = Q[3][cc] + Gf31 * co;
+        Q[4][cc] = Q[4][cc] + Gf41 * co;
+    }
+    const double tx = tq[0], ty = tq[1], tz = tq[2];
+    double c1 = a[0] * tx + a[1] * ty + a[2] * tz;
+    c1 = ((c1 * 1.0 + wy * wz * (b.inyy - b.inzz)) * inxxi) - W[1][0] - rs0i * wx;
+    double c2 = a[3] * tx + a[4] * ty + a[5] * tz;
+    c2 = ((c2 * 1.0 + wz * wx * (b.inzz - b.inxx)) * inyyi) - W[1][1] - rs0i * wy;
+    double c3 = a[6] * tx + a[7] * ty + a[8] * tz;
+    c3 = ((c3 * 1.0 + wx * wy * (b.inxx - b.inyy)) * inzzi) - W[1][2] - rs0i * wz;
+    const double cw[3] = {c1, c2, c3};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        W[0][d] += Gf01 * cw[d];
+        W[1][d] += Gf11 * cw[d];
+        W[2][d] += Gf21 * cw[d];
+        W[3][d] += Gf31 * cw[d];
+        W[4][d] += Gf41 * cw[d];
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            D.c[(k * 3 + d) * nr + i] = C[k][d];
+            D.w[(k * 3 + d) * nr + i] = W[k][d];
+        }
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) D.q[(cc * 5 + k) * nr + i] = Q[k][cc];
 }
 
 __device__ void thermo_corr(const View& v, const Dyn& D) {
