@@ -287,6 +287,25 @@ int mdg_batch_run(mdg_batch* b, int64_t nsteps, mdg_report* reps);
 int mdg_batch_run_async(mdg_batch* b, int64_t nsteps);
 
 /* ---------------------------------------------------------------------------------------------
+ * Configuration files and checkpoints of the resident state.
+ * mdg_write_cfg writes the state in the reference's configuration format (config_output,
+ * src/config.f90:244-301, records of write_rigmol/atmol/surfmol/crystal/thermostat :484-590):
+ * derivatives back to 1 fs units, Fortran E15.8 fields, or with full_precision != 0 the same
+ * layout with 17 significant digits (list-directed input reads both).  molnames: ntype molecule
+ * names as in the .fld file.  Crystal sites are written with their site-type code (1 or 2).
+ * mdg_read_cfg reads such a file (config_input :174-242, then config_init :55-95 and
+ * move_shake_init, src/move.f90:394-396) and installs it as the resident state (mdg_set_state);
+ * names, kinds and counts must match the context; wall positions stay those of mdg_create.
+ * mdg_checkpoint_save / _load write and read the resident state in binary (every integrator,
+ * SHAKE and thermostat array and the step counters), so that a run continues from it as from the
+ * state it saved; the neighbour list is rebuilt at the first step after a load.
+ * ------------------------------------------------------------------------------------------- */
+int mdg_write_cfg(mdg_ctx* ctx, const char* path, const char* const* molnames, int full_precision);
+int mdg_read_cfg(mdg_ctx* ctx, const char* path, const char* const* molnames, const mdg_rigid* body);
+int mdg_checkpoint_save(mdg_ctx* ctx, const char* path);
+int mdg_checkpoint_load(mdg_ctx* ctx, const char* path);
+
+/* ---------------------------------------------------------------------------------------------
  * Learned SHAKE seed.  A small network (9 -> 64 -> 64 -> 3, SiLU) maps rotation-invariant features
  * of a 3-constraint molecule's unconstrained and previous bond vectors to the multipliers that
  * SHAKE accumulates for it; the prediction is applied as one SHAKE-type correction before the

@@ -220,6 +220,12 @@ class Lib:
             g("measure_zero", C.c_int, [C.c_void_p])
             g("measure_do", C.c_int, [C.c_void_p, DP, DP, DP])
             g("measure_get", C.c_int, [C.c_void_p, C.POINTER(MeasureOut)])
+        if self.has("write_cfg"):
+            CPP = C.POINTER(C.c_char_p)
+            g("write_cfg", C.c_int, [C.c_void_p, C.c_char_p, CPP, C.c_int])
+            g("read_cfg", C.c_int, [C.c_void_p, C.c_char_p, CPP, C.POINTER(Rigid)])
+            g("checkpoint_save", C.c_int, [C.c_void_p, C.c_char_p])
+            g("checkpoint_load", C.c_int, [C.c_void_p, C.c_char_p])
         if self.has("widom"):
             g("widom", C.c_int, [C.c_void_p, C.POINTER(WidomParams), DP, DP, I64P, I64P])
         if self.has("run"):
@@ -630,3 +636,37 @@ def _ctx_widom(self, ichmax: int, lwmin: float, lwmax: float, lchmax: int, ilmid
 
 
 Context.widom = _ctx_widom
+
+
+# ---------------------------------------------------------------------------------------------
+# Configuration files and checkpoints (mdg_write_cfg / mdg_read_cfg / mdg_checkpoint_*).
+# ---------------------------------------------------------------------------------------------
+def _molnames(s: System):
+    names = [m.name.encode() for m in s.fld.moltypes]
+    return (C.c_char_p * len(names))(*names)
+
+
+def _ctx_write_cfg(self, path: str, full_precision: bool = False) -> None:
+    """config_output of the resident state (E15.8 fields, or 17 digits with full_precision)."""
+    self._check(self.lib.write_cfg(self.h, path.encode(), _molnames(self.sys), int(full_precision)))
+
+
+def _ctx_read_cfg(self, path: str, s: Optional[System] = None) -> None:
+    """config_input + config_init of a .cfg file, installed as the resident state."""
+    s = s or self.sys
+    self._rigid = rigid_of(s)
+    self._check(self.lib.read_cfg(self.h, path.encode(), _molnames(s), C.byref(self._rigid)))
+
+
+def _ctx_checkpoint_save(self, path: str) -> None:
+    self._check(self.lib.checkpoint_save(self.h, path.encode()))
+
+
+def _ctx_checkpoint_load(self, path: str) -> None:
+    self._check(self.lib.checkpoint_load(self.h, path.encode()))
+
+
+Context.write_cfg = _ctx_write_cfg
+Context.read_cfg = _ctx_read_cfg
+Context.checkpoint_save = _ctx_checkpoint_save
+Context.checkpoint_load = _ctx_checkpoint_load

@@ -200,6 +200,7 @@ struct Ctx {
     bool shake_model = false, shake_record = false;
     int pair_blocks = 0;          // blocks of the real-space loops (0: by head count); autotuned
     Meas meas;                    // measurement histograms (measure.cu)
+    std::vector<int64_t> h_moltypen, h_nt, h_ns, h_itype;  // molecule types and site types (cfgio.cu)
     int64_t widom_cap = 0;        // Widom insertion scratch (widom.cu)
     double *d_widom_pos = nullptr, *d_widom_rot = nullptr, *d_widom_res = nullptr;
     int* d_widom_n = nullptr;
@@ -282,6 +283,8 @@ void measure_force_intra(Ctx& c);  // after force_intra
 void measure_force_sum(Ctx& c);    // after force_sum
 void measure_do_launch(Ctx& c, const double* x, const double* y, const double* z);
 int measure_get(Ctx& c, mdg_measure_out* o);
+// mdgpu.cu
+int resident_alloc(Ctx& c);
 // widom.cu
 int widom(Ctx& c, const mdg_widom_params* p, double* seed, double* pave, int64_t* inave, int64_t* done);
 // shake.cu
@@ -295,6 +298,9 @@ int set_err(Ctx* c, int code, const std::string& msg);
 void* dalloc(Ctx& c, size_t bytes);
 
 }  // namespace mdg
+
+// The opaque context of the C ABI is the device state itself.
+struct mdg_ctx : mdg::Ctx {};
 
 #define MDG_CUDA(call)                                                                   \
     do {                                                                                 \

@@ -306,8 +306,6 @@ int run_force(Ctx& c, bool force_rebuild) {
 
 using namespace mdg;
 
-struct mdg_ctx : Ctx {};
-
 extern "C" {
 
 const char* mdg_last_error(const mdg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
@@ -358,6 +356,10 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
     Ctx& c = *cp;
     cudaGetDevice(&c.device);
     c.sysc = *s;
+    c.h_moltypen.assign(s->moltypen, s->moltypen + s->ntype);
+    c.h_nt.assign(s->nt, s->nt + s->ntype);
+    c.h_ns.assign(s->ns, s->ns + s->ntype);
+    c.h_itype.assign(s->itype, s->itype + s->ntota);
     c.precision = p->precision;
     {
         const char* dbg = getenv("MDG_DEBUG_SYNC");
@@ -814,7 +816,7 @@ int mdg_shake(mdg_ctx* cp, double* x0, double* y0, double* z0, double* xold, dou
 // ---------------------------------------------------------------------------------------------
 // Resident mode
 // ---------------------------------------------------------------------------------------------
-static int resident_alloc(Ctx& c) {
+static int resident_alloc_impl(Ctx& c) {
     if (c.d_thermo) return MDG_OK;
     View& v = c.v;
     const int nion = std::max(v.nliqa - v.nriga, 1), nr = std::max(v.nrig, 1);
@@ -881,7 +883,7 @@ int mdg_set_state(mdg_ctx* cp, const mdg_rigid* b, const mdg_state* st) {
     cudaSetDevice(c.device);
     View& v = c.v;
     MDG_CUDA(cudaStreamSynchronize(c.stream));
-    int rc = resident_alloc(c);
+    int rc = resident_alloc_impl(c);
     if (rc) return rc;
     c.body = *b;
     const int nm = v.nmove, nr = v.nrig, nion = v.nliqa - v.nriga, nold = v.ntota - v.nliqa;
@@ -1586,3 +1588,7 @@ int mdg_widom(mdg_ctx* cp, const mdg_widom_params* prm, double* seed, double* pa
 }
 
 }  // extern "C"
+
+namespace mdg {
+int resident_alloc(Ctx& c) { return resident_alloc_impl(c); }
+}  // namespace mdg
