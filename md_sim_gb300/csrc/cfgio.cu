@@ -407,10 +407,7 @@ int checkpoint_load(Ctx& c, const char* path) {
     const int one = 1;
     MDG_CUDA(cudaMemcpy(c.v.status + ST_FORCE_RB, &one, sizeof(int), cudaMemcpyHostToDevice));
     c.resident = true;
-    if (c.graph_exec) {
-        cudaGraphExecDestroy(c.graph_exec);
-        c.graph_exec = nullptr;
-    }
+    drop_graphs(c);
     return MDG_OK;
 }
 

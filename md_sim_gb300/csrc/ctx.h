@@ -223,7 +223,8 @@ struct Ctx {
     unsigned* d_done = nullptr;   // block counters of the fused integrator kernels
     std::vector<std::pair<void*, size_t>> snap_regions;
     char* d_snap = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;   // resident step
+    cudaGraphExec_t force_exec = nullptr;   // force evaluation of the drop-in path
     int graph_steps = 0;
     int64_t kernels_per_step = 0;
     // host staging (pinned)
@@ -297,6 +298,17 @@ void correct_launch(Ctx& c);
 int set_err(Ctx* c, int code, const std::string& msg);
 void* dalloc(Ctx& c, size_t bytes);
 
+}  // namespace mdg
+
+namespace mdg {
+// Captured graphs hold kernel arguments by value: drop them when a pointer or a launch shape
+// they captured changes (list capacity, tuning, stream, measurement switches, a new state).
+inline void drop_graphs(Ctx& c) {
+    if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+    if (c.force_exec) cudaGraphExecDestroy(c.force_exec);
+    c.graph_exec = nullptr;
+    c.force_exec = nullptr;
+}
 }  // namespace mdg
 
 // The opaque context of the C ABI is the device state itself.

@@ -161,10 +161,7 @@ double self_energy(const mdg_sysdesc* s, const double* x0, const double* y0, con
 
 int alloc_lists(Ctx& c, int maxnb, int maxwnb) {
     View& v = c.v;
-    if (c.graph_exec) {
-        cudaGraphExecDestroy(c.graph_exec);
-        c.graph_exec = nullptr;
-    }
+    drop_graphs(c);
     dfree(c, v.nb);
     dfree(c, v.wnb);
     v.maxnb = std::max(maxnb, 8);
@@ -319,6 +316,7 @@ void mdg_destroy(mdg_ctx* c) {
     for (void* p : c->owned)
         if (p) cudaFree(p);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->force_exec) cudaGraphExecDestroy(c->force_exec);
     if (c->h_acc) cudaFreeHost(c->h_acc);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -688,8 +686,32 @@ int mdg_force_get(mdg_ctx* cp, const double* x0, const double* y0, const double*
         MDG_CUDA(cudaMemcpyAsync(v.cy, cy0, sizeof(double) * nrig, cudaMemcpyHostToDevice, c.stream));
         MDG_CUDA(cudaMemcpyAsync(v.cz, cz0, sizeof(double) * nrig, cudaMemcpyHostToDevice, c.stream));
     }
-    int rc = run_force(c, false);
-    if (rc) return rc;
+    // The force phases run as one captured graph (launched per call; host launch cost of one
+    // graph instead of ~20 kernels), and the results are queued right behind it with the status
+    // words, so the call waits once.  A list overflow (rare: the capacity grows at create) is
+    // handled afterwards by regrowing and redoing the evaluation the eager way.
+    int rc;
+    bool graph_ok = false;
+    if (!c.debug_sync) {
+        if (!c.force_exec) {
+            cudaGraph_t g;
+            MDG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            rc = launch_force(c, false, true);
+            const cudaError_t ce = cudaStreamEndCapture(c.stream, &g);
+            if (rc) return rc;
+            if (ce != cudaSuccess) return set_err(&c, MDG_E_CUDA, std::string("force graph capture: ") + cudaGetErrorString(ce));
+            const cudaError_t ie = cudaGraphInstantiate(&c.force_exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) return set_err(&c, MDG_E_CUDA, std::string("force graph: ") + cudaGetErrorString(ie));
+        }
+        MDG_CUDA(cudaGraphLaunch(c.force_exec, c.stream));
+        MDG_CUDA(cudaMemcpyAsync(c.h_status, v.status, sizeof(int) * ST_NWORDS, cudaMemcpyDeviceToHost, c.stream));
+        graph_ok = true;
+    } else {
+        rc = run_force(c, false);
+        if (rc) return rc;
+    }
+    for (int pass = 0; pass < 2; ++pass) {
     if (ftx && nflex > 0) {
         MDG_CUDA(cudaMemcpyAsync(ftx, c.d_ft, sizeof(double) * nflex, cudaMemcpyDeviceToHost, c.stream));
         MDG_CUDA(cudaMemcpyAsync(fty, c.d_ft + nflex, sizeof(double) * nflex, cudaMemcpyDeviceToHost, c.stream));
@@ -719,6 +741,19 @@ int mdg_force_get(mdg_ctx* cp, const double* x0, const double* y0, const double*
     MDG_CUDA(cudaMemcpyAsync(c.h_acc, v.acc, sizeof(double) * nacc, cudaMemcpyDeviceToHost, c.stream));
     rc = sync_check(c, "mdg_force_get");
     if (rc) return rc;
+    if (!graph_ok || pass == 1) break;
+    // status of the graph's evaluation (read_status's checks, on the copy queued above)
+    if (c.h_status[ST_TC_TIMEOUT]) {
+        rc = read_status(c);
+        if (rc) return rc;
+    }
+    if (!c.h_status[ST_LIST_OVF] && !c.h_status[ST_WLIST_OVF]) break;
+    rc = alloc_lists(c, c.h_status[ST_LIST_OVF] ? c.h_status[ST_LIST_OVF] + c.h_status[ST_LIST_OVF] / 4 + 32 : v.maxnb,
+                     c.h_status[ST_WLIST_OVF] ? c.h_status[ST_WLIST_OVF] + c.h_status[ST_WLIST_OVF] / 4 + 32 : v.maxwnb);
+    if (rc) return rc;
+    rc = run_force(c, true);
+    if (rc) return rc;
+    }
     const double* a = c.h_acc;
     const double* sl = a + 2 * v.nijt;
     double sumlj = 0.0, sumqq = 0.0;
@@ -1122,10 +1157,7 @@ int mdg_set_stream(mdg_ctx* cp, void* stream) {
     MDG_CUDA(cudaStreamSynchronize(c.stream));
     if (!c.own_stream) c.own_stream = c.stream;
     c.stream = stream ? (cudaStream_t)stream : c.own_stream;
-    if (c.graph_exec) {
-        cudaGraphExecDestroy(c.graph_exec);
-        c.graph_exec = nullptr;
-    }
+    drop_graphs(c);
     return MDG_OK;
 }
 
@@ -1225,10 +1257,7 @@ int mdg_shake_set_model(mdg_ctx* cp, const float* w, int64_t n) {
         MDG_CUDA(cudaMemcpy(c.d_mlpw, w, sizeof(float) * n, cudaMemcpyHostToDevice));
         c.shake_model = true;
     }
-    if (c.graph_exec) {
-        cudaGraphExecDestroy(c.graph_exec);
-        c.graph_exec = nullptr;
-    }
+    drop_graphs(c);
     return MDG_OK;
 }
 
@@ -1236,10 +1265,7 @@ int mdg_shake_record(mdg_ctx* cp, int enable) {
     if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
     Ctx& c = *cp;
     c.shake_record = enable != 0;
-    if (c.graph_exec) {
-        cudaGraphExecDestroy(c.graph_exec);
-        c.graph_exec = nullptr;
-    }
+    drop_graphs(c);
     return MDG_OK;
 }
 
@@ -1481,10 +1507,7 @@ int mdg_autotune(mdg_ctx* cp, int32_t reps, mdg_tuning* out) {
             }
         tc_plan_pass1(c, best_tpc, best_mult);
     }
-    if (c.graph_exec) {
-        cudaGraphExecDestroy(c.graph_exec);
-        c.graph_exec = nullptr;
-    }
+    drop_graphs(c);
     const float t1 = time_force(c, reps);
     MDG_CUDA(cudaStreamSynchronize(c.stream));
     int rc = read_status(c);
@@ -1503,10 +1526,7 @@ int mdg_autotune(mdg_ctx* cp, int32_t reps, mdg_tuning* out) {
 // Measurement histograms (measure.cu)
 // ---------------------------------------------------------------------------------------------
 static void drop_graph(Ctx& c) {
-    if (c.graph_exec) {
-        cudaGraphExecDestroy(c.graph_exec);
-        c.graph_exec = nullptr;
-    }
+    drop_graphs(c);
 }
 
 int mdg_measure_init(mdg_ctx* cp, const mdg_measure_params* p, mdg_measure_dims* d) {
