@@ -23,6 +23,7 @@ enum StatusWord {
     ST_SWEEPS = 6,     // SHAKE sweeps of the last call
     ST_OOB = 7,        // debug builds: tag of the first out-of-range index seen
     ST_TC_TIMEOUT = 8, // a tensor-core phase gave up waiting on an mbarrier (tag of the wait)
+    ST_PACK_DONE = 9,  // blocks of the packing kernel finished (its last block resets it)
     ST_NWORDS = 12
 };
 

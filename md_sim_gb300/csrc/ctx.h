@@ -166,7 +166,7 @@ struct Ctx {
     double* d_frc = nullptr;            // 3 x nmove reciprocal forces of the tensor-core sum, merged after the join
     cudaStream_t side = nullptr;        // second stream: the reciprocal sum runs beside the real-space loops
     cudaStream_t side2 = nullptr;       // third stream: the head-wall loop beside the head-head loop
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr, ev_list = nullptr;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the context's stream while a caller's stream is in use
     int device = 0;
@@ -247,7 +247,7 @@ void lr_tail(Ctx& c);
 void pack_setup(Ctx& c);
 // per-evaluation records of the real-space loops and the reciprocal sum; clears the FP64 forces
 // and sums the slab dipole M_z
-void pack_mixed(Ctx& c);
+void pack_mixed(Ctx& c, bool force_rebuild);
 void pairs_mixed(Ctx& c, bool merge);  // head-head pairs into F (then merged into the FP64 forces)
 void walls_mixed(Ctx& c);              // head-wall pairs into F
 // F (+ frc, + the slab dipole term) into the FP64 forces, F cleared
@@ -275,6 +275,7 @@ int mlp_train_host(const float* X, const float* Y, int64_t n, int epochs, int ba
 void dipole_correction(Ctx& c);
 void angle_forces(Ctx& c);
 void force_sum(Ctx& c, double* d_ft, double* d_fc, double* d_tq);
+void merge_force_sum(Ctx& c, const double* frc);  // mixed form without bend angles: merge + force_sum
 // measure.cu
 int measure_init(Ctx& c, const mdg_measure_params* p, mdg_measure_dims* d);
 void measure_zero(Ctx& c);

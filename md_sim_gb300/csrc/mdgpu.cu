@@ -220,6 +220,8 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
     View& v = c.v;
     cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
     if (reset_status) cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
+    const bool hist = c.meas.init && c.meas.force_hist;
+    const bool fused = c.precision == MDG_MIXED && c.nang_terms == 0 && !hist;
     if (c.precision == MDG_MIXED) {
         // The tensor-core reciprocal sum needs only the packed atom records: it runs on a side
         // stream while the main stream does the list, the real-space loops and the wall tail.
@@ -228,7 +230,7 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
         // loop; both add into F with vector reductions.  Fork and join go through events, so the
         // same dependencies hold inside a captured graph.  The reciprocal forces (d_frc), F and the
         // slab dipole term join the FP64 forces in one merge at the end.
-        PHASE(pack_mixed(c), "pack");
+        PHASE(pack_mixed(c, force_rebuild), "pack");  // also decides the list rebuild
         const cudaStream_t s0 = c.stream;
         MDG_CUDA(cudaEventRecord(c.ev_fork, s0));
         MDG_CUDA(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
@@ -236,17 +238,24 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
         recip_tc(c);
         c.stream = s0;
         MDG_CUDA(cudaEventRecord(c.ev_join, c.side));
-        PHASE(nnlist_trigger(c, force_rebuild), "trigger");
+        const bool conc = v.nliqa == v.nmove && v.nwall > 0 && v.nheads > 0;
+        if (conc) {
+            // third branch: the wall tail (positions only) while the list is checked and rebuilt,
+            // then the head-wall loop once the list is there
+            MDG_CUDA(cudaStreamWaitEvent(c.side2, c.ev_fork, 0));
+            c.stream = c.side2;
+            lr_tail(c);
+            c.stream = s0;
+        }
         PHASE(nnlist_build(c), "nnlist");
-        if (v.nliqa == v.nmove && v.nwall > 0 && v.nheads > 0) {
-            MDG_CUDA(cudaEventRecord(c.ev_fork2, s0));
-            MDG_CUDA(cudaStreamWaitEvent(c.side2, c.ev_fork2, 0));
+        if (conc) {
+            MDG_CUDA(cudaEventRecord(c.ev_list, s0));
+            MDG_CUDA(cudaStreamWaitEvent(c.side2, c.ev_list, 0));
             c.stream = c.side2;
             walls_mixed(c);
             c.stream = s0;
             MDG_CUDA(cudaEventRecord(c.ev_join2, c.side2));
             PHASE(pairs_mixed(c, false), "pairs");
-            PHASE(lr_tail(c), "lr_tail");
             MDG_CUDA(cudaStreamWaitEvent(s0, c.ev_join2, 0));
         } else {
             PHASE(pairs_mixed(c, true), "pairs");
@@ -255,7 +264,11 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
             PHASE(lr_tail(c), "lr_tail");
         }
         MDG_CUDA(cudaStreamWaitEvent(s0, c.ev_join, 0));
-        PHASE(merge_mixed(c, c.d_frc, true), "merge");
+        if (fused) {
+            PHASE(merge_force_sum(c, c.d_frc), "merge + force_sum");
+        } else {
+            PHASE(merge_mixed(c, c.d_frc, true), "merge");
+        }
     } else {
         cudaMemsetAsync(v.fx, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
         cudaMemsetAsync(v.fy, 0, sizeof(double) * std::max(v.nmove, 1), c.stream);
@@ -269,14 +282,15 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
         PHASE(recip_fp64(c), "reciprocal");
         PHASE(dipole_correction(c), "dipole");
     }
-    const bool hist = c.meas.init && c.meas.force_hist;
     if (hist) {
         measure_force_real(c);
         measure_force_fouri(c);
     }
-    PHASE(angle_forces(c), "angles");
-    if (hist) measure_force_intra(c);
-    PHASE(force_sum(c, c.d_ft, c.d_fc, c.d_tq), "force_sum");
+    if (!fused) {
+        PHASE(angle_forces(c), "angles");
+        if (hist) measure_force_intra(c);
+        PHASE(force_sum(c, c.d_ft, c.d_fc, c.d_tq), "force_sum");
+    }
     if (hist) measure_force_sum(c);
     return MDG_OK;
 }
@@ -323,7 +337,7 @@ void mdg_destroy(mdg_ctx* c) {
     else if (c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->side2) cudaStreamDestroy(c->side2);
-    for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_fork2, c->ev_join2})
+    for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_fork2, c->ev_join2, c->ev_list})
         if (e) cudaEventDestroy(e);
     delete c;
 }
@@ -376,7 +390,8 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
         cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c.ev_fork2, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c.ev_join2, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&c.ev_join2, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c.ev_list, cudaEventDisableTiming) != cudaSuccess) {
         c.err = "cudaStreamCreate failed";
         return bail(MDG_E_CUDA);
     }
@@ -1180,7 +1195,7 @@ int mdg_phase_times(mdg_ctx* cp, int reps, double* ms) {
         nnlist_build(c);
         cudaEventRecord(ev[1], c.stream);
         if (c.precision == MDG_MIXED) {
-            pack_mixed(c);
+            pack_mixed(c, false);
             pairs_mixed(c, true);
         } else {
             pair_forces_fp64(c);

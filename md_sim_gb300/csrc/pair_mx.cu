@@ -113,11 +113,28 @@ __device__ __forceinline__ uint32_t frac32(double t) {
     return (uint32_t)__double_as_longlong(t + 1572864.0);
 }
 
-// Records of every atom for this evaluation; also clears the FP64 forces and, for the slab
-// variant, sums the dipole M_z = sum q z of the moving atoms (src/forcem.f90:924) into the
-// accumulator block, which the caller zeroed.
-__global__ void k_pack(View v, Pk pk, int dip) {
-    double mz = 0.0;
+// Records of every atom for this evaluation; also clears the FP64 forces, for the slab variant
+// sums the dipole M_z = sum q z of the moving atoms (src/forcem.f90:924) into the accumulator
+// block (which the caller zeroed), and takes the neighbour-list rebuild decision
+// (src/forcem.f90:245-250): the maximum squared displacement of the centres of mass and flexible
+// atoms since the last rebuild, compared by the block that finishes last.
+__global__ void k_pack(View v, Pk pk, int dip, int force) {
+    double mz = 0.0, md = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.nrig + (v.nmove - v.nriga);
+         i += gridDim.x * blockDim.x) {
+        double a, b, c;
+        if (i < v.nrig) {
+            a = v.ocx[i] - v.cx[i];
+            b = v.ocy[i] - v.cy[i];
+            c = v.ocz[i] - v.cz[i];
+        } else {
+            const int k = i - v.nrig, at = k + v.nriga;
+            a = v.ox[k] - v.x[at];
+            b = v.oy[k] - v.y[at];
+            c = v.oz[k] - v.z[at];
+        }
+        md = fmax(md, a * a + b * b + c * c);
+    }
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < v.ntota; a += gridDim.x * blockDim.x) {
         const double x = v.x[a], y = v.y[a], z = v.z[a];
         uint4 p;
@@ -149,6 +166,21 @@ __global__ void k_pack(View v, Pk pk, int dip) {
         pk.Q[a] = q;
     }
     if (dip) block_atomic_sum<256>(mz, &v.acc[2 * v.nijt + ACC_DIPZ]);
+    for (int o = 16; o > 0; o >>= 1) md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&v.acc[2 * v.nijt + ACC_MAXD], md);
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&v.status[ST_PACK_DONE], 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const double aux = fmax(__ldcg(&v.acc[2 * v.nijt + ACC_MAXD]), v.dshsq);
+        v.status[ST_REBUILD] = (force || v.status[ST_FORCE_RB] || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
+        v.status[ST_FORCE_RB] = 0;
+        v.acc[2 * v.nijt + ACC_MAXD] = 0.0;
+        v.status[ST_PACK_DONE] = 0;
+    }
 }
 
 // Pair-type tables in shared memory: per ijt {kind, sig, eps, aa, rhoi, cc}, ijt[it*nit+jt], nsi[it].
@@ -444,10 +476,11 @@ double slab_crf0(const Ctx& c) {
     return -2.0 * (double)3.1415926535898f * c.v.lzi * c.v.lxi * c.v.lyi;
 }
 
-void pack_mixed(Ctx& c) {
+void pack_mixed(Ctx& c, bool force_rebuild) {
     const View& v = c.v;
-    if (v.ntota == 0) return;
-    k_pack<<<std::min((v.ntota + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk, c.variant == MDG_SLAB ? 1 : 0);
+    const int n = std::max(std::max(v.ntota, v.nrig + (v.nmove - v.nriga)), 1);
+    k_pack<<<std::min((n + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk, c.variant == MDG_SLAB ? 1 : 0,
+                                                                    force_rebuild ? 1 : 0);
 }
 
 void merge_mixed(Ctx& c, const double* frc, bool dipole) {
