@@ -17,6 +17,7 @@ CASES = {
     "slab512": lambda: configs.slab_water(nwat=512, cells=6),
     "shake256": lambda: configs.shake_water(nwat=256, cells=6),
     "y_n": lambda: y_n_case()[:2],
+    "electrolyte": lambda: configs.slab_electrolyte(),
 }
 
 

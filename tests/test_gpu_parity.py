@@ -25,6 +25,10 @@ def _cases():
         "slab2048": lambda: configs.slab_water(),
         "shake256": lambda: configs.shake_water(nwat=256, cells=6),
         "y_n": lambda: y_n_case()[:2],
+        # ions between the walls (site types 3 and 4 among waters)
+        "electrolyte": lambda: configs.slab_electrolyte(),
+        # point ions only, with a cutoff below the closest approach: empty real-space sum
+        "ions_empty_real": lambda: configs.ion_lattice(),
     }
 
 
