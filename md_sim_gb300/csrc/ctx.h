@@ -204,6 +204,9 @@ struct Ctx {
     int64_t widom_cap = 0;        // Widom insertion scratch (widom.cu)
     double *d_widom_pos = nullptr, *d_widom_rot = nullptr, *d_widom_res = nullptr;
     int* d_widom_n = nullptr;
+    float* d_widom_akf = nullptr;   // Ak in FP32 (mixed form)
+    float2* d_widom_qsf = nullptr;  // S + S_wall in FP32 (mixed form)
+    float4* d_widom_rsf = nullptr;  // rs offsets and charges in FP32 (mixed form)
     bool widom_attr = false;
     std::vector<int> h_ang_mt;    // molecule type of each angle term
     int64_t nfreed = 0;

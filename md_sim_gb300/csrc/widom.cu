@@ -14,7 +14,8 @@
 //     exp(-beta u) summed over the orientations.
 // The host keeps the positions up to the first overlap (the reference leaves the insertion loop
 // there, src/forcem.f90:1342) unless MDG_WIDOM_SKIP_OVERLAP is set, and accumulates pave/inave.
-// Everything runs in FP64 (the insertion energies enter exponentials).
+// Contexts of the FP64 form run everything in FP64; those of the mixed form run the orientation
+// loop in FP32 (block sums, the wall tail and the exponential stay FP64).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -44,7 +45,31 @@ struct WArgs {
     double pipix, pipiy, pipiz;
     double beta, rinsmin, rwinsmin, crf;
     double q0, q1;        // probe charges (O, H)
+    // mixed form: FP32 operands of the orientation loop
+    const float2* qsf;    // Qsum = S + S_wall in FP32
+    const float* akf;     // Ak in FP32
+    const float4* rsf;    // per site: rs offset (moving sites) and charge, FP32
 };
+
+__device__ __forceinline__ float ewald_ef(float rr, float alfa) {
+    const float ar = alfa * rr;
+    const float t = __fdividef(1.0f, 1.0f + (float)kP * ar);
+    const float e2 = __expf(-ar * ar);
+    return (((((float)kA5 * t + (float)kA4) * t + (float)kA3) * t + (float)kA2) * t + (float)kA1) * t * e2;
+}
+
+// FP32 operands of one call: Qsum per k, and per site its offset rs (as force_sum left it, like
+// the reference's module array) and charge.
+__global__ void k_widom_prep(View v, const double2* __restrict__ sk, const double2* __restrict__ qw, float2* qsf,
+                             int nk, float4* rsf) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nk; k += gridDim.x * blockDim.x)
+        qsf[k] = make_float2((float)(sk[k].x + qw[k].x), (float)(sk[k].y + qw[k].y));
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < v.ntota; a += gridDim.x * blockDim.x) {
+        const bool mv = a < v.nmove;
+        rsf[a] = make_float4(mv ? (float)v.rsx[a] : 0.f, mv ? (float)v.rsy[a] : 0.f, mv ? (float)v.rsz[a] : 0.f,
+                             (float)v.q[a]);
+    }
+}
 
 __device__ __forceinline__ double ewald_e(double rij, double alfa) {
     const double alfar = alfa * rij;
@@ -64,6 +89,9 @@ __device__ double block_sum_d(double x, double* red) {
     return s;
 }
 
+// MX: the orientation loop (real-space erfc terms and the reciprocal term) in FP32 with FP64 sums
+// per block, for contexts of the mixed form; the O scan, the wall tail and exp stay FP64.
+template <bool MX>
 __global__ void __launch_bounds__(kWT) k_widom(View v, WArgs w) {
     extern __shared__ __align__(16) unsigned char sm[];
     int* nb_j = reinterpret_cast<int*>(sm);
@@ -133,70 +161,154 @@ __global__ void __launch_bounds__(kWT) k_widom(View v, WArgs w) {
     for (int r = 0; r < nr; ++r) {
         const double* rr = w.rot + ((size_t)ins * kMaxRot + r) * 6;
         const double sx[3] = {ox, rr[0], rr[3]}, sy[3] = {oy, rr[1], rr[4]}, sz[3] = {oz, rr[2], rr[5]};
-        // ---- real space: the probe's sites against the neighbours' sites
-        double ur = 0.0;
-        for (int k = t; k < nnb; k += kWT) {
-            const int j = nb_j[k];
-            const double xio = nb_d[3 * k], yio = nb_d[3 * k + 1], zio = nb_d[3 * k + 2];
-            const int jt = v.type[j];
-            if (jt == 0) {
-                const int njx = v.nsi[jt];
-                for (int ix = 0; ix < 3; ++ix) {
-                    const double xi = (xio + sx[ix]) - ox, yi = (yio + sy[ix]) - oy, zi = (zio + sz[ix]) - oz;
-                    const double qx = v.facq * qs3[ix];
-                    for (int jx = (ix == 0 ? j + 1 : j); jx < j + njx; ++jx) {
-                        const double xd = xi - v.rsx[jx], yd = yi - v.rsy[jx], zd = zi - v.rsz[jx];
-                        const double rsq = xd * xd + yd * yd + zd * zd;
+        double ur = 0.0, uk = 0.0;
+        if constexpr (!MX) {
+            // ---- real space: the probe's sites against the neighbours' sites
+            for (int k = t; k < nnb; k += kWT) {
+                const int j = nb_j[k];
+                const double xio = nb_d[3 * k], yio = nb_d[3 * k + 1], zio = nb_d[3 * k + 2];
+                const int jt = v.type[j];
+                if (jt == 0) {
+                    const int njx = v.nsi[jt];
+                    for (int ix = 0; ix < 3; ++ix) {
+                        const double xi = (xio + sx[ix]) - ox, yi = (yio + sy[ix]) - oy, zi = (zio + sz[ix]) - oz;
+                        const double qx = v.facq * qs3[ix];
+                        for (int jx = (ix == 0 ? j + 1 : j); jx < j + njx; ++jx) {
+                            const double xd = xi - v.rsx[jx], yd = yi - v.rsy[jx], zd = zi - v.rsz[jx];
+                            const double rsq = xd * xd + yd * yd + zd * zd;
+                            const double rij = sqrt(rsq);
+                            ur += ewald_e(rij, v.alfa) * (qx * v.q[jx] / rij);
+                        }
+                    }
+                } else {
+                    for (int ix = 1; ix < 3; ++ix) {
+                        const double xi = (xio + sx[ix]) - ox, yi = (yio + sy[ix]) - oy, zi = (zio + sz[ix]) - oz;
+                        const double rsq = xi * xi + yi * yi + zi * zi;
                         const double rij = sqrt(rsq);
-                        ur += ewald_e(rij, v.alfa) * (qx * v.q[jx] / rij);
+                        ur += ewald_e(rij, v.alfa) * (v.facq * qs3[ix] * v.q[j] / rij);
                     }
                 }
-            } else {
-                for (int ix = 1; ix < 3; ++ix) {
-                    const double xi = (xio + sx[ix]) - ox, yi = (yio + sy[ix]) - oy, zi = (zio + sz[ix]) - oz;
-                    const double rsq = xi * xi + yi * yi + zi * zi;
-                    const double rij = sqrt(rsq);
-                    ur += ewald_e(rij, v.alfa) * (v.facq * qs3[ix] * v.q[j] / rij);
+            }
+            // ---- reciprocal space: per-site phase tables by repeated multiplication
+            if (t < 9) {
+                const int s = t / 3, ax = t % 3;
+                const double ang = ax == 0 ? w.pipix * sx[s] : (ax == 1 ? w.pipiy * sy[s] : w.pipiz * sz[s]);
+                double2 e1;
+                sincos(ang, &e1.y, &e1.x);
+                if (ax == 0) {
+                    double2* T = el + s * nl;
+                    T[0] = make_double2(1.0, 0.0);
+                    if (w.KL >= 1) T[1] = e1;
+                    for (int l = 2; l <= w.KL; ++l)
+                        T[l] = make_double2(T[l - 1].x * e1.x - T[l - 1].y * e1.y, T[l - 1].x * e1.y + T[l - 1].y * e1.x);
+                } else {
+                    const int K = ax == 1 ? w.KM : w.KN;
+                    double2* T = (ax == 1 ? em + s * nm : en + s * nn) + K;
+                    T[0] = make_double2(1.0, 0.0);
+                    if (K >= 1) T[1] = e1;
+                    for (int l = 2; l <= K; ++l)
+                        T[l] = make_double2(T[l - 1].x * e1.x - T[l - 1].y * e1.y, T[l - 1].x * e1.y + T[l - 1].y * e1.x);
+                    for (int l = 1; l <= K; ++l) T[-l] = make_double2(T[l].x, -T[l].y);
                 }
             }
-        }
-        // ---- reciprocal space: per-site phase tables by repeated multiplication
-        if (t < 9) {
-            const int s = t / 3, ax = t % 3;
-            const double ang = ax == 0 ? w.pipix * sx[s] : (ax == 1 ? w.pipiy * sy[s] : w.pipiz * sz[s]);
-            double2 e1;
-            sincos(ang, &e1.y, &e1.x);
-            if (ax == 0) {
-                double2* T = el + s * nl;
-                T[0] = make_double2(1.0, 0.0);
-                if (w.KL >= 1) T[1] = e1;
-                for (int l = 2; l <= w.KL; ++l)
-                    T[l] = make_double2(T[l - 1].x * e1.x - T[l - 1].y * e1.y, T[l - 1].x * e1.y + T[l - 1].y * e1.x);
-            } else {
-                const int K = ax == 1 ? w.KM : w.KN;
-                double2* T = (ax == 1 ? em + s * nm : en + s * nn) + K;
-                T[0] = make_double2(1.0, 0.0);
-                if (K >= 1) T[1] = e1;
-                for (int l = 2; l <= K; ++l)
-                    T[l] = make_double2(T[l - 1].x * e1.x - T[l - 1].y * e1.y, T[l - 1].x * e1.y + T[l - 1].y * e1.x);
-                for (int l = 1; l <= K; ++l) T[-l] = make_double2(T[l].x, -T[l].y);
-            }
-        }
-        __syncthreads();
-        double uk = 0.0;
-        for (int k = t; k < w.nk; k += kWT) {
-            const int3 kv = w.kvec[k];
-            double xr = 0.0, xi = 0.0;
+            __syncthreads();
+            for (int k = t; k < w.nk; k += kWT) {
+                const int3 kv = w.kvec[k];
+                double xr = 0.0, xi = 0.0;
 #pragma unroll
-            for (int s = 0; s < 3; ++s) {
-                const double2 a = el[s * nl + kv.x], b = em[s * nm + kv.y + w.KM], c = en[s * nn + kv.z + w.KN];
-                const double lr_ = qs3[s] * (a.x * b.x - a.y * b.y), li_ = qs3[s] * (a.x * b.y + a.y * b.x);
-                xr += lr_ * c.x - li_ * c.y;
-                xi += lr_ * c.y + li_ * c.x;
+                for (int s = 0; s < 3; ++s) {
+                    const double2 a = el[s * nl + kv.x], b = em[s * nm + kv.y + w.KM], c = en[s * nn + kv.z + w.KN];
+                    const double lr_ = qs3[s] * (a.x * b.x - a.y * b.y), li_ = qs3[s] * (a.x * b.y + a.y * b.x);
+                    xr += lr_ * c.x - li_ * c.y;
+                    xi += lr_ * c.y + li_ * c.x;
+                }
+                const double2 sk = w.sk[k], q = w.qw[k];
+                const double qr = sk.x + q.x, qi = sk.y + q.y;
+                uk += 0.5 * w.ak[k] * (xr * qr + xi * qi);
             }
-            const double2 sk = w.sk[k], q = w.qw[k];
-            const double qr = sk.x + q.x, qi = sk.y + q.y;
-            uk += 0.5 * w.ak[k] * (xr * qr + xi * qi);
+
+        } else {
+            // ---- the same terms in FP32: site offsets from the O, neighbour sites from the FP32
+            // copy of rs and q
+            const float qx3[3] = {(float)(v.facq * qs3[0]), (float)(v.facq * qs3[1]), (float)(v.facq * qs3[2])};
+            float dsx[3], dsy[3], dsz[3];
+#pragma unroll
+            for (int ix = 0; ix < 3; ++ix) {
+                dsx[ix] = (float)(sx[ix] - ox);
+                dsy[ix] = (float)(sy[ix] - oy);
+                dsz[ix] = (float)(sz[ix] - oz);
+            }
+            const float alfa = (float)v.alfa;
+            float urf = 0.f;
+            for (int k = t; k < nnb; k += kWT) {
+                const int j = nb_j[k];
+                const float xio = (float)nb_d[3 * k], yio = (float)nb_d[3 * k + 1], zio = (float)nb_d[3 * k + 2];
+                const int jt = v.type[j];
+                if (jt == 0) {
+                    const int njx = v.nsi[jt];
+                    for (int ix = 0; ix < 3; ++ix) {
+                        const float xi = xio + dsx[ix], yi = yio + dsy[ix], zi = zio + dsz[ix];
+                        for (int jx = (ix == 0 ? j + 1 : j); jx < j + njx; ++jx) {
+                            const float4 qj = w.rsf[jx];
+                            const float xd = xi - qj.x, yd = yi - qj.y, zd = zi - qj.z;
+                            const float r2 = xd * xd + yd * yd + zd * zd;
+                            const float ri = rsqrtf(r2);
+                            urf += ewald_ef(r2 * ri, alfa) * (qx3[ix] * qj.w * ri);
+                        }
+                    }
+                } else {
+                    const float qj = w.rsf[j].w;
+                    for (int ix = 1; ix < 3; ++ix) {
+                        const float xi = xio + dsx[ix], yi = yio + dsy[ix], zi = zio + dsz[ix];
+                        const float r2 = xi * xi + yi * yi + zi * zi;
+                        const float ri = rsqrtf(r2);
+                        urf += ewald_ef(r2 * ri, alfa) * (qx3[ix] * qj * ri);
+                    }
+                }
+            }
+            ur = (double)urf;
+            float2* elf = reinterpret_cast<float2*>(tab);
+            float2* emf = elf + 3 * nl;
+            float2* enf = emf + 3 * nm;
+            if (t < 9) {
+                const int s = t / 3, ax = t % 3;
+                const double ang = ax == 0 ? w.pipix * sx[s] : (ax == 1 ? w.pipiy * sy[s] : w.pipiz * sz[s]);
+                double cd, sd;
+                sincos(ang, &sd, &cd);
+                const float2 e1 = make_float2((float)cd, (float)sd);
+                if (ax == 0) {
+                    float2* T = elf + s * nl;
+                    T[0] = make_float2(1.f, 0.f);
+                    if (w.KL >= 1) T[1] = e1;
+                    for (int l = 2; l <= w.KL; ++l)
+                        T[l] = make_float2(T[l - 1].x * e1.x - T[l - 1].y * e1.y, T[l - 1].x * e1.y + T[l - 1].y * e1.x);
+                } else {
+                    const int K = ax == 1 ? w.KM : w.KN;
+                    float2* T = (ax == 1 ? emf + s * nm : enf + s * nn) + K;
+                    T[0] = make_float2(1.f, 0.f);
+                    if (K >= 1) T[1] = e1;
+                    for (int l = 2; l <= K; ++l)
+                        T[l] = make_float2(T[l - 1].x * e1.x - T[l - 1].y * e1.y, T[l - 1].x * e1.y + T[l - 1].y * e1.x);
+                    for (int l = 1; l <= K; ++l) T[-l] = make_float2(T[l].x, -T[l].y);
+                }
+            }
+            __syncthreads();
+            const float q3f[3] = {(float)qs3[0], (float)qs3[1], (float)qs3[2]};
+            float ukf = 0.f;
+            for (int k = t; k < w.nk; k += kWT) {
+                const int3 kv = w.kvec[k];
+                float xr = 0.f, xi = 0.f;
+#pragma unroll
+                for (int s = 0; s < 3; ++s) {
+                    const float2 a = elf[s * nl + kv.x], b = emf[s * nm + kv.y + w.KM], cc = enf[s * nn + kv.z + w.KN];
+                    const float lr_ = q3f[s] * (a.x * b.x - a.y * b.y), li_ = q3f[s] * (a.x * b.y + a.y * b.x);
+                    xr += lr_ * cc.x - li_ * cc.y;
+                    xi += lr_ * cc.y + li_ * cc.x;
+                }
+                const float2 q = w.qsf[k];
+                ukf += 0.5f * w.akf[k] * (xr * q.x + xi * q.y);
+            }
+            uk = (double)ukf;
         }
         const double u_real = block_sum_d(ur, red);
         const double u_rec = block_sum_d(uk, red);
@@ -338,11 +450,37 @@ int widom(Ctx& c, const mdg_widom_params* p, double* seed, double* pave, int64_t
     w.q1 = (double)0.4238f;
     const size_t smem = sizeof(int) * kWNb + sizeof(double) * 3 * kWNb +
                         sizeof(double2) * 3 * (size_t)((ks.klmax + 1) + (2 * ks.kmmax + 1) + (2 * ks.knmax + 1));
+    const bool mx = c.precision == MDG_MIXED;
     if (!c.widom_attr) {
-        MDG_CUDA(allow_max_smem(k_widom));
+        MDG_CUDA(allow_max_smem(k_widom<false>));
+        MDG_CUDA(allow_max_smem(k_widom<true>));
         c.widom_attr = true;
     }
-    k_widom<<<(unsigned)nins, kWT, smem, c.stream>>>(v, w);
+    w.qsf = nullptr;
+    w.akf = nullptr;
+    w.rsf = nullptr;
+    if (mx) {
+        if (!c.d_widom_akf) {
+            std::vector<float> akf(std::max(ks.nk, 1));
+            std::vector<double> ak(ks.nk);
+            if (ks.nk) MDG_CUDA(cudaMemcpy(ak.data(), ks.ak, sizeof(double) * ks.nk, cudaMemcpyDeviceToHost));
+            for (int k = 0; k < ks.nk; ++k) akf[k] = (float)ak[k];
+            c.d_widom_akf = (float*)dalloc(c, sizeof(float) * akf.size());
+            c.d_widom_qsf = (float2*)dalloc(c, sizeof(float2) * akf.size());
+            c.d_widom_rsf = (float4*)dalloc(c, sizeof(float4) * std::max(v.ntota, 1));
+            if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "Widom insertion: out of device memory");
+            MDG_CUDA(cudaMemcpy(c.d_widom_akf, akf.data(), sizeof(float) * akf.size(), cudaMemcpyHostToDevice));
+        }
+        const int np = std::max(std::max(ks.nk, v.ntota), 1);
+        k_widom_prep<<<std::min((np + 255) / 256, 152 * 4), 256, 0, c.stream>>>(v, ks.s, ks.qw, c.d_widom_qsf, ks.nk,
+                                                                             c.d_widom_rsf);
+        w.qsf = c.d_widom_qsf;
+        w.akf = c.d_widom_akf;
+        w.rsf = c.d_widom_rsf;
+        k_widom<true><<<(unsigned)nins, kWT, smem, c.stream>>>(v, w);
+    } else {
+        k_widom<false><<<(unsigned)nins, kWT, smem, c.stream>>>(v, w);
+    }
     MDG_CUDA(cudaGetLastError());
     std::vector<double> res(2 * nins);
     MDG_CUDA(cudaMemcpyAsync(res.data(), c.d_widom_res, sizeof(double) * 2 * nins, cudaMemcpyDeviceToHost, c.stream));
