@@ -59,8 +59,8 @@ __device__ __forceinline__ T warp_sum(T v) {
 // a warp (used to spread FP64-heavy per-molecule work over more SMs) reduce within their lanes.
 template <int NT>
 __device__ __forceinline__ void block_atomic_sum(double v, double* dst) {
-    if constexpr (NT < 32) {
-        constexpr unsigned mask = (1u << NT) - 1u;
+    if constexpr (NT <= 32) {
+        constexpr unsigned mask = NT == 32 ? 0xffffffffu : (1u << (NT & 31)) - 1u;
 #pragma unroll
         for (int o = NT / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
         if (threadIdx.x == 0) atomicAdd(dst, v);

@@ -114,6 +114,8 @@ struct Pk {
     float* zlo = nullptr;   // z - z_hi when z is not periodic
     float4* F = nullptr;    // j-side force accumulator (moving atoms)
     uint4* tc = nullptr;    // reciprocal-sum records (moving atoms), or nullptr
+    float* cmax = nullptr;  // scale of the reciprocal sum's pass-2 operand, cleared here for it
+    double* part = nullptr; // per-block slab dipole shares of the packing kernel
     float sx = 0, sy = 0, sz = 0;  // box edge / 2^32
     int zper = 0;
 };
@@ -250,7 +252,8 @@ void lr_tail(Ctx& c);
 void pack_setup(Ctx& c);
 // per-evaluation records of the real-space loops and the reciprocal sum; clears the FP64 forces
 // and sums the slab dipole M_z
-void pack_mixed(Ctx& c, bool force_rebuild);
+// reset_status: also clear the list overflow words; the energy sums are always cleared
+void pack_mixed(Ctx& c, bool force_rebuild, bool reset_status = false);
 void pairs_mixed(Ctx& c, bool merge);  // head-head pairs into F (then merged into the FP64 forces)
 void walls_mixed(Ctx& c);              // head-wall pairs into F
 // F (+ frc, + the slab dipole term) into the FP64 forces, F cleared
@@ -294,9 +297,11 @@ int resident_alloc(Ctx& c);
 int widom(Ctx& c, const mdg_widom_params* p, double* seed, double* pave, int64_t* inave, int64_t* done);
 // shake.cu
 int shake_setup(Ctx& c, const mdg_sysdesc* s);
-void shake_launch(Ctx& c, const double* d_ft);
+void shake_launch(Ctx& c, const double* d_ft, bool kps_clear = false);  // kps_clear: kps already zeroed
 // integrate.cu
-void predict_launch(Ctx& c);
+// clear_acc / clear_kps: also zero the energy sums of the force call next / the surface atoms'
+// kinetic sums of the SHAKE call after it
+void predict_launch(Ctx& c, bool clear_acc = false, bool clear_kps = false);
 void correct_launch(Ctx& c);
 
 int set_err(Ctx* c, int code, const std::string& msg);

@@ -22,7 +22,20 @@ namespace mdg {
 
 namespace {
 
-constexpr int kNT = 16;
+// A warp serves `lanes` molecules (lanes 0..lanes-1). An FP64 instruction costs the SM's FP64
+// pipe about the same whatever the number of active lanes, so large systems pack 32 molecules per
+// warp (blocks of four warps); small ones spread one warp per SM with just enough lanes to cover
+// the molecules, since there the per-molecule chain of dependent FP64 operations sets the time.
+constexpr int kSM = 152;
+
+// unit served by this thread in sweep `r` of the grid-stride loop, or -1
+template <int NT>
+__device__ __forceinline__ int unit_of(int lanes, int r) {
+    const int lane = threadIdx.x & 31;
+    if (lane >= lanes) return -1;
+    const int gw = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
+    return (r * gridDim.x * (NT / 32) + gw) * lanes + lane;
+}
 
 constexpr double Gf01 = F32D(0.348611111), Gf11 = 1.0, Gf21 = F32D(0.916666667), Gf31 = F32D(0.333333333),
                  Gf41 = F32D(0.041666667);
@@ -194,16 +207,27 @@ __device__ void thermo_pred(const View& v, const Dyn& D) {
     for (int k = 0; k < 7; ++k) D.isum[k] = 0.0;  // ready for the next step
 }
 
-__global__ void k_pred(View v, Dyn D) {
+// Sums that the rest of the step accumulates into, zeroed by the predictor (block 0) so that the
+// step graph needs no memset nodes.
+struct Clear {
+    double* p[2];
+    int n[2];
+};
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z) {
     double kp = 0.0, sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
     const int nu = D.nion + v.nrig;
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+    if (blockIdx.x == 0)
+        for (int j = 0; j < 2; ++j)
+            for (int k = threadIdx.x; k < z.n[j]; k += NT) z.p[j][k] = 0.0;
+    for (int r = 0, u; (u = unit_of<NT>(lanes, r)) >= 0 && u < nu; ++r) {
         if (u < D.nion) kp += pred_ion(v, D, u);
         else pred_rigid(v, D, u - D.nion, sc, sw);
     }
-    block_atomic_sum<kNT>(kp, &D.isum[0]);
-    for (int d = 0; d < 3; ++d) block_atomic_sum<kNT>(sc[d], &D.isum[1 + d]);
-    for (int d = 0; d < 3; ++d) block_atomic_sum<kNT>(sw[d], &D.isum[4 + d]);
+    block_atomic_sum<NT>(kp, &D.isum[0]);
+    for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
+    for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
     if (last_block(&D.done[0]) && threadIdx.x == 0) {
         thermo_pred(v, D);
         D.done[0] = 0u;
@@ -357,9 +381,10 @@ __device__ void thermo_corr(const View& v, const Dyn& D) {
 
 // The correctors read the thermostat values of the predictor; the block that finishes last then
 // adds uconf/press and corrects the thermostat.
-__global__ void k_corr(View v, Dyn D, int slab) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_corr(View v, Dyn D, int slab, int lanes) {
     const int nu = D.nion + v.nrig;
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+    for (int r = 0, u; (u = unit_of<NT>(lanes, r)) >= 0 && u < nu; ++r) {
         if (u < D.nion) corr_ion(v, D, u);
         else corr_rigid(v, D, u - D.nion);
     }
@@ -388,20 +413,31 @@ Dyn dyn_of(Ctx& c) {
     return D;
 }
 
-int nblk(int n) { return std::max(1, std::min((n + kNT - 1) / kNT, 152 * 16)); }
+// molecules per warp, and the block size: one warp per block while a warp per SM covers the
+// system, else full warps in blocks of four
+int lanes_of(int n) { return std::max(1, std::min(32, (n + kSM - 1) / kSM)); }
+int nblk(int n, int nt) {
+    const int lanes = lanes_of(n), warps = (n + lanes - 1) / lanes;
+    return std::max(1, std::min((warps + nt / 32 - 1) / (nt / 32), kSM * 8));
+}
 
 }  // namespace
 
-void predict_launch(Ctx& c) {
+void predict_launch(Ctx& c, bool clear_acc, bool clear_kps) {
     const View& v = c.v;
     Dyn D = dyn_of(c);
-    k_pred<<<nblk(D.nion + v.nrig), kNT, 0, c.stream>>>(v, D);
+    const int nu = D.nion + v.nrig, lanes = lanes_of(nu);
+    Clear z{{v.acc, c.d_kps}, {clear_acc ? 2 * v.nijt + ACC_NSLOT : 0, clear_kps && c.d_kps ? v.nit : 0}};
+    if (lanes < 32) k_pred<32><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, lanes, z);
+    else k_pred<128><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, lanes, z);
 }
 
 void correct_launch(Ctx& c) {
     const View& v = c.v;
     Dyn D = dyn_of(c);
-    k_corr<<<nblk(D.nion + v.nrig), kNT, 0, c.stream>>>(v, D, c.variant == MDG_SLAB ? 1 : 0);
+    const int nu = D.nion + v.nrig, lanes = lanes_of(nu), slab = c.variant == MDG_SLAB ? 1 : 0;
+    if (lanes < 32) k_corr<32><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes);
+    else k_corr<128><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes);
 }
 
 }  // namespace mdg

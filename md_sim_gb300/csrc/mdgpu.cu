@@ -215,11 +215,16 @@ int phase_check(Ctx& c, const char* name) {
         if (prc_) return prc_;              \
     } while (0)
 
-// Queues the force phases on device-resident positions (no synchronisation).
-int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
+// Queues the force phases on device-resident positions (no synchronisation).  acc_clear: the
+// energy sums were zeroed by the kernel before (the predictor of a resident step).  In the mixed
+// form the packing kernel clears them (and the overflow words), which keeps memset nodes, slow
+// to start inside a graph, off the critical path.
+int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear = false) {
     View& v = c.v;
-    cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
-    if (reset_status) cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
+    if (c.precision != MDG_MIXED) {
+        if (!acc_clear) cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
+        if (reset_status) cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
+    }
     const bool hist = c.meas.init && c.meas.force_hist;
     const bool fused = c.precision == MDG_MIXED && c.nang_terms == 0 && !hist;
     if (c.precision == MDG_MIXED) {
@@ -230,7 +235,7 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status) {
         // loop; both add into F with vector reductions.  Fork and join go through events, so the
         // same dependencies hold inside a captured graph.  The reciprocal forces (d_frc), F and the
         // slab dipole term join the FP64 forces in one merge at the end.
-        PHASE(pack_mixed(c, force_rebuild), "pack");  // also decides the list rebuild
+        PHASE(pack_mixed(c, force_rebuild, reset_status), "pack");  // also decides the list rebuild
         const cudaStream_t s0 = c.stream;
         MDG_CUDA(cudaEventRecord(c.ev_fork, s0));
         MDG_CUDA(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
@@ -537,6 +542,7 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
         if (rc) return bail(rc);
         pack_setup(c);
         c.pk.tc = c.d_tc_atoms;
+        c.pk.cmax = c.d_tc_cmax;
     }
     rc = nnlist_setup(c, x0, y0, z0);
     if (rc) return bail(rc);
@@ -918,11 +924,12 @@ static void snapshot(Ctx& c, bool restore) {
 
 // One MD step (src/main.f90:60-64): predict, forces, correct, SHAKE.
 static int step_launch(Ctx& c) {
-    predict_launch(c);
-    int rc = launch_force(c, false, false);
+    const bool fp64 = c.precision != MDG_MIXED, shake = c.v.nmove > c.v.nliqa;
+    predict_launch(c, fp64, shake);
+    int rc = launch_force(c, false, false, fp64);
     if (rc) return rc;
     correct_launch(c);
-    if (c.v.nmove > c.v.nliqa) shake_launch(c, c.d_ft);
+    if (shake) shake_launch(c, c.d_ft, true);
     if (c.meas.init && c.meas.profiles) measure_do_launch(c, c.v.x, c.v.y, c.v.z);
     return MDG_OK;
 }

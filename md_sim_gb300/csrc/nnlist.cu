@@ -175,8 +175,11 @@ struct WarpOut {
 
 // One warp per head: the warp walks the neighbouring cells, lanes test 32 candidates at a time
 // and the kept partners (j > i) are appended in order with a ballot.
-__global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* cpos, const double4* hpos) {
+__global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* cpos, const double4* hpos,
+                           int* cell_count) {
     if (!v.status[ST_REBUILD]) return;
+    // the binning counts go back to zero for the next rebuild (zeroed at allocation)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.ncell; i += gridDim.x * blockDim.x) cell_count[i] = 0;
     const int lane = threadIdx.x & 31;
     const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (h >= v.nheads) return;
@@ -398,12 +401,11 @@ void nnlist_build(Ctx& c) {
     const Grid& g = c.grid;
     const int nh = std::max(v.nheads, 1);
     const int nbk = std::max((std::max(nh, std::max(v.nrig, v.nmove - v.nriga)) + kNT - 1) / kNT, 1);
-    cudaMemsetAsync(c.d_cell_count, 0, sizeof(int) * g.ncell, c.stream);
     k_bin_heads<<<nbk, kNT, 0, c.stream>>>(v, g, c.d_head_cell, c.d_cell_count, c.d_hpos);
     k_scan_cells<<<1, kNT, 0, c.stream>>>(v, g.ncell, c.d_cell_count, c.d_cell_start);
     k_scatter_heads<<<(nh + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, c.d_head_cell, c.d_cell_count, c.d_cell_start,
                                                                  c.d_hpos, c.d_cpos);
-    k_build_hh<<<(nh + 3) / 4, 128, 0, c.stream>>>(v, g, c.d_cell_start, c.d_cpos, c.d_hpos);
+    k_build_hh<<<(nh + 3) / 4, 128, 0, c.stream>>>(v, g, c.d_cell_start, c.d_cpos, c.d_hpos, c.d_cell_count);
     if (v.nwall > 0) k_build_hw<<<(nh + 3) / 4, 128, 0, c.stream>>>(v, c.wgrid, c.d_wcell_start, c.d_wpos, c.d_hpos);
 }
 

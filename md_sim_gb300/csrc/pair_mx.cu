@@ -31,6 +31,7 @@ namespace {
 constexpr int kWarps = 8;
 constexpr int kNT = kWarps * 32;
 constexpr int kWSeg = 64;  // wall partners per work item of the head-wall loop
+constexpr int kPackBlocks = 152 * 8;  // most blocks of the packing kernel
 constexpr float kPf = (float)kP, kA1f = (float)kA1, kA2f = (float)kA2, kA3f = (float)kA3, kA4f = (float)kA4,
                 kA5f = (float)kA5;
 
@@ -118,8 +119,9 @@ __device__ __forceinline__ uint32_t frac32(double t) {
 // block (which the caller zeroed), and takes the neighbour-list rebuild decision
 // (src/forcem.f90:245-250): the maximum squared displacement of the centres of mass and flexible
 // atoms since the last rebuild, compared by the block that finishes last.
-__global__ void k_pack(View v, Pk pk, int dip, int force) {
+__global__ void k_pack(View v, Pk pk, int dip, int force, int reset_status) {
     double mz = 0.0, md = 0.0;
+    if (pk.cmax && blockIdx.x == 0 && threadIdx.x == 0) *pk.cmax = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.nrig + (v.nmove - v.nriga);
          i += gridDim.x * blockDim.x) {
         double a, b, c;
@@ -165,20 +167,45 @@ __global__ void k_pack(View v, Pk pk, int dip, int force) {
         }
         pk.Q[a] = q;
     }
-    if (dip) block_atomic_sum<256>(mz, &v.acc[2 * v.nijt + ACC_DIPZ]);
-    for (int o = 16; o > 0; o >>= 1) md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
-    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&v.acc[2 * v.nijt + ACC_MAXD], md);
+    __shared__ double red[8];
     __shared__ bool last;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    mz = warp_sum(mz);
+    if (l == 0) red[w] = mz;
+    for (int o = 16; o > 0; o >>= 1) md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+    if (l == 0) atomic_max_nonneg(&v.acc[2 * v.nijt + ACC_MAXD], md);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int k = 0; k < 8; ++k) b += red[k];
+        pk.part[blockIdx.x] = b;  // this block's share of the slab dipole
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(&v.status[ST_PACK_DONE], 1) == (int)gridDim.x - 1;
     __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        const double aux = fmax(__ldcg(&v.acc[2 * v.nijt + ACC_MAXD]), v.dshsq);
+    if (!last) return;
+    // The last block: the dipole in block order (deterministic), the rebuild decision, and the
+    // energy sums of this evaluation cleared for the loops queued after this kernel.
+    __threadfence();
+    double s = 0.0;
+    for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += __ldcg(&pk.part[b]);
+    s = warp_sum(s);
+    __syncthreads();
+    if (l == 0) red[w] = s;
+    __syncthreads();
+    const int na = 2 * v.nijt + ACC_NSLOT, kmax = 2 * v.nijt + ACC_MAXD, kdip = 2 * v.nijt + ACC_DIPZ;
+    for (int k = threadIdx.x; k < na; k += blockDim.x)
+        if (k != kmax && k != kdip) v.acc[k] = 0.0;
+    if (reset_status && threadIdx.x < 2) v.status[ST_LIST_OVF + threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        double dz = 0.0;
+        for (int k = 0; k < 8; ++k) dz += red[k];
+        v.acc[kdip] = dip ? dz : 0.0;
+        const double aux = fmax(__ldcg(&v.acc[kmax]), v.dshsq);
         v.status[ST_REBUILD] = (force || v.status[ST_FORCE_RB] || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
         v.status[ST_FORCE_RB] = 0;
-        v.acc[2 * v.nijt + ACC_MAXD] = 0.0;
+        v.acc[kmax] = 0.0;
         v.status[ST_PACK_DONE] = 0;
     }
 }
@@ -465,6 +492,7 @@ void pack_setup(Ctx& c) {
     c.pk.Q = (float4*)dalloc(c, sizeof(float4) * n);
     c.pk.zlo = (float*)dalloc(c, sizeof(float) * n);
     c.pk.F = (float4*)dalloc(c, sizeof(float4) * std::max(v.nmove, 1));
+    c.pk.part = (double*)dalloc(c, sizeof(double) * kPackBlocks);
     c.pk.zper = v.bulk ? 1 : 0;
     c.pk.sx = (float)(v.lx / 4294967296.0);
     c.pk.sy = (float)(v.ly / 4294967296.0);
@@ -476,11 +504,11 @@ double slab_crf0(const Ctx& c) {
     return -2.0 * (double)3.1415926535898f * c.v.lzi * c.v.lxi * c.v.lyi;
 }
 
-void pack_mixed(Ctx& c, bool force_rebuild) {
+void pack_mixed(Ctx& c, bool force_rebuild, bool reset_status) {
     const View& v = c.v;
     const int n = std::max(std::max(v.ntota, v.nrig + (v.nmove - v.nriga)), 1);
-    k_pack<<<std::min((n + 255) / 256, 152 * 8), 256, 0, c.stream>>>(v, c.pk, c.variant == MDG_SLAB ? 1 : 0,
-                                                                    force_rebuild ? 1 : 0);
+    k_pack<<<std::min((n + 255) / 256, kPackBlocks), 256, 0, c.stream>>>(v, c.pk, c.variant == MDG_SLAB ? 1 : 0,
+                                                                        force_rebuild ? 1 : 0, reset_status ? 1 : 0);
 }
 
 void merge_mixed(Ctx& c, const double* frc, bool dipole) {

@@ -857,8 +857,7 @@ void recip_tc(Ctx& c) {
     const TcPlan& p = c.tcp;
     if (ks.nk == 0 || v.nmove == 0) return;
     TcDims d{p.KN, p.NN, p.NP, p.KS, ks.nrow, p.nchunk2, (float)ks.pipix, (float)ks.pipiy, (float)ks.pipiz, p.nst2};
-    // c.d_tc_atoms was filled by the packing kernel of the real-space phase of this evaluation
-    cudaMemsetAsync(c.d_tc_cmax, 0, sizeof(float), c.stream);
+    // c.d_tc_atoms was filled, and c.d_tc_cmax cleared, by the packing kernel of this evaluation
     if (p.tpc1 == 4)
         k_tc_sfac<4><<<dim3(p.grid1x, p.nsplit1), P1<4>::kThreads, p.smem1, c.stream>>>(
             v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1);

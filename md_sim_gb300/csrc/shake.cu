@@ -381,10 +381,10 @@ __global__ void k_shake_status(View v, const int* sweeps) {
 }
 
 // Verlet + SHAKE on the device state (x/y/z, xold) with forces d_ft (3 x (nmove - nriga)).
-void shake_launch(Ctx& c, const double* d_ft) {
+void shake_launch(Ctx& c, const double* d_ft, bool kps_clear) {
     const View& v = c.v;
     const int nsurf = v.nmove - v.nliqa;
-    cudaMemsetAsync(c.d_kps, 0, sizeof(double) * v.nit, c.stream);
+    if (!kps_clear) cudaMemsetAsync(c.d_kps, 0, sizeof(double) * v.nit, c.stream);
     if (nsurf > 0)
         k_verlet<<<(nsurf + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, d_ft, c.d_xold, c.d_yold, c.d_zold, c.d_kps);
     if (c.ncons == 0) return;
