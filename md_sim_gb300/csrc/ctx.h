@@ -235,6 +235,7 @@ struct Ctx {
     // host staging (pinned)
     double* h_acc = nullptr;
     int* h_status = nullptr;
+    double* h_small = nullptr;  // pinned: SHAKE's per-type kinetic sums (nit) + its sweep words (1)
     std::string err;
 };
 
@@ -299,6 +300,21 @@ int widom(Ctx& c, const mdg_widom_params* p, double* seed, double* pave, int64_t
 int shake_setup(Ctx& c, const mdg_sysdesc* s);
 void shake_launch(Ctx& c, const double* d_ft, bool kps_clear = false);  // kps_clear: kps already zeroed
 // integrate.cu
+// Arrays of one drop-in call moved by one kernel through the GPU's mapping of pinned host memory
+// (hostio.cu); 8-byte words.
+struct IoBatch {
+    static constexpr int kMax = 24;
+    const unsigned long long* src[kMax];
+    unsigned long long* dst[kMax];
+    long n[kMax];
+    int nseg = 0;
+    long nmax = 0;
+};
+// Queues the move of nwords 8-byte words host -> device (h2d) or back: into the batch when the
+// host side is pinned, else as a cudaMemcpyAsync on the context's stream.
+cudaError_t io_add(Ctx& c, IoBatch& b, void* dst, const void* src, long nwords, bool h2d);
+void io_flush(Ctx& c, IoBatch& b);  // launches the batch's copy kernel and empties it
+
 // clear_acc / clear_kps: also zero the energy sums of the force call next / the surface atoms'
 // kinetic sums of the SHAKE call after it
 void predict_launch(Ctx& c, bool clear_acc = false, bool clear_kps = false);

@@ -338,6 +338,7 @@ void mdg_destroy(mdg_ctx* c) {
     if (c->force_exec) cudaGraphExecDestroy(c->force_exec);
     if (c->h_acc) cudaFreeHost(c->h_acc);
     if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->h_small) cudaFreeHost(c->h_small);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     else if (c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
@@ -524,7 +525,8 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
     c.d_fc = (double*)dalloc(c, sizeof(double) * 3 * std::max(v.nrig, 1));
     c.d_tq = (double*)dalloc(c, sizeof(double) * 3 * std::max(v.nrig, 1));
     if (cudaMallocHost(&c.h_acc, sizeof(double) * (2 * nijt + ACC_NSLOT)) != cudaSuccess ||
-        cudaMallocHost(&c.h_status, sizeof(int) * ST_NWORDS) != cudaSuccess)
+        cudaMallocHost(&c.h_status, sizeof(int) * ST_NWORDS) != cudaSuccess ||
+        cudaMallocHost(&c.h_small, sizeof(double) * (std::max(v.nit, 1) + 1)) != cudaSuccess)
         c.alloc_failed = true;
     if (c.alloc_failed) {
         c.err = "out of device memory";
@@ -696,17 +698,21 @@ int mdg_force_get(mdg_ctx* cp, const double* x0, const double* y0, const double*
     View& v = c.v;
     const int nm = v.nmove, nrig = v.nrig, nflex = v.nmove - v.nriga;
     if (!x0 || !y0 || !z0 || !rsx || !rsy || !rsz) return set_err(&c, MDG_E_ARG, "null position array");
-    MDG_CUDA(cudaMemcpyAsync(v.x, x0, sizeof(double) * nm, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(v.y, y0, sizeof(double) * nm, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(v.z, z0, sizeof(double) * nm, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(v.rsx, rsx, sizeof(double) * nm, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(v.rsy, rsy, sizeof(double) * nm, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(v.rsz, rsz, sizeof(double) * nm, cudaMemcpyHostToDevice, c.stream));
+    if (nrig > 0 && (!cx0 || !cy0 || !cz0)) return set_err(&c, MDG_E_ARG, "null centre array");
+    // inputs: pinned host arrays through one gather kernel, others by copy
+    IoBatch io;
+    MDG_CUDA(io_add(c, io, v.x, x0, nm, true));
+    MDG_CUDA(io_add(c, io, v.y, y0, nm, true));
+    MDG_CUDA(io_add(c, io, v.z, z0, nm, true));
+    MDG_CUDA(io_add(c, io, v.rsx, rsx, nm, true));
+    MDG_CUDA(io_add(c, io, v.rsy, rsy, nm, true));
+    MDG_CUDA(io_add(c, io, v.rsz, rsz, nm, true));
     if (nrig > 0) {
-        MDG_CUDA(cudaMemcpyAsync(v.cx, cx0, sizeof(double) * nrig, cudaMemcpyHostToDevice, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(v.cy, cy0, sizeof(double) * nrig, cudaMemcpyHostToDevice, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(v.cz, cz0, sizeof(double) * nrig, cudaMemcpyHostToDevice, c.stream));
+        MDG_CUDA(io_add(c, io, v.cx, cx0, nrig, true));
+        MDG_CUDA(io_add(c, io, v.cy, cy0, nrig, true));
+        MDG_CUDA(io_add(c, io, v.cz, cz0, nrig, true));
     }
+    io_flush(c, io);
     // The force phases run as one captured graph (launched per call; host launch cost of one
     // graph instead of ~20 kernels), and the results are queued right behind it with the status
     // words, so the call waits once.  A list overflow (rare: the capacity grows at create) is
@@ -726,40 +732,43 @@ int mdg_force_get(mdg_ctx* cp, const double* x0, const double* y0, const double*
             if (ie != cudaSuccess) return set_err(&c, MDG_E_CUDA, std::string("force graph: ") + cudaGetErrorString(ie));
         }
         MDG_CUDA(cudaGraphLaunch(c.force_exec, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(c.h_status, v.status, sizeof(int) * ST_NWORDS, cudaMemcpyDeviceToHost, c.stream));
         graph_ok = true;
     } else {
         rc = run_force(c, false);
         if (rc) return rc;
     }
     for (int pass = 0; pass < 2; ++pass) {
+    // results and the status words, one scatter kernel for the pinned ones
     if (ftx && nflex > 0) {
-        MDG_CUDA(cudaMemcpyAsync(ftx, c.d_ft, sizeof(double) * nflex, cudaMemcpyDeviceToHost, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(fty, c.d_ft + nflex, sizeof(double) * nflex, cudaMemcpyDeviceToHost, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(ftz, c.d_ft + 2 * nflex, sizeof(double) * nflex, cudaMemcpyDeviceToHost, c.stream));
+        MDG_CUDA(io_add(c, io, ftx, c.d_ft, nflex, false));
+        MDG_CUDA(io_add(c, io, fty, c.d_ft + nflex, nflex, false));
+        MDG_CUDA(io_add(c, io, ftz, c.d_ft + 2 * nflex, nflex, false));
     }
     if (nrig > 0) {
         if (fcx) {
-            MDG_CUDA(cudaMemcpyAsync(fcx, c.d_fc, sizeof(double) * nrig, cudaMemcpyDeviceToHost, c.stream));
-            MDG_CUDA(cudaMemcpyAsync(fcy, c.d_fc + nrig, sizeof(double) * nrig, cudaMemcpyDeviceToHost, c.stream));
-            MDG_CUDA(cudaMemcpyAsync(fcz, c.d_fc + 2 * nrig, sizeof(double) * nrig, cudaMemcpyDeviceToHost, c.stream));
+            MDG_CUDA(io_add(c, io, fcx, c.d_fc, nrig, false));
+            MDG_CUDA(io_add(c, io, fcy, c.d_fc + nrig, nrig, false));
+            MDG_CUDA(io_add(c, io, fcz, c.d_fc + 2 * nrig, nrig, false));
         }
         if (tx) {
-            MDG_CUDA(cudaMemcpyAsync(tx, c.d_tq, sizeof(double) * nrig, cudaMemcpyDeviceToHost, c.stream));
-            MDG_CUDA(cudaMemcpyAsync(ty, c.d_tq + nrig, sizeof(double) * nrig, cudaMemcpyDeviceToHost, c.stream));
-            MDG_CUDA(cudaMemcpyAsync(tz, c.d_tq + 2 * nrig, sizeof(double) * nrig, cudaMemcpyDeviceToHost, c.stream));
+            MDG_CUDA(io_add(c, io, tx, c.d_tq, nrig, false));
+            MDG_CUDA(io_add(c, io, ty, c.d_tq + nrig, nrig, false));
+            MDG_CUDA(io_add(c, io, tz, c.d_tq + 2 * nrig, nrig, false));
         }
-        MDG_CUDA(cudaMemcpyAsync(rsx, v.rsx, sizeof(double) * 3, cudaMemcpyDeviceToHost, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(rsy, v.rsy, sizeof(double) * 3, cudaMemcpyDeviceToHost, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(rsz, v.rsz, sizeof(double) * 3, cudaMemcpyDeviceToHost, c.stream));
+        MDG_CUDA(io_add(c, io, rsx, v.rsx, 3, false));
+        MDG_CUDA(io_add(c, io, rsy, v.rsy, 3, false));
+        MDG_CUDA(io_add(c, io, rsz, v.rsz, 3, false));
     }
     if (fx) {
-        MDG_CUDA(cudaMemcpyAsync(fx, v.fx, sizeof(double) * nm, cudaMemcpyDeviceToHost, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(fy, v.fy, sizeof(double) * nm, cudaMemcpyDeviceToHost, c.stream));
-        MDG_CUDA(cudaMemcpyAsync(fz, v.fz, sizeof(double) * nm, cudaMemcpyDeviceToHost, c.stream));
+        MDG_CUDA(io_add(c, io, fx, v.fx, nm, false));
+        MDG_CUDA(io_add(c, io, fy, v.fy, nm, false));
+        MDG_CUDA(io_add(c, io, fz, v.fz, nm, false));
     }
     const int nacc = 2 * v.nijt + ACC_NSLOT;
-    MDG_CUDA(cudaMemcpyAsync(c.h_acc, v.acc, sizeof(double) * nacc, cudaMemcpyDeviceToHost, c.stream));
+    MDG_CUDA(io_add(c, io, c.h_acc, v.acc, nacc, false));
+    static_assert(ST_NWORDS % 2 == 0, "status words move as 8-byte pairs");
+    MDG_CUDA(io_add(c, io, c.h_status, v.status, ST_NWORDS / 2, false));
+    io_flush(c, io);
     rc = sync_check(c, "mdg_force_get");
     if (rc) return rc;
     if (!graph_ok || pass == 1) break;
@@ -829,28 +838,36 @@ int mdg_shake(mdg_ctx* cp, double* x0, double* y0, double* z0, double* xold, dou
     View& v = c.v;
     const int nl = v.nliqa, ns = v.nmove - v.nliqa, nold = v.ntota - v.nliqa, nflex = v.nmove - v.nriga;
     if (ns <= 0) return MDG_OK;
-    MDG_CUDA(cudaMemcpyAsync(v.x + nl, x0 + nl, sizeof(double) * ns, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(v.y + nl, y0 + nl, sizeof(double) * ns, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(v.z + nl, z0 + nl, sizeof(double) * ns, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(c.d_xold, xold, sizeof(double) * nold, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(c.d_yold, yold, sizeof(double) * nold, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(c.d_zold, zold, sizeof(double) * nold, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(c.d_ft_in, ftx, sizeof(double) * nflex, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(c.d_ft_in + nflex, fty, sizeof(double) * nflex, cudaMemcpyHostToDevice, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(c.d_ft_in + 2 * nflex, ftz, sizeof(double) * nflex, cudaMemcpyHostToDevice, c.stream));
+    if (!x0 || !y0 || !z0 || !xold || !yold || !zold || !ftx || !fty || !ftz)
+        return set_err(&c, MDG_E_ARG, "null array");
+    IoBatch io;  // pinned host arrays move through one gather and one scatter kernel
+    MDG_CUDA(io_add(c, io, v.x + nl, x0 + nl, ns, true));
+    MDG_CUDA(io_add(c, io, v.y + nl, y0 + nl, ns, true));
+    MDG_CUDA(io_add(c, io, v.z + nl, z0 + nl, ns, true));
+    MDG_CUDA(io_add(c, io, c.d_xold, xold, nold, true));
+    MDG_CUDA(io_add(c, io, c.d_yold, yold, nold, true));
+    MDG_CUDA(io_add(c, io, c.d_zold, zold, nold, true));
+    MDG_CUDA(io_add(c, io, c.d_ft_in, ftx, nflex, true));
+    MDG_CUDA(io_add(c, io, c.d_ft_in + nflex, fty, nflex, true));
+    MDG_CUDA(io_add(c, io, c.d_ft_in + 2 * nflex, ftz, nflex, true));
+    io_flush(c, io);
     cudaMemsetAsync(v.status + ST_SHAKE_MAXIT, 0, sizeof(int) * 2, c.stream);
     shake_launch(c, c.d_ft_in);
-    MDG_CUDA(cudaMemcpyAsync(x0 + nl, v.x + nl, sizeof(double) * ns, cudaMemcpyDeviceToHost, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(y0 + nl, v.y + nl, sizeof(double) * ns, cudaMemcpyDeviceToHost, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(z0 + nl, v.z + nl, sizeof(double) * ns, cudaMemcpyDeviceToHost, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(xold, c.d_xold, sizeof(double) * nold, cudaMemcpyDeviceToHost, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(yold, c.d_yold, sizeof(double) * nold, cudaMemcpyDeviceToHost, c.stream));
-    MDG_CUDA(cudaMemcpyAsync(zold, c.d_zold, sizeof(double) * nold, cudaMemcpyDeviceToHost, c.stream));
-    std::vector<double> hk(std::max(v.nit, 1));
-    int sw[2] = {0, 1};
-    MDG_CUDA(cudaMemcpyAsync(hk.data(), c.d_kps, sizeof(double) * v.nit, cudaMemcpyDeviceToHost, c.stream));
-    if (c.ncons > 0) MDG_CUDA(cudaMemcpyAsync(sw, c.d_sweeps, sizeof(sw), cudaMemcpyDeviceToHost, c.stream));
-    int rc = read_status(c);
+    MDG_CUDA(io_add(c, io, x0 + nl, v.x + nl, ns, false));
+    MDG_CUDA(io_add(c, io, y0 + nl, v.y + nl, ns, false));
+    MDG_CUDA(io_add(c, io, z0 + nl, v.z + nl, ns, false));
+    MDG_CUDA(io_add(c, io, xold, c.d_xold, nold, false));
+    MDG_CUDA(io_add(c, io, yold, c.d_yold, nold, false));
+    MDG_CUDA(io_add(c, io, zold, c.d_zold, nold, false));
+    double* hk = c.h_small;
+    int* sw = reinterpret_cast<int*>(c.h_small + std::max(v.nit, 1));
+    sw[0] = 0;
+    sw[1] = 1;
+    MDG_CUDA(io_add(c, io, hk, c.d_kps, v.nit, false));
+    if (c.ncons > 0) MDG_CUDA(io_add(c, io, sw, c.d_sweeps, 1, false));  // two int words
+    MDG_CUDA(io_add(c, io, c.h_status, v.status, ST_NWORDS / 2, false));
+    io_flush(c, io);
+    int rc = sync_check(c, "mdg_shake");
     if (rc) return rc;
     double ks = 0.0;
     for (int t = 0; t < v.nit; ++t) {
