@@ -189,6 +189,15 @@ int mdg_shake(mdg_ctx* ctx, double* x0, double* y0, double* z0, double* xold, do
               double* zold, const double* ftx, const double* fty, const double* ftz, double* kps,
               double* tkps, int32_t* sweeps);
 
+/* Transfers of the two calls above.  Arrays in pinned host memory are read and written by the
+ * GPU in place (one gather and one scatter kernel per call, over NVLink-C2C on a Grace-Blackwell
+ * node); other arrays are copied through the driver's staging buffers, with the same results but
+ * a few microseconds more per array.  mdg_pin_host pins an existing host array (for example a
+ * Fortran module array, once after allocation); mdg_unpin_host releases it before it is freed.
+ * No counterpart in the reference (its arrays never leave the host). */
+int mdg_pin_host(void* p, int64_t bytes);
+int mdg_unpin_host(void* p);
+
 /* ---------------------------------------------------------------------------------------------
  * Resident mode: the whole MD step on the device.  The integrator that the reference keeps in
  * Fortran (move_predict / move_correct, src/move.f90:48-383) runs as device kernels around the

@@ -189,6 +189,9 @@ class Lib:
         g("get_lists", C.c_int, [C.c_void_p, I64P, I64P, C.c_int64, I64P, I64P, C.c_int64, I64P, I64P])
         g("force_get", C.c_int, [C.c_void_p] + [DP] * 21 + [C.POINTER(Energies)])
         g("shake", C.c_int, [C.c_void_p] + [DP] * 10 + [C.POINTER(C.c_double), C.POINTER(C.c_int32)])
+        if self.has("pin_host"):
+            g("pin_host", C.c_int, [C.c_void_p, C.c_int64])
+            g("unpin_host", C.c_int, [C.c_void_p])
         if self.has("set_stream"):
             g("set_stream", C.c_int, [C.c_void_p, C.c_void_p])
             g("phase_times", C.c_int, [C.c_void_p, C.c_int, DP])

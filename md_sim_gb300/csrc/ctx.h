@@ -318,7 +318,8 @@ void io_flush(Ctx& c, IoBatch& b);  // launches the batch's copy kernel and empt
 // clear_acc / clear_kps: also zero the energy sums of the force call next / the surface atoms'
 // kinetic sums of the SHAKE call after it
 void predict_launch(Ctx& c, bool clear_acc = false, bool clear_kps = false);
-void correct_launch(Ctx& c);
+// merge: also the mixed form's final merge + force_sum, left out of the force phases before it
+void correct_launch(Ctx& c, bool merge = false);
 
 int set_err(Ctx* c, int code, const std::string& msg);
 void* dalloc(Ctx& c, size_t bytes);

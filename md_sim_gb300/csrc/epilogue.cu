@@ -10,6 +10,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "merge.cuh"
 
 namespace mdg {
 
@@ -108,68 +109,14 @@ __global__ void k_force_sum(View v, double* ft, double* fc, double* tq) {
 }
 
 // For systems without bend angles (and no histograms), the final merge of the mixed form fused
-// with force_sum: per rigid molecule or flexible atom, the FP32 accumulator F, the reciprocal
-// forces frc and the slab dipole term join the FP64 forces, which then give ft, the centre-of-mass
-// forces, the torques and the sum of all forces as k_force_sum does.
-__global__ void k_merge_sum(View v, Pk pk, const double* __restrict__ frc, double crf0, double* ft, double* fc,
-                            double* tq) {
-    const double crf = crf0 != 0.0 ? 2.0 * crf0 * v.facq * v.acc[2 * v.nijt + ACC_DIPZ] : 0.0;
-    auto merged = [&](int a, double& gx, double& gy, double& gz) {
-        const float4 f = pk.F[a];
-        double hx = (double)f.x, hy = (double)f.y, hz = (double)f.z;
-        if (frc) {
-            hx += frc[a];
-            hy += frc[v.nmove + a];
-            hz += frc[2 * v.nmove + a];
-        }
-        if (crf0 != 0.0) hz += crf * v.q[a];
-        gx = v.fx[a] + hx;
-        gy = v.fy[a] + hy;
-        gz = v.fz[a] + hz;
-        v.fx[a] = gx;
-        v.fy[a] = gy;
-        v.fz[a] = gz;
-        pk.F[a] = make_float4(0.f, 0.f, 0.f, 0.f);
-    };
+// with force_sum: per rigid molecule or flexible atom (merge.cuh), then the sum of all forces.
+__global__ void k_merge_sum(View v, MergeArgs A) {
+    const MergeArgs M = merge_begin(v, A);
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    const int nflex = v.nmove - v.nriga;
-    const int nu = v.nrig + nflex;
+    const int nu = v.nrig + (v.nmove - v.nriga);
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
-        if (u < v.nrig) {
-            const int m = u, j = 3 * m;
-            double f0x, f0y, f0z, f1x, f1y, f1z, f2x, f2y, f2z;
-            merged(j, f0x, f0y, f0z);
-            merged(j + 1, f1x, f1y, f1z);
-            merged(j + 2, f2x, f2y, f2z);
-            sx += f0x + f1x + f2x;
-            sy += f0y + f1y + f2y;
-            sz += f0z + f1z + f2z;
-            fc[m] = f0x + f1x + f2x;
-            fc[v.nrig + m] = f0y + f1y + f2y;
-            fc[2 * v.nrig + m] = f0z + f1z + f2z;
-            const double cx = v.cx[m], cy = v.cy[m], cz = v.cz[m];
-            const double r0x = v.x[j] - cx, r1x = v.x[j + 1] - cx, r2x = v.x[j + 2] - cx;
-            const double r0y = v.y[j] - cy, r1y = v.y[j + 1] - cy, r2y = v.y[j + 2] - cy;
-            const double r0z = v.z[j] - cz, r1z = v.z[j + 1] - cz, r2z = v.z[j + 2] - cz;
-            tq[m] = (r0y * f0z - r0z * f0y) + (r1y * f1z - r1z * f1y) + (r2y * f2z - r2z * f2y);
-            tq[v.nrig + m] = (r0z * f0x - r0x * f0z) + (r1z * f1x - r1x * f1z) + (r2z * f2x - r2x * f2z);
-            tq[2 * v.nrig + m] = (r0x * f0y - r0y * f0x) + (r1x * f1y - r1y * f1x) + (r2x * f2y - r2y * f2x);
-            if (m == v.nrig - 1) {
-                v.rsx[0] = r0x; v.rsx[1] = r1x; v.rsx[2] = r2x;
-                v.rsy[0] = r0y; v.rsy[1] = r1y; v.rsy[2] = r2y;
-                v.rsz[0] = r0z; v.rsz[1] = r1z; v.rsz[2] = r2z;
-            }
-        } else {
-            const int k = u - v.nrig, i = v.nriga + k;
-            double gx, gy, gz;
-            merged(i, gx, gy, gz);
-            sx += gx;
-            sy += gy;
-            sz += gz;
-            ft[k] = gx;
-            ft[nflex + k] = gy;
-            ft[2 * nflex + k] = gz;
-        }
+        if (u < v.nrig) merge_rigid(v, M, u, sx, sy, sz);
+        else merge_flex(v, M, u - v.nrig, sx, sy, sz);
     }
     block_atomic_sum<kNT>(sx, &v.acc[2 * v.nijt + ACC_FWS0 + 0]);
     block_atomic_sum<kNT>(sy, &v.acc[2 * v.nijt + ACC_FWS0 + 1]);
@@ -178,12 +125,23 @@ __global__ void k_merge_sum(View v, Pk pk, const double* __restrict__ frc, doubl
 
 }  // namespace
 
+MergeArgs merge_args(const Ctx& c, const double* frc) {
+    const View& v = c.v;
+    MergeArgs A{};
+    A.pk = c.pk;
+    A.frc = frc;
+    A.crf0 = c.variant == MDG_SLAB ? -2.0 * (double)3.1415926535898f * v.lzi * v.lxi * v.lyi : 0.0;
+    A.ft = c.d_ft;
+    A.fc = c.d_fc;
+    A.tq = c.d_tq;
+    return A;
+}
+
 void merge_force_sum(Ctx& c, const double* frc) {
     const View& v = c.v;
     const int n = std::max(v.nrig + (v.nmove - v.nriga), 1);
-    const double crf0 = c.variant == MDG_SLAB ? -2.0 * (double)3.1415926535898f * v.lzi * v.lxi * v.lyi : 0.0;
     const int nb = std::max(1, std::min((n + kNT - 1) / kNT, 152 * 8));
-    k_merge_sum<<<nb, kNT, 0, c.stream>>>(v, c.pk, frc, crf0, c.d_ft, c.d_fc, c.d_tq);
+    k_merge_sum<<<nb, kNT, 0, c.stream>>>(v, merge_args(c, frc));
 }
 
 void dipole_correction(Ctx& c) {

@@ -17,6 +17,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "merge.cuh"
 
 namespace mdg {
 
@@ -380,13 +381,32 @@ __device__ void thermo_corr(const View& v, const Dyn& D) {
 }
 
 // The correctors read the thermostat values of the predictor; the block that finishes last then
-// adds uconf/press and corrects the thermostat.
-template <int NT>
-__global__ void __launch_bounds__(NT) k_corr(View v, Dyn D, int slab, int lanes) {
-    const int nu = D.nion + v.nrig;
+// adds uconf/press and corrects the thermostat.  MERGE: the mixed force form's final merge and
+// force_sum (merge.cuh) run here, each unit's just before its corrector, instead of in a kernel
+// of their own; units past the molecules and ions are the surface atoms, whose forces SHAKE's
+// Verlet step reads next.
+template <int NT, bool MERGE>
+__global__ void __launch_bounds__(NT) k_corr(View v, Dyn D, int slab, int lanes, MergeArgs A) {
+    const int nsurf = MERGE ? v.nmove - v.nliqa : 0;
+    const int nu = D.nion + v.nrig + nsurf;
+    MergeArgs M;
+    if constexpr (MERGE) M = merge_begin(v, A);
+    double sx = 0.0, sy = 0.0, sz = 0.0;
     for (int r = 0, u; (u = unit_of<NT>(lanes, r)) >= 0 && u < nu; ++r) {
-        if (u < D.nion) corr_ion(v, D, u);
-        else corr_rigid(v, D, u - D.nion);
+        if (u < D.nion) {
+            if constexpr (MERGE) merge_flex(v, M, u, sx, sy, sz);
+            corr_ion(v, D, u);
+        } else if (u < D.nion + v.nrig) {
+            if constexpr (MERGE) merge_rigid(v, M, u - D.nion, sx, sy, sz);
+            corr_rigid(v, D, u - D.nion);
+        } else if constexpr (MERGE) {
+            merge_flex(v, M, u - v.nrig, sx, sy, sz);  // surface atom: flexible index nion + s
+        }
+    }
+    if constexpr (MERGE) {
+        block_atomic_sum<NT>(sx, &v.acc[2 * v.nijt + ACC_FWS0 + 0]);
+        block_atomic_sum<NT>(sy, &v.acc[2 * v.nijt + ACC_FWS0 + 1]);
+        block_atomic_sum<NT>(sz, &v.acc[2 * v.nijt + ACC_FWS0 + 2]);
     }
     if (last_block(&D.done[1]) && threadIdx.x == 0) {
         uconf(v, D, slab);
@@ -432,12 +452,19 @@ void predict_launch(Ctx& c, bool clear_acc, bool clear_kps) {
     else k_pred<128><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, lanes, z);
 }
 
-void correct_launch(Ctx& c) {
+void correct_launch(Ctx& c, bool merge) {
     const View& v = c.v;
     Dyn D = dyn_of(c);
-    const int nu = D.nion + v.nrig, lanes = lanes_of(nu), slab = c.variant == MDG_SLAB ? 1 : 0;
-    if (lanes < 32) k_corr<32><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes);
-    else k_corr<128><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes);
+    const int nu = D.nion + v.nrig + (merge ? v.nmove - v.nliqa : 0), lanes = lanes_of(nu);
+    const int slab = c.variant == MDG_SLAB ? 1 : 0;
+    const MergeArgs A = merge ? merge_args(c, c.d_frc) : MergeArgs{};
+    if (merge) {
+        if (lanes < 32) k_corr<32, true><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
+        else k_corr<128, true><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes, A);
+    } else {
+        if (lanes < 32) k_corr<32, false><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
+        else k_corr<128, false><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes, A);
+    }
 }
 
 }  // namespace mdg

@@ -215,18 +215,25 @@ int phase_check(Ctx& c, const char* name) {
         if (prc_) return prc_;              \
     } while (0)
 
+// The mixed form ends in one kernel that merges the force parts and does force_sum, when no bend
+// angles or histograms need the merged site forces first.
+static bool merge_fusable(const Ctx& c) {
+    return c.precision == MDG_MIXED && c.nang_terms == 0 && !(c.meas.init && c.meas.force_hist);
+}
+
 // Queues the force phases on device-resident positions (no synchronisation).  acc_clear: the
 // energy sums were zeroed by the kernel before (the predictor of a resident step).  In the mixed
 // form the packing kernel clears them (and the overflow words), which keeps memset nodes, slow
-// to start inside a graph, off the critical path.
-int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear = false) {
+// to start inside a graph, off the critical path.  defer_merge: leave that final merge kernel to
+// the caller (the resident step fuses it into the corrector).
+int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear = false, bool defer_merge = false) {
     View& v = c.v;
     if (c.precision != MDG_MIXED) {
         if (!acc_clear) cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
         if (reset_status) cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
     }
     const bool hist = c.meas.init && c.meas.force_hist;
-    const bool fused = c.precision == MDG_MIXED && c.nang_terms == 0 && !hist;
+    const bool fused = merge_fusable(c);
     if (c.precision == MDG_MIXED) {
         // The tensor-core reciprocal sum needs only the packed atom records: it runs on a side
         // stream while the main stream does the list, the real-space loops and the wall tail.
@@ -270,7 +277,7 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
         }
         MDG_CUDA(cudaStreamWaitEvent(s0, c.ev_join, 0));
         if (fused) {
-            PHASE(merge_force_sum(c, c.d_frc), "merge + force_sum");
+            if (!defer_merge) PHASE(merge_force_sum(c, c.d_frc), "merge + force_sum");
         } else {
             PHASE(merge_mixed(c, c.d_frc, true), "merge");
         }
@@ -886,6 +893,26 @@ int mdg_shake(mdg_ctx* cp, double* x0, double* y0, double* z0, double* xold, dou
     return MDG_OK;
 }
 
+int mdg_pin_host(void* p, int64_t bytes) {
+    if (!p || bytes <= 0) return set_err(nullptr, MDG_E_ARG, "mdg_pin_host: null pointer or empty range");
+    const cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, MDG_E_CUDA, std::string("mdg_pin_host: ") + cudaGetErrorString(e));
+    }
+    return MDG_OK;
+}
+
+int mdg_unpin_host(void* p) {
+    if (!p) return set_err(nullptr, MDG_E_ARG, "mdg_unpin_host: null pointer");
+    const cudaError_t e = cudaHostUnregister(p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, MDG_E_CUDA, std::string("mdg_unpin_host: ") + cudaGetErrorString(e));
+    }
+    return MDG_OK;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Resident mode
 // ---------------------------------------------------------------------------------------------
@@ -941,11 +968,11 @@ static void snapshot(Ctx& c, bool restore) {
 
 // One MD step (src/main.f90:60-64): predict, forces, correct, SHAKE.
 static int step_launch(Ctx& c) {
-    const bool fp64 = c.precision != MDG_MIXED, shake = c.v.nmove > c.v.nliqa;
+    const bool fp64 = c.precision != MDG_MIXED, shake = c.v.nmove > c.v.nliqa, fuse = merge_fusable(c);
     predict_launch(c, fp64, shake);
-    int rc = launch_force(c, false, false, fp64);
+    int rc = launch_force(c, false, false, fp64, fuse);
     if (rc) return rc;
-    correct_launch(c);
+    correct_launch(c, fuse);
     if (shake) shake_launch(c, c.d_ft, true);
     if (c.meas.init && c.meas.profiles) measure_do_launch(c, c.v.x, c.v.y, c.v.z);
     return MDG_OK;

@@ -7,6 +7,7 @@ pinned and mixed arrays gives the same numbers (bit-exact for SHAKE, whose kerne
 order; within the run-to-run spread of the atomics' summation order for forces).
 """
 import ctypes as C
+import mmap
 
 import numpy as np
 import pytest
@@ -73,6 +74,36 @@ def test_force_get_pinned_equals_pageable(precision, gpulib):
             assert np.array_equal(got["rs"], ref["rs"])
     finally:
         ctx.close()
+
+
+def test_pin_host_arrays(gpulib):
+    """Arrays pinned in place by mdg_pin_host (as a Fortran host would pin its module arrays)."""
+    s, prm = configs.slab_water(nwat=512, cells=6)
+    prm.precision = abi.MDG_MIXED
+    ctx = abi.Context(gpulib, s.copy(), prm)
+    pinned = []
+
+    def pin(a):
+        # its own whole pages (64 KB covers the Arm hosts' page size): ranges that share a page
+        # cannot be registered twice
+        a = np.asarray(a, dtype=np.float64)
+        mm = mmap.mmap(-1, -(-max(a.nbytes, 8) // 65536) * 65536)
+        b = np.frombuffer(mm, dtype=np.float64, count=a.size)
+        b[:] = a
+        assert gpulib.pin_host(b.ctypes.data, b.nbytes) == 0, gpulib.last_error(None)
+        pinned.append((mm, b))
+        return b
+
+    try:
+        ref = _force_get(gpulib, ctx, s.copy(), _pageable, _pageable)
+        got = _force_get(gpulib, ctx, s.copy(), pin, pin)
+        _close(got, ref, 1e-5)
+        assert np.array_equal(got["rs"], ref["rs"])
+    finally:
+        ctx.close()
+        for mm, b in pinned:
+            assert gpulib.unpin_host(b.ctypes.data) == 0
+    assert gpulib.pin_host(None, 8) != 0  # a null range is refused, not pinned
 
 
 def test_shake_pinned_equals_pageable(gpulib):
