@@ -317,7 +317,9 @@ void io_flush(Ctx& c, IoBatch& b);  // launches the batch's copy kernel and empt
 
 // clear_acc / clear_kps: also zero the energy sums of the force call next / the surface atoms'
 // kinetic sums of the SHAKE call after it
-void predict_launch(Ctx& c, bool clear_acc = false, bool clear_kps = false);
+// pack: also write the mixed form's per-atom records, the slab dipole and the list rebuild
+// decision for the force call next (in place of its packing kernel; no surface atoms)
+void predict_launch(Ctx& c, bool clear_acc = false, bool clear_kps = false, bool pack = false);
 // merge: also the mixed form's final merge + force_sum, left out of the force phases before it
 void correct_launch(Ctx& c, bool merge = false);
 

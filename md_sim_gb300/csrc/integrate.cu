@@ -18,6 +18,7 @@
 #include "common.cuh"
 #include "ctx.h"
 #include "merge.cuh"
+#include "pack.cuh"
 
 namespace mdg {
 
@@ -29,13 +30,13 @@ namespace {
 // the molecules, since there the per-molecule chain of dependent FP64 operations sets the time.
 constexpr int kSM = 152;
 
-// unit served by this thread in sweep `r` of the grid-stride loop, or -1
+// unit served by this thread in sweep `r` of the grid-stride loop over the first `nb` blocks, or -1
 template <int NT>
-__device__ __forceinline__ int unit_of(int lanes, int r) {
+__device__ __forceinline__ int unit_of(int lanes, int r, int nb) {
     const int lane = threadIdx.x & 31;
     if (lane >= lanes) return -1;
     const int gw = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
-    return (r * gridDim.x * (NT / 32) + gw) * lanes + lane;
+    return (r * nb * (NT / 32) + gw) * lanes + lane;
 }
 
 constexpr double Gf01 = F32D(0.348611111), Gf11 = 1.0, Gf21 = F32D(0.916666667), Gf31 = F32D(0.333333333),
@@ -66,11 +67,12 @@ struct Dyn {
     int nion;
 };
 
-__device__ __forceinline__ double pred_ion(const View& v, const Dyn& D, int k) {
+__device__ __forceinline__ double pred_ion(const View& v, const Dyn& D, int k, double* xn) {
     const int n = D.nion;
     const int i = v.nriga + k;
     double* X[3] = {v.x, v.y, v.z};
     double s2 = 0.0;
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
         double* x1 = D.xd + (0 * 3 + d) * n;
         double* x2 = D.xd + (1 * 3 + d) * n;
@@ -79,6 +81,7 @@ __device__ __forceinline__ double pred_ion(const View& v, const Dyn& D, int k) {
         double a0 = X[d][i], a1 = x1[k], a2 = x2[k], a3 = x3[k];
         gpred(a0, a1, a2, a3, x4[k]);
         X[d][i] = a0;
+        xn[d] = a0;
         x1[k] = a1;
         x2[k] = a2;
         x3[k] = a3;
@@ -101,7 +104,8 @@ __device__ __forceinline__ bool last_block(unsigned* done) {
 // All of a molecule's state is loaded before anything is stored: the arrays may alias as far as
 // the compiler knows, and loads issued back to back overlap their latency instead of queueing
 // behind the stores (the per-molecule work is short; memory latency, not FP64, bounds it).
-__device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, double* sc, double* sw) {
+__device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, double* sc, double* sw, double* cn,
+                                           double* sx, double* sy, double* sz) {
     const int nr = v.nrig;
     double C[5][3], W[5][3], Q[5][4];
 #pragma unroll
@@ -159,7 +163,8 @@ __device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, d
 #pragma unroll
     for (int k = 0; k < 9; ++k) D.a[k * nr + i] = a[k];
     const int ix = 3 * i;
-    double sx[3], sy[3], sz[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) cn[d] = cx[d];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         sx[j] = cx[0] + a[0] * D.body.xbody[j] + a[3] * D.body.ybody[j] + a[6] * D.body.zbody[j];
@@ -215,23 +220,71 @@ struct Clear {
     int n[2];
 };
 
-template <int NT>
-__global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z) {
+// The records of the force evaluation that follows (pack.cuh), written by the predictor of a
+// resident mixed-precision step from the positions it has just computed: blocks below npred
+// predict and pack their molecules and flexible atoms, the blocks after them pack the wall atoms.
+struct PackArgs {
+    Pk pk;
+    int dip;    // slab dipole term
+    int npred;  // blocks of the predictor proper
+};
+
+template <int NT, bool PACK>
+__global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z, PackArgs P) {
+    __shared__ double red[8];
     double kp = 0.0, sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
+    double mz = 0.0, md = 0.0;
     const int nu = D.nion + v.nrig;
-    if (blockIdx.x == 0)
+    const int npred = PACK ? P.npred : gridDim.x;
+    if (blockIdx.x == 0) {
         for (int j = 0; j < 2; ++j)
             for (int k = threadIdx.x; k < z.n[j]; k += NT) z.p[j][k] = 0.0;
-    for (int r = 0, u; (u = unit_of<NT>(lanes, r)) >= 0 && u < nu; ++r) {
-        if (u < D.nion) kp += pred_ion(v, D, u);
-        else pred_rigid(v, D, u - D.nion, sc, sw);
+        if (PACK && P.pk.cmax && threadIdx.x == 0) *P.pk.cmax = 0.f;
     }
-    block_atomic_sum<NT>(kp, &D.isum[0]);
-    for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
-    for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
-    if (last_block(&D.done[0]) && threadIdx.x == 0) {
-        thermo_pred(v, D);
-        D.done[0] = 0u;
+    if (blockIdx.x < npred) {
+        for (int r = 0, u; (u = unit_of<NT>(lanes, r, npred)) >= 0 && u < nu; ++r) {
+            if (u < D.nion) {
+                double xn[3];
+                kp += pred_ion(v, D, u, xn);
+                if constexpr (PACK) {
+                    const int at = v.nriga + u;
+                    const double a = v.ox[u] - xn[0], b = v.oy[u] - xn[1], c = v.oz[u] - xn[2];
+                    md = fmax(md, a * a + b * b + c * c);
+                    mz += pack_atom(v, P.pk, at, xn[0], xn[1], xn[2], v.rsx[at], v.rsy[at], v.rsz[at], true);
+                }
+            } else {
+                const int i = u - D.nion;
+                double cn[3], px[3], py[3], pz[3];
+                pred_rigid(v, D, i, sc, sw, cn, px, py, pz);
+                if constexpr (PACK) {
+                    const double a = v.ocx[i] - cn[0], b = v.ocy[i] - cn[1], c = v.ocz[i] - cn[2];
+                    md = fmax(md, a * a + b * b + c * c);
+                    // site 0's offset is the stored one (force_sum leaves rsx(1:3) stale), sites 1, 2
+                    // the offsets just computed, as the packing kernel would read them back
+                    const int ix = 3 * i;
+                    mz += pack_atom(v, P.pk, ix, px[0], py[0], pz[0], v.rsx[ix], v.rsy[ix], v.rsz[ix], true);
+#pragma unroll
+                    for (int j = 1; j < 3; ++j)
+                        mz += pack_atom(v, P.pk, ix + j, px[j], py[j], pz[j], px[j] - px[0], py[j] - py[0],
+                                        pz[j] - pz[0], true);
+                }
+            }
+        }
+        block_atomic_sum<NT>(kp, &D.isum[0]);
+        for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
+        for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
+    } else if constexpr (PACK) {
+        const int nw = gridDim.x - npred;
+        for (int a = v.nmove + (blockIdx.x - npred) * NT + threadIdx.x; a < v.ntota; a += nw * NT)
+            pack_atom(v, P.pk, a, v.x[a], v.y[a], v.z[a], 0.0, 0.0, 0.0, false);
+    }
+    if constexpr (PACK) pack_block(v, P.pk, mz, md, red);
+    if (last_block(&D.done[0])) {
+        if constexpr (PACK) pack_close(v, P.pk, P.dip, 0, 0, red);
+        if (threadIdx.x == 0) {
+            thermo_pred(v, D);
+            D.done[0] = 0u;
+        }
     }
 }
 
@@ -392,7 +445,7 @@ __global__ void __launch_bounds__(NT) k_corr(View v, Dyn D, int slab, int lanes,
     MergeArgs M;
     if constexpr (MERGE) M = merge_begin(v, A);
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    for (int r = 0, u; (u = unit_of<NT>(lanes, r)) >= 0 && u < nu; ++r) {
+    for (int r = 0, u; (u = unit_of<NT>(lanes, r, gridDim.x)) >= 0 && u < nu; ++r) {
         if (u < D.nion) {
             if constexpr (MERGE) merge_flex(v, M, u, sx, sy, sz);
             corr_ion(v, D, u);
@@ -443,13 +496,30 @@ int nblk(int n, int nt) {
 
 }  // namespace
 
-void predict_launch(Ctx& c, bool clear_acc, bool clear_kps) {
+void predict_launch(Ctx& c, bool clear_acc, bool clear_kps, bool pack) {
     const View& v = c.v;
     Dyn D = dyn_of(c);
     const int nu = D.nion + v.nrig, lanes = lanes_of(nu);
     Clear z{{v.acc, c.d_kps}, {clear_acc ? 2 * v.nijt + ACC_NSLOT : 0, clear_kps && c.d_kps ? v.nit : 0}};
-    if (lanes < 32) k_pred<32><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, lanes, z);
-    else k_pred<128><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, lanes, z);
+    PackArgs P{};
+    if (pack) {
+        P.pk = c.pk;
+        P.dip = c.variant == MDG_SLAB ? 1 : 0;
+    }
+    const int nwall = v.ntota - v.nmove;
+    if (lanes < 32) {
+        const int nb = nblk(nu, 32);
+        P.npred = nb;
+        const int nwb = pack ? std::min((nwall + 31) / 32, kSM * 8) : 0;
+        if (pack) k_pred<32, true><<<nb + nwb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+        else k_pred<32, false><<<nb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+    } else {
+        const int nb = nblk(nu, 128);
+        P.npred = nb;
+        const int nwb = pack ? std::min((nwall + 127) / 128, kSM * 8) : 0;
+        if (pack) k_pred<128, true><<<nb + nwb, 128, 0, c.stream>>>(v, D, lanes, z, P);
+        else k_pred<128, false><<<nb, 128, 0, c.stream>>>(v, D, lanes, z, P);
+    }
 }
 
 void correct_launch(Ctx& c, bool merge) {

@@ -225,8 +225,10 @@ static bool merge_fusable(const Ctx& c) {
 // energy sums were zeroed by the kernel before (the predictor of a resident step).  In the mixed
 // form the packing kernel clears them (and the overflow words), which keeps memset nodes, slow
 // to start inside a graph, off the critical path.  defer_merge: leave that final merge kernel to
-// the caller (the resident step fuses it into the corrector).
-int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear = false, bool defer_merge = false) {
+// the caller (the resident step fuses it into the corrector).  packed: the records were written by
+// the kernel before (the predictor of a resident step), so the packing kernel is left out.
+int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear = false, bool defer_merge = false,
+                 bool packed = false) {
     View& v = c.v;
     if (c.precision != MDG_MIXED) {
         if (!acc_clear) cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
@@ -242,7 +244,7 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
         // loop; both add into F with vector reductions.  Fork and join go through events, so the
         // same dependencies hold inside a captured graph.  The reciprocal forces (d_frc), F and the
         // slab dipole term join the FP64 forces in one merge at the end.
-        PHASE(pack_mixed(c, force_rebuild, reset_status), "pack");  // also decides the list rebuild
+        if (!packed) PHASE(pack_mixed(c, force_rebuild, reset_status), "pack");  // also decides the list rebuild
         const cudaStream_t s0 = c.stream;
         MDG_CUDA(cudaEventRecord(c.ev_fork, s0));
         MDG_CUDA(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
@@ -969,8 +971,9 @@ static void snapshot(Ctx& c, bool restore) {
 // One MD step (src/main.f90:60-64): predict, forces, correct, SHAKE.
 static int step_launch(Ctx& c) {
     const bool fp64 = c.precision != MDG_MIXED, shake = c.v.nmove > c.v.nliqa, fuse = merge_fusable(c);
-    predict_launch(c, fp64, shake);
-    int rc = launch_force(c, false, false, fp64, fuse);
+    const bool pack = !fp64 && !shake;  // surface atoms move in SHAKE, after the predictor
+    predict_launch(c, fp64, shake, pack);
+    int rc = launch_force(c, false, false, fp64, fuse, pack);
     if (rc) return rc;
     correct_launch(c, fuse);
     if (shake) shake_launch(c, c.d_ft, true);

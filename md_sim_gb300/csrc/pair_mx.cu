@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "pack.cuh"
 
 namespace mdg {
 
@@ -32,6 +33,7 @@ constexpr int kWarps = 8;
 constexpr int kNT = kWarps * 32;
 constexpr int kWSeg = 64;  // wall partners per work item of the head-wall loop
 constexpr int kPackBlocks = 152 * 8;  // most blocks of the packing kernel
+static_assert(kPackBlocks <= kPackParts, "dipole shares");
 constexpr float kPf = (float)kP, kA1f = (float)kA1, kA2f = (float)kA2, kA3f = (float)kA3, kA4f = (float)kA4,
                 kA5f = (float)kA5;
 
@@ -107,19 +109,11 @@ __device__ __forceinline__ void red_v4(float4* p, float a, float b, float c) {
                  : "memory");
 }
 
-// round(t 2^32) mod 2^32 for |t| < 2^19: t + 1.5 2^20 lies in [2^20, 2^21), where the spacing of
-// doubles is 2^-32, so the low 32 bits of its significand are the rounded fraction (two FP64
-// operations per coordinate; the FP64 pipe is narrow on this part).
-__device__ __forceinline__ uint32_t frac32(double t) {
-    return (uint32_t)__double_as_longlong(t + 1572864.0);
-}
-
-// Records of every atom for this evaluation; also clears the FP64 forces, for the slab variant
-// sums the dipole M_z = sum q z of the moving atoms (src/forcem.f90:924) into the accumulator
-// block (which the caller zeroed), and takes the neighbour-list rebuild decision
-// (src/forcem.f90:245-250): the maximum squared displacement of the centres of mass and flexible
-// atoms since the last rebuild, compared by the block that finishes last.
+// Records of every atom for this evaluation (pack.cuh); also clears the FP64 forces, sums the slab
+// dipole, takes the neighbour-list rebuild decision and clears the energy sums (its last block).
 __global__ void k_pack(View v, Pk pk, int dip, int force, int reset_status) {
+    __shared__ double red[8];
+    __shared__ bool last;
     double mz = 0.0, md = 0.0;
     if (pk.cmax && blockIdx.x == 0 && threadIdx.x == 0) *pk.cmax = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.nrig + (v.nmove - v.nriga);
@@ -138,76 +132,17 @@ __global__ void k_pack(View v, Pk pk, int dip, int force, int reset_status) {
         md = fmax(md, a * a + b * b + c * c);
     }
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < v.ntota; a += gridDim.x * blockDim.x) {
-        const double x = v.x[a], y = v.y[a], z = v.z[a];
-        uint4 p;
-        p.x = frac32(x * v.lxi);
-        p.y = frac32(y * v.lyi);
-        const uint32_t uz = frac32(z * v.lzi);
-        if (pk.zper) {
-            p.z = uz;
-        } else {
-            const float zh = (float)z;
-            p.z = __float_as_uint(zh);
-            pk.zlo[a] = (float)(z - (double)zh);
-        }
-        p.w = (uint32_t)v.type[a] | (signbit(z) ? 0x80000000u : 0u);
-        pk.P[a] = p;
-        float4 q = make_float4(0.f, 0.f, 0.f, (float)v.q[a]);
-        if (a < v.nmove) {
-            q.x = (float)v.rsx[a];
-            q.y = (float)v.rsy[a];
-            q.z = (float)v.rsz[a];
-            pk.F[a] = make_float4(0.f, 0.f, 0.f, 0.f);
-            v.fx[a] = 0.0;
-            v.fy[a] = 0.0;
-            v.fz[a] = 0.0;
-            mz += v.q[a] * z;
-            // the reciprocal sum's record: periodic fractions on all three axes and the charge
-            if (pk.tc) pk.tc[a] = make_uint4(p.x, p.y, uz, __float_as_uint(q.w));
-        }
-        pk.Q[a] = q;
+        const bool mv = a < v.nmove;
+        mz += pack_atom(v, pk, a, v.x[a], v.y[a], v.z[a], mv ? v.rsx[a] : 0.0, mv ? v.rsy[a] : 0.0,
+                        mv ? v.rsz[a] : 0.0, mv);
     }
-    __shared__ double red[8];
-    __shared__ bool last;
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    mz = warp_sum(mz);
-    if (l == 0) red[w] = mz;
-    for (int o = 16; o > 0; o >>= 1) md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
-    if (l == 0) atomic_max_nonneg(&v.acc[2 * v.nijt + ACC_MAXD], md);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double b = 0.0;
-        for (int k = 0; k < 8; ++k) b += red[k];
-        pk.part[blockIdx.x] = b;  // this block's share of the slab dipole
-    }
+    pack_block(v, pk, mz, md, red);
     __threadfence();
-    __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(&v.status[ST_PACK_DONE], 1) == (int)gridDim.x - 1;
     __syncthreads();
     if (!last) return;
-    // The last block: the dipole in block order (deterministic), the rebuild decision, and the
-    // energy sums of this evaluation cleared for the loops queued after this kernel.
-    __threadfence();
-    double s = 0.0;
-    for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += __ldcg(&pk.part[b]);
-    s = warp_sum(s);
-    __syncthreads();
-    if (l == 0) red[w] = s;
-    __syncthreads();
-    const int na = 2 * v.nijt + ACC_NSLOT, kmax = 2 * v.nijt + ACC_MAXD, kdip = 2 * v.nijt + ACC_DIPZ;
-    for (int k = threadIdx.x; k < na; k += blockDim.x)
-        if (k != kmax && k != kdip) v.acc[k] = 0.0;
-    if (reset_status && threadIdx.x < 2) v.status[ST_LIST_OVF + threadIdx.x] = 0;
-    if (threadIdx.x == 0) {
-        double dz = 0.0;
-        for (int k = 0; k < 8; ++k) dz += red[k];
-        v.acc[kdip] = dip ? dz : 0.0;
-        const double aux = fmax(__ldcg(&v.acc[kmax]), v.dshsq);
-        v.status[ST_REBUILD] = (force || v.status[ST_FORCE_RB] || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
-        v.status[ST_FORCE_RB] = 0;
-        v.acc[kmax] = 0.0;
-        v.status[ST_PACK_DONE] = 0;
-    }
+    pack_close(v, pk, dip, force, reset_status, red);
+    if (threadIdx.x == 0) v.status[ST_PACK_DONE] = 0;
 }
 
 // Pair-type tables in shared memory: per ijt {kind, sig, eps, aa, rhoi, cc}, ijt[it*nit+jt], nsi[it].
@@ -492,7 +427,7 @@ void pack_setup(Ctx& c) {
     c.pk.Q = (float4*)dalloc(c, sizeof(float4) * n);
     c.pk.zlo = (float*)dalloc(c, sizeof(float) * n);
     c.pk.F = (float4*)dalloc(c, sizeof(float4) * std::max(v.nmove, 1));
-    c.pk.part = (double*)dalloc(c, sizeof(double) * kPackBlocks);
+    c.pk.part = (double*)dalloc(c, sizeof(double) * kPackParts);
     c.pk.zper = v.bulk ? 1 : 0;
     c.pk.sx = (float)(v.lx / 4294967296.0);
     c.pk.sy = (float)(v.ly / 4294967296.0);
