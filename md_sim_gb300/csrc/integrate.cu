@@ -24,10 +24,12 @@ namespace mdg {
 
 namespace {
 
-// A warp serves `lanes` molecules (lanes 0..lanes-1). An FP64 instruction costs the SM's FP64
-// pipe about the same whatever the number of active lanes, so large systems pack 32 molecules per
-// warp (blocks of four warps); small ones spread one warp per SM with just enough lanes to cover
-// the molecules, since there the per-molecule chain of dependent FP64 operations sets the time.
+// A warp serves `lanes` molecules. An FP64 instruction costs the SM's FP64 pipe about the same
+// whatever the number of active lanes, so large systems pack 32 molecules per warp (blocks of four
+// warps); small ones spread one warp per SM with just enough molecules to cover the system, since
+// there the per-molecule chain of dependent FP64 operations sets the time, and with at most 16
+// molecules per warp each molecule takes a pair of lanes (centre and angular velocity on one,
+// orientation on the other) to shorten that chain.
 constexpr int kSM = 152;
 
 // unit served by this thread in sweep `r` of the grid-stride loop over the first `nb` blocks, or -1
@@ -37,6 +39,16 @@ __device__ __forceinline__ int unit_of(int lanes, int r, int nb) {
     if (lane >= lanes) return -1;
     const int gw = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
     return (r * nb * (NT / 32) + gw) * lanes + lane;
+}
+
+// the same for lane pairs (two lanes per unit, `lanes` units per warp, lanes <= 16): role = lane & 1
+template <int NT>
+__device__ __forceinline__ int unit_of_pair(int lanes, int r, int nb, int& role) {
+    const int lane = threadIdx.x & 31, slot = lane >> 1;
+    role = lane & 1;
+    if (slot >= lanes) return -1;
+    const int gw = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
+    return (r * nb * (NT / 32) + gw) * lanes + slot;
 }
 
 constexpr double Gf01 = F32D(0.348611111), Gf11 = 1.0, Gf21 = F32D(0.916666667), Gf31 = F32D(0.333333333),
@@ -101,41 +113,17 @@ __device__ __forceinline__ bool last_block(unsigned* done) {
     return last;
 }
 
-// All of a molecule's state is loaded before anything is stored: the arrays may alias as far as
-// the compiler knows, and loads issued back to back overlap their latency instead of queueing
-// behind the stores (the per-molecule work is short; memory latency, not FP64, bounds it).
-__device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, double* sc, double* sw, double* cn,
-                                           double* sx, double* sy, double* sz) {
-    const int nr = v.nrig;
-    double C[5][3], W[5][3], Q[5][4];
-#pragma unroll
-    for (int k = 0; k < 5; ++k)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            C[k][d] = D.c[(k * 3 + d) * nr + i];
-            W[k][d] = D.w[(k * 3 + d) * nr + i];
-        }
-#pragma unroll
-    for (int k = 0; k < 5; ++k)
-#pragma unroll
-        for (int cc = 0; cc < 4; ++cc) Q[k][cc] = D.q[(cc * 5 + k) * nr + i];
-    double cx[3], qq[4];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        gpred(C[0][d], C[1][d], C[2][d], C[3][d], C[4][d]);
-        sc[d] += C[1][d] * C[1][d];
-        cx[d] = C[0][d];
-        gpred(W[0][d], W[1][d], W[2][d], W[3][d], W[4][d]);
-        sw[d] += W[0][d] * W[0][d];
-    }
-#pragma unroll
-    for (int cc = 0; cc < 4; ++cc) {
-        gpred(Q[0][cc], Q[1][cc], Q[2][cc], Q[3][cc], Q[4][cc]);
-        qq[cc] = Q[0][cc];
-    }
+// Register arithmetic of the rigid-body predictor and corrector, shared by the one-lane forms and
+// the lane-pair forms below (the same operations in the same order, so both give the same bits).
+
+// rotation matrix of the normalised predicted quaternion (src/move.f90:128-146)
+__device__ __forceinline__ void quat_rot(const double* qq, double* qn, double* a) {
     const double cr = 1.0 / sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
     const double q1 = qq[0] * cr, q2 = qq[1] * cr, q3 = qq[2] * cr, q4 = qq[3] * cr;
-    double a[9];
+    qn[0] = q1;
+    qn[1] = q2;
+    qn[2] = q3;
+    qn[3] = q4;
     a[0] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
     a[1] = 2.0 * (q3 * q4 - q1 * q2);
     a[2] = 2.0 * (q2 * q3 + q1 * q4);
@@ -145,6 +133,44 @@ __device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, d
     a[6] = 2.0 * (q2 * q3 - q1 * q4);
     a[7] = -2.0 * (q1 * q3 + q4 * q2);
     a[8] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
+}
+
+// lab-frame position of site j (src/move.f90:148-162)
+__device__ __forceinline__ void site_pos(const double* cx, const double* a, const mdg_rigid& b, int j, double& x,
+                                         double& y, double& z) {
+    x = cx[0] + a[0] * b.xbody[j] + a[3] * b.ybody[j] + a[6] * b.zbody[j];
+    y = cx[1] + a[1] * b.xbody[j] + a[4] * b.ybody[j] + a[7] * b.zbody[j];
+    z = cx[2] + a[2] * b.xbody[j] + a[5] * b.ybody[j] + a[8] * b.zbody[j];
+}
+
+__device__ __forceinline__ void load_cw(const Dyn& D, int nr, int i, double (&C)[5][3], double (&W)[5][3]) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            C[k][d] = D.c[(k * 3 + d) * nr + i];
+            W[k][d] = D.w[(k * 3 + d) * nr + i];
+        }
+}
+
+__device__ __forceinline__ void load_q(const Dyn& D, int nr, int i, double (&Q)[5][4]) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) Q[k][cc] = D.q[(cc * 5 + k) * nr + i];
+}
+
+// predictor of the centre and angular velocity; stores their first four derivatives
+__device__ __forceinline__ void pred_cw(const Dyn& D, int nr, int i, double (&C)[5][3], double (&W)[5][3], double* sc,
+                                        double* sw, double* cx) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        gpred(C[0][d], C[1][d], C[2][d], C[3][d], C[4][d]);
+        sc[d] += C[1][d] * C[1][d];
+        cx[d] = C[0][d];
+        gpred(W[0][d], W[1][d], W[2][d], W[3][d], W[4][d]);
+        sw[d] += W[0][d] * W[0][d];
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
 #pragma unroll
@@ -152,24 +178,42 @@ __device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, d
 #pragma unroll
         for (int k = 0; k < 4; ++k) D.w[(k * 3 + d) * nr + i] = W[k][d];
     }
+}
+
+// predictor of the orientation; stores the quaternion derivatives and the rotation matrix
+__device__ __forceinline__ void pred_q(const Dyn& D, int nr, int i, double (&Q)[5][4], double* a) {
+    double qq[4], qn[4];
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+        gpred(Q[0][cc], Q[1][cc], Q[2][cc], Q[3][cc], Q[4][cc]);
+        qq[cc] = Q[0][cc];
+    }
+    quat_rot(qq, qn, a);
 #pragma unroll
     for (int cc = 0; cc < 4; ++cc)
 #pragma unroll
         for (int k = 1; k < 4; ++k) D.q[(cc * 5 + k) * nr + i] = Q[k][cc];
-    D.q[(0 * 5) * nr + i] = q1;
-    D.q[(1 * 5) * nr + i] = q2;
-    D.q[(2 * 5) * nr + i] = q3;
-    D.q[(3 * 5) * nr + i] = q4;
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) D.q[(cc * 5) * nr + i] = qn[cc];
 #pragma unroll
     for (int k = 0; k < 9; ++k) D.a[k * nr + i] = a[k];
+}
+
+// All of a molecule's state is loaded before anything is stored: the arrays may alias as far as
+// the compiler knows, and loads issued back to back overlap their latency instead of queueing
+// behind the stores (the per-molecule work is short; memory latency, not FP64, bounds it).
+__device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, double* sc, double* sw, double* cn,
+                                           double* sx, double* sy, double* sz) {
+    const int nr = v.nrig;
+    double C[5][3], W[5][3], Q[5][4], a[9];
+    load_cw(D, nr, i, C, W);
+    load_q(D, nr, i, Q);
+    pred_cw(D, nr, i, C, W, sc, sw, cn);
+    pred_q(D, nr, i, Q, a);
     const int ix = 3 * i;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) cn[d] = cx[d];
-#pragma unroll
     for (int j = 0; j < 3; ++j) {
-        sx[j] = cx[0] + a[0] * D.body.xbody[j] + a[3] * D.body.ybody[j] + a[6] * D.body.zbody[j];
-        sy[j] = cx[1] + a[1] * D.body.xbody[j] + a[4] * D.body.ybody[j] + a[7] * D.body.zbody[j];
-        sz[j] = cx[2] + a[2] * D.body.xbody[j] + a[5] * D.body.ybody[j] + a[8] * D.body.zbody[j];
+        site_pos(cn, a, D.body, j, sx[j], sy[j], sz[j]);
         v.x[ix + j] = sx[j];
         v.y[ix + j] = sy[j];
         v.z[ix + j] = sz[j];
@@ -180,6 +224,52 @@ __device__ __forceinline__ void pred_rigid(const View& v, const Dyn& D, int i, d
         v.rsy[ix + j] = sy[j] - sy[0];
         v.rsz[ix + j] = sz[j] - sz[0];
     }
+}
+
+// The same on a pair of lanes (mask: the lanes of the pairs on rigid molecules this sweep): role 0
+// predicts the centre and angular velocity, role 1 the orientation; after the exchange of the
+// centre and the rotation matrix, role 0 places sites 0 and 1, role 1 sites 0 and 2 (returned in
+// slots 0 and 1; each writes its own besides site 0, which role 0 writes).
+__device__ __forceinline__ void pred_rigid_pair(const View& v, const Dyn& D, int i, int role, unsigned mask,
+                                                double* sc, double* sw, double* cn, double* sx, double* sy,
+                                                double* sz) {
+    const int nr = v.nrig;
+    double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    cn[0] = cn[1] = cn[2] = 0.0;
+    if (role == 0) {
+        double C[5][3], W[5][3];
+        load_cw(D, nr, i, C, W);
+        pred_cw(D, nr, i, C, W, sc, sw, cn);
+    } else {
+        double Q[5][4];
+        load_q(D, nr, i, Q);
+        pred_q(D, nr, i, Q, a);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double t = __shfl_xor_sync(mask, role ? a[k] : cn[k], 1);
+        if (role) cn[k] = t;
+        else a[k] = t;
+    }
+#pragma unroll
+    for (int k = 3; k < 9; ++k) {
+        const double t = __shfl_xor_sync(mask, a[k], 1);
+        if (!role) a[k] = t;
+    }
+    const int ix = 3 * i, j1 = role ? 2 : 1;
+    site_pos(cn, a, D.body, 0, sx[0], sy[0], sz[0]);
+    site_pos(cn, a, D.body, j1, sx[1], sy[1], sz[1]);
+    if (role == 0) {
+        v.x[ix] = sx[0];
+        v.y[ix] = sy[0];
+        v.z[ix] = sz[0];
+    }
+    v.x[ix + j1] = sx[1];
+    v.y[ix + j1] = sy[1];
+    v.z[ix + j1] = sz[1];
+    v.rsx[ix + j1] = sx[1] - sx[0];
+    v.rsy[ix + j1] = sy[1] - sy[0];
+    v.rsz[ix + j1] = sz[1] - sz[0];
 }
 
 // thermostat predictor and kinetic energies from the summed isum[0..6] (one thread)
@@ -229,7 +319,7 @@ struct PackArgs {
     int npred;  // blocks of the predictor proper
 };
 
-template <int NT, bool PACK>
+template <int NT, bool PACK, bool PAIR>
 __global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z, PackArgs P) {
     __shared__ double red[8];
     double kp = 0.0, sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
@@ -242,8 +332,21 @@ __global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z, 
         if (PACK && P.pk.cmax && threadIdx.x == 0) *P.pk.cmax = 0.f;
     }
     if (blockIdx.x < npred) {
-        for (int r = 0, u; (u = unit_of<NT>(lanes, r, npred)) >= 0 && u < nu; ++r) {
+        for (int r = 0;; ++r) {
+            int u, role = 0;
+            if constexpr (PAIR) u = unit_of_pair<NT>(lanes, r, npred, role);
+            else u = unit_of<NT>(lanes, r, npred);
+            const bool act = u >= 0 && u < nu;
+            unsigned mask = 0u;
+            if constexpr (PAIR) {
+                if (!__any_sync(0xffffffffu, act)) break;
+                mask = __ballot_sync(0xffffffffu, act && u >= D.nion);
+                if (!act) continue;
+            } else {
+                if (!act) break;
+            }
             if (u < D.nion) {
+                if (role != 0) continue;
                 double xn[3];
                 kp += pred_ion(v, D, u, xn);
                 if constexpr (PACK) {
@@ -252,16 +355,31 @@ __global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z, 
                     md = fmax(md, a * a + b * b + c * c);
                     mz += pack_atom(v, P.pk, at, xn[0], xn[1], xn[2], v.rsx[at], v.rsy[at], v.rsz[at], true);
                 }
+                continue;
+            }
+            const int i = u - D.nion, ix = 3 * i;
+            double cn[3], px[3], py[3], pz[3];
+            if constexpr (PAIR) {
+                pred_rigid_pair(v, D, i, role, mask, sc, sw, cn, px, py, pz);
+                if constexpr (PACK) {
+                    // site 0's offset is the stored one (force_sum leaves rsx(1:3) stale), the others
+                    // the offsets just computed, as the packing kernel would read them back
+                    if (role == 0) {
+                        const double a = v.ocx[i] - cn[0], b = v.ocy[i] - cn[1], c = v.ocz[i] - cn[2];
+                        md = fmax(md, a * a + b * b + c * c);
+                        mz += pack_atom(v, P.pk, ix, px[0], py[0], pz[0], v.rsx[ix], v.rsy[ix], v.rsz[ix], true);
+                        mz += pack_atom(v, P.pk, ix + 1, px[1], py[1], pz[1], px[1] - px[0], py[1] - py[0],
+                                        pz[1] - pz[0], true);
+                    } else {
+                        mz += pack_atom(v, P.pk, ix + 2, px[1], py[1], pz[1], px[1] - px[0], py[1] - py[0],
+                                        pz[1] - pz[0], true);
+                    }
+                }
             } else {
-                const int i = u - D.nion;
-                double cn[3], px[3], py[3], pz[3];
                 pred_rigid(v, D, i, sc, sw, cn, px, py, pz);
                 if constexpr (PACK) {
                     const double a = v.ocx[i] - cn[0], b = v.ocy[i] - cn[1], c = v.ocz[i] - cn[2];
                     md = fmax(md, a * a + b * b + c * c);
-                    // site 0's offset is the stored one (force_sum leaves rsx(1:3) stale), sites 1, 2
-                    // the offsets just computed, as the packing kernel would read them back
-                    const int ix = 3 * i;
                     mz += pack_atom(v, P.pk, ix, px[0], py[0], pz[0], v.rsx[ix], v.rsy[ix], v.rsz[ix], true);
 #pragma unroll
                     for (int j = 1; j < 3; ++j)
@@ -329,43 +447,10 @@ __device__ __forceinline__ void corr_ion(const View& v, const Dyn& D, int k) {
     }
 }
 
-__device__ __forceinline__ void corr_rigid(const View& v, const Dyn& D, int i) {
-    const int nr = v.nrig;
-    const double s0i = D.th[TH_S], rs0i = D.th[TH_RS];
-    const mdg_rigid& b = D.body;
-    const double rcorr = 0.5 / b.mw;
-    const double inxxi = 1.0 / b.inxx, inyyi = 1.0 / b.inyy, inzzi = 1.0 / b.inzz;
-    // loads first (see pred_rigid)
-    double C[5][3], W[5][3], Q[5][4], a[9], fc[3], tq[3];
-#pragma unroll
-    for (int k = 0; k < 5; ++k)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            C[k][d] = D.c[(k * 3 + d) * nr + i];
-            W[k][d] = D.w[(k * 3 + d) * nr + i];
-        }
-#pragma unroll
-    for (int k = 0; k < 5; ++k)
-#pragma unroll
-        for (int cc = 0; cc < 4; ++cc) Q[k][cc] = D.q[(cc * 5 + k) * nr + i];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) a[k] = D.a[k * nr + i];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        fc[d] = D.fc[d * nr + i];
-        tq[d] = D.tq[d * nr + i];
-    }
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const double co = rcorr * fc[d] - C[1][d] * s0i - C[2][d];
-        C[0][d] = C[0][d] + Gf02 * co;
-        C[1][d] = C[1][d] + Gf12 * co;
-        C[2][d] = C[2][d] + Gf22 * co;
-        C[3][d] = C[3][d] + Gf32 * co;
-        C[4][d] = C[4][d] + Gf42 * co;
-    }
+// corrector of the orientation (Q and the predicted angular velocity w0); stores its derivatives
+__device__ __forceinline__ void corr_q(const Dyn& D, int nr, int i, double (&Q)[5][4], const double* w0) {
     const double q1 = Q[0][0], q2 = Q[0][1], q3 = Q[0][2], q4 = Q[0][3];
-    const double wx = W[0][0], wy = W[0][1], wz = W[0][2];
+    const double wx = w0[0], wy = w0[1], wz = w0[2];
     double cq[4];
     cq[0] = 0.5 * (-q3 * wx - q4 * wy + q2 * wz);
     cq[1] = 0.5 * (q4 * wx - q3 * wy - q1 * wz);
@@ -380,6 +465,30 @@ __device__ __forceinline__ void corr_rigid(const View& v, const Dyn& D, int i) {
         Q[3][cc] = Q[3][cc] + Gf31 * co;
         Q[4][cc] = Q[4][cc] + Gf41 * co;
     }
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) D.q[(cc * 5 + k) * nr + i] = Q[k][cc];
+}
+
+// corrector of the centre (force fc) and the angular velocity (torque tq through the rotation
+// matrix a); stores their derivatives
+__device__ __forceinline__ void corr_cw(const Dyn& D, int nr, int i, double (&C)[5][3], double (&W)[5][3],
+                                        const double* a, const double* fc, const double* tq, double s0i,
+                                        double rs0i) {
+    const mdg_rigid& b = D.body;
+    const double rcorr = 0.5 / b.mw;
+    const double inxxi = 1.0 / b.inxx, inyyi = 1.0 / b.inyy, inzzi = 1.0 / b.inzz;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double co = rcorr * fc[d] - C[1][d] * s0i - C[2][d];
+        C[0][d] = C[0][d] + Gf02 * co;
+        C[1][d] = C[1][d] + Gf12 * co;
+        C[2][d] = C[2][d] + Gf22 * co;
+        C[3][d] = C[3][d] + Gf32 * co;
+        C[4][d] = C[4][d] + Gf42 * co;
+    }
+    const double wx = W[0][0], wy = W[0][1], wz = W[0][2];
     const double tx = tq[0], ty = tq[1], tz = tq[2];
     double c1 = a[0] * tx + a[1] * ty + a[2] * tz;
     c1 = ((c1 * 1.0 + wy * wz * (b.inyy - b.inzz)) * inxxi) - W[1][0] - rs0i * wx;
@@ -403,10 +512,52 @@ __device__ __forceinline__ void corr_rigid(const View& v, const Dyn& D, int i) {
             D.c[(k * 3 + d) * nr + i] = C[k][d];
             D.w[(k * 3 + d) * nr + i] = W[k][d];
         }
+}
+
+__device__ __forceinline__ void corr_rigid(const View& v, const Dyn& D, int i) {
+    const int nr = v.nrig;
+    const double s0i = D.th[TH_S], rs0i = D.th[TH_RS];
+    // loads first (see pred_rigid)
+    double C[5][3], W[5][3], Q[5][4], a[9], fc[3], tq[3];
+    load_cw(D, nr, i, C, W);
+    load_q(D, nr, i, Q);
 #pragma unroll
-    for (int k = 0; k < 5; ++k)
+    for (int k = 0; k < 9; ++k) a[k] = D.a[k * nr + i];
 #pragma unroll
-        for (int cc = 0; cc < 4; ++cc) D.q[(cc * 5 + k) * nr + i] = Q[k][cc];
+    for (int d = 0; d < 3; ++d) {
+        fc[d] = D.fc[d * nr + i];
+        tq[d] = D.tq[d * nr + i];
+    }
+    const double w0[3] = {W[0][0], W[0][1], W[0][2]};
+    corr_q(D, nr, i, Q, w0);
+    corr_cw(D, nr, i, C, W, a, fc, tq, s0i, rs0i);
+}
+
+// The same on a pair of lanes: role 0 corrects the centre and angular velocity (with fc, tq),
+// role 1 the orientation, with the predicted angular velocity passed over from role 0.
+__device__ __forceinline__ void corr_rigid_pair(const View& v, const Dyn& D, int i, int role, unsigned mask,
+                                                const double* fc, const double* tq) {
+    const int nr = v.nrig;
+    const double s0i = D.th[TH_S], rs0i = D.th[TH_RS];
+    double C[5][3], W[5][3], Q[5][4], a[9];
+    double w0[3] = {0.0, 0.0, 0.0};
+    if (role == 0) {
+        load_cw(D, nr, i, C, W);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = D.a[k * nr + i];
+        w0[0] = W[0][0];
+        w0[1] = W[0][1];
+        w0[2] = W[0][2];
+    } else {
+        load_q(D, nr, i, Q);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double t = __shfl_xor_sync(mask, w0[d], 1);
+        if (role) w0[d] = t;
+    }
+    if (role == 0) corr_cw(D, nr, i, C, W, a, fc, tq, s0i, rs0i);
+    else corr_q(D, nr, i, Q, w0);
 }
 
 __device__ void thermo_corr(const View& v, const Dyn& D) {
@@ -438,22 +589,52 @@ __device__ void thermo_corr(const View& v, const Dyn& D) {
 // force_sum (merge.cuh) run here, each unit's just before its corrector, instead of in a kernel
 // of their own; units past the molecules and ions are the surface atoms, whose forces SHAKE's
 // Verlet step reads next.
-template <int NT, bool MERGE>
+template <int NT, bool MERGE, bool PAIR>
 __global__ void __launch_bounds__(NT) k_corr(View v, Dyn D, int slab, int lanes, MergeArgs A) {
     const int nsurf = MERGE ? v.nmove - v.nliqa : 0;
     const int nu = D.nion + v.nrig + nsurf;
     MergeArgs M;
     if constexpr (MERGE) M = merge_begin(v, A);
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    for (int r = 0, u; (u = unit_of<NT>(lanes, r, gridDim.x)) >= 0 && u < nu; ++r) {
-        if (u < D.nion) {
-            if constexpr (MERGE) merge_flex(v, M, u, sx, sy, sz);
-            corr_ion(v, D, u);
-        } else if (u < D.nion + v.nrig) {
-            if constexpr (MERGE) merge_rigid(v, M, u - D.nion, sx, sy, sz);
-            corr_rigid(v, D, u - D.nion);
-        } else if constexpr (MERGE) {
-            merge_flex(v, M, u - v.nrig, sx, sy, sz);  // surface atom: flexible index nion + s
+    for (int r = 0;; ++r) {
+        int u, role = 0;
+        if constexpr (PAIR) u = unit_of_pair<NT>(lanes, r, gridDim.x, role);
+        else u = unit_of<NT>(lanes, r, gridDim.x);
+        const bool act = u >= 0 && u < nu;
+        const bool rigid = act && u >= D.nion && u < D.nion + v.nrig;
+        unsigned mask = 0u;
+        if constexpr (PAIR) {
+            if (!__any_sync(0xffffffffu, act)) break;
+            mask = __ballot_sync(0xffffffffu, rigid);
+            if (!act) continue;
+        } else {
+            if (!act) break;
+        }
+        if (rigid) {
+            const int i = u - D.nion;
+            if constexpr (PAIR) {
+                double fc[3] = {0, 0, 0}, tq[3] = {0, 0, 0};
+                if constexpr (MERGE) {
+                    merge_rigid_pair(v, M, i, role, mask, sx, sy, sz, fc, tq);
+                } else if (role == 0) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        fc[d] = D.fc[d * v.nrig + i];
+                        tq[d] = D.tq[d * v.nrig + i];
+                    }
+                }
+                corr_rigid_pair(v, D, i, role, mask, fc, tq);
+            } else {
+                if constexpr (MERGE) merge_rigid(v, M, i, sx, sy, sz);
+                corr_rigid(v, D, i);
+            }
+        } else if (role == 0) {
+            if (u < D.nion) {
+                if constexpr (MERGE) merge_flex(v, M, u, sx, sy, sz);
+                corr_ion(v, D, u);
+            } else if constexpr (MERGE) {
+                merge_flex(v, M, u - v.nrig, sx, sy, sz);  // surface atom: flexible index nion + s
+            }
         }
     }
     if constexpr (MERGE) {
@@ -511,14 +692,19 @@ void predict_launch(Ctx& c, bool clear_acc, bool clear_kps, bool pack) {
         const int nb = nblk(nu, 32);
         P.npred = nb;
         const int nwb = pack ? std::min((nwall + 31) / 32, kSM * 8) : 0;
-        if (pack) k_pred<32, true><<<nb + nwb, 32, 0, c.stream>>>(v, D, lanes, z, P);
-        else k_pred<32, false><<<nb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+        if (lanes <= 16) {  // two lanes per molecule
+            if (pack) k_pred<32, true, true><<<nb + nwb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+            else k_pred<32, false, true><<<nb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+        } else {
+            if (pack) k_pred<32, true, false><<<nb + nwb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+            else k_pred<32, false, false><<<nb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+        }
     } else {
         const int nb = nblk(nu, 128);
         P.npred = nb;
         const int nwb = pack ? std::min((nwall + 127) / 128, kSM * 8) : 0;
-        if (pack) k_pred<128, true><<<nb + nwb, 128, 0, c.stream>>>(v, D, lanes, z, P);
-        else k_pred<128, false><<<nb, 128, 0, c.stream>>>(v, D, lanes, z, P);
+        if (pack) k_pred<128, true, false><<<nb + nwb, 128, 0, c.stream>>>(v, D, lanes, z, P);
+        else k_pred<128, false, false><<<nb, 128, 0, c.stream>>>(v, D, lanes, z, P);
     }
 }
 
@@ -528,12 +714,15 @@ void correct_launch(Ctx& c, bool merge) {
     const int nu = D.nion + v.nrig + (merge ? v.nmove - v.nliqa : 0), lanes = lanes_of(nu);
     const int slab = c.variant == MDG_SLAB ? 1 : 0;
     const MergeArgs A = merge ? merge_args(c, c.d_frc) : MergeArgs{};
-    if (merge) {
-        if (lanes < 32) k_corr<32, true><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
-        else k_corr<128, true><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes, A);
+    if (lanes <= 16) {
+        if (merge) k_corr<32, true, true><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
+        else k_corr<32, false, true><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
+    } else if (lanes < 32) {
+        if (merge) k_corr<32, true, false><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
+        else k_corr<32, false, false><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
     } else {
-        if (lanes < 32) k_corr<32, false><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
-        else k_corr<128, false><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes, A);
+        if (merge) k_corr<128, true, false><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes, A);
+        else k_corr<128, false, false><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes, A);
     }
 }
 

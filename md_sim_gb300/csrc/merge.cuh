@@ -81,6 +81,78 @@ __device__ __forceinline__ void merge_rigid(const View& v, const MergeArgs& M, i
     }
 }
 
+// The same on a pair of lanes (mask: the lanes of the pairs on rigid molecules): role 0 merges
+// sites 0 and 1, role 1 site 2; role 0 receives site 2's force and torque term and forms fc and tq
+// (returned, and stored) in the order of merge_rigid.
+__device__ __forceinline__ void merge_rigid_pair(const View& v, const MergeArgs& M, int m, int role, unsigned mask,
+                                                 double& sx, double& sy, double& sz, double* fc, double* tq) {
+    const int j = 3 * m;
+    const double cx = v.cx[m], cy = v.cy[m], cz = v.cz[m];
+    double px, py, pz, tx, ty, tz;
+    double r0x, r0y, r0z, r1x = 0.0, r1y = 0.0, r1z = 0.0;
+    if (role == 0) {
+        double f0x, f0y, f0z, f1x, f1y, f1z;
+        merged_force(v, M, j, f0x, f0y, f0z);
+        merged_force(v, M, j + 1, f1x, f1y, f1z);
+        r0x = v.x[j] - cx;
+        r1x = v.x[j + 1] - cx;
+        r0y = v.y[j] - cy;
+        r1y = v.y[j + 1] - cy;
+        r0z = v.z[j] - cz;
+        r1z = v.z[j + 1] - cz;
+        px = f0x + f1x;
+        py = f0y + f1y;
+        pz = f0z + f1z;
+        tx = (r0y * f0z - r0z * f0y) + (r1y * f1z - r1z * f1y);
+        ty = (r0z * f0x - r0x * f0z) + (r1z * f1x - r1x * f1z);
+        tz = (r0x * f0y - r0y * f0x) + (r1x * f1y - r1y * f1x);
+    } else {
+        double f2x, f2y, f2z;
+        merged_force(v, M, j + 2, f2x, f2y, f2z);
+        r0x = v.x[j + 2] - cx;  // site 2's offset in slot 0
+        r0y = v.y[j + 2] - cy;
+        r0z = v.z[j + 2] - cz;
+        px = f2x;
+        py = f2y;
+        pz = f2z;
+        tx = (r0y * f2z - r0z * f2y);
+        ty = (r0z * f2x - r0x * f2z);
+        tz = (r0x * f2y - r0y * f2x);
+    }
+    const double qx = __shfl_xor_sync(mask, px, 1), qy = __shfl_xor_sync(mask, py, 1),
+                 qz = __shfl_xor_sync(mask, pz, 1);
+    const double ux = __shfl_xor_sync(mask, tx, 1), uy = __shfl_xor_sync(mask, ty, 1),
+                 uz = __shfl_xor_sync(mask, tz, 1);
+    if (role == 0) {
+        fc[0] = px + qx;
+        fc[1] = py + qy;
+        fc[2] = pz + qz;
+        tq[0] = tx + ux;
+        tq[1] = ty + uy;
+        tq[2] = tz + uz;
+        sx += fc[0];
+        sy += fc[1];
+        sz += fc[2];
+        M.fc[m] = fc[0];
+        M.fc[v.nrig + m] = fc[1];
+        M.fc[2 * v.nrig + m] = fc[2];
+        M.tq[m] = tq[0];
+        M.tq[v.nrig + m] = tq[1];
+        M.tq[2 * v.nrig + m] = tq[2];
+    }
+    if (m == v.nrig - 1) {
+        if (role == 0) {
+            v.rsx[0] = r0x; v.rsx[1] = r1x;
+            v.rsy[0] = r0y; v.rsy[1] = r1y;
+            v.rsz[0] = r0z; v.rsz[1] = r1z;
+        } else {
+            v.rsx[2] = r0x;
+            v.rsy[2] = r0y;
+            v.rsz[2] = r0z;
+        }
+    }
+}
+
 // flexible atom k (atom nriga + k): ft; adds its force to s
 __device__ __forceinline__ void merge_flex(const View& v, const MergeArgs& M, int k, double& sx, double& sy,
                                            double& sz) {
