@@ -314,6 +314,8 @@ struct IoBatch {
 // host side is pinned, else as a cudaMemcpyAsync on the context's stream.
 cudaError_t io_add(Ctx& c, IoBatch& b, void* dst, const void* src, long nwords, bool h2d);
 void io_flush(Ctx& c, IoBatch& b);  // launches the batch's copy kernel and empties it
+cudaError_t pin_host_range(void* p, size_t bytes);  // cudaHostRegister + the registry of io_add
+cudaError_t unpin_host_range(void* p);
 
 // clear_acc / clear_kps: also zero the energy sums of the force call next / the surface atoms'
 // kinetic sums of the SHAKE call after it

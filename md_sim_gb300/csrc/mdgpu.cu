@@ -897,7 +897,7 @@ int mdg_shake(mdg_ctx* cp, double* x0, double* y0, double* z0, double* xold, dou
 
 int mdg_pin_host(void* p, int64_t bytes) {
     if (!p || bytes <= 0) return set_err(nullptr, MDG_E_ARG, "mdg_pin_host: null pointer or empty range");
-    const cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
+    const cudaError_t e = pin_host_range(p, (size_t)bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return set_err(nullptr, MDG_E_CUDA, std::string("mdg_pin_host: ") + cudaGetErrorString(e));
@@ -907,7 +907,7 @@ int mdg_pin_host(void* p, int64_t bytes) {
 
 int mdg_unpin_host(void* p) {
     if (!p) return set_err(nullptr, MDG_E_ARG, "mdg_unpin_host: null pointer");
-    const cudaError_t e = cudaHostUnregister(p);
+    const cudaError_t e = unpin_host_range(p);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return set_err(nullptr, MDG_E_CUDA, std::string("mdg_unpin_host: ") + cudaGetErrorString(e));
