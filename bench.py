@@ -292,6 +292,7 @@ def gpu_arm(args):
     # ---------------- learned SHAKE seed (workloads with SHAKE-constrained molecules): the same
     # start and step count with the seed network active; the headline value is then this run
     learned_rep = None
+    shake_model = None
     if s.ncons > 0 and args.learned and precision == MDG_MIXED:
         from md_sim_gb300 import learned
 
@@ -320,6 +321,7 @@ def gpu_arm(args):
             "tolerance": prm.shake_tol2,
         }
         value, t_step, per_step = learned_rep["value_seeded"], t_seed, per_seed
+        shake_model = w
     drift = None
     if args.drift > 0:
         drift = nve_drift(ctx, s, args.drift)
@@ -333,7 +335,7 @@ def gpu_arm(args):
         cmp64["speedup"] = value / cmp64["value"]
 
     # ---------------- e2e through the drop-in ABI with pinned host buffers
-    e2e = e2e_arm(lib, s_start, prm, args, torch)
+    e2e = e2e_arm(lib, s_start, prm, args, torch, shake_model)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup,
@@ -590,7 +592,7 @@ def fp64_compare(lib, s_start, prm, args, stream, flush, torch):
             "error_vs_fp64": err}
 
 
-def e2e_arm(lib, s, prm, args, torch):
+def e2e_arm(lib, s, prm, args, torch, shake_model=None):
     from md_sim_gb300 import abi
 
     K = min(args.steps, args.e2e_steps)
@@ -632,6 +634,8 @@ def e2e_arm(lib, s, prm, args, torch):
     if s.nrig:
         s0.c[0] = np.stack([traj[0]["cx"], traj[0]["cy"], traj[0]["cz"]])
     dctx = abi.Context(lib, s0, prm)
+    if shake_model is not None:
+        dctx.set_shake_model(shake_model)  # the seed of the resident arm (mdg_shake_set_model)
     if args.autotune:
         dctx.autotune(3)
     nflex = nm - s.nriga
