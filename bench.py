@@ -609,11 +609,11 @@ def e2e_arm(lib, s, prm, args, torch, shake_model=None):
 
     def pinned(n):
         mm = mmap.mmap(-1, -(-max(8 * n, 8) // 65536) * 65536)
-        a = np.frombuffer(mm, dtype=np.float64, count=n)
+        a = np.frombuffer(mm, dtype=np.float64, count=max(n, 1))
         if lib.pin_host(a.ctypes.data, a.nbytes) != 0:
             raise RuntimeError("mdg_pin_host failed: " + (lib.last_error(None) or b"").decode())
         held.append(a)
-        return a
+        return a[:n]
 
     traj = []
     for k in range(K):

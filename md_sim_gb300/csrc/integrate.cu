@@ -272,16 +272,35 @@ __device__ __forceinline__ void pred_rigid_pair(const View& v, const Dyn& D, int
     v.rsz[ix + j1] = sz[1] - sz[0];
 }
 
-// thermostat predictor and kinetic energies from the summed isum[0..6] (one thread)
-__device__ void thermo_pred(const View& v, const Dyn& D) {
+// thermostat predictor and kinetic energies from the summed isum[0..6] (one thread).  Runs in the
+// tail of a kernel, where every dependent round trip to L2 is about a microsecond: all loads are
+// issued first, into registers, then the arithmetic, then the stores.
+struct ThermoIn {
+    double is[7], s[5], rs[5], uc;
+};
+
+__device__ __forceinline__ ThermoIn thermo_pred_load(const Dyn& D) {
+    ThermoIn t;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) t.is[k] = __ldcg(&D.isum[k]);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        t.s[k] = __ldcg(&D.th[TH_S + k]);
+        t.rs[k] = __ldcg(&D.th[TH_RS + k]);
+    }
+    t.uc = __ldcg(&D.th[TH_UCONF]);
+    return t;
+}
+
+__device__ void thermo_pred(const View& v, const Dyn& D, ThermoIn t) {
     double* th = D.th;
     const mdg_rigid& b = D.body;
-    double is[7];
-    for (int k = 0; k < 7; ++k) is[k] = __ldcg(&D.isum[k]);
+    double* is = t.is;
+    double* s = t.s;
+    double* rs = t.rs;
+    const double uc = t.uc;
     const double kp = is[0] + b.mw * (is[1] + is[2] + is[3]);
     const double kw = b.inxx * is[4] + b.inyy * is[5] + b.inzz * is[6];
-    double* s = th + TH_S;
-    double* rs = th + TH_RS;
     if (b.temper == -1.0) {
         s[0] = s[1] = rs[0] = rs[1] = 0.0;
     } else {
@@ -294,12 +313,18 @@ __device__ void thermo_pred(const View& v, const Dyn& D) {
     double rmass = (double)(float)(3 * v.nrig) * tstar * F32D(1e3);
     qmass = qmass / 10.0;
     rmass = rmass / 10.0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        th[TH_S + k] = s[k];
+        th[TH_RS + k] = rs[k];
+    }
     th[TH_KP] = kp;
     th[TH_KW] = kw;
     th[TH_KE] = kp + kw;
-    th[TH_HTOT] = 0.5 * (kp + kw + qmass * s[0] * s[0] + rmass * rs[0] * rs[0]) + th[TH_UCONF];
+    th[TH_HTOT] = 0.5 * (kp + kw + qmass * s[0] * s[0] + rmass * rs[0] * rs[0]) + uc;
     th[TH_SFT] = (kp - (double)(float)(3 * (nfree + v.nrig) - 2) * tstar) / qmass;
     th[TH_SFR] = (kw - (double)(float)(3 * v.nrig + 1) * tstar) / rmass;
+#pragma unroll
     for (int k = 0; k < 7; ++k) D.isum[k] = 0.0;  // ready for the next step
 }
 
@@ -398,31 +423,14 @@ __global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z, 
     }
     if constexpr (PACK) pack_block(v, P.pk, mz, md, red);
     if (last_block(&D.done[0])) {
+        ThermoIn tin;
+        if (threadIdx.x == 0) tin = thermo_pred_load(D);  // issued before the packing's stores
         if constexpr (PACK) pack_close(v, P.pk, P.dip, 0, 0, red);
         if (threadIdx.x == 0) {
-            thermo_pred(v, D);
+            thermo_pred(v, D, tin);
             D.done[0] = 0u;
         }
     }
-}
-
-// uconf = sum(elj) + sum(eqq) + uewa + urf (src/forcem.f90:1055,1079) and the wall pressure.
-__device__ void uconf(const View& v, const Dyn& D, int slab) {
-    const double* a = v.acc;
-    const double* sl = a + 2 * v.nijt;
-    double slj = 0.0, sqq = 0.0;
-    for (int k = 0; k < v.nijt; ++k) {
-        slj += a[k];
-        sqq += a[v.nijt + k];
-    }
-    double urf = 0.0;
-    if (slab) {
-        const double crf = -2.0 * F32D(3.1415926535898) * v.lzi * v.lxi * v.lyi;
-        urf = -crf * v.facq * sl[ACC_DIPZ] * sl[ACC_DIPZ];
-    }
-    D.th[TH_UCONF] = slj + sqq + 0.5 * sl[ACC_UEWA] + urf;
-    D.th[TH_PRESS] = (sl[ACC_FWS + 8] - sl[ACC_FWS + 6]) / (2.0 * v.lx * v.ly) * 1000.0 /
-                     (F32D(6.022045e23) * F32D(1e-30)) * F32D(1e-5);
 }
 
 __device__ __forceinline__ void corr_ion(const View& v, const Dyn& D, int k) {
@@ -560,28 +568,74 @@ __device__ __forceinline__ void corr_rigid_pair(const View& v, const Dyn& D, int
     else corr_q(D, nr, i, Q, w0);
 }
 
-__device__ void thermo_corr(const View& v, const Dyn& D) {
+constexpr int kTailAcc = 512;  // energy sums staged in shared memory by the corrector's tail
+
+// The corrector's tail, every thread of the block that finished last: uconf = sum(elj) + sum(eqq)
+// + uewa + urf (src/forcem.f90:1055,1079), the wall pressure, and the thermostat corrector.  The
+// energy sums are loaded by all threads at once into shared memory and the thermostat words by
+// thread 0, all before any arithmetic (one round trip to L2 instead of one per dependent load);
+// thread 0 then sums in the reference's order.
+__device__ void corr_tail(const View& v, const Dyn& D, int slab, double* sh) {
+    const int na = 2 * v.nijt + ACC_NSLOT;
+    const bool staged = na <= kTailAcc;
+    if (staged)
+        for (int k = threadIdx.x; k < na; k += blockDim.x) sh[k] = __ldcg(&v.acc[k]);
     double* th = D.th;
+    double s[5], rs[5], sft = 0.0, sfr = 0.0, ke = 0.0, steps = 0.0, nreb = 0.0;
+    int reb = 0;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            s[k] = __ldcg(&th[TH_S + k]);
+            rs[k] = __ldcg(&th[TH_RS + k]);
+        }
+        sft = __ldcg(&th[TH_SFT]);
+        sfr = __ldcg(&th[TH_SFR]);
+        ke = __ldcg(&th[TH_KE]);
+        steps = __ldcg(&th[TH_STEPS]);
+        nreb = __ldcg(&th[TH_REBUILDS]);
+        reb = __ldcg(&v.status[ST_REBUILD]);
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double* a = staged ? sh : v.acc;
+    const double* sl = a + 2 * v.nijt;
+    double slj = 0.0, sqq = 0.0;
+    for (int k = 0; k < v.nijt; ++k) {
+        slj += a[k];
+        sqq += a[v.nijt + k];
+    }
+    double urf = 0.0;
+    if (slab) {
+        const double crf = -2.0 * F32D(3.1415926535898) * v.lzi * v.lxi * v.lyi;
+        urf = -crf * v.facq * sl[ACC_DIPZ] * sl[ACC_DIPZ];
+    }
+    th[TH_UCONF] = slj + sqq + 0.5 * sl[ACC_UEWA] + urf;
+    th[TH_PRESS] = (sl[ACC_FWS + 8] - sl[ACC_FWS + 6]) / (2.0 * v.lx * v.ly) * 1000.0 /
+                   (F32D(6.022045e23) * F32D(1e-30)) * F32D(1e-5);
     if (D.body.temper != -1.0) {
-        double* s = th + TH_S;
-        double* rs = th + TH_RS;
-        double rc = th[TH_SFT] - s[1];
+        double rc = sft - s[1];
         s[0] = s[0] + Gf01 * rc;
-        s[1] = th[TH_SFT];
+        s[1] = sft;
         s[2] = s[2] + Gf21 * rc;
         s[3] = s[3] + Gf31 * rc;
         s[4] = s[4] + Gf41 * rc;
-        rc = th[TH_SFR] - rs[1];
+        rc = sfr - rs[1];
         rs[0] = rs[0] + Gf01 * rc;
-        rs[1] = th[TH_SFR];
+        rs[1] = sfr;
         rs[2] = rs[2] + Gf21 * rc;
         rs[3] = rs[3] + Gf31 * rc;
         rs[4] = rs[4] + Gf41 * rc;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            th[TH_S + k] = s[k];
+            th[TH_RS + k] = rs[k];
+        }
     }
     const long nfree = v.nliqa - v.nriga;
-    th[TH_TEMPNOW] = th[TH_KE] * 1000.0 / (3.0 * F32D(8.31441) * (double)(float)(nfree + 2 * v.nrig));
-    th[TH_STEPS] += 1.0;
-    if (v.status[ST_REBUILD]) th[TH_REBUILDS] += 1.0;
+    th[TH_TEMPNOW] = ke * 1000.0 / (3.0 * F32D(8.31441) * (double)(float)(nfree + 2 * v.nrig));
+    th[TH_STEPS] = steps + 1.0;
+    if (reb) th[TH_REBUILDS] = nreb + 1.0;
 }
 
 // The correctors read the thermostat values of the predictor; the block that finishes last then
@@ -642,10 +696,10 @@ __global__ void __launch_bounds__(NT) k_corr(View v, Dyn D, int slab, int lanes,
         block_atomic_sum<NT>(sy, &v.acc[2 * v.nijt + ACC_FWS0 + 1]);
         block_atomic_sum<NT>(sz, &v.acc[2 * v.nijt + ACC_FWS0 + 2]);
     }
-    if (last_block(&D.done[1]) && threadIdx.x == 0) {
-        uconf(v, D, slab);
-        thermo_corr(v, D);
-        D.done[1] = 0u;
+    __shared__ double sh_acc[kTailAcc];
+    if (last_block(&D.done[1])) {
+        if (threadIdx.x == 0) D.done[1] = 0u;
+        corr_tail(v, D, slab, sh_acc);
     }
 }
 

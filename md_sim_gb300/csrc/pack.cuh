@@ -81,13 +81,20 @@ __device__ __forceinline__ void pack_block(const View& v, const Pk& pk, double m
 __device__ __forceinline__ void pack_close(const View& v, const Pk& pk, int dip, int force, int reset_status,
                                            double* red) {
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    const int na = 2 * v.nijt + ACC_NSLOT, kmax = 2 * v.nijt + ACC_MAXD, kdip = 2 * v.nijt + ACC_DIPZ;
     __threadfence();
+    // loads first (the tail of a kernel: one round trip to L2 instead of one per dependent load)
+    double maxd = 0.0;
+    int frb = 0;
+    if (threadIdx.x == 0) {
+        maxd = __ldcg(&v.acc[kmax]);
+        frb = __ldcg(&v.status[ST_FORCE_RB]);
+    }
     double s = 0.0;
     for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += __ldcg(&pk.part[b]);
     s = warp_sum(s);
     if (l == 0) red[w] = s;
     __syncthreads();
-    const int na = 2 * v.nijt + ACC_NSLOT, kmax = 2 * v.nijt + ACC_MAXD, kdip = 2 * v.nijt + ACC_DIPZ;
     for (int k = threadIdx.x; k < na; k += blockDim.x)
         if (k != kmax && k != kdip) v.acc[k] = 0.0;
     if (reset_status && threadIdx.x < 2) v.status[ST_LIST_OVF + threadIdx.x] = 0;
@@ -95,8 +102,8 @@ __device__ __forceinline__ void pack_close(const View& v, const Pk& pk, int dip,
         double dz = 0.0;
         for (int k = 0; k < nw; ++k) dz += red[k];
         v.acc[kdip] = dip ? dz : 0.0;
-        const double aux = fmax(__ldcg(&v.acc[kmax]), v.dshsq);
-        v.status[ST_REBUILD] = (force || v.status[ST_FORCE_RB] || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
+        const double aux = fmax(maxd, v.dshsq);
+        v.status[ST_REBUILD] = (force || frb || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
         v.status[ST_FORCE_RB] = 0;
         v.acc[kmax] = 0.0;
     }
