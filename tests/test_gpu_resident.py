@@ -75,3 +75,56 @@ def test_nve_energy_drift(gpulib):
     h0 = g.run(50)["htot"]
     h1 = g.run(400)["htot"]
     assert abs(h1 - h0) < 0.01 * abs(h0)
+
+
+def _compare_mixed(sg, sr, rg, rr, pos_tol=1e-6, e_tol=2e-5):
+    """Mixed precision against the FP64 oracle: the same trajectory to within what the FP32 force
+    arithmetic moves it in a few steps (positions relative to the box, energies relative)."""
+    L = sg.lx
+    for a, b in ((sg.x0, sr.x0), (sg.y0, sr.y0), (sg.z0, sr.z0)):
+        assert np.abs(a - b).max() < pos_tol * L
+    for key in ("kp", "kw", "ke", "uconf"):
+        assert abs(rg[key] - rr[key]) <= e_tol * (abs(rr[key]) + 1.0), (key, rg[key], rr[key])
+
+
+@pytest.mark.parametrize("name,fn,steps", [
+    # the predictor packs the force records (walls: wall-packing blocks), molecules on lane pairs,
+    # the corrector fused with the final merge
+    ("slab512_nve", lambda: configs.slab_water(nwat=512, cells=6), 10),
+    ("slab512_nvt", lambda: configs.slab_water(nwat=512, cells=6, nvt=True), 10),
+    # point ions among the waters: flexible units beside the molecule pairs
+    ("electrolyte", lambda: configs.slab_electrolyte(), 10),
+    # no walls: packing blocks only for molecules
+    ("bulk256", lambda: configs.bulk_water(), 10),
+    # SHAKE surface molecules: the separate packing kernel, merge fused with the corrector
+    ("shake256", lambda: configs.shake_water(nwat=256, cells=6), 8),
+])
+def test_mixed_run_matches_oracle(name, fn, steps, oracle, gpulib):
+    s, prm = fn()
+    sg, sr = s.copy(), s.copy()
+    pg = abi.RunParams(**{f: getattr(prm, f) for f in prm.__dataclass_fields__})
+    pg.precision = abi.MDG_MIXED
+    g, r = abi.Context(gpulib, sg, pg), abi.Context(oracle, sr, prm)
+    g.set_state(sg)
+    r.set_state(sr)
+    rg, rr = g.run(steps), r.run(steps)
+    g.get_state(sg)
+    r.get_state(sr)
+    _compare_mixed(sg, sr, rg, rr)
+    assert rg["steps"] == steps
+
+
+@pytest.mark.parametrize("nwat,cells", [
+    (3000, 12),   # 20 molecules per warp: one lane each, one warp per block
+    (5200, 16),   # 32 molecules per warp, blocks of four warps
+])
+def test_integrator_layouts_match_oracle(nwat, cells, oracle, gpulib):
+    """The integrator's other lane layouts (larger systems) against the oracle, FP64."""
+    sg, sr, g, r = _pair(lambda: configs.slab_water(nwat=nwat, cells=cells), oracle, gpulib)
+    rg = g.run(3)
+    rr = r.run(3)
+    g.get_state(sg)
+    r.get_state(sr)
+    _compare(sg, sr)
+    for key in ("kp", "kw", "ke", "uconf"):
+        assert abs(rg[key] - rr[key]) <= 1e-9 * (abs(rr[key]) + 1.0), (key, rg[key], rr[key])
