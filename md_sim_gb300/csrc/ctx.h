@@ -150,6 +150,9 @@ struct TcPlan {
     int4* row2 = nullptr;    // pass-2 rows, sorted by their K-step range (nchunk2 x kRC, padded)
     int* nlen2 = nullptr;
     int4* chunk2 = nullptr;  // per pass-2 chunk: image byte offset, first K step, K steps
+    int4* items2 = nullptr;  // per pass-2 CTA: atom tile, first chunk, end chunk, whole tile (1) or piece (0)
+    int nitems2 = 0;
+    int zero2 = 0;           // first atom of the tiles split into pieces (their forces are summed atomically)
     size_t img_bytes = 0;
 };
 

@@ -437,7 +437,13 @@ constexpr uint32_t kTile2 = kNC2 * 32;  // one N x 16 B tile (bytes)
 
 __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restrict__ rows,
                             const int* __restrict__ nlen, const int4* __restrict__ chunks, TcDims d,
-                            unsigned char* img, const float* cmax) {
+                            unsigned char* img, const float* cmax, double* frc, int zero_from, int nmove) {
+    if (blockIdx.y == 0)  // forces of the atoms whose pass-2 tiles are cut into pieces
+        for (int i = zero_from + blockIdx.x * blockDim.x + threadIdx.x; i < nmove; i += gridDim.x * blockDim.x) {
+            frc[i] = 0.0;
+            frc[nmove + i] = 0.0;
+            frc[2 * nmove + i] = 0.0;
+        }
     const float inv = cmax[0] > 0.f ? 1.0f / cmax[0] : 1.0f;
     const int c = blockIdx.y;
     const int4 ch = chunks[c];
@@ -505,7 +511,8 @@ __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
 __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
                                                      const unsigned char* __restrict__ img,
                                                      const int4* __restrict__ rows, const int4* __restrict__ chunks,
-                                                     TcDims d, const float* cmax, double* __restrict__ frc) {
+                                                     const int4* __restrict__ items, TcDims d, const float* cmax,
+                                                     double* __restrict__ frc) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC, d.nst2);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -515,8 +522,10 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     float4* rlm = reinterpret_cast<float4*>(sm + L.off_rows);
     int* err = &v.status[ST_TC_TIMEOUT];
-    const int atom0 = blockIdx.x * 128;
-    const int NC = d.nchunk2;
+    const int4 item = items[blockIdx.x];  // atom tile, chunks [c0, c0 + NC), whole tile or piece
+    const int atom0 = item.x * 128;
+    const int c0 = item.y, NC = item.z - item.y;
+    const int NCT = d.nchunk2;
     if (t == 0) {
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(tc::smem_u32(&full[b]), 1);
@@ -525,7 +534,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
         }
         tc::mbar_fence_init();
     }
-    for (int r = t; r < NC * kRC; r += kT2) {
+    for (int r = t; r < NCT * kRC; r += kT2) {
         const int4 rw = r < d.nrow ? rows[r] : make_int4(0, 0, 0, 0);
         int restart = (r & 7) == 0 || r >= d.nrow;
         if (!restart) {
@@ -570,9 +579,9 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             const uint32_t bbase = tc::smem_u32(sm + L.off_b);
             const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(bbase);
             const bool two = d.nst2 == 2;
-            auto copy = [&](int c) {
+            auto copy = [&](int c) {  // c: index within this item's chunks
                 const int s = two ? (c & 1) : 0;
-                const int4 ch = chunks[c];
+                const int4 ch = chunks[c0 + c];
                 const uint32_t bytes = (uint32_t)ch.z * kTile2;  // hi half, then lo half
                 const uint32_t fb = tc::smem_u32(&full[s]);
                 tc::mbar_expect_tx(fb, 2 * bytes);
@@ -591,7 +600,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 tc::fence_after();
                 const uint32_t dcol = tmem + s * kNC2;
                 const uint64_t dB = dB0 + (uint64_t)((sb * L.img) >> 4);
-                const int4 ch = chunks[c];
+                const int4 ch = chunks[c0 + c];
                 for (int ksl = 0; ksl < ch.z; ++ksl) {
                     const int ks = ch.y + ksl;
                     const uint64_t ah = dA0 + (uint64_t)(ks * 256), al = dA0 + (uint64_t)((d.KS + ks) * 256);
@@ -640,7 +649,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 float ec = 0.f, es = 0.f;
 #pragma unroll
                 for (int rr = 0; rr < 16; ++rr) {
-                    const float4 lm = rlm[c * kRC + hf * 16 + rr];
+                    const float4 lm = rlm[(c0 + c) * kRC + hf * 16 + rr];
                     const int lb = __float_as_int(lm.z);
                     if (rr == 0 || lb < 0) {
                         phase((uint32_t)(lb & 0x7fffffff) * rec.x + (uint32_t)__float_as_int(lm.w) * rec.y, ec, es);
@@ -667,14 +676,22 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             red[256 + ra] = alive ? fz : 0.f;
         }
         tc::named_sync(1, 256);
-        if (hf == 0 && ok) {  // each atom has one writer: plain stores (a timed-out block leaves zeros and its status)
-            fx += red[ra];
+        if (hf == 0 && ok) {  // a whole tile's atoms have one writer: plain stores; pieces add
+            fx += red[ra];       // (a timed-out block leaves zeros and its status)
             fy += red[128 + ra];
             fz += red[256 + ra];
             const double q = alive ? (double)__uint_as_float(rec.w) * (double)cmax[0] : 0.0;
-            frc[at] = q * (double)d.px * (double)fx;
-            frc[v.nmove + at] = q * (double)d.py * (double)fy;
-            frc[2 * v.nmove + at] = q * (double)d.pz * (double)fz;
+            const double gx = q * (double)d.px * (double)fx, gy = q * (double)d.py * (double)fy,
+                         gz = q * (double)d.pz * (double)fz;
+            if (item.w) {
+                frc[at] = gx;
+                frc[v.nmove + at] = gy;
+                frc[2 * v.nmove + at] = gz;
+            } else {
+                atomicAdd(&frc[at], gx);
+                atomicAdd(&frc[v.nmove + at], gy);
+                atomicAdd(&frc[2 * v.nmove + at], gz);
+            }
         }
     }
     __syncthreads();
@@ -827,6 +844,38 @@ int recip_tc_setup(Ctx& c) {
             off += (size_t)2 * nks * kTile2;
         }
         p.img_bytes = off;
+        // Work items of pass 2 (one CTA each): whole atom tiles, except that the tiles of the last,
+        // partial wave (all tiles when there are fewer than one per SM) are cut into pieces of
+        // about equal K-step work, so that the wave fills the SMs; pieces add their forces
+        // atomically into forces zeroed by the operand-packing kernel before.
+        {
+            const int ntile = (v.nmove + 127) / 128, tail = ntile % 152;
+            int ksum = 0;
+            for (int cc = 0; cc < p.nchunk2; ++cc) ksum += chunk2[cc].z;
+            const int S = tail > 0 ? std::min(152 / tail, std::max(1, p.nchunk2 / 2)) : 1;
+            const int first = S >= 2 ? ntile - tail : ntile;
+            std::vector<int4> items;
+            for (int t = 0; t < first; ++t) items.push_back(make_int4(t, 0, p.nchunk2, 1));
+            for (int t = first; t < ntile; ++t) {
+                int c0 = 0, acc = 0;
+                for (int piece = 1; piece <= S && c0 < p.nchunk2; ++piece) {
+                    int c1 = c0;
+                    const long target = (long)ksum * piece / S;
+                    while (c1 < p.nchunk2 && (acc + chunk2[c1].z <= target || c1 == c0)) acc += chunk2[c1++].z;
+                    if (piece == S) {
+                        while (c1 < p.nchunk2) acc += chunk2[c1++].z;
+                    }
+                    items.push_back(make_int4(t, c0, c1, 0));
+                    c0 = c1;
+                }
+            }
+            p.nitems2 = (int)items.size();
+            p.zero2 = std::min(first * 128, v.nmove);
+            p.items2 = (int4*)dalloc(c, sizeof(int4) * std::max(p.nitems2, 1));
+            if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
+            if (p.nitems2 > 0)
+                MDG_CUDA(cudaMemcpy(p.items2, items.data(), sizeof(int4) * p.nitems2, cudaMemcpyHostToDevice));
+        }
         p.row2 = (int4*)dalloc(c, sizeof(int4) * std::max(nrp, 1));
         p.nlen2 = (int*)dalloc(c, sizeof(int) * std::max(nrp, 1));
         p.chunk2 = (int4*)dalloc(c, sizeof(int4) * std::max(p.nchunk2, 1));
@@ -868,10 +917,10 @@ void recip_tc(Ctx& c) {
     k_tc_sreduce<<<(int)((nred + 31) / 32), 32 * kRedG, 0, c.stream>>>(
         v, c.d_tc_part, p.nsplit1, p.rtot, d, ks.row, ks.row_nlen, ks.ak, ks.qw, ks.s, ks.c, c.d_tc_cf, c.d_tc_cmax);
     const int per_chunk = p.KS * kNC2 * 8;  // elements of the widest chunk image
-    k_tc_prep_c<<<dim3((per_chunk + 255) / 256, p.nchunk2), 256, 0, c.stream>>>(c.d_tc_cf, p.row2, p.nlen2, p.chunk2, d,
-                                                                               c.d_tc_img, c.d_tc_cmax);
-    k_tc_force<<<(v.nmove + 127) / 128, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, p.row2, p.chunk2, d,
-                                                                  c.d_tc_cmax, c.d_frc);
+    k_tc_prep_c<<<dim3((per_chunk + 255) / 256, p.nchunk2), 256, 0, c.stream>>>(
+        c.d_tc_cf, p.row2, p.nlen2, p.chunk2, d, c.d_tc_img, c.d_tc_cmax, c.d_frc, p.zero2, v.nmove);
+    k_tc_force<<<p.nitems2, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, p.row2, p.chunk2, p.items2, d,
+                                                      c.d_tc_cmax, c.d_frc);
 }
 
 int umma_selftest(int n, int k, const float* a, const float* b, float* dout, std::string& err) {
