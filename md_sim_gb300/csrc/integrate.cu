@@ -344,19 +344,31 @@ struct PackArgs {
     int npred;  // blocks of the predictor proper
 };
 
+// Blocks of one-warp predictors that also pack (NT 32) carry a second warp that only works in the
+// block that finishes last: it runs the thermostat while the first warp closes the packing.
+template <int NT, bool PACK>
+struct PredBlock {
+    static constexpr int kThreads = (PACK && NT == 32) ? 64 : NT;
+};
+
 template <int NT, bool PACK, bool PAIR>
-__global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z, PackArgs P) {
+__global__ void __launch_bounds__(PredBlock<NT, PACK>::kThreads) k_pred(View v, Dyn D, int lanes, Clear z,
+                                                                        PackArgs P) {
+    constexpr bool kTailWarp = PredBlock<NT, PACK>::kThreads > NT;
     __shared__ double red[8];
     double kp = 0.0, sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
     double mz = 0.0, md = 0.0;
     const int nu = D.nion + v.nrig;
     const int npred = PACK ? P.npred : gridDim.x;
-    if (blockIdx.x == 0) {
+    const bool worker = !kTailWarp || threadIdx.x < NT;
+    if (blockIdx.x == 0 && worker) {
         for (int j = 0; j < 2; ++j)
             for (int k = threadIdx.x; k < z.n[j]; k += NT) z.p[j][k] = 0.0;
         if (PACK && P.pk.cmax && threadIdx.x == 0) *P.pk.cmax = 0.f;
     }
-    if (blockIdx.x < npred) {
+    if (!worker) {
+        // the tail warp: nothing until the block's close
+    } else if (blockIdx.x < npred) {
         for (int r = 0;; ++r) {
             int u, role = 0;
             if constexpr (PAIR) u = unit_of_pair<NT>(lanes, r, npred, role);
@@ -413,22 +425,41 @@ __global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z, 
                 }
             }
         }
-        block_atomic_sum<NT>(kp, &D.isum[0]);
-        for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
-        for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
     } else if constexpr (PACK) {
         const int nw = gridDim.x - npred;
         for (int a = v.nmove + (blockIdx.x - npred) * NT + threadIdx.x; a < v.ntota; a += nw * NT)
             pack_atom(v, P.pk, a, v.x[a], v.y[a], v.z[a], 0.0, 0.0, 0.0, false);
     }
+    if (blockIdx.x < npred) {
+        if constexpr (kTailWarp) {
+            if (worker) {  // one warp: the sums within it
+                block_atomic_sum<NT>(kp, &D.isum[0]);
+                for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
+                for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
+            }
+        } else {
+            block_atomic_sum<NT>(kp, &D.isum[0]);
+            for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
+            for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
+        }
+    }
     if constexpr (PACK) pack_block(v, P.pk, mz, md, red);
     if (last_block(&D.done[0])) {
-        ThermoIn tin;
-        if (threadIdx.x == 0) tin = thermo_pred_load(D);  // issued before the packing's stores
-        if constexpr (PACK) pack_close(v, P.pk, P.dip, 0, 0, red);
-        if (threadIdx.x == 0) {
-            thermo_pred(v, D, tin);
-            D.done[0] = 0u;
+        if constexpr (kTailWarp) {
+            if (threadIdx.x < 32) {
+                pack_close_warp(v, P.pk, P.dip, 0, 0);
+            } else if (threadIdx.x == 32) {
+                thermo_pred(v, D, thermo_pred_load(D));
+                D.done[0] = 0u;
+            }
+        } else {
+            ThermoIn tin;
+            if (threadIdx.x == 0) tin = thermo_pred_load(D);  // issued before the packing's stores
+            if constexpr (PACK) pack_close(v, P.pk, P.dip, 0, 0, red);
+            if (threadIdx.x == 0) {
+                thermo_pred(v, D, tin);
+                D.done[0] = 0u;
+            }
         }
     }
 }
@@ -746,11 +777,12 @@ void predict_launch(Ctx& c, bool clear_acc, bool clear_kps, bool pack) {
         const int nb = nblk(nu, 32);
         P.npred = nb;
         const int nwb = pack ? std::min((nwall + 31) / 32, kSM * 8) : 0;
+        constexpr int kPT = PredBlock<32, true>::kThreads;
         if (lanes <= 16) {  // two lanes per molecule
-            if (pack) k_pred<32, true, true><<<nb + nwb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+            if (pack) k_pred<32, true, true><<<nb + nwb, kPT, 0, c.stream>>>(v, D, lanes, z, P);
             else k_pred<32, false, true><<<nb, 32, 0, c.stream>>>(v, D, lanes, z, P);
         } else {
-            if (pack) k_pred<32, true, false><<<nb + nwb, 32, 0, c.stream>>>(v, D, lanes, z, P);
+            if (pack) k_pred<32, true, false><<<nb + nwb, kPT, 0, c.stream>>>(v, D, lanes, z, P);
             else k_pred<32, false, false><<<nb, 32, 0, c.stream>>>(v, D, lanes, z, P);
         }
     } else {

@@ -90,7 +90,10 @@ __device__ __forceinline__ void pack_close(const View& v, const Pk& pk, int dip,
         maxd = __ldcg(&v.acc[kmax]);
         frb = __ldcg(&v.status[ST_FORCE_RB]);
     }
+    // the shares: several per thread, their loads unrolled ahead of the adds (a loop that adds
+    // each before loading the next pays one L2 round trip per share)
     double s = 0.0;
+#pragma unroll 16
     for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += __ldcg(&pk.part[b]);
     s = warp_sum(s);
     if (l == 0) red[w] = s;
@@ -102,6 +105,34 @@ __device__ __forceinline__ void pack_close(const View& v, const Pk& pk, int dip,
         double dz = 0.0;
         for (int k = 0; k < nw; ++k) dz += red[k];
         v.acc[kdip] = dip ? dz : 0.0;
+        const double aux = fmax(maxd, v.dshsq);
+        v.status[ST_REBUILD] = (force || frb || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
+        v.status[ST_FORCE_RB] = 0;
+        v.acc[kmax] = 0.0;
+    }
+}
+
+// The same close by one warp (no block barrier), so that another warp of the block can run other
+// work at the same time; every lane of the warp calls it.
+__device__ __forceinline__ void pack_close_warp(const View& v, const Pk& pk, int dip, int force, int reset_status) {
+    const int l = threadIdx.x & 31;
+    const int na = 2 * v.nijt + ACC_NSLOT, kmax = 2 * v.nijt + ACC_MAXD, kdip = 2 * v.nijt + ACC_DIPZ;
+    __threadfence();
+    double maxd = 0.0;
+    int frb = 0;
+    if (l == 0) {
+        maxd = __ldcg(&v.acc[kmax]);
+        frb = __ldcg(&v.status[ST_FORCE_RB]);
+    }
+    double s = 0.0;
+#pragma unroll 16
+    for (int b = l; b < gridDim.x; b += 32) s += __ldcg(&pk.part[b]);
+    s = warp_sum(s);
+    for (int k = l; k < na; k += 32)
+        if (k != kmax && k != kdip) v.acc[k] = 0.0;
+    if (reset_status && l < 2) v.status[ST_LIST_OVF + l] = 0;
+    if (l == 0) {
+        v.acc[kdip] = dip ? s : 0.0;
         const double aux = fmax(maxd, v.dshsq);
         v.status[ST_REBUILD] = (force || frb || 4.0 * aux > v.skin * v.skin) ? 1 : 0;
         v.status[ST_FORCE_RB] = 0;
