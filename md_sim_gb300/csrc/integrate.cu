@@ -601,34 +601,19 @@ __device__ __forceinline__ void corr_rigid_pair(const View& v, const Dyn& D, int
 
 constexpr int kTailAcc = 512;  // energy sums staged in shared memory by the corrector's tail
 
-// The corrector's tail, every thread of the block that finished last: uconf = sum(elj) + sum(eqq)
-// + uewa + urf (src/forcem.f90:1055,1079), the wall pressure, and the thermostat corrector.  The
-// energy sums are loaded by all threads at once into shared memory and the thermostat words by
-// thread 0, all before any arithmetic (one round trip to L2 instead of one per dependent load);
-// thread 0 then sums in the reference's order.
-__device__ void corr_tail(const View& v, const Dyn& D, int slab, double* sh) {
+// The corrector's tail, in the block that finished last, as two independent parts on two warps:
+// uconf = sum(elj) + sum(eqq) + uewa + urf (src/forcem.f90:1055,1079) and the wall pressure (the
+// energy sums loaded by one warp at once into shared memory, then summed by its lane 0 in the
+// reference's order), and the thermostat corrector with the step counters.
+__device__ void corr_energy(const View& v, const Dyn& D, int slab, double* sh) {
+    const int l = threadIdx.x & 31;
     const int na = 2 * v.nijt + ACC_NSLOT;
     const bool staged = na <= kTailAcc;
     if (staged)
-        for (int k = threadIdx.x; k < na; k += blockDim.x) sh[k] = __ldcg(&v.acc[k]);
+        for (int k = l; k < na; k += 32) sh[k] = __ldcg(&v.acc[k]);
+    __syncwarp();
+    if (l != 0) return;
     double* th = D.th;
-    double s[5], rs[5], sft = 0.0, sfr = 0.0, ke = 0.0, steps = 0.0, nreb = 0.0;
-    int reb = 0;
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            s[k] = __ldcg(&th[TH_S + k]);
-            rs[k] = __ldcg(&th[TH_RS + k]);
-        }
-        sft = __ldcg(&th[TH_SFT]);
-        sfr = __ldcg(&th[TH_SFR]);
-        ke = __ldcg(&th[TH_KE]);
-        steps = __ldcg(&th[TH_STEPS]);
-        nreb = __ldcg(&th[TH_REBUILDS]);
-        reb = __ldcg(&v.status[ST_REBUILD]);
-    }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
     const double* a = staged ? sh : v.acc;
     const double* sl = a + 2 * v.nijt;
     double slj = 0.0, sqq = 0.0;
@@ -644,6 +629,20 @@ __device__ void corr_tail(const View& v, const Dyn& D, int slab, double* sh) {
     th[TH_UCONF] = slj + sqq + 0.5 * sl[ACC_UEWA] + urf;
     th[TH_PRESS] = (sl[ACC_FWS + 8] - sl[ACC_FWS + 6]) / (2.0 * v.lx * v.ly) * 1000.0 /
                    (F32D(6.022045e23) * F32D(1e-30)) * F32D(1e-5);
+}
+
+// the thermostat corrector and the step counters (one thread; all loads first)
+__device__ void corr_thermo(const View& v, const Dyn& D) {
+    double* th = D.th;
+    double s[5], rs[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        s[k] = __ldcg(&th[TH_S + k]);
+        rs[k] = __ldcg(&th[TH_RS + k]);
+    }
+    const double sft = __ldcg(&th[TH_SFT]), sfr = __ldcg(&th[TH_SFR]), ke = __ldcg(&th[TH_KE]);
+    const double steps = __ldcg(&th[TH_STEPS]), nreb = __ldcg(&th[TH_REBUILDS]);
+    const int reb = __ldcg(&v.status[ST_REBUILD]);
     if (D.body.temper != -1.0) {
         double rc = sft - s[1];
         s[0] = s[0] + Gf01 * rc;
@@ -669,19 +668,26 @@ __device__ void corr_tail(const View& v, const Dyn& D, int slab, double* sh) {
     if (reb) th[TH_REBUILDS] = nreb + 1.0;
 }
 
+// Blocks of one-warp correctors carry a second warp for the tail (as the predictor's).
+template <int NT>
+struct CorrBlock {
+    static constexpr int kThreads = NT == 32 ? 64 : NT;
+};
+
 // The correctors read the thermostat values of the predictor; the block that finishes last then
 // adds uconf/press and corrects the thermostat.  MERGE: the mixed force form's final merge and
 // force_sum (merge.cuh) run here, each unit's just before its corrector, instead of in a kernel
 // of their own; units past the molecules and ions are the surface atoms, whose forces SHAKE's
 // Verlet step reads next.
 template <int NT, bool MERGE, bool PAIR>
-__global__ void __launch_bounds__(NT) k_corr(View v, Dyn D, int slab, int lanes, MergeArgs A) {
+__global__ void __launch_bounds__(CorrBlock<NT>::kThreads) k_corr(View v, Dyn D, int slab, int lanes, MergeArgs A) {
+    constexpr bool kTailWarp = CorrBlock<NT>::kThreads > NT;
     const int nsurf = MERGE ? v.nmove - v.nliqa : 0;
     const int nu = D.nion + v.nrig + nsurf;
     MergeArgs M;
     if constexpr (MERGE) M = merge_begin(v, A);
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    for (int r = 0;; ++r) {
+    for (int r = 0; !kTailWarp || threadIdx.x < NT; ++r) {
         int u, role = 0;
         if constexpr (PAIR) u = unit_of_pair<NT>(lanes, r, gridDim.x, role);
         else u = unit_of<NT>(lanes, r, gridDim.x);
@@ -723,14 +729,20 @@ __global__ void __launch_bounds__(NT) k_corr(View v, Dyn D, int slab, int lanes,
         }
     }
     if constexpr (MERGE) {
-        block_atomic_sum<NT>(sx, &v.acc[2 * v.nijt + ACC_FWS0 + 0]);
-        block_atomic_sum<NT>(sy, &v.acc[2 * v.nijt + ACC_FWS0 + 1]);
-        block_atomic_sum<NT>(sz, &v.acc[2 * v.nijt + ACC_FWS0 + 2]);
+        if (!kTailWarp || threadIdx.x < NT) {
+            block_atomic_sum<NT>(sx, &v.acc[2 * v.nijt + ACC_FWS0 + 0]);
+            block_atomic_sum<NT>(sy, &v.acc[2 * v.nijt + ACC_FWS0 + 1]);
+            block_atomic_sum<NT>(sz, &v.acc[2 * v.nijt + ACC_FWS0 + 2]);
+        }
     }
     __shared__ double sh_acc[kTailAcc];
     if (last_block(&D.done[1])) {
-        if (threadIdx.x == 0) D.done[1] = 0u;
-        corr_tail(v, D, slab, sh_acc);
+        if (threadIdx.x < 32) {
+            if (threadIdx.x == 0) D.done[1] = 0u;
+            corr_energy(v, D, slab, sh_acc);
+        } else if (threadIdx.x == 32) {
+            corr_thermo(v, D);
+        }
     }
 }
 
@@ -800,12 +812,13 @@ void correct_launch(Ctx& c, bool merge) {
     const int nu = D.nion + v.nrig + (merge ? v.nmove - v.nliqa : 0), lanes = lanes_of(nu);
     const int slab = c.variant == MDG_SLAB ? 1 : 0;
     const MergeArgs A = merge ? merge_args(c, c.d_frc) : MergeArgs{};
+    constexpr int kCT = CorrBlock<32>::kThreads;
     if (lanes <= 16) {
-        if (merge) k_corr<32, true, true><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
-        else k_corr<32, false, true><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
+        if (merge) k_corr<32, true, true><<<nblk(nu, 32), kCT, 0, c.stream>>>(v, D, slab, lanes, A);
+        else k_corr<32, false, true><<<nblk(nu, 32), kCT, 0, c.stream>>>(v, D, slab, lanes, A);
     } else if (lanes < 32) {
-        if (merge) k_corr<32, true, false><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
-        else k_corr<32, false, false><<<nblk(nu, 32), 32, 0, c.stream>>>(v, D, slab, lanes, A);
+        if (merge) k_corr<32, true, false><<<nblk(nu, 32), kCT, 0, c.stream>>>(v, D, slab, lanes, A);
+        else k_corr<32, false, false><<<nblk(nu, 32), kCT, 0, c.stream>>>(v, D, slab, lanes, A);
     } else {
         if (merge) k_corr<128, true, false><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes, A);
         else k_corr<128, false, false><<<nblk(nu, 128), 128, 0, c.stream>>>(v, D, slab, lanes, A);
