@@ -204,6 +204,7 @@ struct Ctx {
     float* d_shake_rec = nullptr; // ncons x 12 recorded features / multipliers
     bool shake_model = false, shake_record = false;
     int pair_blocks = 0;          // blocks of the real-space loops (0: by head count); autotuned
+    int pred_parts = 0;           // blocks (dipole shares) of the last packing predictor launch
     Meas meas;                    // measurement histograms (measure.cu)
     std::vector<int64_t> h_moltypen, h_nt, h_ns, h_itype;  // molecule types and site types (cfgio.cu)
     int64_t widom_cap = 0;        // Widom insertion scratch (widom.cu)
@@ -325,6 +326,8 @@ cudaError_t unpin_host_range(void* p);
 // pack: also write the mixed form's per-atom records, the slab dipole and the list rebuild
 // decision for the force call next (in place of its packing kernel; no surface atoms)
 void predict_launch(Ctx& c, bool clear_acc = false, bool clear_kps = false, bool pack = false);
+// after a packing predictor: its packing close (dipole, rebuild decision) and the thermostat predictor
+void step_close_launch(Ctx& c);
 // merge: also the mixed form's final merge + force_sum, left out of the force phases before it
 void correct_launch(Ctx& c, bool merge = false);
 

@@ -344,31 +344,27 @@ struct PackArgs {
     int npred;  // blocks of the predictor proper
 };
 
-// Blocks of one-warp predictors that also pack (NT 32) carry a second warp that only works in the
-// block that finishes last: it runs the thermostat while the first warp closes the packing.
-template <int NT, bool PACK>
-struct PredBlock {
-    static constexpr int kThreads = (PACK && NT == 32) ? 64 : NT;
-};
-
+// A packing predictor has no tail: block 0 clears the energy sums first (all but the displacement
+// maximum, which the blocks raise as they go), and the close of the packing and the thermostat
+// predictor run in k_step_close on the list's stream, off the path of the reciprocal sum.
 template <int NT, bool PACK, bool PAIR>
-__global__ void __launch_bounds__(PredBlock<NT, PACK>::kThreads) k_pred(View v, Dyn D, int lanes, Clear z,
-                                                                        PackArgs P) {
-    constexpr bool kTailWarp = PredBlock<NT, PACK>::kThreads > NT;
+__global__ void __launch_bounds__(NT) k_pred(View v, Dyn D, int lanes, Clear z, PackArgs P) {
     __shared__ double red[8];
     double kp = 0.0, sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
     double mz = 0.0, md = 0.0;
     const int nu = D.nion + v.nrig;
     const int npred = PACK ? P.npred : gridDim.x;
-    const bool worker = !kTailWarp || threadIdx.x < NT;
-    if (blockIdx.x == 0 && worker) {
+    if (blockIdx.x == 0) {
         for (int j = 0; j < 2; ++j)
             for (int k = threadIdx.x; k < z.n[j]; k += NT) z.p[j][k] = 0.0;
-        if (PACK && P.pk.cmax && threadIdx.x == 0) *P.pk.cmax = 0.f;
+        if constexpr (PACK) {
+            const int na = 2 * v.nijt + ACC_NSLOT, kmax = 2 * v.nijt + ACC_MAXD;
+            for (int k = threadIdx.x; k < na; k += NT)
+                if (k != kmax) v.acc[k] = 0.0;
+            if (P.pk.cmax && threadIdx.x == 0) *P.pk.cmax = 0.f;
+        }
     }
-    if (!worker) {
-        // the tail warp: nothing until the block's close
-    } else if (blockIdx.x < npred) {
+    if (blockIdx.x < npred) {
         for (int r = 0;; ++r) {
             int u, role = 0;
             if constexpr (PAIR) u = unit_of_pair<NT>(lanes, r, npred, role);
@@ -431,36 +427,26 @@ __global__ void __launch_bounds__(PredBlock<NT, PACK>::kThreads) k_pred(View v, 
             pack_atom(v, P.pk, a, v.x[a], v.y[a], v.z[a], 0.0, 0.0, 0.0, false);
     }
     if (blockIdx.x < npred) {
-        if constexpr (kTailWarp) {
-            if (worker) {  // one warp: the sums within it
-                block_atomic_sum<NT>(kp, &D.isum[0]);
-                for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
-                for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
-            }
-        } else {
-            block_atomic_sum<NT>(kp, &D.isum[0]);
-            for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
-            for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
-        }
+        block_atomic_sum<NT>(kp, &D.isum[0]);
+        for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sc[d], &D.isum[1 + d]);
+        for (int d = 0; d < 3; ++d) block_atomic_sum<NT>(sw[d], &D.isum[4 + d]);
     }
-    if constexpr (PACK) pack_block(v, P.pk, mz, md, red);
-    if (last_block(&D.done[0])) {
-        if constexpr (kTailWarp) {
-            if (threadIdx.x < 32) {
-                pack_close_warp(v, P.pk, P.dip, 0, 0);
-            } else if (threadIdx.x == 32) {
-                thermo_pred(v, D, thermo_pred_load(D));
-                D.done[0] = 0u;
-            }
-        } else {
-            ThermoIn tin;
-            if (threadIdx.x == 0) tin = thermo_pred_load(D);  // issued before the packing's stores
-            if constexpr (PACK) pack_close(v, P.pk, P.dip, 0, 0, red);
-            if (threadIdx.x == 0) {
-                thermo_pred(v, D, tin);
-                D.done[0] = 0u;
-            }
-        }
+    if constexpr (PACK) {
+        pack_block(v, P.pk, mz, md, red);
+    } else if (last_block(&D.done[0]) && threadIdx.x == 0) {
+        thermo_pred(v, D, thermo_pred_load(D));
+        D.done[0] = 0u;
+    }
+}
+
+// After a packing predictor (one block of two warps): the close of its packing (slab dipole from
+// the nparts block shares, list rebuild decision) on one warp and the thermostat predictor on the
+// other.
+__global__ void __launch_bounds__(64) k_step_close(View v, Dyn D, Pk pk, int dip, int nparts) {
+    if (threadIdx.x < 32) {
+        pack_close_warp(v, pk, dip, 0, 0, nparts, false);
+    } else if (threadIdx.x == 32) {
+        thermo_pred(v, D, thermo_pred_load(D));
     }
 }
 
@@ -789,21 +775,26 @@ void predict_launch(Ctx& c, bool clear_acc, bool clear_kps, bool pack) {
         const int nb = nblk(nu, 32);
         P.npred = nb;
         const int nwb = pack ? std::min((nwall + 31) / 32, kSM * 8) : 0;
-        constexpr int kPT = PredBlock<32, true>::kThreads;
+        c.pred_parts = nb + nwb;
         if (lanes <= 16) {  // two lanes per molecule
-            if (pack) k_pred<32, true, true><<<nb + nwb, kPT, 0, c.stream>>>(v, D, lanes, z, P);
+            if (pack) k_pred<32, true, true><<<nb + nwb, 32, 0, c.stream>>>(v, D, lanes, z, P);
             else k_pred<32, false, true><<<nb, 32, 0, c.stream>>>(v, D, lanes, z, P);
         } else {
-            if (pack) k_pred<32, true, false><<<nb + nwb, kPT, 0, c.stream>>>(v, D, lanes, z, P);
+            if (pack) k_pred<32, true, false><<<nb + nwb, 32, 0, c.stream>>>(v, D, lanes, z, P);
             else k_pred<32, false, false><<<nb, 32, 0, c.stream>>>(v, D, lanes, z, P);
         }
     } else {
         const int nb = nblk(nu, 128);
         P.npred = nb;
         const int nwb = pack ? std::min((nwall + 127) / 128, kSM * 8) : 0;
+        c.pred_parts = nb + nwb;
         if (pack) k_pred<128, true, false><<<nb + nwb, 128, 0, c.stream>>>(v, D, lanes, z, P);
         else k_pred<128, false, false><<<nb, 128, 0, c.stream>>>(v, D, lanes, z, P);
     }
+}
+
+void step_close_launch(Ctx& c) {
+    k_step_close<<<1, 64, 0, c.stream>>>(c.v, dyn_of(c), c.pk, c.variant == MDG_SLAB ? 1 : 0, c.pred_parts);
 }
 
 void correct_launch(Ctx& c, bool merge) {

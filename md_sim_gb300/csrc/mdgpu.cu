@@ -252,6 +252,8 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
         recip_tc(c);
         c.stream = s0;
         MDG_CUDA(cudaEventRecord(c.ev_join, c.side));
+        // after a packing predictor, its close runs here, ahead of the list it decides
+        if (packed) step_close_launch(c);
         const bool conc = v.nliqa == v.nmove && v.nwall > 0 && v.nheads > 0;
         if (conc) {
             // third branch: the wall tail (positions only) while the list is checked and rebuilt,

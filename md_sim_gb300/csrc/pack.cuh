@@ -112,12 +112,13 @@ __device__ __forceinline__ void pack_close(const View& v, const Pk& pk, int dip,
     }
 }
 
-// The same close by one warp (no block barrier), so that another warp of the block can run other
-// work at the same time; every lane of the warp calls it.
-__device__ __forceinline__ void pack_close_warp(const View& v, const Pk& pk, int dip, int force, int reset_status) {
+// The same close by one warp of a later kernel (no block barrier, so that another warp can run
+// other work at the same time), over the nparts shares of the packing kernel; zero_acc: also clear
+// the energy sums (else the packing kernel did).  Every lane of the warp calls it.
+__device__ __forceinline__ void pack_close_warp(const View& v, const Pk& pk, int dip, int force, int reset_status,
+                                                int nparts, bool zero_acc) {
     const int l = threadIdx.x & 31;
     const int na = 2 * v.nijt + ACC_NSLOT, kmax = 2 * v.nijt + ACC_MAXD, kdip = 2 * v.nijt + ACC_DIPZ;
-    __threadfence();
     double maxd = 0.0;
     int frb = 0;
     if (l == 0) {
@@ -126,10 +127,11 @@ __device__ __forceinline__ void pack_close_warp(const View& v, const Pk& pk, int
     }
     double s = 0.0;
 #pragma unroll 16
-    for (int b = l; b < gridDim.x; b += 32) s += __ldcg(&pk.part[b]);
+    for (int b = l; b < nparts; b += 32) s += __ldcg(&pk.part[b]);
     s = warp_sum(s);
-    for (int k = l; k < na; k += 32)
-        if (k != kmax && k != kdip) v.acc[k] = 0.0;
+    if (zero_acc)
+        for (int k = l; k < na; k += 32)
+            if (k != kmax && k != kdip) v.acc[k] = 0.0;
     if (reset_status && l < 2) v.status[ST_LIST_OVF + l] = 0;
     if (l == 0) {
         v.acc[kdip] = dip ? s : 0.0;
