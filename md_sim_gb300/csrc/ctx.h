@@ -205,6 +205,8 @@ struct Ctx {
     bool shake_model = false, shake_record = false;
     int pair_blocks = 0;          // blocks of the real-space loops (0: by head count); autotuned
     int pred_parts = 0;           // blocks (dipole shares) of the last packing predictor launch
+    int pack_parts = 0;           // blocks of the last packing kernel launch, and its forced rebuild
+    bool pack_force = false;
     Meas meas;                    // measurement histograms (measure.cu)
     std::vector<int64_t> h_moltypen, h_nt, h_ns, h_itype;  // molecule types and site types (cfgio.cu)
     int64_t widom_cap = 0;        // Widom insertion scratch (widom.cu)
@@ -257,8 +259,11 @@ void lr_tail(Ctx& c);
 void pack_setup(Ctx& c);
 // per-evaluation records of the real-space loops and the reciprocal sum; clears the FP64 forces
 // and sums the slab dipole M_z
-// reset_status: also clear the list overflow words; the energy sums are always cleared
-void pack_mixed(Ctx& c, bool force_rebuild, bool reset_status = false);
+// reset_status: also clear the list overflow words; the energy sums are always cleared.
+// defer_close: the dipole and the rebuild decision are left to pack_close_launch (next, on the
+// stream that builds the list)
+void pack_mixed(Ctx& c, bool force_rebuild, bool reset_status = false, bool defer_close = false);
+void pack_close_launch(Ctx& c);
 void pairs_mixed(Ctx& c, bool merge);  // head-head pairs into F (then merged into the FP64 forces)
 void walls_mixed(Ctx& c);              // head-wall pairs into F
 // F (+ frc, + the slab dipole term) into the FP64 forces, F cleared

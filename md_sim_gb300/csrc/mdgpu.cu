@@ -244,7 +244,7 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
         // loop; both add into F with vector reductions.  Fork and join go through events, so the
         // same dependencies hold inside a captured graph.  The reciprocal forces (d_frc), F and the
         // slab dipole term join the FP64 forces in one merge at the end.
-        if (!packed) PHASE(pack_mixed(c, force_rebuild, reset_status), "pack");  // also decides the list rebuild
+        if (!packed) PHASE(pack_mixed(c, force_rebuild, reset_status, true), "pack");
         const cudaStream_t s0 = c.stream;
         MDG_CUDA(cudaEventRecord(c.ev_fork, s0));
         MDG_CUDA(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
@@ -252,8 +252,9 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
         recip_tc(c);
         c.stream = s0;
         MDG_CUDA(cudaEventRecord(c.ev_join, c.side));
-        // after a packing predictor, its close runs here, ahead of the list it decides
+        // the packing's close (dipole, rebuild decision) runs here, ahead of the list it decides
         if (packed) step_close_launch(c);
+        else pack_close_launch(c);
         const bool conc = v.nliqa == v.nmove && v.nwall > 0 && v.nheads > 0;
         if (conc) {
             // third branch: the wall tail (positions only) while the list is checked and rebuilt,

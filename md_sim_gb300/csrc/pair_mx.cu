@@ -111,11 +111,20 @@ __device__ __forceinline__ void red_v4(float4* p, float a, float b, float c) {
 
 // Records of every atom for this evaluation (pack.cuh); also clears the FP64 forces, sums the slab
 // dipole, takes the neighbour-list rebuild decision and clears the energy sums (its last block).
-__global__ void k_pack(View v, Pk pk, int dip, int force, int reset_status) {
+// defer_close: no last-block tail; block 0 clears the energy sums (all but the displacement
+// maximum) and the overflow words first, and k_pack_close closes the packing on another stream
+// while the reciprocal sum starts.
+__global__ void k_pack(View v, Pk pk, int dip, int force, int reset_status, int defer_close) {
     __shared__ double red[8];
     __shared__ bool last;
     double mz = 0.0, md = 0.0;
     if (pk.cmax && blockIdx.x == 0 && threadIdx.x == 0) *pk.cmax = 0.f;
+    if (defer_close && blockIdx.x == 0) {
+        const int na = 2 * v.nijt + ACC_NSLOT, kmax = 2 * v.nijt + ACC_MAXD;
+        for (int k = threadIdx.x; k < na; k += blockDim.x)
+            if (k != kmax) v.acc[k] = 0.0;
+        if (reset_status && threadIdx.x < 2) v.status[ST_LIST_OVF + threadIdx.x] = 0;
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.nrig + (v.nmove - v.nriga);
          i += gridDim.x * blockDim.x) {
         double a, b, c;
@@ -137,6 +146,7 @@ __global__ void k_pack(View v, Pk pk, int dip, int force, int reset_status) {
                         mv ? v.rsz[a] : 0.0, mv);
     }
     pack_block(v, pk, mz, md, red);
+    if (defer_close) return;
     __threadfence();
     if (threadIdx.x == 0) last = atomicAdd(&v.status[ST_PACK_DONE], 1) == (int)gridDim.x - 1;
     __syncthreads();
@@ -439,11 +449,23 @@ double slab_crf0(const Ctx& c) {
     return -2.0 * (double)3.1415926535898f * c.v.lzi * c.v.lxi * c.v.lyi;
 }
 
-void pack_mixed(Ctx& c, bool force_rebuild, bool reset_status) {
+__global__ void __launch_bounds__(32) k_pack_close(View v, Pk pk, int dip, int force, int nparts) {
+    pack_close_warp(v, pk, dip, force, 0, nparts, false);
+}
+
+void pack_mixed(Ctx& c, bool force_rebuild, bool reset_status, bool defer_close) {
     const View& v = c.v;
     const int n = std::max(std::max(v.ntota, v.nrig + (v.nmove - v.nriga)), 1);
-    k_pack<<<std::min((n + 255) / 256, kPackBlocks), 256, 0, c.stream>>>(v, c.pk, c.variant == MDG_SLAB ? 1 : 0,
-                                                                        force_rebuild ? 1 : 0, reset_status ? 1 : 0);
+    const int nb = std::min((n + 255) / 256, kPackBlocks);
+    c.pack_parts = nb;
+    c.pack_force = force_rebuild;
+    k_pack<<<nb, 256, 0, c.stream>>>(v, c.pk, c.variant == MDG_SLAB ? 1 : 0, force_rebuild ? 1 : 0,
+                                     reset_status ? 1 : 0, defer_close ? 1 : 0);
+}
+
+void pack_close_launch(Ctx& c) {
+    k_pack_close<<<1, 32, 0, c.stream>>>(c.v, c.pk, c.variant == MDG_SLAB ? 1 : 0, c.pack_force ? 1 : 0,
+                                         c.pack_parts);
 }
 
 void merge_mixed(Ctx& c, const double* frc, bool dipole) {
