@@ -266,7 +266,7 @@ def gpu_arm(args):
     s, prm, desc = make_workload(args.config)
     precision = MDG_MIXED if args.precision == "mixed" else MDG_FP64
     prm.precision = precision
-    dev = torch.device("cuda:0")
+    dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -388,7 +388,7 @@ def replicas_arm(args):
     systems = configs.replica_slabs(n=n)
     t_build = time.perf_counter() - t0
     precision = MDG_MIXED if args.precision == "mixed" else MDG_FP64
-    dev = torch.device("cuda:0")
+    dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     ctxs = []
@@ -542,10 +542,20 @@ def nve_drift(ctx, s, nsteps, every=100):
             "unit": "htot in the reference's energy unit (kJ/mol)"}
 
 
+def _barrier():
+    """All ranks of a multi-GPU replica run meet here (no-op on one GPU)."""
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
 def time_resident(ctx, K, stream, flush, torch):
-    """K resident steps, each bracketed by CUDA events on the library stream, L2 flushed between."""
+    """K resident steps, each bracketed by CUDA events on the library stream, L2 flushed between;
+    under torchrun the ranks start and end the timed region together (barriers)."""
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     torch.cuda.synchronize()
+    _barrier()
     with torch.cuda.stream(stream):
         for k in range(K):
             flush.zero_()
@@ -553,7 +563,39 @@ def time_resident(ctx, K, stream, flush, torch):
             ctx.run_async(1)
             ev[k][1].record(stream)
     stream.synchronize()
+    torch.cuda.synchronize()
+    _barrier()
     return [a.elapsed_time(b) for a, b in ev]
+
+
+def aggregate_ranks(out, world):
+    """Replicas only: every rank ran the same system on its own GPU with no exchange.  The job's
+    value is world x the per-replica value at the slowest rank's step time (max over ranks)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(out["ms_per_step"])], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    per = out["value"] * out["ms_per_step"] / ms  # the per-replica value at the slowest step time
+    out = dict(out)
+    if isinstance(out.get("e2e"), dict) and "value" in out["e2e"]:
+        e = torch.tensor([float(out["e2e"]["value"])], dtype=torch.float64)
+        if dist.get_backend() == "nccl":
+            e = e.cuda()
+        dist.all_reduce(e, op=dist.ReduceOp.MIN)  # the slowest rank's drop-in calls
+        out["e2e"] = dict(out["e2e"], value=float(e.item()) * world)
+    if "gpu_launches" in out:
+        out["gpu_launches"] = int(out["gpu_launches"]) * world
+    out["replica_value"] = per
+    out["value"] = per * world
+    out["ms_per_step"] = ms
+    out["n_gpus"] = world
+    out["scaling"] = "weak"
+    out["config"] = dict(out["config"], parallelism=f"replicas x{world} (independent systems, no collective)")
+    return out
 
 
 def fp64_compare(lib, s_start, prm, args, stream, flush, torch):
@@ -760,10 +802,18 @@ def main():
             return
         print(json.dumps(reference_arm(args)))
         return
-    if args.gpus > 1 or int(os.environ.get("WORLD_SIZE", "1")) > 1:
-        # replicas only: every rank runs its own independent system; rank 0 reports its own
-        pass
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        # replicas only: every rank runs its own independent system on its own GPU
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend="nccl")
+        args.cpu_baseline = False  # the CPU baseline is rank 0's at one GPU only
     out = replicas_arm(args) if args.config == "replicas64" else gpu_arm(args)
+    if world > 1:
+        out = aggregate_ranks(out, world)
     if rank == 0:
         print(json.dumps(out))
 

@@ -1,0 +1,50 @@
+"""bench.py's multi-GPU replica aggregation (replicas only: independent systems, no exchange),
+exercised with two gloo ranks on the CPU."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, q):
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+
+    # rank 1 is the slower one: 0.2 ms per step against 0.1
+    ms = 0.1 * (rank + 1)
+    out = {"value": 86400e-6 / (ms * 1e-3), "ms_per_step": ms, "n_gpus": 1, "config": {"workload": "w"},
+           "e2e": {"value": 100.0 * (rank + 1), "unit": "ns/day"}, "gpu_launches": 15}
+    q.put((rank, bench.aggregate_ranks(out, world)))
+    dist.destroy_process_group()
+
+
+def test_aggregate_two_ranks():
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+    for r in (0, 1):
+        o = res[r]
+        assert o["n_gpus"] == 2 and o["scaling"] == "weak"
+        assert o["ms_per_step"] == pytest.approx(0.2)               # the slowest rank's step
+        assert o["value"] == pytest.approx(2 * 86400e-6 / 0.2e-3)   # two replicas at that pace
+        assert o["e2e"]["value"] == pytest.approx(2 * 100.0)        # the slowest rank's calls, x2
+        assert o["gpu_launches"] == 30
