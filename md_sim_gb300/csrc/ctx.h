@@ -265,7 +265,7 @@ void pack_setup(Ctx& c);
 void pack_mixed(Ctx& c, bool force_rebuild, bool reset_status = false, bool defer_close = false);
 void pack_close_launch(Ctx& c);
 void pairs_mixed(Ctx& c, bool merge);  // head-head pairs into F (then merged into the FP64 forces)
-void walls_mixed(Ctx& c);              // head-wall pairs into F
+void walls_mixed(Ctx& c, bool concurrent = false);  // head-wall pairs into F (concurrent: beside the other branches)
 // F (+ frc, + the slab dipole term) into the FP64 forces, F cleared
 void merge_mixed(Ctx& c, const double* frc, bool dipole);
 // recip.cu

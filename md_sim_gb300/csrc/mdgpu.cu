@@ -269,7 +269,7 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
             MDG_CUDA(cudaEventRecord(c.ev_list, s0));
             MDG_CUDA(cudaStreamWaitEvent(c.side2, c.ev_list, 0));
             c.stream = c.side2;
-            walls_mixed(c);
+            walls_mixed(c, true);
             c.stream = s0;
             MDG_CUDA(cudaEventRecord(c.ev_join2, c.side2));
             PHASE(pairs_mixed(c, false), "pairs");
