@@ -446,8 +446,8 @@ int mdg_selftest_umma(int n, int k, const float* a, const float* b, float* d);
 /* ---------------------------------------------------------------------------------------------
  * Allocation-free reciprocal sum.  This entry point has no counterpart in the reference: it is
  * offered to callers that must not allocate device memory while they run (a host that sized its
- * device memory once at start-up, a framework whose caching allocator owns the device memory, or
- * work queued into a CUDA stream capture).  It computes the reciprocal-space Ewald forces and energy
+ * device memory once at start-up and may not grow it, or a framework whose caching allocator owns
+ * all of the device memory).  It computes the reciprocal-space Ewald forces and energy
  * of force_fouri (src/forcem.f90:827-937, no static walls, no slab term) for n charges, with the
  * same kernels and results as the reciprocal phase of mdg_force_get.
  *

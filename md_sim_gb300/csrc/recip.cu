@@ -361,7 +361,7 @@ void recip_fp64(Ctx& c) {
 // Some callers cannot allocate device memory while they run: a host that has sized its device
 // memory once at start-up and forbids later driver allocations, a framework whose caching
 // allocator owns all device memory (a cudaMalloc behind its back fragments the pool and
-// synchronises the device), or code that queues work into a CUDA stream capture.  For them the
+// synchronises the device).  For them the
 // structure-factor sum runs here with all of its scratch in one static device array that the
 // library carries (every GPU that loads the library holds it until the process exits).  The caller
 // passes device arrays in and out; nothing is allocated by this path.

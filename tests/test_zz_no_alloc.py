@@ -2,7 +2,7 @@
 
 mdg_recip_forces_noalloc exists for callers that must not allocate device memory while they run
 (a host that sized its device memory once at start-up, a framework whose caching allocator owns
-the device memory, work queued into a stream capture).  It keeps its scratch in a static device
+all of the device memory).  It keeps its scratch in a static device
 array, so this test checks that two calls in a row, sharing that array, both reproduce the
 reciprocal forces and energy that mdg_force_get computes for the same charges, within the FP64
 tolerance of the other parity tests.  The system is a lattice of point ions whose real-space sum
