@@ -1,4 +1,7 @@
-"""Regenerates tests/golden/*.npz (run in the build container, where the reference tree exists).
+"""Regenerates tests/golden/*.npz from the reference's fixture directory src/sim.
+
+Usage: python tests/golden/make_golden.py <reference checkout>/src/sim
+(or set MDSIM_REF_SIM to that directory).
 
 y_n_case.npz: the reference's interfacial sample (src/sim/y.fld, y.top, y.inp and the evolved
 state y_n.cfg: 258 rigid waters, 54 surface OH bound to a 3189-site rutile slab, angles and
@@ -16,20 +19,20 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-REF = "/root/reference/src/sim"
-
-
 def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MDSIM_REF_SIM")
+    if not ref or not os.path.isdir(ref):
+        raise SystemExit("usage: make_golden.py <reference>/src/sim (or MDSIM_REF_SIM=<dir>)")
     import build as oracle_build
     from md_sim_gb300 import abi
     from md_sim_gb300 import system as S
 
-    inp = S.parse_inp(open(os.path.join(REF, "y.inp")).read())
-    fld_t = open(os.path.join(REF, "y.fld")).read()
-    top_t = open(os.path.join(REF, "y.top")).read()
+    inp = S.parse_inp(open(os.path.join(ref, "y.inp")).read())
+    fld_t = open(os.path.join(ref, "y.fld")).read()
+    top_t = open(os.path.join(ref, "y.top")).read()
     fld = S.parse_fld(fld_t)
     top = S.parse_top(top_t, fld)
-    s = S.parse_cfg(open(os.path.join(REF, "y_n.cfg")).read(), fld, top, inp.dt)
+    s = S.parse_cfg(open(os.path.join(ref, "y_n.cfg")).read(), fld, top, inp.dt)
     s.rsx_after_predict()
     s.shake_init()
     oracle_build.build()
