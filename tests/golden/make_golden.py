@@ -19,6 +19,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MDSIM_REF_SIM")
     if not ref or not os.path.isdir(ref):
