@@ -161,6 +161,12 @@ int mdg_nnlist_make(mdg_ctx* ctx, const double* x0, const double* y0, const doub
 int mdg_get_lists(mdg_ctx* ctx, int64_t* li, int64_t* lj, int64_t cap, int64_t* wi, int64_t* wj,
                   int64_t wcap, int64_t* ipack, int64_t* wpack);
 
+/* The context's k set (force_fouri_init's selection, src/forcem.f90:743-776): kl, km, kn of each
+ * valid k vector in the reference's order and its Ak, for the first min(cap, nk) entries (any
+ * pointer may be NULL).  Returns nk, or a negative error code.  Mirrors the oracle's table of the
+ * same name, so that tests can compare the two k sets. */
+int64_t mdg_kvectors(mdg_ctx* ctx, int32_t* kl, int32_t* km, int32_t* kn, double* ak, int64_t cap);
+
 /* Replaces force_get (src/forcem.f90:93-129) with force_real, force_fouri, force_intra and the
  * serial force_sum (src/forcem_3d.f90:1031-1058), including the rebuild trigger
  * (src/forcem.f90:245-250).

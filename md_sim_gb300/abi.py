@@ -188,6 +188,9 @@ class Lib:
         g("nnlist_make", C.c_int, [C.c_void_p] + [DP] * 6 + [I64P, I64P])
         g("get_lists", C.c_int, [C.c_void_p, I64P, I64P, C.c_int64, I64P, I64P, C.c_int64, I64P, I64P])
         g("force_get", C.c_int, [C.c_void_p] + [DP] * 21 + [C.POINTER(Energies)])
+        if self.has("kvectors"):
+            I32P = C.POINTER(C.c_int32)
+            g("kvectors", C.c_int64, [C.c_void_p, I32P, I32P, I32P, DP, C.c_int64])
         g("shake", C.c_int, [C.c_void_p] + [DP] * 10 + [C.POINTER(C.c_double), C.POINTER(C.c_int32)])
         if self.has("pin_host"):
             g("pin_host", C.c_int, [C.c_void_p, C.c_int64])
@@ -309,6 +312,16 @@ class Context:
         self._check(self.lib.get_lists(self.h, _p(li, C.c_int64), _p(lj, C.c_int64), n,
                                        _p(wi, C.c_int64), _p(wj, C.c_int64), nw, C.byref(ip), C.byref(wp)))
         return (li[:n], lj[:n]), (wi[:nw], wj[:nw])
+
+    def kvectors(self):
+        """The context's k set: (kl, km, kn) int32 arrays in the reference's order and Ak."""
+        n = int(self.lib.kvectors(self.h, None, None, None, None, 0))
+        if n < 0:
+            self._check(n)
+        kl, km, kn = (np.zeros(max(n, 1), np.int32) for _ in range(3))
+        ak = np.zeros(max(n, 1))
+        self.lib.kvectors(self.h, _p(kl, C.c_int32), _p(km, C.c_int32), _p(kn, C.c_int32), _dp(ak), n)
+        return kl[:n], km[:n], kn[:n], ak[:n]
 
     def force_get(self, s: Optional[System] = None, want_sites: bool = True) -> Dict[str, object]:
         """One force evaluation; updates s.rsx[0:3] as force_sum does."""

@@ -664,6 +664,27 @@ int mdg_nnlist_make(mdg_ctx* cp, const double* x0, const double* y0, const doubl
     return mdg_get_lists(cp, nullptr, nullptr, 0, nullptr, nullptr, 0, ipack, wpack);
 }
 
+// k set of the context (src/forcem.f90:743-776): kl, km, kn per valid k in the reference's order and
+// Ak; returns the number of k vectors, or a negative error code.
+int64_t mdg_kvectors(mdg_ctx* cp, int32_t* kl, int32_t* km, int32_t* kn, double* ak, int64_t cap) {
+    if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");
+    Ctx& c = *cp;
+    cudaSetDevice(c.device);
+    const KSet& ks = c.ks;
+    const int64_t n = std::min<int64_t>(ks.nk, std::max<int64_t>(cap, 0));
+    if (n > 0 && (kl || km || kn)) {
+        std::vector<int3> kv((size_t)n);
+        MDG_CUDA(cudaMemcpy(kv.data(), ks.kvec, sizeof(int3) * n, cudaMemcpyDeviceToHost));
+        for (int64_t k = 0; k < n; ++k) {
+            if (kl) kl[k] = kv[k].x;
+            if (km) km[k] = kv[k].y;
+            if (kn) kn[k] = kv[k].z;
+        }
+    }
+    if (n > 0 && ak) MDG_CUDA(cudaMemcpy(ak, ks.ak, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return ks.nk;
+}
+
 int mdg_get_lists(mdg_ctx* cp, int64_t* li, int64_t* lj, int64_t cap, int64_t* wi, int64_t* wj, int64_t wcap,
                   int64_t* ipack, int64_t* wpack) {
     if (!cp) return set_err(nullptr, MDG_E_ARG, "null context");

@@ -64,7 +64,9 @@ def _check_forces(og, orf):
     for key in ("elj", "eqq"):
         d = np.abs(og[key] - orf[key]).max()
         assert d <= ENERGY_RTOL * scale, f"{key} diff {d:.3e} (scale {scale:.3e})"
-    for key in ("uewa", "urf", "ulr", "uconf", "uavex", "ewqLL", "ewqWW", "ewqWL"):
+    # uself includes the rigid-molecule and constraint exclusions with the transposed constraint
+    # read of src/forcem.f90:812-813 (Q7)
+    for key in ("uewa", "urf", "ulr", "uself", "uconf", "uavex", "ewqLL", "ewqWW", "ewqWL"):
         d = abs(og[key] - orf[key])
         assert d <= ENERGY_RTOL * scale, f"{key}: {og[key]!r} vs {orf[key]!r}"
     fs = np.abs(orf["fws"]).max() + 1.0
