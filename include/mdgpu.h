@@ -255,6 +255,32 @@ int mdg_run(mdg_ctx* ctx, int64_t nsteps, mdg_report* rep);
 int mdg_run_async(mdg_ctx* ctx, int64_t nsteps);
 int mdg_check(mdg_ctx* ctx, mdg_report* rep);
 
+/* ---------------------------------------------------------------------------------------------
+ * Host integrator for drop-in callers.  The reference keeps move_predict / move_correct
+ * (src/move.f90:48-383) in Fortran around its force call; a caller that replaces only force_get
+ * (and move_shake) with this library keeps them too.  These calls are that integrator on host
+ * arrays for callers written in C or C++: one host thread, no device memory, the reference's
+ * arithmetic order.  A drop-in step is
+ *     mdg_host_predict -> mdg_force_get (x0.., cx[0].., rsx..) -> mdg_host_correct
+ *     (-> mdg_shake when there are surface atoms)
+ * and reproduces the resident step of mdg_run to rounding.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct mdg_host_gear mdg_host_gear;
+/* sys: the description given to mdg_create (counts and masses are copied); body: the rigid water. */
+int mdg_host_gear_create(const mdg_sysdesc* sys, const mdg_rigid* body, mdg_host_gear** out);
+void mdg_host_gear_destroy(mdg_host_gear* g);
+/* move_predict (src/move.f90:48-217) on st in place: flexible atoms nriga+1..nliqa, centres,
+ * quaternions (normalised), body angular velocities, rotation matrices (kept in g), water site
+ * positions and H offsets rsx(ix+2:ix+3), the thermostat predictor; kinetic energies, htot. */
+int mdg_host_predict(mdg_host_gear* g, mdg_state* st);
+/* move_correct (src/move.f90:220-383) with the outputs of the mdg_force_get call on the predicted
+ * positions: ft* (nmove - nriga), fc* and t* (nrig), and that call's uconf. */
+int mdg_host_correct(mdg_host_gear* g, mdg_state* st, const double* ftx, const double* fty, const double* ftz,
+                     const double* fcx, const double* fcy, const double* fcz, const double* tx, const double* ty,
+                     const double* tz, double uconf);
+/* kp, kw, ke, htot (last predict), tempnow, uconf (last correct); the other fields are untouched. */
+int mdg_host_report(const mdg_host_gear* g, mdg_report* rep);
+
 /* Kernel launches of one resident-mode step (counted in the captured step graph; 0 before the
  * first mdg_run / mdg_run_async). */
 int64_t mdg_kernels_per_step(const mdg_ctx* ctx);

@@ -234,6 +234,12 @@ class Lib:
             g("checkpoint_load", C.c_int, [C.c_void_p, C.c_char_p])
         if self.has("widom"):
             g("widom", C.c_int, [C.c_void_p, C.POINTER(WidomParams), DP, DP, I64P, I64P])
+        if self.has("host_gear_create"):
+            g("host_gear_create", C.c_int, [C.POINTER(SysDesc), C.POINTER(Rigid), C.POINTER(C.c_void_p)])
+            g("host_gear_destroy", None, [C.c_void_p])
+            g("host_predict", C.c_int, [C.c_void_p, C.POINTER(State)])
+            g("host_correct", C.c_int, [C.c_void_p, C.POINTER(State)] + [DP] * 9 + [C.c_double])
+            g("host_report", C.c_int, [C.c_void_p, C.POINTER(Report)])
         if self.has("run"):
             g("set_state", C.c_int, [C.c_void_p, C.POINTER(Rigid), C.POINTER(State)])
             g("get_state", C.c_int, [C.c_void_p, C.POINTER(State)])
@@ -372,9 +378,17 @@ class Context:
 class _StateArrays:
     """Contiguous copies of a System's integrator state, bound into an mdg_state struct."""
 
-    def __init__(self, s: System):
+    def __init__(self, s: System, alloc=None):
+        """alloc(n) -> an empty float64 array of n elements (e.g. pinned host memory); numpy's
+        allocator by default."""
         nl, nr = s.nliqa, max(s.nrig, 1)
-        c = np.ascontiguousarray
+        if alloc is None:
+            c = np.ascontiguousarray
+        else:
+            def c(a):
+                out = alloc(len(a))
+                out[:] = a
+                return out
         self.x = [c(s.x0), c(s.y0), c(s.z0)]
         self.xd = [[c(s.xd[k, d]) for d in range(3)] for k in range(4)]
         self.c = [[c(s.c[k, d]) if s.nrig else np.zeros(nr) for d in range(3)] for k in range(5)]
@@ -445,6 +459,87 @@ def _ctx_run(self, nsteps: int) -> Dict[str, float]:
     rep = Report()
     self._check(self.lib.run(self.h, int(nsteps), C.byref(rep)))
     return {f: getattr(rep, f) for f, _ in Report._fields_}
+
+
+class HostGear:
+    """The drop-in MD step of a caller that keeps the integrator on the host (mdg_host_*):
+    predict on the host arrays, one force call of `ctx` (the GPU library or the oracle) on them,
+    correct, and SHAKE through `ctx` when the system has surface atoms (src/main.f90:58-68).
+    The state lives in contiguous copies of the System's arrays until write_back()."""
+
+    def __init__(self, lib: Lib, s: System, alloc=None):
+        """alloc(n): allocator of the host arrays (state, forces), e.g. pinned memory."""
+        self.lib, self.sys = lib, s
+        self._desc, self._keep = make_sysdesc(s)
+        self._rigid = rigid_of(s)
+        alloc = alloc or (lambda n: np.zeros(n))
+        h = C.c_void_p()
+        rc = lib.host_gear_create(C.byref(self._desc), C.byref(self._rigid), C.byref(h))
+        if rc != MDG_OK:
+            raise MdgError(rc, "mdg_host_gear_create failed")
+        self.h = h
+        self.arr = _StateArrays(s, alloc)
+        nflex, nrig = max(s.nmove - s.nriga, 1), max(s.nrig, 1)
+
+        def zeros(n):
+            a = alloc(n)
+            a[:] = 0.0
+            return a
+
+        self.ft = [zeros(nflex) for _ in range(3)]
+        self.fc = [zeros(nrig) for _ in range(3)]
+        self.tq = [zeros(nrig) for _ in range(3)]
+        self.elj, self.eqq = zeros(s.nijt), zeros(s.nijt)
+        self.e = Energies()
+        self.e.elj, self.e.eqq = _dp(self.elj), _dp(self.eqq)
+        self.shake = s.nmove > s.nliqa
+        self.sweeps, self.tk = C.c_int32(), C.c_double()
+
+    def predict(self):
+        rc = self.lib.host_predict(self.h, C.byref(self.arr.st))
+        if rc != MDG_OK:
+            raise MdgError(rc, "mdg_host_predict failed")
+
+    def correct(self, uconf: float):
+        rc = self.lib.host_correct(self.h, C.byref(self.arr.st), *[_dp(a) for a in self.ft + self.fc + self.tq],
+                                   float(uconf))
+        if rc != MDG_OK:
+            raise MdgError(rc, "mdg_host_correct failed")
+
+    def step(self, ctx: "Context", nsteps: int = 1):
+        a = self.arr
+        cx0 = [_dp(x) for x in a.c[0]]
+        for _ in range(nsteps):
+            self.predict()
+            ctx._check(ctx.lib.force_get(ctx.h, *[_dp(x) for x in a.x], *cx0, *[_dp(x) for x in a.rs],
+                                         *[_dp(x) for x in self.ft + self.fc + self.tq], None, None, None,
+                                         C.byref(self.e)))
+            self.correct(self.e.uconf)
+            if self.shake:
+                ctx._check(ctx.lib.shake(ctx.h, *[_dp(x) for x in a.x], *[_dp(x) for x in a.old],
+                                         *[_dp(x) for x in self.ft], None, C.byref(self.tk), C.byref(self.sweeps)))
+
+    def report(self) -> Dict[str, float]:
+        rep = Report()
+        self.lib.host_report(self.h, C.byref(rep))
+        return {"kp": rep.kp, "kw": rep.kw, "ke": rep.ke, "htot": rep.htot, "tempnow": rep.tempnow,
+                "uconf": rep.uconf}
+
+    def write_back(self, s: Optional[System] = None) -> System:
+        s = s or self.sys
+        self.arr.write_back(s)
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.host_gear_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 Context.set_state = _ctx_set_state

@@ -18,7 +18,9 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxe
 # SHAKE's FP64 update and convergence test, and the bin indices of the measurement histograms,
 # follow the reference operation by operation; no multiply-add contraction there, so that sweep
 # counts and histogram bins match the reference's rounding
-PER_FILE = {"shake.cu": ["-fmad=false"], "measure.cu": ["-fmad=false"]}
+PER_FILE = {"shake.cu": ["-fmad=false"], "measure.cu": ["-fmad=false"],
+            # the host integrator follows the reference's arithmetic order, without host FMA fusion
+            "hostgear.cu": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def _nvcc():

@@ -1,0 +1,293 @@
+// hostgear.cu - the reference's Gear predictor-corrector on host arrays, for drop-in callers.
+//
+// In the reference, move_predict (src/move.f90:48-217) and move_correct (src/move.f90:220-383)
+// stay in Fortran around the force call: a drop-in caller of mdg_force_get keeps them on the host
+// and the library only replaces force_get / nnlist_make / move_shake.  This file is that host
+// integrator for callers written in C or C++ (and the stand-in for the Fortran one when the
+// end-to-end cost of a drop-in MD step is measured): rigid waters (centre, quaternion and body
+// angular velocity, 5-value Gear with the reference's coefficients, Q11) and flexible atoms
+// nriga+1..nliqa, with the Nose-type thermostat of src/move.f90:168-217,356-375.  Surface atoms
+// (nliqa+1..nmove) move in mdg_shake, as in the reference (src/move.f90:376).
+//
+// One host thread, the reference's loops over the molecules; no device memory.  The arithmetic is
+// the reference's operation by operation (this file is compiled without multiply-add
+// contraction), so a drop-in loop reproduces the library's resident steps to rounding.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <new>
+#include <vector>
+
+#include "../../include/mdgpu.h"
+
+struct mdg_host_gear {
+    int64_t nrig = 0, nriga = 0, nliqa = 0;
+    std::vector<double> mi, mii;  // masses and inverse masses of the flexible atoms nriga..nliqa-1
+    mdg_rigid body{};
+    std::vector<double> A;        // rotation matrices, [9][nrig] (a11, a12, ..., a33 of src/config.f90)
+    double kp = 0, kw = 0, ke = 0, htot = 0, sft = 0, sfr = 0, uconf = 0;
+};
+
+namespace {
+
+// single-precision literals of the reference (Q1, src/move.f90:224-225)
+inline double F(float x) { return (double)x; }
+const double kG01 = F(0.348611111f), kG21 = F(0.916666667f), kG31 = F(0.333333333f), kG41 = F(0.041666667f);
+const double kG02 = F(0.158300000f), kG12 = F(0.757000000f), kG42 = F(0.083333333f);
+const double kR = F(8.31441f);  // PH_R, src/global.f90:21
+
+// 5-value Gear predictor of one coordinate (src/move.f90:56-66)
+inline void predict4(double& a0, double& a1, double& a2, double& a3, double a4) {
+    a0 = a0 + a1 + a2 + a3 + a4;
+    a1 = a1 + 2 * a2 + 3 * a3 + 4 * a4;
+    a2 = a2 + 3 * a3 + 6 * a4;
+    a3 = a3 + 4 * a4;
+}
+
+inline void correct5(double& a0, double& a1, double& a2, double& a3, double& a4, double c, double g0, double g1,
+                     double g2, double g3, double g4) {
+    a0 = a0 + g0 * c;
+    a1 = a1 + g1 * c;
+    a2 = a2 + g2 * c;
+    a3 = a3 + g3 * c;
+    a4 = a4 + g4 * c;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdg_host_gear_create(const mdg_sysdesc* s, const mdg_rigid* body, mdg_host_gear** out) {
+    if (!s || !body || !out) return MDG_E_ARG;
+    if (s->nrig < 0 || s->nriga != 3 * s->nrig || s->nliqa < s->nriga || s->nmove < s->nliqa || !s->mi || !s->mii)
+        return MDG_E_ARG;
+    mdg_host_gear* g = new (std::nothrow) mdg_host_gear();
+    if (!g) return MDG_E_ARG;
+    g->nrig = s->nrig;
+    g->nriga = s->nriga;
+    g->nliqa = s->nliqa;
+    g->mi.assign(s->mi + s->nriga, s->mi + s->nliqa);
+    g->mii.assign(s->mii + s->nriga, s->mii + s->nliqa);
+    g->body = *body;
+    g->A.assign(9 * (size_t)std::max<int64_t>(s->nrig, 1), 0.0);
+    *out = g;
+    return MDG_OK;
+}
+
+void mdg_host_gear_destroy(mdg_host_gear* g) { delete g; }
+
+// move_predict (src/move.f90:48-217) on the caller's state: predicted flexible atoms, centres,
+// angular velocities and quaternions (normalised), rotation matrices, site positions and the
+// offsets rsx(ix+2:ix+3) of the water H sites (src/move.f90:148-162; rsx(ix+1) is left alone, Q3),
+// the thermostat predictor, kp / kw / ke / htot and the thermostat forces sft / sfr.  htot uses
+// the uconf of the previous mdg_host_correct (0 before the first).
+int mdg_host_predict(mdg_host_gear* g, mdg_state* st) {
+    if (!g || !st) return MDG_E_ARG;
+    const int64_t nrig = g->nrig, n0 = g->nriga, n1 = g->nliqa;
+    const mdg_rigid& b = g->body;
+    double kp = 0.0;
+    for (int64_t i = n0; i < n1; ++i) {
+        predict4(st->x0[i], st->xd[0][i], st->xd[1][i], st->xd[2][i], st->xd[3][i]);
+        predict4(st->y0[i], st->yd[0][i], st->yd[1][i], st->yd[2][i], st->yd[3][i]);
+        predict4(st->z0[i], st->zd[0][i], st->zd[1][i], st->zd[2][i], st->zd[3][i]);
+    }
+    for (int64_t i = n0; i < n1; ++i)
+        kp += g->mi[i - n0] * (st->xd[0][i] * st->xd[0][i] + st->yd[0][i] * st->yd[0][i] + st->zd[0][i] * st->zd[0][i]);
+    // one loop per quantity, in the reference's order (src/move.f90:72-136): each streams a few
+    // arrays, so a host core's prefetchers keep up; every sum runs in molecule order
+    double sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
+    double* A = g->A.data();
+    {
+        double* const* c3[3] = {st->cx, st->cy, st->cz};
+        for (int d = 0; d < 3; ++d) {
+            double* const* a = c3[d];
+            for (int64_t i = 0; i < nrig; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
+        }
+        for (int d = 0; d < 3; ++d)
+            for (int64_t i = 0; i < nrig; ++i) sc[d] += c3[d][1][i] * c3[d][1][i];
+    }
+    {
+        double* const* w3[3] = {st->wx, st->wy, st->wz};
+        for (int d = 0; d < 3; ++d) {
+            double* const* a = w3[d];
+            for (int64_t i = 0; i < nrig; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
+        }
+        for (int d = 0; d < 3; ++d)
+            for (int64_t i = 0; i < nrig; ++i) sw[d] += w3[d][0][i] * w3[d][0][i];
+    }
+    for (int c = 0; c < 4; ++c) {
+        double* const* a = st->q[c];
+        for (int64_t i = 0; i < nrig; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
+    }
+    {
+        double *Q1 = st->q[0][0], *Q2 = st->q[1][0], *Q3 = st->q[2][0], *Q4 = st->q[3][0];
+        double* a[9];
+        for (int k = 0; k < 9; ++k) a[k] = A + (size_t)k * nrig;
+        for (int64_t i = 0; i < nrig; ++i) {
+            double q1 = Q1[i], q2 = Q2[i], q3 = Q3[i], q4 = Q4[i];
+            const double cr = 1.0 / std::sqrt(q1 * q1 + q2 * q2 + q3 * q3 + q4 * q4);
+            q1 = q1 * cr;
+            q2 = q2 * cr;
+            q3 = q3 * cr;
+            q4 = q4 * cr;
+            Q1[i] = q1;
+            Q2[i] = q2;
+            Q3[i] = q3;
+            Q4[i] = q4;
+            // rotation matrix (src/move.f90:128-136)
+            a[0][i] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
+            a[1][i] = 2.0 * (q3 * q4 - q1 * q2);
+            a[2][i] = 2.0 * (q2 * q3 + q1 * q4);
+            a[3][i] = -2.0 * (q1 * q2 + q3 * q4);
+            a[4][i] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4;
+            a[5][i] = 2.0 * (q2 * q4 - q1 * q3);
+            a[6][i] = 2.0 * (q2 * q3 - q1 * q4);
+            a[7][i] = -2.0 * (q1 * q3 + q4 * q2);
+            a[8][i] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
+        }
+        // sites from the centre and the body frame, H offsets from the O (src/move.f90:140-162)
+        const double *CX = st->cx[0], *CY = st->cy[0], *CZ = st->cz[0];
+        for (int64_t i = 0; i < nrig; ++i) {
+            const int64_t ix = 3 * i;
+            for (int j = 0; j < 3; ++j) {
+                st->x0[ix + j] = CX[i] + a[0][i] * b.xbody[j] + a[3][i] * b.ybody[j] + a[6][i] * b.zbody[j];
+                st->y0[ix + j] = CY[i] + a[1][i] * b.xbody[j] + a[4][i] * b.ybody[j] + a[7][i] * b.zbody[j];
+                st->z0[ix + j] = CZ[i] + a[2][i] * b.xbody[j] + a[5][i] * b.ybody[j] + a[8][i] * b.zbody[j];
+            }
+            for (int j = 1; j < 3; ++j) {
+                st->rsx[ix + j] = st->x0[ix + j] - st->x0[ix];
+                st->rsy[ix + j] = st->y0[ix + j] - st->y0[ix];
+                st->rsz[ix + j] = st->z0[ix + j] - st->z0[ix];
+            }
+        }
+    }
+    kp = kp + b.mw * (sc[0] + sc[1] + sc[2]);
+    const double kw = b.inxx * sw[0] + b.inyy * sw[1] + b.inzz * sw[2];
+    if (b.temper == -1.0) {
+        st->s[0] = st->s[1] = st->rs[0] = st->rs[1] = 0.0;
+    } else {
+        predict4(st->s[0], st->s[1], st->s[2], st->s[3], st->s[4]);
+        predict4(st->rs[0], st->rs[1], st->rs[2], st->rs[3], st->rs[4]);
+    }
+    g->kp = kp;
+    g->kw = kw;
+    g->ke = kp + kw;
+    // thermostat masses and forces (src/move.f90:173-217)
+    const int64_t nfree = g->nliqa - g->nriga;
+    const double ts = kR * b.temper / 1000.0;
+    const double qmass = (double)(float)(3 * (nfree + nrig)) * ts * F(2e3f) / 10.0;
+    const double rmass = (double)(float)(3 * nrig) * ts * F(1e3f) / 10.0;
+    g->htot = 0.5 * (g->ke + qmass * st->s[0] * st->s[0] + rmass * st->rs[0] * st->rs[0]) + g->uconf;
+    g->sft = (kp - (double)(float)(3 * (nfree + nrig) - 2) * ts) / qmass;
+    g->sfr = (kw - (double)(float)(3 * nrig + 1) * ts) / rmass;
+    return MDG_OK;
+}
+
+// move_correct (src/move.f90:220-383) with the outputs of mdg_force_get for the positions of the
+// preceding mdg_host_predict: ftx.. (nmove - nriga, flexible atoms first), fcx.. and tx.. (nrig).
+// uconf is the configurational energy of that force call (kept for the next htot).
+int mdg_host_correct(mdg_host_gear* g, mdg_state* st, const double* ftx, const double* fty, const double* ftz,
+                     const double* fcx, const double* fcy, const double* fcz, const double* tx, const double* ty,
+                     const double* tz, double uconf) {
+    if (!g || !st) return MDG_E_ARG;
+    const int64_t nrig = g->nrig, n0 = g->nriga, n1 = g->nliqa;
+    const mdg_rigid& b = g->body;
+    const double s0i = st->s[0], rs0i = st->rs[0];
+    if (n1 > n0 && (!ftx || !fty || !ftz)) return MDG_E_ARG;
+    if (nrig > 0 && (!fcx || !fcy || !fcz || !tx || !ty || !tz)) return MDG_E_ARG;
+    for (int64_t i = n0; i < n1; ++i) {
+        const double mii = g->mii[i - n0];
+        const double* f[3] = {ftx, fty, ftz};
+        double* x[3] = {st->x0, st->y0, st->z0};
+        double* const* xd[3] = {st->xd, st->yd, st->zd};
+        for (int d = 0; d < 3; ++d) {
+            const double c = 0.5 * f[d][i - n0] * mii - xd[d][0][i] * s0i - xd[d][1][i];
+            x[d][i] = x[d][i] + kG02 * c;
+            xd[d][0][i] = xd[d][0][i] + kG12 * c;
+            xd[d][1][i] = xd[d][1][i] + c;
+            xd[d][2][i] = xd[d][2][i] + 0.5 * c;
+            xd[d][3][i] = xd[d][3][i] + kG42 * c;
+        }
+    }
+    const double rc = 0.5 / b.mw;
+    const double inxxi = 1.0 / b.inxx, inyyi = 1.0 / b.inyy, inzzi = 1.0 / b.inzz;
+    // centre (src/move.f90:262-281)
+    {
+        const double* f3[3] = {fcx, fcy, fcz};
+        double* const* cm[3] = {st->cx, st->cy, st->cz};
+        for (int d = 0; d < 3; ++d) {
+            double* const* a = cm[d];
+            const double* f = f3[d];
+            for (int64_t i = 0; i < nrig; ++i) {
+                const double c = rc * f[i] - a[1][i] * s0i - a[2][i];
+                correct5(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i], c, kG02, kG12, 1.0, 0.5, kG42);
+            }
+        }
+    }
+    // quaternions from the angular velocity before its correction (src/move.f90:283-317)
+    for (int64_t i = 0; i < nrig; ++i) {
+        const double q1 = st->q[0][0][i], q2 = st->q[1][0][i], q3 = st->q[2][0][i], q4 = st->q[3][0][i];
+        const double wx = st->wx[0][i], wy = st->wy[0][i], wz = st->wz[0][i];
+        const double cq[4] = {0.5 * (-q3 * wx - q4 * wy + q2 * wz), 0.5 * (q4 * wx - q3 * wy - q1 * wz),
+                              0.5 * (q1 * wx + q2 * wy + q4 * wz), 0.5 * (-q2 * wx + q1 * wy - q3 * wz)};
+        for (int c = 0; c < 4; ++c) {
+            double* const* a = st->q[c];
+            const double co = cq[c] - a[1][i];
+            correct5(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i], co, kG01, 1.0, kG21, kG31, kG41);
+        }
+    }
+    // body angular velocity: Euler's equations with the lab torque rotated into the body frame
+    // (src/move.f90:319-354)
+    {
+        const double* a[9];
+        for (int k = 0; k < 9; ++k) a[k] = g->A.data() + (size_t)k * nrig;
+        for (int64_t i = 0; i < nrig; ++i) {
+            const double wx = st->wx[0][i], wy = st->wy[0][i], wz = st->wz[0][i];
+            const double t0 = tx[i], t1 = ty[i], t2 = tz[i];
+            double c1 = a[0][i] * t0 + a[1][i] * t1 + a[2][i] * t2;
+            c1 = ((c1 + wy * wz * (b.inyy - b.inzz)) * inxxi) - st->wx[1][i] - rs0i * wx;
+            double c2 = a[3][i] * t0 + a[4][i] * t1 + a[5][i] * t2;
+            c2 = ((c2 + wz * wx * (b.inzz - b.inxx)) * inyyi) - st->wy[1][i] - rs0i * wy;
+            double c3 = a[6][i] * t0 + a[7][i] * t1 + a[8][i] * t2;
+            c3 = ((c3 + wx * wy * (b.inxx - b.inyy)) * inzzi) - st->wz[1][i] - rs0i * wz;
+            correct5(st->wx[0][i], st->wx[1][i], st->wx[2][i], st->wx[3][i], st->wx[4][i], c1, kG01, 1.0, kG21, kG31,
+                     kG41);
+            correct5(st->wy[0][i], st->wy[1][i], st->wy[2][i], st->wy[3][i], st->wy[4][i], c2, kG01, 1.0, kG21, kG31,
+                     kG41);
+            correct5(st->wz[0][i], st->wz[1][i], st->wz[2][i], st->wz[3][i], st->wz[4][i], c3, kG01, 1.0, kG21, kG31,
+                     kG41);
+        }
+    }
+    if (b.temper != -1.0) {  // thermostat corrector (src/move.f90:356-375)
+        double c = g->sft - st->s[1];
+        st->s[0] = st->s[0] + kG01 * c;
+        st->s[1] = g->sft;
+        st->s[2] = st->s[2] + kG21 * c;
+        st->s[3] = st->s[3] + kG31 * c;
+        st->s[4] = st->s[4] + kG41 * c;
+        c = g->sfr - st->rs[1];
+        st->rs[0] = st->rs[0] + kG01 * c;
+        st->rs[1] = g->sfr;
+        st->rs[2] = st->rs[2] + kG21 * c;
+        st->rs[3] = st->rs[3] + kG31 * c;
+        st->rs[4] = st->rs[4] + kG41 * c;
+    }
+    g->uconf = uconf;
+    return MDG_OK;
+}
+
+// The scalars the reference prints after a step (src/main.f90:320-335): kp, kw, ke and htot of
+// the last mdg_host_predict, tempnow, and the uconf of the last mdg_host_correct.
+int mdg_host_report(const mdg_host_gear* g, mdg_report* rep) {
+    if (!g || !rep) return MDG_E_ARG;
+    rep->kp = g->kp;
+    rep->kw = g->kw;
+    rep->ke = g->ke;
+    rep->htot = g->htot;
+    const int64_t nfree = g->nliqa - g->nriga;
+    rep->tempnow = g->ke * 1000.0 / (3.0 * kR * (double)(float)(nfree + 2 * g->nrig));
+    rep->uconf = g->uconf;
+    return MDG_OK;
+}
+
+}  // extern "C"
