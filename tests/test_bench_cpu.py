@@ -25,7 +25,13 @@ def _rank(rank, world, port, q):
     ms = 0.1 * (rank + 1)
     out = {"value": 86400e-6 / (ms * 1e-3), "ms_per_step": ms, "n_gpus": 1, "config": {"workload": "w"},
            "e2e": {"value": 100.0 * (rank + 1), "unit": "ns/day"}, "gpu_launches": 15}
-    q.put((rank, bench.aggregate_ranks(out, world)))
+    single = bench.aggregate_ranks(out, world)
+    # replica batches: rank r holds the replicas r, r + world, ... of 5 (3 and 2 here), each at
+    # the rank's step time
+    nloc = len(bench.replica_partition(5, rank, world))
+    rep = {"value": nloc * 86400e-6 / (ms * 1e-3), "ms_per_step": ms, "n_gpus": 1, "config": {"workload": "r"},
+           "replicas_this_rank": nloc, "gpu_launches": 10}
+    q.put((rank, (single, bench.aggregate_ranks(rep, world))))
     dist.destroy_process_group()
 
 
@@ -42,9 +48,22 @@ def test_aggregate_two_ranks():
     for p in procs:
         p.join(timeout=60)
     for r in (0, 1):
-        o = res[r]
+        o, b = res[r]
         assert o["n_gpus"] == 2 and o["scaling"] == "weak"
         assert o["ms_per_step"] == pytest.approx(0.2)               # the slowest rank's step
         assert o["value"] == pytest.approx(2 * 86400e-6 / 0.2e-3)   # two replicas at that pace
         assert o["e2e"]["value"] == pytest.approx(2 * 100.0)        # the slowest rank's calls, x2
         assert o["gpu_launches"] == 30
+        assert b["replicas_total"] == 5
+        assert b["value"] == pytest.approx(5 * 86400e-6 / 0.2e-3)   # all five replicas at the slow pace
+        assert b["gpu_launches"] == 20
+
+
+def test_replica_partition_covers_each_replica_once():
+    import bench
+
+    for n, world in ((64, 1), (64, 2), (64, 3), (64, 8), (5, 8)):
+        parts = [bench.replica_partition(n, r, world) for r in range(world)]
+        flat = sorted(i for p in parts for i in p)
+        assert flat == list(range(n))
+        assert max(len(p) for p in parts) - min(len(p) for p in parts) <= 1
