@@ -513,10 +513,13 @@ def equilibrate(ctx, s: S.System, steps: int = 400, T: float = 300.0, every: int
 
 
 def ion_lattice(n_side: int = 6, spacing: float = 2.8, rcut: float = 2.0, alpha: float = 0.35,
-                kmax: int = 6, seed: int = 21, jitter: float = 0.2) -> Tuple[S.System, RunParams]:
+                kmax: int = 6, seed: int = 21, jitter: float = 0.2,
+                shuffle: bool = False) -> Tuple[S.System, RunParams]:
     """Rocksalt arrangement of +1/-1 point ions (two atmol types, no vdW) in a cubic periodic box,
     jittered; rcut below the closest approach so that the real-space sum is empty and the
-    forces of force_get are the reciprocal-space forces alone."""
+    forces of force_get are the reciprocal-space forces alone.  shuffle=True deals the charges to
+    the lattice sites at random (still neutral): the alternating crystal's reciprocal forces
+    nearly cancel, the shuffled one's are of the order of the single terms."""
     n = n_side ** 3
     if n % 2:
         raise ValueError("n_side must be even")
@@ -524,6 +527,8 @@ def ion_lattice(n_side: int = 6, spacing: float = 2.8, rcut: float = 2.0, alpha:
     g = np.stack(np.meshgrid(*[np.arange(n_side)] * 3, indexing="ij"), -1).reshape(-1, 3)
     par = g.sum(1) % 2
     rng = np.random.default_rng(seed)
+    if shuffle:
+        par = rng.permutation(par)
     pos = g * spacing + rng.uniform(-jitter, jitter, size=(n, 3)) - 0.5 * L
     cat = S.MolType("Na", "atmol", int((par == 0).sum()), ["Na"], [1], [22.99e-3], [1.0], ns=1)
     an = S.MolType("Cl", "atmol", int((par == 1).sum()), ["Cl"], [1], [35.45e-3], [-1.0], ns=1)
