@@ -148,6 +148,9 @@ struct TcPlan {
     int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, grid1x = 0, rtot = 0, tpc1 = 0, smem1 = 0, smem2 = 0;
     int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0, nlist2 = 0, mult1 = 2, nst2 = 2;
     int4* row2 = nullptr;    // pass-2 rows, sorted by their K-step range (nchunk2 x kRC, padded)
+    int* rorig2 = nullptr;   // pass-2 row -> row of the k set (-1: padding)
+    float* rowsc = nullptr;  // per row of the k set: max |C| max(1, |n|) of this evaluation
+    float* rsc2 = nullptr;   // the same in pass-2 order (written by the operand packing)
     int* nlen2 = nullptr;
     int4* chunk2 = nullptr;  // per pass-2 chunk: image byte offset, first K step, K steps
     int4* items2 = nullptr;  // per pass-2 CTA: atom tile, first chunk, end chunk, whole tile (1) or piece (0)

@@ -123,7 +123,7 @@ __device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t&
 template <int TPC>
 __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
     k_tc_sfac(View v, const uint4* __restrict__ atoms, int chunk, const int4* __restrict__ rows, TcDims d, int NM,
-              int KM, float* __restrict__ part, int rtot, uint32_t ncols) {
+              int KM, float* __restrict__ part, int rtot, uint32_t ncols, float* __restrict__ rowsc) {
     constexpr int kProd = P1<TPC>::kProd, kS = P1<TPC>::kS;
     extern __shared__ __align__(1024) unsigned char sm[];
     const P1Layout L = p1_layout(TPC, kS, d.NP, NM);
@@ -195,6 +195,7 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
         // ---------------- producers
         const int r = t;                                 // CTA row (tile = r / 128)
         const int row = row0 + r;
+        if (blockIdx.y == 0 && row < d.nrow) rowsc[row] = 0.f;  // k_tc_sreduce takes the maximum
         int li = kMaxNL - 1, mi = NM;                    // zero slots for padding rows
         if (row < d.nrow) {
             const int4 rw = rows[row];
@@ -357,7 +358,7 @@ __global__ void __launch_bounds__(32 * kRedG) k_tc_sreduce(View v, const float* 
                                                           const int* __restrict__ nlen,
                                                           const double* __restrict__ ak,
                                                           const double2* __restrict__ qw, double2* S, double2* C,
-                                                          float2* Cf, float* cmax) {
+                                                          float2* Cf, float* cmax, float* rowsc) {
     __shared__ float4 sh[kRedG][32];
     const int le = threadIdx.x & 31, g = threadIdx.x >> 5;
     const long total = (long)d.nrow * d.NN;
@@ -411,6 +412,7 @@ __global__ void __launch_bounds__(32 * kRedG) k_tc_sreduce(View v, const float* 
         Cf[k] = make_float2((float)cv.x, (float)cv.y);
         const float w = (float)max(1, abs(n));
         mx = fmaxf(fabsf((float)cv.x), fabsf((float)cv.y)) * w;
+        atomicMax(reinterpret_cast<unsigned int*>(&rowsc[row]), __float_as_uint(mx));
     }
     if (g == 0) {  // warp 0 holds the block's entries
         ew = warp_sum(ew);
@@ -425,7 +427,8 @@ __global__ void __launch_bounds__(32 * kRedG) k_tc_sreduce(View v, const float* 
 }
 
 // ---------------------------------------------------------------------------------------------
-// C(k) packed as the pass-2 B operand.  Pass 2 takes the rows sorted by the K steps their n range
+// C(k) packed as the pass-2 B operand, each row scaled by its own maximum (the epilogue
+// multiplies it back).  Pass 2 takes the rows sorted by the K steps their n range
 // covers (row2, nlen2), so that chunk c (rows kRC c .. kRC c + kRC - 1 of that order) multiplies
 // only the K steps ks_lo .. ks_lo + nks - 1 its rows use (chunk2[c] = image byte offset, ks_lo,
 // nks).  Columns col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part;
@@ -437,15 +440,19 @@ constexpr uint32_t kTile2 = kNC2 * 32;  // one N x 16 B tile (bytes)
 
 __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restrict__ rows,
                             const int* __restrict__ nlen, const int4* __restrict__ chunks, TcDims d,
-                            unsigned char* img, const float* cmax, double* frc, int zero_from, int nmove) {
+                            unsigned char* img, const float* __restrict__ rowsc, const int* __restrict__ rorig,
+                            float* __restrict__ rsc2, double* frc, int zero_from, int nmove) {
     if (blockIdx.y == 0)  // forces of the atoms whose pass-2 tiles are cut into pieces
         for (int i = zero_from + blockIdx.x * blockDim.x + threadIdx.x; i < nmove; i += gridDim.x * blockDim.x) {
             frc[i] = 0.0;
             frc[nmove + i] = 0.0;
             frc[2 * nmove + i] = 0.0;
         }
-    const float inv = cmax[0] > 0.f ? 1.0f / cmax[0] : 1.0f;
     const int c = blockIdx.y;
+    if (blockIdx.x == 0 && threadIdx.x < kRC) {  // the chunk's row scales, for the force epilogue
+        const int ro = rorig[c * kRC + threadIdx.x];
+        rsc2[c * kRC + threadIdx.x] = ro >= 0 ? rowsc[ro] : 0.f;
+    }
     const int4 ch = chunks[c];
     const int nks = ch.z;
     const int total = nks * kNC2 * 8;
@@ -462,6 +469,10 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
             const int4 rw = rows[row];
             const int n = ni - d.KN;
             if (n >= rw.z && n < rw.z + nl) {
+                // each row's C scaled by its own max |n C|: under one scale for all rows the
+                // large-k rows' C would fall below FP16's normal range
+                const float sr = rowsc[rorig[row]];
+                const float inv = sr > 0.f ? 1.0f / sr : 1.0f;
                 const float2 cv = Cf[rw.w + n - rw.z];
                 const float sc = (tt ? (float)n : 1.0f) * inv;
                 const float cr = cv.x * sc, ci = cv.y * sc;
@@ -493,7 +504,7 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
 constexpr int kT2 = 288;  // epilogue warps 0-7 (two per TMEM lane quarter, one per half chunk), issuer warp 8
 
 struct P2Layout {
-    uint32_t a_bytes, img, off_a, off_b, off_rows, off_red, total;
+    uint32_t a_bytes, img, off_a, off_b, off_rows, off_rsc, off_red, total;
 };
 
 __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
@@ -503,7 +514,8 @@ __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
     L.off_a = 1024;
     L.off_b = L.off_a + L.a_bytes;
     L.off_rows = L.off_b + nst * L.img;
-    L.off_red = L.off_rows + nrow_pad * 16;    // rows: (float l, float m, l | restart << 31, m)
+    L.off_rsc = L.off_rows + nrow_pad * 16;    // rows: (float l, float m, l | restart << 31, m)
+    L.off_red = L.off_rsc + nrow_pad * 4;      // row scales of this evaluation
     L.total = L.off_red + 3 * 128 * 4;         // second-half force partials of the 128 atoms
     return L;
 }
@@ -511,8 +523,8 @@ __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
 __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
                                                      const unsigned char* __restrict__ img,
                                                      const int4* __restrict__ rows, const int4* __restrict__ chunks,
-                                                     const int4* __restrict__ items, TcDims d, const float* cmax,
-                                                     double* __restrict__ frc) {
+                                                     const int4* __restrict__ items, TcDims d,
+                                                     const float* __restrict__ rsc_g, double* __restrict__ frc) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC, d.nst2);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -521,6 +533,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     uint64_t* afree = mdone + 2;                         // [2] accumulator drained (4 epilogue warps)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     float4* rlm = reinterpret_cast<float4*>(sm + L.off_rows);
+    float* rsc = reinterpret_cast<float*>(sm + L.off_rsc);
     int* err = &v.status[ST_TC_TIMEOUT];
     const int4 item = items[blockIdx.x];  // atom tile, chunks [c0, c0 + NC), whole tile or piece
     const int atom0 = item.x * 128;
@@ -542,6 +555,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             restart = pw.x != rw.x || pw.y + 1 != rw.y;
         }
         rlm[r] = make_float4((float)rw.x, (float)rw.y, __int_as_float(rw.x | (restart << 31)), __int_as_float(rw.y));
+        rsc[r] = rsc_g[r];
     }
     if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 256);
     // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part (warps 0-7, half of K each)
@@ -650,6 +664,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
 #pragma unroll
                 for (int rr = 0; rr < 16; ++rr) {
                     const float4 lm = rlm[(c0 + c) * kRC + hf * 16 + rr];
+                    const float scr = rsc[(c0 + c) * kRC + hf * 16 + rr];
                     const int lb = __float_as_int(lm.z);
                     if (rr == 0 || lb < 0) {
                         phase((uint32_t)(lb & 0x7fffffff) * rec.x + (uint32_t)__float_as_int(lm.w) * rec.y, ec, es);
@@ -660,10 +675,10 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                     }
                     const float v0 = __uint_as_float(raw[rr * 4 + 0]), v1 = __uint_as_float(raw[rr * 4 + 1]);
                     const float v2 = __uint_as_float(raw[rr * 4 + 2]), v3 = __uint_as_float(raw[rr * 4 + 3]);
-                    const float s0 = ec * v1 + es * v0;
+                    const float s0 = (ec * v1 + es * v0) * scr;
                     fx = fmaf(lm.x, s0, fx);
                     fy = fmaf(lm.y, s0, fy);
-                    fz += ec * v3 + es * v2;
+                    fz = fmaf(ec * v3 + es * v2, scr, fz);
                 }
             }
         }
@@ -680,7 +695,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             fx += red[ra];       // (a timed-out block leaves zeros and its status)
             fy += red[128 + ra];
             fz += red[256 + ra];
-            const double q = alive ? (double)__uint_as_float(rec.w) * (double)cmax[0] : 0.0;
+            const double q = alive ? (double)__uint_as_float(rec.w) : 0.0;
             const double gx = q * (double)d.px * (double)fx, gy = q * (double)d.py * (double)fy,
                          gz = q * (double)d.pz * (double)fz;
             if (item.w) {
@@ -828,7 +843,7 @@ int recip_tc_setup(Ctx& c) {
             return wa != wb ? wa > wb : klo[a] < klo[b];
         });
         std::vector<int4> row2(nrp, make_int4(0, 0, 0, 0)), chunk2(p.nchunk2);
-        std::vector<int> nlen2(nrp, 0);
+        std::vector<int> nlen2(nrp, 0), rorig2(nrp, -1);
         size_t off = 0;
         for (int cc = 0; cc < p.nchunk2; ++cc) {
             int lo = 1 << 30, hi = -1;
@@ -836,6 +851,7 @@ int recip_tc_setup(Ctx& c) {
                 const int r = order[k];
                 row2[k] = ks.h_row[r];
                 nlen2[k] = ks.h_nlen[r];
+                rorig2[k] = r;
                 lo = std::min(lo, klo[r]);
                 hi = std::max(hi, khi[r]);
             }
@@ -876,6 +892,9 @@ int recip_tc_setup(Ctx& c) {
             if (p.nitems2 > 0)
                 MDG_CUDA(cudaMemcpy(p.items2, items.data(), sizeof(int4) * p.nitems2, cudaMemcpyHostToDevice));
         }
+        p.rorig2 = (int*)dalloc(c, sizeof(int) * std::max(nrp, 1));
+        p.rsc2 = (float*)dalloc(c, sizeof(float) * std::max(nrp, 1));
+        p.rowsc = (float*)dalloc(c, sizeof(float) * std::max(nr, 1));
         p.row2 = (int4*)dalloc(c, sizeof(int4) * std::max(nrp, 1));
         p.nlen2 = (int*)dalloc(c, sizeof(int) * std::max(nrp, 1));
         p.chunk2 = (int4*)dalloc(c, sizeof(int4) * std::max(p.nchunk2, 1));
@@ -884,6 +903,8 @@ int recip_tc_setup(Ctx& c) {
             MDG_CUDA(cudaMemcpy(p.row2, row2.data(), sizeof(int4) * nrp, cudaMemcpyHostToDevice));
             MDG_CUDA(cudaMemcpy(p.nlen2, nlen2.data(), sizeof(int) * nrp, cudaMemcpyHostToDevice));
             MDG_CUDA(cudaMemcpy(p.chunk2, chunk2.data(), sizeof(int4) * p.nchunk2, cudaMemcpyHostToDevice));
+            MDG_CUDA(cudaMemcpy(p.rorig2, rorig2.data(), sizeof(int) * nrp, cudaMemcpyHostToDevice));
+            MDG_CUDA(cudaMemset(p.rsc2, 0, sizeof(float) * nrp));
         }
     }
     c.d_tc_atoms = (uint4*)dalloc(c, sizeof(uint4) * std::max(v.nmove, 1));
@@ -909,18 +930,19 @@ void recip_tc(Ctx& c) {
     // c.d_tc_atoms was filled, and c.d_tc_cmax cleared, by the packing kernel of this evaluation
     if (p.tpc1 == 4)
         k_tc_sfac<4><<<dim3(p.grid1x, p.nsplit1), P1<4>::kThreads, p.smem1, c.stream>>>(
-            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1);
+            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1, p.rowsc);
     else
         k_tc_sfac<2><<<dim3(p.grid1x, p.nsplit1), P1<2>::kThreads, p.smem1, c.stream>>>(
-            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1);
+            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1, p.rowsc);
     const long nred = (long)ks.nrow * p.NN;
     k_tc_sreduce<<<(int)((nred + 31) / 32), 32 * kRedG, 0, c.stream>>>(
-        v, c.d_tc_part, p.nsplit1, p.rtot, d, ks.row, ks.row_nlen, ks.ak, ks.qw, ks.s, ks.c, c.d_tc_cf, c.d_tc_cmax);
+        v, c.d_tc_part, p.nsplit1, p.rtot, d, ks.row, ks.row_nlen, ks.ak, ks.qw, ks.s, ks.c, c.d_tc_cf, c.d_tc_cmax,
+        p.rowsc);
     const int per_chunk = p.KS * kNC2 * 8;  // elements of the widest chunk image
     k_tc_prep_c<<<dim3((per_chunk + 255) / 256, p.nchunk2), 256, 0, c.stream>>>(
-        c.d_tc_cf, p.row2, p.nlen2, p.chunk2, d, c.d_tc_img, c.d_tc_cmax, c.d_frc, p.zero2, v.nmove);
+        c.d_tc_cf, p.row2, p.nlen2, p.chunk2, d, c.d_tc_img, p.rowsc, p.rorig2, p.rsc2, c.d_frc, p.zero2, v.nmove);
     k_tc_force<<<p.nitems2, kT2, p.smem2, c.stream>>>(v, c.d_tc_atoms, c.d_tc_img, p.row2, p.chunk2, p.items2, d,
-                                                      c.d_tc_cmax, c.d_frc);
+                                                      p.rsc2, c.d_frc);
 }
 
 int umma_selftest(int n, int k, const float* a, const float* b, float* dout, std::string& err) {
