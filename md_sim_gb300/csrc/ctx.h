@@ -147,6 +147,7 @@ struct TcPlan {
     int KN = 0, NN = 0, NP = 0, KS = 0, KM = 0, NM = 0;
     int ncols1 = 0, mtiles = 0, nchunk2 = 0, chunk1 = 0, nsplit1 = 0, grid1x = 0, rtot = 0, tpc1 = 0, smem1 = 0, smem2 = 0;
     int ntile2 = 0, nparts2 = 0, cper2 = 0, grid2 = 0, nlist2 = 0, mult1 = 2, nst2 = 2;
+    int G1 = 4;  // n-side pass 1: groups of 16 atoms per TMEM accumulation chain
     int4* row2 = nullptr;    // pass-2 rows, sorted by their K-step range (nchunk2 x kRC, padded)
     int* rorig2 = nullptr;   // pass-2 row -> row of the k set (-1: padding)
     float* rowsc = nullptr;  // per row of the k set: max |C| max(1, |n|) of this evaluation

@@ -1617,8 +1617,11 @@ int mdg_autotune(mdg_ctx* cp, int32_t reps, mdg_tuning* out) {
     int best_tpc = c.tcp.tpc1, best_mult = c.tcp.mult1;
     if (c.precision == MDG_MIXED && c.tcp.ready) {
         best = time_force(c, reps);
-        for (int tpc : {4, 2})
+        // the n-side form when it applies (its accumulation chains are short), its atom split tuned
+        const bool nside = c.tcp.tpc1 == 1;
+        for (int tpc : {1, 4, 2})
             for (int m : {1, 2, 4}) {
+                if ((tpc == 1) != nside) continue;
                 if (tc_plan_pass1(c, tpc, m)) continue;
                 const float t = time_force(c, reps);
                 if (t < best * kTuneGain) {
@@ -1636,7 +1639,7 @@ int mdg_autotune(mdg_ctx* cp, int32_t reps, mdg_tuning* out) {
     if (rc) return rc;
     if (out) {
         out->pair_blocks = best_pb;
-        out->tc_rows_per_cta = 128 * best_tpc;
+        out->tc_rows_per_cta = best_tpc == 1 ? 256 : 128 * best_tpc;
         out->tc_atom_splits = c.tcp.nsplit1;
         out->ms_before = t0;
         out->ms_after = t1;

@@ -347,6 +347,377 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// pass 1, n-side form (2 NN <= 128): the same structure factor with the roles of the operands
+// swapped, D[(re|im, n) lane, (l, m) row] over K = atoms:
+//   A (M = 128 lanes): e^{i n tz} in the 2x2 real block form (part 0: cos / sin, part 1: -sin /
+//     cos), lanes n (re) and NN + n (im), zero beyond 2 NN;
+//   B (N = 256 rows): the real (part 0) and imaginary (part 1) parts of q e^{i(l tx + m ty)}.
+// Every tcgen05.mma is M = 128, N = 256 (128 cycles at the dense rate), 6 per group of 16 atoms
+// (2 parts x hi*hi, hi*lo, lo*hi).  Roles:
+//   row warps (16, two threads per CTA row, 8 atoms each): the B entries from two tables by
+//     128-bit shared loads and packed f32x2 arithmetic, hi/lo split, stored in the UMMA layout;
+//     and the A operand e^{i n tz} of the group (one (n, atom pair) item per thread);
+//   table warps (2): per group, ahead of the row warps, the atom records and the tables
+//     e^{i m ty} (all m) and q e^{i l tx} (the CTA's l range), by __sincosf of exact fixed-point
+//     phases;
+//   issuer (1 thread): 6 MMAs per group, with slot and phase counters (no division in its loop:
+//     the issuer's instructions per MMA decide whether the tensor pipe runs at its rate).
+// Accumulation: the tensor core's FP32 accumulation loses magnitude in every step (measured on
+// this GPU: about 1.5e-8 of the running sum per accumulating MMA, always towards zero), so long
+// chains bias S(k).  The chain is cut every G groups: two TMEM accumulators alternate, and the
+// row warps add the finished one into FP32 registers (round to nearest, unbiased) while the next
+// chain runs, then write their sums as this CTA's partial [split][lane][row].
+// Every wait is bounded; a timeout anywhere sets a shared abort flag that ends all waits.
+// ---------------------------------------------------------------------------------------------
+constexpr int kRW = 16;                  // row warps
+constexpr int kTW = 2;                   // table warps
+constexpr int kT1b = (kRW + kTW + 1) * 32;
+constexpr int kS1b = 3;                  // stages (A and B of one group)
+constexpr uint32_t kBSt = 4 * 8192;      // B: [p][h] tiles of 256 x 16 halves
+constexpr uint32_t kASt = 4 * 4096;      // A: [p][h] tiles of 128 x 16 halves
+constexpr uint32_t kSt1b = kBSt + kASt;
+constexpr int kMaxNL2 = 32;              // l values per CTA (slot kMaxNL2 - 1 stays zero)
+constexpr uint32_t kTabRow = 144;        // table row: 8 atom pairs x float4 + 16 B (bank spread)
+
+struct P1bLayout {
+    uint32_t off_st, off_tab, tab_m, tab_l, tab, total;
+};
+// per table buffer: 16 atom records, then e^{i m ty} (slot NM zero), then q e^{i l tx}
+__host__ __device__ inline P1bLayout p1b_layout(int NM) {
+    P1bLayout L;
+    L.off_st = 1024;
+    L.off_tab = L.off_st + kS1b * kSt1b;
+    L.tab_m = (uint32_t)(NM + 1) * kTabRow;
+    L.tab_l = (uint32_t)kMaxNL2 * kTabRow;
+    L.tab = kGA * 16 + L.tab_m + L.tab_l;
+    L.total = L.off_tab + 2 * L.tab;
+    return L;
+}
+
+// bounded mbarrier wait that also ends when another thread of the CTA has given up (*ab != 0)
+__device__ __forceinline__ bool wait_ab(uint32_t addr, uint32_t parity, volatile int* ab, int* err, int tag) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (*ab) return false;
+        if (it > 32) __nanosleep(it < 2048 ? 32 : 256);
+    }
+    *ab = 1;
+    if (err) atomicCAS(err, 0, tag);
+    return false;
+}
+__device__ __forceinline__ bool wait_ab_warp(uint32_t addr, uint32_t parity, volatile int* ab, int* err, int tag) {
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0) ok = wait_ab(addr, parity, ab, err, tag) ? 1 : 0;
+    __syncwarp();
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+// named barrier 2 over the two table warps with an AND of their flags
+__device__ __forceinline__ bool tab_all(bool ok) {
+    uint32_t res;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, 2, %2, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(res)
+        : "r"((uint32_t)ok), "n"(kTW * 32)
+        : "memory");
+    return res != 0;
+}
+
+typedef unsigned long long f2t;  // two packed floats (f32x2)
+__device__ __forceinline__ f2t f2pk(float a, float b) {
+    f2t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 f2up(f2t r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ f2t f2mul(f2t a, f2t b) {
+    f2t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2t f2fma(f2t a, f2t b, f2t c) {
+    f2t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2t f2sub(f2t a, f2t b) {
+    f2t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// hi/lo FP16 split of a packed pair
+__device__ __forceinline__ void split_f2(f2t x, uint32_t& hi, uint32_t& lo) {
+    const float2 v = f2up(x);
+    const __half2 h = __floats2half2_rn(v.x, v.y);
+    const float2 hf = __half22float2(h);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    const float2 r = f2up(f2sub(x, f2pk(hf.x, hf.y)));
+    lo = pack_h2(r.x, r.y);
+}
+
+// 19 warps launch as 20 for register allocation: at most 96 registers per thread
+__global__ void __launch_bounds__(kT1b, 1)
+    k_tc_sfac2(View v, const uint4* __restrict__ atoms, int chunk, const int4* __restrict__ rows, TcDims d, int NM,
+               int KM, float* __restrict__ part, int rtot, int G, float* __restrict__ rowsc) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const P1bLayout L = p1b_layout(NM);
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm);           // [kS1b] stage written (16 row warps)
+    uint64_t* empty = full + kS1b;                              // [kS1b] stage's MMAs done
+    uint64_t* tabFull = empty + kS1b;                           // [2] tables written (2 table warps)
+    uint64_t* tabEmpty = tabFull + 2;                           // [2] tables read (16 row warps)
+    uint64_t* chainDone = tabEmpty + 2;                         // [2] accumulation chain's MMAs done
+    uint64_t* drained = chainDone + 2;                          // [2] accumulator read out (16 row warps)
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
+    volatile int* ab = reinterpret_cast<volatile int*>(sm + 520);
+    int* err = &v.status[ST_TC_TIMEOUT];
+    const int a0 = blockIdx.y * chunk, a1 = min(v.nmove, a0 + chunk);
+    const int ngroup = a1 > a0 ? (a1 - a0 + kGA - 1) / kGA : 0;
+    const int nchain = (ngroup + G - 1) / G;
+    const int row0 = blockIdx.x * 256;
+    const int rlast = min(row0 + 256, d.nrow) - 1;
+    const int l_lo = rows[row0].x, nl = min(rows[rlast].x - l_lo + 1, kMaxNL2 - 1);
+    if (t == 0) {
+        for (int i = 0; i < kS1b; ++i) {
+            tc::mbar_init(tc::smem_u32(&full[i]), kRW);
+            tc::mbar_init(tc::smem_u32(&empty[i]), 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(tc::smem_u32(&tabFull[i]), kTW);
+            tc::mbar_init(tc::smem_u32(&tabEmpty[i]), kRW);
+            tc::mbar_init(tc::smem_u32(&chainDone[i]), 1);
+            tc::mbar_init(tc::smem_u32(&drained[i]), kRW);
+        }
+        *ab = 0;
+        tc::mbar_fence_init();
+    }
+    // zero the stages (A lanes beyond 2 NN stay zero) and the tables (their zero slots)
+    for (uint32_t o = t * 16; o < L.total - L.off_st; o += kT1b * 16)
+        *reinterpret_cast<uint4*>(sm + L.off_st + o) = make_uint4(0, 0, 0, 0);
+    if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 512);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tslot;
+    if (warp < kRW) {
+        // ---------------- row warps: B entries and A operand, then chain drains into FP32 registers
+        const int r = t >> 1, h = t & 1;              // CTA row, atom half (atoms 8 h .. 8 h + 7)
+        const int row = row0 + r;
+        if (blockIdx.y == 0 && h == 0 && row < d.nrow) rowsc[row] = 0.f;  // k_tc_sreduce takes the maximum
+        int li = kMaxNL2 - 1, mi = NM;                // zero slots for padding rows
+        if (row < d.nrow) {
+            const int4 rw = rows[row];
+            li = min(rw.x - l_lo, kMaxNL2 - 2);
+            mi = rw.y + KM;
+        }
+        // this thread's A item (n, atom pair), if any
+        const bool has_item = t < d.NN * 8;
+        const int ijp = t & 7, ini = t >> 3;
+        const uint32_t ore = tc::tile_off(ini, 2 * ijp), oim = tc::tile_off(d.NN + ini, 2 * ijp);
+        const uint32_t nfac = (uint32_t)(ini - d.KN);
+        const int q = warp & 3, wq = warp >> 2;       // TMEM lane quarter, column block of the drains
+        float acc[64];
+#pragma unroll
+        for (int i = 0; i < 64; ++i) acc[i] = 0.f;
+        bool alive = true;
+        int nd = 0;                                    // chains drained
+        auto drain = [&](int c) {
+            const int b = c & 1;
+            alive = wait_ab_warp(tc::smem_u32(&chainDone[b]), (c >> 1) & 1, ab, err, 41);
+            if (!alive) return;
+            tc::fence_after();
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                float raw[16];
+                tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + b * 256 + wq * 64 + cc * 16, raw);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) acc[cc * 16 + i] += raw[i];
+            }
+            tc::fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(tc::smem_u32(&drained[b]));
+        };
+        const uint32_t o8 = tc::tile_off(r, 8 * h);
+        int s = 0, gi = 0;                             // stage, group within the chain
+        uint32_t rnd = 0;                              // parity of the stage's use
+        for (int g = 0; g < ngroup && alive; ++g) {
+            if (gi == 0 && g >= 2 * G) {
+                drain(nd++);
+                if (!alive) break;
+            }
+            const int tb = g & 1;
+            alive = wait_ab_warp(tc::smem_u32(&tabFull[tb]), (g >> 1) & 1, ab, err, 42);
+            if (alive && g >= kS1b) alive = wait_ab_warp(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
+            if (!alive) break;
+            const unsigned char* tbase = sm + L.off_tab + tb * L.tab;
+            const float4* tm = reinterpret_cast<const float4*>(tbase + kGA * 16 + mi * kTabRow) + 4 * h;
+            const float4* tl = reinterpret_cast<const float4*>(tbase + kGA * 16 + L.tab_m + li * kTabRow) + 4 * h;
+            unsigned char* st = sm + L.off_st + s * kSt1b;
+            uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float4 el = tl[k], em = tm[k];   // (re a, re a+1, im a, im a+1)
+                const f2t elr = f2pk(el.x, el.y), eli = f2pk(el.z, el.w);
+                const f2t emr = f2pk(em.x, em.y), emi = f2pk(em.z, em.w);
+                const f2t re = f2sub(f2mul(elr, emr), f2mul(eli, emi));
+                const f2t im = f2fma(elr, emi, f2mul(eli, emr));
+                split_f2(re, rh[k], rl[k]);
+                split_f2(im, ih[k], il[k]);
+            }
+            *reinterpret_cast<uint4*>(st + 0 * 8192 + o8) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+            *reinterpret_cast<uint4*>(st + 1 * 8192 + o8) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+            *reinterpret_cast<uint4*>(st + 2 * 8192 + o8) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+            *reinterpret_cast<uint4*>(st + 3 * 8192 + o8) = make_uint4(il[0], il[1], il[2], il[3]);
+            if (has_item) {                            // A: e^{i n tz} of two atoms, lanes n and NN + n
+                const uint4* rc = reinterpret_cast<const uint4*>(tbase);
+                float c0, s0, c1, s1;
+                phase(nfac * rc[2 * ijp].z, c0, s0);
+                phase(nfac * rc[2 * ijp + 1].z, c1, s1);
+                uint32_t ch, cl, sh, sl;
+                split2(c0, c1, ch, cl);
+                split2(s0, s1, sh, sl);
+                unsigned char* as = st + kBSt;
+                *reinterpret_cast<uint32_t*>(as + 0 * 4096 + ore) = ch;  // part 0: cos / sin
+                *reinterpret_cast<uint32_t*>(as + 0 * 4096 + oim) = sh;
+                *reinterpret_cast<uint32_t*>(as + 1 * 4096 + ore) = cl;
+                *reinterpret_cast<uint32_t*>(as + 1 * 4096 + oim) = sl;
+                *reinterpret_cast<uint32_t*>(as + 2 * 4096 + ore) = sh ^ 0x80008000u;  // part 1: -sin / cos
+                *reinterpret_cast<uint32_t*>(as + 2 * 4096 + oim) = ch;
+                *reinterpret_cast<uint32_t*>(as + 3 * 4096 + ore) = sl ^ 0x80008000u;
+                *reinterpret_cast<uint32_t*>(as + 3 * 4096 + oim) = cl;
+            }
+            tc::fence_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+                tc::mbar_arrive(tc::smem_u32(&full[s]));
+                tc::mbar_arrive(tc::smem_u32(&tabEmpty[tb]));
+            }
+            if (++s == kS1b) {
+                s = 0;
+                rnd ^= 1u;
+            }
+            if (++gi == G) gi = 0;
+        }
+        while (alive && nd < nchain) drain(nd++);
+        // this CTA's partial: lane (re|im, n) of the quarter, 64 consecutive rows
+        const int lanei = q * 32 + lane;
+        if (alive && !*ab && lanei < 2 * d.NN) {
+            float4* dst = reinterpret_cast<float4*>(part + (size_t)blockIdx.y * d.NP * rtot + (size_t)lanei * rtot +
+                                                    row0 + wq * 64);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                dst[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
+        }
+    } else if (warp < kRW + kTW) {
+        // ---------------- table warps: atom records and the two phase tables of each group
+        const int tt = t - kRW * 32;
+        uint4 nxt = make_uint4(0, 0, 0, 0);
+        if (tt < kGA && ngroup > 0 && a0 + tt < a1) nxt = atoms[a0 + tt];
+        const int items = (NM + nl) * 8;
+        bool ok = true;
+        for (int g = 0; g < ngroup; ++g) {
+            const int tb = g & 1;
+            // both table warps take the same decision (and meet at the same barrier) every group
+            ok = tab_all(ok && !*ab);
+            if (!ok) break;
+            if (g >= 2) ok = wait_ab_warp(tc::smem_u32(&tabEmpty[tb]), ((g >> 1) - 1) & 1, ab, err, 44);
+            ok = tab_all(ok);
+            if (!ok) break;
+            unsigned char* tbase = sm + L.off_tab + tb * L.tab;
+            uint4* recs = reinterpret_cast<uint4*>(tbase);
+            if (tt < kGA) recs[tt] = nxt;             // padding atoms: zero charge, zero entries
+            tc::named_sync(2, kTW * 32);
+            if (tt < kGA) {
+                const int an = a0 + (g + 1) * kGA + tt;
+                nxt = (g + 1 < ngroup && an < a1) ? atoms[an] : make_uint4(0, 0, 0, 0);
+            }
+            unsigned char* tmb = tbase + kGA * 16;
+#pragma unroll 2
+            for (int it = tt; it < items; it += kTW * 32) {
+                const int jp = it & 7, idx = it >> 3;
+                const uint4 r0 = recs[2 * jp], r1 = recs[2 * jp + 1];
+                float c0, s0, c1, s1;
+                if (idx < NM) {                          // e^{i m ty}
+                    const uint32_t m = (uint32_t)(idx - KM);
+                    phase(m * r0.y, c0, s0);
+                    phase(m * r1.y, c1, s1);
+                    *reinterpret_cast<float4*>(tmb + idx * kTabRow + jp * 16) = make_float4(c0, c1, s0, s1);
+                } else {                                 // q e^{i l tx}
+                    const int lx = idx - NM;
+                    const uint32_t l = (uint32_t)(lx + l_lo);
+                    phase(l * r0.x, c0, s0);
+                    phase(l * r1.x, c1, s1);
+                    const float q0 = __uint_as_float(r0.w), q1 = __uint_as_float(r1.w);
+                    *reinterpret_cast<float4*>(tmb + L.tab_m + lx * kTabRow + jp * 16) =
+                        make_float4(q0 * c0, q1 * c1, q0 * s0, q1 * s1);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tabFull[tb]));
+        }
+    } else if (lane == 0) {
+        // ---------------- issuer
+        const uint32_t idesc = idesc_e(128, 256);
+        const uint64_t dS0 = tc::desc(tc::smem_u32(sm + L.off_st));
+        int issued = -1, s = 0, gi = 0, c = 0, is = 0;
+        uint32_t rnd = 0, irnd = 0;
+        for (int g = 0; g < ngroup; ++g) {
+            const int b = c & 1;
+            const bool first = gi == 0, last = gi == G - 1 || g == ngroup - 1;
+            bool ok = true;
+            if (first && c >= 2) ok = wait_ab(tc::smem_u32(&drained[b]), ((c >> 1) - 1) & 1, ab, err, 46);
+            if (ok) ok = wait_ab(tc::smem_u32(&full[s]), rnd, ab, err, 47);
+            if (!ok) break;
+            tc::fence_after();
+            const uint32_t dcol = tmem + b * 256;
+            const uint64_t ds = dS0 + (uint64_t)((s * kSt1b) >> 4);
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                const uint64_t bh = ds + (uint64_t)(((p * 2 + 0) * 8192) >> 4);
+                const uint64_t bl = ds + (uint64_t)(((p * 2 + 1) * 8192) >> 4);
+                const uint64_t ah = ds + (uint64_t)((kBSt + (p * 2 + 0) * 4096) >> 4);
+                const uint64_t al = ds + (uint64_t)((kBSt + (p * 2 + 1) * 4096) >> 4);
+                tc::mma_bf16(dcol, ah, bh, idesc, (first && p == 0) ? 0u : 1u);
+                tc::mma_bf16(dcol, ah, bl, idesc, 1u);
+                tc::mma_bf16(dcol, al, bh, idesc, 1u);
+            }
+            tc::commit(tc::smem_u32(&empty[s]));
+            if (last) tc::commit(tc::smem_u32(&chainDone[b]));
+            issued = g;
+            is = s;
+            irnd = rnd;
+            if (++s == kS1b) {
+                s = 0;
+                rnd ^= 1u;
+            }
+            if (++gi == G) {
+                gi = 0;
+                ++c;
+            }
+        }
+        // let the issued MMAs finish (bounded) before the block frees its TMEM
+        if (issued >= 0) tc::mbar_wait(tc::smem_u32(&empty[is]), irnd, nullptr, 0);
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, 512);
+    }
+}
+
 // Split-K reduction of pass 1 fused with the energy (src/forcem.f90:880-885,917), C(k) = Ak
 // conj(S + S_wall) and the scale max |C| max(1, |n|) of the pass-2 operand.  A block takes 32
 // consecutive (row, n) entries (row fastest, so each warp's loads are coalesced); warp g adds the
@@ -781,6 +1152,29 @@ int tc_plan_pass1(Ctx& c, int tpc, int mult) {
     View& v = c.v;
     KSet& ks = c.ks;
     TcPlan& p = c.tcp;
+    if (tpc == 1) {
+        // n-side form: 2 NN lanes in one 128-lane accumulator, 256 rows per CTA whose l range
+        // fits the table
+        if (2 * p.NN > 128) return 1;
+        for (int r0 = 0; r0 < ks.nrow; r0 += 256) {
+            const int r1 = std::min(r0 + 256, ks.nrow) - 1;
+            if (ks.h_row[r1].x - ks.h_row[r0].x + 1 > kMaxNL2 - 1) return 1;
+        }
+        const size_t smem = p1b_layout(p.NM).total;
+        if (smem > 227 * 1024) return 1;
+        p.smem1 = (int)smem;
+        p.tpc1 = 1;
+        p.ncols1 = 512;
+        p.grid1x = (ks.nrow + 255) / 256;
+        p.rtot = p.grid1x * 256;
+        p.nsplit1 = std::max(1, std::min(std::max(1, 76 * mult / p.grid1x), (v.nmove + kGA - 1) / kGA));
+        p.chunk1 = (v.nmove + p.nsplit1 - 1) / p.nsplit1;
+        p.chunk1 = std::max(kGA, (p.chunk1 + kGA - 1) / kGA * kGA);
+        p.nsplit1 = std::max(1, (v.nmove + p.chunk1 - 1) / p.chunk1);
+        p.mult1 = mult;
+        p.G1 = 4;
+        return 0;
+    }
     if (tpc == 4 && p.NP > 128) return 1;
     if (kGA * p.NM > kMaxItems * 128 * tpc || kGA * (kMaxNL - 1) > kMaxItems * 128 * tpc ||
         p.NN * (kGA / 2) > kMaxItems * 128 * tpc)
@@ -812,12 +1206,13 @@ int recip_tc_setup(Ctx& c) {
     p.NM = 2 * ks.kmmax + 1;
     if (p.NP > 256) return set_err(&c, MDG_E_UNSUPPORTED, "knmax too large for the tensor-core reciprocal sum");
     if (ks.klmax + 1 > kMaxNL - 1) return set_err(&c, MDG_E_UNSUPPORTED, "klmax too large for the tensor-core reciprocal sum");
-    const int tpc0 = p.NP <= 128 ? 4 : 2;
+    // the n-side form where it applies, else the row-side form with 4 or 2 row tiles per CTA
+    const int tpc0 = !tc_plan_pass1(c, 1, 2) ? 1 : p.NP <= 128 ? 4 : 2;
     if (tc_plan_pass1(c, tpc0, 2) && tc_plan_pass1(c, 2, 2))
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core table fill");
     // the partial-sum buffer is sized for the largest split the autotuner may choose
     size_t part_max = 0;
-    for (int tpc : {2, 4})
+    for (int tpc : {1, 2, 4})
         for (int m = 1; m <= 4; m *= 2)
             if (!tc_plan_pass1(c, tpc, m)) part_max = std::max(part_max, (size_t)p.nsplit1 * p.NP * p.rtot);
     if (tc_plan_pass1(c, tpc0, 2) && tc_plan_pass1(c, 2, 2)) return set_err(&c, MDG_E_UNSUPPORTED, "tensor-core plan");
@@ -914,6 +1309,7 @@ int recip_tc_setup(Ctx& c) {
     c.d_tc_cf = (float2*)dalloc(c, sizeof(float2) * std::max(ks.nk, 1));
     c.d_frc = (double*)dalloc(c, sizeof(double) * 3 * std::max(v.nmove, 1));
     if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
+    MDG_CUDA(allow_max_smem(k_tc_sfac2));
     MDG_CUDA(allow_max_smem(k_tc_sfac<4>));
     MDG_CUDA(allow_max_smem(k_tc_sfac<2>));
     MDG_CUDA(allow_max_smem(k_tc_force));
@@ -928,7 +1324,10 @@ void recip_tc(Ctx& c) {
     if (ks.nk == 0 || v.nmove == 0) return;
     TcDims d{p.KN, p.NN, p.NP, p.KS, ks.nrow, p.nchunk2, (float)ks.pipix, (float)ks.pipiy, (float)ks.pipiz, p.nst2};
     // c.d_tc_atoms was filled, and c.d_tc_cmax cleared, by the packing kernel of this evaluation
-    if (p.tpc1 == 4)
+    if (p.tpc1 == 1)
+        k_tc_sfac2<<<dim3(p.grid1x, p.nsplit1), kT1b, p.smem1, c.stream>>>(
+            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, p.G1, p.rowsc);
+    else if (p.tpc1 == 4)
         k_tc_sfac<4><<<dim3(p.grid1x, p.nsplit1), P1<4>::kThreads, p.smem1, c.stream>>>(
             v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1, p.rowsc);
     else
