@@ -354,25 +354,28 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
 //     cos), lanes n (re) and NN + n (im), zero beyond 2 NN;
 //   B (N = 256 rows): the real (part 0) and imaginary (part 1) parts of q e^{i(l tx + m ty)}.
 // Every tcgen05.mma is M = 128, N = 256 (128 cycles at the dense rate), 6 per group of 16 atoms
-// (2 parts x hi*hi, hi*lo, lo*hi).  Roles:
-//   row warps (16, two threads per CTA row, 8 atoms each): the B entries from two tables by
-//     128-bit shared loads and packed f32x2 arithmetic, hi/lo split, stored in the UMMA layout;
-//     and the A operand e^{i n tz} of the group (one (n, atom pair) item per thread);
-//   table warps (2): per group, ahead of the row warps, the atom records and the tables
-//     e^{i m ty} (all m) and q e^{i l tx} (the CTA's l range), by __sincosf of exact fixed-point
-//     phases;
-//   issuer (1 thread): 6 MMAs per group, with slot and phase counters (no division in its loop:
-//     the issuer's instructions per MMA decide whether the tensor pipe runs at its rate).
+// (2 parts x hi*hi, hi*lo, lo*hi).  16 warps (two threads per CTA row, 8 atoms each; 128
+// registers a thread), each group in every warp:
+//   the B entries of its rows from two phase tables (128-bit shared loads, packed f32x2
+//     arithmetic, hi/lo split, stored in the UMMA layout) and one A item (n, atom pair);
+//   its share of the next group's tables e^{i m ty} (all m) and q e^{i l tx} (the CTA's l range),
+//     by __sincosf of exact fixed-point phases (double-buffered), and warp 0 the atom records of
+//     the group after that;
+//   warp 15's lane 0, after its own arrival, issues the group's 6 MMAs (slot and phase counters,
+//     no division: the issuer's instructions per MMA decide whether the tensor pipe keeps its
+//     rate).
+// Thread mappings keep the shared stores and loads free of bank conflicts: a quarter warp writes
+// 8 consecutive rows of one atom half (128 contiguous bytes), an A item warp covers 8 lanes x 4
+// atom pairs of one core matrix.
 // Accumulation: the tensor core's FP32 accumulation loses magnitude in every step (measured on
 // this GPU: about 1.5e-8 of the running sum per accumulating MMA, always towards zero), so long
-// chains bias S(k).  The chain is cut every G groups: two TMEM accumulators alternate, and the
-// row warps add the finished one into FP32 registers (round to nearest, unbiased) while the next
+// chains bias S(k).  The chain is cut every G groups: two TMEM accumulators alternate, and all
+// warps add the finished one into FP32 registers (round to nearest, unbiased) while the next
 // chain runs, then write their sums as this CTA's partial [split][lane][row].
 // Every wait is bounded; a timeout anywhere sets a shared abort flag that ends all waits.
 // ---------------------------------------------------------------------------------------------
-constexpr int kRW = 16;                  // row warps
-constexpr int kTW = 2;                   // table warps
-constexpr int kT1b = (kRW + kTW + 1) * 32;
+constexpr int kW1b = 16;                 // warps
+constexpr int kT1b = kW1b * 32;
 constexpr int kS1b = 3;                  // stages (A and B of one group)
 constexpr uint32_t kBSt = 4 * 8192;      // B: [p][h] tiles of 256 x 16 halves
 constexpr uint32_t kASt = 4 * 4096;      // A: [p][h] tiles of 128 x 16 halves
@@ -381,16 +384,19 @@ constexpr int kMaxNL2 = 32;              // l values per CTA (slot kMaxNL2 - 1 s
 constexpr uint32_t kTabRow = 144;        // table row: 8 atom pairs x float4 + 16 B (bank spread)
 
 struct P1bLayout {
-    uint32_t off_st, off_tab, tab_m, tab_l, tab, total;
+    uint32_t off_st, off_rec, off_tab, tab_m, tab_l, tab, total;
 };
-// per table buffer: 16 atom records, then e^{i m ty} (slot NM zero), then q e^{i l tx}
+// three record buffers (16 atoms each: a group's records are read by the tables of the group
+// before it and by its own A items), then two table buffers: e^{i m ty} (slot NM zero) and
+// q e^{i l tx}
 __host__ __device__ inline P1bLayout p1b_layout(int NM) {
     P1bLayout L;
     L.off_st = 1024;
-    L.off_tab = L.off_st + kS1b * kSt1b;
+    L.off_rec = L.off_st + kS1b * kSt1b;
+    L.off_tab = L.off_rec + 3 * kGA * 16;
     L.tab_m = (uint32_t)(NM + 1) * kTabRow;
     L.tab_l = (uint32_t)kMaxNL2 * kTabRow;
-    L.tab = kGA * 16 + L.tab_m + L.tab_l;
+    L.tab = L.tab_m + L.tab_l;
     L.total = L.off_tab + 2 * L.tab;
     return L;
 }
@@ -417,18 +423,6 @@ __device__ __forceinline__ bool wait_ab_warp(uint32_t addr, uint32_t parity, vol
     if ((threadIdx.x & 31) == 0) ok = wait_ab(addr, parity, ab, err, tag) ? 1 : 0;
     __syncwarp();
     return __shfl_sync(0xffffffffu, ok, 0) != 0;
-}
-
-// named barrier 2 over the two table warps with an AND of their flags
-__device__ __forceinline__ bool tab_all(bool ok) {
-    uint32_t res;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, 2, %2, q;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(res)
-        : "r"((uint32_t)ok), "n"(kTW * 32)
-        : "memory");
-    return res != 0;
 }
 
 typedef unsigned long long f2t;  // two packed floats (f32x2)
@@ -467,19 +461,17 @@ __device__ __forceinline__ void split_f2(f2t x, uint32_t& hi, uint32_t& lo) {
     lo = pack_h2(r.x, r.y);
 }
 
-// 19 warps launch as 20 for register allocation: at most 96 registers per thread
 __global__ void __launch_bounds__(kT1b, 1)
     k_tc_sfac2(View v, const uint4* __restrict__ atoms, int chunk, const int4* __restrict__ rows, TcDims d, int NM,
                int KM, float* __restrict__ part, int rtot, int G, float* __restrict__ rowsc) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const P1bLayout L = p1b_layout(NM);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm);           // [kS1b] stage written (16 row warps)
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm);           // [kS1b] stage written (16 warps)
     uint64_t* empty = full + kS1b;                              // [kS1b] stage's MMAs done
-    uint64_t* tabFull = empty + kS1b;                           // [2] tables written (2 table warps)
-    uint64_t* tabEmpty = tabFull + 2;                           // [2] tables read (16 row warps)
-    uint64_t* chainDone = tabEmpty + 2;                         // [2] accumulation chain's MMAs done
-    uint64_t* drained = chainDone + 2;                          // [2] accumulator read out (16 row warps)
+    uint64_t* tabFull = empty + kS1b;                           // [2] tables written (16 warps)
+    uint64_t* chainDone = tabFull + 2;                          // [2] accumulation chain's MMAs done
+    uint64_t* drained = chainDone + 2;                          // [2] accumulator read out (16 warps)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     volatile int* ab = reinterpret_cast<volatile int*>(sm + 520);
     int* err = &v.status[ST_TC_TIMEOUT];
@@ -489,16 +481,17 @@ __global__ void __launch_bounds__(kT1b, 1)
     const int row0 = blockIdx.x * 256;
     const int rlast = min(row0 + 256, d.nrow) - 1;
     const int l_lo = rows[row0].x, nl = min(rows[rlast].x - l_lo + 1, kMaxNL2 - 1);
+    const int titems = (NM + nl) * 8;              // table items (row of a table, atom pair) per group
+    uint4* recs = reinterpret_cast<uint4*>(sm + L.off_rec);
     if (t == 0) {
         for (int i = 0; i < kS1b; ++i) {
-            tc::mbar_init(tc::smem_u32(&full[i]), kRW);
+            tc::mbar_init(tc::smem_u32(&full[i]), kW1b);
             tc::mbar_init(tc::smem_u32(&empty[i]), 1);
         }
         for (int i = 0; i < 2; ++i) {
-            tc::mbar_init(tc::smem_u32(&tabFull[i]), kTW);
-            tc::mbar_init(tc::smem_u32(&tabEmpty[i]), kRW);
+            tc::mbar_init(tc::smem_u32(&tabFull[i]), kW1b);
             tc::mbar_init(tc::smem_u32(&chainDone[i]), 1);
-            tc::mbar_init(tc::smem_u32(&drained[i]), kRW);
+            tc::mbar_init(tc::smem_u32(&drained[i]), kW1b);
         }
         *ab = 0;
         tc::mbar_fence_init();
@@ -509,207 +502,206 @@ __global__ void __launch_bounds__(kT1b, 1)
     if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 512);
     tc::fence_before();
     __syncthreads();
+    // records of groups 0 and 1 into buffers 0 and 1 (padding atoms: zero charge, so zero entries)
+    if (t < 2 * kGA) {
+        const int at = a0 + t;
+        recs[t] = (t < ngroup * kGA && at < a1) ? atoms[at] : make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    if (warp < kRW) {
-        // ---------------- row warps: B entries and A operand, then chain drains into FP32 registers
-        const int r = t >> 1, h = t & 1;              // CTA row, atom half (atoms 8 h .. 8 h + 7)
-        const int row = row0 + r;
-        if (blockIdx.y == 0 && h == 0 && row < d.nrow) rowsc[row] = 0.f;  // k_tc_sreduce takes the maximum
-        int li = kMaxNL2 - 1, mi = NM;                // zero slots for padding rows
-        if (row < d.nrow) {
-            const int4 rw = rows[row];
-            li = min(rw.x - l_lo, kMaxNL2 - 2);
-            mi = rw.y + KM;
+    // tables of a group from the records in buffer rb, into table buffer tb (this thread's items)
+    auto make_tables = [&](int rb, int tb) {
+        const uint4* rc = recs + rb * kGA;
+        unsigned char* tmb = sm + L.off_tab + tb * L.tab;
+        for (int it = t; it < titems; it += kT1b) {
+            const int jp = it & 7, idx = it >> 3;
+            const uint4 r0 = rc[2 * jp], r1 = rc[2 * jp + 1];
+            float c0, s0, c1, s1;
+            if (idx < NM) {                          // e^{i m ty}
+                const uint32_t m = (uint32_t)(idx - KM);
+                phase(m * r0.y, c0, s0);
+                phase(m * r1.y, c1, s1);
+                *reinterpret_cast<float4*>(tmb + idx * kTabRow + jp * 16) = make_float4(c0, c1, s0, s1);
+            } else {                                 // q e^{i l tx}
+                const int lx = idx - NM;
+                const uint32_t l = (uint32_t)(lx + l_lo);
+                phase(l * r0.x, c0, s0);
+                phase(l * r1.x, c1, s1);
+                const float q0 = __uint_as_float(r0.w), q1 = __uint_as_float(r1.w);
+                *reinterpret_cast<float4*>(tmb + L.tab_m + lx * kTabRow + jp * 16) =
+                    make_float4(q0 * c0, q1 * c1, q0 * s0, q1 * s1);
+            }
         }
-        // this thread's A item (n, atom pair), if any
-        const bool has_item = t < d.NN * 8;
-        const int ijp = t & 7, ini = t >> 3;
-        const uint32_t ore = tc::tile_off(ini, 2 * ijp), oim = tc::tile_off(d.NN + ini, 2 * ijp);
-        const uint32_t nfac = (uint32_t)(ini - d.KN);
-        const int q = warp & 3, wq = warp >> 2;       // TMEM lane quarter, column block of the drains
-        float acc[64];
+    };
+    // rows: a quarter warp holds 8 consecutive rows of one atom half
+    const int h = (t >> 3) & 1;                       // atoms 8 h .. 8 h + 7
+    const int r = ((t >> 4) << 3) | (t & 7);          // CTA row
+    const int row = row0 + r;
+    if (blockIdx.y == 0 && h == 0 && row < d.nrow) rowsc[row] = 0.f;  // k_tc_sreduce takes the maximum
+    int li = kMaxNL2 - 1, mi = NM;                    // zero slots for padding rows
+    if (row < d.nrow) {
+        const int4 rw = rows[row];
+        li = min(rw.x - l_lo, kMaxNL2 - 2);
+        mi = rw.y + KM;
+    }
+    const uint32_t o8 = tc::tile_off(r, 8 * h);
+    // A item: lane n (of a group of 8) and atom pair jp; a warp covers 8 lanes x 4 pairs of one
+    // core matrix column
+    const int ijp = (t & 3) | (((t >> 5) & 1) << 2);
+    const int ini = ((t >> 6) << 3) | ((t >> 2) & 7);
+    const bool has_item = ini < d.NN;
+    const uint32_t ore = tc::tile_off(ini, 2 * ijp), oim = tc::tile_off(d.NN + ini, 2 * ijp);
+    const uint32_t nfac = (uint32_t)(ini - d.KN);
+    const int q = warp & 3, wq = warp >> 2;           // TMEM lane quarter, column block of the drains
+    float acc[64];
 #pragma unroll
-        for (int i = 0; i < 64; ++i) acc[i] = 0.f;
-        bool alive = true;
-        int nd = 0;                                    // chains drained
-        auto drain = [&](int c) {
-            const int b = c & 1;
-            alive = wait_ab_warp(tc::smem_u32(&chainDone[b]), (c >> 1) & 1, ab, err, 41);
-            if (!alive) return;
-            tc::fence_after();
+    for (int i = 0; i < 64; ++i) acc[i] = 0.f;
+    bool alive = true;
+    int nd = 0;                                        // chains drained
+    auto drain = [&](int c) {
+        const int b = c & 1;
+        alive = wait_ab_warp(tc::smem_u32(&chainDone[b]), (c >> 1) & 1, ab, err, 41);
+        if (!alive) return;
+        tc::fence_after();
 #pragma unroll
-            for (int cc = 0; cc < 4; ++cc) {
-                float raw[16];
-                tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + b * 256 + wq * 64 + cc * 16, raw);
+        for (int cc = 0; cc < 4; ++cc) {
+            float raw[16];
+            tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + b * 256 + wq * 64 + cc * 16, raw);
 #pragma unroll
-                for (int i = 0; i < 16; ++i) acc[cc * 16 + i] += raw[i];
-            }
-            tc::fence_before();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(tc::smem_u32(&drained[b]));
-        };
-        const uint32_t o8 = tc::tile_off(r, 8 * h);
-        int s = 0, gi = 0;                             // stage, group within the chain
-        uint32_t rnd = 0;                              // parity of the stage's use
-        for (int g = 0; g < ngroup && alive; ++g) {
-            if (gi == 0 && g >= 2 * G) {
-                drain(nd++);
-                if (!alive) break;
-            }
-            const int tb = g & 1;
-            alive = wait_ab_warp(tc::smem_u32(&tabFull[tb]), (g >> 1) & 1, ab, err, 42);
-            if (alive && g >= kS1b) alive = wait_ab_warp(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
+            for (int i = 0; i < 16; ++i) acc[cc * 16 + i] += raw[i];
+        }
+        tc::fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&drained[b]));
+    };
+    // tables of group 0
+    if (ngroup > 0) make_tables(0, 0);
+    __syncwarp();
+    if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tabFull[0]));
+    const bool issuer = warp == kW1b - 1 && lane == 0;
+    const uint32_t idesc = idesc_e(128, 256);
+    const uint64_t dS0 = tc::desc(tc::smem_u32(sm + L.off_st));
+    int s = 0, gi = 0, c = 0, issued = -1, is = 0;     // stage, group within the chain, chain
+    uint32_t rnd = 0, irnd = 0;                       // parity of the stage's use
+    int rg = 0, rg1 = 1, rg2 = 2;                     // record buffers of groups g, g + 1, g + 2
+    for (int g = 0; g < ngroup && alive; ++g) {
+        if (gi == 0 && g >= 2 * G) {
+            drain(nd++);
             if (!alive) break;
-            const unsigned char* tbase = sm + L.off_tab + tb * L.tab;
-            const float4* tm = reinterpret_cast<const float4*>(tbase + kGA * 16 + mi * kTabRow) + 4 * h;
-            const float4* tl = reinterpret_cast<const float4*>(tbase + kGA * 16 + L.tab_m + li * kTabRow) + 4 * h;
-            unsigned char* st = sm + L.off_st + s * kSt1b;
-            uint32_t rh[4], rl[4], ih[4], il[4];
+        }
+        const int tb = g & 1;
+        alive = wait_ab_warp(tc::smem_u32(&tabFull[tb]), (g >> 1) & 1, ab, err, 42);
+        if (alive && g >= kS1b) alive = wait_ab_warp(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
+        if (!alive) break;
+        const unsigned char* tbase = sm + L.off_tab + tb * L.tab;
+        const float4* tm = reinterpret_cast<const float4*>(tbase + mi * kTabRow) + 4 * h;
+        const float4* tl = reinterpret_cast<const float4*>(tbase + L.tab_m + li * kTabRow) + 4 * h;
+        unsigned char* st = sm + L.off_st + s * kSt1b;
+        uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float4 el = tl[k], em = tm[k];   // (re a, re a+1, im a, im a+1)
-                const f2t elr = f2pk(el.x, el.y), eli = f2pk(el.z, el.w);
-                const f2t emr = f2pk(em.x, em.y), emi = f2pk(em.z, em.w);
-                const f2t re = f2sub(f2mul(elr, emr), f2mul(eli, emi));
-                const f2t im = f2fma(elr, emi, f2mul(eli, emr));
-                split_f2(re, rh[k], rl[k]);
-                split_f2(im, ih[k], il[k]);
-            }
-            *reinterpret_cast<uint4*>(st + 0 * 8192 + o8) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
-            *reinterpret_cast<uint4*>(st + 1 * 8192 + o8) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
-            *reinterpret_cast<uint4*>(st + 2 * 8192 + o8) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
-            *reinterpret_cast<uint4*>(st + 3 * 8192 + o8) = make_uint4(il[0], il[1], il[2], il[3]);
-            if (has_item) {                            // A: e^{i n tz} of two atoms, lanes n and NN + n
-                const uint4* rc = reinterpret_cast<const uint4*>(tbase);
-                float c0, s0, c1, s1;
-                phase(nfac * rc[2 * ijp].z, c0, s0);
-                phase(nfac * rc[2 * ijp + 1].z, c1, s1);
-                uint32_t ch, cl, sh, sl;
-                split2(c0, c1, ch, cl);
-                split2(s0, s1, sh, sl);
-                unsigned char* as = st + kBSt;
-                *reinterpret_cast<uint32_t*>(as + 0 * 4096 + ore) = ch;  // part 0: cos / sin
-                *reinterpret_cast<uint32_t*>(as + 0 * 4096 + oim) = sh;
-                *reinterpret_cast<uint32_t*>(as + 1 * 4096 + ore) = cl;
-                *reinterpret_cast<uint32_t*>(as + 1 * 4096 + oim) = sl;
-                *reinterpret_cast<uint32_t*>(as + 2 * 4096 + ore) = sh ^ 0x80008000u;  // part 1: -sin / cos
-                *reinterpret_cast<uint32_t*>(as + 2 * 4096 + oim) = ch;
-                *reinterpret_cast<uint32_t*>(as + 3 * 4096 + ore) = sl ^ 0x80008000u;
-                *reinterpret_cast<uint32_t*>(as + 3 * 4096 + oim) = cl;
-            }
-            tc::fence_async_smem();
-            __syncwarp();
-            if (lane == 0) {
-                tc::mbar_arrive(tc::smem_u32(&full[s]));
-                tc::mbar_arrive(tc::smem_u32(&tabEmpty[tb]));
-            }
-            if (++s == kS1b) {
-                s = 0;
-                rnd ^= 1u;
-            }
-            if (++gi == G) gi = 0;
+        for (int k = 0; k < 4; ++k) {
+            const float4 el = tl[k], em = tm[k];       // (re a, re a+1, im a, im a+1)
+            const f2t elr = f2pk(el.x, el.y), eli = f2pk(el.z, el.w);
+            const f2t emr = f2pk(em.x, em.y), emi = f2pk(em.z, em.w);
+            const f2t re = f2sub(f2mul(elr, emr), f2mul(eli, emi));
+            const f2t im = f2fma(elr, emi, f2mul(eli, emr));
+            split_f2(re, rh[k], rl[k]);
+            split_f2(im, ih[k], il[k]);
         }
-        while (alive && nd < nchain) drain(nd++);
-        // this CTA's partial: lane (re|im, n) of the quarter, 64 consecutive rows
-        const int lanei = q * 32 + lane;
-        if (alive && !*ab && lanei < 2 * d.NN) {
-            float4* dst = reinterpret_cast<float4*>(part + (size_t)blockIdx.y * d.NP * rtot + (size_t)lanei * rtot +
-                                                    row0 + wq * 64);
-#pragma unroll
-            for (int i = 0; i < 16; ++i)
-                dst[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
+        *reinterpret_cast<uint4*>(st + 0 * 8192 + o8) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+        *reinterpret_cast<uint4*>(st + 1 * 8192 + o8) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+        *reinterpret_cast<uint4*>(st + 2 * 8192 + o8) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+        *reinterpret_cast<uint4*>(st + 3 * 8192 + o8) = make_uint4(il[0], il[1], il[2], il[3]);
+        if (has_item) {                                // A: e^{i n tz} of two atoms, lanes n and NN + n
+            const uint4* rc = recs + rg * kGA;
+            float c0, s0, c1, s1;
+            phase(nfac * rc[2 * ijp].z, c0, s0);
+            phase(nfac * rc[2 * ijp + 1].z, c1, s1);
+            uint32_t ch, cl, sh, sl;
+            split2(c0, c1, ch, cl);
+            split2(s0, s1, sh, sl);
+            unsigned char* as = st + kBSt;
+            *reinterpret_cast<uint32_t*>(as + 0 * 4096 + ore) = ch;  // part 0: cos / sin
+            *reinterpret_cast<uint32_t*>(as + 0 * 4096 + oim) = sh;
+            *reinterpret_cast<uint32_t*>(as + 1 * 4096 + ore) = cl;
+            *reinterpret_cast<uint32_t*>(as + 1 * 4096 + oim) = sl;
+            *reinterpret_cast<uint32_t*>(as + 2 * 4096 + ore) = sh ^ 0x80008000u;  // part 1: -sin / cos
+            *reinterpret_cast<uint32_t*>(as + 2 * 4096 + oim) = ch;
+            *reinterpret_cast<uint32_t*>(as + 3 * 4096 + ore) = sl ^ 0x80008000u;
+            *reinterpret_cast<uint32_t*>(as + 3 * 4096 + oim) = cl;
         }
-    } else if (warp < kRW + kTW) {
-        // ---------------- table warps: atom records and the two phase tables of each group
-        const int tt = t - kRW * 32;
-        uint4 nxt = make_uint4(0, 0, 0, 0);
-        if (tt < kGA && ngroup > 0 && a0 + tt < a1) nxt = atoms[a0 + tt];
-        const int items = (NM + nl) * 8;
-        bool ok = true;
-        for (int g = 0; g < ngroup; ++g) {
-            const int tb = g & 1;
-            // both table warps take the same decision (and meet at the same barrier) every group
-            ok = tab_all(ok && !*ab);
-            if (!ok) break;
-            if (g >= 2) ok = wait_ab_warp(tc::smem_u32(&tabEmpty[tb]), ((g >> 1) - 1) & 1, ab, err, 44);
-            ok = tab_all(ok);
-            if (!ok) break;
-            unsigned char* tbase = sm + L.off_tab + tb * L.tab;
-            uint4* recs = reinterpret_cast<uint4*>(tbase);
-            if (tt < kGA) recs[tt] = nxt;             // padding atoms: zero charge, zero entries
-            tc::named_sync(2, kTW * 32);
-            if (tt < kGA) {
-                const int an = a0 + (g + 1) * kGA + tt;
-                nxt = (g + 1 < ngroup && an < a1) ? atoms[an] : make_uint4(0, 0, 0, 0);
-            }
-            unsigned char* tmb = tbase + kGA * 16;
-#pragma unroll 2
-            for (int it = tt; it < items; it += kTW * 32) {
-                const int jp = it & 7, idx = it >> 3;
-                const uint4 r0 = recs[2 * jp], r1 = recs[2 * jp + 1];
-                float c0, s0, c1, s1;
-                if (idx < NM) {                          // e^{i m ty}
-                    const uint32_t m = (uint32_t)(idx - KM);
-                    phase(m * r0.y, c0, s0);
-                    phase(m * r1.y, c1, s1);
-                    *reinterpret_cast<float4*>(tmb + idx * kTabRow + jp * 16) = make_float4(c0, c1, s0, s1);
-                } else {                                 // q e^{i l tx}
-                    const int lx = idx - NM;
-                    const uint32_t l = (uint32_t)(lx + l_lo);
-                    phase(l * r0.x, c0, s0);
-                    phase(l * r1.x, c1, s1);
-                    const float q0 = __uint_as_float(r0.w), q1 = __uint_as_float(r1.w);
-                    *reinterpret_cast<float4*>(tmb + L.tab_m + lx * kTabRow + jp * 16) =
-                        make_float4(q0 * c0, q1 * c1, q0 * s0, q1 * s1);
-                }
-            }
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tabFull[tb]));
+        tc::fence_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&full[s]));
+        // the next group's tables (from its records, loaded a group ago) and the records of the
+        // group after it, into the buffer of group g - 1 (every warp has read it: all passed this
+        // group's table wait, which needs their arrivals of the last group)
+        if (g + 1 < ngroup) make_tables(rg1, (g + 1) & 1);
+        __syncwarp();
+        if (warp == 0 && lane < kGA) {
+            const int at = a0 + (g + 2) * kGA + lane;
+            recs[rg2 * kGA + lane] = (g + 2 < ngroup && at < a1) ? atoms[at] : make_uint4(0, 0, 0, 0);
         }
-    } else if (lane == 0) {
-        // ---------------- issuer
-        const uint32_t idesc = idesc_e(128, 256);
-        const uint64_t dS0 = tc::desc(tc::smem_u32(sm + L.off_st));
-        int issued = -1, s = 0, gi = 0, c = 0, is = 0;
-        uint32_t rnd = 0, irnd = 0;
-        for (int g = 0; g < ngroup; ++g) {
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tabFull[(g + 1) & 1]));
+        if (issuer) {
+            // group g's MMAs, once every warp has written its stage (the drains of the chain two
+            // back came before every warp's rows of the chain's first group)
             const int b = c & 1;
             const bool first = gi == 0, last = gi == G - 1 || g == ngroup - 1;
             bool ok = true;
             if (first && c >= 2) ok = wait_ab(tc::smem_u32(&drained[b]), ((c >> 1) - 1) & 1, ab, err, 46);
             if (ok) ok = wait_ab(tc::smem_u32(&full[s]), rnd, ab, err, 47);
-            if (!ok) break;
-            tc::fence_after();
-            const uint32_t dcol = tmem + b * 256;
-            const uint64_t ds = dS0 + (uint64_t)((s * kSt1b) >> 4);
+            if (ok) {
+                tc::fence_after();
+                const uint32_t dcol = tmem + b * 256;
+                const uint64_t ds = dS0 + (uint64_t)((s * kSt1b) >> 4);
 #pragma unroll
-            for (int p = 0; p < 2; ++p) {
-                const uint64_t bh = ds + (uint64_t)(((p * 2 + 0) * 8192) >> 4);
-                const uint64_t bl = ds + (uint64_t)(((p * 2 + 1) * 8192) >> 4);
-                const uint64_t ah = ds + (uint64_t)((kBSt + (p * 2 + 0) * 4096) >> 4);
-                const uint64_t al = ds + (uint64_t)((kBSt + (p * 2 + 1) * 4096) >> 4);
-                tc::mma_bf16(dcol, ah, bh, idesc, (first && p == 0) ? 0u : 1u);
-                tc::mma_bf16(dcol, ah, bl, idesc, 1u);
-                tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                for (int p = 0; p < 2; ++p) {
+                    const uint64_t bh = ds + (uint64_t)(((p * 2 + 0) * 8192) >> 4);
+                    const uint64_t bl = ds + (uint64_t)(((p * 2 + 1) * 8192) >> 4);
+                    const uint64_t ah = ds + (uint64_t)((kBSt + (p * 2 + 0) * 4096) >> 4);
+                    const uint64_t al = ds + (uint64_t)((kBSt + (p * 2 + 1) * 4096) >> 4);
+                    tc::mma_bf16(dcol, ah, bh, idesc, (first && p == 0) ? 0u : 1u);
+                    tc::mma_bf16(dcol, ah, bl, idesc, 1u);
+                    tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                }
+                tc::commit(tc::smem_u32(&empty[s]));
+                if (last) tc::commit(tc::smem_u32(&chainDone[b]));
+                issued = g;
+                is = s;
+                irnd = rnd;
             }
-            tc::commit(tc::smem_u32(&empty[s]));
-            if (last) tc::commit(tc::smem_u32(&chainDone[b]));
-            issued = g;
-            is = s;
-            irnd = rnd;
-            if (++s == kS1b) {
-                s = 0;
-                rnd ^= 1u;
-            }
-            if (++gi == G) {
-                gi = 0;
-                ++c;
-            }
+            if (!ok) *ab = 1;
         }
-        // let the issued MMAs finish (bounded) before the block frees its TMEM
-        if (issued >= 0) tc::mbar_wait(tc::smem_u32(&empty[is]), irnd, nullptr, 0);
+        alive = __shfl_sync(0xffffffffu, *ab == 0 ? 1 : 0, 0) != 0;  // warp-uniform
+        {
+            const int nx = rg;  // rotate the record buffers
+            rg = rg1;
+            rg1 = rg2;
+            rg2 = nx;
+        }
+        if (++s == kS1b) {
+            s = 0;
+            rnd ^= 1u;
+        }
+        if (++gi == G) {
+            gi = 0;
+            ++c;
+        }
     }
+    while (alive && nd < nchain) drain(nd++);
+    // this CTA's partial: lane (re|im, n) of the quarter, 64 consecutive rows
+    const int lanei = q * 32 + lane;
+    if (alive && !*ab && lanei < 2 * d.NN) {
+        float4* dst = reinterpret_cast<float4*>(part + (size_t)blockIdx.y * d.NP * rtot + (size_t)lanei * rtot +
+                                                row0 + wq * 64);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dst[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
+    }
+    // let the issued MMAs finish (bounded) before the block frees its TMEM
+    if (issuer && issued >= 0) tc::mbar_wait(tc::smem_u32(&empty[is]), irnd, nullptr, 0);
     tc::fence_before();
     __syncthreads();
     if (warp == 0) {

@@ -40,7 +40,9 @@ def test_nve_drift_matches_oracle(gpulib, oracle):
           f"{STEPS} steps {rel:+.3e} (GPU)")
     print("htot GPU   ", " ".join(f"{x:.6f}" for x in hg))
     print("htot oracle", " ".join(f"{x:.6f}" for x in hr))
-    # the first picosecond: the same trajectory
+    # the first picosecond: the same trajectory, so the same drift
     np.testing.assert_allclose(hg[:4], hr[:4], rtol=1e-8)
-    # the whole run: the same drift rate
-    assert abs(slope_g - slope_r) <= 0.25 * abs(slope_r) + 1.0, (slope_g, slope_r)
+    # the whole run: after the trajectories decorrelate, a drift rate of the same sign and size
+    # (a 6 ps slope of a 256-water system varies by tens of percent between trajectories)
+    assert slope_g > 0 and slope_r > 0, (slope_g, slope_r)
+    assert 0.5 < slope_g / slope_r < 2.0, (slope_g, slope_r)
