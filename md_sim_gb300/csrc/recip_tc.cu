@@ -354,19 +354,18 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
 //     cos), lanes n (re) and NN + n (im), zero beyond 2 NN;
 //   B (N = 256 rows): the real (part 0) and imaginary (part 1) parts of q e^{i(l tx + m ty)}.
 // Every tcgen05.mma is M = 128, N = 256 (128 cycles at the dense rate), 6 per group of 16 atoms
-// (2 parts x hi*hi, hi*lo, lo*hi).  16 warps (two threads per CTA row, 8 atoms each; 128
-// registers a thread), each group in every warp:
-//   the B entries of its rows from two phase tables (128-bit shared loads, packed f32x2
-//     arithmetic, hi/lo split, stored in the UMMA layout) and one A item (n, atom pair);
-//   its share of the next group's tables e^{i m ty} (all m) and q e^{i l tx} (the CTA's l range),
-//     by __sincosf of exact fixed-point phases (double-buffered), and warp 0 the atom records of
-//     the group after that;
-//   warp 15's lane 0, after its own arrival, issues the group's 6 MMAs (slot and phase counters,
-//     no division: the issuer's instructions per MMA decide whether the tensor pipe keeps its
-//     rate).
-// Thread mappings keep the shared stores and loads free of bank conflicts: a quarter warp writes
-// 8 consecutive rows of one atom half (128 contiguous bytes), an A item warp covers 8 lanes x 4
-// atom pairs of one core matrix.
+// (2 parts x hi*hi, hi*lo, lo*hi).  The CTA's atom records (a contiguous chunk, at most
+// kMaxChunk1b atoms) arrive in shared memory by one bulk copy; then 16 warps (two threads per CTA
+// row, 8 atoms each; 128 registers a thread) produce, group after group and without waiting for
+// one another,
+//   the B entries of their rows, each by one __sincosf of the exact fixed-point phase
+//     l ux + m uy (mod 2^32) times q, split hi/lo and stored in the UMMA layout, and
+//   one A item (n, atom pair) each,
+// and arrive on the stage's barrier; warp 15's lane 0, after its own arrival, issues the group's
+// 6 MMAs (slot and phase counters, no division: the issuer's instructions per MMA decide whether
+// the tensor pipe keeps its rate).  Thread mappings keep the shared stores free of bank
+// conflicts: a quarter warp writes 8 consecutive rows of one atom half (128 contiguous bytes); an
+// A item warp covers 8 lanes x 4 atom pairs of one core matrix column.
 // Accumulation: the tensor core's FP32 accumulation loses magnitude in every step (measured on
 // this GPU: about 1.5e-8 of the running sum per accumulating MMA, always towards zero), so long
 // chains bias S(k).  The chain is cut every G groups: two TMEM accumulators alternate, and all
@@ -380,24 +379,16 @@ constexpr int kS1b = 3;                  // stages (A and B of one group)
 constexpr uint32_t kBSt = 4 * 8192;      // B: [p][h] tiles of 256 x 16 halves
 constexpr uint32_t kASt = 4 * 4096;      // A: [p][h] tiles of 128 x 16 halves
 constexpr uint32_t kSt1b = kBSt + kASt;
-constexpr int kMaxNL2 = 32;              // l values per CTA (slot kMaxNL2 - 1 stays zero)
-constexpr uint32_t kTabRow = 144;        // table row: 8 atom pairs x float4 + 16 B (bank spread)
+constexpr int kMaxChunk1b = 3072;        // atoms per CTA (records in shared memory: 48 KB)
 
 struct P1bLayout {
-    uint32_t off_st, off_rec, off_tab, tab_m, tab_l, tab, total;
+    uint32_t off_st, off_rec, total;
 };
-// three record buffers (16 atoms each: a group's records are read by the tables of the group
-// before it and by its own A items), then two table buffers: e^{i m ty} (slot NM zero) and
-// q e^{i l tx}
-__host__ __device__ inline P1bLayout p1b_layout(int NM) {
+__host__ __device__ inline P1bLayout p1b_layout() {
     P1bLayout L;
     L.off_st = 1024;
     L.off_rec = L.off_st + kS1b * kSt1b;
-    L.off_tab = L.off_rec + 3 * kGA * 16;
-    L.tab_m = (uint32_t)(NM + 1) * kTabRow;
-    L.tab_l = (uint32_t)kMaxNL2 * kTabRow;
-    L.tab = L.tab_m + L.tab_l;
-    L.total = L.off_tab + 2 * L.tab;
+    L.total = L.off_rec + kMaxChunk1b * 16;
     return L;
 }
 
@@ -462,16 +453,16 @@ __device__ __forceinline__ void split_f2(f2t x, uint32_t& hi, uint32_t& lo) {
 }
 
 __global__ void __launch_bounds__(kT1b, 1)
-    k_tc_sfac2(View v, const uint4* __restrict__ atoms, int chunk, const int4* __restrict__ rows, TcDims d, int NM,
-               int KM, float* __restrict__ part, int rtot, int G, float* __restrict__ rowsc) {
+    k_tc_sfac2(View v, const uint4* __restrict__ atoms, int chunk, const int4* __restrict__ rows, TcDims d, int KM,
+               float* __restrict__ part, int rtot, int G, float* __restrict__ rowsc) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    const P1bLayout L = p1b_layout(NM);
+    const P1bLayout L = p1b_layout();
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     uint64_t* full = reinterpret_cast<uint64_t*>(sm);           // [kS1b] stage written (16 warps)
     uint64_t* empty = full + kS1b;                              // [kS1b] stage's MMAs done
-    uint64_t* tabFull = empty + kS1b;                           // [2] tables written (16 warps)
-    uint64_t* chainDone = tabFull + 2;                          // [2] accumulation chain's MMAs done
+    uint64_t* chainDone = empty + kS1b;                         // [2] accumulation chain's MMAs done
     uint64_t* drained = chainDone + 2;                          // [2] accumulator read out (16 warps)
+    uint64_t* recbar = drained + 2;                             // records landed
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     volatile int* ab = reinterpret_cast<volatile int*>(sm + 520);
     int* err = &v.status[ST_TC_TIMEOUT];
@@ -479,71 +470,47 @@ __global__ void __launch_bounds__(kT1b, 1)
     const int ngroup = a1 > a0 ? (a1 - a0 + kGA - 1) / kGA : 0;
     const int nchain = (ngroup + G - 1) / G;
     const int row0 = blockIdx.x * 256;
-    const int rlast = min(row0 + 256, d.nrow) - 1;
-    const int l_lo = rows[row0].x, nl = min(rows[rlast].x - l_lo + 1, kMaxNL2 - 1);
-    const int titems = (NM + nl) * 8;              // table items (row of a table, atom pair) per group
-    uint4* recs = reinterpret_cast<uint4*>(sm + L.off_rec);
+    const uint4* recs = reinterpret_cast<const uint4*>(sm + L.off_rec);
     if (t == 0) {
         for (int i = 0; i < kS1b; ++i) {
             tc::mbar_init(tc::smem_u32(&full[i]), kW1b);
             tc::mbar_init(tc::smem_u32(&empty[i]), 1);
         }
         for (int i = 0; i < 2; ++i) {
-            tc::mbar_init(tc::smem_u32(&tabFull[i]), kW1b);
             tc::mbar_init(tc::smem_u32(&chainDone[i]), 1);
             tc::mbar_init(tc::smem_u32(&drained[i]), kW1b);
         }
+        tc::mbar_init(tc::smem_u32(recbar), 1);
         *ab = 0;
         tc::mbar_fence_init();
     }
-    // zero the stages (A lanes beyond 2 NN stay zero) and the tables (their zero slots)
+    // zero the stages (A lanes beyond 2 NN stay zero) and the records (padding atoms: zero
+    // charge, so zero entries)
     for (uint32_t o = t * 16; o < L.total - L.off_st; o += kT1b * 16)
         *reinterpret_cast<uint4*>(sm + L.off_st + o) = make_uint4(0, 0, 0, 0);
     if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 512);
+    tc::fence_async_smem();
     tc::fence_before();
-    __syncthreads();
-    // records of groups 0 and 1 into buffers 0 and 1 (padding atoms: zero charge, so zero entries)
-    if (t < 2 * kGA) {
-        const int at = a0 + t;
-        recs[t] = (t < ngroup * kGA && at < a1) ? atoms[at] : make_uint4(0, 0, 0, 0);
-    }
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    // tables of a group from the records in buffer rb, into table buffer tb (this thread's items)
-    auto make_tables = [&](int rb, int tb) {
-        const uint4* rc = recs + rb * kGA;
-        unsigned char* tmb = sm + L.off_tab + tb * L.tab;
-        for (int it = t; it < titems; it += kT1b) {
-            const int jp = it & 7, idx = it >> 3;
-            const uint4 r0 = rc[2 * jp], r1 = rc[2 * jp + 1];
-            float c0, s0, c1, s1;
-            if (idx < NM) {                          // e^{i m ty}
-                const uint32_t m = (uint32_t)(idx - KM);
-                phase(m * r0.y, c0, s0);
-                phase(m * r1.y, c1, s1);
-                *reinterpret_cast<float4*>(tmb + idx * kTabRow + jp * 16) = make_float4(c0, c1, s0, s1);
-            } else {                                 // q e^{i l tx}
-                const int lx = idx - NM;
-                const uint32_t l = (uint32_t)(lx + l_lo);
-                phase(l * r0.x, c0, s0);
-                phase(l * r1.x, c1, s1);
-                const float q0 = __uint_as_float(r0.w), q1 = __uint_as_float(r1.w);
-                *reinterpret_cast<float4*>(tmb + L.tab_m + lx * kTabRow + jp * 16) =
-                    make_float4(q0 * c0, q1 * c1, q0 * s0, q1 * s1);
-            }
-        }
-    };
+    if (t == 0 && a1 > a0) {
+        const uint32_t bytes = (uint32_t)(a1 - a0) * 16u;
+        tc::mbar_expect_tx(tc::smem_u32(recbar), bytes);
+        tc::bulk_g2s(tc::smem_u32(sm + L.off_rec), atoms + a0, bytes, tc::smem_u32(recbar));
+    }
     // rows: a quarter warp holds 8 consecutive rows of one atom half
-    const int h = (t >> 3) & 1;                       // atoms 8 h .. 8 h + 7
+    const int h = (t >> 3) & 1;                       // atoms 8 h .. 8 h + 7 of each group
     const int r = ((t >> 4) << 3) | (t & 7);          // CTA row
     const int row = row0 + r;
     if (blockIdx.y == 0 && h == 0 && row < d.nrow) rowsc[row] = 0.f;  // k_tc_sreduce takes the maximum
-    int li = kMaxNL2 - 1, mi = NM;                    // zero slots for padding rows
+    uint32_t lu = 0, mu = 0;
+    float rmask = 0.f;                                // padding rows: zero entries
     if (row < d.nrow) {
         const int4 rw = rows[row];
-        li = min(rw.x - l_lo, kMaxNL2 - 2);
-        mi = rw.y + KM;
+        lu = (uint32_t)rw.x;
+        mu = (uint32_t)rw.y;
+        rmask = 1.f;
     }
     const uint32_t o8 = tc::tile_off(r, 8 * h);
     // A item: lane n (of a group of 8) and atom pair jp; a warp covers 8 lanes x 4 pairs of one
@@ -557,7 +524,7 @@ __global__ void __launch_bounds__(kT1b, 1)
     float acc[64];
 #pragma unroll
     for (int i = 0; i < 64; ++i) acc[i] = 0.f;
-    bool alive = true;
+    bool alive = a1 <= a0 || wait_ab_warp(tc::smem_u32(recbar), 0, ab, err, 40);
     int nd = 0;                                        // chains drained
     auto drain = [&](int c) {
         const int b = c & 1;
@@ -575,46 +542,36 @@ __global__ void __launch_bounds__(kT1b, 1)
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(tc::smem_u32(&drained[b]));
     };
-    // tables of group 0
-    if (ngroup > 0) make_tables(0, 0);
-    __syncwarp();
-    if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tabFull[0]));
     const bool issuer = warp == kW1b - 1 && lane == 0;
     const uint32_t idesc = idesc_e(128, 256);
     const uint64_t dS0 = tc::desc(tc::smem_u32(sm + L.off_st));
     int s = 0, gi = 0, c = 0, issued = -1, is = 0;     // stage, group within the chain, chain
     uint32_t rnd = 0, irnd = 0;                       // parity of the stage's use
-    int rg = 0, rg1 = 1, rg2 = 2;                     // record buffers of groups g, g + 1, g + 2
     for (int g = 0; g < ngroup && alive; ++g) {
         if (gi == 0 && g >= 2 * G) {
             drain(nd++);
             if (!alive) break;
         }
-        const int tb = g & 1;
-        alive = wait_ab_warp(tc::smem_u32(&tabFull[tb]), (g >> 1) & 1, ab, err, 42);
-        if (alive && g >= kS1b) alive = wait_ab_warp(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
+        if (g >= kS1b) alive = wait_ab_warp(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
         if (!alive) break;
-        const unsigned char* tbase = sm + L.off_tab + tb * L.tab;
-        const float4* tm = reinterpret_cast<const float4*>(tbase + mi * kTabRow) + 4 * h;
-        const float4* tl = reinterpret_cast<const float4*>(tbase + L.tab_m + li * kTabRow) + 4 * h;
         unsigned char* st = sm + L.off_st + s * kSt1b;
+        const uint4* rc = recs + g * kGA;
         uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float4 el = tl[k], em = tm[k];       // (re a, re a+1, im a, im a+1)
-            const f2t elr = f2pk(el.x, el.y), eli = f2pk(el.z, el.w);
-            const f2t emr = f2pk(em.x, em.y), emi = f2pk(em.z, em.w);
-            const f2t re = f2sub(f2mul(elr, emr), f2mul(eli, emi));
-            const f2t im = f2fma(elr, emi, f2mul(eli, emr));
-            split_f2(re, rh[k], rl[k]);
-            split_f2(im, ih[k], il[k]);
+            const uint4 r0 = rc[8 * h + 2 * k], r1 = rc[8 * h + 2 * k + 1];
+            float c0, s0, c1, s1;
+            phase(lu * r0.x + mu * r0.y, c0, s0);
+            phase(lu * r1.x + mu * r1.y, c1, s1);
+            const float q0 = __uint_as_float(r0.w) * rmask, q1 = __uint_as_float(r1.w) * rmask;
+            split2(q0 * c0, q1 * c1, rh[k], rl[k]);
+            split2(q0 * s0, q1 * s1, ih[k], il[k]);
         }
         *reinterpret_cast<uint4*>(st + 0 * 8192 + o8) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
         *reinterpret_cast<uint4*>(st + 1 * 8192 + o8) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
         *reinterpret_cast<uint4*>(st + 2 * 8192 + o8) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
         *reinterpret_cast<uint4*>(st + 3 * 8192 + o8) = make_uint4(il[0], il[1], il[2], il[3]);
         if (has_item) {                                // A: e^{i n tz} of two atoms, lanes n and NN + n
-            const uint4* rc = recs + rg * kGA;
             float c0, s0, c1, s1;
             phase(nfac * rc[2 * ijp].z, c0, s0);
             phase(nfac * rc[2 * ijp + 1].z, c1, s1);
@@ -634,20 +591,9 @@ __global__ void __launch_bounds__(kT1b, 1)
         tc::fence_async_smem();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(tc::smem_u32(&full[s]));
-        // the next group's tables (from its records, loaded a group ago) and the records of the
-        // group after it, into the buffer of group g - 1 (every warp has read it: all passed this
-        // group's table wait, which needs their arrivals of the last group)
-        if (g + 1 < ngroup) make_tables(rg1, (g + 1) & 1);
-        __syncwarp();
-        if (warp == 0 && lane < kGA) {
-            const int at = a0 + (g + 2) * kGA + lane;
-            recs[rg2 * kGA + lane] = (g + 2 < ngroup && at < a1) ? atoms[at] : make_uint4(0, 0, 0, 0);
-        }
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tabFull[(g + 1) & 1]));
         if (issuer) {
             // group g's MMAs, once every warp has written its stage (the drains of the chain two
-            // back came before every warp's rows of the chain's first group)
+            // back came before every warp's entries of the chain's first group)
             const int b = c & 1;
             const bool first = gi == 0, last = gi == G - 1 || g == ngroup - 1;
             bool ok = true;
@@ -676,12 +622,6 @@ __global__ void __launch_bounds__(kT1b, 1)
             if (!ok) *ab = 1;
         }
         alive = __shfl_sync(0xffffffffu, *ab == 0 ? 1 : 0, 0) != 0;  // warp-uniform
-        {
-            const int nx = rg;  // rotate the record buffers
-            rg = rg1;
-            rg1 = rg2;
-            rg2 = nx;
-        }
         if (++s == kS1b) {
             s = 0;
             rnd ^= 1u;
@@ -700,8 +640,9 @@ __global__ void __launch_bounds__(kT1b, 1)
 #pragma unroll
         for (int i = 0; i < 16; ++i) dst[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
     }
-    // let the issued MMAs finish (bounded) before the block frees its TMEM
+    // let the issued MMAs (and the record copy) finish (bounded) before the block frees its TMEM
     if (issuer && issued >= 0) tc::mbar_wait(tc::smem_u32(&empty[is]), irnd, nullptr, 0);
+    if (t == 0 && a1 > a0 && !alive) tc::mbar_wait(tc::smem_u32(recbar), 0, nullptr, 0);
     tc::fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -1145,14 +1086,10 @@ int tc_plan_pass1(Ctx& c, int tpc, int mult) {
     KSet& ks = c.ks;
     TcPlan& p = c.tcp;
     if (tpc == 1) {
-        // n-side form: 2 NN lanes in one 128-lane accumulator, 256 rows per CTA whose l range
-        // fits the table
+        // n-side form: 2 NN lanes in one 128-lane accumulator, 256 rows per CTA, at most
+        // kMaxChunk1b atoms per CTA (their records in shared memory)
         if (2 * p.NN > 128) return 1;
-        for (int r0 = 0; r0 < ks.nrow; r0 += 256) {
-            const int r1 = std::min(r0 + 256, ks.nrow) - 1;
-            if (ks.h_row[r1].x - ks.h_row[r0].x + 1 > kMaxNL2 - 1) return 1;
-        }
-        const size_t smem = p1b_layout(p.NM).total;
+        const size_t smem = p1b_layout().total;
         if (smem > 227 * 1024) return 1;
         p.smem1 = (int)smem;
         p.tpc1 = 1;
@@ -1160,8 +1097,10 @@ int tc_plan_pass1(Ctx& c, int tpc, int mult) {
         p.grid1x = (ks.nrow + 255) / 256;
         p.rtot = p.grid1x * 256;
         p.nsplit1 = std::max(1, std::min(std::max(1, 76 * mult / p.grid1x), (v.nmove + kGA - 1) / kGA));
+        p.nsplit1 = std::max(p.nsplit1, (v.nmove + kMaxChunk1b - 1) / kMaxChunk1b);
         p.chunk1 = (v.nmove + p.nsplit1 - 1) / p.nsplit1;
         p.chunk1 = std::max(kGA, (p.chunk1 + kGA - 1) / kGA * kGA);
+        if (p.chunk1 > kMaxChunk1b) return 1;
         p.nsplit1 = std::max(1, (v.nmove + p.chunk1 - 1) / p.chunk1);
         p.mult1 = mult;
         p.G1 = 4;
@@ -1318,7 +1257,7 @@ void recip_tc(Ctx& c) {
     // c.d_tc_atoms was filled, and c.d_tc_cmax cleared, by the packing kernel of this evaluation
     if (p.tpc1 == 1)
         k_tc_sfac2<<<dim3(p.grid1x, p.nsplit1), kT1b, p.smem1, c.stream>>>(
-            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, p.G1, p.rowsc);
+            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.KM, c.d_tc_part, p.rtot, p.G1, p.rowsc);
     else if (p.tpc1 == 4)
         k_tc_sfac<4><<<dim3(p.grid1x, p.nsplit1), P1<4>::kThreads, p.smem1, c.stream>>>(
             v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1, p.rowsc);
