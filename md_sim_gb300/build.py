@@ -20,7 +20,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxe
 # counts and histogram bins match the reference's rounding
 PER_FILE = {"shake.cu": ["-fmad=false"], "measure.cu": ["-fmad=false"],
             # the host integrator follows the reference's arithmetic order, without host FMA fusion
-            "hostgear.cu": ["-Xcompiler", "-ffp-contract=off"]}
+            "hostgear.cu": ["-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp"]}
 
 
 def _nvcc():
@@ -61,7 +61,7 @@ def build(verbose=False, debug=False):
         objs = list(ex.map(lambda s: _compile(s, extra, out), srcs))
     if not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs):
         tmp = lib + ".tmp"
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcuda", "-lgomp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

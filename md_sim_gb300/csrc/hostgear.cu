@@ -9,14 +9,21 @@
 // nriga+1..nliqa, with the Nose-type thermostat of src/move.f90:168-217,356-375.  Surface atoms
 // (nliqa+1..nmove) move in mdg_shake, as in the reference (src/move.f90:376).
 //
-// One host thread, the reference's loops over the molecules; no device memory.  The arithmetic is
-// the reference's operation by operation (this file is compiled without multiply-add
-// contraction), so a drop-in loop reproduces the library's resident steps to rounding.
+// The reference's loops over the molecules, split into contiguous ranges of molecules over the host
+// threads (OpenMP; MDG_HOST_THREADS if set, else all cores the process may run on, one thread
+// below 2,048 molecules): each thread runs every loop on its own range, so a molecule's arrays stay in
+// one core's cache from one loop to the next.  The sums (kinetic energies) run afterwards on one
+// thread in molecule order, so the result does not depend on the thread count.  No device memory.
+// The arithmetic is the reference's operation by operation (this file is compiled without
+// multiply-add contraction), so a drop-in loop reproduces the library's resident steps to rounding.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <new>
 #include <vector>
+
+#include <omp.h>
 
 #include "../../include/mdgpu.h"
 
@@ -26,6 +33,7 @@ struct mdg_host_gear {
     mdg_rigid body{};
     std::vector<double> A;        // rotation matrices, [9][nrig] (a11, a12, ..., a33 of src/config.f90)
     double kp = 0, kw = 0, ke = 0, htot = 0, sft = 0, sfr = 0, uconf = 0;
+    int nthreads = 1;
 };
 
 namespace {
@@ -53,6 +61,18 @@ inline void correct5(double& a0, double& a1, double& a2, double& a3, double& a4,
     a4 = a4 + g4 * c;
 }
 
+// [lo, hi) of thread k of nt over n items
+inline void split_range(int64_t n, int k, int nt, int64_t& lo, int64_t& hi) {
+    lo = n * k / nt;
+    hi = n * (k + 1) / nt;
+}
+
+int host_threads(int64_t nmol) {
+    int nt = nmol < 2048 ? 1 : omp_get_num_procs();
+    if (const char* e = std::getenv("MDG_HOST_THREADS")) nt = std::atoi(e);
+    return std::max(1, std::min(nt, 64));
+}
+
 }  // namespace
 
 extern "C" {
@@ -70,6 +90,7 @@ int mdg_host_gear_create(const mdg_sysdesc* s, const mdg_rigid* body, mdg_host_g
     g->mii.assign(s->mii + s->nriga, s->mii + s->nliqa);
     g->body = *body;
     g->A.assign(9 * (size_t)std::max<int64_t>(s->nrig, 1), 0.0);
+    g->nthreads = host_threads(std::max(s->nrig, s->nliqa - s->nriga));
     *out = g;
     return MDG_OK;
 }
@@ -85,45 +106,38 @@ int mdg_host_predict(mdg_host_gear* g, mdg_state* st) {
     if (!g || !st) return MDG_E_ARG;
     const int64_t nrig = g->nrig, n0 = g->nriga, n1 = g->nliqa;
     const mdg_rigid& b = g->body;
-    double kp = 0.0;
-    for (int64_t i = n0; i < n1; ++i) {
-        predict4(st->x0[i], st->xd[0][i], st->xd[1][i], st->xd[2][i], st->xd[3][i]);
-        predict4(st->y0[i], st->yd[0][i], st->yd[1][i], st->yd[2][i], st->yd[3][i]);
-        predict4(st->z0[i], st->zd[0][i], st->zd[1][i], st->zd[2][i], st->zd[3][i]);
-    }
-    for (int64_t i = n0; i < n1; ++i)
-        kp += g->mi[i - n0] * (st->xd[0][i] * st->xd[0][i] + st->yd[0][i] * st->yd[0][i] + st->zd[0][i] * st->zd[0][i]);
-    // one loop per quantity, in the reference's order (src/move.f90:72-136): each streams a few
-    // arrays, so a host core's prefetchers keep up; every sum runs in molecule order
-    double sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
     double* A = g->A.data();
+#pragma omp parallel num_threads(g->nthreads) if (g->nthreads > 1)
     {
+        const int nt = omp_get_num_threads(), k = omp_get_thread_num();
+        int64_t lo, hi;
+        split_range(n1 - n0, k, nt, lo, hi);
+        for (int64_t i = n0 + lo; i < n0 + hi; ++i) {
+            predict4(st->x0[i], st->xd[0][i], st->xd[1][i], st->xd[2][i], st->xd[3][i]);
+            predict4(st->y0[i], st->yd[0][i], st->yd[1][i], st->yd[2][i], st->yd[3][i]);
+            predict4(st->z0[i], st->zd[0][i], st->zd[1][i], st->zd[2][i], st->zd[3][i]);
+        }
+        // one loop per quantity, in the reference's order (src/move.f90:72-136), each over this
+        // thread's molecules
+        split_range(nrig, k, nt, lo, hi);
         double* const* c3[3] = {st->cx, st->cy, st->cz};
         for (int d = 0; d < 3; ++d) {
             double* const* a = c3[d];
-            for (int64_t i = 0; i < nrig; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
+            for (int64_t i = lo; i < hi; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
         }
-        for (int d = 0; d < 3; ++d)
-            for (int64_t i = 0; i < nrig; ++i) sc[d] += c3[d][1][i] * c3[d][1][i];
-    }
-    {
         double* const* w3[3] = {st->wx, st->wy, st->wz};
         for (int d = 0; d < 3; ++d) {
             double* const* a = w3[d];
-            for (int64_t i = 0; i < nrig; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
+            for (int64_t i = lo; i < hi; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
         }
-        for (int d = 0; d < 3; ++d)
-            for (int64_t i = 0; i < nrig; ++i) sw[d] += w3[d][0][i] * w3[d][0][i];
-    }
-    for (int c = 0; c < 4; ++c) {
-        double* const* a = st->q[c];
-        for (int64_t i = 0; i < nrig; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
-    }
-    {
+        for (int c = 0; c < 4; ++c) {
+            double* const* a = st->q[c];
+            for (int64_t i = lo; i < hi; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
+        }
         double *Q1 = st->q[0][0], *Q2 = st->q[1][0], *Q3 = st->q[2][0], *Q4 = st->q[3][0];
         double* a[9];
-        for (int k = 0; k < 9; ++k) a[k] = A + (size_t)k * nrig;
-        for (int64_t i = 0; i < nrig; ++i) {
+        for (int m = 0; m < 9; ++m) a[m] = A + (size_t)m * nrig;
+        for (int64_t i = lo; i < hi; ++i) {
             double q1 = Q1[i], q2 = Q2[i], q3 = Q3[i], q4 = Q4[i];
             const double cr = 1.0 / std::sqrt(q1 * q1 + q2 * q2 + q3 * q3 + q4 * q4);
             q1 = q1 * cr;
@@ -147,7 +161,7 @@ int mdg_host_predict(mdg_host_gear* g, mdg_state* st) {
         }
         // sites from the centre and the body frame, H offsets from the O (src/move.f90:140-162)
         const double *CX = st->cx[0], *CY = st->cy[0], *CZ = st->cz[0];
-        for (int64_t i = 0; i < nrig; ++i) {
+        for (int64_t i = lo; i < hi; ++i) {
             const int64_t ix = 3 * i;
             for (int j = 0; j < 3; ++j) {
                 st->x0[ix + j] = CX[i] + a[0][i] * b.xbody[j] + a[3][i] * b.ybody[j] + a[6][i] * b.zbody[j];
@@ -159,6 +173,23 @@ int mdg_host_predict(mdg_host_gear* g, mdg_state* st) {
                 st->rsy[ix + j] = st->y0[ix + j] - st->y0[ix];
                 st->rsz[ix + j] = st->z0[ix + j] - st->z0[ix];
             }
+        }
+    }
+    // kinetic sums on one thread, each in molecule order
+    double kp = 0.0;
+    for (int64_t i = n0; i < n1; ++i)
+        kp += g->mi[i - n0] * (st->xd[0][i] * st->xd[0][i] + st->yd[0][i] * st->yd[0][i] + st->zd[0][i] * st->zd[0][i]);
+    double sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
+    {
+        const double *vx = st->cx[1], *vy = st->cy[1], *vz = st->cz[1];
+        const double *wx = st->wx[0], *wy = st->wy[0], *wz = st->wz[0];
+        for (int64_t i = 0; i < nrig; ++i) {
+            sc[0] += vx[i] * vx[i];
+            sc[1] += vy[i] * vy[i];
+            sc[2] += vz[i] * vz[i];
+            sw[0] += wx[i] * wx[i];
+            sw[1] += wy[i] * wy[i];
+            sw[2] += wz[i] * wz[i];
         }
     }
     kp = kp + b.mw * (sc[0] + sc[1] + sc[2]);
@@ -195,67 +226,74 @@ int mdg_host_correct(mdg_host_gear* g, mdg_state* st, const double* ftx, const d
     const double s0i = st->s[0], rs0i = st->rs[0];
     if (n1 > n0 && (!ftx || !fty || !ftz)) return MDG_E_ARG;
     if (nrig > 0 && (!fcx || !fcy || !fcz || !tx || !ty || !tz)) return MDG_E_ARG;
-    for (int64_t i = n0; i < n1; ++i) {
-        const double mii = g->mii[i - n0];
-        const double* f[3] = {ftx, fty, ftz};
-        double* x[3] = {st->x0, st->y0, st->z0};
-        double* const* xd[3] = {st->xd, st->yd, st->zd};
-        for (int d = 0; d < 3; ++d) {
-            const double c = 0.5 * f[d][i - n0] * mii - xd[d][0][i] * s0i - xd[d][1][i];
-            x[d][i] = x[d][i] + kG02 * c;
-            xd[d][0][i] = xd[d][0][i] + kG12 * c;
-            xd[d][1][i] = xd[d][1][i] + c;
-            xd[d][2][i] = xd[d][2][i] + 0.5 * c;
-            xd[d][3][i] = xd[d][3][i] + kG42 * c;
-        }
-    }
     const double rc = 0.5 / b.mw;
     const double inxxi = 1.0 / b.inxx, inyyi = 1.0 / b.inyy, inzzi = 1.0 / b.inzz;
-    // centre (src/move.f90:262-281)
+#pragma omp parallel num_threads(g->nthreads) if (g->nthreads > 1)
     {
-        const double* f3[3] = {fcx, fcy, fcz};
-        double* const* cm[3] = {st->cx, st->cy, st->cz};
-        for (int d = 0; d < 3; ++d) {
-            double* const* a = cm[d];
-            const double* f = f3[d];
-            for (int64_t i = 0; i < nrig; ++i) {
-                const double c = rc * f[i] - a[1][i] * s0i - a[2][i];
-                correct5(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i], c, kG02, kG12, 1.0, 0.5, kG42);
+        const int nt = omp_get_num_threads(), k = omp_get_thread_num();
+        int64_t lo, hi;
+        split_range(n1 - n0, k, nt, lo, hi);
+        for (int64_t i = n0 + lo; i < n0 + hi; ++i) {
+            const double mii = g->mii[i - n0];
+            const double* f[3] = {ftx, fty, ftz};
+            double* x[3] = {st->x0, st->y0, st->z0};
+            double* const* xd[3] = {st->xd, st->yd, st->zd};
+            for (int d = 0; d < 3; ++d) {
+                const double c = 0.5 * f[d][i - n0] * mii - xd[d][0][i] * s0i - xd[d][1][i];
+                x[d][i] = x[d][i] + kG02 * c;
+                xd[d][0][i] = xd[d][0][i] + kG12 * c;
+                xd[d][1][i] = xd[d][1][i] + c;
+                xd[d][2][i] = xd[d][2][i] + 0.5 * c;
+                xd[d][3][i] = xd[d][3][i] + kG42 * c;
             }
         }
-    }
-    // quaternions from the angular velocity before its correction (src/move.f90:283-317)
-    for (int64_t i = 0; i < nrig; ++i) {
-        const double q1 = st->q[0][0][i], q2 = st->q[1][0][i], q3 = st->q[2][0][i], q4 = st->q[3][0][i];
-        const double wx = st->wx[0][i], wy = st->wy[0][i], wz = st->wz[0][i];
-        const double cq[4] = {0.5 * (-q3 * wx - q4 * wy + q2 * wz), 0.5 * (q4 * wx - q3 * wy - q1 * wz),
-                              0.5 * (q1 * wx + q2 * wy + q4 * wz), 0.5 * (-q2 * wx + q1 * wy - q3 * wz)};
-        for (int c = 0; c < 4; ++c) {
-            double* const* a = st->q[c];
-            const double co = cq[c] - a[1][i];
-            correct5(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i], co, kG01, 1.0, kG21, kG31, kG41);
+        split_range(nrig, k, nt, lo, hi);
+        // centre (src/move.f90:262-281)
+        {
+            const double* f3[3] = {fcx, fcy, fcz};
+            double* const* cm[3] = {st->cx, st->cy, st->cz};
+            for (int d = 0; d < 3; ++d) {
+                double* const* a = cm[d];
+                const double* f = f3[d];
+                for (int64_t i = lo; i < hi; ++i) {
+                    const double c = rc * f[i] - a[1][i] * s0i - a[2][i];
+                    correct5(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i], c, kG02, kG12, 1.0, 0.5, kG42);
+                }
+            }
         }
-    }
-    // body angular velocity: Euler's equations with the lab torque rotated into the body frame
-    // (src/move.f90:319-354)
-    {
-        const double* a[9];
-        for (int k = 0; k < 9; ++k) a[k] = g->A.data() + (size_t)k * nrig;
-        for (int64_t i = 0; i < nrig; ++i) {
+        // quaternions from the angular velocity before its correction (src/move.f90:283-317)
+        for (int64_t i = lo; i < hi; ++i) {
+            const double q1 = st->q[0][0][i], q2 = st->q[1][0][i], q3 = st->q[2][0][i], q4 = st->q[3][0][i];
             const double wx = st->wx[0][i], wy = st->wy[0][i], wz = st->wz[0][i];
-            const double t0 = tx[i], t1 = ty[i], t2 = tz[i];
-            double c1 = a[0][i] * t0 + a[1][i] * t1 + a[2][i] * t2;
-            c1 = ((c1 + wy * wz * (b.inyy - b.inzz)) * inxxi) - st->wx[1][i] - rs0i * wx;
-            double c2 = a[3][i] * t0 + a[4][i] * t1 + a[5][i] * t2;
-            c2 = ((c2 + wz * wx * (b.inzz - b.inxx)) * inyyi) - st->wy[1][i] - rs0i * wy;
-            double c3 = a[6][i] * t0 + a[7][i] * t1 + a[8][i] * t2;
-            c3 = ((c3 + wx * wy * (b.inxx - b.inyy)) * inzzi) - st->wz[1][i] - rs0i * wz;
-            correct5(st->wx[0][i], st->wx[1][i], st->wx[2][i], st->wx[3][i], st->wx[4][i], c1, kG01, 1.0, kG21, kG31,
-                     kG41);
-            correct5(st->wy[0][i], st->wy[1][i], st->wy[2][i], st->wy[3][i], st->wy[4][i], c2, kG01, 1.0, kG21, kG31,
-                     kG41);
-            correct5(st->wz[0][i], st->wz[1][i], st->wz[2][i], st->wz[3][i], st->wz[4][i], c3, kG01, 1.0, kG21, kG31,
-                     kG41);
+            const double cq[4] = {0.5 * (-q3 * wx - q4 * wy + q2 * wz), 0.5 * (q4 * wx - q3 * wy - q1 * wz),
+                                  0.5 * (q1 * wx + q2 * wy + q4 * wz), 0.5 * (-q2 * wx + q1 * wy - q3 * wz)};
+            for (int c = 0; c < 4; ++c) {
+                double* const* a = st->q[c];
+                const double co = cq[c] - a[1][i];
+                correct5(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i], co, kG01, 1.0, kG21, kG31, kG41);
+            }
+        }
+        // body angular velocity: Euler's equations with the lab torque rotated into the body frame
+        // (src/move.f90:319-354)
+        {
+            const double* a[9];
+            for (int m = 0; m < 9; ++m) a[m] = g->A.data() + (size_t)m * nrig;
+            for (int64_t i = lo; i < hi; ++i) {
+                const double wx = st->wx[0][i], wy = st->wy[0][i], wz = st->wz[0][i];
+                const double t0 = tx[i], t1 = ty[i], t2 = tz[i];
+                double c1 = a[0][i] * t0 + a[1][i] * t1 + a[2][i] * t2;
+                c1 = ((c1 + wy * wz * (b.inyy - b.inzz)) * inxxi) - st->wx[1][i] - rs0i * wx;
+                double c2 = a[3][i] * t0 + a[4][i] * t1 + a[5][i] * t2;
+                c2 = ((c2 + wz * wx * (b.inzz - b.inxx)) * inyyi) - st->wy[1][i] - rs0i * wy;
+                double c3 = a[6][i] * t0 + a[7][i] * t1 + a[8][i] * t2;
+                c3 = ((c3 + wx * wy * (b.inxx - b.inyy)) * inzzi) - st->wz[1][i] - rs0i * wz;
+                correct5(st->wx[0][i], st->wx[1][i], st->wx[2][i], st->wx[3][i], st->wx[4][i], c1, kG01, 1.0, kG21, kG31,
+                         kG41);
+                correct5(st->wy[0][i], st->wy[1][i], st->wy[2][i], st->wy[3][i], st->wy[4][i], c2, kG01, 1.0, kG21, kG31,
+                         kG41);
+                correct5(st->wz[0][i], st->wz[1][i], st->wz[2][i], st->wz[3][i], st->wz[4][i], c3, kG01, 1.0, kG21, kG31,
+                         kG41);
+            }
         }
     }
     if (b.temper != -1.0) {  // thermostat corrector (src/move.f90:356-375)

@@ -26,8 +26,12 @@ def _state_arrays(s):
     return out
 
 
+@pytest.mark.parametrize("threads", ["1", "3"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_host_integrator_matches_oracle_loop(name, oracle, gpulib):
+def test_host_integrator_matches_oracle_loop(name, threads, oracle, gpulib, monkeypatch):
+    """The host threads split the molecules into ranges; the result does not depend on their
+    number (MDG_HOST_THREADS is read when the integrator is created)."""
+    monkeypatch.setenv("MDG_HOST_THREADS", threads)
     make, steps = CASES[name]
     s, prm = make()
     sa, sb = s.copy(), s.copy()
