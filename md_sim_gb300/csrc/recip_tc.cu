@@ -373,8 +373,8 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
 // chain runs, then write their sums as this CTA's partial [split][lane][row].
 // Every wait is bounded; a timeout anywhere sets a shared abort flag that ends all waits.
 // ---------------------------------------------------------------------------------------------
-constexpr int kW1b = 16;                 // warps
-constexpr int kT1b = kW1b * 32;
+constexpr int kW1b = 16;                 // producer warps
+constexpr int kT1b = kW1b * 32 + 32;     // + the MMA issuer warp (warp 16, lane 0)
 constexpr int kS1b = 3;                  // stages (A and B of one group)
 constexpr uint32_t kBSt = 4 * 8192;      // B: [p][h] tiles of 256 x 16 halves
 constexpr uint32_t kASt = 4 * 4096;      // A: [p][h] tiles of 128 x 16 halves
@@ -453,16 +453,16 @@ __device__ __forceinline__ void split_f2(f2t x, uint32_t& hi, uint32_t& lo) {
 }
 
 __global__ void __launch_bounds__(kT1b, 1)
-    k_tc_sfac2(View v, const uint4* __restrict__ atoms, int chunk, const int4* __restrict__ rows, TcDims d, int KM,
+    k_tc_sfac2(View v, const uint4* __restrict__ atoms, int chunk, const int4* __restrict__ rows, TcDims d,
                float* __restrict__ part, int rtot, int G, float* __restrict__ rowsc) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const P1bLayout L = p1b_layout();
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm);           // [kS1b] stage written (16 warps)
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm);          // [kS1b] stage written (16 warps)
     uint64_t* empty = full + kS1b;                              // [kS1b] stage's MMAs done
-    uint64_t* chainDone = empty + kS1b;                         // [2] accumulation chain's MMAs done
-    uint64_t* drained = chainDone + 2;                          // [2] accumulator read out (16 warps)
-    uint64_t* recbar = drained + 2;                             // records landed
+    uint64_t* chainDone = empty + kS1b;                         // accumulation chain's MMAs done
+    uint64_t* drained = chainDone + 1;                          // chain added to the sums (16 warps)
+    uint64_t* recbar = drained + 1;                             // records landed
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     volatile int* ab = reinterpret_cast<volatile int*>(sm + 520);
     int* err = &v.status[ST_TC_TIMEOUT];
@@ -470,22 +470,19 @@ __global__ void __launch_bounds__(kT1b, 1)
     const int ngroup = a1 > a0 ? (a1 - a0 + kGA - 1) / kGA : 0;
     const int nchain = (ngroup + G - 1) / G;
     const int row0 = blockIdx.x * 256;
-    const uint4* recs = reinterpret_cast<const uint4*>(sm + L.off_rec);
     if (t == 0) {
         for (int i = 0; i < kS1b; ++i) {
             tc::mbar_init(tc::smem_u32(&full[i]), kW1b);
             tc::mbar_init(tc::smem_u32(&empty[i]), 1);
         }
-        for (int i = 0; i < 2; ++i) {
-            tc::mbar_init(tc::smem_u32(&chainDone[i]), 1);
-            tc::mbar_init(tc::smem_u32(&drained[i]), kW1b);
-        }
+        tc::mbar_init(tc::smem_u32(chainDone), 1);
+        tc::mbar_init(tc::smem_u32(drained), kW1b);
         tc::mbar_init(tc::smem_u32(recbar), 1);
         *ab = 0;
         tc::mbar_fence_init();
     }
     // zero the stages (A lanes beyond 2 NN stay zero) and the records (padding atoms: zero
-    // charge, so zero entries)
+    // charge, so zero A entries)
     for (uint32_t o = t * 16; o < L.total - L.off_st; o += kT1b * 16)
         *reinterpret_cast<uint4*>(sm + L.off_st + o) = make_uint4(0, 0, 0, 0);
     if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 512);
@@ -499,150 +496,169 @@ __global__ void __launch_bounds__(kT1b, 1)
         tc::mbar_expect_tx(tc::smem_u32(recbar), bytes);
         tc::bulk_g2s(tc::smem_u32(sm + L.off_rec), atoms + a0, bytes, tc::smem_u32(recbar));
     }
-    // rows: a quarter warp holds 8 consecutive rows of one atom half
-    const int h = (t >> 3) & 1;                       // atoms 8 h .. 8 h + 7 of each group
-    const int r = ((t >> 4) << 3) | (t & 7);          // CTA row
-    const int row = row0 + r;
-    if (blockIdx.y == 0 && h == 0 && row < d.nrow) rowsc[row] = 0.f;  // k_tc_sreduce takes the maximum
-    uint32_t lu = 0, mu = 0;
-    float rmask = 0.f;                                // padding rows: zero entries
-    if (row < d.nrow) {
-        const int4 rw = rows[row];
-        lu = (uint32_t)rw.x;
-        mu = (uint32_t)rw.y;
-        rmask = 1.f;
-    }
-    const uint32_t o8 = tc::tile_off(r, 8 * h);
-    // A item: lane n (of a group of 8) and atom pair jp; a warp covers 8 lanes x 4 pairs of one
-    // core matrix column
-    const int ijp = (t & 3) | (((t >> 5) & 1) << 2);
-    const int ini = ((t >> 6) << 3) | ((t >> 2) & 7);
-    const bool has_item = ini < d.NN;
-    const uint32_t ore = tc::tile_off(ini, 2 * ijp), oim = tc::tile_off(d.NN + ini, 2 * ijp);
-    const uint32_t nfac = (uint32_t)(ini - d.KN);
-    const int q = warp & 3, wq = warp >> 2;           // TMEM lane quarter, column block of the drains
-    float acc[64];
-#pragma unroll
-    for (int i = 0; i < 64; ++i) acc[i] = 0.f;
-    bool alive = a1 <= a0 || wait_ab_warp(tc::smem_u32(recbar), 0, ab, err, 40);
-    int nd = 0;                                        // chains drained
-    auto drain = [&](int c) {
-        const int b = c & 1;
-        alive = wait_ab_warp(tc::smem_u32(&chainDone[b]), (c >> 1) & 1, ab, err, 41);
-        if (!alive) return;
-        tc::fence_after();
-#pragma unroll
-        for (int cc = 0; cc < 4; ++cc) {
-            float raw[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + b * 256 + wq * 64 + cc * 16, raw);
-#pragma unroll
-            for (int i = 0; i < 16; ++i) acc[cc * 16 + i] += raw[i];
+    if (warp < kW1b) {
+        const uint4* recs = reinterpret_cast<const uint4*>(sm + L.off_rec);
+        // B entries: a warp holds 16 consecutive rows, its half warps the two atom halves (a half
+        // warp reads one record; a quarter warp stores 8 rows of one atom half, 128 contiguous bytes)
+        const int h = (t >> 4) & 1;                   // atoms 8 h .. 8 h + 7 of each group
+        const int r = ((t >> 5) << 4) | (t & 15);     // CTA row
+        const int row = row0 + r;
+        if (blockIdx.y == 0 && h == 0 && row < d.nrow) rowsc[row] = 0.f;  // k_tc_sreduce takes the maximum
+        uint32_t lu = 0, mu = 0;                      // padding rows: phase 0 (their sums are not read)
+        if (row < d.nrow) {
+            const int4 rw = rows[row];
+            lu = (uint32_t)rw.x;
+            mu = (uint32_t)rw.y;
         }
-        tc::fence_before();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&drained[b]));
-    };
-    const bool issuer = warp == kW1b - 1 && lane == 0;
-    const uint32_t idesc = idesc_e(128, 256);
-    const uint64_t dS0 = tc::desc(tc::smem_u32(sm + L.off_st));
-    int s = 0, gi = 0, c = 0, issued = -1, is = 0;     // stage, group within the chain, chain
-    uint32_t rnd = 0, irnd = 0;                       // parity of the stage's use
-    for (int g = 0; g < ngroup && alive; ++g) {
-        if (gi == 0 && g >= 2 * G) {
-            drain(nd++);
-            if (!alive) break;
-        }
-        if (g >= kS1b) alive = wait_ab_warp(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
-        if (!alive) break;
-        unsigned char* st = sm + L.off_st + s * kSt1b;
-        const uint4* rc = recs + g * kGA;
-        uint32_t rh[4], rl[4], ih[4], il[4];
+        const uint32_t o8 = tc::tile_off(r, 8 * h);
+        // A item: lane n (of a group of 8) and atom pair jp; a warp covers 8 lanes x 4 pairs of
+        // one core matrix column
+        const int ijp = (t & 3) | (((t >> 5) & 1) << 2);
+        const int ini = ((t >> 6) << 3) | ((t >> 2) & 7);
+        const bool has_item = ini < d.NN;
+        const uint32_t ore = tc::tile_off(ini, 2 * ijp), oim = tc::tile_off(d.NN + ini, 2 * ijp);
+        const uint32_t nfac = (uint32_t)(ini - d.KN);
+        const int q = warp & 3, wq = warp >> 2;       // TMEM lane quarter, column block of the drains
+        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + wq * 64;  // this warp's TMEM block
+        bool alive = a1 <= a0 || wait_ab_warp(tc::smem_u32(recbar), 0, ab, err, 40);
+        int nd = 0;                                    // chains added to the sums
+        // chain c (columns 0-255) added in FP32 to the sums (columns 256-511), then the chain
+        // accumulator is free for the next chain
+        auto drain = [&](int c) {
+            alive = wait_ab_warp(tc::smem_u32(chainDone), (uint32_t)(c & 1), ab, err, 41);
+            if (!alive) return;
+            tc::fence_after();
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint4 r0 = rc[8 * h + 2 * k], r1 = rc[8 * h + 2 * k + 1];
-            float c0, s0, c1, s1;
-            phase(lu * r0.x + mu * r0.y, c0, s0);
-            phase(lu * r1.x + mu * r1.y, c1, s1);
-            const float q0 = __uint_as_float(r0.w) * rmask, q1 = __uint_as_float(r1.w) * rmask;
-            split2(q0 * c0, q1 * c1, rh[k], rl[k]);
-            split2(q0 * s0, q1 * s1, ih[k], il[k]);
-        }
-        *reinterpret_cast<uint4*>(st + 0 * 8192 + o8) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
-        *reinterpret_cast<uint4*>(st + 1 * 8192 + o8) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
-        *reinterpret_cast<uint4*>(st + 2 * 8192 + o8) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
-        *reinterpret_cast<uint4*>(st + 3 * 8192 + o8) = make_uint4(il[0], il[1], il[2], il[3]);
-        if (has_item) {                                // A: e^{i n tz} of two atoms, lanes n and NN + n
-            float c0, s0, c1, s1;
-            phase(nfac * rc[2 * ijp].z, c0, s0);
-            phase(nfac * rc[2 * ijp + 1].z, c1, s1);
-            uint32_t ch, cl, sh, sl;
-            split2(c0, c1, ch, cl);
-            split2(s0, s1, sh, sl);
-            unsigned char* as = st + kBSt;
-            *reinterpret_cast<uint32_t*>(as + 0 * 4096 + ore) = ch;  // part 0: cos / sin
-            *reinterpret_cast<uint32_t*>(as + 0 * 4096 + oim) = sh;
-            *reinterpret_cast<uint32_t*>(as + 1 * 4096 + ore) = cl;
-            *reinterpret_cast<uint32_t*>(as + 1 * 4096 + oim) = sl;
-            *reinterpret_cast<uint32_t*>(as + 2 * 4096 + ore) = sh ^ 0x80008000u;  // part 1: -sin / cos
-            *reinterpret_cast<uint32_t*>(as + 2 * 4096 + oim) = ch;
-            *reinterpret_cast<uint32_t*>(as + 3 * 4096 + ore) = sl ^ 0x80008000u;
-            *reinterpret_cast<uint32_t*>(as + 3 * 4096 + oim) = cl;
-        }
-        tc::fence_async_smem();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&full[s]));
-        if (issuer) {
-            // group g's MMAs, once every warp has written its stage (the drains of the chain two
-            // back came before every warp's entries of the chain's first group)
-            const int b = c & 1;
-            const bool first = gi == 0, last = gi == G - 1 || g == ngroup - 1;
-            bool ok = true;
-            if (first && c >= 2) ok = wait_ab(tc::smem_u32(&drained[b]), ((c >> 1) - 1) & 1, ab, err, 46);
-            if (ok) ok = wait_ab(tc::smem_u32(&full[s]), rnd, ab, err, 47);
-            if (ok) {
-                tc::fence_after();
-                const uint32_t dcol = tmem + b * 256;
-                const uint64_t ds = dS0 + (uint64_t)((s * kSt1b) >> 4);
+            for (int cc = 0; cc < 4; ++cc) {
+                uint32_t raw[16], sum[16];
+                tc::tmem_ld16_nw(tq + cc * 16, raw);
+                if (c > 0) tc::tmem_ld16_nw(tq + 256 + cc * 16, sum);
+                tc::tmem_wait_ld();
+                if (c > 0) {
 #pragma unroll
-                for (int p = 0; p < 2; ++p) {
-                    const uint64_t bh = ds + (uint64_t)(((p * 2 + 0) * 8192) >> 4);
-                    const uint64_t bl = ds + (uint64_t)(((p * 2 + 1) * 8192) >> 4);
-                    const uint64_t ah = ds + (uint64_t)((kBSt + (p * 2 + 0) * 4096) >> 4);
-                    const uint64_t al = ds + (uint64_t)((kBSt + (p * 2 + 1) * 4096) >> 4);
-                    tc::mma_bf16(dcol, ah, bh, idesc, (first && p == 0) ? 0u : 1u);
-                    tc::mma_bf16(dcol, ah, bl, idesc, 1u);
-                    tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                    for (int i = 0; i < 16; ++i) raw[i] = __float_as_uint(__uint_as_float(raw[i]) + __uint_as_float(sum[i]));
                 }
-                tc::commit(tc::smem_u32(&empty[s]));
-                if (last) tc::commit(tc::smem_u32(&chainDone[b]));
-                issued = g;
-                is = s;
-                irnd = rnd;
+                tc::tmem_st16(tq + 256 + cc * 16, raw);
             }
-            if (!ok) *ab = 1;
-        }
-        alive = __shfl_sync(0xffffffffu, *ab == 0 ? 1 : 0, 0) != 0;  // warp-uniform
-        if (++s == kS1b) {
-            s = 0;
-            rnd ^= 1u;
-        }
-        if (++gi == G) {
-            gi = 0;
-            ++c;
-        }
-    }
-    while (alive && nd < nchain) drain(nd++);
-    // this CTA's partial: lane (re|im, n) of the quarter, 64 consecutive rows
-    const int lanei = q * 32 + lane;
-    if (alive && !*ab && lanei < 2 * d.NN) {
-        float4* dst = reinterpret_cast<float4*>(part + (size_t)blockIdx.y * d.NP * rtot + (size_t)lanei * rtot +
-                                                row0 + wq * 64);
+            tc::tmem_wait_st();
+            tc::fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(tc::smem_u32(drained));
+        };
+        int s = 0, gi = 0;                             // stage, group within the chain
+        uint32_t rnd = 0;                             // parity of the stage's use
+        for (int g = 0; g < ngroup && alive; ++g) {
+            if (gi == 1 && g > G) {  // one group into chain c + 1: chain c's MMAs are (nearly) done
+                drain(nd++);
+                if (!alive) break;
+            }
+            if (g >= kS1b) alive = wait_ab_warp(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
+            if (!alive) break;
+            unsigned char* st = sm + L.off_st + s * kSt1b;
+            const uint4* rc = recs + g * kGA;
+            uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) dst[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
+            for (int k = 0; k < 4; ++k) {
+                const uint2 r0 = *reinterpret_cast<const uint2*>(&rc[8 * h + 2 * k]);
+                const uint2 r1 = *reinterpret_cast<const uint2*>(&rc[8 * h + 2 * k + 1]);
+                float c0, s0, c1, s1;
+                phase(lu * r0.x + mu * r0.y, c0, s0);
+                phase(lu * r1.x + mu * r1.y, c1, s1);
+                split2(c0, c1, rh[k], rl[k]);
+                split2(s0, s1, ih[k], il[k]);
+            }
+            *reinterpret_cast<uint4*>(st + 0 * 8192 + o8) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+            *reinterpret_cast<uint4*>(st + 1 * 8192 + o8) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+            *reinterpret_cast<uint4*>(st + 2 * 8192 + o8) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+            *reinterpret_cast<uint4*>(st + 3 * 8192 + o8) = make_uint4(il[0], il[1], il[2], il[3]);
+            if (has_item) {  // A: q e^{i n tz} of two atoms, lanes n and NN + n
+                const uint2 z0 = *reinterpret_cast<const uint2*>(&rc[2 * ijp].z);
+                const uint2 z1 = *reinterpret_cast<const uint2*>(&rc[2 * ijp + 1].z);
+                float c0, s0, c1, s1;
+                phase(nfac * z0.x, c0, s0);
+                phase(nfac * z1.x, c1, s1);
+                const float q0 = __uint_as_float(z0.y), q1 = __uint_as_float(z1.y);
+                uint32_t ch, cl, sh, sl;
+                split2(q0 * c0, q1 * c1, ch, cl);
+                split2(q0 * s0, q1 * s1, sh, sl);
+                unsigned char* as = st + kBSt;
+                *reinterpret_cast<uint32_t*>(as + 0 * 4096 + ore) = ch;  // part 0: cos / sin
+                *reinterpret_cast<uint32_t*>(as + 0 * 4096 + oim) = sh;
+                *reinterpret_cast<uint32_t*>(as + 1 * 4096 + ore) = cl;
+                *reinterpret_cast<uint32_t*>(as + 1 * 4096 + oim) = sl;
+                *reinterpret_cast<uint32_t*>(as + 2 * 4096 + ore) = sh ^ 0x80008000u;  // part 1: -sin / cos
+                *reinterpret_cast<uint32_t*>(as + 2 * 4096 + oim) = ch;
+                *reinterpret_cast<uint32_t*>(as + 3 * 4096 + ore) = sl ^ 0x80008000u;
+                *reinterpret_cast<uint32_t*>(as + 3 * 4096 + oim) = cl;
+            }
+            tc::fence_async_smem();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(tc::smem_u32(&full[s]));
+            alive = __shfl_sync(0xffffffffu, *ab == 0 ? 1 : 0, 0) != 0;  // warp-uniform
+            if (++s == kS1b) {
+                s = 0;
+                rnd ^= 1u;
+            }
+            if (++gi == G) gi = 0;
+        }
+        while (alive && nd < nchain) drain(nd++);
+        // this CTA's partial: lane (re|im, n) of the quarter, 64 consecutive rows
+        const int lanei = q * 32 + lane;
+        if (__shfl_sync(0xffffffffu, (alive && !*ab) ? 1 : 0, 0)) {  // warp-uniform: the loads are collective
+            tc::fence_after();
+            float4* dst = reinterpret_cast<float4*>(part + (size_t)blockIdx.y * d.NP * rtot + (size_t)lanei * rtot +
+                                                    row0 + wq * 64);
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                float sum[16];
+                tc::tmem_ld16(tq + 256 + cc * 16, sum);
+                if (lanei < 2 * d.NN)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        dst[cc * 4 + i] = make_float4(sum[4 * i], sum[4 * i + 1], sum[4 * i + 2], sum[4 * i + 3]);
+            }
+        }
+    } else if (lane == 0) {
+        // the issuer: group g's 6 MMAs once the 16 producer warps have written its stage (and,
+        // at a chain's start, added the previous chain to the sums); it produces nothing, so an
+        // issue that waits for room in the MMA queue delays no entries
+        const uint32_t idesc = idesc_e(128, 256);
+        const uint64_t dS0 = tc::desc(tc::smem_u32(sm + L.off_st));
+        int s = 0, gi = 0, c = 0, ls = -1;
+        uint32_t rnd = 0, lr = 0;
+        for (int g = 0; g < ngroup; ++g) {
+            if (!wait_ab(tc::smem_u32(&full[s]), rnd, ab, err, 47)) break;
+            if (gi == 0 && c > 0 && !wait_ab(tc::smem_u32(drained), (uint32_t)((c - 1) & 1), ab, err, 48)) break;
+            tc::fence_after();
+            const bool first = gi == 0, last = gi == G - 1 || g == ngroup - 1;
+            const uint64_t ds = dS0 + (uint64_t)((s * kSt1b) >> 4);
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                const uint64_t bh = ds + (uint64_t)(((p * 2 + 0) * 8192) >> 4);
+                const uint64_t bl = ds + (uint64_t)(((p * 2 + 1) * 8192) >> 4);
+                const uint64_t ah = ds + (uint64_t)((kBSt + (p * 2 + 0) * 4096) >> 4);
+                const uint64_t al = ds + (uint64_t)((kBSt + (p * 2 + 1) * 4096) >> 4);
+                tc::mma_bf16(tmem, ah, bh, idesc, (first && p == 0) ? 0u : 1u);
+                tc::mma_bf16(tmem, ah, bl, idesc, 1u);
+                tc::mma_bf16(tmem, al, bh, idesc, 1u);
+            }
+            tc::commit(tc::smem_u32(&empty[s]));
+            if (last) tc::commit(tc::smem_u32(chainDone));
+            ls = s;
+            lr = rnd;
+            if (++s == kS1b) {
+                s = 0;
+                rnd ^= 1u;
+            }
+            if (++gi == G) {
+                gi = 0;
+                ++c;
+            }
+        }
+        // let the issued MMAs and the record copy finish (bounded) before the block frees its TMEM
+        if (ls >= 0) tc::mbar_wait(tc::smem_u32(&empty[ls]), lr, nullptr, 0);
+        if (a1 > a0) tc::mbar_wait(tc::smem_u32(recbar), 0, nullptr, 0);
     }
-    // let the issued MMAs (and the record copy) finish (bounded) before the block frees its TMEM
-    if (issuer && issued >= 0) tc::mbar_wait(tc::smem_u32(&empty[is]), irnd, nullptr, 0);
-    if (t == 0 && a1 > a0 && !alive) tc::mbar_wait(tc::smem_u32(recbar), 0, nullptr, 0);
     tc::fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -1103,7 +1119,7 @@ int tc_plan_pass1(Ctx& c, int tpc, int mult) {
         if (p.chunk1 > kMaxChunk1b) return 1;
         p.nsplit1 = std::max(1, (v.nmove + p.chunk1 - 1) / p.chunk1);
         p.mult1 = mult;
-        p.G1 = 4;
+        p.G1 = 8;
         return 0;
     }
     if (tpc == 4 && p.NP > 128) return 1;
@@ -1257,7 +1273,7 @@ void recip_tc(Ctx& c) {
     // c.d_tc_atoms was filled, and c.d_tc_cmax cleared, by the packing kernel of this evaluation
     if (p.tpc1 == 1)
         k_tc_sfac2<<<dim3(p.grid1x, p.nsplit1), kT1b, p.smem1, c.stream>>>(
-            v, c.d_tc_atoms, p.chunk1, ks.row, d, p.KM, c.d_tc_part, p.rtot, p.G1, p.rowsc);
+            v, c.d_tc_atoms, p.chunk1, ks.row, d, c.d_tc_part, p.rtot, p.G1, p.rowsc);
     else if (p.tpc1 == 4)
         k_tc_sfac<4><<<dim3(p.grid1x, p.nsplit1), P1<4>::kThreads, p.smem1, c.stream>>>(
             v, c.d_tc_atoms, p.chunk1, ks.row, d, p.NM, p.KM, c.d_tc_part, p.rtot, (uint32_t)p.ncols1, p.rowsc);
