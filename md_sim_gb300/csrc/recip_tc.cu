@@ -813,15 +813,17 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
 //
 // One CTA per 128 atoms.  The CTA builds A = e^{i n tz} of its atoms (K = 2 (n + KN) + part) and
 // walks the chunk images of C (32 rows each: N = 128 columns = T and T' x re/im), double-buffered:
-// the issuer thread starts the copy of chunk c + 1 as soon as the MMAs of chunk c are issued (its
-// stage is free once the MMAs of chunk c - 1 are done), so the copy overlaps the MMAs; per chunk
-// 3 (hi/lo) products per K step accumulate into one of two TMEM accumulators, which the four
-// epilogue warps (one thread per atom) drain while the next chunk runs.  Per row the epilogue
+// a copier warp starts the copy of chunk c + 1 as soon as the MMAs of chunk c - 1 are done (its
+// stage is then free), so the copy overlaps the MMAs of chunk c; the issuer warp is a separate
+// warp because an issue waits for room in the tensor core's queue (about 640 cycles of work), and
+// a copy started after the issue of a chunk (21 MMAs, 1344 cycles) began too late to land before
+// that chunk ended.  Per chunk 3 (hi/lo) products per K step accumulate into one of two TMEM
+// accumulators, which the epilogue warps drain while the next chunk runs.  Per row the epilogue
 // forms Im(e^{i(l tx + m ty)} T) with the row phase advanced along m by a complex multiply
 // (recomputed by __sincosf at rows flagged in the shared row table: every 8th row and each change
 // of l).
 // ---------------------------------------------------------------------------------------------
-constexpr int kT2 = 288;  // epilogue warps 0-7 (two per TMEM lane quarter, one per half chunk), issuer warp 8
+constexpr int kT2 = 320;  // epilogue warps 0-7 (two per TMEM lane quarter, one per half chunk), issuer warp 8, copier warp 9
 
 struct P2Layout {
     uint32_t a_bytes, img, off_a, off_b, off_rows, off_rsc, off_red, total;
@@ -907,23 +909,36 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    if (warp == 8) {
+    const bool two = d.nst2 == 2;
+    if (warp == 9) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_e(128, kNC2);
+            // the copier: chunk c's image into its stage as soon as the MMAs that read the stage
+            // before (chunk c - 2, or c - 1 with one stage) are done, independently of the issuer,
+            // whose issue waits for room in the tensor core's queue
             const uint32_t bbase = tc::smem_u32(sm + L.off_b);
-            const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(bbase);
-            const bool two = d.nst2 == 2;
-            auto copy = [&](int c) {  // c: index within this item's chunks
+            int last = -1;
+            for (int c = 0; c < NC; ++c) {
                 const int s = two ? (c & 1) : 0;
+                const int cp = two ? c - 2 : c - 1;  // the chunk whose MMAs last read the stage
+                if (cp >= 0 && !tc::mbar_wait(tc::smem_u32(&mdone[cp & 1]), (uint32_t)((cp >> 1) & 1), err, 21)) break;
                 const int4 ch = chunks[c0 + c];
                 const uint32_t bytes = (uint32_t)ch.z * kTile2;  // hi half, then lo half
                 const uint32_t fb = tc::smem_u32(&full[s]);
                 tc::mbar_expect_tx(fb, 2 * bytes);
                 tc::bulk_g2s(bbase + s * L.img, img + ch.x, bytes, fb);
                 tc::bulk_g2s(bbase + s * L.img + bytes, img + ch.x + bytes, bytes, fb);
-            };
+                last = c;
+            }
+            // the last copy lands (bounded) before the block can exit
+            if (last >= 0)
+                tc::mbar_wait(tc::smem_u32(&full[two ? (last & 1) : 0]), (uint32_t)(two ? ((last >> 1) & 1) : (last & 1)),
+                              nullptr, 0);
+        }
+    } else if (warp == 8) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_e(128, kNC2);
+            const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(tc::smem_u32(sm + L.off_b));
             bool alive = true;
-            if (NC > 0) copy(0);
             for (int c = 0; c < NC && alive; ++c) {
                 const int s = c & 1;              // accumulator
                 const int sb = two ? s : 0;       // chunk image stage
@@ -944,14 +959,6 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                     tc::mma_bf16(dcol, al, bh, idesc, 1u);
                 }
                 tc::commit(tc::smem_u32(&mdone[s]));
-                // next chunk's copy: into the other stage once the MMAs of chunk c - 1 are done, or
-                // with one stage, into the same stage once those of chunk c are done
-                if (c + 1 < NC) {
-                    if (two && c >= 1) alive = tc::mbar_wait(tc::smem_u32(&mdone[s ^ 1]), ((c - 1) >> 1) & 1, err, 21);
-                    if (!two) alive = tc::mbar_wait(tc::smem_u32(&mdone[s]), (c >> 1) & 1, err, 21);
-                    if (!alive) break;
-                    copy(c + 1);
-                }
             }
             // on a timeout, let issued work drain (bounded) before the block frees its TMEM
             if (!alive && NC > 0) tc::mbar_wait(tc::smem_u32(&mdone[(NC - 1) & 1]), ((NC - 1) >> 1) & 1, nullptr, 0);
