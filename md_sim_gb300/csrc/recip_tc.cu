@@ -826,7 +826,7 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
 constexpr int kT2 = 320;  // epilogue warps 0-7 (two per TMEM lane quarter, one per half chunk), issuer warp 8, copier warp 9
 
 struct P2Layout {
-    uint32_t a_bytes, img, off_a, off_b, off_rows, off_rsc, off_red, total;
+    uint32_t a_bytes, img, off_a, off_b, off_rows, off_rsc, off_red, off_ch, total;
 };
 
 __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
@@ -838,7 +838,8 @@ __host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
     L.off_rows = L.off_b + nst * L.img;
     L.off_rsc = L.off_rows + nrow_pad * 16;    // rows: (float l, float m, l | restart << 31, m)
     L.off_red = L.off_rsc + nrow_pad * 4;      // row scales of this evaluation
-    L.total = L.off_red + 3 * 128 * 4;         // second-half force partials of the 128 atoms
+    L.off_ch = L.off_red + 3 * 128 * 4;         // second-half force partials of the 128 atoms
+    L.total = L.off_ch + 16 * nrow_pad / kRC;   // the chunk table (an L2 round trip per chunk otherwise)
     return L;
 }
 
@@ -861,6 +862,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     const int atom0 = item.x * 128;
     const int c0 = item.y, NC = item.z - item.y;
     const int NCT = d.nchunk2;
+    int4* chs = reinterpret_cast<int4*>(sm + L.off_ch);  // this item's chunks
     if (t == 0) {
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(tc::smem_u32(&full[b]), 1);
@@ -869,59 +871,22 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
         }
         tc::mbar_fence_init();
     }
-    for (int r = t; r < NCT * kRC; r += kT2) {
-        const int4 rw = r < d.nrow ? rows[r] : make_int4(0, 0, 0, 0);
-        int restart = (r & 7) == 0 || r >= d.nrow;
-        if (!restart) {
-            const int4 pw = rows[r - 1];  // 0 < r < nrow here
-            restart = pw.x != rw.x || pw.y + 1 != rw.y;
-        }
-        rlm[r] = make_float4((float)rw.x, (float)rw.y, __int_as_float(rw.x | (restart << 31)), __int_as_float(rw.y));
-        rsc[r] = rsc_g[r];
-    }
-    if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 256);
-    // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part (warps 0-7, half of K each)
-    if (t < 256) {
-        const int mrow = t & 127, half = t >> 7;
-        const int at = atom0 + mrow;
-        const uint32_t uz = at < v.nmove ? atoms[at].z : 0u;
-        const int ksplit = (d.KS + 1) / 2;
-        const int ks0 = half ? ksplit : 0, ks1 = half ? d.KS : ksplit;
-        for (int ks = ks0; ks < ks1; ++ks) {
-            uint32_t wh[8], wl[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int ni = ks * 8 + i;
-                float c = 0.f, s = 0.f;
-                if (at < v.nmove && ni < d.NN) phase((uint32_t)(ni - d.KN) * uz, c, s);
-                split2(c, s, wh[i], wl[i]);
-            }
-            unsigned char* th = sm + L.off_a + (0 * d.KS + ks) * 4096;
-            unsigned char* tlo = sm + L.off_a + (1 * d.KS + ks) * 4096;
-            *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 0)) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
-            *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 8)) = make_uint4(wh[4], wh[5], wh[6], wh[7]);
-            *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 0)) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
-            *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 8)) = make_uint4(wl[4], wl[5], wl[6], wl[7]);
-        }
-    }
-    tc::fence_async_smem();
-    tc::fence_before();
+    for (int c = t; c < NC; c += kT2) chs[c] = chunks[c0 + c];
     __syncthreads();
-    tc::fence_after();
-    const uint32_t tmem = *tslot;
     const bool two = d.nst2 == 2;
     if (warp == 9) {
         if (lane == 0) {
             // the copier: chunk c's image into its stage as soon as the MMAs that read the stage
             // before (chunk c - 2, or c - 1 with one stage) are done, independently of the issuer,
-            // whose issue waits for room in the tensor core's queue
+            // whose issue waits for room in the tensor core's queue; the first copies overlap the
+            // other warps' set-up
             const uint32_t bbase = tc::smem_u32(sm + L.off_b);
             int last = -1;
             for (int c = 0; c < NC; ++c) {
                 const int s = two ? (c & 1) : 0;
                 const int cp = two ? c - 2 : c - 1;  // the chunk whose MMAs last read the stage
                 if (cp >= 0 && !tc::mbar_wait(tc::smem_u32(&mdone[cp & 1]), (uint32_t)((cp >> 1) & 1), err, 21)) break;
-                const int4 ch = chunks[c0 + c];
+                const int4 ch = chs[c];
                 const uint32_t bytes = (uint32_t)ch.z * kTile2;  // hi half, then lo half
                 const uint32_t fb = tc::smem_u32(&full[s]);
                 tc::mbar_expect_tx(fb, 2 * bytes);
@@ -934,112 +899,155 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 tc::mbar_wait(tc::smem_u32(&full[two ? (last & 1) : 0]), (uint32_t)(two ? ((last >> 1) & 1) : (last & 1)),
                               nullptr, 0);
         }
-    } else if (warp == 8) {
-        if (lane == 0) {
-            const uint32_t idesc = idesc_e(128, kNC2);
-            const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(tc::smem_u32(sm + L.off_b));
+    } else {
+        constexpr int kTS = 9 * 32;  // threads of the set-up: all warps but the copier
+        for (int r = t; r < NCT * kRC; r += kTS) {
+            const int4 rw = r < d.nrow ? rows[r] : make_int4(0, 0, 0, 0);
+            int restart = (r & 7) == 0 || r >= d.nrow;
+            if (!restart) {
+                const int4 pw = rows[r - 1];  // 0 < r < nrow here
+                restart = pw.x != rw.x || pw.y + 1 != rw.y;
+            }
+            rlm[r] = make_float4((float)rw.x, (float)rw.y, __int_as_float(rw.x | (restart << 31)), __int_as_float(rw.y));
+            rsc[r] = rsc_g[r];
+        }
+        if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 256);
+        // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part (warps 0-7, half of K each)
+        if (t < 256) {
+            const int mrow = t & 127, half = t >> 7;
+            const int at = atom0 + mrow;
+            const uint32_t uz = at < v.nmove ? atoms[at].z : 0u;
+            const int ksplit = (d.KS + 1) / 2;
+            const int ks0 = half ? ksplit : 0, ks1 = half ? d.KS : ksplit;
+            for (int ks = ks0; ks < ks1; ++ks) {
+                uint32_t wh[8], wl[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int ni = ks * 8 + i;
+                    float c = 0.f, s = 0.f;
+                    if (at < v.nmove && ni < d.NN) phase((uint32_t)(ni - d.KN) * uz, c, s);
+                    split2(c, s, wh[i], wl[i]);
+                }
+                unsigned char* th = sm + L.off_a + (0 * d.KS + ks) * 4096;
+                unsigned char* tlo = sm + L.off_a + (1 * d.KS + ks) * 4096;
+                *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 0)) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+                *reinterpret_cast<uint4*>(th + tc::tile_off(mrow, 8)) = make_uint4(wh[4], wh[5], wh[6], wh[7]);
+                *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 0)) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+                *reinterpret_cast<uint4*>(tlo + tc::tile_off(mrow, 8)) = make_uint4(wl[4], wl[5], wl[6], wl[7]);
+            }
+        }
+        tc::fence_async_smem();
+        tc::fence_before();
+        tc::named_sync(2, kTS);
+        tc::fence_after();
+        const uint32_t tmem = *tslot;
+        if (warp == 8) {
+            if (lane == 0) {
+                const uint32_t idesc = idesc_e(128, kNC2);
+                const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(tc::smem_u32(sm + L.off_b));
+                bool alive = true;
+                for (int c = 0; c < NC && alive; ++c) {
+                    const int s = c & 1;              // accumulator
+                    const int sb = two ? s : 0;       // chunk image stage
+                    alive = tc::mbar_wait(tc::smem_u32(&full[sb]), two ? ((c >> 1) & 1) : (c & 1), err, 22);
+                    if (!alive) break;
+                    if (c >= 2) alive = tc::mbar_wait(tc::smem_u32(&afree[s]), ((c >> 1) - 1) & 1, err, 23);
+                    if (!alive) break;
+                    tc::fence_after();
+                    const uint32_t dcol = tmem + s * kNC2;
+                    const uint64_t dB = dB0 + (uint64_t)((sb * L.img) >> 4);
+                    const int4 ch = chs[c];
+                    for (int ksl = 0; ksl < ch.z; ++ksl) {
+                        const int ks = ch.y + ksl;
+                        const uint64_t ah = dA0 + (uint64_t)(ks * 256), al = dA0 + (uint64_t)((d.KS + ks) * 256);
+                        const uint64_t bh = dB + (uint64_t)(ksl * (kTile2 >> 4)), bl = dB + (uint64_t)((ch.z + ksl) * (kTile2 >> 4));
+                        tc::mma_bf16(dcol, ah, bh, idesc, ksl > 0 ? 1u : 0u);
+                        tc::mma_bf16(dcol, ah, bl, idesc, 1u);
+                        tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                    }
+                    tc::commit(tc::smem_u32(&mdone[s]));
+                }
+                // on a timeout, let issued work drain (bounded) before the block frees its TMEM
+                if (!alive && NC > 0) tc::mbar_wait(tc::smem_u32(&mdone[(NC - 1) & 1]), ((NC - 1) >> 1) & 1, nullptr, 0);
+            }
+        } else {
+            // warp w reads TMEM lanes 32 (w & 3) .. + 31 (its atoms) and the half chunk w >> 2 (16 rows)
+            const int quad = warp & 3, hf = warp >> 2;
+            const int at = atom0 + quad * 32 + lane;
+            const bool ok = at < v.nmove;
+            const uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
+            float dyc, dys;
+            phase(rec.y, dyc, dys);
+            float fx = 0.f, fy = 0.f, fz = 0.f;
             bool alive = true;
             for (int c = 0; c < NC && alive; ++c) {
-                const int s = c & 1;              // accumulator
-                const int sb = two ? s : 0;       // chunk image stage
-                alive = tc::mbar_wait(tc::smem_u32(&full[sb]), two ? ((c >> 1) & 1) : (c & 1), err, 22);
-                if (!alive) break;
-                if (c >= 2) alive = tc::mbar_wait(tc::smem_u32(&afree[s]), ((c >> 1) - 1) & 1, err, 23);
+                const int s = c & 1;
+                alive = tc::mbar_wait_warp(tc::smem_u32(&mdone[s]), (c >> 1) & 1, err, 24);
                 if (!alive) break;
                 tc::fence_after();
-                const uint32_t dcol = tmem + s * kNC2;
-                const uint64_t dB = dB0 + (uint64_t)((sb * L.img) >> 4);
-                const int4 ch = chunks[c0 + c];
-                for (int ksl = 0; ksl < ch.z; ++ksl) {
-                    const int ks = ch.y + ksl;
-                    const uint64_t ah = dA0 + (uint64_t)(ks * 256), al = dA0 + (uint64_t)((d.KS + ks) * 256);
-                    const uint64_t bh = dB + (uint64_t)(ksl * (kTile2 >> 4)), bl = dB + (uint64_t)((ch.z + ksl) * (kTile2 >> 4));
-                    tc::mma_bf16(dcol, ah, bh, idesc, ksl > 0 ? 1u : 0u);
-                    tc::mma_bf16(dcol, ah, bl, idesc, 1u);
-                    tc::mma_bf16(dcol, al, bh, idesc, 1u);
-                }
-                tc::commit(tc::smem_u32(&mdone[s]));
-            }
-            // on a timeout, let issued work drain (bounded) before the block frees its TMEM
-            if (!alive && NC > 0) tc::mbar_wait(tc::smem_u32(&mdone[(NC - 1) & 1]), ((NC - 1) >> 1) & 1, nullptr, 0);
-        }
-    } else {
-        // warp w reads TMEM lanes 32 (w & 3) .. + 31 (its atoms) and the half chunk w >> 2 (16 rows)
-        const int quad = warp & 3, hf = warp >> 2;
-        const int at = atom0 + quad * 32 + lane;
-        const bool ok = at < v.nmove;
-        const uint4 rec = ok ? atoms[at] : make_uint4(0, 0, 0, 0);
-        float dyc, dys;
-        phase(rec.y, dyc, dys);
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        bool alive = true;
-        for (int c = 0; c < NC && alive; ++c) {
-            const int s = c & 1;
-            alive = tc::mbar_wait_warp(tc::smem_u32(&mdone[s]), (c >> 1) & 1, err, 24);
-            if (!alive) break;
-            tc::fence_after();
-            {
-                uint32_t raw[64];
+                {
+                    uint32_t raw[64];
 #pragma unroll
-                for (int cc = 0; cc < 4; ++cc)
-                    tc::tmem_ld16_nw(tmem + ((uint32_t)(quad * 32) << 16) + s * kNC2 + hf * 64 + cc * 16, raw + cc * 16);
-                tc::tmem_wait_ld();
-                tc::fence_before();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(tc::smem_u32(&afree[s]));
-                float ec = 0.f, es = 0.f;
+                    for (int cc = 0; cc < 4; ++cc)
+                        tc::tmem_ld16_nw(tmem + ((uint32_t)(quad * 32) << 16) + s * kNC2 + hf * 64 + cc * 16, raw + cc * 16);
+                    tc::tmem_wait_ld();
+                    tc::fence_before();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(tc::smem_u32(&afree[s]));
+                    float ec = 0.f, es = 0.f;
 #pragma unroll
-                for (int rr = 0; rr < 16; ++rr) {
-                    const float4 lm = rlm[(c0 + c) * kRC + hf * 16 + rr];
-                    const float scr = rsc[(c0 + c) * kRC + hf * 16 + rr];
-                    const int lb = __float_as_int(lm.z);
-                    if (rr == 0 || lb < 0) {
-                        phase((uint32_t)(lb & 0x7fffffff) * rec.x + (uint32_t)__float_as_int(lm.w) * rec.y, ec, es);
-                    } else {
-                        const float nc = ec * dyc - es * dys;
-                        es = ec * dys + es * dyc;
-                        ec = nc;
+                    for (int rr = 0; rr < 16; ++rr) {
+                        const float4 lm = rlm[(c0 + c) * kRC + hf * 16 + rr];
+                        const float scr = rsc[(c0 + c) * kRC + hf * 16 + rr];
+                        const int lb = __float_as_int(lm.z);
+                        if (rr == 0 || lb < 0) {
+                            phase((uint32_t)(lb & 0x7fffffff) * rec.x + (uint32_t)__float_as_int(lm.w) * rec.y, ec, es);
+                        } else {
+                            const float nc = ec * dyc - es * dys;
+                            es = ec * dys + es * dyc;
+                            ec = nc;
+                        }
+                        const float v0 = __uint_as_float(raw[rr * 4 + 0]), v1 = __uint_as_float(raw[rr * 4 + 1]);
+                        const float v2 = __uint_as_float(raw[rr * 4 + 2]), v3 = __uint_as_float(raw[rr * 4 + 3]);
+                        const float s0 = (ec * v1 + es * v0) * scr;
+                        fx = fmaf(lm.x, s0, fx);
+                        fy = fmaf(lm.y, s0, fy);
+                        fz = fmaf(ec * v3 + es * v2, scr, fz);
                     }
-                    const float v0 = __uint_as_float(raw[rr * 4 + 0]), v1 = __uint_as_float(raw[rr * 4 + 1]);
-                    const float v2 = __uint_as_float(raw[rr * 4 + 2]), v3 = __uint_as_float(raw[rr * 4 + 3]);
-                    const float s0 = (ec * v1 + es * v0) * scr;
-                    fx = fmaf(lm.x, s0, fx);
-                    fy = fmaf(lm.y, s0, fy);
-                    fz = fmaf(ec * v3 + es * v2, scr, fz);
                 }
             }
-        }
-        // the second-half warps hand their partial sums to the first-half warps through shared memory
-        float* red = reinterpret_cast<float*>(sm + L.off_red);
-        const int ra = quad * 32 + lane;
-        if (hf == 1) {
-            red[ra] = alive ? fx : 0.f;
-            red[128 + ra] = alive ? fy : 0.f;
-            red[256 + ra] = alive ? fz : 0.f;
-        }
-        tc::named_sync(1, 256);
-        if (hf == 0 && ok) {  // a whole tile's atoms have one writer: plain stores; pieces add
-            fx += red[ra];       // (a timed-out block leaves zeros and its status)
-            fy += red[128 + ra];
-            fz += red[256 + ra];
-            const double q = alive ? (double)__uint_as_float(rec.w) : 0.0;
-            const double gx = q * (double)d.px * (double)fx, gy = q * (double)d.py * (double)fy,
-                         gz = q * (double)d.pz * (double)fz;
-            if (item.w) {
-                frc[at] = gx;
-                frc[v.nmove + at] = gy;
-                frc[2 * v.nmove + at] = gz;
-            } else {
-                atomicAdd(&frc[at], gx);
-                atomicAdd(&frc[v.nmove + at], gy);
-                atomicAdd(&frc[2 * v.nmove + at], gz);
+            // the second-half warps hand their partial sums to the first-half warps through shared memory
+            float* red = reinterpret_cast<float*>(sm + L.off_red);
+            const int ra = quad * 32 + lane;
+            if (hf == 1) {
+                red[ra] = alive ? fx : 0.f;
+                red[128 + ra] = alive ? fy : 0.f;
+                red[256 + ra] = alive ? fz : 0.f;
+            }
+            tc::named_sync(1, 256);
+            if (hf == 0 && ok) {  // a whole tile's atoms have one writer: plain stores; pieces add
+                fx += red[ra];       // (a timed-out block leaves zeros and its status)
+                fy += red[128 + ra];
+                fz += red[256 + ra];
+                const double q = alive ? (double)__uint_as_float(rec.w) : 0.0;
+                const double gx = q * (double)d.px * (double)fx, gy = q * (double)d.py * (double)fy,
+                             gz = q * (double)d.pz * (double)fz;
+                if (item.w) {
+                    frc[at] = gx;
+                    frc[v.nmove + at] = gy;
+                    frc[2 * v.nmove + at] = gz;
+                } else {
+                    atomicAdd(&frc[at], gx);
+                    atomicAdd(&frc[v.nmove + at], gy);
+                    atomicAdd(&frc[2 * v.nmove + at], gz);
+                }
             }
         }
     }
     __syncthreads();
     if (warp == 0) {
         tc::fence_after();
-        tc::tmem_dealloc(tmem, 256);
+        tc::tmem_dealloc(*tslot, 256);
     }
 }
 
