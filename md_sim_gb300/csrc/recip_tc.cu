@@ -39,7 +39,7 @@ struct TcDims {
     int KS;          // pass-2 K steps (2 NN rounded up to 16, / 16)
     int nrow, nchunk2;
     float px, py, pz;
-    int nst2;        // pass-2 chunk image stages in shared memory (2; 1 when two do not fit)
+    int nst2;        // pass-2 slot groups of kPer2 K steps in shared memory (as many as fit)
 };
 
 __device__ __forceinline__ void phase(uint32_t u, float& c, float& s) {
@@ -752,9 +752,10 @@ __global__ void __launch_bounds__(32 * kRedG) k_tc_sreduce(View v, const float* 
 // covers (row2, nlen2), so that chunk c (rows kRC c .. kRC c + kRC - 1 of that order) multiplies
 // only the K steps ks_lo .. ks_lo + nks - 1 its rows use (chunk2[c] = image byte offset, ks_lo,
 // nks).  Columns col = 4 r_local + 2 t + comp (t: T or T', comp: re or im), K = 2 (n + KN) + part;
-// the image of a chunk is [hi | lo][nks] tiles of N x 16.  One thread per (K step, column, n).
+// the image of a chunk is [nks][hi | lo] tiles of N x 16, so that one K step (its hi and lo tiles)
+// is one contiguous copy.  One thread per (K step, column, n).
 // ---------------------------------------------------------------------------------------------
-constexpr int kRC = 32;                 // rows per pass-2 chunk
+constexpr int kRC = 64;                 // rows per pass-2 chunk
 constexpr int kNC2 = 4 * kRC;           // pass-2 MMA N
 constexpr uint32_t kTile2 = kNC2 * 32;  // one N x 16 B tile (bytes)
 
@@ -803,45 +804,55 @@ __global__ void k_tc_prep_c(const float2* __restrict__ Cf, const int4* __restric
         uint32_t hi, lo;
         split2(v0, v1, hi, lo);
         const uint32_t off = tc::tile_off(col, 2 * i8);
-        *reinterpret_cast<uint32_t*>(base + ksl * kTile2 + off) = hi;
-        *reinterpret_cast<uint32_t*>(base + (nks + ksl) * kTile2 + off) = lo;
+        *reinterpret_cast<uint32_t*>(base + (2 * ksl) * kTile2 + off) = hi;
+        *reinterpret_cast<uint32_t*>(base + (2 * ksl + 1) * kTile2 + off) = lo;
     }
 }
 
 // ---------------------------------------------------------------------------------------------
 // pass 2: forces
 //
-// One CTA per 128 atoms.  The CTA builds A = e^{i n tz} of its atoms (K = 2 (n + KN) + part) and
-// walks the chunk images of C (32 rows each: N = 128 columns = T and T' x re/im), double-buffered:
-// a copier warp starts the copy of chunk c + 1 as soon as the MMAs of chunk c - 1 are done (its
-// stage is then free), so the copy overlaps the MMAs of chunk c; the issuer warp is a separate
-// warp because an issue waits for room in the tensor core's queue (about 640 cycles of work), and
-// a copy started after the issue of a chunk (21 MMAs, 1344 cycles) began too late to land before
-// that chunk ended.  Per chunk 3 (hi/lo) products per K step accumulate into one of two TMEM
-// accumulators, which the epilogue warps drain while the next chunk runs.  Per row the epilogue
-// forms Im(e^{i(l tx + m ty)} T) with the row phase advanced along m by a complex multiply
-// (recomputed by __sincosf at rows flagged in the shared row table: every 8th row and each change
-// of l).
+// One CTA per 128 atoms (M = 128).  The CTA builds A = e^{i n tz} of its atoms (K = 2 (n + KN) +
+// part) once and walks the chunks of C: 64 rows each, N = 256 columns = T and T' x re/im of the 64
+// rows, so an MMA reads 12 KB of shared memory per 128 cycles; with N = 128 (32-row chunks) it
+// read 8 KB per 64 cycles, the whole shared-memory bandwidth, and with the image copies beside it
+// ran at about half its rate.  A chunk's K steps stream through a ring of 16 KB slots (one K
+// step's hi and lo tiles): a copier warp fills each slot as soon as the 3 MMAs that read it before
+// are done, an issuer warp issues the 3 (hi/lo) products per K step into one of two TMEM
+// accumulators (the issuer does nothing else: an issue waits for room in the tensor core's queue
+// of about 640 cycles of work), and 16 epilogue warps (four per TMEM lane quarter, 16 rows of a
+// chunk each) drain the accumulator of chunk c while chunk c + 1 runs.  Per row the epilogue forms
+// Im(e^{i(l tx + m ty)} T) with the row phase advanced along m by a complex multiply (recomputed by
+// __sincosf at rows flagged in the row table: every 8th row and each change of l).
 // ---------------------------------------------------------------------------------------------
-constexpr int kT2 = 320;  // epilogue warps 0-7 (two per TMEM lane quarter, one per half chunk), issuer warp 8, copier warp 9
+constexpr int kEW2 = 16;                  // epilogue warps
+constexpr int kT2 = (kEW2 + 2) * 32;      // + the issuer warp (16) and the copier warp (17)
+constexpr int kSlot2 = 2 * (int)kTile2;   // one K step of a chunk image: hi and lo tiles
+constexpr int kPer2 = 3;                  // K steps per copy (a 1-D bulk copy costs about 400 ns
+                                          // whatever its size up to tens of KB, and one thread's
+                                          // copies run one after another: few large copies)
 
 struct P2Layout {
-    uint32_t a_bytes, img, off_a, off_b, off_rows, off_rsc, off_red, off_ch, total;
+    uint32_t a_bytes, off_a, off_ring, off_rows, off_rsc, off_red, off_ch, total;
+    int nslot;
 };
 
-__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nst) {
+// A (hi, lo), the ring of K-step slots (groups of kPer2, as many groups as fit), the row table,
+// the force partials of row parts 1-3, the chunk table
+__host__ __device__ inline P2Layout p2_layout(int KS, int nrow_pad, int nslot) {
     P2Layout L;
     L.a_bytes = 2 * KS * 4096;                 // [h][ks] 128 x 16
-    L.img = 2 * KS * kTile2;                   // a chunk image [h][ks] 128 x 16
     L.off_a = 1024;
-    L.off_b = L.off_a + L.a_bytes;
-    L.off_rows = L.off_b + nst * L.img;
+    L.off_ring = L.off_a + L.a_bytes;
+    L.nslot = nslot;
+    L.off_rows = L.off_ring + nslot * kPer2 * kSlot2;
     L.off_rsc = L.off_rows + nrow_pad * 16;    // rows: (float l, float m, l | restart << 31, m)
     L.off_red = L.off_rsc + nrow_pad * 4;      // row scales of this evaluation
-    L.off_ch = L.off_red + 3 * 128 * 4;         // second-half force partials of the 128 atoms
-    L.total = L.off_ch + 16 * nrow_pad / kRC;   // the chunk table (an L2 round trip per chunk otherwise)
+    L.off_ch = L.off_red + 3 * 3 * 128 * 4;
+    L.total = L.off_ch + 16 * (nrow_pad / kRC);
     return L;
 }
+constexpr int kMaxSlot2 = 12;
 
 __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __restrict__ atoms,
                                                      const unsigned char* __restrict__ img,
@@ -850,57 +861,64 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                                                      const float* __restrict__ rsc_g, double* __restrict__ frc) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const P2Layout L = p2_layout(d.KS, d.nchunk2 * kRC, d.nst2);
+    const int R = L.nslot;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm);   // [2] chunk image landed
-    uint64_t* mdone = full + 2;                          // [2] MMAs of the chunk done (accumulator ready)
-    uint64_t* afree = mdone + 2;                         // [2] accumulator drained (4 epilogue warps)
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm);   // [R] slot group landed
+    uint64_t* empty = full + kMaxSlot2;                  // [R] the group's MMAs done
+    uint64_t* mdone = empty + kMaxSlot2;                 // [2] MMAs of the chunk done (accumulator ready)
+    uint64_t* afree = mdone + 2;                         // [2] accumulator read out (16 epilogue warps)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 512);
     float4* rlm = reinterpret_cast<float4*>(sm + L.off_rows);
     float* rsc = reinterpret_cast<float*>(sm + L.off_rsc);
+    int4* chs = reinterpret_cast<int4*>(sm + L.off_ch);  // this item's chunks
     int* err = &v.status[ST_TC_TIMEOUT];
     const int4 item = items[blockIdx.x];  // atom tile, chunks [c0, c0 + NC), whole tile or piece
     const int atom0 = item.x * 128;
     const int c0 = item.y, NC = item.z - item.y;
     const int NCT = d.nchunk2;
-    int4* chs = reinterpret_cast<int4*>(sm + L.off_ch);  // this item's chunks
     if (t == 0) {
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < R; ++b) {
             tc::mbar_init(tc::smem_u32(&full[b]), 1);
+            tc::mbar_init(tc::smem_u32(&empty[b]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
             tc::mbar_init(tc::smem_u32(&mdone[b]), 1);
-            tc::mbar_init(tc::smem_u32(&afree[b]), 8);
+            tc::mbar_init(tc::smem_u32(&afree[b]), kEW2);
         }
         tc::mbar_fence_init();
     }
     for (int c = t; c < NC; c += kT2) chs[c] = chunks[c0 + c];
     __syncthreads();
-    const bool two = d.nst2 == 2;
-    if (warp == 9) {
+    if (warp == kEW2 + 1) {
         if (lane == 0) {
-            // the copier: chunk c's image into its stage as soon as the MMAs that read the stage
-            // before (chunk c - 2, or c - 1 with one stage) are done, independently of the issuer,
-            // whose issue waits for room in the tensor core's queue; the first copies overlap the
-            // other warps' set-up
-            const uint32_t bbase = tc::smem_u32(sm + L.off_b);
-            int last = -1;
-            for (int c = 0; c < NC; ++c) {
-                const int s = two ? (c & 1) : 0;
-                const int cp = two ? c - 2 : c - 1;  // the chunk whose MMAs last read the stage
-                if (cp >= 0 && !tc::mbar_wait(tc::smem_u32(&mdone[cp & 1]), (uint32_t)((cp >> 1) & 1), err, 21)) break;
-                const int4 ch = chs[c];
-                const uint32_t bytes = (uint32_t)ch.z * kTile2;  // hi half, then lo half
-                const uint32_t fb = tc::smem_u32(&full[s]);
-                tc::mbar_expect_tx(fb, 2 * bytes);
-                tc::bulk_g2s(bbase + s * L.img, img + ch.x, bytes, fb);
-                tc::bulk_g2s(bbase + s * L.img + bytes, img + ch.x + bytes, bytes, fb);
-                last = c;
+            // the copier: the item's chunk images are one contiguous byte range of U K steps; it
+            // streams through R slot groups of kPer2 K steps, one bulk copy per group as soon as
+            // the MMAs that read the group before are done; the first copies overlap the other
+            // warps' set-up
+            const uint32_t ring = tc::smem_u32(sm + L.off_ring);
+            int U = 0;
+            for (int c = 0; c < NC; ++c) U += chs[c].z;
+            const unsigned char* src = NC > 0 ? img + chs[0].x : img;
+            int grp = 0, ls = -1;
+            uint32_t ph = 0, lph = 0;                // parity of the group's use
+            for (int u0 = 0, j = 0; u0 < U; u0 += kPer2, ++j) {
+                if (j >= R && !tc::mbar_wait(tc::smem_u32(&empty[grp]), ph ^ 1u, err, 21)) break;
+                const uint32_t bytes = (uint32_t)(min(kPer2, U - u0) * kSlot2);
+                const uint32_t fb = tc::smem_u32(&full[grp]);
+                tc::mbar_expect_tx(fb, bytes);
+                tc::bulk_g2s(ring + grp * (kPer2 * kSlot2), src + (size_t)u0 * kSlot2, bytes, fb);
+                ls = grp;
+                lph = ph;
+                if (++grp == R) {
+                    grp = 0;
+                    ph ^= 1u;
+                }
             }
             // the last copy lands (bounded) before the block can exit
-            if (last >= 0)
-                tc::mbar_wait(tc::smem_u32(&full[two ? (last & 1) : 0]), (uint32_t)(two ? ((last >> 1) & 1) : (last & 1)),
-                              nullptr, 0);
+            if (ls >= 0) tc::mbar_wait(tc::smem_u32(&full[ls]), lph, nullptr, 0);
         }
     } else {
-        constexpr int kTS = 9 * 32;  // threads of the set-up: all warps but the copier
+        constexpr int kTS = (kEW2 + 1) * 32;  // threads of the set-up: all warps but the copier
         for (int r = t; r < NCT * kRC; r += kTS) {
             const int4 rw = r < d.nrow ? rows[r] : make_int4(0, 0, 0, 0);
             int restart = (r & 7) == 0 || r >= d.nrow;
@@ -911,15 +929,14 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
             rlm[r] = make_float4((float)rw.x, (float)rw.y, __int_as_float(rw.x | (restart << 31)), __int_as_float(rw.y));
             rsc[r] = rsc_g[r];
         }
-        if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 256);
-        // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part (warps 0-7, half of K each)
-        if (t < 256) {
-            const int mrow = t & 127, half = t >> 7;
+        if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 512);
+        // A: e^{i n tz} of this block's atoms, K = 2 (n + KN) + part (the epilogue warps, a
+        // quarter of the K steps each)
+        if (t < kEW2 * 32) {
+            const int mrow = t & 127, kq = t >> 7;
             const int at = atom0 + mrow;
             const uint32_t uz = at < v.nmove ? atoms[at].z : 0u;
-            const int ksplit = (d.KS + 1) / 2;
-            const int ks0 = half ? ksplit : 0, ks1 = half ? d.KS : ksplit;
-            for (int ks = ks0; ks < ks1; ++ks) {
+            for (int ks = kq; ks < d.KS; ks += 4) {
                 uint32_t wh[8], wl[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
@@ -941,37 +958,50 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
         tc::named_sync(2, kTS);
         tc::fence_after();
         const uint32_t tmem = *tslot;
-        if (warp == 8) {
+        if (warp == kEW2) {
             if (lane == 0) {
                 const uint32_t idesc = idesc_e(128, kNC2);
-                const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dB0 = tc::desc(tc::smem_u32(sm + L.off_b));
+                const uint64_t dA0 = tc::desc(tc::smem_u32(sm + L.off_a)), dR0 = tc::desc(tc::smem_u32(sm + L.off_ring));
                 bool alive = true;
+                int grp = 0, pos = 0, u = 0, U = 0;   // slot group, K step within it, K steps issued, all
+                uint32_t ph = 0;
+                for (int c = 0; c < NC; ++c) U += chs[c].z;
                 for (int c = 0; c < NC && alive; ++c) {
                     const int s = c & 1;              // accumulator
-                    const int sb = two ? s : 0;       // chunk image stage
-                    alive = tc::mbar_wait(tc::smem_u32(&full[sb]), two ? ((c >> 1) & 1) : (c & 1), err, 22);
-                    if (!alive) break;
                     if (c >= 2) alive = tc::mbar_wait(tc::smem_u32(&afree[s]), ((c >> 1) - 1) & 1, err, 23);
                     if (!alive) break;
-                    tc::fence_after();
                     const uint32_t dcol = tmem + s * kNC2;
-                    const uint64_t dB = dB0 + (uint64_t)((sb * L.img) >> 4);
                     const int4 ch = chs[c];
                     for (int ksl = 0; ksl < ch.z; ++ksl) {
+                        if (pos == 0) {
+                            alive = tc::mbar_wait(tc::smem_u32(&full[grp]), ph, err, 22);
+                            if (!alive) break;
+                            tc::fence_after();
+                        }
                         const int ks = ch.y + ksl;
                         const uint64_t ah = dA0 + (uint64_t)(ks * 256), al = dA0 + (uint64_t)((d.KS + ks) * 256);
-                        const uint64_t bh = dB + (uint64_t)(ksl * (kTile2 >> 4)), bl = dB + (uint64_t)((ch.z + ksl) * (kTile2 >> 4));
+                        const uint64_t bh = dR0 + (uint64_t)(((grp * kPer2 + pos) * kSlot2) >> 4), bl = bh + (uint64_t)(kTile2 >> 4);
                         tc::mma_bf16(dcol, ah, bh, idesc, ksl > 0 ? 1u : 0u);
                         tc::mma_bf16(dcol, ah, bl, idesc, 1u);
                         tc::mma_bf16(dcol, al, bh, idesc, 1u);
+                        ++u;
+                        if (++pos == kPer2 || u == U) {  // the group's last K step: free it once read
+                            tc::commit(tc::smem_u32(&empty[grp]));
+                            pos = 0;
+                            if (++grp == R) {
+                                grp = 0;
+                                ph ^= 1u;
+                            }
+                        }
                     }
-                    tc::commit(tc::smem_u32(&mdone[s]));
+                    if (alive) tc::commit(tc::smem_u32(&mdone[s]));
                 }
-                // on a timeout, let issued work drain (bounded) before the block frees its TMEM
-                if (!alive && NC > 0) tc::mbar_wait(tc::smem_u32(&mdone[(NC - 1) & 1]), ((NC - 1) >> 1) & 1, nullptr, 0);
+                // let the issued work finish (bounded) before the block frees its TMEM
+                if (NC > 0) tc::mbar_wait(tc::smem_u32(&mdone[(NC - 1) & 1]), ((NC - 1) >> 1) & 1, nullptr, 0);
             }
         } else {
-            // warp w reads TMEM lanes 32 (w & 3) .. + 31 (its atoms) and the half chunk w >> 2 (16 rows)
+            // warp w reads TMEM lanes 32 (w & 3) .. + 31 (its atoms) and rows 16 (w >> 2) .. + 15 of
+            // each chunk, 8 rows (32 columns) at a time
             const int quad = warp & 3, hf = warp >> 2;
             const int at = atom0 + quad * 32 + lane;
             const bool ok = at < v.nmove;
@@ -985,20 +1015,25 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                 alive = tc::mbar_wait_warp(tc::smem_u32(&mdone[s]), (c >> 1) & 1, err, 24);
                 if (!alive) break;
                 tc::fence_after();
-                {
-                    uint32_t raw[64];
+                float ec = 0.f, es = 0.f;
+                const int cid = c0 + c;
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc)
-                        tc::tmem_ld16_nw(tmem + ((uint32_t)(quad * 32) << 16) + s * kNC2 + hf * 64 + cc * 16, raw + cc * 16);
+                for (int half = 0; half < 2; ++half) {
+                    uint32_t raw[32];
+                    const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + s * kNC2 + hf * 64 + half * 32;
+                    tc::tmem_ld16_nw(ta, raw);
+                    tc::tmem_ld16_nw(ta + 16, raw + 16);
                     tc::tmem_wait_ld();
-                    tc::fence_before();
-                    __syncwarp();
-                    if (lane == 0) tc::mbar_arrive(tc::smem_u32(&afree[s]));
-                    float ec = 0.f, es = 0.f;
+                    if (half == 1) {  // the accumulator is read out: chunk c + 2 may use it
+                        tc::fence_before();
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&afree[s]));
+                    }
 #pragma unroll
-                    for (int rr = 0; rr < 16; ++rr) {
-                        const float4 lm = rlm[(c0 + c) * kRC + hf * 16 + rr];
-                        const float scr = rsc[(c0 + c) * kRC + hf * 16 + rr];
+                    for (int rr = 0; rr < 8; ++rr) {
+                        const int row = cid * kRC + hf * 16 + half * 8 + rr;
+                        const float4 lm = rlm[row];
+                        const float scr = rsc[row];
                         const int lb = __float_as_int(lm.z);
                         if (rr == 0 || lb < 0) {
                             phase((uint32_t)(lb & 0x7fffffff) * rec.x + (uint32_t)__float_as_int(lm.w) * rec.y, ec, es);
@@ -1016,19 +1051,23 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
                     }
                 }
             }
-            // the second-half warps hand their partial sums to the first-half warps through shared memory
+            // the warps of row parts 1-3 hand their partial sums to those of part 0 through shared memory
             float* red = reinterpret_cast<float*>(sm + L.off_red);
             const int ra = quad * 32 + lane;
-            if (hf == 1) {
-                red[ra] = alive ? fx : 0.f;
-                red[128 + ra] = alive ? fy : 0.f;
-                red[256 + ra] = alive ? fz : 0.f;
+            if (hf > 0) {
+                float* rp = red + (hf - 1) * 384;
+                rp[ra] = alive ? fx : 0.f;
+                rp[128 + ra] = alive ? fy : 0.f;
+                rp[256 + ra] = alive ? fz : 0.f;
             }
-            tc::named_sync(1, 256);
+            tc::named_sync(1, kEW2 * 32);
             if (hf == 0 && ok) {  // a whole tile's atoms have one writer: plain stores; pieces add
-                fx += red[ra];       // (a timed-out block leaves zeros and its status)
-                fy += red[128 + ra];
-                fz += red[256 + ra];
+#pragma unroll
+                for (int pp = 0; pp < 3; ++pp) {  // (a timed-out block leaves zeros and its status)
+                    fx += red[pp * 384 + ra];
+                    fy += red[pp * 384 + 128 + ra];
+                    fz += red[pp * 384 + 256 + ra];
+                }
                 const double q = alive ? (double)__uint_as_float(rec.w) : 0.0;
                 const double gx = q * (double)d.px * (double)fx, gy = q * (double)d.py * (double)fy,
                              gz = q * (double)d.pz * (double)fz;
@@ -1047,7 +1086,7 @@ __global__ void __launch_bounds__(kT2, 1) k_tc_force(View v, const uint4* __rest
     __syncthreads();
     if (warp == 0) {
         tc::fence_after();
-        tc::tmem_dealloc(*tslot, 256);
+        tc::tmem_dealloc(*tslot, 512);
     }
 }
 
@@ -1180,7 +1219,8 @@ int recip_tc_setup(Ctx& c) {
     if (tc_plan_pass1(c, tpc0, 2) && tc_plan_pass1(c, 2, 2)) return set_err(&c, MDG_E_UNSUPPORTED, "tensor-core plan");
     p.mtiles = (ks.nrow + 127) / 128;
     p.nchunk2 = (ks.nrow + kRC - 1) / kRC;
-    p.nst2 = p2_layout(p.KS, p.nchunk2 * kRC, 2).total <= 227 * 1024 ? 2 : 1;
+    p.nst2 = kMaxSlot2;  // slot groups of the pass-2 ring: as many as fit
+    while (p.nst2 > 2 && p2_layout(p.KS, p.nchunk2 * kRC, p.nst2).total > 227 * 1024) --p.nst2;
     p.smem2 = (int)p2_layout(p.KS, p.nchunk2 * kRC, p.nst2).total;
     if (p.smem2 > 227 * 1024)
         return set_err(&c, MDG_E_UNSUPPORTED, "k range too large for the tensor-core shared-memory tiles");
