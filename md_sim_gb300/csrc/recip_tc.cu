@@ -416,6 +416,25 @@ __device__ __forceinline__ bool wait_ab_warp(uint32_t addr, uint32_t parity, vol
     return __shfl_sync(0xffffffffu, ok, 0) != 0;
 }
 
+// bounded mbarrier wait by a whole warp: every lane polls (one instruction, so the lanes agree),
+// which keeps the warp converged; false once the abort flag is set or the limit is reached
+__device__ __forceinline__ bool wait_all(uint32_t addr, uint32_t parity, volatile int* ab, int* err, int tag) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (__all_sync(0xffffffffu, ok != 0)) return true;
+        if (*ab) return false;
+        if (it > 32) __nanosleep(it < 2048 ? 32 : 256);
+    }
+    *ab = 1;
+    if (err && (threadIdx.x & 31) == 0) atomicCAS(err, 0, tag);
+    return false;
+}
+
 typedef unsigned long long f2t;  // two packed floats (f32x2)
 __device__ __forceinline__ f2t f2pk(float a, float b) {
     f2t r;
@@ -441,6 +460,14 @@ __device__ __forceinline__ f2t f2sub(f2t a, f2t b) {
     f2t d;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
+}
+// hi/lo FP16 split of two floats with one packed subtraction
+__device__ __forceinline__ void split2p(float a, float b, uint32_t& hi, uint32_t& lo) {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    const float2 r = f2up(f2sub(f2pk(a, b), f2pk(hf.x, hf.y)));
+    lo = pack_h2(r.x, r.y);
 }
 // hi/lo FP16 split of a packed pair
 __device__ __forceinline__ void split_f2(f2t x, uint32_t& hi, uint32_t& lo) {
@@ -516,16 +543,17 @@ __global__ void __launch_bounds__(kT1b, 1)
         const int ijp = (t & 3) | (((t >> 5) & 1) << 2);
         const int ini = ((t >> 6) << 3) | ((t >> 2) & 7);
         const bool has_item = ini < d.NN;
+        const bool warp_items = __any_sync(0xffffffffu, has_item);  // warp-uniform
         const uint32_t ore = tc::tile_off(ini, 2 * ijp), oim = tc::tile_off(d.NN + ini, 2 * ijp);
         const uint32_t nfac = (uint32_t)(ini - d.KN);
         const int q = warp & 3, wq = warp >> 2;       // TMEM lane quarter, column block of the drains
         const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + wq * 64;  // this warp's TMEM block
-        bool alive = a1 <= a0 || wait_ab_warp(tc::smem_u32(recbar), 0, ab, err, 40);
+        bool alive = a1 <= a0 || wait_all(tc::smem_u32(recbar), 0, ab, err, 40);
         int nd = 0;                                    // chains added to the sums
         // chain c (columns 0-255) added in FP32 to the sums (columns 256-511), then the chain
         // accumulator is free for the next chain
         auto drain = [&](int c) {
-            alive = wait_ab_warp(tc::smem_u32(chainDone), (uint32_t)(c & 1), ab, err, 41);
+            alive = wait_all(tc::smem_u32(chainDone), (uint32_t)(c & 1), ab, err, 41);
             if (!alive) return;
             tc::fence_after();
 #pragma unroll
@@ -552,7 +580,7 @@ __global__ void __launch_bounds__(kT1b, 1)
                 drain(nd++);
                 if (!alive) break;
             }
-            if (g >= kS1b) alive = wait_ab_warp(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
+            if (g >= kS1b) alive = wait_all(tc::smem_u32(&empty[s]), rnd ^ 1u, ab, err, 43);
             if (!alive) break;
             unsigned char* st = sm + L.off_st + s * kSt1b;
             const uint4* rc = recs + g * kGA;
@@ -564,14 +592,14 @@ __global__ void __launch_bounds__(kT1b, 1)
                 float c0, s0, c1, s1;
                 phase(lu * r0.x + mu * r0.y, c0, s0);
                 phase(lu * r1.x + mu * r1.y, c1, s1);
-                split2(c0, c1, rh[k], rl[k]);
-                split2(s0, s1, ih[k], il[k]);
+                split2p(c0, c1, rh[k], rl[k]);
+                split2p(s0, s1, ih[k], il[k]);
             }
             *reinterpret_cast<uint4*>(st + 0 * 8192 + o8) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
             *reinterpret_cast<uint4*>(st + 1 * 8192 + o8) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
             *reinterpret_cast<uint4*>(st + 2 * 8192 + o8) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
             *reinterpret_cast<uint4*>(st + 3 * 8192 + o8) = make_uint4(il[0], il[1], il[2], il[3]);
-            if (has_item) {  // A: q e^{i n tz} of two atoms, lanes n and NN + n
+            if (warp_items) {  // A: q e^{i n tz} of two atoms, lanes n and NN + n
                 const uint2 z0 = *reinterpret_cast<const uint2*>(&rc[2 * ijp].z);
                 const uint2 z1 = *reinterpret_cast<const uint2*>(&rc[2 * ijp + 1].z);
                 float c0, s0, c1, s1;
@@ -579,22 +607,24 @@ __global__ void __launch_bounds__(kT1b, 1)
                 phase(nfac * z1.x, c1, s1);
                 const float q0 = __uint_as_float(z0.y), q1 = __uint_as_float(z1.y);
                 uint32_t ch, cl, sh, sl;
-                split2(q0 * c0, q1 * c1, ch, cl);
-                split2(q0 * s0, q1 * s1, sh, sl);
-                unsigned char* as = st + kBSt;
-                *reinterpret_cast<uint32_t*>(as + 0 * 4096 + ore) = ch;  // part 0: cos / sin
-                *reinterpret_cast<uint32_t*>(as + 0 * 4096 + oim) = sh;
-                *reinterpret_cast<uint32_t*>(as + 1 * 4096 + ore) = cl;
-                *reinterpret_cast<uint32_t*>(as + 1 * 4096 + oim) = sl;
-                *reinterpret_cast<uint32_t*>(as + 2 * 4096 + ore) = sh ^ 0x80008000u;  // part 1: -sin / cos
-                *reinterpret_cast<uint32_t*>(as + 2 * 4096 + oim) = ch;
-                *reinterpret_cast<uint32_t*>(as + 3 * 4096 + ore) = sl ^ 0x80008000u;
-                *reinterpret_cast<uint32_t*>(as + 3 * 4096 + oim) = cl;
+                split2p(q0 * c0, q1 * c1, ch, cl);
+                split2p(q0 * s0, q1 * s1, sh, sl);
+                if (has_item) {
+                    unsigned char* as = st + kBSt;
+                    *reinterpret_cast<uint32_t*>(as + 0 * 4096 + ore) = ch;  // part 0: cos / sin
+                    *reinterpret_cast<uint32_t*>(as + 0 * 4096 + oim) = sh;
+                    *reinterpret_cast<uint32_t*>(as + 1 * 4096 + ore) = cl;
+                    *reinterpret_cast<uint32_t*>(as + 1 * 4096 + oim) = sl;
+                    *reinterpret_cast<uint32_t*>(as + 2 * 4096 + ore) = sh ^ 0x80008000u;  // part 1: -sin / cos
+                    *reinterpret_cast<uint32_t*>(as + 2 * 4096 + oim) = ch;
+                    *reinterpret_cast<uint32_t*>(as + 3 * 4096 + ore) = sl ^ 0x80008000u;
+                    *reinterpret_cast<uint32_t*>(as + 3 * 4096 + oim) = cl;
+                }
             }
             tc::fence_async_smem();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(tc::smem_u32(&full[s]));
-            alive = __shfl_sync(0xffffffffu, *ab == 0 ? 1 : 0, 0) != 0;  // warp-uniform
+            alive = *ab == 0;  // one shared load for the warp: the same value in every lane
             if (++s == kS1b) {
                 s = 0;
                 rnd ^= 1u;
