@@ -10,7 +10,7 @@ lines (`other_configs`).
             device), inputs resident in HBM; each of the K timed steps is bracketed by CUDA events
             on the library's stream and L2 is flushed (256 MB write) between steps.
   e2e       ns/day of the drop-in MD step a Fortran host makes: the Gear predictor on host arrays
-            (mdg_host_predict, one host thread, as the reference's move_predict), mdg_force_get
+            (mdg_host_predict on all host cores, the reference's move_predict), mdg_force_get
             with the host arrays pinned (positions host->device, forces, torques and energies back),
             the Gear corrector on the host (mdg_host_correct) and mdg_shake for surface atoms; the
             whole step is inside the timed region (host clock).
@@ -457,7 +457,7 @@ def e2e_arm(lib, s_start, prm, args, shake_model=None):
     step = np.array(tp) + np.array(tf) + np.array(tc) + np.array(ts)
     t = float(np.mean(step))
     return {"value": ns_per_day(t, s.dt), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "path": ("drop-in MD step: mdg_host_predict (one host thread) -> mdg_force_get -> mdg_host_correct"
+            "path": ("drop-in MD step: mdg_host_predict (host cores, OpenMP) -> mdg_force_get -> mdg_host_correct"
                      + (" -> mdg_shake" if shake else "") + ", host arrays pinned once by mdg_pin_host"),
             "steps": K, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "host_integrator_ms": float(np.mean(tp) + np.mean(tc)) * 1e3, "force_call_ms": float(np.mean(tf)) * 1e3,

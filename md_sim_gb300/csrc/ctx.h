@@ -118,6 +118,10 @@ struct Pk {
     double* part = nullptr; // per-block slab dipole shares of the packing kernel
     float sx = 0, sy = 0, sz = 0;  // box edge / 2^32
     int zper = 0;
+    // the pair loops' parameters in FP32, rounded once on the host (a conversion from FP64 in
+    // every warp of the pair kernels kept the GPU's narrow FP64 pipe busy)
+    float alfa = 0, spii = 0, facq = 0, rcutsq = 0;
+    const float* par = nullptr;  // per pair type: vdW kind (int bits), sig, eps, aa, rhoi, cc
 };
 
 // Measurement arrays on the device and their bin parameters (measure.cu), passed by value.

@@ -562,6 +562,17 @@ int mdg_create(const mdg_sysdesc* s, const mdg_params* p, const double* x0, cons
         pack_setup(c);
         c.pk.tc = c.d_tc_atoms;
         c.pk.cmax = c.d_tc_cmax;
+        std::vector<float> parf(6 * (size_t)std::max<int64_t>(nijt, 1), 0.f);
+        for (int64_t k = 0; k < nijt; ++k) {
+            int bits = (int)s->vdwnum[k];
+            std::memcpy(&parf[6 * k + 0], &bits, 4);
+            parf[6 * k + 1] = (float)s->sig[k];
+            parf[6 * k + 2] = (float)s->eps[k];
+            parf[6 * k + 3] = (float)s->aa[k];
+            parf[6 * k + 4] = (float)s->rhoi[k];
+            parf[6 * k + 5] = (float)s->cc[k];
+        }
+        c.pk.par = upload(c, parf);
     }
     rc = nnlist_setup(c, x0, y0, z0);
     if (rc) return bail(rc);

@@ -162,20 +162,13 @@ struct Tables {
     int* nsi;
 };
 
-__device__ __forceinline__ Tables load_tables(const View& v, double* s_e, int nextra) {
+__device__ __forceinline__ Tables load_tables(const View& v, const Pk& pk, double* s_e, int nextra) {
     Tables t;
     t.par = reinterpret_cast<float*>(s_e + 2 * v.nijt + nextra);
     t.ijt = reinterpret_cast<int*>(t.par + 6 * v.nijt);
     t.nsi = t.ijt + v.nit * v.nit;
     for (int k = threadIdx.x; k < 2 * v.nijt + nextra; k += blockDim.x) s_e[k] = 0.0;
-    for (int k = threadIdx.x; k < v.nijt; k += blockDim.x) {
-        t.par[6 * k + 0] = __int_as_float(v.vdw[k]);
-        t.par[6 * k + 1] = (float)v.sig[k];
-        t.par[6 * k + 2] = (float)v.eps[k];
-        t.par[6 * k + 3] = (float)v.aa[k];
-        t.par[6 * k + 4] = (float)v.rhoi[k];
-        t.par[6 * k + 5] = (float)v.cc[k];
-    }
+    for (int k = threadIdx.x; k < 6 * v.nijt; k += blockDim.x) t.par[k] = pk.par[k];
     for (int k = threadIdx.x; k < v.nit * v.nit; k += blockDim.x) t.ijt[k] = v.ijt[k];
     for (int k = threadIdx.x; k < v.nit; k += blockDim.x) t.nsi[k] = v.nsi[k];
     __syncthreads();
@@ -215,11 +208,11 @@ __device__ __forceinline__ float vdw_term(const float* par, float rsqi, float ri
 template <int ZPER>
 __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
     extern __shared__ double s_e[];
-    const Tables T = load_tables(v, s_e, 0);
+    const Tables T = load_tables(v, pk, s_e, 0);
     const int lane = threadIdx.x & 31;
     const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * kWarps;
-    const float alfa = (float)v.alfa, spii = (float)v.spii, facq = (float)v.facq, rcutsq = (float)v.rcutsq;
+    const float alfa = pk.alfa, spii = pk.spii, facq = pk.facq, rcutsq = pk.rcutsq;
     EAcc e;
     for (int h = warp; h < v.nheads; h += nwarps) {
         const int i = v.head_atom[h];
@@ -305,11 +298,11 @@ __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
 template <int ZPER>
 __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
     extern __shared__ double s_e[];
-    const Tables T = load_tables(v, s_e, 6);
+    const Tables T = load_tables(v, pk, s_e, 6);
     const int lane = threadIdx.x & 31;
     const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * kWarps;
-    const float alfa = (float)v.alfa, spii = (float)v.spii, facq = (float)v.facq, rcutsq = (float)v.rcutsq;
+    const float alfa = pk.alfa, spii = pk.spii, facq = pk.facq, rcutsq = pk.rcutsq;
     // energy sums per wall site type (the last two site types): the two alternate from partner to
     // partner, and one accumulator per type avoids a flush on every change
     EAcc ew[2];
@@ -442,6 +435,10 @@ void pack_setup(Ctx& c) {
     c.pk.sx = (float)(v.lx / 4294967296.0);
     c.pk.sy = (float)(v.ly / 4294967296.0);
     c.pk.sz = (float)(v.lz / 4294967296.0);
+    c.pk.alfa = (float)v.alfa;
+    c.pk.spii = (float)v.spii;
+    c.pk.facq = (float)v.facq;
+    c.pk.rcutsq = (float)v.rcutsq;
 }
 
 double slab_crf0(const Ctx& c) {
