@@ -259,8 +259,11 @@ int mdg_check(mdg_ctx* ctx, mdg_report* rep);
  * Host integrator for drop-in callers.  The reference keeps move_predict / move_correct
  * (src/move.f90:48-383) in Fortran around its force call; a caller that replaces only force_get
  * (and move_shake) with this library keeps them too.  These calls are that integrator on host
- * arrays for callers written in C or C++: one host thread, no device memory, the reference's
- * arithmetic order.  A drop-in step is
+ * arrays for callers written in C or C++: the molecules split into ranges over the host threads
+ * (OpenMP; MDG_HOST_THREADS, read at mdg_host_gear_create, else all cores the process may use,
+ * one thread below 2,048 molecules), kinetic sums in molecule order on one thread, so results do
+ * not depend on the thread count; no device memory, the reference's arithmetic order.  A drop-in
+ * step is
  *     mdg_host_predict -> mdg_force_get (x0.., cx[0].., rsx..) -> mdg_host_correct
  *     (-> mdg_shake when there are surface atoms)
  * and reproduces the resident step of mdg_run to rounding.
