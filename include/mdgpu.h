@@ -284,6 +284,24 @@ int mdg_host_correct(mdg_host_gear* g, mdg_state* st, const double* ftx, const d
 /* kp, kw, ke, htot (last predict), tempnow, uconf (last correct); the other fields are untouched. */
 int mdg_host_report(const mdg_host_gear* g, mdg_report* rep);
 
+/* ---------------------------------------------------------------------------------------------
+ * The reference's input files read on the host, for callers written in C or C++: sysdef_input /
+ * sysdef_init (src/sysdef.f90:83-340, :356-457) on the .fld and .top files and config_input /
+ * config_init (src/config.f90:174-242, :55-95, config_quatsite :303-329) on the .cfg file (whose
+ * first record also gives the box).  dt: the time step in fs (the .inp value).  The handle owns
+ * the description's tables, the rigid-water body (temper -1: set it from the .inp for NVT) and the
+ * state, ready for mdg_create (positions: the state's x0/y0/z0 and cx[0]..) and mdg_set_state or
+ * the drop-in loop; molnames serves mdg_write_cfg / mdg_read_cfg.  Errors (file, format, the
+ * reference's sysdef_input checks) return MDG_E_ARG with the message in mdg_last_error(NULL).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct mdg_sysdef mdg_sysdef;
+int mdg_sysdef_load(const char* fld_path, const char* top_path, const char* cfg_path, double dt, mdg_sysdef** out);
+const mdg_sysdesc* mdg_sysdef_desc(const mdg_sysdef* sd);
+const mdg_rigid* mdg_sysdef_rigid(const mdg_sysdef* sd);
+mdg_state* mdg_sysdef_state(mdg_sysdef* sd);
+const char* const* mdg_sysdef_molnames(const mdg_sysdef* sd);
+void mdg_sysdef_free(mdg_sysdef* sd);
+
 /* Kernel launches of one resident-mode step (counted in the captured step graph; 0 before the
  * first mdg_run / mdg_run_async). */
 int64_t mdg_kernels_per_step(const mdg_ctx* ctx);

@@ -192,6 +192,12 @@ class Lib:
             I32P = C.POINTER(C.c_int32)
             g("kvectors", C.c_int64, [C.c_void_p, I32P, I32P, I32P, DP, C.c_int64])
         g("shake", C.c_int, [C.c_void_p] + [DP] * 10 + [C.POINTER(C.c_double), C.POINTER(C.c_int32)])
+        if self.has("sysdef_load"):
+            g("sysdef_load", C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_double, C.POINTER(C.c_void_p)])
+            g("sysdef_desc", C.POINTER(SysDesc), [C.c_void_p])
+            g("sysdef_rigid", C.POINTER(Rigid), [C.c_void_p])
+            g("sysdef_state", C.POINTER(State), [C.c_void_p])
+            g("sysdef_free", None, [C.c_void_p])
         if self.has("pin_host"):
             g("pin_host", C.c_int, [C.c_void_p, C.c_int64])
             g("unpin_host", C.c_int, [C.c_void_p])

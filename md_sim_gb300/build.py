@@ -20,7 +20,8 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxe
 # counts and histogram bins match the reference's rounding
 PER_FILE = {"shake.cu": ["-fmad=false"], "measure.cu": ["-fmad=false"],
             # the host integrator follows the reference's arithmetic order, without host FMA fusion
-            "hostgear.cu": ["-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp"]}
+            "hostgear.cu": ["-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp"],
+            "sysdef.cu": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def _nvcc():
