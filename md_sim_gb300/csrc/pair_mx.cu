@@ -227,24 +227,33 @@ __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
         float fix[3] = {0, 0, 0}, fiy[3] = {0, 0, 0}, fiz[3] = {0, 0, 0};
         const int n = v.nbcnt[h];
         const int* nb = v.nb + (size_t)h * v.maxnb;
+        // software pipeline over the lane's partners: the record of the next partner and the
+        // index of the one after are loaded while this one is computed (one warp per head and
+        // one block per SM leave few warps to hide the dependent gathers otherwise)
+        int j1 = lane < n ? nb[lane] : 0;
+        int j2 = lane + 32 < n ? nb[lane + 32] : 0;
+        uint4 p1 = lane < n ? pk.P[j1] : make_uint4(0u, 0u, 0u, 0u);
         for (int k = lane; k < n; k += 32) {
-            const int j = nb[k];
-            const uint4 pj = pk.P[j];
+            const int j = j1;
+            const uint4 pj = p1;
+            j1 = j2;
+            if (k + 32 < n) p1 = pk.P[j1];
+            if (k + 64 < n) j2 = nb[k + 64];
+            const int jt = (int)(pj.w & 0x7fffffffu);
+            const int nsi_j = T.nsi[jt];
+            float4 sj[3];  // the partner's sites, requested before the distance test
+#pragma unroll
+            for (int b = 0; b < 3; ++b) sj[b] = b < nsi_j ? pk.Q[j + b] : make_float4(0.f, 0.f, 0.f, 0.f);
             float xio, yio, zio;
             head_vec<ZPER>(pi, zli, pj, pk, j, xio, yio, zio);
             const float rsq = xio * xio + yio * yio + zio * zio;
             if (rsq > rcutsq) continue;
-            const int jt = (int)(pj.w & 0x7fffffffu);
             const int ijt = T.ijt[it * v.nit + jt];
-            const int nsi_j = T.nsi[jt];
             const float rinv = rsqrtf(rsq);
             const float rsqi = rinv * rinv;
             const float rij = rsq * rinv;
             float fij;
             const float elj = vdw_term(T.par + 6 * ijt, rsqi, rinv, rij, &fij);
-            float4 sj[3];
-#pragma unroll
-            for (int b = 0; b < 3; ++b) sj[b] = b < nsi_j ? pk.Q[j + b] : make_float4(0.f, 0.f, 0.f, 0.f);
             float ff;
             const float auxq = facq * si[0].w * sj[0].w * rinv;
             float eqq = erfc_as(alfa * rij, &ff, spii) * auxq;
