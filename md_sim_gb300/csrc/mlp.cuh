@@ -65,5 +65,33 @@ __device__ __forceinline__ void forward(const float* W, const float in[9], float
     for (int c = 0; c < NO; ++c) out[c] = y[c] * W[OYS + c] + W[OYM + c];
 }
 
+// The same forward pass by a whole block (at least 64 threads; every thread calls it): thread o
+// computes hidden unit o of each layer and threads 0-2 the outputs, each with the operations of
+// forward() in its order, so the outputs are identical to it.  in and out live in shared memory;
+// h is shared scratch of 2 * NH floats.
+__device__ __forceinline__ void forward_block(const float* W, const float* in, float* h, float* out) {
+    const int o = threadIdx.x;
+    if (o < NH) {
+        float z = W[OB1 + o];
+#pragma unroll
+        for (int i = 0; i < NI; ++i) z = fmaf(W[OW1 + o * NI + i], (in[i] - W[OXM + i]) * W[OXS + i], z);
+        h[o] = silu(z);
+    }
+    __syncthreads();
+    if (o < NH) {
+        float z = W[OB2 + o];
+#pragma unroll 8
+        for (int i = 0; i < NH; ++i) z = fmaf(W[OW2 + o * NH + i], h[i], z);
+        h[NH + o] = silu(z);
+    }
+    __syncthreads();
+    if (o < NO) {
+        float y = W[OB3 + o];
+        for (int k = 0; k < NH; ++k) y = fmaf(W[OW3 + o * NH + k], h[NH + k], y);
+        out[o] = y * W[OYS + o] + W[OYM + o];
+    }
+    __syncthreads();
+}
+
 }  // namespace mlp
 }  // namespace mdg

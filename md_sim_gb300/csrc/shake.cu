@@ -24,6 +24,7 @@ namespace mdg {
 namespace {
 
 constexpr int kNT = 128;
+constexpr int kMolNT = 64;
 constexpr int kMaxAt = 6;
 
 struct ShakeArgs {
@@ -158,10 +159,8 @@ __device__ void bonds(const View& v, const Mol& m, const double* px, const doubl
 
 // Network seed: predicted accumulated multipliers applied along the old bonds, the same update as a
 // SHAKE correction (src/move.f90:498-510) with all three constraints at once.
-__device__ void seed_mol(const View& v, const Mol& m, const float* W, const float f[9], double* px, double* py,
-                         double* pz, const double r[3][3], double* gacc) {
-    float y[3];
-    mlp::forward(W, f, y);
+__device__ void apply_seed(const View& v, const Mol& m, const float y[3], double* px, double* py, double* pz,
+                           const double r[3][3], double* gacc) {
     for (int c = 0; c < 3; ++c) {
         const int a = m.ca[c], b = m.cb[c];
         const double ma = v.mii[m.at[a]], mb = v.mii[m.at[b]];
@@ -171,6 +170,13 @@ __device__ void seed_mol(const View& v, const Mol& m, const float* W, const floa
         px[a] += r[c][0] * ma * g; py[a] += r[c][1] * ma * g; pz[a] += r[c][2] * ma * g;
         px[b] -= r[c][0] * mb * g; py[b] -= r[c][1] * mb * g; pz[b] -= r[c][2] * mb * g;
     }
+}
+
+__device__ void seed_mol(const View& v, const Mol& m, const float* W, const float f[9], double* px, double* py,
+                         double* pz, const double r[3][3], double* gacc) {
+    float y[3];
+    mlp::forward(W, f, y);
+    apply_seed(v, m, y, px, py, pz, r, gacc);
 }
 
 __device__ void load_weights(const float* mlpw, float* W) {
@@ -183,21 +189,35 @@ __global__ void k_shake_init(ShakeArgs A) {
 }
 
 __global__ void k_shake_last(View v, ShakeArgs A) {
+    // one block: the seeding network's forward pass for the last molecule runs on the block's
+    // threads (identical outputs to the one-thread form of k_shake_mol); its sweeps on thread 0
     __shared__ float W[mlp::NW];
+    __shared__ float fin[mlp::NI], hid[2 * mlp::NH], yout[mlp::NO];
+    __shared__ int seeded;
     if (A.mlpw) load_weights(A.mlpw, W);
-    __syncthreads();
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
     Mol m;
     load_mol(A, A.ncons - 1, m);
     double px[kMaxAt], py[kMaxAt], pz[kMaxAt], ox[kMaxAt], oy[kMaxAt], oz[kMaxAt];
-    unsigned moved;
-    gather(v, A, m, px, py, pz, ox, oy, oz, moved);
-    if (A.mlpw && m.n == 3) {
-        double p[3][3], r[3][3], g[3] = {0, 0, 0};
-        float f[9];
-        bonds(v, m, px, py, pz, ox, oy, oz, p, r);
-        mlp::features(p, r, m.l2, f);
-        seed_mol(v, m, W, f, px, py, pz, r, g);
+    unsigned moved = 0;
+    double r[3][3];
+    if (threadIdx.x == 0) {
+        gather(v, A, m, px, py, pz, ox, oy, oz, moved);
+        seeded = A.mlpw && m.n == 3 ? 1 : 0;
+        if (seeded) {
+            double p[3][3];
+            float f[9];
+            bonds(v, m, px, py, pz, ox, oy, oz, p, r);
+            mlp::features(p, r, m.l2, f);
+            for (int k = 0; k < mlp::NI; ++k) fin[k] = f[k];
+        }
+    }
+    __syncthreads();
+    if (seeded) mlp::forward_block(W, fin, hid, yout);
+    if (threadIdx.x != 0) return;
+    if (seeded) {
+        double g[3] = {0, 0, 0};
+        const float y[3] = {yout[0], yout[1], yout[2]};
+        apply_seed(v, m, y, px, py, pz, r, g);
     }
     int fail = 0, s = 0;
     bool done = false;
@@ -402,7 +422,9 @@ void shake_launch(Ctx& c, const double* d_ft, bool kps_clear) {
     } else {
         k_shake_last<<<1, 128, 0, c.stream>>>(v, A);
     }
-    k_shake_mol<<<(c.ncons + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, A);
+    // one thread per molecule, 64 per block: the molecules are few (8,192 at most in the benchmark
+    // systems) and their sweeps are chains of FP64 operations, so they are spread over the SMs
+    k_shake_mol<<<(c.ncons + kMolNT - 1) / kMolNT, kMolNT, 0, c.stream>>>(v, A);
     k_shake_status<<<1, 1, 0, c.stream>>>(v, c.d_sweeps);
 }
 
