@@ -6,11 +6,15 @@
 //              q_j kz sum_{l,m} Im( e^{i(l tx_j + m ty_j)} T'_j(l,m) ) with
 //   T_j(l,m) = sum_n C(l,m,n) e^{i n tz_j},  T'_j(l,m) = sum_n n C(l,m,n) e^{i n tz_j}   (pass 2)
 // with C = Ak conj(S + S_wall).  Both are complex matrix products written as real ones:
-//   pass 1: D[(l,m) row, (re|im, n)] over K = atoms, A = [Re | Im] of the row factor, B = the
-//           2x2 real block form of e^{i n tz}, M = 128 rows per CTA, split-K over atom chunks;
+//   pass 1: the structure factor over K = atoms, split-K over atom chunks, in one of two forms:
+//           n-side (k_tc_sfac2, used when 2 (2 KN + 1) <= 128): D[(re|im, n) lane, (l, m) row],
+//           A = q e^{i n tz} in the 2x2 real block form, B = e^{i(l tx + m ty)}, N = 256 rows per
+//           CTA; row-side (k_tc_sfac): D[(l, m) row, (re|im, n)], A = [Re | Im] of the row factor,
+//           B = the 2x2 block form of e^{i n tz}, M = 128 rows per tile;
 //   pass 2: D[atom, (row, T|T', re|im)] over K = (n, re|im), A = e^{i n tz} per atom (built once
-//           per CTA), B = packed C chunks streamed with cp.async.bulk, two TMEM accumulators
-//           double-buffered against the epilogue that forms Im(e T) per row.
+//           per CTA), B = packed C chunks streamed with cp.async.bulk through a ring of K-step
+//           slots, two TMEM accumulators double-buffered against the epilogue that forms
+//           Im(e T) per row.
 // Operands are hi/lo splits (x = hi + lo, FP16 halves here; the self test exercises BF16) and every
 // product is hi*hi + hi*lo + lo*hi with FP32 accumulation in TMEM.  Phases come from exact 32-bit fixed-point fractions of the box
 // (u = frac(x/L) 2^32, so l*u wraps modulo one period) evaluated with __sincosf on [-pi, pi).
@@ -30,7 +34,7 @@ namespace {
 constexpr float kPhase = 1.4629180792671596e-09f;  // 2 pi / 2^32
 
 // Operands are FP16 hi/lo splits (11 + 11 significant bits; BF16 would give 8 + 8); all are O(1)
-// (phase factors, charges, and C(k) scaled by the step's max |n C|).
+// (phase factors, charges, and C(k) scaled per (l, m) row by the row's max |C| max(1, |n|)).
 __device__ __forceinline__ uint32_t idesc_e(int M, int N) { return tc::idesc_f16(M, N); }
 
 struct TcDims {
@@ -350,27 +354,27 @@ __global__ void __launch_bounds__(P1<TPC>::kThreads, 1)
 // ---------------------------------------------------------------------------------------------
 // pass 1, n-side form (2 NN <= 128): the same structure factor with the roles of the operands
 // swapped, D[(re|im, n) lane, (l, m) row] over K = atoms:
-//   A (M = 128 lanes): e^{i n tz} in the 2x2 real block form (part 0: cos / sin, part 1: -sin /
+//   A (M = 128 lanes): q e^{i n tz} in the 2x2 real block form (part 0: cos / sin, part 1: -sin /
 //     cos), lanes n (re) and NN + n (im), zero beyond 2 NN;
-//   B (N = 256 rows): the real (part 0) and imaginary (part 1) parts of q e^{i(l tx + m ty)}.
+//   B (N = 256 rows): the real (part 0) and imaginary (part 1) parts of e^{i(l tx + m ty)}.
 // Every tcgen05.mma is M = 128, N = 256 (128 cycles at the dense rate), 6 per group of 16 atoms
 // (2 parts x hi*hi, hi*lo, lo*hi).  The CTA's atom records (a contiguous chunk, at most
-// kMaxChunk1b atoms) arrive in shared memory by one bulk copy; then 16 warps (two threads per CTA
-// row, 8 atoms each; 128 registers a thread) produce, group after group and without waiting for
-// one another,
+// kMaxChunk1b atoms) arrive in shared memory by one bulk copy; then 16 producer warps (two
+// threads per CTA row, 8 atoms each) write, group after group,
 //   the B entries of their rows, each by one __sincosf of the exact fixed-point phase
-//     l ux + m uy (mod 2^32) times q, split hi/lo and stored in the UMMA layout, and
-//   one A item (n, atom pair) each,
-// and arrive on the stage's barrier; warp 15's lane 0, after its own arrival, issues the group's
-// 6 MMAs (slot and phase counters, no division: the issuer's instructions per MMA decide whether
-// the tensor pipe keeps its rate).  Thread mappings keep the shared stores free of bank
-// conflicts: a quarter warp writes 8 consecutive rows of one atom half (128 contiguous bytes); an
-// A item warp covers 8 lanes x 4 atom pairs of one core matrix column.
+//     l ux + m uy (mod 2^32), split hi/lo and stored in the UMMA layout, and
+//   one A item (n, atom pair) per thread of the first 14 warps,
+// and arrive on the stage's barrier.  A separate issuer warp (lane 0) waits for the 16 arrivals
+// and issues the group's 6 MMAs: an issue waits for room in the tensor core's queue (about 640
+// cycles of work), which stalled whichever producer warp issued.  Thread mappings keep the
+// shared stores free of bank conflicts: a quarter warp writes 8 consecutive rows of one atom half
+// (128 contiguous bytes); an A item warp covers 8 lanes x 4 atom pairs of one core matrix column.
 // Accumulation: the tensor core's FP32 accumulation loses magnitude in every step (measured on
 // this GPU: about 1.5e-8 of the running sum per accumulating MMA, always towards zero), so long
-// chains bias S(k).  The chain is cut every G groups: two TMEM accumulators alternate, and all
-// warps add the finished one into FP32 registers (round to nearest, unbiased) while the next
-// chain runs, then write their sums as this CTA's partial [split][lane][row].
+// chains bias S(k).  The chain is cut every G groups: it accumulates in TMEM columns 0-255, and
+// one group into the next chain the producers add it in FP32 (round to nearest, unbiased) to the
+// sums in TMEM columns 256-511; the issuer starts a chain only after all have done so.  At the
+// end the sums are this CTA's partial [split][lane][row].
 // Every wait is bounded; a timeout anywhere sets a shared abort flag that ends all waits.
 // ---------------------------------------------------------------------------------------------
 constexpr int kW1b = 16;                 // producer warps
