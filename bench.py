@@ -668,6 +668,7 @@ def replicas_arm(args, rank=0, world=1):
     t_tune = time.perf_counter() - t0
     batch = abi.Batch(lib, ctxs)
     batch.set_stream(stream.cuda_stream)
+    batch.set_mode(abi.MDG_BATCH_PHASES if args.batch_mode == "phases" else abi.MDG_BATCH_GRAPHS)
     batch.run(args.warmup)                # untimed: graph build and warm-up
     # The thinnest films (a few hundred waters on the widest walls) heat up by several hundred K
     # per 100 steps under NVE even after the rescaled start (the oracle's own dynamics do the
@@ -690,6 +691,24 @@ def replicas_arm(args, rank=0, world=1):
     for c in ctxs:
         c.check()
     t_batch = float(np.sum(per_step)) / K * 1e-3
+    phased = batch.phased()
+    # the other graph form of the same batch, for comparison (untimed warm-up, then Ko steps)
+    other = "graphs" if args.batch_mode == "phases" else "phases"
+    batch.set_mode(abi.MDG_BATCH_GRAPHS if other == "graphs" else abi.MDG_BATCH_PHASES)
+    batch.run_async(3)
+    torch.cuda.synchronize()
+    Ko = max(5, K // 4)
+    eo = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Ko)]
+    with torch.cuda.stream(stream):
+        for k in range(Ko):
+            flush.zero_()
+            eo[k][0].record(stream)
+            batch.run_async(1)
+            eo[k][1].record(stream)
+    stream.synchronize()
+    t_other = float(np.sum([a.elapsed_time(b) for a, b in eo])) / Ko * 1e-3
+    for c in ctxs:
+        c.check()
     # the same replicas one after another, each with its own graph, on the same stream
     for c in ctxs:
         c.set_stream(stream.cuda_stream)
@@ -729,6 +748,9 @@ def replicas_arm(args, rank=0, world=1):
         "sequential": {"ms_per_step": t_seq * 1e3, "value": ns_per_day(t_seq, dt) * nloc, "unit": "replica-ns/day",
                        "how": "each replica's own graph, one after another on one stream"},
         "batch_speedup_vs_sequential": t_seq / t_batch,
+        "batch_mode": {"timed": args.batch_mode, "replicas_in_batched_loops": phased,
+                       other: {"ms_per_step": t_other * 1e3, "value": ns_per_day(t_other, dt) * nloc,
+                               "steps": Ko}},
         "setup_s": {"build": t_build, "create": t_create, "equilibration": t_equil, "autotune": t_tune},
         "tuning": _tuning_summary(tunings),
         "clocks": clk.summary(),
@@ -865,6 +887,9 @@ def main():
     ap.add_argument("--extra", default="slab2048,shake8k",
                     help="workloads measured after the headline one, as compact lines (empty: none)")
     ap.add_argument("--replicas", type=int, default=64)
+    ap.add_argument("--batch-mode", choices=("phases", "graphs"), default="phases",
+                    help="replica batch graph form: real-space loops of all replicas in one kernel each "
+                         "(phases) or every replica's own step graph as a child graph (graphs)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--fp64-steps", type=int, default=20,
                     help="steps of the plain FP64 GPU comparison arm (0 = skip)")

@@ -332,8 +332,9 @@ int mdg_autotune(mdg_ctx* ctx, int32_t reps, mdg_tuning* out);
 
 /* ---------------------------------------------------------------------------------------------
  * Replica batches (no reference counterpart; the reference runs one system per MPI job).
- * Independent contexts in resident mode, stepped together by one CUDA graph whose per-replica
- * step graphs are parallel branches, so that many small systems share the GPU in one launch.
+ * Independent contexts in resident mode, stepped together by one CUDA graph launch, so that many
+ * small systems share the GPU: by default their real-space loops run as one kernel over all of
+ * them (mdg_batch_set_mode below).
  * ------------------------------------------------------------------------------------------- */
 typedef struct mdg_batch mdg_batch;
 /* ctxs: n contexts on one device, each after mdg_set_state; they stay owned by the caller and
@@ -347,6 +348,17 @@ int mdg_batch_set_stream(mdg_batch* b, void* stream);
 int mdg_batch_run(mdg_batch* b, int64_t nsteps, mdg_report* reps);
 /* nsteps graph launches on the batch stream, no checks (for timing; then mdg_check per context) */
 int mdg_batch_run_async(mdg_batch* b, int64_t nsteps);
+/* Graph form of the batch (the next run builds it):
+ *   MDG_BATCH_PHASES (default)  phase order: the head-head and head-wall loops of all replicas in
+ *       the mixed form with walls and no surface atoms run as one persistent kernel each over all
+ *       their heads (pair_blocks / wall_blocks blocks; 0 = 1216), between the replicas' own list
+ *       builds and their merge, corrector and SHAKE; other replicas step as in their own graphs;
+ *   MDG_BATCH_GRAPHS  every replica's own step graph as a parallel child graph. */
+#define MDG_BATCH_GRAPHS 0
+#define MDG_BATCH_PHASES 1
+int mdg_batch_set_mode(mdg_batch* b, int mode, int pair_blocks, int wall_blocks);
+/* replicas whose real-space loops ran in the batch's kernels at the last graph build */
+int mdg_batch_phased(const mdg_batch* b);
 
 /* ---------------------------------------------------------------------------------------------
  * Configuration files and checkpoints of the resident state.

@@ -24,6 +24,7 @@ DP = C.POINTER(C.c_double)
 MDG_OK = 0
 MDG_SLAB, MDG_BULK = 0, 1
 MDG_FP64, MDG_MIXED = 0, 1
+MDG_BATCH_GRAPHS, MDG_BATCH_PHASES = 0, 1
 MDG_QUIRK_CLEAN_SHAKE_DONE = 1
 
 ERRORS = {
@@ -226,6 +227,9 @@ class Lib:
             g("batch_set_stream", C.c_int, [C.c_void_p, C.c_void_p])
             g("batch_run", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p])
             g("batch_run_async", C.c_int, [C.c_void_p, C.c_int64])
+        if self.has("batch_set_mode"):
+            g("batch_set_mode", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int])
+            g("batch_phased", C.c_int, [C.c_void_p])
         if self.has("measure_init"):
             g("measure_init", C.c_int, [C.c_void_p, C.POINTER(MeasureParams), C.POINTER(MeasureDims)])
             g("measure_enable", C.c_int, [C.c_void_p, C.c_int, C.c_int])
@@ -644,6 +648,15 @@ class Batch:
 
     def run_async(self, nsteps: int):
         self._check(self.lib.batch_run_async(self.h, int(nsteps)))
+
+    def set_mode(self, mode: int, pair_blocks: int = 0, wall_blocks: int = 0):
+        """MDG_BATCH_PHASES (the replicas' real-space loops in one kernel each) or MDG_BATCH_GRAPHS
+        (every replica's own step graph as a child graph); takes effect at the next run."""
+        self._check(self.lib.batch_set_mode(self.h, int(mode), int(pair_blocks), int(wall_blocks)))
+
+    def phased(self) -> int:
+        """Replicas whose real-space loops ran in the batch's kernels at the last graph build."""
+        return int(self.lib.batch_phased(self.h))
 
     def close(self):
         if getattr(self, "h", None):

@@ -233,6 +233,7 @@ struct Ctx {
     std::vector<double> h_qs_wall;  // wall charges (for the static structure factor)
     double *d_ft = nullptr, *d_fc = nullptr, *d_tq = nullptr;  // force_sum outputs
     bool alloc_failed = false;
+    int batch_stage = 0;          // captures of a phase-ordered replica batch: 1 up to the list, 2 after the loops
     bool debug_sync = false;
     // resident mode
     bool resident = false;
@@ -276,6 +277,25 @@ void pairs_mixed(Ctx& c, bool merge);  // head-head pairs into F (then merged in
 void walls_mixed(Ctx& c, bool concurrent = false);  // head-wall pairs into F (concurrent: beside the other branches)
 // F (+ frc, + the slab dipole term) into the FP64 forces, F cleared
 void merge_mixed(Ctx& c, const double* frc, bool dipole);
+// The head-head and head-wall loops of several systems (each in the concurrent form: walls, no
+// surface atoms) as one launch each per z treatment; descriptors and item tables on the device.
+struct RsBatch {
+    struct Group {
+        void* reps = nullptr;     // device: one view + packed records per system
+        int* first_p = nullptr;   // device: first head-head item of each system, nrep + 1
+        int* first_w = nullptr;   // device: first head-wall item of each system, nrep + 1
+        int nrep = 0, items_p = 0, items_w = 0;
+        size_t smem_p = 0, smem_w = 0;
+    };
+    Group g[2];                   // z not periodic / periodic in the real-space loops
+    void* d_buf = nullptr;
+    size_t cap = 0;
+    int blocks_p = 152 * 8, blocks_w = 152 * 8;  // measured best on 64 slab replicas (152 to 1216 tried)
+};
+// (Re)writes the descriptors from the systems' current views (after any list regrowth).
+int rs_batch_setup(RsBatch& rb, const std::vector<Ctx*>& cs, std::string& err);
+void rs_batch_launch(const RsBatch& rb, cudaStream_t s_pair, cudaStream_t s_wall);
+void rs_batch_free(RsBatch& rb);
 // recip.cu
 int recip_setup(Ctx& c, int64_t kmax, const double* x0, const double* y0, const double* z0);
 void recip_fp64(Ctx& c);

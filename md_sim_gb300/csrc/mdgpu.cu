@@ -227,16 +227,24 @@ static bool merge_fusable(const Ctx& c) {
 // to start inside a graph, off the critical path.  defer_merge: leave that final merge kernel to
 // the caller (the resident step fuses it into the corrector).  packed: the records were written by
 // the kernel before (the predictor of a resident step), so the packing kernel is left out.
+// batch_stage (replica batches in phase order, mixed form with walls and no surface atoms): 1 stops
+// after the list build with the head-head and head-wall loops left to the batch's kernels, 2 goes
+// on from there (0: the whole evaluation).
+static bool batch_phased(const Ctx& c) {
+    const View& v = c.v;
+    return c.precision == MDG_MIXED && v.nliqa == v.nmove && v.nwall > 0 && v.nheads > 0;
+}
+
 int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear = false, bool defer_merge = false,
                  bool packed = false) {
     View& v = c.v;
+    const bool hist = c.meas.init && c.meas.force_hist;
+    const bool fused = merge_fusable(c);
     if (c.precision != MDG_MIXED) {
         if (!acc_clear) cudaMemsetAsync(v.acc, 0, sizeof(double) * (2 * v.nijt + ACC_NSLOT), c.stream);
         if (reset_status) cudaMemsetAsync(v.status, 0, sizeof(int) * 2, c.stream);
     }
-    const bool hist = c.meas.init && c.meas.force_hist;
-    const bool fused = merge_fusable(c);
-    if (c.precision == MDG_MIXED) {
+    if (c.precision == MDG_MIXED && c.batch_stage != 2) {
         // The tensor-core reciprocal sum needs only the packed atom records: it runs on a side
         // stream while the main stream does the list, the real-space loops and the wall tail.
         // Without surface atoms (whose z forces after the head-head loop are booked to the walls,
@@ -265,6 +273,12 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
             c.stream = s0;
         }
         PHASE(nnlist_build(c), "nnlist");
+        if (conc && c.batch_stage == 1) {
+            // the loops run in the batch's kernels once every system's list is built
+            MDG_CUDA(cudaEventRecord(c.ev_join2, c.side2));
+            MDG_CUDA(cudaStreamWaitEvent(s0, c.ev_join2, 0));
+            return MDG_OK;
+        }
         if (conc) {
             MDG_CUDA(cudaEventRecord(c.ev_list, s0));
             MDG_CUDA(cudaStreamWaitEvent(c.side2, c.ev_list, 0));
@@ -280,7 +294,9 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
             PHASE(walls_mixed(c), "walls");
             PHASE(lr_tail(c), "lr_tail");
         }
-        MDG_CUDA(cudaStreamWaitEvent(s0, c.ev_join, 0));
+    }
+    if (c.precision == MDG_MIXED) {
+        MDG_CUDA(cudaStreamWaitEvent(c.stream, c.ev_join, 0));
         if (fused) {
             if (!defer_merge) PHASE(merge_force_sum(c, c.d_frc), "merge + force_sum");
         } else {
@@ -1012,9 +1028,9 @@ static void snapshot(Ctx& c, bool restore) {
 static int step_launch(Ctx& c) {
     const bool fp64 = c.precision != MDG_MIXED, shake = c.v.nmove > c.v.nliqa, fuse = merge_fusable(c);
     const bool pack = !fp64 && !shake;  // surface atoms move in SHAKE, after the predictor
-    predict_launch(c, fp64, shake, pack);
+    if (c.batch_stage != 2) predict_launch(c, fp64, shake, pack);
     int rc = launch_force(c, false, false, fp64, fuse, pack);
-    if (rc) return rc;
+    if (rc || c.batch_stage == 1) return rc;
     correct_launch(c, fuse);
     if (shake) shake_launch(c, c.d_ft, true);
     if (c.meas.init && c.meas.profiles) measure_do_launch(c, c.v.x, c.v.y, c.v.z);
@@ -1410,13 +1426,24 @@ int mdg_mlp_train(const float* x, const float* y, int64_t n, int epochs, int bat
 }
 
 // ---------------------------------------------------------------------------------------------
-// Replica batches: independent contexts stepped by one graph launch (their per-step graphs are
-// parallel child graphs of one graph, so the kernels of small systems fill the GPU together).
+// Replica batches: independent contexts stepped by one graph launch.  Two graph forms:
+//   MDG_BATCH_GRAPHS  every replica's step graph is a parallel child graph of one graph, so the
+//                     kernels of small systems fill the GPU together;
+//   MDG_BATCH_PHASES  phase order: every replica's predictor, packing, list build and reciprocal
+//                     branch as in its own step, then the head-head and head-wall loops of all
+//                     replicas (those in the concurrent mixed form: walls, no surface atoms) as
+//                     one persistent kernel each over all their heads, then every replica's merge,
+//                     corrector and SHAKE.  Other replicas keep their whole step in the graph.
 // ---------------------------------------------------------------------------------------------
 struct mdg_batch {
     std::vector<mdg_ctx*> ctx;
     cudaStream_t stream = nullptr;      // stream the batch graph is launched on
     cudaStream_t own_stream = nullptr;  // the batch's own stream (the only one it destroys)
+    cudaStream_t cs = nullptr, cs2 = nullptr;  // capture streams of the phase-ordered graph
+    std::vector<cudaEvent_t> ev;        // its fork and join events: 4 + 2 per replica
+    RsBatch rb;                         // descriptors of the batched real-space loops
+    int mode = MDG_BATCH_PHASES;
+    int phased = 0;                     // replicas in the batched loops (last graph build)
     cudaGraphExec_t exec = nullptr;
     int device = 0;
     std::string err;
@@ -1428,8 +1455,90 @@ static int batch_err(mdg_batch* b, int code, const std::string& m) {
     return code;
 }
 
+static int batch_graph_phases(mdg_batch* b) {
+    const size_t n = b->ctx.size();
+    if (!b->cs) {
+        // the batched loops hold up every replica's merge: as urgent as the reciprocal branches
+        int prio_lo = 0, prio_hi = 0;
+        cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+        if (cudaStreamCreateWithPriority(&b->cs, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&b->cs2, cudaStreamNonBlocking, prio_hi) != cudaSuccess)
+            return batch_err(b, MDG_E_CUDA, "batch: capture streams");
+    }
+    while (b->ev.size() < 4 + 2 * n) {
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return batch_err(b, MDG_E_CUDA, "batch: events");
+        b->ev.push_back(e);
+    }
+    std::vector<Ctx*> ph;
+    std::vector<char> is_ph(n, 0);
+    for (size_t i = 0; i < n; ++i)
+        if (batch_phased(*b->ctx[i])) {
+            ph.push_back(b->ctx[i]);
+            is_ph[i] = 1;
+        }
+    std::string err;
+    int rc = rs_batch_setup(b->rb, ph, err);
+    if (rc) return batch_err(b, rc, err);
+    b->phased = (int)ph.size();
+    cudaEvent_t ev0 = b->ev[0], evf = b->ev[1], evw = b->ev[2], evrs = b->ev[3];
+    auto ev_pre = [&](size_t i) { return b->ev[4 + 2 * i]; };
+    auto ev_post = [&](size_t i) { return b->ev[5 + 2 * i]; };
+    if (cudaStreamBeginCapture(b->cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return batch_err(b, MDG_E_CUDA, "batch: capture");
+    auto fail = [&](int code, const std::string& m) {
+        cudaGraph_t gg = nullptr;
+        cudaStreamEndCapture(b->cs, &gg);
+        if (gg) cudaGraphDestroy(gg);
+        cudaGetLastError();
+        for (auto* cp : b->ctx) cp->batch_stage = 0;
+        return batch_err(b, code, m);
+    };
+    bool ok = cudaEventRecord(ev0, b->cs) == cudaSuccess;
+    for (size_t i = 0; i < n && ok; ++i) {
+        Ctx& c = *b->ctx[i];
+        ok = cudaStreamWaitEvent(c.stream, ev0, 0) == cudaSuccess;
+        c.batch_stage = is_ph[i] ? 1 : 0;
+        rc = step_launch(c);
+        c.batch_stage = 0;
+        if (rc) return fail(rc, "replica " + std::to_string(i) + ": " + c.err);
+        ok = ok && cudaEventRecord(ev_pre(i), c.stream) == cudaSuccess;
+    }
+    if (ok && !ph.empty()) {
+        for (size_t i = 0; i < n && ok; ++i)
+            if (is_ph[i]) ok = cudaStreamWaitEvent(b->cs, ev_pre(i), 0) == cudaSuccess;
+        ok = ok && cudaEventRecord(evf, b->cs) == cudaSuccess && cudaStreamWaitEvent(b->cs2, evf, 0) == cudaSuccess;
+        if (ok) rs_batch_launch(b->rb, b->cs, b->cs2);
+        ok = ok && cudaEventRecord(evw, b->cs2) == cudaSuccess && cudaStreamWaitEvent(b->cs, evw, 0) == cudaSuccess &&
+             cudaEventRecord(evrs, b->cs) == cudaSuccess;
+        for (size_t i = 0; i < n && ok; ++i) {
+            if (!is_ph[i]) continue;
+            Ctx& c = *b->ctx[i];
+            ok = cudaStreamWaitEvent(c.stream, evrs, 0) == cudaSuccess;
+            c.batch_stage = 2;
+            rc = step_launch(c);
+            c.batch_stage = 0;
+            if (rc) return fail(rc, "replica " + std::to_string(i) + ": " + c.err);
+            ok = ok && cudaEventRecord(ev_post(i), c.stream) == cudaSuccess;
+        }
+    }
+    for (size_t i = 0; i < n && ok; ++i)
+        ok = cudaStreamWaitEvent(b->cs, is_ph[i] ? ev_post(i) : ev_pre(i), 0) == cudaSuccess;
+    if (!ok) return fail(MDG_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(cudaGetLastError()));
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(b->cs, &g);
+    if (ce != cudaSuccess) return batch_err(b, MDG_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(ce));
+    const cudaError_t e = cudaGraphInstantiate(&b->exec, g, cudaGraphInstantiateFlagUseNodePriority);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return batch_err(b, MDG_E_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
+    return MDG_OK;
+}
+
 static int batch_graph(mdg_batch* b) {
     if (b->exec) return MDG_OK;
+    if (b->mode == MDG_BATCH_PHASES) return batch_graph_phases(b);
+    b->phased = 0;
     cudaGraph_t g;
     if (cudaGraphCreate(&g, 0) != cudaSuccess) return batch_err(b, MDG_E_CUDA, "cudaGraphCreate failed");
     for (size_t i = 0; i < b->ctx.size(); ++i) {
@@ -1481,6 +1590,10 @@ void mdg_batch_destroy(mdg_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);  // a caller's stream stays the caller's
+    if (b->cs) cudaStreamDestroy(b->cs);
+    if (b->cs2) cudaStreamDestroy(b->cs2);
+    for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
+    rs_batch_free(b->rb);
     delete b;
 }
 
@@ -1493,6 +1606,22 @@ int mdg_batch_set_stream(mdg_batch* b, void* stream) {
     b->stream = stream ? (cudaStream_t)stream : b->own_stream;
     return MDG_OK;
 }
+
+int mdg_batch_set_mode(mdg_batch* b, int mode, int pair_blocks, int wall_blocks) {
+    if (!b) return batch_err(nullptr, MDG_E_ARG, "null batch");
+    if ((mode != MDG_BATCH_GRAPHS && mode != MDG_BATCH_PHASES) || pair_blocks < 0 || wall_blocks < 0)
+        return batch_err(b, MDG_E_ARG, "mdg_batch_set_mode: bad argument");
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    b->mode = mode;
+    b->rb.blocks_p = pair_blocks > 0 ? pair_blocks : RsBatch().blocks_p;
+    b->rb.blocks_w = wall_blocks > 0 ? wall_blocks : RsBatch().blocks_w;
+    return MDG_OK;
+}
+
+int mdg_batch_phased(const mdg_batch* b) { return b ? b->phased : 0; }
 
 int mdg_batch_run_async(mdg_batch* b, int64_t nsteps) {
     if (!b) return batch_err(nullptr, MDG_E_ARG, "null batch");

@@ -46,7 +46,6 @@ struct Kahan {
         s = t;
     }
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-    __device__ __forceinline__ float valuef() const { return s - c; }
 };
 
 __device__ __forceinline__ float warp_sumf(float x) {
@@ -71,17 +70,19 @@ __device__ __forceinline__ void e_flush(EAcc& e, double* s_e, int nijt) {
     e.qq = Kahan();
 }
 
-// End of the loops: lanes holding the warp's (largest) pair type reduce with shuffles, one shared
-// atomic per warp; lanes left with another type (mixed-type systems) flush one by one.
+// End of the loops: lanes holding the warp's (largest) pair type reduce with shuffles in FP64 (a
+// warp's total grows with the heads it took, and an FP32 reduction of it would round at that
+// size), one shared atomic per warp; lanes left with another type (mixed-type systems) flush one
+// by one.
 __device__ __forceinline__ void e_final(EAcc& e, double* s_e, int nijt) {
     const int ij0 = __reduce_max_sync(0xffffffffu, e.ijt);
     if (ij0 < 0) return;
     const bool mine = e.ijt == ij0;
-    const float lj = warp_sumf(mine ? e.lj.valuef() : 0.f);
-    const float qq = warp_sumf(mine ? e.qq.valuef() : 0.f);
+    const double lj = warp_sum(mine ? e.lj.value() : 0.0);
+    const double qq = warp_sum(mine ? e.qq.value() : 0.0);
     if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&s_e[ij0], (double)lj);
-        atomicAdd(&s_e[nijt + ij0], (double)qq);
+        atomicAdd(&s_e[ij0], lj);
+        atomicAdd(&s_e[nijt + ij0], qq);
     }
     if (!mine) e_flush(e, s_e, nijt);
 }
@@ -205,16 +206,13 @@ __device__ __forceinline__ float vdw_term(const float* par, float rsqi, float ri
     return 0.f;
 }
 
+// The head-head loop of one warp over the heads h0, h0 + hs, ... below v.nheads.
 template <int ZPER>
-__global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
-    extern __shared__ double s_e[];
-    const Tables T = load_tables(v, pk, s_e, 0);
+__device__ __forceinline__ void pair_heads(const View& v, const Pk& pk, const Tables& T, int h0, int hs, EAcc& e,
+                                           double* s_e) {
     const int lane = threadIdx.x & 31;
-    const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const int nwarps = gridDim.x * kWarps;
     const float alfa = pk.alfa, spii = pk.spii, facq = pk.facq, rcutsq = pk.rcutsq;
-    EAcc e;
-    for (int h = warp; h < v.nheads; h += nwarps) {
+    for (int h = h0; h < v.nheads; h += hs) {
         const int i = v.head_atom[h];
         const uint4 pi = pk.P[i];
         const int it = (int)(pi.w & 0x7fffffffu);
@@ -298,34 +296,60 @@ __global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
             if (lane == 0) red_v4(&pk.F[i + a], sx, sy, sz);
         }
     }
+}
+
+// The block's energy sums into the system's accumulators (all threads; the shared sums are free
+// for the next system's tables afterwards).
+__device__ __forceinline__ void pair_flush(const View& v, EAcc& e, double* s_e) {
     e_final(e, s_e, v.nijt);
+    e = EAcc();
     __syncthreads();
     for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x)
         if (s_e[k] != 0.0) atomicAdd(&v.acc[k], s_e[k]);
+    __syncthreads();
 }
 
 template <int ZPER>
-__global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
+__global__ void __launch_bounds__(kNT) k_pair_mx(View v, Pk pk) {
     extern __shared__ double s_e[];
-    const Tables T = load_tables(v, pk, s_e, 6);
-    const int lane = threadIdx.x & 31;
-    const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const int nwarps = gridDim.x * kWarps;
-    const float alfa = pk.alfa, spii = pk.spii, facq = pk.facq, rcutsq = pk.rcutsq;
-    // energy sums per wall site type (the last two site types): the two alternate from partner to
-    // partner, and one accumulator per type avoids a flush on every change
+    const Tables T = load_tables(v, pk, s_e, 0);
+    EAcc e;
+    pair_heads<ZPER>(v, pk, T, blockIdx.x * kWarps + (threadIdx.x >> 5), gridDim.x * kWarps, e, s_e);
+    pair_flush(v, e, s_e);
+}
+
+// Head-wall work units of a system: (head, segment of seg wall partners), so that the few heads
+// next to a wall with hundreds of partners are shared by several warps (seg = kWSeg for one
+// system; a batch of systems has parallelism to spare and takes kWSegBatch, which halves the per-unit
+// work of the head's loads and reductions).  A lane sees at most seg / 32 partners per unit, so its
+// FP32 sums within a unit are short and need no compensation.
+constexpr int kWSegBatch = 256;
+__host__ __device__ __forceinline__ long wall_units(const View& v, int seg) {
+    return (long)v.nheads * ((v.maxwnb + seg - 1) / seg);
+}
+
+// Energy sums per wall site type (the last two site types; the two alternate from partner to
+// partner, and one accumulator per type avoids a flush on every change) and the wall reaction
+// sums of the lane, added per work unit.
+struct WAcc {
     EAcc ew[2];
+    double ws[6] = {0, 0, 0, 0, 0, 0};
+    double* s_e = nullptr;  // the block's shared energy sums
+};
+
+// The head-wall loop of one warp over the units u0, u0 + us, ... below wall_units(v, seg).
+template <int ZPER>
+__device__ __forceinline__ void wall_heads(const View& v, const Pk& pk, const Tables& T, long u0, long us, int seg,
+                                           WAcc& w) {
+    const int lane = threadIdx.x & 31;
+    const float alfa = pk.alfa, spii = pk.spii, facq = pk.facq, rcutsq = pk.rcutsq;
     const int wt0 = v.nit - 2;
-    double ws[6] = {0, 0, 0, 0, 0, 0};  // wall reaction sums of this lane, added per work item
-    // work items: (head, segment of kWSeg wall partners), so that the few heads next to a wall
-    // with hundreds of partners are shared by several warps.  A lane sees at most kWSeg / 32
-    // partners per item, so its FP32 sums within an item are short and need no compensation.
-    const int nseg = (v.maxwnb + kWSeg - 1) / kWSeg;
+    const int nseg = (v.maxwnb + seg - 1) / seg;
     const long nitems = (long)v.nheads * nseg;
-    for (long item = warp; item < nitems; item += nwarps) {
-        const int h = (int)(item / nseg), seg = (int)(item % nseg);
-        const int n = min(v.wnbcnt[h], (seg + 1) * kWSeg);
-        if (seg * kWSeg >= n) continue;
+    for (long item = u0; item < nitems; item += us) {
+        const int h = (int)(item / nseg), sg = (int)(item % nseg);
+        const int n = min(v.wnbcnt[h], (sg + 1) * seg);
+        if (sg * seg >= n) continue;
         const int i = v.head_atom[h];
         const uint4 pi = pk.P[i];
         const int it = (int)(pi.w & 0x7fffffffu);
@@ -335,22 +359,40 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
         float4 si[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) si[a] = a < nsi_i ? pk.Q[i + a] : make_float4(0.f, 0.f, 0.f, 0.f);
-        float fix[3] = {0, 0, 0}, fiy[3] = {0, 0, 0}, fiz[3] = {0, 0, 0}, wsi[6] = {0, 0, 0, 0, 0, 0};
+        float fix[3] = {0, 0, 0}, fiy[3] = {0, 0, 0}, fiz[3] = {0, 0, 0};
+        // wall reaction sums of this unit, lower wall (z < 0) in l*, upper in u*: plain registers
+        // updated through selects (x - 0 is exact, so each sum is what a per-wall array gives)
+        float lx = 0.f, ly = 0.f, lz = 0.f, ux = 0.f, uy = 0.f, uz = 0.f;
         const int* nb = v.wnb + (size_t)h * v.maxwnb;
-        for (int k = seg * kWSeg + lane; k < n; k += 32) {
-            const int j = nb[k];
-            const uint4 pj = pk.P[j];
+        const float* qw = reinterpret_cast<const float*>(pk.Q) + 3;  // charges: Q[j].w = qw[4 j]
+        // software pipeline as in the head-head loop: the next partner's record and charge and
+        // the index after it load while this partner is computed
+        const int k0 = sg * seg + lane;
+        int j1 = k0 < n ? nb[k0] : 0;
+        int j2 = k0 + 32 < n ? nb[k0 + 32] : 0;
+        uint4 p1 = k0 < n ? pk.P[j1] : make_uint4(0u, 0u, 0u, 0u);
+        float q1 = k0 < n ? qw[4 * (size_t)j1] : 0.f;
+        for (int k = k0; k < n; k += 32) {
+            const int j = j1;
+            const uint4 pj = p1;
+            const float qj = q1;
+            j1 = j2;
+            if (k + 32 < n) {
+                p1 = pk.P[j1];
+                q1 = qw[4 * (size_t)j1];
+            }
+            if (k + 64 < n) j2 = nb[k + 64];
             float xi, yi, zi;
             head_vec<ZPER>(pi, zli, pj, pk, j, xi, yi, zi);
             const float rsq = xi * xi + yi * yi + zi * zi;
             if (rsq > rcutsq) continue;
-            const int so = (pj.w & 0x80000000u) ? 0 : 3;
+            const bool lower = (pj.w & 0x80000000u) != 0;
             const int jt = (int)(pj.w & 0x7fffffffu);
             const int ijt = T.ijt[it * v.nit + jt];
             const float rinv = rsqrtf(rsq);
             float fij;
             const float elj = vdw_term(T.par + 6 * ijt, rinv * rinv, rinv, rsq * rinv, &fij);
-            const float qx = facq * pk.Q[j].w;
+            const float qx = facq * qj;
             float eqq = 0.f;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
@@ -367,11 +409,15 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
                 fiy[a] = fmaf(yd, fij, fiy[a]);
                 fiz[a] = fmaf(zd, fij, fiz[a]);
                 if (book) {
-                    wsi[so] -= xd * fij; wsi[so + 1] -= yd * fij; wsi[so + 2] -= zd * fij;
+                    const float sx = xd * fij, sy = yd * fij, sz = zd * fij;
+                    lx -= lower ? sx : 0.f; ly -= lower ? sy : 0.f; lz -= lower ? sz : 0.f;
+                    ux -= lower ? 0.f : sx; uy -= lower ? 0.f : sy; uz -= lower ? 0.f : sz;
                 }
                 fij = 0.f;
             }
-            e_add(ew[min(max(jt - wt0, 0), 1)], ijt, elj, eqq, s_e, v.nijt);
+            // energy sums per wall site type (the last two site types)
+            if (jt > wt0) e_add(w.ew[1], ijt, elj, eqq, w.s_e, v.nijt);
+            else e_add(w.ew[0], ijt, elj, eqq, w.s_e, v.nijt);
         }
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -379,16 +425,25 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
             const float sx = warp_sumf(fix[a]), sy = warp_sumf(fiy[a]), sz = warp_sumf(fiz[a]);
             if (lane == 0) red_v4(&pk.F[i + a], sx, sy, sz);
         }
-        if (book)
-#pragma unroll
-            for (int k = 0; k < 6; ++k) ws[k] += (double)wsi[k];
+        if (book) {
+            w.ws[0] += (double)lx; w.ws[1] += (double)ly; w.ws[2] += (double)lz;
+            w.ws[3] += (double)ux; w.ws[4] += (double)uy; w.ws[5] += (double)uz;
+        }
     }
-    e_final(ew[0], s_e, v.nijt);
-    e_final(ew[1], s_e, v.nijt);
+}
+
+// The block's energy and wall reaction sums into the system's accumulators (all threads).
+__device__ __forceinline__ void wall_flush(const View& v, WAcc& w) {
+    double* s_e = w.s_e;
+    e_final(w.ew[0], s_e, v.nijt);
+    e_final(w.ew[1], s_e, v.nijt);
+    w.ew[0] = EAcc();
+    w.ew[1] = EAcc();
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        const double s = warp_sum(ws[k]);
-        if (lane == 0 && s != 0.0) atomicAdd(&s_e[2 * v.nijt + k], s);
+        const double s = warp_sum(w.ws[k]);
+        if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(&s_e[2 * v.nijt + k], s);
+        w.ws[k] = 0.0;
     }
     __syncthreads();
     for (int k = threadIdx.x; k < 2 * v.nijt; k += blockDim.x)
@@ -398,6 +453,111 @@ __global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
         const double s = s_e[2 * v.nijt + threadIdx.x];
         if (s != 0.0) atomicAdd(&v.acc[2 * v.nijt + ACC_FWS + comp * 3 + (sg ? 2 : 0)], s);
     }
+    __syncthreads();
+}
+
+template <int ZPER>
+__global__ void __launch_bounds__(kNT) k_wall_mx(View v, Pk pk) {
+    extern __shared__ double s_e[];
+    const Tables T = load_tables(v, pk, s_e, 6);
+    WAcc w;
+    w.s_e = s_e;
+    wall_heads<ZPER>(v, pk, T, blockIdx.x * kWarps + (threadIdx.x >> 5), (long)gridDim.x * kWarps, kWSeg, w);
+    wall_flush(v, w);
+}
+
+// ---- the same loops over several systems in one launch (replica batches) -------------------
+// Each system's heads (or head-wall units) are cut into work items of about kItemUnits units; the
+// items of system r are r's first item .. its next system's first item, and item k of a system with
+// n items holds its units k, k + n, k + 2n, ... (a stride through the whole system, so that items
+// near a wall and items in the middle of a film cost alike).  Block b walks the items
+// [b N / G, (b + 1) N / G) of all N in order: its system changes only a few times, and then it
+// flushes the finished system's energies and loads the next one's view and tables into shared
+// memory.
+constexpr int kItemUnits = 64;
+
+struct alignas(16) RsRep {
+    View v;
+    Pk pk;
+};
+
+// View and Pk copied word by word into shared memory (plain data: pointers, sizes, scalars).
+__device__ __forceinline__ void load_rep(const RsRep* __restrict__ src, RsRep* dst) {
+    static_assert(sizeof(RsRep) % 8 == 0, "word copy");
+    const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(RsRep) / 8); k += blockDim.x) d[k] = s[k];
+    __syncthreads();
+}
+
+// The system of item it: the first r with first[r + 1] > it, searched from r (items in order).
+__device__ __forceinline__ int rep_of(const int* __restrict__ first, int nrep, int it, int r) {
+    if (r < 0) {
+        int lo = 0, hi = nrep - 1;  // first[0] = 0 <= it < first[nrep]
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (first[mid] <= it) lo = mid;
+            else hi = mid - 1;
+        }
+        r = lo;
+    }
+    while (r < nrep - 1 && first[r + 1] <= it) ++r;
+    return r;
+}
+
+template <int ZPER>
+__global__ void __launch_bounds__(kNT) k_pair_mx_batch(const RsRep* __restrict__ reps, const int* __restrict__ first,
+                                                        int nrep) {
+    extern __shared__ double s_e[];
+    __shared__ alignas(16) unsigned char sr_raw[sizeof(RsRep)];  // RsRep has member initialisers
+    RsRep& sr = *reinterpret_cast<RsRep*>(sr_raw);
+    const int nitems = first[nrep];
+    const int b0 = (int)((long)nitems * blockIdx.x / gridDim.x);
+    const int b1 = (int)((long)nitems * (blockIdx.x + 1) / gridDim.x);
+    const int warp = threadIdx.x >> 5;
+    int r = -1;
+    Tables T{};
+    EAcc e;
+    for (int it = b0; it < b1; ++it) {
+        const int rn = rep_of(first, nrep, it, r);
+        if (rn != r) {
+            if (r >= 0) pair_flush(sr.v, e, s_e);
+            load_rep(reps + rn, &sr);
+            T = load_tables(sr.v, sr.pk, s_e, 0);
+            r = rn;
+        }
+        const int n = first[r + 1] - first[r], k = it - first[r];
+        pair_heads<ZPER>(sr.v, sr.pk, T, k + n * warp, n * kWarps, e, s_e);
+    }
+    if (r >= 0) pair_flush(sr.v, e, s_e);
+}
+
+template <int ZPER>
+__global__ void __launch_bounds__(kNT) k_wall_mx_batch(const RsRep* __restrict__ reps, const int* __restrict__ first,
+                                                        int nrep) {
+    extern __shared__ double s_e[];
+    __shared__ alignas(16) unsigned char sr_raw[sizeof(RsRep)];  // RsRep has member initialisers
+    RsRep& sr = *reinterpret_cast<RsRep*>(sr_raw);
+    const int nitems = first[nrep];
+    const int b0 = (int)((long)nitems * blockIdx.x / gridDim.x);
+    const int b1 = (int)((long)nitems * (blockIdx.x + 1) / gridDim.x);
+    const int warp = threadIdx.x >> 5;
+    int r = -1;
+    Tables T{};
+    WAcc w;
+    w.s_e = s_e;
+    for (int it = b0; it < b1; ++it) {
+        const int rn = rep_of(first, nrep, it, r);
+        if (rn != r) {
+            if (r >= 0) wall_flush(sr.v, w);
+            load_rep(reps + rn, &sr);
+            T = load_tables(sr.v, sr.pk, s_e, 6);
+            r = rn;
+        }
+        const long n = first[r + 1] - first[r], k = it - first[r];
+        wall_heads<ZPER>(sr.v, sr.pk, T, k + n * warp, n * kWarps, kWSegBatch, w);
+    }
+    if (r >= 0) wall_flush(sr.v, w);
 }
 
 // F (and the reciprocal forces frc, 3 x nmove, when given) into the FP64 forces; F cleared.
@@ -503,6 +663,93 @@ void walls_mixed(Ctx& c, bool concurrent) {
     if (concurrent) nb = std::min(nb, 152);
     if (c.pk.zper) k_wall_mx<1><<<nb, kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
     else k_wall_mx<0><<<nb, kNT, table_smem(v, 6), c.stream>>>(v, c.pk);
+}
+
+// ---- replica batches: host side ------------------------------------------------------------
+int rs_batch_setup(RsBatch& rb, const std::vector<Ctx*>& cs, std::string& err) {
+    std::vector<RsRep> reps[2];
+    std::vector<int> fp[2], fw[2];
+    size_t smem[2][2] = {{0, 0}, {0, 0}};
+    for (Ctx* c : cs) {
+        const int g = c->pk.zper ? 1 : 0;
+        RsRep r;
+        r.v = c->v;
+        r.pk = c->pk;
+        if (fp[g].empty()) {
+            fp[g].push_back(0);
+            fw[g].push_back(0);
+        }
+        const long nw = wall_units(c->v, kWSegBatch);
+        fp[g].push_back(fp[g].back() + (c->v.nheads + kItemUnits - 1) / kItemUnits);
+        fw[g].push_back(fw[g].back() + (int)((nw + kItemUnits - 1) / kItemUnits));
+        reps[g].push_back(r);
+        smem[g][0] = std::max(smem[g][0], table_smem(c->v, 0));
+        smem[g][1] = std::max(smem[g][1], table_smem(c->v, 6));
+    }
+    size_t need = 0;
+    size_t off[2][3];
+    for (int g = 0; g < 2; ++g) {
+        off[g][0] = need;
+        need += (sizeof(RsRep) * reps[g].size() + 255) & ~size_t(255);
+        off[g][1] = need;
+        need += (sizeof(int) * fp[g].size() + 255) & ~size_t(255);
+        off[g][2] = need;
+        need += (sizeof(int) * fw[g].size() + 255) & ~size_t(255);
+    }
+    if (need > rb.cap) {
+        if (rb.d_buf) cudaFree(rb.d_buf);
+        rb.d_buf = nullptr;
+        rb.cap = 0;
+        if (cudaMalloc(&rb.d_buf, need) != cudaSuccess) {
+            err = "replica batch: descriptor allocation failed";
+            return MDG_E_CUDA;
+        }
+        rb.cap = need;
+    }
+    unsigned char* base = static_cast<unsigned char*>(rb.d_buf);
+    for (int g = 0; g < 2; ++g) {
+        RsBatch::Group& G = rb.g[g];
+        G = RsBatch::Group();
+        G.nrep = (int)reps[g].size();
+        if (G.nrep == 0) continue;
+        G.reps = base + off[g][0];
+        G.first_p = reinterpret_cast<int*>(base + off[g][1]);
+        G.first_w = reinterpret_cast<int*>(base + off[g][2]);
+        G.items_p = fp[g].back();
+        G.items_w = fw[g].back();
+        G.smem_p = smem[g][0];
+        G.smem_w = smem[g][1];
+        if (cudaMemcpy(G.reps, reps[g].data(), sizeof(RsRep) * G.nrep, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(G.first_p, fp[g].data(), sizeof(int) * fp[g].size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(G.first_w, fw[g].data(), sizeof(int) * fw[g].size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            err = "replica batch: descriptor upload failed";
+            return MDG_E_CUDA;
+        }
+    }
+    return MDG_OK;
+}
+
+void rs_batch_launch(const RsBatch& rb, cudaStream_t sp, cudaStream_t sw) {
+    for (int g = 0; g < 2; ++g) {
+        const RsBatch::Group& G = rb.g[g];
+        if (G.nrep == 0) continue;
+        const RsRep* reps = static_cast<const RsRep*>(G.reps);
+        if (G.items_w > 0) {
+            const int nb = std::max(1, std::min(rb.blocks_w, G.items_w));
+            if (g) k_wall_mx_batch<1><<<nb, kNT, G.smem_w, sw>>>(reps, G.first_w, G.nrep);
+            else k_wall_mx_batch<0><<<nb, kNT, G.smem_w, sw>>>(reps, G.first_w, G.nrep);
+        }
+        if (G.items_p > 0) {
+            const int nb = std::max(1, std::min(rb.blocks_p, G.items_p));
+            if (g) k_pair_mx_batch<1><<<nb, kNT, G.smem_p, sp>>>(reps, G.first_p, G.nrep);
+            else k_pair_mx_batch<0><<<nb, kNT, G.smem_p, sp>>>(reps, G.first_p, G.nrep);
+        }
+    }
+}
+
+void rs_batch_free(RsBatch& rb) {
+    if (rb.d_buf) cudaFree(rb.d_buf);
+    rb = RsBatch();
 }
 
 }  // namespace mdg
