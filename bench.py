@@ -865,6 +865,8 @@ def profile_run(args):
     from md_sim_gb300.abi import MDG_FP64, MDG_MIXED
 
     lib = md_sim_gb300.load()
+    if args.config == "replicas64":
+        return profile_batch(args, lib)
     s, prm, desc = make_workload(args.config)
     prm.precision = MDG_MIXED if args.precision == "mixed" else MDG_FP64
     ctx = abi.Context(lib, s, prm)
@@ -874,6 +876,36 @@ def profile_run(args):
     rep = ctx.check()
     print(json.dumps({"profile_steps": args.steps, "kernels_per_step": ctx.kernels_per_step(),
                       "tempnow": rep["tempnow"]}))
+
+
+def profile_batch(args, lib):
+    """Replica batch for ncu: create, one checked batch step per graph form, then one step in phase
+    order inside the NVTX range "phases" and one as child graphs inside "graphs"."""
+    import torch
+
+    from md_sim_gb300 import abi, configs
+
+    ctxs = []
+    for s, prm in configs.replica_slabs(n=args.replicas):
+        prm.precision = abi.MDG_MIXED
+        c = abi.Context(lib, s, prm)
+        c.set_state(s)
+        ctxs.append(c)
+    batch = abi.Batch(lib, ctxs)
+    out = {"profile_steps": 1, "replicas": len(ctxs)}
+    for name, mode in (("phases", abi.MDG_BATCH_PHASES), ("graphs", abi.MDG_BATCH_GRAPHS)):
+        batch.set_mode(mode)
+        batch.run(1)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push(name)
+        batch.run_async(1)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        out[name + "_phased"] = batch.phased()
+    for c in ctxs:
+        c.check()
+    batch.close()
+    print(json.dumps(out))
 
 
 def main():
