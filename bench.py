@@ -709,6 +709,7 @@ def replicas_arm(args, rank=0, world=1):
     t_other = float(np.sum([a.elapsed_time(b) for a, b in eo])) / Ko * 1e-3
     for c in ctxs:
         c.check()
+    batch.close()  # the replicas step alone again with their own plans
     # the same replicas one after another, each with its own graph, on the same stream
     for c in ctxs:
         c.set_stream(stream.cuda_stream)
@@ -727,7 +728,6 @@ def replicas_arm(args, rank=0, world=1):
     t_seq = a_.elapsed_time(b_) * 1e-3 / Ks
     for c in ctxs:
         c.check()
-    batch.close()
     atoms = int(sum(s.ntota for s, _ in systems))
     waters = int(sum(s.nrig for s, _ in systems))
     dt = systems[0][0].dt

@@ -348,7 +348,11 @@ int mdg_batch_set_stream(mdg_batch* b, void* stream);
 int mdg_batch_run(mdg_batch* b, int64_t nsteps, mdg_report* reps);
 /* nsteps graph launches on the batch stream, no checks (for timing; then mdg_check per context) */
 int mdg_batch_run_async(mdg_batch* b, int64_t nsteps);
-/* Graph form of the batch (the next run builds it):
+/* Replicas in a batch share the GPU: while a batch exists, the tensor-core reciprocal passes of its
+ * mixed-precision replicas are planned for throughput (the fewest CTAs: pass 1 in chunks of about
+ * 1024 atoms, pass 2 whole atom tiles) instead of spreading each replica over every SM;
+ * mdg_batch_destroy restores each replica's own plan.
+ * Graph form of the batch (the next run builds it):
  *   MDG_BATCH_PHASES (default)  phase order: the head-head and head-wall loops of all replicas in
  *       the mixed form with walls and no surface atoms run as one persistent kernel each over all
  *       their heads (pair_blocks / wall_blocks blocks; 0 = 1216), between the replicas' own list

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 import dataclasses
+import weakref
 from typing import Dict, Optional
 
 import numpy as np
@@ -291,6 +292,9 @@ class Context:
         self.eqq = np.zeros(n)
 
     def close(self):
+        # a batch over this context goes first (mdg_batch_destroy restores its replicas' plans)
+        for b in list(getattr(self, "_batches", ())):
+            b.close()
         if getattr(self, "h", None):
             self.lib.destroy(self.h)
             self.h = None
@@ -633,6 +637,10 @@ class Batch:
         if rc != MDG_OK:
             raise MdgError(rc, (lib.batch_last_error(None) or b"").decode())
         self.h = h
+        for c in self.ctxs:  # closing a context closes this batch first
+            if not hasattr(c, "_batches"):
+                c._batches = weakref.WeakSet()
+            c._batches.add(self)
 
     def _check(self, rc):
         if rc != MDG_OK:

@@ -160,6 +160,11 @@ struct TcPlan {
     int4* chunk2 = nullptr;  // per pass-2 chunk: image byte offset, first K step, K steps
     int4* items2 = nullptr;  // per pass-2 CTA: atom tile, first chunk, end chunk, whole tile (1) or piece (0)
     int nitems2 = 0;
+    int4* items2_k[2] = {nullptr, nullptr};  // the item tables: pieces (system alone), whole tiles (throughput)
+    int nitems2_k[2] = {0, 0}, zero2_k[2] = {0, 0};
+    std::vector<int> h_chunk_ks;  // K steps of each pass-2 chunk (host)
+    bool throughput = false;      // planned for throughput among many systems (recip_tc_throughput)
+    int mult_alone = 2;           // pass-1 CTA multiple of the plan for the system alone
     int zero2 = 0;           // first atom of the tiles split into pieces (their forces are summed atomically)
     size_t img_bytes = 0;
 };
@@ -259,6 +264,19 @@ struct Ctx {
 int nnlist_setup(Ctx& c, const double* x0, const double* y0, const double* z0);
 void nnlist_trigger(Ctx& c, bool force);
 void nnlist_build(Ctx& c);
+// The list build of several systems as five launches in all (replica batches); descriptors and
+// block tables on the device, rewritten from the systems' current views by the setup.
+struct LsBatch {
+    void* d_buf = nullptr;
+    size_t cap = 0;
+    void* reps = nullptr;
+    int* first[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int nblk[5] = {0, 0, 0, 0, 0};
+    int nrep = 0;
+};
+int ls_batch_setup(LsBatch& lb, const std::vector<Ctx*>& cs, std::string& err);
+void ls_batch_launch(const LsBatch& lb, cudaStream_t st);
+void ls_batch_free(LsBatch& lb);
 // pair.cu
 void pair_forces_fp64(Ctx& c);
 void wall_forces_fp64(Ctx& c);
@@ -307,6 +325,10 @@ void recip_energy_launch(Ctx& c);
 // recip_tc.cu
 int recip_tc_setup(Ctx& c);
 int tc_plan_pass1(Ctx& c, int tpc, int mult);
+// on: the fewest CTAs per pass (pass 1 in chunks of about 1024 atoms, pass 2 whole tiles), for a
+// system stepped among many in one graph; off: back to the plan for the system alone.  Drops the
+// context's captured graphs.
+int recip_tc_throughput(Ctx& c, bool on);
 void recip_tc(Ctx& c);
 int umma_selftest(int n, int k, const float* a, const float* b, float* d, std::string& err);
 // mlp.cu

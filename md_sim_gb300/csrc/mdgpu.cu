@@ -228,8 +228,8 @@ static bool merge_fusable(const Ctx& c) {
 // the caller (the resident step fuses it into the corrector).  packed: the records were written by
 // the kernel before (the predictor of a resident step), so the packing kernel is left out.
 // batch_stage (replica batches in phase order, mixed form with walls and no surface atoms): 1 stops
-// after the list build with the head-head and head-wall loops left to the batch's kernels, 2 goes
-// on from there (0: the whole evaluation).
+// after the rebuild decision with the list build and the head-head and head-wall loops left to the
+// batch's kernels, 2 goes on from there (0: the whole evaluation).
 static bool batch_phased(const Ctx& c) {
     const View& v = c.v;
     return c.precision == MDG_MIXED && v.nliqa == v.nmove && v.nwall > 0 && v.nheads > 0;
@@ -272,13 +272,14 @@ int launch_force(Ctx& c, bool force_rebuild, bool reset_status, bool acc_clear =
             lr_tail(c);
             c.stream = s0;
         }
-        PHASE(nnlist_build(c), "nnlist");
         if (conc && c.batch_stage == 1) {
-            // the loops run in the batch's kernels once every system's list is built
+            // the list build and the loops run in the batch's kernels once every system has its
+            // rebuild decision
             MDG_CUDA(cudaEventRecord(c.ev_join2, c.side2));
             MDG_CUDA(cudaStreamWaitEvent(s0, c.ev_join2, 0));
             return MDG_OK;
         }
+        PHASE(nnlist_build(c), "nnlist");
         if (conc) {
             MDG_CUDA(cudaEventRecord(c.ev_list, s0));
             MDG_CUDA(cudaStreamWaitEvent(c.side2, c.ev_list, 0));
@@ -1429,11 +1430,12 @@ int mdg_mlp_train(const float* x, const float* y, int64_t n, int epochs, int bat
 // Replica batches: independent contexts stepped by one graph launch.  Two graph forms:
 //   MDG_BATCH_GRAPHS  every replica's step graph is a parallel child graph of one graph, so the
 //                     kernels of small systems fill the GPU together;
-//   MDG_BATCH_PHASES  phase order: every replica's predictor, packing, list build and reciprocal
-//                     branch as in its own step, then the head-head and head-wall loops of all
-//                     replicas (those in the concurrent mixed form: walls, no surface atoms) as
-//                     one persistent kernel each over all their heads, then every replica's merge,
-//                     corrector and SHAKE.  Other replicas keep their whole step in the graph.
+//   MDG_BATCH_PHASES  phase order: every replica's predictor, packing close (rebuild decision),
+//                     wall tail and reciprocal branch as in its own step, then, for the replicas
+//                     in the concurrent mixed form (walls, no surface atoms), the list build as
+//                     five launches in all and the head-head and head-wall loops as one persistent
+//                     kernel each over all their heads, then every replica's merge, corrector and
+//                     SHAKE.  Other replicas keep their whole step in the graph.
 // ---------------------------------------------------------------------------------------------
 struct mdg_batch {
     std::vector<mdg_ctx*> ctx;
@@ -1442,6 +1444,7 @@ struct mdg_batch {
     cudaStream_t cs = nullptr, cs2 = nullptr;  // capture streams of the phase-ordered graph
     std::vector<cudaEvent_t> ev;        // its fork and join events: 4 + 2 per replica
     RsBatch rb;                         // descriptors of the batched real-space loops
+    LsBatch lb;                         // and of the batched list build
     int mode = MDG_BATCH_PHASES;
     int phased = 0;                     // replicas in the batched loops (last graph build)
     cudaGraphExec_t exec = nullptr;
@@ -1480,6 +1483,7 @@ static int batch_graph_phases(mdg_batch* b) {
         }
     std::string err;
     int rc = rs_batch_setup(b->rb, ph, err);
+    if (!rc) rc = ls_batch_setup(b->lb, ph, err);
     if (rc) return batch_err(b, rc, err);
     b->phased = (int)ph.size();
     cudaEvent_t ev0 = b->ev[0], evf = b->ev[1], evw = b->ev[2], evrs = b->ev[3];
@@ -1508,6 +1512,7 @@ static int batch_graph_phases(mdg_batch* b) {
     if (ok && !ph.empty()) {
         for (size_t i = 0; i < n && ok; ++i)
             if (is_ph[i]) ok = cudaStreamWaitEvent(b->cs, ev_pre(i), 0) == cudaSuccess;
+        if (ok) ls_batch_launch(b->lb, b->cs);
         ok = ok && cudaEventRecord(evf, b->cs) == cudaSuccess && cudaStreamWaitEvent(b->cs2, evf, 0) == cudaSuccess;
         if (ok) rs_batch_launch(b->rb, b->cs, b->cs2);
         ok = ok && cudaEventRecord(evw, b->cs2) == cudaSuccess && cudaStreamWaitEvent(b->cs, evw, 0) == cudaSuccess &&
@@ -1535,8 +1540,22 @@ static int batch_graph_phases(mdg_batch* b) {
     return MDG_OK;
 }
 
+// Replicas in a batch share the GPU, so their tensor-core passes take the fewest CTAs (each CTA
+// holds an SM for its set-up; one system alone instead spreads its passes over every SM).
+static int batch_plans(mdg_batch* b, bool on) {
+    for (size_t i = 0; i < b->ctx.size(); ++i) {
+        Ctx& c = *b->ctx[i];
+        if (c.precision != MDG_MIXED || !c.tcp.ready) continue;
+        const int rc = recip_tc_throughput(c, on);
+        if (rc) return batch_err(b, rc, "replica " + std::to_string(i) + ": " + c.err);
+    }
+    return MDG_OK;
+}
+
 static int batch_graph(mdg_batch* b) {
     if (b->exec) return MDG_OK;
+    const int prc = batch_plans(b, true);
+    if (prc) return prc;
     if (b->mode == MDG_BATCH_PHASES) return batch_graph_phases(b);
     b->phased = 0;
     cudaGraph_t g;
@@ -1589,11 +1608,13 @@ void mdg_batch_destroy(mdg_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
+    batch_plans(b, false);  // the contexts step alone again with their own plans
     if (b->own_stream) cudaStreamDestroy(b->own_stream);  // a caller's stream stays the caller's
     if (b->cs) cudaStreamDestroy(b->cs);
     if (b->cs2) cudaStreamDestroy(b->cs2);
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
     rs_batch_free(b->rb);
+    ls_batch_free(b->lb);
     delete b;
 }
 
@@ -1754,6 +1775,10 @@ int mdg_autotune(mdg_ctx* cp, int32_t reps, mdg_tuning* out) {
     }
     c.pair_blocks = best_pb;
     // structure-factor split: row tiles per CTA x atom splits
+    if (c.precision == MDG_MIXED && c.tcp.ready) {
+        const int trc = recip_tc_throughput(c, false);  // tune the plan for the system alone
+        if (trc) return trc;
+    }
     int best_tpc = c.tcp.tpc1, best_mult = c.tcp.mult1;
     if (c.precision == MDG_MIXED && c.tcp.ready) {
         best = time_force(c, reps);

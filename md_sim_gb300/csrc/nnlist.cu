@@ -60,10 +60,15 @@ __global__ void k_trigger_decide(View v, int force) {
     v.acc[2 * v.nijt + ACC_MAXD] = 0.0;
 }
 
+// The list build's kernels are written as block bodies with an explicit block index and block
+// count, so that one launch can serve several systems (replica batches: each block finds its system
+// and its block within that system's grid, the same grid a launch for that system alone has).
+
 // Bin heads: cell index + count; saves the reference positions of the rebuild.
-__global__ void k_bin_heads(View v, Grid g, int* head_cell, int* cell_count, double4* hpos) {
+__device__ __forceinline__ void bin_heads(const View& v, const Grid& g, int* head_cell, int* cell_count,
+                                          double4* hpos, int bid, int nblk) {
     if (!v.status[ST_REBUILD]) return;
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = bid * blockDim.x + threadIdx.x;
     if (h < v.nheads) {
         const int a = v.head_atom[h];
         const double wx = wrap(v.x[a], v.lx, g.periodic[0]);
@@ -75,20 +80,24 @@ __global__ void k_bin_heads(View v, Grid g, int* head_cell, int* cell_count, dou
         atomicAdd(&cell_count[c], 1);
     }
     // reference positions (src/nnlist.f90:99-119)
-    for (int i = h; i < v.nrig; i += gridDim.x * blockDim.x) {
+    for (int i = h; i < v.nrig; i += nblk * blockDim.x) {
         v.ocx[i] = v.cx[i];
         v.ocy[i] = v.cy[i];
         v.ocz[i] = v.cz[i];
     }
-    for (int i = h; i < v.nmove - v.nriga; i += gridDim.x * blockDim.x) {
+    for (int i = h; i < v.nmove - v.nriga; i += nblk * blockDim.x) {
         v.ox[i] = v.x[i + v.nriga];
         v.oy[i] = v.y[i + v.nriga];
         v.oz[i] = v.z[i + v.nriga];
     }
 }
 
+__global__ void k_bin_heads(View v, Grid g, int* head_cell, int* cell_count, double4* hpos) {
+    bin_heads(v, g, head_cell, cell_count, hpos, blockIdx.x, gridDim.x);
+}
+
 // Exclusive scan of the cell counts (one block) -> cell_start; resets counts to use as cursors.
-__global__ void k_scan_cells(View v, int ncell, int* cell_count, int* cell_start) {
+__device__ __forceinline__ void scan_cells(const View& v, int ncell, int* cell_count, int* cell_start) {
     if (!v.status[ST_REBUILD]) return;
     __shared__ int carry;
     __shared__ int part[kNT];
@@ -116,15 +125,24 @@ __global__ void k_scan_cells(View v, int ncell, int* cell_count, int* cell_start
     if (threadIdx.x == 0) cell_start[ncell] = carry;
 }
 
-__global__ void k_scatter_heads(View v, const int* head_cell, int* cell_count, const int* cell_start,
-                                const double4* hpos, float4* cpos) {
+__global__ void k_scan_cells(View v, int ncell, int* cell_count, int* cell_start) {
+    scan_cells(v, ncell, cell_count, cell_start);
+}
+
+__device__ __forceinline__ void scatter_heads(const View& v, const int* head_cell, int* cell_count,
+                                              const int* cell_start, const double4* hpos, float4* cpos, int bid) {
     if (!v.status[ST_REBUILD]) return;
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = bid * blockDim.x + threadIdx.x;
     if (h >= v.nheads) return;
     const int c = head_cell[h];
     const int slot = cell_start[c] + atomicAdd(&cell_count[c], 1);
     const double4 p = hpos[h];
     cpos[slot] = make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float(v.head_atom[h]));
+}
+
+__global__ void k_scatter_heads(View v, const int* head_cell, int* cell_count, const int* cell_start,
+                                const double4* hpos, float4* cpos) {
+    scatter_heads(v, head_cell, cell_count, cell_start, hpos, cpos, blockIdx.x);
 }
 
 __device__ __forceinline__ bool excluded(const View& v, int i, int j) {
@@ -175,13 +193,13 @@ struct WarpOut {
 
 // One warp per head: the warp walks the neighbouring cells, lanes test 32 candidates at a time
 // and the kept partners (j > i) are appended in order with a ballot.
-__global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* cpos, const double4* hpos,
-                           int* cell_count) {
+__device__ __forceinline__ void build_hh(const View& v, const Grid& g, const int* cell_start, const float4* cpos,
+                                         const double4* hpos, int* cell_count, int bid, int nblk) {
     if (!v.status[ST_REBUILD]) return;
     // the binning counts go back to zero for the next rebuild (zeroed at allocation)
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.ncell; i += gridDim.x * blockDim.x) cell_count[i] = 0;
+    for (int i = bid * blockDim.x + threadIdx.x; i < g.ncell; i += nblk * blockDim.x) cell_count[i] = 0;
     const int lane = threadIdx.x & 31;
-    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int h = (bid * blockDim.x + threadIdx.x) >> 5;
     if (h >= v.nheads) return;
     const int ia = v.head_atom[h];
     const double4 pw = hpos[h];
@@ -242,11 +260,17 @@ __global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* 
     }
 }
 
+__global__ void k_build_hh(View v, Grid g, const int* cell_start, const float4* cpos, const double4* hpos,
+                           int* cell_count) {
+    build_hh(v, g, cell_start, cpos, hpos, cell_count, blockIdx.x, gridDim.x);
+}
+
 // One warp per head: all wall atoms within rskin (src/nnlist.f90:143-161).
-__global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4* wpos, const double4* hpos) {
+__device__ __forceinline__ void build_hw(const View& v, const Grid& g, const int* wcell_start, const float4* wpos,
+                                         const double4* hpos, int bid) {
     if (!v.status[ST_REBUILD]) return;
     const int lane = threadIdx.x & 31;
-    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int h = (bid * blockDim.x + threadIdx.x) >> 5;
     if (h >= v.nheads) return;
     const int ia = v.head_atom[h];
     const double xi = v.x[ia], yi = v.y[ia], zi = v.z[ia];
@@ -301,6 +325,67 @@ __global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4*
         if (cnt > v.maxwnb) atomicMax(&v.status[ST_WLIST_OVF], cnt);
         v.wnbcnt[h] = min(cnt, v.maxwnb);
     }
+}
+
+__global__ void k_build_hw(View v, Grid g, const int* wcell_start, const float4* wpos, const double4* hpos) {
+    build_hw(v, g, wcell_start, wpos, hpos, blockIdx.x);
+}
+
+// ---- the list build of several systems, one launch per kernel ----------------------------------
+// Per system: its view, grids and list scratch.  first[k] (k = bin, scan, scatter, head-head,
+// head-wall) holds each system's first block in launch k (nrep + 1 entries); a block serves the
+// system r with first[k][r] <= block < first[k][r + 1], as block (block - first[k][r]) of a grid
+// of first[k][r + 1] - first[k][r] blocks.
+struct alignas(16) LsRep {
+    View v;
+    Grid g, wg;
+    int *head_cell, *cell_count, *cell_start, *wcell_start;
+    double4* hpos;
+    float4 *cpos, *wpos;
+};
+
+// the system of block b: the largest r with first[r] <= b (first[0] = 0 <= b < first[nrep])
+__device__ __forceinline__ int rep_of_block(const int* __restrict__ first, int nrep, int b) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(kNT) k_bin_heads_b(const LsRep* __restrict__ reps, const int* __restrict__ first,
+                                                     int nrep) {
+    const int r = rep_of_block(first, nrep, blockIdx.x);
+    const LsRep& R = reps[r];
+    bin_heads(R.v, R.g, R.head_cell, R.cell_count, R.hpos, blockIdx.x - first[r], first[r + 1] - first[r]);
+}
+
+__global__ void __launch_bounds__(kNT) k_scan_cells_b(const LsRep* __restrict__ reps) {
+    const LsRep& R = reps[blockIdx.x];  // one block per system
+    scan_cells(R.v, R.g.ncell, R.cell_count, R.cell_start);
+}
+
+__global__ void __launch_bounds__(kNT) k_scatter_heads_b(const LsRep* __restrict__ reps,
+                                                         const int* __restrict__ first, int nrep) {
+    const int r = rep_of_block(first, nrep, blockIdx.x);
+    const LsRep& R = reps[r];
+    scatter_heads(R.v, R.head_cell, R.cell_count, R.cell_start, R.hpos, R.cpos, blockIdx.x - first[r]);
+}
+
+__global__ void __launch_bounds__(128) k_build_hh_b(const LsRep* __restrict__ reps, const int* __restrict__ first,
+                                                    int nrep) {
+    const int r = rep_of_block(first, nrep, blockIdx.x);
+    const LsRep& R = reps[r];
+    build_hh(R.v, R.g, R.cell_start, R.cpos, R.hpos, R.cell_count, blockIdx.x - first[r], first[r + 1] - first[r]);
+}
+
+__global__ void __launch_bounds__(128) k_build_hw_b(const LsRep* __restrict__ reps, const int* __restrict__ first,
+                                                    int nrep) {
+    const int r = rep_of_block(first, nrep, blockIdx.x);
+    const LsRep& R = reps[r];
+    build_hw(R.v, R.wg, R.wcell_start, R.wpos, R.hpos, blockIdx.x - first[r]);
 }
 
 Grid make_grid(double lx, double ly, double lz, double rs, int pz, double zlo, double zhi) {
@@ -396,17 +481,91 @@ void nnlist_trigger(Ctx& c, bool force) {
     k_trigger_decide<<<1, 1, 0, c.stream>>>(v, force ? 1 : 0);
 }
 
+// Blocks of the five list launches of one system: bin, scan, scatter, head-head, head-wall.
+static void list_blocks(const View& v, int nb[5]) {
+    const int nh = std::max(v.nheads, 1);
+    nb[0] = std::max((std::max(nh, std::max(v.nrig, v.nmove - v.nriga)) + kNT - 1) / kNT, 1);
+    nb[1] = 1;
+    nb[2] = (nh + kNT - 1) / kNT;
+    nb[3] = (nh + 3) / 4;
+    nb[4] = v.nwall > 0 ? (nh + 3) / 4 : 0;
+}
+
 void nnlist_build(Ctx& c) {
     View& v = c.v;
     const Grid& g = c.grid;
-    const int nh = std::max(v.nheads, 1);
-    const int nbk = std::max((std::max(nh, std::max(v.nrig, v.nmove - v.nriga)) + kNT - 1) / kNT, 1);
-    k_bin_heads<<<nbk, kNT, 0, c.stream>>>(v, g, c.d_head_cell, c.d_cell_count, c.d_hpos);
-    k_scan_cells<<<1, kNT, 0, c.stream>>>(v, g.ncell, c.d_cell_count, c.d_cell_start);
-    k_scatter_heads<<<(nh + kNT - 1) / kNT, kNT, 0, c.stream>>>(v, c.d_head_cell, c.d_cell_count, c.d_cell_start,
-                                                                 c.d_hpos, c.d_cpos);
-    k_build_hh<<<(nh + 3) / 4, 128, 0, c.stream>>>(v, g, c.d_cell_start, c.d_cpos, c.d_hpos, c.d_cell_count);
-    if (v.nwall > 0) k_build_hw<<<(nh + 3) / 4, 128, 0, c.stream>>>(v, c.wgrid, c.d_wcell_start, c.d_wpos, c.d_hpos);
+    int nb[5];
+    list_blocks(v, nb);
+    k_bin_heads<<<nb[0], kNT, 0, c.stream>>>(v, g, c.d_head_cell, c.d_cell_count, c.d_hpos);
+    k_scan_cells<<<nb[1], kNT, 0, c.stream>>>(v, g.ncell, c.d_cell_count, c.d_cell_start);
+    k_scatter_heads<<<nb[2], kNT, 0, c.stream>>>(v, c.d_head_cell, c.d_cell_count, c.d_cell_start, c.d_hpos,
+                                                  c.d_cpos);
+    k_build_hh<<<nb[3], 128, 0, c.stream>>>(v, g, c.d_cell_start, c.d_cpos, c.d_hpos, c.d_cell_count);
+    if (nb[4] > 0) k_build_hw<<<nb[4], 128, 0, c.stream>>>(v, c.wgrid, c.d_wcell_start, c.d_wpos, c.d_hpos);
+}
+
+int ls_batch_setup(LsBatch& lb, const std::vector<Ctx*>& cs, std::string& err) {
+    const int nrep = (int)cs.size();
+    lb.nrep = nrep;
+    if (nrep == 0) return MDG_OK;
+    std::vector<LsRep> reps(nrep);
+    std::vector<int> first(5 * (nrep + 1), 0);
+    for (int r = 0; r < nrep; ++r) {
+        const Ctx& c = *cs[r];
+        LsRep& R = reps[r];
+        R.v = c.v;
+        R.g = c.grid;
+        R.wg = c.wgrid;
+        R.head_cell = c.d_head_cell;
+        R.cell_count = c.d_cell_count;
+        R.cell_start = c.d_cell_start;
+        R.wcell_start = c.d_wcell_start;
+        R.hpos = c.d_hpos;
+        R.cpos = c.d_cpos;
+        R.wpos = c.d_wpos;
+        int nb[5];
+        list_blocks(c.v, nb);
+        for (int k = 0; k < 5; ++k) first[k * (nrep + 1) + r + 1] = first[k * (nrep + 1) + r] + nb[k];
+    }
+    const size_t off_first = (sizeof(LsRep) * nrep + 255) & ~size_t(255);
+    const size_t need = off_first + sizeof(int) * first.size();
+    if (need > lb.cap) {
+        if (lb.d_buf) cudaFree(lb.d_buf);
+        lb.d_buf = nullptr;
+        lb.cap = 0;
+        if (cudaMalloc(&lb.d_buf, need) != cudaSuccess) {
+            err = "replica batch: list descriptor allocation failed";
+            return MDG_E_CUDA;
+        }
+        lb.cap = need;
+    }
+    unsigned char* base = static_cast<unsigned char*>(lb.d_buf);
+    lb.reps = base;
+    for (int k = 0; k < 5; ++k) {
+        lb.first[k] = reinterpret_cast<int*>(base + off_first) + k * (nrep + 1);
+        lb.nblk[k] = first[k * (nrep + 1) + nrep];
+    }
+    if (cudaMemcpy(base, reps.data(), sizeof(LsRep) * nrep, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(base + off_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        err = "replica batch: list descriptor upload failed";
+        return MDG_E_CUDA;
+    }
+    return MDG_OK;
+}
+
+void ls_batch_launch(const LsBatch& lb, cudaStream_t st) {
+    if (lb.nrep == 0) return;
+    const LsRep* reps = static_cast<const LsRep*>(lb.reps);
+    k_bin_heads_b<<<lb.nblk[0], kNT, 0, st>>>(reps, lb.first[0], lb.nrep);
+    k_scan_cells_b<<<lb.nrep, kNT, 0, st>>>(reps);
+    k_scatter_heads_b<<<lb.nblk[2], kNT, 0, st>>>(reps, lb.first[2], lb.nrep);
+    k_build_hh_b<<<lb.nblk[3], 128, 0, st>>>(reps, lb.first[3], lb.nrep);
+    if (lb.nblk[4] > 0) k_build_hw_b<<<lb.nblk[4], 128, 0, st>>>(reps, lb.first[4], lb.nrep);
+}
+
+void ls_batch_free(LsBatch& lb) {
+    if (lb.d_buf) cudaFree(lb.d_buf);
+    lb = LsBatch();
 }
 
 }  // namespace mdg

@@ -1185,10 +1185,16 @@ __global__ void __launch_bounds__(128, 1) k_umma_selftest(const float* A, const 
 // Pass-1 launch plan: tpc row tiles per CTA (2 or 4) and mult x (152 / row-tile groups) atom
 // splits (mult 2 is the default; the autotuner tries the others).  Returns nonzero when the
 // combination does not fit (TMEM columns or table capacity).
+// mult: CTAs about 76 mult per launch (one system alone: fill the GPU), or 0 for the fewest
+// CTAs of about kThroughputChunk atoms each (a system among many in one graph, where the GPU is
+// full anyway and each CTA's set-up is paid in SM time).
+constexpr int kThroughputChunk = 1024;
+
 int tc_plan_pass1(Ctx& c, int tpc, int mult) {
     View& v = c.v;
     KSet& ks = c.ks;
     TcPlan& p = c.tcp;
+    const int nthr = std::max(1, (v.nmove + kThroughputChunk - 1) / kThroughputChunk);
     if (tpc == 1) {
         // n-side form: 2 NN lanes in one 128-lane accumulator, 256 rows per CTA, at most
         // kMaxChunk1b atoms per CTA (their records in shared memory)
@@ -1200,7 +1206,8 @@ int tc_plan_pass1(Ctx& c, int tpc, int mult) {
         p.ncols1 = 512;
         p.grid1x = (ks.nrow + 255) / 256;
         p.rtot = p.grid1x * 256;
-        p.nsplit1 = std::max(1, std::min(std::max(1, 76 * mult / p.grid1x), (v.nmove + kGA - 1) / kGA));
+        p.nsplit1 = mult > 0 ? std::max(1, std::min(std::max(1, 76 * mult / p.grid1x), (v.nmove + kGA - 1) / kGA))
+                             : nthr;
         p.nsplit1 = std::max(p.nsplit1, (v.nmove + kMaxChunk1b - 1) / kMaxChunk1b);
         p.chunk1 = (v.nmove + p.nsplit1 - 1) / p.nsplit1;
         p.chunk1 = std::max(kGA, (p.chunk1 + kGA - 1) / kGA * kGA);
@@ -1221,12 +1228,79 @@ int tc_plan_pass1(Ctx& c, int tpc, int mult) {
     p.ncols1 = tpc * (p.NP <= 128 ? 128 : 256);
     p.grid1x = (ks.nrow + tpc * 128 - 1) / (tpc * 128);
     p.rtot = p.grid1x * tpc * 128;
-    p.nsplit1 = std::max(1, std::min(std::max(1, 76 * mult / p.grid1x), (v.nmove + 127) / 128));
+    p.nsplit1 = mult > 0 ? std::max(1, std::min(std::max(1, 76 * mult / p.grid1x), (v.nmove + 127) / 128)) : nthr;
     p.chunk1 = (v.nmove + p.nsplit1 - 1) / p.nsplit1;
     p.chunk1 = std::max(kGA, (p.chunk1 + kGA - 1) / kGA * kGA);
     p.nsplit1 = std::max(1, (v.nmove + p.chunk1 - 1) / p.chunk1);
     p.mult1 = mult;
     return 0;
+}
+
+// Work items of pass 2 (one CTA each): whole atom tiles; with pieces, the tiles of the last,
+// partial wave (all tiles when there are fewer than one per SM) are cut into pieces of about equal
+// K-step work, so that the wave fills the SMs (a system alone); pieces add their forces
+// atomically into forces zeroed by the operand-packing kernel before.
+static std::vector<int4> tc_items2(const Ctx& c, bool pieces, int& zero) {
+    const View& v = c.v;
+    const TcPlan& p = c.tcp;
+    const std::vector<int>& cks = p.h_chunk_ks;
+    const int ntile = (v.nmove + 127) / 128, tail = ntile % 152;
+    int ksum = 0;
+    for (int cc = 0; cc < p.nchunk2; ++cc) ksum += cks[cc];
+    const int S = pieces && tail > 0 ? std::min(152 / tail, std::max(1, p.nchunk2 / 2)) : 1;
+    const int first = S >= 2 ? ntile - tail : ntile;
+    std::vector<int4> items;
+    for (int t = 0; t < first; ++t) items.push_back(make_int4(t, 0, p.nchunk2, 1));
+    for (int t = first; t < ntile; ++t) {
+        int c0 = 0, acc = 0;
+        for (int piece = 1; piece <= S && c0 < p.nchunk2; ++piece) {
+            int c1 = c0;
+            const long target = (long)ksum * piece / S;
+            while (c1 < p.nchunk2 && (acc + cks[c1] <= target || c1 == c0)) acc += cks[c1++];
+            if (piece == S) {
+                while (c1 < p.nchunk2) acc += cks[c1++];
+            }
+            items.push_back(make_int4(t, c0, c1, 0));
+            c0 = c1;
+        }
+    }
+    zero = std::min(first * 128, v.nmove);
+    return items;
+}
+
+// Both item tables (pieces for the system alone, whole tiles for throughput) go to the device once,
+// so that switching plans is host bookkeeping only.
+static int tc_plan_items2(Ctx& c) {
+    TcPlan& p = c.tcp;
+    for (int k = 0; k < 2; ++k) {
+        int zero = 0;
+        const std::vector<int4> items = tc_items2(c, k == 0, zero);
+        p.items2_k[k] = (int4*)dalloc(c, sizeof(int4) * std::max(items.size(), (size_t)1));
+        if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
+        p.nitems2_k[k] = (int)items.size();
+        p.zero2_k[k] = zero;
+        if (!items.empty())
+            MDG_CUDA(cudaMemcpy(p.items2_k[k], items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+    }
+    p.items2 = p.items2_k[0];
+    p.nitems2 = p.nitems2_k[0];
+    p.zero2 = p.zero2_k[0];
+    return MDG_OK;
+}
+
+int recip_tc_throughput(Ctx& c, bool on) {
+    TcPlan& p = c.tcp;
+    if (!p.ready || on == p.throughput) return MDG_OK;
+    if (on) p.mult_alone = p.mult1;
+    if (tc_plan_pass1(c, p.tpc1, on ? 0 : p.mult_alone))
+        return set_err(&c, MDG_E_UNSUPPORTED, "tensor-core plan");
+    const int k = on ? 1 : 0;
+    p.items2 = p.items2_k[k];
+    p.nitems2 = p.nitems2_k[k];
+    p.zero2 = p.zero2_k[k];
+    p.throughput = on;
+    drop_graphs(c);
+    return MDG_OK;
 }
 
 int recip_tc_setup(Ctx& c) {
@@ -1248,7 +1322,7 @@ int recip_tc_setup(Ctx& c) {
     // the partial-sum buffer is sized for the largest split the autotuner may choose
     size_t part_max = 0;
     for (int tpc : {1, 2, 4})
-        for (int m = 1; m <= 4; m *= 2)
+        for (int m : {0, 1, 2, 4})
             if (!tc_plan_pass1(c, tpc, m)) part_max = std::max(part_max, (size_t)p.nsplit1 * p.NP * p.rtot);
     if (tc_plan_pass1(c, tpc0, 2) && tc_plan_pass1(c, 2, 2)) return set_err(&c, MDG_E_UNSUPPORTED, "tensor-core plan");
     p.mtiles = (ks.nrow + 127) / 128;
@@ -1291,38 +1365,10 @@ int recip_tc_setup(Ctx& c) {
             off += (size_t)2 * nks * kTile2;
         }
         p.img_bytes = off;
-        // Work items of pass 2 (one CTA each): whole atom tiles, except that the tiles of the last,
-        // partial wave (all tiles when there are fewer than one per SM) are cut into pieces of
-        // about equal K-step work, so that the wave fills the SMs; pieces add their forces
-        // atomically into forces zeroed by the operand-packing kernel before.
-        {
-            const int ntile = (v.nmove + 127) / 128, tail = ntile % 152;
-            int ksum = 0;
-            for (int cc = 0; cc < p.nchunk2; ++cc) ksum += chunk2[cc].z;
-            const int S = tail > 0 ? std::min(152 / tail, std::max(1, p.nchunk2 / 2)) : 1;
-            const int first = S >= 2 ? ntile - tail : ntile;
-            std::vector<int4> items;
-            for (int t = 0; t < first; ++t) items.push_back(make_int4(t, 0, p.nchunk2, 1));
-            for (int t = first; t < ntile; ++t) {
-                int c0 = 0, acc = 0;
-                for (int piece = 1; piece <= S && c0 < p.nchunk2; ++piece) {
-                    int c1 = c0;
-                    const long target = (long)ksum * piece / S;
-                    while (c1 < p.nchunk2 && (acc + chunk2[c1].z <= target || c1 == c0)) acc += chunk2[c1++].z;
-                    if (piece == S) {
-                        while (c1 < p.nchunk2) acc += chunk2[c1++].z;
-                    }
-                    items.push_back(make_int4(t, c0, c1, 0));
-                    c0 = c1;
-                }
-            }
-            p.nitems2 = (int)items.size();
-            p.zero2 = std::min(first * 128, v.nmove);
-            p.items2 = (int4*)dalloc(c, sizeof(int4) * std::max(p.nitems2, 1));
-            if (c.alloc_failed) return set_err(&c, MDG_E_CUDA, "out of device memory for the tensor-core reciprocal sum");
-            if (p.nitems2 > 0)
-                MDG_CUDA(cudaMemcpy(p.items2, items.data(), sizeof(int4) * p.nitems2, cudaMemcpyHostToDevice));
-        }
+        p.h_chunk_ks.resize(p.nchunk2);
+        for (int cc = 0; cc < p.nchunk2; ++cc) p.h_chunk_ks[cc] = chunk2[cc].z;
+        const int rc = tc_plan_items2(c);
+        if (rc) return rc;
         p.rorig2 = (int*)dalloc(c, sizeof(int) * std::max(nrp, 1));
         p.rsc2 = (float*)dalloc(c, sizeof(float) * std::max(nrp, 1));
         p.rowsc = (float*)dalloc(c, sizeof(float) * std::max(nr, 1));
