@@ -7,7 +7,8 @@
 // test on wrapped coordinates and then the reference's own FP64 test, evaluated with the same
 // roundings (separate multiplies and adds, anint = round half away from zero), so the kept set
 // is identical to the reference's.  Pairs are stored under the lower atom index as in
-// list1/list2 (i < j); head-wall pairs under the head.
+// list1/list2 (i < j); head-wall pairs under the head.  The *_b kernels run the same block bodies
+// for many systems in one launch each (replica batches).
 #include <algorithm>
 #include <cmath>
 #include <cstring>

@@ -18,7 +18,8 @@
 // Energies per lane are compensated FP32 sums.  k_wall_mx does the head-wall loop
 // (src/forcem.f90:418-498) the same way over (head, segment) work items, with the wall reaction
 // sums of each item added into FP64 per lane.  The pair loops issue no FP64 instructions (the
-// FP64 pipe of GB300 is narrow).
+// FP64 pipe of GB300 is narrow).  k_pair_mx_batch and k_wall_mx_batch run the same loop bodies
+// over the heads of many systems at once (replica batches), one persistent launch each.
 #include <algorithm>
 
 #include "common.cuh"
