@@ -12,8 +12,9 @@
 // The reference's loops over the molecules, split into contiguous ranges of molecules over the host
 // threads (OpenMP; MDG_HOST_THREADS if set, else all cores the process may run on, one thread
 // below 2,048 molecules): each thread runs every loop on its own range, so a molecule's arrays stay in
-// one core's cache from one loop to the next.  The sums (kinetic energies) run afterwards on one
-// thread in molecule order, so the result does not depend on the thread count.  No device memory.
+// one core's cache from one loop to the next.  The kinetic sums are seven independent chains, each
+// summed in molecule order by one thread (several chains at once), so the result does not depend
+// on the thread count.  No device memory.
 // The arithmetic is the reference's operation by operation (this file is compiled without
 // multiply-add contraction), so a drop-in loop reproduces the library's resident steps to rounding.
 #include <algorithm>
@@ -107,6 +108,22 @@ int mdg_host_predict(mdg_host_gear* g, mdg_state* st) {
     const int64_t nrig = g->nrig, n0 = g->nriga, n1 = g->nliqa;
     const mdg_rigid& b = g->body;
     double* A = g->A.data();
+    // kinetic sums: seven independent chains (flexible atoms; centre velocity x, y, z; angular
+    // velocity x, y, z), each summed in molecule order by one thread as the reference does, so the
+    // result does not depend on the thread count; several threads run different chains at once
+    double chain[7] = {0, 0, 0, 0, 0, 0, 0};
+    auto run_chain = [&](int ch) {
+        double s = 0.0;
+        if (ch == 0) {
+            for (int64_t i = n0; i < n1; ++i)
+                s += g->mi[i - n0] * (st->xd[0][i] * st->xd[0][i] + st->yd[0][i] * st->yd[0][i] + st->zd[0][i] * st->zd[0][i]);
+        } else {
+            const double* a = ch == 1 ? st->cx[1] : ch == 2 ? st->cy[1] : ch == 3 ? st->cz[1]
+                            : ch == 4 ? st->wx[0] : ch == 5 ? st->wy[0] : st->wz[0];
+            for (int64_t i = 0; i < nrig; ++i) s += a[i] * a[i];
+        }
+        chain[ch] = s;
+    };
 #pragma omp parallel num_threads(g->nthreads) if (g->nthreads > 1)
     {
         const int nt = omp_get_num_threads(), k = omp_get_thread_num();
@@ -174,24 +191,11 @@ int mdg_host_predict(mdg_host_gear* g, mdg_state* st) {
                 st->rsz[ix + j] = st->z0[ix + j] - st->z0[ix];
             }
         }
+#pragma omp barrier
+        for (int ch = k; ch < 7; ch += nt) run_chain(ch);
     }
-    // kinetic sums on one thread, each in molecule order
-    double kp = 0.0;
-    for (int64_t i = n0; i < n1; ++i)
-        kp += g->mi[i - n0] * (st->xd[0][i] * st->xd[0][i] + st->yd[0][i] * st->yd[0][i] + st->zd[0][i] * st->zd[0][i]);
-    double sc[3] = {0, 0, 0}, sw[3] = {0, 0, 0};
-    {
-        const double *vx = st->cx[1], *vy = st->cy[1], *vz = st->cz[1];
-        const double *wx = st->wx[0], *wy = st->wy[0], *wz = st->wz[0];
-        for (int64_t i = 0; i < nrig; ++i) {
-            sc[0] += vx[i] * vx[i];
-            sc[1] += vy[i] * vy[i];
-            sc[2] += vz[i] * vz[i];
-            sw[0] += wx[i] * wx[i];
-            sw[1] += wy[i] * wy[i];
-            sw[2] += wz[i] * wz[i];
-        }
-    }
+    double kp = chain[0];
+    const double sc[3] = {chain[1], chain[2], chain[3]}, sw[3] = {chain[4], chain[5], chain[6]};
     kp = kp + b.mw * (sc[0] + sc[1] + sc[2]);
     const double kw = b.inxx * sw[0] + b.inyy * sw[1] + b.inzz * sw[2];
     if (b.temper == -1.0) {
