@@ -32,7 +32,6 @@ struct mdg_host_gear {
     int64_t nrig = 0, nriga = 0, nliqa = 0;
     std::vector<double> mi, mii;  // masses and inverse masses of the flexible atoms nriga..nliqa-1
     mdg_rigid body{};
-    std::vector<double> A;        // rotation matrices, [9][nrig] (a11, a12, ..., a33 of src/config.f90)
     double kp = 0, kw = 0, ke = 0, htot = 0, sft = 0, sfr = 0, uconf = 0;
     int nthreads = 1;
 };
@@ -60,6 +59,38 @@ inline void correct5(double& a0, double& a1, double& a2, double& a3, double& a4,
     a2 = a2 + g2 * c;
     a3 = a3 + g3 * c;
     a4 = a4 + g4 * c;
+}
+
+// normalised quaternion and its rotation matrix (src/move.f90:120-136)
+inline void quat_rot(const double* qq, double* qn, double* a) {
+    const double cr = 1.0 / std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
+    const double q1 = qq[0] * cr, q2 = qq[1] * cr, q3 = qq[2] * cr, q4 = qq[3] * cr;
+    qn[0] = q1;
+    qn[1] = q2;
+    qn[2] = q3;
+    qn[3] = q4;
+    a[0] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
+    a[1] = 2.0 * (q3 * q4 - q1 * q2);
+    a[2] = 2.0 * (q2 * q3 + q1 * q4);
+    a[3] = -2.0 * (q1 * q2 + q3 * q4);
+    a[4] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4;
+    a[5] = 2.0 * (q2 * q4 - q1 * q3);
+    a[6] = 2.0 * (q2 * q3 - q1 * q4);
+    a[7] = -2.0 * (q1 * q3 + q4 * q2);
+    a[8] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
+}
+
+// rotation matrix of an already normalised quaternion: the same products as quat_rot's
+inline void rot_of(double q1, double q2, double q3, double q4, double* a) {
+    a[0] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
+    a[1] = 2.0 * (q3 * q4 - q1 * q2);
+    a[2] = 2.0 * (q2 * q3 + q1 * q4);
+    a[3] = -2.0 * (q1 * q2 + q3 * q4);
+    a[4] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4;
+    a[5] = 2.0 * (q2 * q4 - q1 * q3);
+    a[6] = 2.0 * (q2 * q3 - q1 * q4);
+    a[7] = -2.0 * (q1 * q3 + q4 * q2);
+    a[8] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
 }
 
 // [lo, hi) of thread k of nt over n items
@@ -90,7 +121,6 @@ int mdg_host_gear_create(const mdg_sysdesc* s, const mdg_rigid* body, mdg_host_g
     g->mi.assign(s->mi + s->nriga, s->mi + s->nliqa);
     g->mii.assign(s->mii + s->nriga, s->mii + s->nliqa);
     g->body = *body;
-    g->A.assign(9 * (size_t)std::max<int64_t>(s->nrig, 1), 0.0);
     g->nthreads = host_threads(std::max(s->nrig, s->nliqa - s->nriga));
     *out = g;
     return MDG_OK;
@@ -107,7 +137,6 @@ int mdg_host_predict(mdg_host_gear* g, mdg_state* st) {
     if (!g || !st) return MDG_E_ARG;
     const int64_t nrig = g->nrig, n0 = g->nriga, n1 = g->nliqa;
     const mdg_rigid& b = g->body;
-    double* A = g->A.data();
     // kinetic sums: seven independent chains (flexible atoms; centre velocity x, y, z; angular
     // velocity x, y, z), each summed in molecule order by one thread as the reference does, so the
     // result does not depend on the thread count; several threads run different chains at once
@@ -151,44 +180,33 @@ int mdg_host_predict(mdg_host_gear* g, mdg_state* st) {
             double* const* a = st->q[c];
             for (int64_t i = lo; i < hi; ++i) predict4(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i]);
         }
+        // normalised quaternion, rotation matrix (in registers; the corrector rebuilds it from the
+        // same quaternion), sites from the centre and the body frame, H offsets from the O
+        // (src/move.f90:120-162)
         double *Q1 = st->q[0][0], *Q2 = st->q[1][0], *Q3 = st->q[2][0], *Q4 = st->q[3][0];
-        double* a[9];
-        for (int m = 0; m < 9; ++m) a[m] = A + (size_t)m * nrig;
-        for (int64_t i = lo; i < hi; ++i) {
-            double q1 = Q1[i], q2 = Q2[i], q3 = Q3[i], q4 = Q4[i];
-            const double cr = 1.0 / std::sqrt(q1 * q1 + q2 * q2 + q3 * q3 + q4 * q4);
-            q1 = q1 * cr;
-            q2 = q2 * cr;
-            q3 = q3 * cr;
-            q4 = q4 * cr;
-            Q1[i] = q1;
-            Q2[i] = q2;
-            Q3[i] = q3;
-            Q4[i] = q4;
-            // rotation matrix (src/move.f90:128-136)
-            a[0][i] = -q1 * q1 + q2 * q2 - q3 * q3 + q4 * q4;
-            a[1][i] = 2.0 * (q3 * q4 - q1 * q2);
-            a[2][i] = 2.0 * (q2 * q3 + q1 * q4);
-            a[3][i] = -2.0 * (q1 * q2 + q3 * q4);
-            a[4][i] = q1 * q1 - q2 * q2 - q3 * q3 + q4 * q4;
-            a[5][i] = 2.0 * (q2 * q4 - q1 * q3);
-            a[6][i] = 2.0 * (q2 * q3 - q1 * q4);
-            a[7][i] = -2.0 * (q1 * q3 + q4 * q2);
-            a[8][i] = -q1 * q1 - q2 * q2 + q3 * q3 + q4 * q4;
-        }
-        // sites from the centre and the body frame, H offsets from the O (src/move.f90:140-162)
         const double *CX = st->cx[0], *CY = st->cy[0], *CZ = st->cz[0];
         for (int64_t i = lo; i < hi; ++i) {
+            double qn[4], r[9];
+            const double qq[4] = {Q1[i], Q2[i], Q3[i], Q4[i]};
+            quat_rot(qq, qn, r);
+            Q1[i] = qn[0];
+            Q2[i] = qn[1];
+            Q3[i] = qn[2];
+            Q4[i] = qn[3];
             const int64_t ix = 3 * i;
+            double sx[3], sy[3], sz[3];
             for (int j = 0; j < 3; ++j) {
-                st->x0[ix + j] = CX[i] + a[0][i] * b.xbody[j] + a[3][i] * b.ybody[j] + a[6][i] * b.zbody[j];
-                st->y0[ix + j] = CY[i] + a[1][i] * b.xbody[j] + a[4][i] * b.ybody[j] + a[7][i] * b.zbody[j];
-                st->z0[ix + j] = CZ[i] + a[2][i] * b.xbody[j] + a[5][i] * b.ybody[j] + a[8][i] * b.zbody[j];
+                sx[j] = CX[i] + r[0] * b.xbody[j] + r[3] * b.ybody[j] + r[6] * b.zbody[j];
+                sy[j] = CY[i] + r[1] * b.xbody[j] + r[4] * b.ybody[j] + r[7] * b.zbody[j];
+                sz[j] = CZ[i] + r[2] * b.xbody[j] + r[5] * b.ybody[j] + r[8] * b.zbody[j];
+                st->x0[ix + j] = sx[j];
+                st->y0[ix + j] = sy[j];
+                st->z0[ix + j] = sz[j];
             }
             for (int j = 1; j < 3; ++j) {
-                st->rsx[ix + j] = st->x0[ix + j] - st->x0[ix];
-                st->rsy[ix + j] = st->y0[ix + j] - st->y0[ix];
-                st->rsz[ix + j] = st->z0[ix + j] - st->z0[ix];
+                st->rsx[ix + j] = sx[j] - sx[0];
+                st->rsy[ix + j] = sy[j] - sy[0];
+                st->rsz[ix + j] = sz[j] - sz[0];
             }
         }
 #pragma omp barrier
@@ -265,39 +283,35 @@ int mdg_host_correct(mdg_host_gear* g, mdg_state* st, const double* ftx, const d
                 }
             }
         }
-        // quaternions from the angular velocity before its correction (src/move.f90:283-317)
+        // per molecule: the quaternion corrector from the angular velocity before its correction
+        // (src/move.f90:283-317), then the body angular velocity by Euler's equations with the lab
+        // torque rotated into the body frame by the matrix of the predicted quaternion
+        // (src/move.f90:319-354); both read their inputs before either writes
         for (int64_t i = lo; i < hi; ++i) {
             const double q1 = st->q[0][0][i], q2 = st->q[1][0][i], q3 = st->q[2][0][i], q4 = st->q[3][0][i];
             const double wx = st->wx[0][i], wy = st->wy[0][i], wz = st->wz[0][i];
+            double a[9];
+            rot_of(q1, q2, q3, q4, a);
             const double cq[4] = {0.5 * (-q3 * wx - q4 * wy + q2 * wz), 0.5 * (q4 * wx - q3 * wy - q1 * wz),
                                   0.5 * (q1 * wx + q2 * wy + q4 * wz), 0.5 * (-q2 * wx + q1 * wy - q3 * wz)};
             for (int c = 0; c < 4; ++c) {
-                double* const* a = st->q[c];
-                const double co = cq[c] - a[1][i];
-                correct5(a[0][i], a[1][i], a[2][i], a[3][i], a[4][i], co, kG01, 1.0, kG21, kG31, kG41);
+                double* const* qa = st->q[c];
+                const double co = cq[c] - qa[1][i];
+                correct5(qa[0][i], qa[1][i], qa[2][i], qa[3][i], qa[4][i], co, kG01, 1.0, kG21, kG31, kG41);
             }
-        }
-        // body angular velocity: Euler's equations with the lab torque rotated into the body frame
-        // (src/move.f90:319-354)
-        {
-            const double* a[9];
-            for (int m = 0; m < 9; ++m) a[m] = g->A.data() + (size_t)m * nrig;
-            for (int64_t i = lo; i < hi; ++i) {
-                const double wx = st->wx[0][i], wy = st->wy[0][i], wz = st->wz[0][i];
-                const double t0 = tx[i], t1 = ty[i], t2 = tz[i];
-                double c1 = a[0][i] * t0 + a[1][i] * t1 + a[2][i] * t2;
-                c1 = ((c1 + wy * wz * (b.inyy - b.inzz)) * inxxi) - st->wx[1][i] - rs0i * wx;
-                double c2 = a[3][i] * t0 + a[4][i] * t1 + a[5][i] * t2;
-                c2 = ((c2 + wz * wx * (b.inzz - b.inxx)) * inyyi) - st->wy[1][i] - rs0i * wy;
-                double c3 = a[6][i] * t0 + a[7][i] * t1 + a[8][i] * t2;
-                c3 = ((c3 + wx * wy * (b.inxx - b.inyy)) * inzzi) - st->wz[1][i] - rs0i * wz;
-                correct5(st->wx[0][i], st->wx[1][i], st->wx[2][i], st->wx[3][i], st->wx[4][i], c1, kG01, 1.0, kG21, kG31,
-                         kG41);
-                correct5(st->wy[0][i], st->wy[1][i], st->wy[2][i], st->wy[3][i], st->wy[4][i], c2, kG01, 1.0, kG21, kG31,
-                         kG41);
-                correct5(st->wz[0][i], st->wz[1][i], st->wz[2][i], st->wz[3][i], st->wz[4][i], c3, kG01, 1.0, kG21, kG31,
-                         kG41);
-            }
+            const double t0 = tx[i], t1 = ty[i], t2 = tz[i];
+            double c1 = a[0] * t0 + a[1] * t1 + a[2] * t2;
+            c1 = ((c1 + wy * wz * (b.inyy - b.inzz)) * inxxi) - st->wx[1][i] - rs0i * wx;
+            double c2 = a[3] * t0 + a[4] * t1 + a[5] * t2;
+            c2 = ((c2 + wz * wx * (b.inzz - b.inxx)) * inyyi) - st->wy[1][i] - rs0i * wy;
+            double c3 = a[6] * t0 + a[7] * t1 + a[8] * t2;
+            c3 = ((c3 + wx * wy * (b.inxx - b.inyy)) * inzzi) - st->wz[1][i] - rs0i * wz;
+            correct5(st->wx[0][i], st->wx[1][i], st->wx[2][i], st->wx[3][i], st->wx[4][i], c1, kG01, 1.0, kG21, kG31,
+                     kG41);
+            correct5(st->wy[0][i], st->wy[1][i], st->wy[2][i], st->wy[3][i], st->wy[4][i], c2, kG01, 1.0, kG21, kG31,
+                     kG41);
+            correct5(st->wz[0][i], st->wz[1][i], st->wz[2][i], st->wz[3][i], st->wz[4][i], c3, kG01, 1.0, kG21, kG31,
+                     kG41);
         }
     }
     if (b.temper != -1.0) {  // thermostat corrector (src/move.f90:356-375)
