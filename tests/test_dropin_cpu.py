@@ -26,11 +26,13 @@ def _state_arrays(s):
     return out
 
 
-@pytest.mark.parametrize("threads", ["1", "3"])
+@pytest.mark.parametrize("threads", ["1", "2", "3", "8"])
 @pytest.mark.parametrize("name", list(CASES))
 def test_host_integrator_matches_oracle_loop(name, threads, oracle, gpulib, monkeypatch):
-    """The host threads split the molecules into ranges; the result does not depend on their
-    number (MDG_HOST_THREADS is read when the integrator is created)."""
+    """The host threads split the molecules into ranges, and the seven kinetic sums run as
+    separate chains (several per thread below seven threads, one per thread from seven on); the
+    result does not depend on their number (MDG_HOST_THREADS is read when the integrator is
+    created)."""
     monkeypatch.setenv("MDG_HOST_THREADS", threads)
     make, steps = CASES[name]
     s, prm = make()
