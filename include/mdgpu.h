@@ -527,8 +527,8 @@ int mdg_selftest_umma(int n, int k, const float* a, const float* b, float* d);
  * alpha and kmax as in mdg_params (alpha must be given).  Allocates nothing: its scratch is a static
  * device array of MDG_NOALLOC_MAX_K k vectors (about 2 MB) that every GPU loading the library keeps
  * until the process exits; larger k sets are rejected with MDG_E_UNSUPPORTED.  The first call on a
- * device looks up that array's device address, so make the first call on each device before any
- * stream capture.  Calls share the one array: calls whose GPU work overlaps (other streams, other
+ * device also looks up that array's device address (a runtime query).  Calls share the one array:
+ * calls whose GPU work overlaps (other streams, other
  * host threads' streams) race on it; host calls themselves are serialised.  The call returns once
  * the work is queued; errors of argument checking are returned, mdg_last_error(NULL) has the text.
  * ------------------------------------------------------------------------------------------- */
