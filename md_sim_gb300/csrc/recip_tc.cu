@@ -413,12 +413,6 @@ __device__ __forceinline__ bool wait_ab(uint32_t addr, uint32_t parity, volatile
     if (err) atomicCAS(err, 0, tag);
     return false;
 }
-__device__ __forceinline__ bool wait_ab_warp(uint32_t addr, uint32_t parity, volatile int* ab, int* err, int tag) {
-    int ok = 1;
-    if ((threadIdx.x & 31) == 0) ok = wait_ab(addr, parity, ab, err, tag) ? 1 : 0;
-    __syncwarp();
-    return __shfl_sync(0xffffffffu, ok, 0) != 0;
-}
 
 // bounded mbarrier wait by a whole warp: every lane polls (one instruction, so the lanes agree),
 // which keeps the warp converged; false once the abort flag is set or the limit is reached
@@ -450,16 +444,6 @@ __device__ __forceinline__ float2 f2up(f2t r) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
     return v;
 }
-__device__ __forceinline__ f2t f2mul(f2t a, f2t b) {
-    f2t d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2t f2fma(f2t a, f2t b, f2t c) {
-    f2t d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
 __device__ __forceinline__ f2t f2sub(f2t a, f2t b) {
     f2t d;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
@@ -471,15 +455,6 @@ __device__ __forceinline__ void split2p(float a, float b, uint32_t& hi, uint32_t
     const float2 hf = __half22float2(h);
     hi = *reinterpret_cast<const uint32_t*>(&h);
     const float2 r = f2up(f2sub(f2pk(a, b), f2pk(hf.x, hf.y)));
-    lo = pack_h2(r.x, r.y);
-}
-// hi/lo FP16 split of a packed pair
-__device__ __forceinline__ void split_f2(f2t x, uint32_t& hi, uint32_t& lo) {
-    const float2 v = f2up(x);
-    const __half2 h = __floats2half2_rn(v.x, v.y);
-    const float2 hf = __half22float2(h);
-    hi = *reinterpret_cast<const uint32_t*>(&h);
-    const float2 r = f2up(f2sub(x, f2pk(hf.x, hf.y)));
     lo = pack_h2(r.x, r.y);
 }
 
