@@ -602,6 +602,17 @@ def _summary(o):
     return keep
 
 
+def replica_extra(args, arm):
+    """Config 4 as an extra line beside the single systems: the batch arm's compact record, or its
+    error (the headline line is printed either way)."""
+    try:
+        o = arm(args)
+        return {k: o[k] for k in ("value", "unit", "ms_per_step", "config", "per_replica_ns_per_day", "sequential",
+                                  "batch_speedup_vs_sequential", "batch_mode", "step_ms_min_median_max", "clocks")}
+    except Exception as e:  # noqa: BLE001
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def gpu_arm(args):
     import torch
 
@@ -620,14 +631,7 @@ def gpu_arm(args):
         out["other_configs"] = {}
         for name in extras:
             if name == "replicas64":
-                # config 4 beside the single systems; its own failure is reported in its entry
-                try:
-                    o = replicas_arm(args)
-                    out["other_configs"][name] = {k: o[k] for k in (
-                        "value", "unit", "ms_per_step", "config", "per_replica_ns_per_day", "sequential",
-                        "batch_speedup_vs_sequential", "batch_mode", "step_ms_min_median_max", "clocks")}
-                except Exception as e:  # noqa: BLE001
-                    out["other_configs"][name] = {"error": f"{type(e).__name__}: {e}"}
+                out["other_configs"][name] = replica_extra(args, replicas_arm)
                 continue
             o = run_workload(lib, name, args, torch, stream, flush, pk, fp64_peak, headline=False)
             out["other_configs"][name] = _summary(o)

@@ -67,3 +67,19 @@ def test_replica_partition_covers_each_replica_once():
         flat = sorted(i for p in parts for i in p)
         assert flat == list(range(n))
         assert max(len(p) for p in parts) - min(len(p) for p in parts) <= 1
+
+
+def test_replica_extra_reports_its_own_failure():
+    """The config-4 extra line keeps the arm's compact record, or the arm's error in its own entry,
+    so that the headline line is printed either way."""
+    import bench
+
+    def failing(args):
+        raise RuntimeError("replica batch: no device")
+
+    assert bench.replica_extra(None, failing) == {"error": "RuntimeError: replica batch: no device"}
+    keys = ("value", "unit", "ms_per_step", "config", "per_replica_ns_per_day", "sequential",
+            "batch_speedup_vs_sequential", "batch_mode", "step_ms_min_median_max", "clocks")
+    full = {k: 1 for k in keys}
+    full["extra_key"] = 2
+    assert bench.replica_extra(None, lambda args: full) == {k: 1 for k in keys}
