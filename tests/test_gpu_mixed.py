@@ -1,6 +1,6 @@
 """Mixed precision (FP32 pair arithmetic with compensated sums, FP64 accumulation) against the
-FP64 path of the same library on the same inputs: force rel-RMS <= 1e-5, energies within 1e-5
-of the energy scale."""
+FP64 path of the same library and against the FP64 oracle directly, on the same inputs: force
+rel-RMS <= 1e-5, energies within 1e-5 of the energy scale."""
 import numpy as np
 import pytest
 
@@ -22,17 +22,19 @@ CASES = {
 
 
 @pytest.mark.parametrize("name", list(CASES))
-def test_mixed_forces_vs_fp64(name, gpulib):
+def test_mixed_forces_vs_fp64(name, gpulib, oracle):
     s, prm = CASES[name]()
-    s64, s32 = s.copy(), s.copy()
+    s64, s32, so = s.copy(), s.copy(), s.copy()
     p64 = abi.RunParams(**{**prm.__dict__, "precision": abi.MDG_FP64})
     p32 = abi.RunParams(**{**prm.__dict__, "precision": abi.MDG_MIXED})
     a = abi.Context(gpulib, s64, p64).force_get(s64)
     b = abi.Context(gpulib, s32, p32).force_get(s32)
-    rel = np.linalg.norm(b["f"] - a["f"]) / np.linalg.norm(a["f"])
-    assert rel <= MIXED_FORCE_RTOL, rel
+    r = abi.Context(oracle, so, p64).force_get(so)
     scale = np.abs(a["elj"]).sum() + np.abs(a["eqq"]).sum() + abs(a["uewa"]) + 1.0
-    assert abs(b["uconf"] - a["uconf"]) <= 1e-5 * scale
+    for ref in (a, r):  # the library's FP64 form, then the oracle
+        rel = np.linalg.norm(b["f"] - ref["f"]) / np.linalg.norm(ref["f"])
+        assert rel <= MIXED_FORCE_RTOL, rel
+        assert abs(b["uconf"] - ref["uconf"]) <= 1e-5 * scale
 
 
 @pytest.mark.parametrize("name", ["slab512", "bulk256"])
